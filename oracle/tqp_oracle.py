@@ -1,0 +1,468 @@
+"""Parity oracle: a CPU (numpy) restatement of TQP-Inmem's relational operators.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module.  It
+is used by ``tests/`` (as the checker), by ``__graft_entry__.smoke()`` (to
+check one small GPU invocation) and by ``bench.py`` (the timed CPU baseline,
+and the ``--impl reference`` arm).  It never produces a product result.
+
+The oracle is pinned against golden vectors produced by running the
+reference's own operators (``tests/golden/make_golden.py`` ->
+``tests/golden/*.npz``; checked by ``tests/test_oracle_golden.py``).
+
+Each function cites the reference code it restates (paths are relative to
+the TQP-Inmem source tree).  Where the reference is non-deterministic, the
+oracle picks one deterministic answer that the reference can also produce:
+
+* group order: the reference orders groups by a random linear hash of the key
+  tuple (``operators/aggregate.py:320-327``); the oracle orders them by key
+  tuple, ascending.  For one non-negative key the two orders coincide.
+* pairs inside one build-key bucket: the reference sorts build keys with an
+  unstable sort (``operators/hashjoin.py:43``); the oracle uses a stable one
+  (ascending build row inside a bucket).
+"""
+from __future__ import annotations
+
+import datetime as _dt
+from typing import Dict, List, Sequence, Tuple
+
+import numpy as np
+
+# constants.py:3-9
+EPS = 1e-5
+NULL = -64
+
+_EPOCH = _dt.date(1990, 1, 1)  # conversion.py:11 (YEAR_START = 1990)
+
+
+# ---------------------------------------------------------------------------
+# Literals (conversion.py:20-33, parsing.py:15-16)
+# ---------------------------------------------------------------------------
+def get_id(name: str) -> int:
+    """parsing.py:15-16"""
+    return int(name.split("#")[-1].replace("L", ""))
+
+
+def is_date(s: str) -> bool:
+    """conversion.py:20-21"""
+    return len(s) == 10 and s.count("-") == 2 and s.replace("-", "").isdigit()
+
+
+def is_float(s: str) -> bool:
+    """conversion.py:23-24"""
+    return s.replace(".", "").replace("-", "").replace("E", "").isdigit()
+
+
+def date_to_days(s: str) -> int:
+    """conversion.py:26-29: days between the date and 1990-01-01."""
+    return (_dt.date.fromisoformat(s) - _EPOCH).days
+
+
+# ---------------------------------------------------------------------------
+# Filter: operators/filter.py:14-162
+# ---------------------------------------------------------------------------
+def _cmp(op: str, a, b):
+    return {"<=": np.less_equal, ">=": np.greater_equal, "<": np.less, ">": np.greater,
+            "=": np.equal, "<>": np.not_equal}[op](a, b)
+
+
+def _is_int(a: np.ndarray) -> bool:
+    return a.dtype.kind in "iu"
+
+
+def _torch_compare(op: str, col: np.ndarray, lit):
+    """A column compared with a Python scalar, with torch's type promotion.
+
+    An integer column against a Python float is compared in float32 (torch's
+    default dtype); every other combination compares exactly.
+    """
+    if _is_int(col) and isinstance(lit, float):
+        return _cmp(op, col.astype(np.float32), np.float32(lit))
+    if _is_int(col):
+        return _cmp(op, col.astype(np.int64), np.int64(lit))
+    return _cmp(op, col, np.float64(lit))
+
+
+def _isclose(a: np.ndarray, b: float, rtol=1e-5, atol=EPS) -> np.ndarray:
+    """torch.isclose(a, full(b), atol=eps) as used at filter.py:160-161."""
+    err = np.abs(a - b)
+    allowed = atol + np.abs(rtol * b)
+    return (a == b) | (np.isfinite(err) & (err <= allowed))
+
+
+def eval_filter(tree, cols: Dict[int, np.ndarray], rows: int | None = None, subquery=None):
+    """Evaluate a parsed filter tree into a bool mask (filter.py:14-162).
+
+    String predicates (StartsWith/Contains/LIKE, multi-char equality) are not
+    restated: they are outside the hot path.
+    """
+    if rows is None:
+        rows = next(iter(cols.values())).shape[0]
+    if isinstance(tree, str):                                      # :18-35
+        if tree == "Subquery":
+            return subquery
+        if is_date(tree):
+            return date_to_days(tree)
+        if is_float(tree):
+            return float(tree) if "." in tree else int(tree)
+        if "#" in tree and not tree.startswith("Brand#"):
+            return cols[get_id(tree)].reshape(-1) if cols[get_id(tree)].ndim == 2 and cols[get_id(tree)].shape[1] == 1 else cols[get_id(tree)]
+        return tree
+    if len(tree) == 1:                                             # :37-38
+        return eval_filter(tree[0], cols, rows, subquery)
+    if len(tree) == 3 and tree[1] == "#":                          # :40-44
+        return cols[int(tree[-1])]
+    if len(tree) == 2:                                             # :46-86
+        if tree[0] == "NOT":
+            return ~eval_filter(tree[1], cols, rows, subquery)
+        if tree[0] == "isnotnull":
+            return np.ones(rows, dtype=bool)
+        if tree[0] == "cast":
+            literal, _, cast_type = tree[1][0].split(" ")
+            if cast_type == "double":
+                return eval_filter(literal, cols, rows, subquery)
+        raise NotImplementedError(f"filter function {tree[0]!r} is not on the oracle's path")
+    op = tree[-2]
+    if op == "IN":                                                 # :90-119
+        L = eval_filter(tree[0], cols, rows, subquery)
+        mask = np.zeros(rows, dtype=bool)
+        for r in tree[-1]:
+            if _is_int(L):
+                if len(r) == 1 and not r.lstrip("-").isdigit():
+                    mask |= L == ord(r)
+                else:
+                    mask |= L.astype(np.int64) == int(r)
+            else:
+                mask |= L == float(r)
+        return mask
+    if op not in ("<=", ">=", "<", ">", "=", "AND", "OR"):         # :129-140
+        raise NotImplementedError(f"filter operation {op!r} is not on the oracle's path")
+    L = eval_filter(tree[0], cols, rows, subquery)
+    R = eval_filter(tree[-1], cols, rows, subquery)
+    if op == "AND":
+        return np.logical_and(L, R)
+    if op == "OR":
+        return np.logical_or(L, R)
+    if isinstance(R, float):                                       # :145-149
+        if op == "<=":
+            return _torch_compare("<=", L, R + EPS)
+        if op == ">=":
+            return _torch_compare(">=", L, R - EPS)
+    if isinstance(R, str):                                         # :151-158
+        if len(R) == 1:
+            return _torch_compare(op, L, ord(R))
+        raise NotImplementedError("multi-character string compare is not on the oracle's path")
+    if op == "=" and L.dtype == np.float64:                        # :160-161
+        if not isinstance(R, float):
+            raise TypeError("isclose against a non-float literal (the reference raises here too)")
+        return _isclose(L, R)
+    if isinstance(R, np.ndarray):
+        return _cmp(op, L, R)
+    return _torch_compare(op, L, R)                                # :162
+
+
+# ---------------------------------------------------------------------------
+# Late materialisation: IO/vortex_pipeline.py:51-66
+# ---------------------------------------------------------------------------
+def apply_mask_map(cols: Dict[int, np.ndarray], mask_map: Dict[int, int]) -> Dict[int, np.ndarray]:
+    """Compacts every column that has a mask (``tensor[mask]``, :58) and drops
+    the mask columns themselves (:61-64)."""
+    masks = set(mask_map.values())
+    out = {}
+    for cid, a in cols.items():
+        if cid in masks:
+            continue
+        out[cid] = a[cols[mask_map[cid]]] if cid in mask_map else a
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Join: operators/hashjoin.py:24-177
+# ---------------------------------------------------------------------------
+def join_indices(left: np.ndarray, right: np.ndarray, jtype: str = "inner"):
+    """Sort-based equi-join of two key columns (hashjoin.py:24-151).
+
+    Returns (left_idx, right_idx) as int64; for ``right-outer`` unmatched right
+    rows are appended with left index ``NULL`` (:135-158).
+    """
+    left = left.reshape(-1)
+    right = right.reshape(-1)
+    perm = np.argsort(left, kind="stable")                         # :41-44
+    sorted_keys = left[perm]
+    uniq, starts, counts = np.unique(sorted_keys, return_index=True, return_counts=True)  # :48-52
+    pos = np.searchsorted(uniq, right)                             # :57
+    in_range = pos < uniq.size                                     # :59
+    eq = np.zeros(right.size, dtype=bool)
+    eq[in_range] = uniq[pos[in_range]] == right[in_range]          # :60-61
+    mr = np.nonzero(eq)[0]                                         # :65
+    if mr.size:
+        b = pos[mr]
+        lens = counts[b]
+        cr = np.repeat(mr, lens)                                   # :93
+        offs = np.arange(cr.size) - np.repeat(np.cumsum(lens) - lens, lens)
+        cs = perm[np.repeat(starts[b], lens) + offs]               # :77-86
+    else:
+        cs = np.zeros(0, np.int64)
+        cr = np.zeros(0, np.int64)
+    cs = cs.astype(np.int64)
+    cr = cr.astype(np.int64)
+    if jtype == "inner":                                           # :118-120
+        return cs, cr
+    matched = np.unique(cr)
+    if jtype == "right-semi":                                      # :121-124
+        return np.zeros(0, np.int64), matched
+    unmatched = np.setdiff1d(np.arange(right.size, dtype=np.int64), matched)
+    if jtype == "right-anti":                                      # :125-134
+        return np.zeros(0, np.int64), unmatched
+    if jtype == "right-outer":                                     # :135-158
+        if cs.size == 0:
+            # :154 only pads the left index when there was at least one match
+            return cs, np.concatenate([cr, unmatched])
+        return (np.concatenate([cs, np.full(unmatched.size, NULL, np.int64)]),
+                np.concatenate([cr, unmatched]))
+    raise ValueError(jtype)
+
+
+def index_with_null(data: np.ndarray, idx: np.ndarray) -> np.ndarray:
+    """conversion.py:52-57"""
+    m = idx == NULL
+    out = data[np.where(m, 0, idx)]
+    out = out.copy()
+    out[m] = NULL
+    return out
+
+
+def join_vortex(cols: Dict[int, np.ndarray], args: dict, leftcol: int, rightcol: int, jtype: str):
+    """hashjoin.py:179-248: late-materialised inputs, join, gathered outputs.
+
+    ``cols`` maps column id -> array (masks included).  Returns a new dict
+    with the output columns replaced and the operator's row count.
+    """
+    mask_map = {int(k): v for k, v in args.get("mask map", {}).items()}
+    groups = [args["left group"], args["right group"]]
+    out_ids, inp = [], {}
+    for side in (0, 1):
+        for c in args["materialized in"]:
+            if c in groups[side]:
+                inp[c] = cols[c]
+                out_ids.append(c)
+                if c in mask_map:
+                    inp[mask_map[c]] = cols[mask_map[c]]
+    used_masks = {c: mask_map[c] for c in out_ids if c in mask_map}
+    m = apply_mask_map(inp, used_masks)
+    li, ri = join_indices(m[leftcol], m[rightcol], jtype)
+    sel = index_with_null if (jtype == "right-outer" and li.size > 0) else (lambda x, i: x[i])
+    res = dict(cols)
+    for c in out_ids:
+        a = m[c]
+        if c in groups[0]:
+            res[c] = sel(a, li) if a.shape[0] > 0 else a[:0]
+        else:
+            res[c] = a[ri] if a.shape[0] > 0 else a[:0]
+    rows = next(iter(res.values())).shape[0]
+    return res, rows
+
+
+# ---------------------------------------------------------------------------
+# Aggregate: operators/aggregate.py:58-393
+# ---------------------------------------------------------------------------
+class _V:
+    """A value during expression evaluation: an array or a Python scalar."""
+
+
+def _promote(a, b):
+    """torch result type of a binary op between arrays/Python scalars.
+
+    Supported: f64 with anything -> f64; integers with integers -> int64.
+    An integer tensor with a Python float (or a true division of integers)
+    gives float32 in torch; that case is rejected, as it is by the product.
+    """
+    def kind(x):
+        if isinstance(x, np.ndarray):
+            return "f" if x.dtype.kind == "f" else ("b" if x.dtype == bool else "i")
+        return "pf" if isinstance(x, float) else "pi"
+    ka, kb = kind(a), kind(b)
+    if "f" in (ka, kb):
+        return np.float64
+    if ("pf" in (ka, kb)):
+        raise NotImplementedError("integer column with a float literal promotes to float32 in torch")
+    return np.int64
+
+
+def eval_agg_expr(tree, cols: Dict[int, np.ndarray]):
+    """Row-wise expression part of aggregate.py:58-233 (arithmetic only)."""
+    if isinstance(tree, str):                                      # :59-67
+        if tree.isdigit():
+            return int(tree)
+        if is_float(tree):
+            return float(tree)
+        if "#" in tree and tree.split("#")[-1].replace("L", "").isdigit():
+            return cols[get_id(tree)]
+        return tree
+    if len(tree) == 1:
+        return eval_agg_expr(tree[0], cols)
+    if len(tree) == 3 and tree[1] == "#":
+        return eval_agg_expr(tree[0], cols)
+    op = tree[-2]
+    if op == "AS":
+        return eval_agg_expr(tree[0], cols)
+    if op not in "+-*/":
+        raise NotImplementedError(f"aggregate expression operation {op!r}")
+    L = eval_agg_expr(tree[0], cols)
+    R = eval_agg_expr(tree[-1], cols)
+    if op == "/":
+        t = np.float64 if _promote(L, R) == np.float64 else None
+        if t is None:
+            raise NotImplementedError("integer true division promotes to float32 in torch")
+    t = _promote(L, R)
+    La = np.asarray(L, dtype=t) if not isinstance(L, np.ndarray) else L.astype(t, copy=False)
+    Ra = np.asarray(R, dtype=t) if not isinstance(R, np.ndarray) else R.astype(t, copy=False)
+    with np.errstate(all="ignore"):
+        return {"+": np.add, "-": np.subtract, "*": np.multiply, "/": np.true_divide}[op](La, Ra)
+
+
+def group_rows(key_cols: Sequence[np.ndarray]) -> Tuple[List[np.ndarray], np.ndarray]:
+    """Group ids of key tuples (aggregate.py:298-333), ordered by key tuple."""
+    n = key_cols[0].shape[0]
+    flat = [k.reshape(n, -1) for k in key_cols]
+    if n == 0:
+        return [k.reshape(0, -1)[:0] for k in key_cols], np.zeros(0, np.int64)
+    order = np.lexsort([f[:, j] for f in reversed(flat) for j in reversed(range(f.shape[1]))])
+    stacked = [f[order] for f in flat]
+    change = np.zeros(n, dtype=bool)
+    change[0] = True
+    for s in stacked:
+        change[1:] |= np.any(s[1:] != s[:-1], axis=1)
+    gid_sorted = np.cumsum(change) - 1
+    inverse = np.empty(n, np.int64)
+    inverse[order] = gid_sorted
+    firsts = order[change]
+    return [f[firsts] for f in flat], inverse
+
+
+def reduce_groups(fn: str, v, inverse: np.ndarray, G: int, n: int) -> np.ndarray:
+    """The reductions of aggregate.py:122-195 (both the bincount and the
+    2-step scatter_reduce forms compute the same mathematical result)."""
+    if isinstance(v, int):                                          # :149-152
+        v = np.full(n, v, np.int64)
+    elif isinstance(v, float):
+        v = np.full(n, v, np.float64)
+    is_int = v.dtype.kind in "iub"
+    if fn == "min":                                                 # :154-160
+        init = np.iinfo(np.int64).max if is_int else np.finfo(np.float64).max
+        out = np.full(G, init, dtype=np.int64 if is_int else np.float64)
+        np.minimum.at(out, inverse, v)
+        return out
+    if fn == "max":                                                 # :161-167 (initial value 0)
+        out = np.zeros(G, dtype=np.int64 if is_int else np.float64)
+        np.maximum.at(out, inverse, v)
+        return out
+    if fn == "avg":                                                 # :168-177
+        s = np.bincount(inverse, weights=v.astype(np.float64), minlength=G)
+        c = np.bincount(inverse, minlength=G)
+        with np.errstate(all="ignore"):
+            return s / c
+    if fn == "count":                                               # :184-185
+        v = (v != NULL).astype(np.int64)
+        is_int = True
+    s = np.bincount(inverse, weights=v.astype(np.float64), minlength=G)   # :187-190
+    if is_int:                                                      # :192-193
+        return np.round(s).astype(np.int64)
+    return s
+
+
+def fsum_groups(v: np.ndarray, inverse: np.ndarray, G: int) -> np.ndarray:
+    """Correctly rounded per-group sums (math.fsum), the accuracy reference."""
+    import math
+    order = np.argsort(inverse, kind="stable")
+    bounds = np.searchsorted(inverse[order], np.arange(G + 1))
+    vs = v[order]
+    return np.array([math.fsum(vs[bounds[g]:bounds[g + 1]]) for g in range(G)], dtype=np.float64)
+
+
+def _strip(tree):
+    while isinstance(tree, list) and len(tree) == 1:
+        tree = tree[0]
+    return tree
+
+
+def _is_key(tree) -> bool:
+    return isinstance(tree, str) or (len(tree) == 3 and tree[1] == "AS" and isinstance(tree[0], str))
+
+
+def _right_most(tree):
+    """parsing.py:42-45"""
+    return _right_most(tree[-1]) if isinstance(tree, list) else tree
+
+
+def _agg_fn_and_arg(tree):
+    """Walks [[fn, arg], '#', id] / [.., 'AS', name] down to (fn, arg)."""
+    t = tree
+    while True:
+        t = _strip(t)
+        if isinstance(t, list) and len(t) == 3 and t[1] in ("#", "AS"):
+            t = t[0]
+            continue
+        break
+    if not (isinstance(t, list) and len(t) == 2 and t[0] in ("sum", "avg", "count", "min", "max")):
+        raise NotImplementedError(f"aggregate result {tree!r} is not a plain aggregate call")
+    return t[0], t[1]
+
+
+def tqp_hash_aggregate(cols: Dict[int, np.ndarray], args: dict):
+    """aggregate.py:236-393: returns {out id: array} (keys as [G, 1])."""
+    assert not args["is partial"]
+    mask_map = {int(k): v for k, v in (args.get("mask map") or {}).items()}
+    inp = {c: cols[c] for c in args["input ids"]}
+    for k, v in mask_map.items():
+        if k in inp:
+            inp[v] = cols[v]
+    m = apply_mask_map(inp, {k: v for k, v in mask_map.items() if k in args["input ids"]})
+    n = next(iter(m.values())).shape[0]
+    if args["keys"]:
+        key_ids = [get_id(k) for k in args["keys"]]
+        ukeys, inverse = group_rows([m[k] for k in key_ids])
+        G = ukeys[0].shape[0]
+    else:
+        key_ids, ukeys, inverse, G = [], [], np.zeros(n, np.int64), 1
+    out = {}
+    for tree in args["results"]:
+        tree = _strip(tree)
+        oid = get_id(_right_most(tree))
+        if _is_key(tree):
+            kid = get_id(tree if isinstance(tree, str) else tree[0])
+            out[oid] = ukeys[key_ids.index(kid)].reshape(G, -1).astype(m[kid].dtype)
+        else:
+            fn, arg = _agg_fn_and_arg(tree)
+            out[oid] = reduce_groups(fn, eval_agg_expr(arg, m), inverse, G, n)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Sort: operators/sort.py:6-58
+# ---------------------------------------------------------------------------
+def _stable_order(x: np.ndarray, desc: bool) -> np.ndarray:
+    if x.ndim == 2:                                                 # :31-35 (unique ranks of rows)
+        _, inv = np.unique(x, axis=0, return_inverse=True)
+        x = inv.reshape(-1)
+    if not desc:
+        return np.argsort(x, kind="stable")
+    if x.dtype.kind == "f":
+        return np.argsort(-x, kind="stable")
+    return np.argsort(~x.astype(np.int64), kind="stable")
+
+
+def sort_perm(key_cols: Sequence[np.ndarray], descs: Sequence[bool]) -> np.ndarray:
+    """LSD sequence of stable sorts from the last key to the first (:22-35)."""
+    n = key_cols[0].shape[0]
+    perm = np.arange(n, dtype=np.int64)
+    for k, d in zip(reversed(list(key_cols)), reversed(list(descs))):
+        perm = perm[_stable_order(k[perm], d)]
+    return perm
+
+
+def tqp_sort(cols: Dict[int, np.ndarray], args: dict, with_limit: bool):
+    """sort.py:6-58: returns {id: reordered array} for every input id."""
+    perm = sort_perm([cols[k] for k in args["key ids"]], args["key orders"])
+    if with_limit:
+        perm = perm[: args["limit"]]
+    return {c: cols[c][perm] for c in args["input ids"]}

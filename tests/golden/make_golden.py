@@ -1,0 +1,486 @@
+"""Generate golden input/output vectors by running TQP-Inmem's own operators.
+
+This script is run by hand in a container where the TQP-Inmem source tree is
+mounted (default ``/root/reference``; override with ``TQP_REFERENCE``).  It
+imports the reference's operator modules unmodified and calls them through
+their public API on CPU torch:
+
+* ``operators/filter.py``    ``tqp_filter``
+* ``operators/hashjoin.py``  ``join_vortex`` / ``join_kernel_new``
+* ``operators/aggregate.py`` ``tqp_hash_aggregate``
+* ``operators/sort.py``      ``tqp_sort``
+
+Three adaptations make them run on a machine without CUDA, pandas, pyspark
+and pyparsing, and none of them touches the operators' arithmetic:
+
+1. ``pandas``/``pyspark``/``pyparsing`` are replaced by empty stand-in modules
+   (only ``pd.Timestamp`` is evaluated at import time, by ``conversion.py``).
+   ``parsing`` is replaced by a module built from the reference's own
+   ``get_id``/``get_name``/``get_literals``/``right_most`` function bodies,
+   extracted from ``parsing.py`` with ``ast`` (the rest of that file needs
+   Spark).
+2. ``IO/vortex_pipeline.py`` is compiled from its own source with the
+   ``assert ...is_cuda`` statements removed (the operators put CPU tensors
+   through it here).
+3. A ``TorchFunctionMode`` rewrites ``device='cuda'`` arguments to ``cpu`` and
+   ``torch.cuda.synchronize`` becomes a no-op.
+
+Each case is written to ``tests/golden/<case>.npz`` with its inputs, the
+operator arguments (JSON) and the outputs.  The fixtures are small (a few
+thousand to ~150k rows) so the tests that read them run in seconds.
+"""
+from __future__ import annotations
+
+import ast
+import copy
+import json
+import os
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+import torch
+from torch.overrides import TorchFunctionMode
+
+REF = Path(os.environ.get("TQP_REFERENCE", "/root/reference"))
+OUT = Path(__file__).resolve().parent
+
+
+# --------------------------------------------------------------------------
+# Loading the reference on CPU
+# --------------------------------------------------------------------------
+class _CudaToCpu(TorchFunctionMode):
+    """Rewrites device='cuda...' keyword arguments to the CPU."""
+
+    def __torch_function__(self, func, types_, args=(), kwargs=None):
+        kwargs = dict(kwargs or {})
+        dev = kwargs.get("device")
+        if dev is not None:
+            if (isinstance(dev, str) and dev.startswith("cuda")) or (
+                isinstance(dev, torch.device) and dev.type == "cuda"
+            ):
+                kwargs["device"] = "cpu"
+        return func(*args, **kwargs)
+
+
+def _stub(name: str, **attrs) -> types.ModuleType:
+    m = types.ModuleType(name)
+    for k, v in attrs.items():
+        setattr(m, k, v)
+    sys.modules[name] = m
+    return m
+
+
+def _module_from_functions(name: str, path: Path, fnames: set[str]) -> types.ModuleType:
+    tree = ast.parse(path.read_text())
+    body = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in fnames]
+    mod = types.ModuleType(name)
+    exec(compile(ast.Module(body=body, type_ignores=[]), str(path), "exec"), mod.__dict__)
+    mod.__dict__["re"] = __import__("re")
+    sys.modules[name] = mod
+    return mod
+
+
+class _StripCudaAsserts(ast.NodeTransformer):
+    def visit_Assert(self, node):
+        return None if "is_cuda" in ast.unparse(node) else node
+
+
+def load_reference():
+    class _Timestamp:  # conversion.py computes one epoch at import time
+        def __init__(self, *a, **k):
+            pass
+
+    _stub("pandas", Timestamp=_Timestamp, Timedelta=None, DataFrame=None)
+    _stub("pyspark")
+    _stub("pyspark.sql", SparkSession=None)
+    _stub("pyspark.sql.types", StructType=None, DateType=None, StructField=None,
+          IntegerType=None, StringType=None, DoubleType=None)
+    _stub("pyparsing")
+    _stub("expression", parse=None)
+    sys.path.insert(0, str(REF))
+    _module_from_functions("parsing", REF / "parsing.py",
+                           {"get_id", "get_name", "get_literals", "right_most"})
+    import IO  # noqa: F401  (package)
+    src = (REF / "IO" / "vortex_pipeline.py").read_text()
+    tree = _StripCudaAsserts().visit(ast.parse(src))
+    ast.fix_missing_locations(tree)
+    vp = types.ModuleType("IO.vortex_pipeline")
+    vp.__file__ = str(REF / "IO" / "vortex_pipeline.py")
+    sys.modules["IO.vortex_pipeline"] = vp
+    exec(compile(tree, vp.__file__, "exec"), vp.__dict__)
+    torch.cuda.synchronize = lambda *a, **k: None
+    from utility import logger
+    logger.set_perf_logger(None, False)      # as main.py does before running queries
+    logger.set_message_logger(None, False)
+    from operators import filter as f, hashjoin as hj, aggregate as ag, sort as so
+    import variable
+    return f, hj, ag, so, variable
+
+
+class _Pool:
+    """Stands in for IO/pinned_mem.GPUMemory: plain allocations, no slab."""
+
+    def malloc_like(self, t):
+        return 0, torch.empty_like(t)
+
+
+# --------------------------------------------------------------------------
+# Synthetic inputs (same distributions as the benchmark generators)
+# --------------------------------------------------------------------------
+def lineitem_like(rng, n):
+    return {
+        "quantity": rng.integers(1, 51, n).astype(np.float64),
+        "price": rng.integers(90000, 10495001, n).astype(np.float64) / 100.0,
+        "discount": rng.integers(0, 11, n).astype(np.float64) / 100.0,
+        "tax": rng.integers(0, 9, n).astype(np.float64) / 100.0,
+        "flag": rng.integers(0, 3, n).astype(np.uint8),
+        "status": rng.integers(0, 2, n).astype(np.uint8),
+        "ship_date": rng.integers(0, 2557, n).astype(np.int32),
+    }
+
+
+CASES = {}
+
+
+def case(fn):
+    CASES[fn.__name__] = fn
+    return fn
+
+
+def _save(name, inputs: dict, args: dict, outputs: dict):
+    arrays = {f"in_{k}": np.ascontiguousarray(v) for k, v in inputs.items()}
+    arrays.update({f"out_{k}": np.ascontiguousarray(v) for k, v in outputs.items()})
+    arrays["args"] = np.array(json.dumps(args))
+    np.savez_compressed(OUT / f"{name}.npz", **arrays)
+    sizes = {k: v.shape for k, v in outputs.items()}
+    print(f"{name}: {len(inputs)} inputs, outputs {sizes}")
+
+
+def _tg(V, cols: dict, types_: dict):
+    return {cid: V(torch.from_numpy(np.ascontiguousarray(a)), types_[cid]) for cid, a in cols.items()}
+
+
+# --------------------------------------------------------------------------
+# Cases
+# --------------------------------------------------------------------------
+@case
+def filter_agg_sort_lineitem(ref):
+    """Filter (ship_date <= 2470) -> 2-key group-by with 8 aggregates -> sort."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(11)
+    n = 20000
+    t = lineitem_like(rng, n)
+    ids = {"quantity": 1, "price": 2, "discount": 3, "tax": 4, "flag": 5, "status": 6, "ship_date": 7}
+    types_ = {1: "float", 2: "float", 3: "float", 4: "float", 5: "int", 6: "int", 7: "date"}
+    cols = {ids[k]: v for k, v in t.items()}
+    tg = _tg(V.Variable, cols, types_)
+    fargs = {"name": "Filter", "filter tree": [[["isnotnull", ["ship_date#7"]], "AND", ["ship_date#7", "<=", "2470"]]],
+             "materialized in": [7], "out mask id": 900}
+    f.tqp_filter(False, tg, copy.deepcopy(fargs), None, None, _Pool(), "f")
+    mask = tg[900].tensor.numpy().copy()
+    results = [
+        "flag#5", "status#6",
+        [[["sum", ["quantity#1"]], "#", "101"], "AS", "sum_qty#201"],
+        [[["sum", ["price#2"]], "#", "102"], "AS", "sum_base_price#202"],
+        [[["sum", [["price#2", "*", ["1.0", "-", "discount#3"]]]], "#", "103"], "AS", "sum_disc_price#203"],
+        [[["sum", [[["price#2", "*", ["1.0", "-", "discount#3"]], "*", ["1.0", "+", "tax#4"]]]], "#", "104"], "AS", "sum_charge#204"],
+        [[["avg", ["quantity#1"]], "#", "105"], "AS", "avg_qty#205"],
+        [[["avg", ["price#2"]], "#", "106"], "AS", "avg_price#206"],
+        [[["avg", ["discount#3"]], "#", "107"], "AS", "avg_disc#207"],
+        [[["count", ["1"]], "#", "108L"], "AS", "count_order#208"],
+    ]
+    aargs = {"name": "Aggregate", "is partial": False, "keys": ["flag#5", "status#6"],
+             "input ids": [1, 2, 3, 4, 5, 6], "results": results,
+             "out agg ids": [201, 202, 203, 204, 205, 206, 207, 208],
+             "mask map": {1: 900, 2: 900, 3: 900, 4: 900, 5: 900, 6: 900}}
+    torch.manual_seed(0)
+    ag.tqp_hash_aggregate(False, tg, copy.deepcopy(aargs), _Pool(), None, "a")
+    sargs = {"name": "Sort", "input ids": [5, 6, 201, 202, 203, 204, 205, 206, 207, 208],
+             "key ids": [5, 6], "key orders": [False, False]}
+    so.tqp_sort(False, tg, copy.deepcopy(sargs), False, "s")
+    outs = {"mask": mask}
+    for cid in sargs["input ids"]:
+        outs[str(cid)] = tg[cid].tensor.numpy()
+    _save("filter_agg_sort_lineitem", {str(k): v for k, v in cols.items()},
+          {"filter": fargs, "aggregate": _jsonable(aargs), "sort": sargs, "types": types_}, outs)
+
+
+def _jsonable(d):
+    d = copy.deepcopy(d)
+    if "mask map" in d:
+        d["mask map"] = {str(k): v for k, v in d["mask map"].items()}
+    return d
+
+
+@case
+def filter_predicates(ref):
+    """One table, many predicate trees through tqp_filter (int, date, float+eps, isclose, IN, NOT, char)."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(12)
+    n = 5003
+    cols = {
+        1: rng.integers(0, 2557, n).astype(np.int32),                      # date
+        2: (rng.integers(0, 11, n) / 100.0).astype(np.float64),            # float (0.00..0.10)
+        3: rng.integers(-50, 50, n).astype(np.int64),                      # int
+        4: rng.integers(65, 70, n).astype(np.uint8),                       # 1-char flags 'A'..'E'
+        5: rng.normal(0, 1000, n).astype(np.float64),                      # float, signed
+    }
+    cols[2][:7] = [0.05, 0.05 + 1e-6, 0.05 - 1e-6, 0.05 + 2e-5, 0.06, 0.07 - 1e-9, 0.0]
+    cols[5][:4] = [0.0, -0.0, 100.5, 100.5 + 2e-5]
+    types_ = {1: "date", 2: "float", 3: "int", 4: "int", 5: "float"}
+    trees = [
+        ["d#1", "<=", "2470"],
+        ["d#1", "<", "1170"],
+        ["d#1", ">", "1170"],
+        ["d#1", ">=", "100"],
+        ["d#1", "=", "42"],
+        [[["d#1", ">=", "100"], "AND", ["d#1", "<", "500"]], "OR", ["d#1", ">", "2500"]],
+        ["x#2", "<=", "0.05"],
+        ["x#2", ">=", "0.05"],
+        ["x#2", "<", "0.05"],
+        ["x#2", ">", "0.07"],
+        ["x#2", "=", "0.06"],
+        [["x#2", ">=", "0.02"], "AND", ["x#2", "<=", "0.04"]],
+        ["NOT", [["x#2", ">", "0.08"]]],
+        ["k#3", "IN", ["1", "5", "-7", "49"]],
+        [["isnotnull", ["k#3"]], "AND", ["k#3", "<", "0"]],
+        ["c#4", "=", "B"],
+        [["c#4", "=", "A"], "OR", ["c#4", "=", "E"]],
+        ["y#5", "<=", "100.5"],
+        ["y#5", ">=", "-3.25"],
+        ["y#5", "=", "100.5"],
+        ["y#5", "<=", "0"],
+        ["d#1", "<=", "100.5"],
+        [["NOT", [["d#1", "<", "1000"]]], "AND", [["y#5", ">", "0.0"], "OR", ["k#3", "=", "3"]]],
+    ]
+    outs = {}
+    for i, tree in enumerate(trees):
+        used = sorted({int(s.split("#")[1]) for s in _leaves(tree) if "#" in s})
+        tg = _tg(V.Variable, {c: cols[c] for c in used}, types_)
+        fa = {"name": "Filter", "filter tree": [tree], "materialized in": used, "out mask id": 999}
+        f.tqp_filter(False, tg, fa, None, None, _Pool(), "f")
+        outs[f"mask{i}"] = tg[999].tensor.numpy().astype(np.bool_)
+    _save("filter_predicates", {str(k): v for k, v in cols.items()},
+          {"trees": trees, "types": types_}, outs)
+
+
+def _leaves(t):
+    if isinstance(t, str):
+        yield t
+    else:
+        for e in t:
+            yield from _leaves(e)
+
+
+def _join_case(ref, name, rng, nb, npb, key_gen, jtype):
+    f, hj, ag, so, V = ref
+    bkey = key_gen(rng, nb)
+    cols = {
+        11: bkey,
+        12: rng.integers(0, 2557, nb).astype(np.int32),
+        21: rng.integers(1, max(2, nb) + 1, npb).astype(np.int32),
+        22: rng.integers(0, 2557, npb).astype(np.int32),
+        23: rng.integers(90000, 10495001, npb).astype(np.float64) / 100.0,
+        24: rng.integers(0, 11, npb).astype(np.float64) / 100.0,
+    }
+    types_ = {11: "int", 12: "date", 21: "int", 22: "date", 23: "float", 24: "float"}
+    tg = _tg(V.Variable, cols, types_)
+    f1 = {"name": "Filter", "filter tree": [["bd#12", "<", "1170"]], "materialized in": [12], "out mask id": 901}
+    f2 = {"name": "Filter", "filter tree": [["pd#22", ">", "1170"]], "materialized in": [22], "out mask id": 902}
+    f.tqp_filter(False, tg, copy.deepcopy(f1), None, None, _Pool(), "f1")
+    f.tqp_filter(False, tg, copy.deepcopy(f2), None, None, _Pool(), "f2")
+    jargs = {"name": "Join", "left group": [11, 12], "right group": [21, 22, 23, 24],
+             "materialized in": [11, 21, 23, 24], "mask map": {11: 901, 21: 902, 23: 902, 24: 902},
+             "left keys": [11], "right keys": [21], "join type": jtype}
+    jt = {"Inner": "inner", "LeftSemi": "right-semi", "LeftOuter": "right-outer", "LeftAnti": "right-anti"}[jtype]
+    rows = hj.join_vortex(False, tg, copy.deepcopy(jargs), 11, 21, [], jt, None, _Pool(), "j")
+    outs = {"rows": np.array(rows), "mask901": tg[901].tensor.numpy(), "mask902": tg[902].tensor.numpy()}
+    for k in [11, 21, 23, 24]:
+        outs[str(k)] = tg[k].tensor.numpy()
+    args = {"filters": [f1, f2], "join": _jsonable(jargs), "type": jt, "types": types_}
+    if jtype == "Inner":
+        aargs = {"name": "Aggregate", "is partial": False, "keys": ["bkey#11"], "input ids": [11, 23, 24],
+                 "results": ["bkey#11", [[["sum", [["price#23", "*", ["1.0", "-", "disc#24"]]]], "#", "301"], "AS", "revenue#302"]],
+                 "out agg ids": [302]}
+        torch.manual_seed(1)
+        ag.tqp_hash_aggregate(False, tg, copy.deepcopy(aargs), _Pool(), None, "a")
+        outs["agg_key"] = tg[11].tensor.numpy()
+        outs["agg_revenue"] = tg[302].tensor.numpy()
+        targs = {"name": "take ordered", "limit": 10, "input ids": [11, 302], "key ids": [302], "key orders": [True]}
+        so.tqp_sort(False, tg, copy.deepcopy(targs), True, "t")
+        outs["top_key"] = tg[11].tensor.numpy()
+        outs["top_revenue"] = tg[302].tensor.numpy()
+        args.update({"aggregate": aargs, "topk": targs})
+    _save(name, {str(k): v for k, v in cols.items()}, args, outs)
+
+
+@case
+def join_agg_topk_unique(ref):
+    """Filtered build (unique keys) x filtered probe -> inner join -> group-by build key -> top-10."""
+    _join_case(ref, "join_agg_topk_unique", np.random.default_rng(13), 6000, 24000,
+               lambda rng, n: (rng.permutation(n) + 1).astype(np.int32), "Inner")
+
+
+@case
+def join_duplicates(ref):
+    """Build keys with duplicates (lmax > 1), inner join."""
+    _join_case(ref, "join_duplicates", np.random.default_rng(14), 3000, 9000,
+               lambda rng, n: rng.integers(1, n // 3 + 1, n).astype(np.int32), "Inner")
+
+
+@case
+def join_semi(ref):
+    _join_case(ref, "join_semi", np.random.default_rng(15), 2000, 7000,
+               lambda rng, n: rng.integers(1, n // 2 + 1, n).astype(np.int32), "LeftSemi")
+
+
+@case
+def join_anti(ref):
+    _join_case(ref, "join_anti", np.random.default_rng(16), 2000, 7000,
+               lambda rng, n: rng.integers(1, n // 2 + 1, n).astype(np.int32), "LeftAnti")
+
+
+@case
+def join_outer(ref):
+    _join_case(ref, "join_outer", np.random.default_rng(17), 2000, 7000,
+               lambda rng, n: rng.integers(1, n // 2 + 1, n).astype(np.int32), "LeftOuter")
+
+
+@case
+def join_kernel_direct(ref):
+    """join_kernel_new called directly: int64 keys, negative keys, empty-match and no-duplicate edge cases."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(18)
+    outs, inputs = {}, {}
+    specs = [
+        ("neg", rng.integers(-1000, 1000, 1500).astype(np.int64), rng.integers(-1200, 1200, 4000).astype(np.int64)),
+        ("nomatch", np.arange(0, 500, dtype=np.int64), np.arange(1000, 1400, dtype=np.int64)),
+        ("big", (rng.integers(0, 2**40, 800) * 3).astype(np.int64), None),
+        ("single", np.array([7], dtype=np.int64), np.array([7, 7, 1, 7], dtype=np.int64)),
+    ]
+    for name, lk, rk in specs:
+        if rk is None:
+            rk = np.concatenate([lk[rng.integers(0, lk.size, 1500)], rng.integers(0, 2**40, 500).astype(np.int64)])
+        L = {1: V.Variable(torch.from_numpy(lk), "int"), 2: V.Variable(torch.arange(lk.size, dtype=torch.int64), "int")}
+        R = {3: V.Variable(torch.from_numpy(rk), "int"), 4: V.Variable(torch.arange(rk.size, dtype=torch.int64), "int")}
+        res = hj.join_kernel_new(False, L, R, 1, 3, [], [2, 4], False, "inner", None, None)
+        inputs[f"{name}_left"], inputs[f"{name}_right"] = lk, rk
+        outs[f"{name}_lidx"] = res[0].numpy()
+        outs[f"{name}_ridx"] = res[1].numpy()
+    _save("join_kernel_direct", inputs, {"specs": [s[0] for s in specs]}, outs)
+
+
+@case
+def aggregate_ops(ref):
+    """Group-by over int32+int64 keys with sum/avg/count/min/max on int and float values; global aggregate."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(19)
+    n = 30000
+    cols = {
+        1: rng.integers(-3, 4, n).astype(np.int32),
+        2: rng.integers(0, 200, n).astype(np.int64),
+        3: rng.normal(10.0, 50.0, n).astype(np.float64),
+        4: rng.integers(0, 1000, n).astype(np.int64),
+    }
+    types_ = {1: "int", 2: "int", 3: "float", 4: "int"}
+    results = [
+        "k1#1", "k2#2",
+        [[["sum", ["v#3"]], "#", "401"], "AS", "s#501"],
+        [[["avg", ["v#3"]], "#", "402"], "AS", "a#502"],
+        [[["min", ["v#3"]], "#", "403"], "AS", "mn#503"],
+        [[["max", ["w#4"]], "#", "404"], "AS", "mx#504"],
+        [[["sum", ["w#4"]], "#", "405"], "AS", "si#505"],
+        [[["count", ["w#4"]], "#", "406L"], "AS", "c#506"],
+        [[["sum", [["v#3", "*", "2.5"]]], "#", "407"], "AS", "e#507"],
+        [[["min", ["w#4"]], "#", "408"], "AS", "mni#508"],
+    ]
+    aargs = {"name": "Aggregate", "is partial": False, "keys": ["k1#1", "k2#2"], "input ids": [1, 2, 3, 4],
+             "results": results, "out agg ids": [501, 502, 503, 504, 505, 506, 507, 508]}
+    tg = _tg(V.Variable, cols, types_)
+    torch.manual_seed(2)
+    ag.tqp_hash_aggregate(False, tg, copy.deepcopy(aargs), _Pool(), None, "a")
+    outs = {str(c): tg[c].tensor.numpy() for c in [1, 2, 501, 502, 503, 504, 505, 506, 507, 508]}
+    # global (no keys) aggregate over the same table
+    gres = [[[["sum", ["v#3"]], "#", "411"], "AS", "gs#511"],
+            [[["count", ["1"]], "#", "412L"], "AS", "gc#512"],
+            [[["max", ["v#3"]], "#", "413"], "AS", "gm#513"],
+            [[["avg", ["w#4"]], "#", "414"], "AS", "ga#514"]]
+    gargs = {"name": "Aggregate", "is partial": False, "keys": None, "input ids": [3, 4],
+             "results": gres, "out agg ids": [511, 512, 513, 514]}
+    tg2 = _tg(V.Variable, {3: cols[3], 4: cols[4]}, types_)
+    ag.tqp_hash_aggregate(False, tg2, copy.deepcopy(gargs), _Pool(), None, "g")
+    for c in [511, 512, 513, 514]:
+        outs[str(c)] = tg2[c].tensor.numpy()
+    _save("aggregate_ops", {str(k): v for k, v in cols.items()},
+          {"aggregate": aargs, "global": gargs, "types": types_}, outs)
+
+
+@case
+def aggregate_two_step(ref):
+    """rows/groups >= 2^16 selects the reference's 2-step scatter_reduce path."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(20)
+    n = 140000
+    cols = {1: rng.integers(0, 2, n).astype(np.int64),
+            2: (rng.integers(90000, 10495001, n) / 100.0).astype(np.float64),
+            3: rng.integers(1, 51, n).astype(np.int64)}
+    types_ = {1: "int", 2: "float", 3: "int"}
+    results = ["g#1",
+               [[["sum", ["p#2"]], "#", "601"], "AS", "s#701"],
+               [[["avg", ["p#2"]], "#", "602"], "AS", "a#702"],
+               [[["min", ["p#2"]], "#", "603"], "AS", "mn#703"],
+               [[["max", ["q#3"]], "#", "604"], "AS", "mx#704"],
+               [[["count", ["1"]], "#", "605L"], "AS", "c#705"],
+               [[["sum", ["q#3"]], "#", "606"], "AS", "sq#706"]]
+    aargs = {"name": "Aggregate", "is partial": False, "keys": ["g#1"], "input ids": [1, 2, 3],
+             "results": results, "out agg ids": [701, 702, 703, 704, 705, 706]}
+    tg = _tg(V.Variable, cols, types_)
+    torch.manual_seed(3)
+    ag.tqp_hash_aggregate(False, tg, copy.deepcopy(aargs), _Pool(), None, "a")
+    outs = {str(c): tg[c].tensor.numpy() for c in [1, 701, 702, 703, 704, 705, 706]}
+    _save("aggregate_two_step", {str(k): v for k, v in cols.items()}, {"aggregate": aargs, "types": types_}, outs)
+
+
+@case
+def sort_multikey(ref):
+    """tqp_sort: multi-key (desc float, asc int, desc int), ties, limit; plus [G,1] 2-D keys."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(21)
+    n = 4000
+    cols = {1: rng.integers(0, 5, n).astype(np.float64) * 0.5,
+            2: rng.integers(-20, 20, n).astype(np.int64),
+            3: rng.integers(0, 3, n).astype(np.int32),
+            4: np.arange(n, dtype=np.int64),
+            5: rng.integers(0, 4, (n, 1)).astype(np.uint8)}
+    cols[1][:3] = [-0.0, 0.0, -1.5]
+    types_ = {1: "float", 2: "int", 3: "date", 4: "int", 5: "int"}
+    outs = {}
+    specs = [
+        ({"input ids": [1, 2, 3, 4], "key ids": [1, 2, 3], "key orders": [True, False, True]}, False),
+        ({"input ids": [1, 2, 3, 4], "key ids": [2], "key orders": [True], "limit": 25}, True),
+        ({"input ids": [1, 2, 4], "key ids": [1], "key orders": [False], "limit": 100}, True),
+        ({"input ids": [5, 4], "key ids": [5, 2], "key orders": [False, True]}, False),
+    ]
+    for i, (sa, lim) in enumerate(specs):
+        used = sorted(set(sa["input ids"]) | set(sa["key ids"]))
+        tg = _tg(V.Variable, {c: cols[c] for c in used}, types_)
+        so.tqp_sort(False, tg, copy.deepcopy(sa), lim, "s")
+        for c in sa["input ids"]:
+            outs[f"s{i}_{c}"] = tg[c].tensor.numpy()
+    _save("sort_multikey", {str(k): v for k, v in cols.items()},
+          {"specs": [[s, l] for s, l in specs], "types": types_}, outs)
+
+
+def main(argv):
+    ref = load_reference()
+    with _CudaToCpu():
+        for name, fn in CASES.items():
+            if len(argv) > 1 and name not in argv[1:]:
+                continue
+            fn(ref)
+
+
+if __name__ == "__main__":
+    main(sys.argv)

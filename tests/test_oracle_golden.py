@@ -1,0 +1,141 @@
+"""Pins the oracle against golden vectors produced by the reference's own
+operators (tests/golden/make_golden.py).  CPU only."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import tqp_oracle as O
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def load(name):
+    z = np.load(GOLD / f"{name}.npz", allow_pickle=False)
+    ins = {int(k[3:]) if k[3:].isdigit() else k[3:]: z[k] for k in z.files if k.startswith("in_")}
+    outs = {k[4:]: z[k] for k in z.files if k.startswith("out_")}
+    return ins, outs, json.loads(str(z["args"]))
+
+
+def _by_key(keys, *vals):
+    order = np.lexsort([k.reshape(-1) for k in reversed(keys)])
+    return [k.reshape(-1)[order] for k in keys], [v[order] for v in vals]
+
+
+def assert_f64_close(a, b, rel=1e-12):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    assert a.shape == b.shape
+    scale = np.maximum(np.abs(a), np.abs(b))
+    assert np.all(np.abs(a - b) <= rel * scale + 1e-300), (a, b)
+
+
+def test_filter_predicates():
+    ins, outs, args = load("filter_predicates")
+    for i, tree in enumerate(args["trees"]):
+        got = O.eval_filter([tree], ins)
+        np.testing.assert_array_equal(got.reshape(-1), outs[f"mask{i}"], err_msg=str(tree))
+
+
+def test_filter_agg_sort_lineitem():
+    ins, outs, args = load("filter_agg_sort_lineitem")
+    mask = O.eval_filter(args["filter"]["filter tree"], {7: ins[7]})
+    np.testing.assert_array_equal(mask, outs["mask"])
+    cols = dict(ins)
+    cols[900] = mask
+    agg = O.tqp_hash_aggregate(cols, args["aggregate"])
+    srt = O.tqp_sort(agg, args["sort"], False)
+    for cid in args["sort"]["input ids"]:
+        g, o = outs[str(cid)], srt[cid]
+        assert g.dtype == o.dtype and g.shape == o.shape, cid
+        if g.dtype == np.float64:
+            assert_f64_close(o, g)
+        else:
+            np.testing.assert_array_equal(o, g)
+
+
+@pytest.mark.parametrize("name", ["join_agg_topk_unique", "join_duplicates", "join_semi", "join_anti", "join_outer"])
+def test_join_cases(name):
+    ins, outs, args = load(name)
+    cols = dict(ins)
+    for fa in args["filters"]:
+        used = fa["materialized in"]
+        cols[fa["out mask id"]] = O.eval_filter(fa["filter tree"], {c: ins[c] for c in used})
+    np.testing.assert_array_equal(cols[901], outs["mask901"])
+    np.testing.assert_array_equal(cols[902], outs["mask902"])
+    res, rows = O.join_vortex(cols, args["join"], 11, 21, args["type"])
+    assert rows == int(outs["rows"].reshape(-1)[0])
+    # pairs are compared as sorted sets of output rows
+    ids = (11, 21, 23, 24)
+    if outs["11"].size == 0:          # semi / anti joins output no build-side rows
+        assert res[11].size == 0
+        ids = (21, 23, 24)
+    got = np.stack([res[c].astype(np.float64) for c in ids], 1)
+    exp = np.stack([outs[str(c)].astype(np.float64) for c in ids], 1)
+    np.testing.assert_array_equal(got[np.lexsort(got.T[::-1])], exp[np.lexsort(exp.T[::-1])])
+    if "aggregate" in args:
+        agg = O.tqp_hash_aggregate(res, args["aggregate"])
+        (gk,), (gv,) = _by_key([outs["agg_key"]], outs["agg_revenue"])
+        np.testing.assert_array_equal(agg[11].reshape(-1), gk)
+        assert_f64_close(agg[302], gv)
+        top = O.tqp_sort({11: agg[11], 302: agg[302]}, args["topk"], True)
+        np.testing.assert_array_equal(top[11], outs["top_key"])
+        assert_f64_close(top[302], outs["top_revenue"])
+
+
+def test_join_kernel_direct():
+    ins, outs, args = load("join_kernel_direct")
+    for name in args["specs"]:
+        li, ri = O.join_indices(ins[f"{name}_left"], ins[f"{name}_right"], "inner")
+        got = np.stack([li, ri], 1)
+        exp = np.stack([outs[f"{name}_lidx"], outs[f"{name}_ridx"]], 1)
+        np.testing.assert_array_equal(got[np.lexsort(got.T[::-1])], exp[np.lexsort(exp.T[::-1])])
+        # probe-row order is the reference's (ascending matched right row)
+        np.testing.assert_array_equal(ri, outs[f"{name}_ridx"])
+
+
+def test_aggregate_ops():
+    ins, outs, args = load("aggregate_ops")
+    agg = O.tqp_hash_aggregate(dict(ins), args["aggregate"])
+    ids = args["aggregate"]["out agg ids"]
+    keys_g, vals_g = _by_key([outs["1"], outs["2"]], *[outs[str(i)] for i in ids])
+    np.testing.assert_array_equal(agg[1].reshape(-1), keys_g[0])
+    np.testing.assert_array_equal(agg[2].reshape(-1), keys_g[1])
+    for i, g in zip(ids, vals_g):
+        assert agg[i].dtype == g.dtype, i
+        if g.dtype == np.float64:
+            assert_f64_close(agg[i], g)
+        else:
+            np.testing.assert_array_equal(agg[i], g)
+    glob = O.tqp_hash_aggregate({3: ins[3], 4: ins[4]}, args["global"])
+    for i in args["global"]["out agg ids"]:
+        g = outs[str(i)]
+        assert glob[i].dtype == g.dtype
+        assert_f64_close(glob[i], g) if g.dtype == np.float64 else np.testing.assert_array_equal(glob[i], g)
+
+
+def test_aggregate_two_step():
+    ins, outs, args = load("aggregate_two_step")
+    agg = O.tqp_hash_aggregate(dict(ins), args["aggregate"])
+    ids = args["aggregate"]["out agg ids"]
+    (k,), vals = _by_key([outs["1"]], *[outs[str(i)] for i in ids])
+    np.testing.assert_array_equal(agg[1].reshape(-1), k)
+    for i, g in zip(ids, vals):
+        assert agg[i].dtype == g.dtype
+        assert_f64_close(agg[i], g) if g.dtype == np.float64 else np.testing.assert_array_equal(agg[i], g)
+
+
+def test_sort_multikey():
+    ins, outs, args = load("sort_multikey")
+    for i, (spec, lim) in enumerate(args["specs"]):
+        res = O.tqp_sort(ins, spec, lim)
+        for c in spec["input ids"]:
+            np.testing.assert_array_equal(res[c], outs[f"s{i}_{c}"], err_msg=f"spec {i} col {c}")
+
+
+def test_fsum_truth_close_to_bincount():
+    rng = np.random.default_rng(5)
+    v = rng.integers(90000, 10495001, 200000) / 100.0
+    inv = rng.integers(0, 4, v.size)
+    assert_f64_close(O.fsum_groups(v, inv, 4), np.bincount(inv, weights=v, minlength=4), rel=1e-13)

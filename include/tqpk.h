@@ -1,0 +1,299 @@
+/*
+ * tqpk.h - C ABI of libtqpk.so, the GB300 (sm_103a) kernels behind TQP-Inmem's
+ * relational operator hot path.
+ *
+ * Every pointer named d_* or passed inside a column descriptor is a device
+ * pointer; h_* pointers are host pointers.  Every entry point returns an int
+ * status (TQPK_OK = 0, negative on error) and enqueues its work on the given
+ * CUDA stream.  Entry points whose contract says "synchronises" wait on that
+ * stream before returning (they need a device-side count on the host, as the
+ * reference does with .item()/nonzero at the same places).
+ *
+ * Reference interfaces replaced (paths inside TQP-Inmem):
+ *   tqpk_filter_mask        operators/filter.py:14-162 (evaluate), :164-204 (tqp_filter)
+ *   tqpk_compact            IO/vortex_pipeline.py:51-66 (tensor[mask] late materialisation)
+ *   tqpk_groupby_*          operators/aggregate.py:236-393 (tqp_hash_aggregate / agg_wrapper / evaluate)
+ *   tqpk_argsort_stable     operators/sort.py:22-35 (LSD sequence of stable torch.sort)
+ *   tqpk_topk_stable        operators/sort.py:41-42 (full sort, then perm[:limit])
+ *   tqpk_join_*             operators/hashjoin.py:24-177 (join_kernel_new), :179-248 (join_vortex)
+ *   tqpk_gather             hashjoin.py:153-175 + conversion.py:52-57 (x[idx], index_with_null)
+ *   tqpk_pipeline_*         fused forms of filter -> join -> aggregate (main.py:152-253 call order)
+ */
+#ifndef TQPK_H
+#define TQPK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void* tqpk_stream; /* a cudaStream_t */
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  TQPK_OK = 0,
+  TQPK_EINVAL = -1,       /* bad argument (null pointer, size, count)              */
+  TQPK_ENOMEM = -2,       /* workspace too small                                   */
+  TQPK_ETIMEOUT = -3,     /* a bounded device-side wait gave up                    */
+  TQPK_EDTYPE = -4,       /* unsupported dtype code                                */
+  TQPK_ECUDA = -5,        /* CUDA launch/runtime error                             */
+  TQPK_ECAPACITY = -6,    /* output capacity too small (required size returned)    */
+  TQPK_EUNSUPPORTED = -7  /* shape the kernels do not handle (caller must not fall back) */
+};
+
+/* ---- dtype codes (constants.py:3-6: string int8, int int64, float f64, date int32)
+ * TQPK_ROWID is accepted only as a tqpk_compact output: it writes each kept
+ * row's index (int64) and ignores the input pointer.                        */
+enum { TQPK_ROWID = 0, TQPK_I8 = 1, TQPK_U8 = 2, TQPK_I32 = 3, TQPK_I64 = 4, TQPK_F64 = 5, TQPK_BOOL = 6 };
+
+#define TQPK_MAX_COLS 16
+#define TQPK_MAX_PRED 32
+#define TQPK_MAX_KEYS 4
+#define TQPK_MAX_EXPR 32
+#define TQPK_MAX_ACCS 16
+#define TQPK_NULL_INDEX (-64) /* constants.py:9 null, used by index_with_null */
+
+/* ---- predicate program (filter.py:14-162) --------------------------------
+ * Postfix program over up to TQPK_MAX_COLS columns.  CMP pushes
+ * (col <cmp> literal) evaluated in `domain`; AND/OR pop two, NOT pops one;
+ * TRUE pushes all-true (isnotnull, filter.py:67-69); MASK pushes a bool column.
+ *   domain I64: integer column vs Python int, exact.
+ *   domain F64: float64 column (or int column vs int literal on a float column).
+ *   domain F32: integer column vs Python float (torch promotes to float32).
+ *   ISCLOSE: |x - lit| <= lit_aux (allowed error, precomputed as atol + |rtol*lit|)
+ *            or x == lit, as torch.isclose (filter.py:160-161).
+ * Float literals for <= and >= arrive with the reference's +-eps already added
+ * (filter.py:145-149).                                                      */
+enum { TQPK_P_CMP = 1, TQPK_P_AND = 2, TQPK_P_OR = 3, TQPK_P_NOT = 4, TQPK_P_TRUE = 5,
+       TQPK_P_FALSE = 6, TQPK_P_MASK = 7, TQPK_P_CMPCOL = 8 /* cols[col] <cmp> cols[lit_i] */ };
+enum { TQPK_LT = 0, TQPK_LE = 1, TQPK_GT = 2, TQPK_GE = 3, TQPK_EQ = 4, TQPK_NE = 5, TQPK_ISCLOSE = 6 };
+enum { TQPK_DOM_I64 = 0, TQPK_DOM_F64 = 1, TQPK_DOM_F32 = 2 };
+
+typedef struct {
+  int32_t op, col, cmp, domain;
+  int64_t lit_i;
+  double lit_f;
+  double lit_aux;
+} tqpk_pred_insn;
+
+typedef struct {
+  int32_t n_insn;
+  int32_t n_cols;
+  const void* cols[TQPK_MAX_COLS];
+  int32_t dtypes[TQPK_MAX_COLS];
+  tqpk_pred_insn insn[TQPK_MAX_PRED];
+} tqpk_predicate;
+
+/* ---- row expressions (aggregate.py:58-233, arithmetic part) --------------
+ * Straight-line SSA program: instruction i writes register i.  Operands a, b
+ * are earlier register numbers.  Arithmetic follows torch's promotion:
+ * registers are float64 or int64 (`type`); float64 arithmetic is IEEE
+ * round-to-nearest per operation (no contraction), as torch evaluates it.   */
+enum { TQPK_X_COL = 1, TQPK_X_CONST = 2, TQPK_X_ADD = 3, TQPK_X_SUB = 4, TQPK_X_MUL = 5,
+       TQPK_X_DIV = 6, TQPK_X_TOF64 = 7 };
+
+typedef struct {
+  int32_t op, type; /* type: TQPK_I64 or TQPK_F64 */
+  int32_t a, b;     /* operand registers */
+  int32_t col;      /* TQPK_X_COL: column slot */
+  int32_t pad;
+  int64_t ci;       /* TQPK_X_CONST integer value */
+  double cf;        /* TQPK_X_CONST float value */
+} tqpk_expr_insn;
+
+/* Accumulators (aggregate.py:122-195).  sum/avg/count/min/max of the
+ * reference map onto these; avg = SUM / COUNT_ROWS at emit.
+ * MAX starts from 0 and MIN from the dtype maximum, as the reference's
+ * scatter_reduce initial tensors do (aggregate.py:154-167).               */
+enum { TQPK_ACC_SUM = 1, TQPK_ACC_COUNT_NOTNULL = 2, TQPK_ACC_COUNT_ROWS = 3, TQPK_ACC_MIN = 4,
+       TQPK_ACC_MAX = 5 };
+
+typedef struct {
+  int32_t kind;  /* TQPK_ACC_* */
+  int32_t type;  /* TQPK_F64 or TQPK_I64: register type of `reg` */
+  int32_t reg;   /* expression register accumulated (ignored by COUNT_ROWS) */
+  int32_t pad;
+  int64_t init_i; /* MIN/MAX initial value for I64 */
+  double init_f;  /* MIN/MAX initial value for F64 */
+} tqpk_acc;
+
+typedef struct {
+  int32_t n_keys;
+  const void* keys[TQPK_MAX_KEYS];
+  int32_t key_dtypes[TQPK_MAX_KEYS];
+  int32_t n_cols;
+  const void* cols[TQPK_MAX_COLS];
+  int32_t col_dtypes[TQPK_MAX_COLS];
+  int32_t n_expr;
+  tqpk_expr_insn expr[TQPK_MAX_EXPR];
+  int32_t n_accs;
+  tqpk_acc accs[TQPK_MAX_ACCS];
+} tqpk_groupby_spec;
+
+/* Plan chosen from the key ranges (tqpk_groupby_plan). */
+enum { TQPK_GB_GLOBAL_ONE = 0, TQPK_GB_DENSE_PRIVATE = 1, TQPK_GB_DENSE_SHARED = 2,
+       TQPK_GB_DENSE_GLOBAL = 3, TQPK_GB_HASH = 4 };
+
+typedef struct {
+  int32_t mode;
+  int32_t threads;
+  int64_t n_rows;                /* rows passing the filter */
+  int64_t slots;                 /* dense slots or hash capacity */
+  int64_t key_min[TQPK_MAX_KEYS];
+  int64_t key_range[TQPK_MAX_KEYS];
+  int64_t key_stride[TQPK_MAX_KEYS];
+  size_t ws_bytes;               /* workspace needed by run + emit */
+} tqpk_gb_plan;
+
+/* ---- general --------------------------------------------------------- */
+int tqpk_version(void);
+const char* tqpk_status_string(int status);
+/* Number of kernel launches this thread has issued through the library. */
+int64_t tqpk_launch_count(void);
+/* Writes sizeof() of tqpk_pred_insn, tqpk_predicate, tqpk_expr_insn, tqpk_acc,
+ * tqpk_groupby_spec, tqpk_gb_plan, tqpk_join_plan (in that order, up to n of
+ * them) so bindings can verify their struct layouts; returns the count.   */
+int tqpk_abi_sizes(int64_t* out, int n);
+
+/* Kernel timing (for roofline measurement): after tqpk_timing_begin(id),
+ * every launch of kernel `id` is bracketed by CUDA events on its stream;
+ * tqpk_timing_end synchronises on them and returns the summed device time.
+ * Ids: 1 filter mask, 3 group-by, 5 join probe, 6 fused probe+aggregate,
+ * 7 fused build, 8 fused top-k, 9 star-join probe, 10 batched work queue.  */
+int tqpk_timing_begin(int32_t kernel_id);
+int tqpk_timing_end(double* h_total_ms, int32_t* h_launches);
+
+/* ---- (a) filter -------------------------------------------------------- */
+/* mask[i] = pred(row i) for i < n; *d_count += number of true rows.
+ * d_count may be NULL.  Replaces filter.py:14-204.                         */
+int tqpk_filter_mask(const tqpk_predicate* h_pred, int64_t n, uint8_t* d_mask,
+                     unsigned long long* d_count, tqpk_stream stream);
+
+/* Stream compaction, stable: keeps rows where d_mask[i] != 0 (or, when
+ * d_mask is NULL, where the predicate holds).  Writes *d_count (int64).
+ * Replaces vortex_pipeline.py:58 (tensor[mask]) for up to TQPK_MAX_COLS
+ * columns in one pass.                                                    */
+size_t tqpk_compact_workspace_bytes(int64_t n);
+int tqpk_compact(const tqpk_predicate* h_pred, const uint8_t* d_mask, int64_t n, int32_t ncols,
+                 const void* const* h_cols_in, const int32_t* h_dtypes, void* const* h_cols_out,
+                 int64_t* d_count, void* d_ws, size_t ws_bytes, tqpk_stream stream);
+
+/* ---- (d) group-by aggregation ----------------------------------------- */
+/* Computes the key ranges of the rows passing the filter (d_mask or h_pred,
+ * either may be NULL) and picks the kernel.  Synchronises.                */
+int tqpk_groupby_plan(const tqpk_groupby_spec* h_spec, const tqpk_predicate* h_pred,
+                      const uint8_t* d_mask, int64_t n, tqpk_gb_plan* h_plan,
+                      void* d_scratch32, tqpk_stream stream);
+/* Accumulates every passing row into the plan's table (filter fused: rows
+ * that fail the predicate are never materialised) and counts the groups
+ * into *h_groups.  Synchronises.                                          */
+int tqpk_groupby_run(const tqpk_groupby_spec* h_spec, const tqpk_gb_plan* h_plan,
+                     const tqpk_predicate* h_pred, const uint8_t* d_mask, int64_t n, void* d_ws,
+                     size_t ws_bytes, int64_t* h_groups, tqpk_stream stream);
+/* Writes the groups in ascending key-tuple order: one column per key (in the
+ * key's dtype) and n_out value columns.  h_out_ops holds 4 ints per output:
+ * {op, a, b, dtype}: op TQPK_OUT_ACC copies accumulator a; TQPK_OUT_AVG
+ * writes acc a / acc b in float64 (aggregate.py:168-177).  dtype is the
+ * output column's dtype code.  groups must be the count run returned.      */
+enum { TQPK_OUT_ACC = 0, TQPK_OUT_AVG = 1 };
+int tqpk_groupby_emit(const tqpk_groupby_spec* h_spec, const tqpk_gb_plan* h_plan, void* d_ws,
+                      int64_t groups, void* const* h_out_keys, int32_t n_out, const int32_t* h_out_ops,
+                      void* const* h_out_cols, tqpk_stream stream);
+
+/* ---- (b) sort ---------------------------------------------------------- */
+/* Stable LSD radix sort of keys[perm_in[i]] (perm_in NULL = identity) with
+ * payload perm_in[i]; writes the sorted permutation (int64) to d_perm_out.
+ * One call is one iteration of sort.py:26-35's key loop.  descending keeps
+ * ties in input order (torch.sort(stable=True, descending=True)).
+ * Float keys: -0.0 sorts equal to +0.0 and NaN sorts as the largest value. */
+size_t tqpk_sort_workspace_bytes(int64_t n);
+int tqpk_argsort_stable(const void* d_keys, int32_t key_dtype, int32_t descending,
+                        const int64_t* d_perm_in, int64_t n, int64_t* d_perm_out, void* d_ws,
+                        size_t ws_bytes, tqpk_stream stream);
+
+/* ---- (e) top-k ------------------------------------------------------------
+ * The first k entries of the stable sort of keys[perm_in[i]]:
+ * d_perm_out[0..k) = perm_in of the k smallest (largest if descending) keys,
+ * ties in input order.  Equals sort.py:41-42 (full stable sort, then
+ * perm[:limit]) without sorting the rest.                                   */
+size_t tqpk_topk_workspace_bytes(int64_t n, int64_t k);
+int tqpk_topk_stable(const void* d_keys, int32_t key_dtype, int32_t descending,
+                     const int64_t* d_perm_in, int64_t n, int64_t k, int64_t* d_perm_out,
+                     void* d_ws, size_t ws_bytes, tqpk_stream stream);
+
+/* ---- (c) join ---------------------------------------------------------- */
+enum { TQPK_JOIN_DIRECT = 1, TQPK_JOIN_SORTED = 2 };
+enum { TQPK_JT_INNER = 0, TQPK_JT_SEMI = 1, TQPK_JT_ANTI = 2, TQPK_JT_OUTER = 3 };
+
+typedef struct {
+  int32_t mode;        /* TQPK_JOIN_DIRECT (dense key range) or TQPK_JOIN_SORTED */
+  int32_t unique;      /* build keys are unique (set by tqpk_join_build) */
+  int64_t nb_rows;     /* build rows passing the build filter */
+  int64_t key_min, key_max;
+  int64_t slots;       /* DIRECT: key_max - key_min + 1 */
+  int64_t n_unique;    /* SORTED: distinct build keys (set by tqpk_join_build) */
+  size_t ws_bytes;     /* build workspace (kept alive until the probes are done) */
+} tqpk_join_plan;
+
+/* Build-side key range of the rows passing the build mask; picks the mode.
+ * Synchronises.                                                            */
+int tqpk_join_plan_build(const void* d_build_keys, int32_t key_dtype, const uint8_t* d_build_mask,
+                         int64_t nb, tqpk_join_plan* h_plan, void* d_scratch32,
+                         tqpk_stream stream);
+/* Builds the directory (DIRECT: key -> build row, CSR of rows for duplicate
+ * keys; SORTED: radix-sorted (key,row) with run starts).  Synchronises to
+ * learn whether the build keys are unique.                                  */
+int tqpk_join_build(tqpk_join_plan* h_plan, const void* d_build_keys, int32_t key_dtype,
+                    const uint8_t* d_build_mask, int64_t nb, void* d_ws, size_t ws_bytes,
+                    tqpk_stream stream);
+/* Probes every probe row passing its mask against the directory that
+ * tqpk_join_build left in d_build_ws and writes the matches in the
+ * reference's order (ascending probe row; inside one build-key bucket,
+ * ascending build row) as int64 row ids of the ORIGINAL (uncompacted)
+ * inputs.  INNER writes pairs; SEMI/ANTI write probe rows only (d_out_build
+ * unused, may be NULL); OUTER writes the pairs, then the unmatched probe rows
+ * with build id TQPK_NULL_INDEX.  *h_count is the number of outputs; when it
+ * exceeds capacity only the first `capacity` are written and TQPK_ECAPACITY
+ * is returned (call again with a larger buffer).  Synchronises.             */
+size_t tqpk_join_probe_workspace_bytes(int64_t np);
+int tqpk_join_probe(const tqpk_join_plan* h_plan, const void* d_build_ws, const void* d_probe_keys,
+                    int32_t probe_dtype, const uint8_t* d_probe_mask, int64_t np, int32_t join_type,
+                    int64_t* d_out_build, int64_t* d_out_probe, int64_t capacity, int64_t* h_count,
+                    void* d_probe_ws, size_t probe_ws_bytes, tqpk_stream stream);
+
+/* ---- fused pipelines ------------------------------------------------------
+ * Filter -> inner join on a unique build key -> sum(expr) group by build key
+ * -> top-k by the sum (k <= 32), with no host synchronisation: the main.py
+ * plan Filter(build), Filter(probe), Join, Aggregate, take ordered in three
+ * kernels.  [key_min, key_max] is the build table's key domain (a table
+ * statistic); the directory has one slot per key in it.  h_values holds the
+ * expression program over probe columns, value_reg the register summed.
+ * d_out_keys/d_out_vals receive min(k, groups) rows ordered by the sum
+ * (descending when `descending`), ties by ascending key; *d_out_count that
+ * count and *d_groups_out (may be NULL) the number of groups.  A repeated
+ * build key or one outside [key_min, key_max] sets the workspace error word
+ * (read it with tqpk_pipeline_error: TQPK_EUNSUPPORTED / TQPK_EINVAL); the
+ * caller then runs the operator path instead.                              */
+size_t tqpk_pipeline_join_agg_topk_workspace_bytes(int64_t key_min, int64_t key_max);
+int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t build_dtype, int64_t nb,
+                                const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max,
+                                const void* d_probe_fk, int32_t probe_dtype, int64_t np,
+                                const tqpk_predicate* h_probe_pred, const tqpk_groupby_spec* h_values,
+                                int32_t value_reg, int32_t k, int32_t descending, void* d_ws, size_t ws_bytes,
+                                int64_t* d_out_keys, double* d_out_vals, int64_t* d_out_count,
+                                int64_t* d_groups_out, tqpk_stream stream);
+/* Reads (synchronising) the error word a fused pipeline left in its workspace. */
+int tqpk_pipeline_error(const void* d_ws, int* h_err, tqpk_stream stream);
+
+/* Multi-column gather: out_c[j] = in_c[idx[j]]; with null_aware, an index
+ * equal to TQPK_NULL_INDEX gives the value -64 (conversion.py:52-57).       */
+int tqpk_gather(int32_t ncols, const void* const* h_cols_in, const int32_t* h_dtypes,
+                const int64_t* d_idx, int64_t n_idx, int32_t null_aware, void* const* h_cols_out,
+                tqpk_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TQPK_H */

@@ -1,0 +1,29 @@
+"""Loading helpers for tests/golden/*.npz (written by tests/golden/make_golden.py)."""
+import json
+from pathlib import Path
+
+import numpy as np
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def load(name):
+    z = np.load(GOLD / f"{name}.npz", allow_pickle=False)
+    ins = {int(k[3:]) if k[3:].isdigit() else k[3:]: z[k] for k in z.files if k.startswith("in_")}
+    outs = {k[4:]: z[k] for k in z.files if k.startswith("out_")}
+    return ins, outs, json.loads(str(z["args"]))
+
+
+def assert_f64_close(a, b, rel=1e-12):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    same_nan = np.isnan(a) & np.isnan(b)
+    scale = np.maximum(np.abs(a), np.abs(b))
+    ok = (np.abs(a - b) <= rel * scale) | same_nan | (a == b)
+    assert np.all(ok), (a[~ok][:5], b[~ok][:5])
+
+
+def rows_sorted(*cols):
+    m = np.stack([np.asarray(c).reshape(-1).astype(np.float64) for c in cols], 1)
+    return m[np.lexsort(m.T[::-1])] if m.size else m

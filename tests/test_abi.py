@@ -1,0 +1,71 @@
+"""libtqpk.so builds, loads without a GPU and exports every include/tqpk.h symbol."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from tqpk import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def declared_functions():
+    text = (ROOT / "include" / "tqpk.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tqpk_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("tqpk_filter_mask", "tqpk_compact", "tqpk_groupby_plan", "tqpk_groupby_run", "tqpk_groupby_emit",
+                 "tqpk_argsort_stable", "tqpk_topk_stable", "tqpk_join_plan_build", "tqpk_join_build",
+                 "tqpk_join_probe", "tqpk_gather"):
+        assert must in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    raw = ctypes.CDLL(str(Path(lib._name)))
+    missing = [n for n in declared_functions() if not hasattr(raw, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header():
+    from tqpk import _lib
+    assert set(declared_functions()) <= set(_lib.SIGNATURES), set(declared_functions()) - set(_lib.SIGNATURES)
+
+
+def test_struct_layouts_match(lib):
+    # load() already compared every ctypes struct size with the library's sizeof()
+    from tqpk import _lib
+    sizes = (ctypes.c_int64 * 7)()
+    assert lib.tqpk_abi_sizes(sizes, 7) == 7
+    assert sizes[0] == ctypes.sizeof(_lib.PredInsn) == 40
+
+
+def test_status_strings(lib):
+    from tqpk import _lib
+    assert lib.tqpk_status_string(_lib.OK) == b"ok"
+    assert lib.tqpk_status_string(_lib.ETIMEOUT) == b"bounded device wait expired"
+    with pytest.raises(TimeoutError):
+        _lib.check(_lib.ETIMEOUT, "x")
+    with pytest.raises(NotImplementedError):
+        _lib.check(_lib.EUNSUPPORTED, "x")
+
+
+def test_invalid_arguments_rejected_without_gpu(lib):
+    # argument checks run before any CUDA call
+    from tqpk import _lib
+    p = _lib.Predicate()
+    p.n_insn = 1
+    p.n_cols = 0
+    p.insn[0] = _lib.PredInsn(_lib.P_CMP, 3, _lib.LE, _lib.DOM_I64, 0, 0.0, 0.0)
+    assert lib.tqpk_filter_mask(ctypes.byref(p), 10, 1 << 20, None, None) == _lib.EINVAL
+    assert lib.tqpk_filter_mask(None, 10, 1 << 20, None, None) == _lib.EINVAL
+    assert lib.tqpk_argsort_stable(1 << 20, 77, 0, None, 10, 1 << 20, 1 << 20, 1 << 30, None) == _lib.EDTYPE
+    assert lib.tqpk_gather(1, None, None, None, -1, 0, None, None) == _lib.EINVAL

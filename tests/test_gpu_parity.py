@@ -1,0 +1,343 @@
+"""GPU parity: the CUDA path (through the drop-in operators and the C ABI)
+against golden vectors from the reference and against the oracle.
+
+Tolerances: masks, keys, counts, join pairs, sort orders bit-exact; float64
+sums and averages within 1e-12 relative (and within 1e-12 of math.fsum)."""
+import copy
+
+import numpy as np
+import pytest
+import torch
+
+from golden_io import assert_f64_close, load, rows_sorted
+from oracle import tqp_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need CUDA")
+    from tqpk import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def V(a, t="int"):
+    from tqpk.variable import Variable
+    return Variable(torch.from_numpy(np.ascontiguousarray(a)).cuda(), t)
+
+
+def tg_from(ins, types):
+    return {int(k): V(v, types[str(k)]) for k, v in ins.items() if isinstance(k, int)}
+
+
+def np_(t):
+    return t.detach().cpu().numpy()
+
+
+# ------------------------------------------------------------------ filter
+def test_filter_predicates_golden():
+    from tqpk.operators import tqp_filter
+    ins, outs, args = load("filter_predicates")
+    for i, tree in enumerate(args["trees"]):
+        used = sorted({int(s.split("#")[1]) for s in _leaves(tree) if "#" in s})
+        tg = {c: V(ins[c], args["types"][str(c)]) for c in used}
+        tqp_filter(True, tg, {"filter tree": [tree], "materialized in": used, "out mask id": 999},
+                   None, None, None, "f")
+        np.testing.assert_array_equal(np_(tg[999].tensor), outs[f"mask{i}"], err_msg=str(tree))
+
+
+def _leaves(t):
+    if isinstance(t, str):
+        yield t
+    else:
+        for e in t:
+            yield from _leaves(e)
+
+
+@pytest.mark.parametrize("n,offset", [(1, 0), (3, 0), (4097, 0), (1_000_003, 0), (100_003, 1), (100_003, 3)])
+def test_filter_matches_oracle_sizes_and_alignment(n, offset):
+    from tqpk.operators import tqp_filter
+    _, _, args = load("filter_predicates")
+    rng = np.random.default_rng(n + offset)
+    base = {1: rng.integers(0, 2557, n + offset).astype(np.int32),
+            2: (rng.integers(0, 11, n + offset) / 100.0),
+            3: rng.integers(-50, 50, n + offset).astype(np.int64),
+            4: rng.integers(65, 70, n + offset).astype(np.uint8),
+            5: rng.normal(0, 1000, n + offset)}
+    dev = {c: torch.from_numpy(a).cuda()[offset:] for c, a in base.items()}   # unaligned views when offset > 0
+    host = {c: a[offset:] for c, a in base.items()}
+    for tree in args["trees"]:
+        used = sorted({int(s.split("#")[1]) for s in _leaves(tree) if "#" in s})
+        from tqpk.variable import Variable
+        tg = {c: Variable(dev[c], args["types"][str(c)]) for c in used}
+        tqp_filter(True, tg, {"filter tree": [tree], "materialized in": used, "out mask id": 999}, None, None, None, "f")
+        np.testing.assert_array_equal(np_(tg[999].tensor), O.eval_filter([tree], host), err_msg=str(tree))
+
+
+@pytest.mark.parametrize("n", [0, 1, 5, 4096, 4097, 333_333])
+@pytest.mark.parametrize("density", [0.0, 0.03, 0.5, 1.0])
+def test_compact_stable(n, density):
+    from tqpk.ops import compact
+    rng = np.random.default_rng(n)
+    m = rng.random(n) < density
+    a = rng.integers(-2**40, 2**40, n)
+    b = rng.integers(0, 255, n).astype(np.uint8)
+    c = rng.random(n)
+    d = rng.integers(0, 1 << 30, n).astype(np.int32)
+    cols = [torch.from_numpy(x).cuda() for x in (a, b, c, d)]
+    out, cnt = compact(cols, mask=torch.from_numpy(m).cuda(), with_row_ids=True)
+    assert cnt == int(m.sum())
+    for got, exp in zip(out, (a[m], b[m], c[m], d[m], np.nonzero(m)[0])):
+        np.testing.assert_array_equal(np_(got), exp)
+
+
+# ------------------------------------------------------------------ filter + aggregate + sort (lineitem)
+def test_filter_agg_sort_lineitem_golden():
+    from tqpk.operators import tqp_filter, tqp_hash_aggregate, tqp_sort
+    ins, outs, args = load("filter_agg_sort_lineitem")
+    tg = tg_from(ins, args["types"])
+    tqp_filter(True, tg, copy.deepcopy(args["filter"]), None, None, None, "f")
+    np.testing.assert_array_equal(np_(tg[900].tensor), outs["mask"])
+    aargs = copy.deepcopy(args["aggregate"])
+    aargs["mask map"] = {int(k): v for k, v in aargs["mask map"].items()}
+    tqp_hash_aggregate(True, tg, aargs, None, None, "a")
+    tqp_sort(True, tg, copy.deepcopy(args["sort"]), False, "s")
+    for cid in args["sort"]["input ids"]:
+        g, o = outs[str(cid)], np_(tg[cid].tensor)
+        assert g.dtype == o.dtype and g.shape == o.shape, (cid, g.dtype, o.dtype, g.shape, o.shape)
+        if g.dtype == np.float64:
+            assert_f64_close(o, g)
+        else:
+            np.testing.assert_array_equal(o, g)
+
+
+def test_lineitem_scaled_vs_oracle_and_fsum():
+    from tqpk import datagen
+    from tqpk.operators import tqp_filter, tqp_hash_aggregate
+    _, _, args = load("filter_agg_sort_lineitem")
+    t = datagen.lineitem(2_000_003, seed=3)
+    ids = {"quantity": 1, "price": 2, "discount": 3, "tax": 4, "flag": 5, "status": 6, "ship_date": 7}
+    cols = {ids[k]: v for k, v in t.items()}
+    tg = {c: V(a, args["types"][str(c)]) for c, a in cols.items()}
+    tqp_filter(True, tg, copy.deepcopy(args["filter"]), None, None, None, "f")
+    aargs = copy.deepcopy(args["aggregate"])
+    aargs["mask map"] = {int(k): v for k, v in aargs["mask map"].items()}
+    tqp_hash_aggregate(True, tg, aargs, None, None, "a")
+    mask = cols[7] <= datagen.SHIP_DATE_MAX
+    ocols = dict(cols)
+    ocols[900] = mask
+    ref = O.tqp_hash_aggregate(ocols, copy.deepcopy(aargs))
+    np.testing.assert_array_equal(np_(tg[5].tensor), ref[5])
+    np.testing.assert_array_equal(np_(tg[6].tensor), ref[6])
+    for a in aargs["out agg ids"]:
+        if ref[a].dtype == np.float64:
+            assert_f64_close(np_(tg[a].tensor), ref[a])
+        else:
+            np.testing.assert_array_equal(np_(tg[a].tensor), ref[a])
+    # accuracy against the correctly rounded sum
+    flag, status = cols[5][mask], cols[6][mask]
+    _, inv = O.group_rows([flag, status])
+    G = int(inv.max()) + 1
+    truth = O.fsum_groups(cols[2][mask] * (1.0 - cols[3][mask]), inv, G)
+    assert_f64_close(np_(tg[203].tensor), truth)
+
+
+# ------------------------------------------------------------------ joins
+@pytest.mark.parametrize("name", ["join_agg_topk_unique", "join_duplicates", "join_semi", "join_anti", "join_outer"])
+def test_join_golden(name):
+    from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
+    ins, outs, args = load(name)
+    tg = tg_from(ins, args["types"])
+    for fa in args["filters"]:
+        tqp_filter(True, tg, copy.deepcopy(fa), None, None, None, "f")
+    np.testing.assert_array_equal(np_(tg[901].tensor), outs["mask901"])
+    jargs = copy.deepcopy(args["join"])
+    jargs["mask map"] = {int(k): v for k, v in jargs["mask map"].items()}
+    rows = join_vortex(True, tg, jargs, 11, 21, [], args["type"], None, None, "j")
+    assert rows == int(outs["rows"].reshape(-1)[0])
+    ids = (11, 21, 23, 24) if outs["11"].size else (21, 23, 24)
+    if not outs["11"].size:
+        assert tg[11].tensor.numel() == 0
+    np.testing.assert_array_equal(rows_sorted(*[np_(tg[c].tensor) for c in ids]),
+                                  rows_sorted(*[outs[str(c)] for c in ids]))
+    if "aggregate" in args:
+        if name == "join_agg_topk_unique":   # unique build keys: the reference's exact row order
+            for c in ids:
+                np.testing.assert_array_equal(np_(tg[c].tensor), outs[str(c)])
+        tqp_hash_aggregate(True, tg, copy.deepcopy(args["aggregate"]), None, None, "a")
+        order = np.argsort(outs["agg_key"].reshape(-1), kind="stable")
+        np.testing.assert_array_equal(np_(tg[11].tensor), outs["agg_key"][order])
+        assert_f64_close(np_(tg[302].tensor), outs["agg_revenue"][order])
+        tqp_sort(True, tg, copy.deepcopy(args["topk"]), True, "t")
+        np.testing.assert_array_equal(np_(tg[11].tensor), outs["top_key"])
+        assert_f64_close(np_(tg[302].tensor), outs["top_revenue"])
+
+
+def test_join_kernel_direct_golden():
+    from tqpk.operators import join_kernel_new
+    from tqpk.variable import Variable
+    ins, outs, args = load("join_kernel_direct")
+    for name in args["specs"]:
+        lk, rk = ins[f"{name}_left"], ins[f"{name}_right"]
+        Lt = {1: V(lk), 2: Variable(torch.arange(lk.size, device="cuda"), "int")}
+        Rt = {3: V(rk), 4: Variable(torch.arange(rk.size, device="cuda"), "int")}
+        li, ri = join_kernel_new(True, Lt, Rt, 1, 3, [], [2, 4], False, "inner", None, None)
+        np.testing.assert_array_equal(rows_sorted(np_(li), np_(ri)),
+                                      rows_sorted(outs[f"{name}_lidx"], outs[f"{name}_ridx"]))
+        np.testing.assert_array_equal(np_(ri), outs[f"{name}_ridx"])
+
+
+@pytest.mark.parametrize("nb,np_rows,dups,sparse", [(200_000, 800_000, False, False), (50_000, 300_000, True, False),
+                                                    (40_000, 100_000, False, True), (30_000, 90_000, True, True),
+                                                    (1, 10, False, False), (0, 100, False, False)])
+def test_join_scaled_vs_oracle(nb, np_rows, dups, sparse):
+    from tqpk.ops import join_build, join_probe
+    rng = np.random.default_rng(nb + np_rows)
+    if dups:
+        bk = rng.integers(1, max(2, nb // 3), nb)
+    else:
+        bk = rng.permutation(nb) + 1
+    if sparse:
+        bk = bk * 1_000_003 + 17
+    pk = bk[rng.integers(0, max(nb, 1), np_rows)] if nb else rng.integers(0, 5, np_rows)
+    pk = np.where(rng.random(np_rows) < 0.3, pk + 1, pk)
+    bm = rng.random(nb) < 0.6
+    pm = rng.random(np_rows) < 0.7
+    for dt in (np.int32, np.int64) if not sparse else (np.int64,):
+        b = join_build(torch.from_numpy(bk.astype(dt)).cuda(), torch.from_numpy(bm).cuda())
+        for jt in ("inner", "right-semi", "right-anti", "right-outer"):
+            bi, pi = join_probe(b, torch.from_numpy(pk.astype(dt)).cuda(), torch.from_numpy(pm).cuda(), jt)
+            bsel, psel = np.nonzero(bm)[0], np.nonzero(pm)[0]
+            li, ri = O.join_indices(bk[bm], pk[pm], jt)
+            exp_b = np.where(li == O.NULL, O.NULL, bsel[np.where(li == O.NULL, 0, li)]) if li.size else li
+            exp_p = psel[ri]
+            if jt in ("right-semi", "right-anti"):
+                np.testing.assert_array_equal(np_(pi), exp_p)
+            else:
+                if jt == "right-outer" and li.size == 0:
+                    exp_b = np.full(exp_p.size, O.NULL)
+                np.testing.assert_array_equal(np_(pi), exp_p)            # probe order is the reference's
+                np.testing.assert_array_equal(np_(bi), exp_b)            # stable bucket order
+
+
+# ------------------------------------------------------------------ aggregates
+def test_aggregate_ops_golden():
+    from tqpk.operators import tqp_hash_aggregate
+    ins, outs, args = load("aggregate_ops")
+    tg = tg_from(ins, args["types"])
+    tqp_hash_aggregate(True, tg, copy.deepcopy(args["aggregate"]), None, None, "a")
+    ids = args["aggregate"]["out agg ids"]
+    order = np.lexsort([outs["2"].reshape(-1), outs["1"].reshape(-1)])
+    np.testing.assert_array_equal(np_(tg[1].tensor), outs["1"][order])
+    np.testing.assert_array_equal(np_(tg[2].tensor), outs["2"][order])
+    for i in ids:
+        g = outs[str(i)][order]
+        o = np_(tg[i].tensor)
+        assert o.dtype == g.dtype, (i, o.dtype, g.dtype)
+        assert_f64_close(o, g) if g.dtype == np.float64 else np.testing.assert_array_equal(o, g)
+    tg2 = tg_from({3: ins[3], 4: ins[4]}, args["types"])
+    tqp_hash_aggregate(True, tg2, copy.deepcopy(args["global"]), None, None, "g")
+    for i in args["global"]["out agg ids"]:
+        g, o = outs[str(i)], np_(tg2[i].tensor)
+        assert o.dtype == g.dtype and o.shape == g.shape
+        assert_f64_close(o, g) if g.dtype == np.float64 else np.testing.assert_array_equal(o, g)
+
+
+def test_aggregate_two_step_golden():
+    from tqpk.operators import tqp_hash_aggregate
+    ins, outs, args = load("aggregate_two_step")
+    tg = tg_from(ins, args["types"])
+    tqp_hash_aggregate(True, tg, copy.deepcopy(args["aggregate"]), None, None, "a")
+    order = np.argsort(outs["1"].reshape(-1), kind="stable")
+    np.testing.assert_array_equal(np_(tg[1].tensor), outs["1"][order])
+    for i in args["aggregate"]["out agg ids"]:
+        g, o = outs[str(i)][order], np_(tg[i].tensor)
+        assert o.dtype == g.dtype
+        assert_f64_close(o, g) if g.dtype == np.float64 else np.testing.assert_array_equal(o, g)
+
+
+def test_aggregate_high_cardinality_vs_oracle():
+    from tqpk.operators import tqp_hash_aggregate
+    rng = np.random.default_rng(9)
+    n = 1_500_000
+    cols = {1: rng.integers(1, 600_000, n).astype(np.int32), 2: rng.integers(90000, 10495001, n) / 100.0,
+            3: rng.integers(0, 11, n) / 100.0}
+    args = {"is partial": False, "keys": ["k#1"], "input ids": [1, 2, 3],
+            "results": ["k#1", [[["sum", [["p#2", "*", ["1.0", "-", "d#3"]]]], "#", "9"], "AS", "r#10"],
+                        [[["count", ["1"]], "#", "8L"], "AS", "c#11"], [[["max", ["p#2"]], "#", "7"], "AS", "m#12"]],
+            "out agg ids": [10, 11, 12]}
+    tg = {1: V(cols[1]), 2: V(cols[2], "float"), 3: V(cols[3], "float")}
+    tqp_hash_aggregate(True, tg, copy.deepcopy(args), None, None, "a")
+    ref = O.tqp_hash_aggregate(cols, copy.deepcopy(args))
+    np.testing.assert_array_equal(np_(tg[1].tensor), ref[1])
+    assert_f64_close(np_(tg[10].tensor), ref[10])
+    np.testing.assert_array_equal(np_(tg[11].tensor), ref[11])
+    np.testing.assert_array_equal(np_(tg[12].tensor), ref[12])
+
+
+def test_aggregate_empty_and_all_filtered():
+    from tqpk.operators import tqp_filter, tqp_hash_aggregate
+    n = 1000
+    cols = {1: np.zeros(n, np.int32), 2: np.ones(n), 7: np.arange(n, dtype=np.int32)}
+    tg = {1: V(cols[1]), 2: V(cols[2], "float"), 7: V(cols[7], "date")}
+    tqp_filter(True, tg, {"filter tree": [["d#7", "<", "0"]], "materialized in": [7], "out mask id": 99},
+               None, None, None, "f")
+    args = {"is partial": False, "keys": ["k#1"], "input ids": [1, 2],
+            "results": ["k#1", [[["sum", ["p#2"]], "#", "9"], "AS", "r#10"]], "out agg ids": [10],
+            "mask map": {1: 99, 2: 99}}
+    tqp_hash_aggregate(True, tg, args, None, None, "a")
+    assert tg[10].tensor.numel() == 0 and tuple(tg[1].tensor.shape) == (0, 1)
+
+
+# ------------------------------------------------------------------ sort / top-k
+def test_sort_multikey_golden():
+    from tqpk.operators import tqp_sort
+    ins, outs, args = load("sort_multikey")
+    for i, (spec, lim) in enumerate(args["specs"]):
+        used = sorted(set(spec["input ids"]) | set(spec["key ids"]))
+        tg = {c: V(ins[c], args["types"][str(c)]) for c in used}
+        tqp_sort(True, tg, copy.deepcopy(spec), lim, "s")
+        for c in spec["input ids"]:
+            np.testing.assert_array_equal(np_(tg[c].tensor), outs[f"s{i}_{c}"], err_msg=f"spec {i} col {c}")
+
+
+@pytest.mark.parametrize("dtype", [np.int32, np.int64, np.float64, np.uint8, np.int8])
+@pytest.mark.parametrize("desc", [False, True])
+def test_argsort_stable_vs_numpy(dtype, desc):
+    from tqpk.ops import argsort_stable, topk_stable
+    rng = np.random.default_rng(3)
+    n = 1_000_003
+    if dtype == np.float64:
+        k = rng.integers(-500, 500, n) * 0.25
+        k[:4] = [-0.0, 0.0, np.inf, -np.inf]
+    elif dtype in (np.uint8, np.int8):
+        k = rng.integers(np.iinfo(dtype).min, np.iinfo(dtype).max, n).astype(dtype)
+    else:
+        k = rng.integers(np.iinfo(dtype).min // 2, np.iinfo(dtype).max // 2, n).astype(dtype)
+        k[rng.integers(0, n, n // 2)] = 7     # heavy ties
+    k = k.astype(dtype)
+    perm_in = rng.permutation(n)
+    got = np_(argsort_stable(torch.from_numpy(k).cuda(), desc, torch.from_numpy(perm_in).cuda()))
+    exp = perm_in[O._stable_order(k[perm_in], desc)]
+    np.testing.assert_array_equal(got, exp)
+    for kk in (1, 10, 100, 5000):
+        top = np_(topk_stable(torch.from_numpy(k).cuda(), kk, desc, torch.from_numpy(perm_in).cuda()))
+        np.testing.assert_array_equal(top, exp[:kk])
+
+
+# ------------------------------------------------------------------ loud failures
+def test_cpu_tensors_and_unsupported_shapes_raise():
+    from tqpk.ops import argsort_stable
+    from tqpk.operators import tqp_filter, tqp_hash_aggregate
+    with pytest.raises(ValueError):
+        argsort_stable(torch.zeros(10, dtype=torch.int32))
+    tg = {1: V(np.zeros(10, np.int8).reshape(5, 2))}
+    with pytest.raises(NotImplementedError):
+        tqp_filter(True, tg, {"filter tree": [["s#1", "=", "AB"]], "materialized in": [1], "out mask id": 2},
+                   None, None, None, "f")
+    with pytest.raises(NotImplementedError):
+        tqp_filter(False, tg, {"filter tree": [["s#1", "=", "A"]], "materialized in": [1], "out mask id": 2},
+                   None, None, None, "f")

@@ -1,0 +1,499 @@
+// groupby.cu - kernel (d): group-by aggregation fused with the filter.
+//
+// Reference: operators/aggregate.py:236-393.  The reference compacts every
+// input column with the filter mask (vortex_pipeline.py:58), hashes the key
+// tuple with random coefficients and sorts it (torch.unique(dim=0), :318-327),
+// then makes one full pass per aggregate (bincount / scatter_reduce, :122-195)
+// with the expression temporaries materialised (:203-233).
+//
+// Here one pass reads each needed column once; rows failing the filter are
+// skipped in registers (never compacted), the expression program runs in
+// registers, and every accumulator is updated in the same pass.  Groups are
+// addressed by a mixed-radix slot computed from the key ranges (one cheap
+// min/max pre-pass over the key columns), so no hashing or sorting is needed
+// and the groups come out in ascending key-tuple order:
+//
+//   DENSE_PRIVATE  slots*accs small: every thread owns a private copy of the
+//                  table in shared memory (plain loads/stores, no atomics --
+//                  shared-memory f64 atomics serialise badly on GB300).
+//   DENSE_SHARED   up to ~12k slot*accs: one table per CTA, shared atomics.
+//   DENSE_GLOBAL   up to max(4*rows, 2^20) slots: global (L2) atomics.
+//
+// FP64 work is the limit on GB300 (FP64 runs at 1/64 of the FP32 rate), so
+// the expression program is straight-line with shared subexpressions and no
+// FP64 atomics in shared memory.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace tqpk {
+
+struct GbDev {
+  int nk;
+  int64_t kmin[TQPK_MAX_KEYS];
+  int64_t kstride[TQPK_MAX_KEYS];
+  int64_t krange[TQPK_MAX_KEYS];
+  int64_t slots;
+};
+
+__device__ __forceinline__ uint64_t acc_init(const tqpk_acc& a) {
+  if (a.kind == TQPK_ACC_MIN || a.kind == TQPK_ACC_MAX)
+    return a.type == TQPK_F64 ? f64_ordered(a.init_f) : static_cast<uint64_t>(a.init_i);
+  return 0ull;
+}
+
+// Evaluates the expression program for one row into reg[] (int64 or f64 bits).
+__device__ __forceinline__ void eval_expr(const tqpk_groupby_spec& S, int64_t row, uint64_t* reg) {
+  for (int i = 0; i < S.n_expr; ++i) {
+    const tqpk_expr_insn& X = S.expr[i];
+    uint64_t r = 0;
+    const bool f = X.type == TQPK_F64;
+    switch (X.op) {
+      case TQPK_X_COL:
+        r = f ? d2u(ld_f64(S.cols[X.col], S.col_dtypes[X.col], row))
+              : static_cast<uint64_t>(ld_int(S.cols[X.col], S.col_dtypes[X.col], row));
+        break;
+      case TQPK_X_CONST: r = f ? d2u(X.cf) : static_cast<uint64_t>(X.ci); break;
+      case TQPK_X_TOF64: r = d2u(static_cast<double>(static_cast<int64_t>(reg[X.a]))); break;
+      case TQPK_X_ADD:
+        r = f ? d2u(__dadd_rn(u2d(reg[X.a]), u2d(reg[X.b]))) : reg[X.a] + reg[X.b];
+        break;
+      case TQPK_X_SUB:
+        r = f ? d2u(__dsub_rn(u2d(reg[X.a]), u2d(reg[X.b]))) : reg[X.a] - reg[X.b];
+        break;
+      case TQPK_X_MUL:
+        r = f ? d2u(__dmul_rn(u2d(reg[X.a]), u2d(reg[X.b])))
+              : static_cast<uint64_t>(static_cast<int64_t>(reg[X.a]) * static_cast<int64_t>(reg[X.b]));
+        break;
+      case TQPK_X_DIV: r = d2u(__ddiv_rn(u2d(reg[X.a]), u2d(reg[X.b]))); break;
+    }
+    reg[i] = r;
+  }
+}
+
+// Plain (owner-only) update of one accumulator cell.
+__device__ __forceinline__ void acc_plain(uint64_t* p, const tqpk_acc& a, const uint64_t* reg) {
+  switch (a.kind) {
+    case TQPK_ACC_SUM:
+      if (a.type == TQPK_F64) *p = d2u(__dadd_rn(u2d(*p), u2d(reg[a.reg])));
+      else *p += reg[a.reg];
+      break;
+    case TQPK_ACC_COUNT_ROWS: *p += 1; break;
+    case TQPK_ACC_COUNT_NOTNULL:
+      if (a.type == TQPK_F64) *p += (u2d(reg[a.reg]) != (double)TQPK_NULL_INDEX);
+      else *p += (static_cast<int64_t>(reg[a.reg]) != TQPK_NULL_INDEX);
+      break;
+    case TQPK_ACC_MIN:
+      if (a.type == TQPK_F64) *p = min(*p, f64_ordered(u2d(reg[a.reg])));
+      else *p = static_cast<uint64_t>(min(static_cast<int64_t>(*p), static_cast<int64_t>(reg[a.reg])));
+      break;
+    case TQPK_ACC_MAX:
+      if (a.type == TQPK_F64) *p = max(*p, f64_ordered(u2d(reg[a.reg])));
+      else *p = static_cast<uint64_t>(max(static_cast<int64_t>(*p), static_cast<int64_t>(reg[a.reg])));
+      break;
+  }
+}
+
+// Merge a value (already in accumulator encoding) into a shared cell atomically.
+__device__ __forceinline__ void acc_merge_atomic(uint64_t* p, const tqpk_acc& a, uint64_t v) {
+  switch (a.kind) {
+    case TQPK_ACC_SUM:
+      if (a.type == TQPK_F64) atomicAdd(reinterpret_cast<double*>(p), u2d(v));
+      else atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+      break;
+    case TQPK_ACC_COUNT_ROWS:
+    case TQPK_ACC_COUNT_NOTNULL: atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v); break;
+    case TQPK_ACC_MIN:
+      if (a.type == TQPK_F64) atomicMin(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+      else atomicMin(reinterpret_cast<long long*>(p), (long long)v);
+      break;
+    case TQPK_ACC_MAX:
+      if (a.type == TQPK_F64) atomicMax(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v);
+      else atomicMax(reinterpret_cast<long long*>(p), (long long)v);
+      break;
+  }
+}
+
+// Accumulator encoding of one row's contribution.
+__device__ __forceinline__ uint64_t acc_value(const tqpk_acc& a, const uint64_t* reg) {
+  switch (a.kind) {
+    case TQPK_ACC_SUM: return reg[a.reg];
+    case TQPK_ACC_COUNT_ROWS: return 1ull;
+    case TQPK_ACC_COUNT_NOTNULL:
+      return a.type == TQPK_F64 ? (u2d(reg[a.reg]) != (double)TQPK_NULL_INDEX)
+                                : (static_cast<int64_t>(reg[a.reg]) != TQPK_NULL_INDEX);
+    default: return a.type == TQPK_F64 ? f64_ordered(u2d(reg[a.reg])) : reg[a.reg];
+  }
+}
+
+__device__ __forceinline__ uint64_t combine_plain(const tqpk_acc& a, uint64_t x, uint64_t y) {
+  switch (a.kind) {
+    case TQPK_ACC_SUM: return a.type == TQPK_F64 ? d2u(__dadd_rn(u2d(x), u2d(y))) : x + y;
+    case TQPK_ACC_COUNT_ROWS:
+    case TQPK_ACC_COUNT_NOTNULL: return x + y;
+    case TQPK_ACC_MIN:
+      return a.type == TQPK_F64 ? min(x, y) : (uint64_t)min((int64_t)x, (int64_t)y);
+    default: return a.type == TQPK_F64 ? max(x, y) : (uint64_t)max((int64_t)x, (int64_t)y);
+  }
+}
+
+enum { MODE_PRIVATE = 1, MODE_SHARED = 2, MODE_GLOBAL = 3 };
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_groupby_dense(const __grid_constant__ tqpk_groupby_spec S,
+                                                       const __grid_constant__ tqpk_predicate P, RowFilter F,
+                                                       int64_t n, GbDev G, uint64_t* __restrict__ gacc,
+                                                       int keys_vec) {
+  extern __shared__ uint64_t sm[];
+  const int A = S.n_accs;
+  const int T = blockDim.x;
+  const int64_t K = G.slots;
+  if (MODE == MODE_PRIVATE) {
+    for (int64_t i = threadIdx.x; i < K * A * T; i += T) sm[i] = acc_init(S.accs[(i / T) % A]);
+  } else if (MODE == MODE_SHARED) {
+    for (int64_t i = threadIdx.x; i < K * A; i += T) sm[i] = acc_init(S.accs[i % A]);
+  }
+  __syncthreads();
+  uint64_t reg[TQPK_MAX_EXPR];
+  const int64_t groups = (n + 3) >> 2;
+  for (int64_t g = blockIdx.x * (int64_t)T + threadIdx.x; g < groups; g += (int64_t)gridDim.x * T) {
+    const int64_t r0 = g << 2;
+    const uint32_t b = filter4(F, P, r0, n);
+    if (!b) continue;
+    int64_t slot[4] = {0, 0, 0, 0};
+    for (int k = 0; k < G.nk; ++k) {
+      int64_t x[4];
+      ld4_int(S.keys[k], S.key_dtypes[k], r0, n, keys_vec, x);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) slot[j] += (x[j] - G.kmin[k]) * G.kstride[k];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (!((b >> j) & 1u)) continue;
+      eval_expr(S, r0 + j, reg);
+      for (int a = 0; a < A; ++a) {
+        if (MODE == MODE_PRIVATE) {
+          acc_plain(&sm[(slot[j] * A + a) * T + threadIdx.x], S.accs[a], reg);
+        } else if (MODE == MODE_SHARED) {
+          acc_merge_atomic(&sm[slot[j] * A + a], S.accs[a], acc_value(S.accs[a], reg));
+        } else {
+          acc_merge_atomic(&gacc[(int64_t)a * K + slot[j]], S.accs[a], acc_value(S.accs[a], reg));
+        }
+      }
+    }
+  }
+  if (MODE == MODE_GLOBAL) return;
+  __syncthreads();
+  // Flush the CTA's table into the global accumulators.
+  if (MODE == MODE_PRIVATE) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = T >> 5;
+    for (int64_t c = warp; c < K * A; c += nw) {
+      const tqpk_acc& a = S.accs[c % A];
+      uint64_t v = acc_init(a);
+      for (int t = lane; t < T; t += 32) v = combine_plain(a, v, sm[c * T + t]);
+#pragma unroll
+      for (int o = 16; o; o >>= 1) v = combine_plain(a, v, __shfl_xor_sync(0xffffffffu, v, o));
+      if (lane == 0 && v != acc_init(a)) acc_merge_atomic(&gacc[(c % A) * K + c / A], a, v);
+    }
+  } else {
+    for (int64_t c = threadIdx.x; c < K * A; c += T) {
+      const tqpk_acc& a = S.accs[c % A];
+      const uint64_t v = sm[c];
+      if (v != acc_init(a)) acc_merge_atomic(&gacc[(c % A) * K + c / A], a, v);
+    }
+  }
+}
+
+__global__ void k_init_accs(const __grid_constant__ tqpk_groupby_spec S, uint64_t* gacc, int64_t K) {
+  const int64_t total = K * S.n_accs;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+    gacc[i] = acc_init(S.accs[i / K]);
+}
+
+// Counts occupied slots (accumulator 0 is the row count).
+__global__ void k_count_groups(const uint64_t* cnt, int64_t K, unsigned long long* groups) {
+  unsigned local = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < K; i += (int64_t)gridDim.x * blockDim.x)
+    local += cnt[i] != 0;
+  local = __reduce_add_sync(0xffffffffu, local);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(groups, (unsigned long long)local);
+}
+
+struct EmitOut {
+  int n;
+  int op[TQPK_MAX_ACCS];
+  int a[TQPK_MAX_ACCS];
+  int b[TQPK_MAX_ACCS];
+  int dt[TQPK_MAX_ACCS];
+  void* col[TQPK_MAX_ACCS];
+  void* key[TQPK_MAX_KEYS];
+  int key_dt[TQPK_MAX_KEYS];
+};
+
+__device__ __forceinline__ void store_as(void* col, int dt, int64_t i, uint64_t v, bool is_f64) {
+  switch (dt) {
+    case TQPK_F64: static_cast<double*>(col)[i] = is_f64 ? u2d(v) : (double)(int64_t)v; break;
+    case TQPK_I64: static_cast<int64_t*>(col)[i] = is_f64 ? (int64_t)u2d(v) : (int64_t)v; break;
+    case TQPK_I32: static_cast<int32_t*>(col)[i] = (int32_t)(int64_t)v; break;
+    case TQPK_I8: static_cast<int8_t*>(col)[i] = (int8_t)(int64_t)v; break;
+    default: static_cast<uint8_t*>(col)[i] = (uint8_t)(int64_t)v; break;
+  }
+}
+
+// Ordered emission of the occupied slots (ascending slot = ascending key tuple).
+__global__ void __launch_bounds__(kBlock) k_emit_dense(const __grid_constant__ tqpk_groupby_spec S, GbDev G,
+                                                       const uint64_t* __restrict__ gacc, int force_one,
+                                                       const __grid_constant__ EmitOut E, uint64_t* status,
+                                                       int* tile_ctr, int* err) {
+  __shared__ int s_tile;
+  __shared__ uint64_t s_excl;
+  __shared__ int sw[kBlock / 32 + 1];
+  if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1);
+  __syncthreads();
+  const int64_t tile = s_tile;
+  const int64_t K = G.slots;
+  const int64_t s0 = tile * kTile + threadIdx.x * kItems;
+  uint32_t bits = 0;
+  for (int j = 0; j < kItems; ++j) {
+    const int64_t s = s0 + j;
+    if (s < K && (gacc[s] != 0 || force_one)) bits |= 1u << j;
+  }
+  int total;
+  const int excl = block_excl_scan<kBlock, int>(__popc(bits), total, sw);
+  if (threadIdx.x < 32) {
+    uint64_t e = lookback_warp(status, tile, (uint64_t)total, err);
+    if (threadIdx.x == 0) s_excl = e;
+  }
+  __syncthreads();
+  int64_t pos = (int64_t)s_excl + excl;
+  while (bits) {
+    const int j = __ffs(bits) - 1;
+    bits &= bits - 1;
+    const int64_t s = s0 + j;
+    for (int k = 0; k < G.nk; ++k) {
+      const int64_t key = G.kmin[k] + (s / G.kstride[k]) % G.krange[k];
+      store_as(E.key[k], E.key_dt[k], pos, (uint64_t)key, false);
+    }
+    for (int o = 0; o < E.n; ++o) {
+      const tqpk_acc& a = S.accs[E.a[o]];
+      uint64_t v = gacc[(int64_t)E.a[o] * K + s];
+      bool f = a.type == TQPK_F64 && a.kind != TQPK_ACC_COUNT_ROWS && a.kind != TQPK_ACC_COUNT_NOTNULL;
+      if (f && (a.kind == TQPK_ACC_MIN || a.kind == TQPK_ACC_MAX)) v = d2u(f64_from_ordered(v));
+      if (E.op[o] == TQPK_OUT_AVG) {
+        const double num = f ? u2d(v) : (double)(int64_t)v;
+        const double den = (double)(int64_t)gacc[(int64_t)E.b[o] * K + s];
+        v = d2u(__ddiv_rn(num, den));
+        f = true;
+      } else if (a.kind == TQPK_ACC_COUNT_ROWS || a.kind == TQPK_ACC_COUNT_NOTNULL) {
+        f = false;
+      }
+      store_as(E.col[o], E.dt[o], pos, v, f);
+    }
+    ++pos;
+  }
+}
+
+// ---------------------------------------------------------------- host side
+static GbDev to_dev(const tqpk_gb_plan& p, int nk) {
+  GbDev G;
+  G.nk = nk;
+  for (int k = 0; k < TQPK_MAX_KEYS; ++k) {
+    G.kmin[k] = p.key_min[k];
+    G.kstride[k] = p.key_stride[k] ? p.key_stride[k] : 1;
+    G.krange[k] = p.key_range[k] ? p.key_range[k] : 1;
+  }
+  G.slots = p.slots;
+  return G;
+}
+
+static int check_spec(const tqpk_groupby_spec* S) {
+  if (!S) return TQPK_EINVAL;
+  if (S->n_keys < 0 || S->n_keys > TQPK_MAX_KEYS || S->n_cols < 0 || S->n_cols > TQPK_MAX_COLS ||
+      S->n_expr < 0 || S->n_expr > TQPK_MAX_EXPR || S->n_accs < 1 || S->n_accs > TQPK_MAX_ACCS)
+    return TQPK_EINVAL;
+  if (S->accs[0].kind != TQPK_ACC_COUNT_ROWS) return TQPK_EINVAL;  // accumulator 0 marks occupied groups
+  for (int k = 0; k < S->n_keys; ++k)
+    if (!S->keys[k] || !is_int_dtype(S->key_dtypes[k])) return TQPK_EDTYPE;
+  for (int c = 0; c < S->n_cols; ++c)
+    if (!S->cols[c] || !dtype_size(S->col_dtypes[c])) return TQPK_EDTYPE;
+  for (int i = 0; i < S->n_expr; ++i) {
+    const tqpk_expr_insn& X = S->expr[i];
+    if (X.type != TQPK_F64 && X.type != TQPK_I64) return TQPK_EDTYPE;
+    if (X.op == TQPK_X_COL && (X.col < 0 || X.col >= S->n_cols)) return TQPK_EINVAL;
+    if (X.op >= TQPK_X_ADD && X.op <= TQPK_X_DIV && (X.a < 0 || X.a >= i || X.b < 0 || X.b >= i)) return TQPK_EINVAL;
+    if (X.op == TQPK_X_TOF64 && (X.a < 0 || X.a >= i)) return TQPK_EINVAL;
+    if (X.op == TQPK_X_DIV && X.type != TQPK_F64) return TQPK_EUNSUPPORTED;
+    if (X.op < TQPK_X_COL || X.op > TQPK_X_TOF64) return TQPK_EINVAL;
+  }
+  for (int a = 0; a < S->n_accs; ++a) {
+    const tqpk_acc& A = S->accs[a];
+    if (A.kind < TQPK_ACC_SUM || A.kind > TQPK_ACC_MAX) return TQPK_EINVAL;
+    if (A.kind != TQPK_ACC_COUNT_ROWS && (A.reg < 0 || A.reg >= S->n_expr)) return TQPK_EINVAL;
+  }
+  return TQPK_OK;
+}
+
+constexpr int64_t kPrivateBudget = 96 * 1024;  // bytes of shared memory per CTA for private tables
+
+}  // namespace tqpk
+
+using namespace tqpk;
+
+extern "C" int tqpk_groupby_plan(const tqpk_groupby_spec* S, const tqpk_predicate* pred, const uint8_t* mask,
+                                 int64_t n, tqpk_gb_plan* plan, void* scratch, tqpk_stream stream) {
+  int rc = check_spec(S);
+  if (rc) return rc;
+  if ((rc = check_pred(pred))) return rc;
+  if (!plan || n < 0) return TQPK_EINVAL;
+  *plan = tqpk_gb_plan{};
+  int64_t mn[TQPK_MAX_KEYS], mx[TQPK_MAX_KEYS], rows = 0;
+  rc = key_ranges(pred, mask, n, S->n_keys, S->keys, S->key_dtypes, mn, mx, &rows, scratch,
+                  static_cast<cudaStream_t>(stream));
+  if (rc) return rc;
+  plan->n_rows = rows;
+  int64_t K = 1;
+  bool overflow = false;
+  for (int k = S->n_keys - 1; k >= 0; --k) {
+    const int64_t range = rows ? (mx[k] - mn[k] + 1) : 1;
+    if (range <= 0 || range > (int64_t(1) << 40)) overflow = true;
+    plan->key_min[k] = rows ? mn[k] : 0;
+    plan->key_range[k] = range;
+    plan->key_stride[k] = K;
+    if (!overflow && K > (int64_t(1) << 62) / range) overflow = true;
+    if (!overflow) K *= range;
+  }
+  if (S->n_keys > 0 && rows == 0) K = 1;  // no group at all; keep a 1-slot table
+  const int64_t A = S->n_accs;
+  if (S->n_keys == 0) {
+    plan->mode = TQPK_GB_GLOBAL_ONE;
+  } else if (overflow || K > std::max<int64_t>(4 * rows, int64_t(1) << 20)) {
+    plan->mode = TQPK_GB_HASH;  // key space too sparse for a dense table
+  } else if (K * A * 8 * 256 <= kPrivateBudget) {
+    plan->mode = TQPK_GB_DENSE_PRIVATE;
+  } else if (K * A * 8 * 128 <= kPrivateBudget) {
+    plan->mode = TQPK_GB_DENSE_PRIVATE;
+  } else if (K * A * 8 <= kPrivateBudget) {
+    plan->mode = TQPK_GB_DENSE_SHARED;
+  } else {
+    plan->mode = TQPK_GB_DENSE_GLOBAL;
+  }
+  if (plan->mode == TQPK_GB_GLOBAL_ONE) K = 1;
+  plan->threads = (plan->mode == TQPK_GB_DENSE_PRIVATE && K * A * 8 * 256 > kPrivateBudget) ? 128 : 256;
+  if (plan->mode == TQPK_GB_GLOBAL_ONE) plan->threads = (K * A * 8 * 256 <= kPrivateBudget) ? 256 : 128;
+  plan->slots = K;
+  if (plan->mode == TQPK_GB_HASH) {
+    plan->ws_bytes = 0;
+    return TQPK_EUNSUPPORTED;
+  }
+  plan->ws_bytes = 512 + align_up((size_t)(K * A * 8), 256) + compact_status_bytes(K);
+  return TQPK_OK;
+}
+
+extern "C" int tqpk_groupby_run(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, const tqpk_predicate* pred,
+                                const uint8_t* mask, int64_t n, void* ws, size_t ws_bytes, int64_t* h_groups,
+                                tqpk_stream stream) {
+  int rc = check_spec(S);
+  if (rc) return rc;
+  if ((rc = check_pred(pred))) return rc;
+  if (!plan || !ws || ws_bytes < plan->ws_bytes || !h_groups || n < 0) return !ws || ws_bytes < (plan ? plan->ws_bytes : 0) ? TQPK_ENOMEM : TQPK_EINVAL;
+  if (plan->mode == TQPK_GB_HASH) return TQPK_EUNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int64_t K = plan->slots, A = S->n_accs;
+  char* base = static_cast<char*>(ws);
+  unsigned long long* d_groups = reinterpret_cast<unsigned long long*>(base);
+  uint64_t* gacc = reinterpret_cast<uint64_t*>(base + 512);
+  TQPK_CUDA(cudaMemsetAsync(d_groups, 0, 8, s));
+  k_init_accs<<<grid_for(K * A, 4), kBlock, 0, s>>>(*S, gacc, K);
+  TQPK_CHECK_LAUNCH();
+  const GbDev G = to_dev(*plan, S->n_keys);
+  const RowFilter F = make_filter(pred, mask);
+  bool kvec = true;
+  for (int k = 0; k < S->n_keys; ++k) kvec = kvec && aligned16(S->keys[k]);
+  const tqpk_predicate& P = *pred_or_empty(pred);
+  if (n > 0 && plan->n_rows > 0) {
+    const int T = plan->threads;
+    const int64_t groups4 = (n + 3) / 4;
+    if (plan->mode == TQPK_GB_DENSE_PRIVATE || plan->mode == TQPK_GB_GLOBAL_ONE) {
+      const size_t smem = (size_t)(K * A * 8 * T);
+      TQPK_CUDA(cudaFuncSetAttribute(k_groupby_dense<MODE_PRIVATE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+      int g = (int)std::min<int64_t>((groups4 + T - 1) / T, (int64_t)num_sms() * 2);
+      timing_before(KID_GROUPBY, s);
+      k_groupby_dense<MODE_PRIVATE><<<std::max(g, 1), T, smem, s>>>(*S, P, F, n, G, gacc, kvec);
+      timing_after(KID_GROUPBY, s);
+    } else if (plan->mode == TQPK_GB_DENSE_SHARED) {
+      const size_t smem = (size_t)(K * A * 8);
+      TQPK_CUDA(cudaFuncSetAttribute(k_groupby_dense<MODE_SHARED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+      int g = (int)std::min<int64_t>((groups4 + 255) / 256, (int64_t)num_sms() * 2);
+      timing_before(KID_GROUPBY, s);
+      k_groupby_dense<MODE_SHARED><<<std::max(g, 1), 256, smem, s>>>(*S, P, F, n, G, gacc, kvec);
+      timing_after(KID_GROUPBY, s);
+    } else {
+      int g = grid_for(groups4, 8);
+      timing_before(KID_GROUPBY, s);
+      k_groupby_dense<MODE_GLOBAL><<<g, 256, 0, s>>>(*S, P, F, n, G, gacc, kvec);
+      timing_after(KID_GROUPBY, s);
+    }
+    TQPK_CHECK_LAUNCH();
+  }
+  int64_t groups = 0;
+  if (S->n_keys == 0) {
+    groups = 1;  // a global aggregate always has one group (aggregate.py:291-295)
+  } else if (plan->n_rows > 0) {
+    k_count_groups<<<grid_for(K, 4), kBlock, 0, s>>>(gacc, K, d_groups);
+    TQPK_CHECK_LAUNCH();
+    unsigned long long h = 0;
+    TQPK_CUDA(cudaMemcpyAsync(&h, d_groups, 8, cudaMemcpyDeviceToHost, s));
+    TQPK_CUDA(cudaStreamSynchronize(s));
+    groups = (int64_t)h;
+  } else {
+    TQPK_CUDA(cudaStreamSynchronize(s));
+  }
+  *h_groups = groups;
+  return TQPK_OK;
+}
+
+extern "C" int tqpk_groupby_emit(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, void* ws, int64_t groups,
+                                 void* const* out_keys, int32_t n_out, const int32_t* ops, void* const* out_cols,
+                                 tqpk_stream stream) {
+  int rc = check_spec(S);
+  if (rc) return rc;
+  if (!plan || !ws || n_out < 0 || n_out > TQPK_MAX_ACCS || groups < 0) return TQPK_EINVAL;
+  if (plan->mode == TQPK_GB_HASH) return TQPK_EUNSUPPORTED;
+  if (groups == 0) return TQPK_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  EmitOut E;
+  E.n = n_out;
+  for (int o = 0; o < n_out; ++o) {
+    E.op[o] = ops[4 * o];
+    E.a[o] = ops[4 * o + 1];
+    E.b[o] = ops[4 * o + 2];
+    E.dt[o] = ops[4 * o + 3];
+    E.col[o] = out_cols[o];
+    if (E.a[o] < 0 || E.a[o] >= S->n_accs || !E.col[o] || !dtype_size(E.dt[o])) return TQPK_EINVAL;
+    if (E.op[o] == TQPK_OUT_AVG && (E.b[o] < 0 || E.b[o] >= S->n_accs)) return TQPK_EINVAL;
+  }
+  for (int k = 0; k < S->n_keys; ++k) {
+    if (!out_keys[k]) return TQPK_EINVAL;
+    E.key[k] = out_keys[k];
+    E.key_dt[k] = S->key_dtypes[k];
+  }
+  const int64_t K = plan->slots, A = S->n_accs;
+  char* base = static_cast<char*>(ws);
+  uint64_t* gacc = reinterpret_cast<uint64_t*>(base + 512);
+  void* cws = base + 512 + align_up((size_t)(K * A * 8), 256);
+  const int64_t tiles = (K + kTile - 1) / kTile;
+  WsCursor cur(cws, compact_status_bytes(K));
+  int* ctl = cur.take<int>(64);
+  uint64_t* status = cur.take<uint64_t>(tiles);
+  if (!ctl || !status) return TQPK_ENOMEM;
+  TQPK_CUDA(cudaMemsetAsync(cws, 0, cur.off, s));
+  const GbDev G = to_dev(*plan, S->n_keys);
+  k_emit_dense<<<(int)tiles, kBlock, 0, s>>>(*S, G, gacc, S->n_keys == 0 ? 1 : 0, E, status, ctl, ctl + 1);
+  TQPK_CHECK_LAUNCH();
+  int err = 0;
+  TQPK_CUDA(cudaMemcpyAsync(&err, ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+  TQPK_CUDA(cudaStreamSynchronize(s));
+  return err ? err : TQPK_OK;
+}

@@ -1,0 +1,17 @@
+"""Drop-in replacements for TQP-Inmem's hot-path operators.
+
+Same names, arguments, return values, ``tensor_group`` mutations and errors
+as the reference functions; the work runs in libtqpk.so:
+
+  filter.tqp_filter             operators/filter.py:164-204
+  hashjoin.join_vortex          operators/hashjoin.py:179-248
+  hashjoin.join_kernel_new      operators/hashjoin.py:24-177
+  aggregate.tqp_hash_aggregate  operators/aggregate.py:236-393
+  sort.tqp_sort                 operators/sort.py:6-58
+"""
+from .filter import tqp_filter
+from .hashjoin import join_vortex, join_kernel_new
+from .aggregate import tqp_hash_aggregate
+from .sort import tqp_sort
+
+__all__ = ["tqp_filter", "join_vortex", "join_kernel_new", "tqp_hash_aggregate", "tqp_sort"]

@@ -1,0 +1,87 @@
+"""Drop-in ``tqp_hash_aggregate`` (operators/aggregate.py:236-393).
+
+Keeps the reference's argument handling (``input ids``/``mask map``/``keys``/
+``results``/``out agg ids``), its ``tensor_group`` writes (key columns as
+[G, 1] tensors with the input key's type, aggregates typed by their dtype,
+:380-390) and its return value (rows of the first ``tensor_group`` entry).
+
+The filter mask is applied inside the aggregation kernel (the reference
+compacts every input column first, vortex_pipeline.py:58), every aggregate is
+computed in the same pass, and groups come out in ascending key order (the
+reference's order is the ascending order of a random linear hash of the key
+tuple, :320-327; for one non-negative key the two coincide).
+"""
+from __future__ import annotations
+
+import torch
+
+from ..expr import compile_aggregate
+from ..ops import groupby
+from ..variable import make_like, torch_to_type
+from .filter import _require_gpu
+
+
+def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_pool, name="aggregation"):
+    _require_gpu(gpu_enable)
+    assert not args["is partial"]
+    transfer_set = args["input ids"]
+    agg_mask_map = {}
+    if "mask map" in args:                              # aggregate.py:249-257
+        for k, v in args["mask map"].items():
+            if k in transfer_set:
+                agg_mask_map[k] = v
+                if v not in transfer_set:
+                    transfer_set.append(v)
+    mask_ids = set(agg_mask_map.values())
+    data_ids = [c for c in transfer_set if c not in mask_ids]
+    if len(mask_ids) > 1:
+        raise NotImplementedError(f"aggregate inputs carry different masks {mask_ids}")
+    if mask_ids and any(c not in agg_mask_map for c in data_ids):
+        raise NotImplementedError("aggregate mixes masked and unmasked input columns")
+    mask = tensor_group[next(iter(mask_ids))].tensor if mask_ids else None
+
+    key_ids, key_ids_new, key_types_name = [], [], []
+    for tree in args["results"]:                        # aggregate.py:265-275
+        t = tree
+        while isinstance(t, list) and len(t) == 1:
+            t = t[0]
+        if isinstance(t, str) or (len(t) == 3 and t[1] == "AS" and isinstance(t[0], str)):
+            kid = int((t if isinstance(t, str) else t[0]).split("#")[-1].replace("L", ""))
+            key_ids.append(kid)
+            key_types_name.append(tensor_group[kid].tensor_type)
+    agg_ids = args["out agg ids"]
+
+    cols = {c: tensor_group[c].tensor for c in data_ids}
+    proto = tensor_group[data_ids[0]] if data_ids else None
+    n = next(iter(cols.values())).shape[0] if cols else 0
+    device = next(iter(cols.values())).device if cols else torch.device("cuda")
+    if all(tensor_group[c].tensor.numel() == 0 for c in transfer_set):
+        # vortex_pipeline.py:51-52: empty inputs give empty (float32) outputs
+        keys_out = {k: torch.tensor([], device=device) for k in range(len(key_ids))}
+        vals_out = {a: torch.tensor([], device=device) for a in agg_ids}
+        prog = None
+    else:
+        prog = compile_aggregate(args, cols)
+        keys, vals_out, G, _ = groupby(prog, n, device, mask=mask)
+        keys_out = {}
+        for i, (oid, kid) in enumerate(prog.key_outputs):
+            keys_out[i] = keys[prog.key_ids.index(kid)].reshape(G, 1)
+    key_out_ids = [oid for (oid, _) in prog.key_outputs] if prog else \
+        [int((t if isinstance(t, str) else t[-1]).split("#")[-1].replace("L", "")) for t in _key_trees(args)]
+    for a in agg_ids:                                   # aggregate.py:383-390
+        v = vals_out[a]
+        tensor_group[a] = make_like(proto, v, torch_to_type(v.dtype))
+    for i, oid in enumerate(key_out_ids):
+        tensor_group[oid] = make_like(proto, keys_out[i], key_types_name[i])
+    return list(tensor_group.values())[0].tensor.size(0)
+
+
+def _key_trees(args):
+    out = []
+    for tree in args["results"]:
+        t = tree
+        while isinstance(t, list) and len(t) == 1:
+            t = t[0]
+        if isinstance(t, str) or (len(t) == 3 and t[1] == "AS" and isinstance(t[0], str)):
+            out.append(t)
+    return out

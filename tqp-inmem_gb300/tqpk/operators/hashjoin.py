@@ -1,0 +1,152 @@
+"""Drop-in ``join_vortex`` / ``join_kernel_new`` (operators/hashjoin.py).
+
+``join_vortex`` keeps the reference's argument handling (hashjoin.py:191-208:
+key normalisation, ``materialized in`` per side, masks popped from
+``args['mask map']``) and its return value (the row count of the first
+``tensor_group`` entry, :248).  The work differs in three places, none of
+which changes a result:
+
+* masked inputs are not compacted (vortex_pipeline.py:58); the build and the
+  probe skip failing rows in place and emit ids of the original rows;
+* the sort / unique_consecutive / searchsorted / padded-matrix expansion
+  (:39-97) is one directory build plus one single-pass probe kernel;
+* the output columns are gathered by one multi-column gather kernel
+  (:153-175, with index_with_null for right-outer, conversion.py:52-57).
+
+Extra join conditions (:100-108, e.g. the second key of a two-key join,
+main.py:208-217) are evaluated on the gathered pair columns with the
+predicate kernel and the pairs compacted; they are supported for inner joins.
+"""
+from __future__ import annotations
+
+from typing import Dict, List
+
+import torch
+
+from .. import _lib as L
+from ..ops import compact, filter_mask, gather, join_build, join_probe
+from ..predicate import compile_filter
+from ..variable import make_like
+from .filter import _require_gpu
+
+LEFT, RIGHT = 0, 1
+
+
+def _normalize(v):
+    if hasattr(v, "normalize"):
+        v.normalize()
+    elif v.tensor.dim() == 2:
+        v.tensor = v.tensor.squeeze()
+
+
+def _side_mask(tensor_group, cols: List[int], mask_map: Dict[int, int], key: int):
+    """The one mask shared by a side's columns (None when the side is unfiltered)."""
+    masks = {mask_map.get(c) for c in cols}
+    if len(masks) > 1:
+        raise NotImplementedError(f"columns of one join side carry different masks {masks}")
+    m = masks.pop() if masks else None
+    if key not in cols:
+        m = mask_map.get(key, m)
+    return tensor_group[m].tensor if m is not None else None
+
+
+def _pairs(tensors_left, tensors_right, left_key, right_key, condition_list, jtype, left_mask, right_mask):
+    lk = tensors_left[left_key].tensor
+    rk = tensors_right[right_key].tensor
+    if condition_list and jtype != "inner":
+        raise NotImplementedError("join conditions are supported for inner joins only")
+    b = join_build(lk, left_mask)
+    bi, pi = join_probe(b, rk, right_mask, jtype)
+    for cond in condition_list:                       # hashjoin.py:100-108
+        ids = set()
+        _collect_ids(cond, ids)
+        cols = {}
+        for cid in ids:
+            if cid in tensors_left:
+                cols[cid] = gather([tensors_left[cid].tensor], bi)[0]
+            else:
+                cols[cid] = gather([tensors_right[cid].tensor], pi)[0]
+        pred = compile_filter(cond, cols)
+        keep, _ = filter_mask(pred, int(bi.numel()), bi.device)
+        (bi, pi), _ = compact([bi, pi], mask=keep)
+    return bi, pi, b.plan.nb_rows
+
+
+def _collect_ids(tree, out):
+    if isinstance(tree, str):
+        if "#" in tree and not tree.startswith("Brand#"):
+            out.add(int(tree.split("#")[-1].replace("L", "")))
+    elif isinstance(tree, list):
+        if len(tree) == 3 and tree[1] == "#":
+            out.add(int(tree[-1]))
+            return
+        for e in tree:
+            _collect_ids(e, out)
+
+
+def join_kernel_new(gpu_enable, tensors_left, tensors_right, left_key, right_key, condition_list, join_output_keys,
+                    return_global_index, type, left_global_idx, right_global_idx, left_mask=None, right_mask=None):
+    """hashjoin.py:24-177 on unmasked (already materialised) inputs."""
+    assert type in {"inner", "right-semi", "right-anti", "right-outer"}, "Invalid Join type."
+    _normalize(tensors_left[left_key])
+    _normalize(tensors_right[right_key])
+    bi, pi, _ = _pairs(tensors_left, tensors_right, left_key, right_key, condition_list, type, left_mask, right_mask)
+    return _outputs(tensors_left, tensors_right, join_output_keys, type, bi, pi, return_global_index,
+                    left_global_idx, right_global_idx)
+
+
+def _outputs(tensors_left, tensors_right, keys, jtype, bi, pi, return_global_index=False, lg=None, rg=None,
+             left_rows=None, right_rows=None):
+    null_aware = False
+    if jtype == "right-outer":
+        n_pairs = int((bi != L.NULL_INDEX).sum().item()) if bi.numel() else 0
+        if n_pairs == 0:          # hashjoin.py:154: no null padding without a match
+            bi = bi[:0]
+        else:
+            null_aware = True
+    elif jtype in ("right-semi", "right-anti"):
+        bi = torch.empty(0, dtype=torch.int64, device=pi.device)
+    lcols = [k for k in keys if k in tensors_left]
+    rcols = [k for k in keys if k not in tensors_left]
+    lout = gather([tensors_left[k].tensor for k in lcols], bi, null_aware) if lcols else []
+    rout = gather([tensors_right[k].tensor for k in rcols], pi) if rcols else []
+    res, li, ri = [], iter(lout), iter(rout)
+    for k in keys:                                     # hashjoin.py:161-172
+        if k in tensors_left:
+            rows = left_rows if left_rows is not None else tensors_left[k].tensor.shape[0]
+            res.append(next(li) if rows > 0 else torch.tensor([]))
+        else:
+            rows = right_rows if right_rows is not None else tensors_right[k].tensor.shape[0]
+            res.append(next(ri) if rows > 0 else torch.tensor([]))
+    if return_global_index:
+        res.extend(gather([lg.tensor], bi, null_aware) + gather([rg.tensor], pi))
+    return res
+
+
+def join_vortex(gpu_enable, tensor_group, args, leftcol, rightcol, condition_list, type, cpu_mem_pool,
+                gpu_mem_pool, name):
+    _require_gpu(gpu_enable)
+    join_key_index = [leftcol, rightcol]
+    groupings = [args["left group"], args["right group"]]
+    join_mask_map, join_output = {}, []
+    side_cols = [[], []]
+    for side in (LEFT, RIGHT):                         # hashjoin.py:198-208
+        _normalize(tensor_group[join_key_index[side]])
+        for used_col in args["materialized in"]:
+            if used_col in groupings[side]:
+                join_output.append(used_col)
+                side_cols[side].append(used_col)
+                if "mask map" in args and used_col in args["mask map"]:
+                    join_mask_map[used_col] = args["mask map"].pop(used_col)
+    masks = [_side_mask(tensor_group, side_cols[s] or [join_key_index[s]], join_mask_map, join_key_index[s])
+             for s in (LEFT, RIGHT)]
+    tl = {k: tensor_group[k] for k in groupings[LEFT] if k in tensor_group}
+    tr = {k: tensor_group[k] for k in groupings[RIGHT] if k in tensor_group}
+    if leftcol not in tl or rightcol not in tr:
+        raise KeyError("join key is not in its side's group")
+    bi, pi, nb_rows = _pairs(tl, tr, leftcol, rightcol, condition_list, type, masks[LEFT], masks[RIGHT])
+    np_rows = int(masks[RIGHT].sum().item()) if masks[RIGHT] is not None else tr[rightcol].tensor.shape[0]
+    outs = _outputs(tl, tr, join_output, type, bi, pi, left_rows=nb_rows, right_rows=np_rows)
+    for i, k in enumerate(join_output):                # hashjoin.py:234-238
+        tensor_group[k] = make_like(tensor_group[k], outs[i], tensor_group[k].tensor_type)
+    return next(iter(tensor_group.values())).tensor.size(0)

@@ -1,0 +1,58 @@
+"""Drop-in ``tqp_sort`` (operators/sort.py:6-58).
+
+The reference runs one stable torch.sort per key, last key first, each time
+gathering the key through ``perm`` (:26-35), then slices ``perm[:limit]``
+(:41-42) and gathers every input column (:44-54).  Here each key is one
+tqpk_argsort_stable call that sorts keys[perm] and permutes perm in the same
+kernels; with a limit the first key uses the stable top-k, which returns the
+same rows as the full sort followed by the slice.  A [N, w] key (the
+reference ranks its rows with unique(dim=0)) is sorted as w stable passes,
+last byte column first, which gives the same lexicographic order and ties.
+"""
+from __future__ import annotations
+
+import torch
+
+from ..ops import argsort_stable, gather, topk_stable
+from ..variable import make_like
+from .filter import _require_gpu
+
+
+def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
+    _require_gpu(gpu_enable)
+    limit = args["limit"] if with_limit else None
+    input_ids = args["input ids"]
+    rows = tensor_group[input_ids[0]].tensor.shape[0]
+    key_ids, key_descs = args["key ids"], args["key orders"]
+    k0 = tensor_group[key_ids[0]].tensor
+    if k0.numel() * k0.element_size() >= 8_000_000_000:   # sort.py:22-23, 38-39
+        raise RuntimeError("sort input exceeds in-memory limit")
+    device = k0.device
+    perm = torch.arange(rows, device=device, dtype=torch.int64)
+    steps = []
+    for key_id, desc in zip(reversed(key_ids), reversed(key_descs)):
+        col = tensor_group[key_id].tensor
+        if col.dim() == 2 and col.shape[1] > 1:
+            steps += [(col[:, c].contiguous(), desc) for c in reversed(range(col.shape[1]))]
+        else:
+            steps.append((col.reshape(-1), desc))
+    for i, (key, desc) in enumerate(steps):
+        last = i == len(steps) - 1
+        if last and limit is not None:
+            perm = topk_stable(key, limit, desc, perm)
+        else:
+            perm = argsort_stable(key, desc, perm)
+    if limit is not None:
+        perm = perm[:limit]
+    for key_id in input_ids:                              # sort.py:44-54
+        t = tensor_group[key_id].tensor
+        if not t.is_cuda:
+            t = t.to(device)
+        if t.dim() == 2 and t.shape[1] == 1:
+            out = gather([t.reshape(-1)], perm)[0].reshape(-1, 1)
+        elif t.dim() == 2:
+            out = t.index_select(0, perm)    # multi-byte string rows: not on the kernel path
+        else:
+            out = gather([t], perm)[0]
+        tensor_group[key_id] = make_like(tensor_group[key_id], out, tensor_group[key_id].tensor_type)
+    return rows

@@ -1,0 +1,247 @@
+"""Tensor-level wrappers of the libtqpk C ABI.
+
+Every function takes device tensors, allocates outputs and workspaces through
+torch's caching allocator, launches on the current CUDA stream and raises a
+Python exception for a non-zero status.  There is no CPU or torch fallback:
+if libtqpk.so is missing or a shape is unsupported the call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import torch
+
+from . import _lib as L
+from .dtypes import code_of, dtype_of
+from .expr import AggregateProgram
+from .predicate import CompiledPredicate
+
+
+def _ws(nbytes: int, device) -> torch.Tensor:
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+
+
+def _stream(device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _col1d(t: torch.Tensor) -> torch.Tensor:
+    if t.dim() == 2 and t.shape[1] == 1:
+        t = t.reshape(-1)
+    if t.dim() != 1:
+        raise NotImplementedError(f"2-D column {tuple(t.shape)} is not on the kernel path")
+    return t.contiguous()
+
+
+def _check_cuda(*ts):
+    for t in ts:
+        if t is not None and not t.is_cuda:
+            raise ValueError("tqpk kernels take CUDA tensors (no CPU fallback)")
+
+
+def _vp_array(ptrs: Sequence[Optional[int]]):
+    arr = (C.c_void_p * max(len(ptrs), 1))()
+    for i, p in enumerate(ptrs):
+        arr[i] = p
+    return arr
+
+
+def _i32_array(vals: Sequence[int]):
+    arr = (C.c_int32 * max(len(vals), 1))()
+    for i, v in enumerate(vals):
+        arr[i] = v
+    return arr
+
+
+# ---------------------------------------------------------------- (a) filter
+def filter_mask(pred: CompiledPredicate, n: int, device) -> Tuple[torch.Tensor, torch.Tensor]:
+    """Bool mask of the predicate over n rows and a device count of true rows."""
+    lib = L.load()
+    mask = torch.empty(n, dtype=torch.bool, device=device)
+    count = torch.zeros(1, dtype=torch.int64, device=device)
+    _check_cuda(*pred.tensors)
+    L.check(lib.tqpk_filter_mask(C.byref(pred.struct), n, mask.data_ptr() if n else None, count.data_ptr(),
+                                 _stream(device)), "tqpk_filter_mask")
+    return mask, count
+
+
+def compact(cols: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = None,
+            pred: Optional[CompiledPredicate] = None, with_row_ids: bool = False) -> Tuple[List[torch.Tensor], int]:
+    """Stable compaction of columns by a mask (or a predicate): tensor[mask]."""
+    lib = L.load()
+    cols = [_col1d(c) for c in cols]
+    if mask is None and pred is None:
+        raise ValueError("compact needs a mask or a predicate")
+    n = int(mask.numel()) if mask is not None else (int(cols[0].numel()) if cols else 0)
+    device = (mask if mask is not None else cols[0]).device
+    _check_cuda(mask, *cols)
+    outs = [torch.empty(n, dtype=c.dtype, device=device) for c in cols]
+    dts = [code_of(c.dtype) for c in cols]
+    ins = [c.data_ptr() for c in cols]
+    optr = [o.data_ptr() for o in outs]
+    if with_row_ids:
+        rid = torch.empty(n, dtype=torch.int64, device=device)
+        outs.append(rid)
+        ins.append(None)
+        optr.append(rid.data_ptr())
+        dts.append(-1)
+    if len(ins) > L.MAX_COLS:
+        raise NotImplementedError(f"compaction of more than {L.MAX_COLS} columns")
+    cnt = torch.zeros(1, dtype=torch.int64, device=device)
+    ws = _ws(lib.tqpk_compact_workspace_bytes(n), device)
+    dt_arr = _i32_array([d if d >= 0 else L.ROWID for d in dts])
+    L.check(lib.tqpk_compact(C.byref(pred.struct) if pred is not None else None,
+                             mask.data_ptr() if mask is not None else None, n, len(ins), _vp_array(ins), dt_arr,
+                             _vp_array(optr), cnt.data_ptr(), ws.data_ptr(), ws.numel(), _stream(device)),
+            "tqpk_compact")
+    m = int(cnt.item())
+    return [o[:m] for o in outs], m
+
+
+# ---------------------------------------------------------------- (d) group-by
+def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor] = None,
+            pred: Optional[CompiledPredicate] = None):
+    """Runs the compiled aggregate; returns (key columns [G], {out id: column}, G)."""
+    lib = L.load()
+    _check_cuda(mask, *prog.tensors)
+    s = _stream(device)
+    plan = L.GbPlan()
+    scratch = _ws(256, device)
+    pp = C.byref(pred.struct) if pred is not None else None
+    mp = mask.data_ptr() if mask is not None else None
+    L.check(lib.tqpk_groupby_plan(C.byref(prog.spec), pp, mp, n, C.byref(plan), scratch.data_ptr(), s),
+            "tqpk_groupby_plan")
+    ws = _ws(plan.ws_bytes, device)
+    groups = C.c_int64(0)
+    L.check(lib.tqpk_groupby_run(C.byref(prog.spec), C.byref(plan), pp, mp, n, ws.data_ptr(), ws.numel(),
+                                 C.byref(groups), s), "tqpk_groupby_run")
+    G = groups.value
+    keys = [torch.empty(G, dtype=dtype_of(prog.spec.key_dtypes[k]), device=device) for k in range(prog.spec.n_keys)]
+    outs = [torch.empty(G, dtype=dt, device=device) for (_, _, _, _, dt) in prog.outputs]
+    ops = []
+    for (_, op, a, b, dt) in prog.outputs:
+        ops += [op, a, b, code_of(dt)]
+    L.check(lib.tqpk_groupby_emit(C.byref(prog.spec), C.byref(plan), ws.data_ptr(), G,
+                                  _vp_array([k.data_ptr() for k in keys]), len(outs), _i32_array(ops),
+                                  _vp_array([o.data_ptr() for o in outs]), s), "tqpk_groupby_emit")
+    return keys, {oid: o for (oid, *_), o in zip(prog.outputs, outs)}, G, plan
+
+
+# ---------------------------------------------------------------- (b) sort / (e) top-k
+def argsort_stable(keys: torch.Tensor, descending: bool = False,
+                   perm_in: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Stable sort of keys[perm_in] -> permuted perm_in (int64)."""
+    lib = L.load()
+    keys = _col1d(keys)
+    n = int(perm_in.numel()) if perm_in is not None else int(keys.numel())
+    _check_cuda(keys, perm_in)
+    out = torch.empty(n, dtype=torch.int64, device=keys.device)
+    if n == 0:
+        return out
+    ws = _ws(lib.tqpk_sort_workspace_bytes(n), keys.device)
+    L.check(lib.tqpk_argsort_stable(keys.data_ptr(), code_of(keys.dtype), int(bool(descending)),
+                                    perm_in.data_ptr() if perm_in is not None else None, n, out.data_ptr(),
+                                    ws.data_ptr(), ws.numel(), _stream(keys.device)), "tqpk_argsort_stable")
+    return out
+
+
+def topk_stable(keys: torch.Tensor, k: int, descending: bool = False,
+                perm_in: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """First k of the stable sort of keys[perm_in] (ties in input order)."""
+    lib = L.load()
+    keys = _col1d(keys)
+    n = int(perm_in.numel()) if perm_in is not None else int(keys.numel())
+    m = max(0, min(int(k), n))
+    _check_cuda(keys, perm_in)
+    out = torch.empty(m, dtype=torch.int64, device=keys.device)
+    if m == 0:
+        return out
+    ws = _ws(lib.tqpk_topk_workspace_bytes(n, m), keys.device)
+    L.check(lib.tqpk_topk_stable(keys.data_ptr(), code_of(keys.dtype), int(bool(descending)),
+                                 perm_in.data_ptr() if perm_in is not None else None, n, m, out.data_ptr(),
+                                 ws.data_ptr(), ws.numel(), _stream(keys.device)), "tqpk_topk_stable")
+    return out
+
+
+# ---------------------------------------------------------------- (c) join
+JOIN_TYPES = {"inner": L.JT_INNER, "right-semi": L.JT_SEMI, "right-anti": L.JT_ANTI, "right-outer": L.JT_OUTER}
+
+
+@dataclass
+class JoinBuild:
+    plan: L.JoinPlan
+    ws: torch.Tensor
+    keys: torch.Tensor
+    device: torch.device
+
+
+def join_build(keys: torch.Tensor, mask: Optional[torch.Tensor] = None) -> JoinBuild:
+    lib = L.load()
+    keys = _col1d(keys)
+    _check_cuda(keys, mask)
+    if keys.dtype == torch.float64:
+        raise NotImplementedError("join on a float64 key is not on the kernel path")
+    dev = keys.device
+    s = _stream(dev)
+    plan = L.JoinPlan()
+    scratch = _ws(256, dev)
+    mp = mask.data_ptr() if mask is not None else None
+    n = int(keys.numel())
+    L.check(lib.tqpk_join_plan_build(keys.data_ptr() if n else None, code_of(keys.dtype), mp, n, C.byref(plan),
+                                     scratch.data_ptr(), s), "tqpk_join_plan_build")
+    ws = _ws(plan.ws_bytes, dev)
+    L.check(lib.tqpk_join_build(C.byref(plan), keys.data_ptr() if n else None, code_of(keys.dtype), mp, n,
+                                ws.data_ptr(), ws.numel(), s), "tqpk_join_build")
+    return JoinBuild(plan, ws, keys, dev)
+
+
+def join_probe(build: JoinBuild, probe_keys: torch.Tensor, probe_mask: Optional[torch.Tensor] = None,
+               join_type: str = "inner") -> Tuple[torch.Tensor, torch.Tensor]:
+    """(build_idx, probe_idx) int64 row ids of the original inputs."""
+    lib = L.load()
+    pk = _col1d(probe_keys)
+    _check_cuda(pk, probe_mask)
+    if pk.dtype == torch.float64:
+        raise NotImplementedError("join on a float64 key is not on the kernel path")
+    jt = JOIN_TYPES[join_type]
+    dev = build.device
+    s = _stream(dev)
+    n = int(pk.numel())
+    pws = _ws(lib.tqpk_join_probe_workspace_bytes(n), dev)
+    mp = probe_mask.data_ptr() if probe_mask is not None else None
+    # Unique build keys (and semi/anti joins) give at most one output per probe row.
+    cap = n if (build.plan.unique or jt in (L.JT_SEMI, L.JT_ANTI)) else 0
+    for _ in range(2):
+        ob = torch.empty(cap, dtype=torch.int64, device=dev)
+        op = torch.empty(cap, dtype=torch.int64, device=dev)
+        cnt = C.c_int64(0)
+        st = lib.tqpk_join_probe(C.byref(build.plan), build.ws.data_ptr(), pk.data_ptr() if n else None,
+                                 code_of(pk.dtype), mp, n, jt, ob.data_ptr() if cap else None,
+                                 op.data_ptr() if cap else None, cap, C.byref(cnt), pws.data_ptr(), pws.numel(), s)
+        if st == L.ECAPACITY:
+            cap = cnt.value
+            continue
+        L.check(st, "tqpk_join_probe")
+        m = cnt.value
+        return ob[:m], op[:m]
+    raise RuntimeError("tqpk_join_probe: output size changed between calls")
+
+
+def gather(cols: Sequence[torch.Tensor], idx: torch.Tensor, null_aware: bool = False) -> List[torch.Tensor]:
+    """out_c = col_c[idx]; with null_aware an index of -64 yields -64 (index_with_null)."""
+    lib = L.load()
+    cols = [_col1d(c) for c in cols]
+    _check_cuda(idx, *cols)
+    n = int(idx.numel())
+    outs = [torch.empty(n, dtype=c.dtype, device=idx.device) for c in cols]
+    if n == 0 or not cols:
+        return outs
+    if len(cols) > L.MAX_COLS:
+        return gather(cols[:L.MAX_COLS], idx, null_aware) + gather(cols[L.MAX_COLS:], idx, null_aware)
+    L.check(lib.tqpk_gather(len(cols), _vp_array([c.data_ptr() for c in cols]),
+                            _i32_array([code_of(c.dtype) for c in cols]), idx.contiguous().data_ptr(), n,
+                            int(bool(null_aware)), _vp_array([o.data_ptr() for o in outs]), _stream(idx.device)),
+            "tqpk_gather")
+    return outs

@@ -1,0 +1,77 @@
+"""Fused query pipelines over device-resident columns (no host sync inside).
+
+``JoinAggTopK`` runs the plan main.py executes as Filter(build),
+Filter(probe), Join, Aggregate(sum(expr) group by build key), take ordered
+(limit k) -- the shape of the filtered equi-join + aggregate + top-10
+workload -- as tqpk_pipeline_join_agg_topk: build, probe+aggregate, top-k.
+The same trees and argument dicts as the operators are accepted, so a plan
+can be routed here when its build key is a primary key (unique); if the
+kernel finds a repeated build key it reports it and ``result()`` raises, so
+the caller can run the operator path instead.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, Optional
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .dtypes import code_of
+from .expr import compile_aggregate
+from .predicate import compile_filter
+
+
+class JoinAggTopK:
+    def __init__(self, build_keys: torch.Tensor, key_min: int, key_max: int, probe_fk: torch.Tensor,
+                 build_cols: Dict[int, torch.Tensor], build_filter, probe_cols: Dict[int, torch.Tensor],
+                 probe_filter, value_tree, k: int = 10, descending: bool = True):
+        self.lib = L.load()
+        self.dev = build_keys.device
+        self.bk = build_keys.contiguous()
+        self.pk = probe_fk.contiguous()
+        self.key_min, self.key_max = int(key_min), int(key_max)
+        self.bpred = compile_filter(build_filter, build_cols) if build_filter is not None else None
+        self.ppred = compile_filter(probe_filter, probe_cols) if probe_filter is not None else None
+        prog = compile_aggregate({"keys": None, "results": [[[["sum", value_tree], "#", "1"], "AS", "v#1"]]},
+                                 probe_cols)
+        self.prog = prog
+        self.value_reg = prog.spec.accs[prog.outputs[0][2]].reg
+        if not 1 <= k <= 32:
+            raise NotImplementedError("the fused top-k handles k <= 32")
+        self.k, self.desc = int(k), bool(descending)
+        nbytes = self.lib.tqpk_pipeline_join_agg_topk_workspace_bytes(self.key_min, self.key_max)
+        self.ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.dev)
+        self.out_keys = torch.empty(self.k, dtype=torch.int64, device=self.dev)
+        self.out_vals = torch.empty(self.k, dtype=torch.float64, device=self.dev)
+        self.out_count = torch.zeros(1, dtype=torch.int64, device=self.dev)
+        self.groups = torch.zeros(1, dtype=torch.int64, device=self.dev)
+
+    @property
+    def workspace_bytes(self) -> int:
+        return int(self.ws.numel())
+
+    def run(self, stream=None):
+        s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
+        L.check(self.lib.tqpk_pipeline_join_agg_topk(
+            self.bk.data_ptr(), code_of(self.bk.dtype), self.bk.numel(),
+            C.byref(self.bpred.struct) if self.bpred else None, self.key_min, self.key_max,
+            self.pk.data_ptr(), code_of(self.pk.dtype), self.pk.numel(),
+            C.byref(self.ppred.struct) if self.ppred else None, C.byref(self.prog.spec), self.value_reg,
+            self.k, int(self.desc), self.ws.data_ptr(), self.ws.numel(), self.out_keys.data_ptr(),
+            self.out_vals.data_ptr(), self.out_count.data_ptr(), self.groups.data_ptr(), s),
+            "tqpk_pipeline_join_agg_topk")
+
+    def check_error(self, stream=None):
+        s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
+        err = C.c_int(0)
+        L.check(self.lib.tqpk_pipeline_error(self.ws.data_ptr(), C.byref(err), s), "tqpk_pipeline_error")
+        if err.value:
+            L.check(err.value, "fused join pipeline (repeated or out-of-domain build key)")
+
+    def result(self):
+        """(keys int64[m], sums float64[m], groups) after the last run (synchronises)."""
+        self.check_error()
+        m = int(self.out_count.item())
+        return (self.out_keys[:m].cpu().numpy(), self.out_vals[:m].cpu().numpy(), int(self.groups.item()))

@@ -1,0 +1,234 @@
+"""Compiles TQP-Inmem filter trees into the device predicate program.
+
+The input is the parsed tree the reference's ``operators/filter.py:evaluate``
+walks (``filter.py:14-162``): nested lists of strings such as
+``[['isnotnull', ['d#7']], 'AND', ['d#7', '<=', '1998-09-02']]``.  The output
+is a postfix ``tqpk_predicate`` (include/tqpk.h) whose comparisons carry the
+reference's exact semantics:
+
+* float literals with ``<=``/``>=`` get the reference's ``+-eps``
+  (``filter.py:145-149``), computed here in Python double arithmetic exactly
+  as the reference does;
+* ``=`` on a float64 column is ``torch.isclose(atol=eps)`` (``:160-161``); the
+  allowed error ``atol + |rtol * lit|`` is precomputed the same way;
+* an integer column against a Python float compares in float32, the dtype
+  torch promotes that pair to;
+* ``isnotnull`` is all-true (``:67-69``), ``IN`` is an OR of equalities
+  (``:90-119``), a one-character string literal compares with ``ord``.
+
+String predicates (StartsWith / Contains / LIKE / multi-character equality /
+substring) are not on the kernel path and raise ``NotImplementedError``.
+"""
+from __future__ import annotations
+
+import datetime as _dt
+from dataclasses import dataclass, field
+from typing import Any, Dict, List
+
+import numpy as np
+
+from . import _lib as L
+from .dtypes import code_of
+
+EPS = 1e-5        # constants.py:8
+RTOL = 1e-5       # torch.isclose default rtol
+_EPOCH = _dt.date(1990, 1, 1)   # conversion.py:11
+
+_CMP = {"<": L.LT, "<=": L.LE, ">": L.GT, ">=": L.GE, "=": L.EQ, "<>": L.NE}
+_FLIP = {"<": ">", "<=": ">=", ">": "<", ">=": "<=", "=": "=", "<>": "<>"}
+
+
+def get_id(name: str) -> int:
+    """parsing.py:15-16"""
+    return int(name.split("#")[-1].replace("L", ""))
+
+
+def _is_date(s: str) -> bool:
+    return len(s) == 10 and s.count("-") == 2 and s.replace("-", "").isdigit()
+
+
+def _is_float(s: str) -> bool:
+    return s.replace(".", "").replace("-", "").replace("E", "").isdigit()
+
+
+@dataclass
+class _Col:
+    cid: int
+
+
+@dataclass
+class CompiledPredicate:
+    """A predicate program plus the column tensors it reads (kept alive)."""
+    struct: Any
+    tensors: List[Any] = field(default_factory=list)
+    col_ids: List[int] = field(default_factory=list)
+
+    def bind(self):
+        return self.struct
+
+
+class _Compiler:
+    def __init__(self, columns: Dict[int, Any], subquery=None):
+        self.columns = columns
+        self.subquery = subquery
+        self.insn: List[tuple] = []
+        self.slots: Dict[int, int] = {}
+
+    # -- values -------------------------------------------------------------
+    def value(self, tree):
+        if isinstance(tree, str):
+            if tree == "Subquery":
+                if self.subquery is None:
+                    raise ValueError("filter references a subquery result but none was given")
+                return self.subquery
+            if _is_date(tree):
+                return (_dt.date.fromisoformat(tree) - _EPOCH).days
+            if _is_float(tree):
+                return float(tree) if "." in tree else int(tree)
+            if "#" in tree and not tree.startswith("Brand#"):
+                return _Col(get_id(tree))
+            return tree
+        if len(tree) == 1:
+            return self.value(tree[0])
+        if len(tree) == 3 and tree[1] == "#":
+            return _Col(int(tree[-1]))
+        if len(tree) == 2 and tree[0] == "cast":
+            literal, _, cast_type = tree[1][0].split(" ")
+            if cast_type == "double":
+                return self.value(literal)
+        return None  # a boolean sub-expression
+
+    def slot(self, cid: int) -> int:
+        if cid not in self.slots:
+            if cid not in self.columns:
+                raise KeyError(f"filter column {cid} is not among the operator's inputs")
+            if len(self.slots) >= L.MAX_COLS:
+                raise NotImplementedError(f"predicate reads more than {L.MAX_COLS} columns")
+            self.slots[cid] = len(self.slots)
+        return self.slots[cid]
+
+    def col_tensor(self, cid: int):
+        t = self.columns[cid]
+        if t.dim() == 2 and t.shape[1] == 1:
+            t = t.reshape(-1)
+        if t.dim() != 1:
+            raise NotImplementedError("string (2-D) columns are not on the kernel path")
+        return t
+
+    def dtype(self, cid: int) -> int:
+        return code_of(self.col_tensor(cid).dtype)
+
+    # -- emission -------------------------------------------------------------
+    def emit_cmp(self, col: _Col, op: str, lit):
+        dt = self.dtype(col.cid)
+        s = self.slot(col.cid)
+        if dt == L.F64:
+            self.insn.append((L.P_CMP, s, _CMP[op], L.DOM_F64, 0, float(lit), 0.0))
+        elif isinstance(lit, float):
+            self.insn.append((L.P_CMP, s, _CMP[op], L.DOM_F32, 0, float(np.float32(lit)), 0.0))
+        else:
+            self.insn.append((L.P_CMP, s, _CMP[op], L.DOM_I64, int(lit), 0.0, 0.0))
+
+    def emit(self, tree):
+        """Emits code that pushes a bool mask for `tree`."""
+        if isinstance(tree, list) and len(tree) == 1:
+            return self.emit(tree[0])
+        if isinstance(tree, str) or (len(tree) == 3 and tree[1] == "#"):
+            v = self.value(tree)
+            if isinstance(v, _Col) and self.col_tensor(v.cid).dtype.is_floating_point is False \
+                    and self.dtype(v.cid) in (L.BOOL,):
+                self.insn.append((L.P_MASK, self.slot(v.cid), 0, 0, 0, 0.0, 0.0))
+                return
+            raise NotImplementedError(f"filter leaf {tree!r} is not a boolean")
+        if len(tree) == 2:
+            head = tree[0]
+            if head == "NOT":
+                self.emit(tree[1])
+                self.insn.append((L.P_NOT, 0, 0, 0, 0, 0.0, 0.0))
+                return
+            if head == "isnotnull":
+                self.insn.append((L.P_TRUE, 0, 0, 0, 0, 0.0, 0.0))
+                return
+            if head in ("StartsWith", "EndsWith", "Contains", "substring"):
+                raise NotImplementedError(f"string predicate {head} is not on the kernel path")
+            raise ValueError(f"Unsupported Function: {head}")
+        op = tree[-2]
+        if op == "IN":
+            L_ = self.value(tree[0])
+            if not isinstance(L_, _Col):
+                raise NotImplementedError("IN on a non-column operand")
+            dt = self.dtype(L_.cid)
+            if dt in (L.I64, L.I32):
+                vals = [int(r) for r in tree[-1]]
+            elif dt == L.F64:
+                vals = [float(r) for r in tree[-1]]
+            else:
+                raise AssertionError("IN supports int/date/float columns only (filter.py:96-102)")
+            if not vals:
+                self.insn.append((L.P_FALSE, 0, 0, 0, 0, 0.0, 0.0))
+                return
+            for i, r in enumerate(vals):
+                self.emit_cmp(L_, "=", r) if dt != L.F64 else self.insn.append(
+                    (L.P_CMP, self.slot(L_.cid), L.EQ, L.DOM_F64, 0, r, 0.0))
+                if i:
+                    self.insn.append((L.P_OR, 0, 0, 0, 0, 0.0, 0.0))
+            return
+        if op == "LIKE":
+            raise NotImplementedError("LIKE is not on the kernel path")
+        if op in ("AND", "OR"):
+            self.emit(tree[0])
+            self.emit(tree[-1])
+            self.insn.append((L.P_AND if op == "AND" else L.P_OR, 0, 0, 0, 0, 0.0, 0.0))
+            return
+        if op not in ("<=", ">=", "<", ">", "="):
+            raise ValueError(f"Unsupported Operation: {op}")
+        Lv = self.value(tree[0])
+        Rv = self.value(tree[-1])
+        if isinstance(Lv, _Col) and isinstance(Rv, _Col):
+            da, db = self.dtype(Lv.cid), self.dtype(Rv.cid)
+            dom = L.DOM_F64 if L.F64 in (da, db) else L.DOM_I64
+            self.insn.append((L.P_CMPCOL, self.slot(Lv.cid), _CMP[op], dom, self.slot(Rv.cid), 0.0, 0.0))
+            return
+        if not isinstance(Lv, _Col):
+            if isinstance(Rv, _Col):      # literal <op> column: same comparison mirrored
+                Lv, Rv, op = Rv, Lv, _FLIP[op]
+            else:
+                raise NotImplementedError(f"comparison without a column operand: {tree!r}")
+        if isinstance(Rv, float):                          # filter.py:145-149
+            if op == "<=":
+                return self.emit_cmp(Lv, "<=", Rv + EPS)
+            if op == ">=":
+                return self.emit_cmp(Lv, ">=", Rv - EPS)
+        if isinstance(Rv, str):                            # filter.py:151-158
+            if len(Rv) == 1:
+                return self.emit_cmp(Lv, op, ord(Rv))
+            raise NotImplementedError("multi-character string comparison is not on the kernel path")
+        if op == "=" and self.dtype(Lv.cid) == L.F64:     # filter.py:160-161
+            if not isinstance(Rv, float):
+                raise TypeError("isclose against a non-float literal (the reference raises here too)")
+            allowed = EPS + abs(RTOL * Rv)
+            self.insn.append((L.P_CMP, self.slot(Lv.cid), L.ISCLOSE, L.DOM_F64, 0, Rv, allowed))
+            return
+        return self.emit_cmp(Lv, op, Rv)
+
+
+def compile_filter(tree, columns: Dict[int, Any], subquery=None) -> CompiledPredicate:
+    """Compiles a filter tree over ``columns`` (id -> 1-D device tensor)."""
+    c = _Compiler(columns, subquery)
+    c.emit(tree)
+    if len(c.insn) > L.MAX_PRED:
+        raise NotImplementedError(f"predicate longer than {L.MAX_PRED} instructions")
+    p = L.Predicate()
+    p.n_insn = len(c.insn)
+    p.n_cols = len(c.slots)
+    tensors = []
+    ids = [None] * len(c.slots)
+    for cid, s in c.slots.items():
+        t = c.col_tensor(cid).contiguous()
+        tensors.append(t)
+        ids[s] = cid
+        p.cols[s] = t.data_ptr()
+        p.dtypes[s] = code_of(t.dtype)
+    for i, (op, col, cmp, dom, li, lf, la) in enumerate(c.insn):
+        p.insn[i] = L.PredInsn(op, col, cmp, dom, li, lf, la)
+    return CompiledPredicate(p, tensors, ids)

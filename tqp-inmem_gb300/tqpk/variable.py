@@ -1,0 +1,59 @@
+"""Column container with the same interface as TQP-Inmem's ``variable.py``.
+
+The drop-in operators accept any object with ``.tensor`` and ``.tensor_type``
+(normally the reference's own ``variable.Variable``) and build their outputs
+with the class of the input they replace, so the plan executor keeps seeing
+its own type.  This class is the stand-in for callers without the reference
+tree (tests, the benchmark).  Reference: variable.py:9-61, constants.py:3-6.
+"""
+from __future__ import annotations
+
+import torch
+
+string_dtype = torch.int8
+int_dtype = torch.int64
+float_dtype = torch.float64
+date_dtype = torch.int32
+
+
+class Variable:
+    """variable.py:9-43"""
+
+    def __init__(self, tensor, tensor_type: str, backing_mem_ptr=None, var_state="cpu resident",
+                 is_sorted: bool = False):
+        self.tensor = tensor
+        self.tensor_type = tensor_type
+        self.state = var_state
+        self.backing_mem_ptr = backing_mem_ptr
+        self.is_sorted = is_sorted
+
+    def __repr__(self):
+        return f"Variable (tensor size = {self.tensor.shape} ({self.tensor.dtype}), tensor type = '{self.tensor_type}')"
+
+    def __iter__(self):
+        yield self.tensor
+        yield self.tensor_type
+
+    def normalize(self):
+        if self.tensor.dim() == 2:
+            self.tensor = self.tensor.squeeze()
+        if self.tensor.dim() == 0:
+            self.tensor = self.tensor.unsqueeze(0)
+        assert self.tensor.dim() == 1
+
+
+def torch_to_type(dtype) -> str:
+    """variable.py:45-52"""
+    if dtype == float_dtype:
+        return "float"
+    if dtype == date_dtype:
+        return "date"
+    if dtype == int_dtype:
+        return "int"
+    return "string"
+
+
+def make_like(proto, tensor, tensor_type: str):
+    """A new column of the same class as `proto` (the caller's Variable type)."""
+    cls = type(proto) if proto is not None and hasattr(proto, "tensor_type") else Variable
+    return cls(tensor, tensor_type)

@@ -208,7 +208,121 @@ class FilterGroupBy:
         return O.tqp_sort(agg, self.sargs, False)
 
 
-WORKLOADS = {c.name: c for c in (JoinAggTop10, FilterGroupBy)}
+class StarJoin:
+    name = "star_join"
+    NF, NA, NB, NC = 59_986_052, 2_000_000, 15_000_000, 1_500_000
+
+    def __init__(self, scale: float = 1.0):
+        from tqpk import datagen
+        nf, na, nb, nc = (max(1000, int(x * scale)) for x in (self.NF, self.NA, self.NB, self.NC))
+        self.n = (nf, na, nb, nc)
+        self.t = datagen.star_tables(nf, na, nb, nc, seed=11)
+        self.fact_rows = nf
+        self.config = {"workload": "star join fact x A(category = 1) x B x C, sum(price*(1-discount)) and count "
+                                   "group by C key, top-100", "fact_rows": nf, "a_rows": na, "b_rows": nb,
+                       "c_rows": nc, "l2": "inputs (1.4 GB) larger than L2"}
+        t = self.t
+        self.cols = {31: t["a_key"], 32: t["a_cat"], 41: t["f_fka"], 42: t["f_fkb"], 43: t["f_price"],
+                     44: t["f_discount"], 51: t["b_key"], 52: t["b_fkc"], 61: t["c_key"]}
+        self.types = {31: "int", 32: "int", 41: "int", 42: "int", 43: "float", 44: "float", 51: "int", 52: "int",
+                      61: "int"}
+        self.fa = {"filter tree": [["cat#32", "=", str(datagen.STAR_CATEGORY)]], "materialized in": [32],
+                   "out mask id": 901}
+        # join keys are always part of 'materialized in' (parsing.py:408-410 adds 'join in')
+        self.j1 = ({"left group": [31, 32], "right group": [41, 42, 43, 44], "materialized in": [31, 41, 42, 43, 44],
+                    "mask map": {31: 901}}, 31, 41)
+        self.j2 = ({"left group": [51, 52], "right group": [31, 41, 42, 43, 44],
+                    "materialized in": [51, 52, 42, 43, 44]}, 51, 42)
+        self.j3 = ({"left group": [61], "right group": [51, 52, 42, 43, 44], "materialized in": [61, 52, 43, 44]},
+                   61, 52)
+        self.value_tree = [["p#43", "*", ["1.0", "-", "d#44"]]]
+        self.aargs = {"is partial": False, "keys": ["c#61"], "input ids": [61, 43, 44],
+                      "results": ["c#61", [[["sum", self.value_tree], "#", "71"], "AS", "rev#72"],
+                                  [[["count", ["1"]], "#", "73L"], "AS", "cnt#74"]],
+                      "out agg ids": [72, 74]}
+        self.targs = {"limit": 100, "input ids": [61, 72, 74], "key ids": [72], "key orders": [True]}
+
+    def algorithmic_bytes(self):
+        nf, na, nb, nc = self.n
+        return nf * 24 + na * 5 + nb * 8 + nc * 4
+
+    def dominant(self):
+        from tqpk import _lib as L
+        return L.KID_STAR_PROBE, "k_star_probe", self.n[0] * 24
+
+    def setup_device(self, dev):
+        import torch
+        from tqpk.pipeline import StarAggTopK
+        d = {c: torch.from_numpy(a).to(dev) for c, a in self.cols.items()}
+        self.d = d
+        dom = lambda a: (int(a.min()), int(a.max()))  # noqa: E731  (table statistics)
+        self.pipe = StarAggTopK(d[41], d[42], {43: d[43], 44: d[44]}, None, self.value_tree,
+                                d[31], {32: d[32]}, self.fa["filter tree"], dom(self.cols[31]),
+                                d[51], d[52], dom(self.cols[51]), d[61], dom(self.cols[61]), k=100)
+        self.host = {c: torch.from_numpy(a).pin_memory() for c, a in self.cols.items()}
+        self.dev = dev
+
+    def step_device(self):
+        self.pipe.run()
+
+    def device_result(self):
+        k, v, c, _ = self.pipe.result()
+        return k, v, c
+
+    def _plan(self, tg, ops):
+        f, j, a, s = ops
+        f(tg, copy.deepcopy(self.fa))
+        for args, lk, rk in (self.j1, self.j2, self.j3):
+            tg = j(tg, copy.deepcopy(args), lk, rk)
+        tg = a(tg, copy.deepcopy(self.aargs))
+        return s(tg, copy.deepcopy(self.targs))
+
+    def step_e2e(self):
+        from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
+        from tqpk.variable import Variable
+        tg = {c: Variable(h.to(self.dev, non_blocking=True), self.types[c]) for c, h in self.host.items()}
+
+        def f(tg, a):
+            tqp_filter(True, tg, a, None, None, None, "f")
+
+        def j(tg, a, lk, rk):
+            join_vortex(True, tg, a, lk, rk, [], "inner", None, None, "j")
+            return tg
+
+        def ag(tg, a):
+            tqp_hash_aggregate(True, tg, a, None, None, "a")
+            return tg
+
+        def so(tg, a):
+            tqp_sort(True, tg, a, True, "t")
+            return tg
+        tg = self._plan(tg, (f, j, ag, so))
+        out = [tg[c].tensor.to("cpu").numpy().reshape(-1) for c in (61, 72, 74)]
+        h2d = sum(h.numel() * h.element_size() for h in self.host.values())
+        return tuple(out), h2d, sum(o.nbytes for o in out)
+
+    def oracle(self, cols=None):
+        from oracle import tqp_oracle as O
+        cols = dict(self.cols if cols is None else cols)
+
+        def f(tg, a):
+            tg[a["out mask id"]] = O.eval_filter(a["filter tree"], {c: tg[c] for c in a["materialized in"]})
+
+        def j(tg, a, lk, rk):
+            return O.join_vortex(tg, a, lk, rk, "inner")[0]
+
+        def ag(tg, a):
+            out = dict(tg)
+            out.update(O.tqp_hash_aggregate(tg, a))
+            return out
+
+        def so(tg, a):
+            return O.tqp_sort(tg, a, True)
+        r = self._plan(cols, (f, j, ag, so))
+        return r[61].reshape(-1), r[72], r[74]
+
+
+WORKLOADS = {c.name: c for c in (JoinAggTop10, FilterGroupBy, StarJoin)}
 
 
 # ---------------------------------------------------------------------------- helpers
@@ -298,7 +412,13 @@ def max_over_ranks(x, world):
 
 
 def compare(workload, got, exp):
-    if isinstance(workload, JoinAggTop10):
+    if isinstance(workload, StarJoin):
+        gk, gv, gc = got
+        ek, ev, ec = exp
+        assert np.array_equal(np.asarray(gk).reshape(-1), ek), (gk[:5], ek[:5])
+        assert np.all(np.abs(np.asarray(gv) - ev) <= 1e-12 * np.abs(ev)), (gv[:5], ev[:5])
+        assert np.array_equal(np.asarray(gc).reshape(-1), ec)
+    elif isinstance(workload, JoinAggTop10):
         gk, gv = got
         ek, ev = exp
         assert np.array_equal(np.asarray(gk).reshape(-1), np.asarray(ek).reshape(-1)), (gk, ek)

@@ -265,7 +265,7 @@ int tqpk_join_probe(const tqpk_join_plan* h_plan, const void* d_build_ws, const 
 
 /* ---- fused pipelines ------------------------------------------------------
  * Filter -> inner join on a unique build key -> sum(expr) group by build key
- * -> top-k by the sum (k <= 32), with no host synchronisation: the main.py
+ * -> top-k by the sum (k <= 256), with no host synchronisation: the main.py
  * plan Filter(build), Filter(probe), Join, Aggregate, take ordered in three
  * kernels.  [key_min, key_max] is the build table's key domain (a table
  * statistic); the directory has one slot per key in it.  h_values holds the
@@ -284,6 +284,22 @@ int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t build_dtype, i
                                 int32_t value_reg, int32_t k, int32_t descending, void* d_ws, size_t ws_bytes,
                                 int64_t* d_out_keys, double* d_out_vals, int64_t* d_out_count,
                                 int64_t* d_groups_out, tqpk_stream stream);
+/* Star join: fact (fkA, fkB, value columns) joins dimension A (filtered by
+ * h_a_pred), dimension B (whose column fkC references C) and dimension C;
+ * sum(expr) and count(*) grouped by the C key, top-k by the sum (k <= 256).
+ * Every dimension key must be unique (a primary key) inside its stated
+ * domain [min, max]; otherwise the workspace error word is set.  Outputs:
+ * keys (C key), sums, counts (may be NULL), *d_out_count rows.              */
+size_t tqpk_pipeline_star_workspace_bytes(int64_t a_slots, int64_t b_slots, int64_t c_slots);
+int tqpk_pipeline_star_agg_topk(const void* d_f_fka, int32_t f_fka_dtype, const void* d_f_fkb, int32_t f_fkb_dtype,
+                                int64_t nf, const tqpk_predicate* h_fact_pred, const tqpk_groupby_spec* h_values,
+                                int32_t value_reg, const void* d_a_key, int32_t a_dtype, int64_t na,
+                                const tqpk_predicate* h_a_pred, int64_t a_min, int64_t a_max, const void* d_b_key,
+                                int32_t b_dtype, const void* d_b_fkc, int32_t b_fkc_dtype, int64_t nb,
+                                int64_t b_min, int64_t b_max, const void* d_c_key, int32_t c_dtype, int64_t nc,
+                                int64_t c_min, int64_t c_max, int32_t k, int32_t descending, void* d_ws,
+                                size_t ws_bytes, int64_t* d_out_keys, double* d_out_vals, int64_t* d_out_counts,
+                                int64_t* d_out_count, int64_t* d_groups_out, tqpk_stream stream);
 /* Reads (synchronising) the error word a fused pipeline left in its workspace. */
 int tqpk_pipeline_error(const void* d_ws, int* h_err, tqpk_stream stream);
 

@@ -339,14 +339,33 @@ def group_rows(key_cols: Sequence[np.ndarray]) -> Tuple[List[np.ndarray], np.nda
     return [f[firsts] for f in flat], inverse
 
 
+def _sum_2steps(inverse: np.ndarray, v: np.ndarray, G: int, S: int) -> np.ndarray:
+    """scatter_reduce_2steps 'sum' (aggregate.py:133-147): row i goes to sub-slot
+    i % S of its group, sub-slots are accumulated in row order, then each
+    group's S sub-slots are summed (pairwise, as a torch/numpy row sum)."""
+    flat = inverse * S + (np.arange(inverse.size) % S)
+    part = np.bincount(flat, weights=v, minlength=G * S)
+    return part.reshape(G, S).sum(axis=1)
+
+
 def reduce_groups(fn: str, v, inverse: np.ndarray, G: int, n: int) -> np.ndarray:
-    """The reductions of aggregate.py:122-195 (both the bincount and the
-    2-step scatter_reduce forms compute the same mathematical result)."""
+    """The reductions of aggregate.py:122-195, including the 2-step
+    sub-slot form the reference switches to when rows/groups >= 2^16
+    (:127-131); the two forms differ only in float summation order."""
     if isinstance(v, int):                                          # :149-152
         v = np.full(n, v, np.int64)
     elif isinstance(v, float):
         v = np.full(n, v, np.float64)
+    two_step = G > 0 and n / G >= (1 << 16)                         # :127-131
+    S = max(1, n // (G << 6)) if two_step else 1
     is_int = v.dtype.kind in "iub"
+    if two_step and fn in ("sum", "avg", "count"):
+        vv = (v != NULL).astype(np.float64) if fn == "count" else v.astype(np.float64)
+        s = _sum_2steps(inverse, vv, G, S)
+        if fn == "avg":
+            with np.errstate(all="ignore"):
+                return s / _sum_2steps(inverse, np.ones(n), G, S)
+        return np.round(s).astype(np.int64) if (is_int or fn == "count") else s
     if fn == "min":                                                 # :154-160
         init = np.iinfo(np.int64).max if is_int else np.finfo(np.float64).max
         out = np.full(G, init, dtype=np.int64 if is_int else np.float64)

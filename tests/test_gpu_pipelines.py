@@ -1,0 +1,101 @@
+"""GPU parity of the fused pipelines against the oracle's operator sequence.
+
+Keys and order bit-exact, float64 sums within 1e-12 relative."""
+import copy
+
+import numpy as np
+import pytest
+import torch
+
+from golden_io import assert_f64_close
+from oracle import tqp_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    from tqpk import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def _oracle_join(cols, f1, f2, k):
+    jargs = {"left group": [11, 12], "right group": [21, 22, 23, 24], "materialized in": [11, 21, 23, 24],
+             "mask map": {11: 901, 21: 902, 23: 902, 24: 902}}
+    aargs = {"is partial": False, "keys": ["k#11"], "input ids": [11, 23, 24],
+             "results": ["k#11", [[["sum", [["p#23", "*", ["1.0", "-", "d#24"]]]], "#", "1"], "AS", "r#302"]],
+             "out agg ids": [302]}
+    oc = dict(cols)
+    oc[901] = O.eval_filter(f1, {12: cols[12]}) if f1 else np.ones(cols[11].size, bool)
+    oc[902] = O.eval_filter(f2, {22: cols[22]}) if f2 else np.ones(cols[21].size, bool)
+    res, _ = O.join_vortex(oc, jargs, 11, 21, "inner")
+    agg = O.tqp_hash_aggregate(res, aargs)
+    top = O.tqp_sort({11: agg[11], 302: agg[302]}, {"limit": k, "input ids": [11, 302], "key ids": [302],
+                                                    "key orders": [True]}, True)
+    return top[11].reshape(-1), top[302], agg[11].shape[0]
+
+
+@pytest.mark.parametrize("nb,np_rows,k,offset,dtype,filters", [
+    (100_000, 400_000, 10, 0, np.int32, True),
+    (3_000, 20_000, 200, 1_000_000, np.int64, True),
+    (50, 300, 256, -20, np.int32, False),
+    (1, 10, 10, 5, np.int64, True),
+    (20_000, 0, 10, 0, np.int32, True),
+])
+def test_join_pipeline_vs_oracle(nb, np_rows, k, offset, dtype, filters):
+    from tqpk.pipeline import JoinAggTopK
+    rng = np.random.default_rng(nb + np_rows)
+    cols = {11: (rng.permutation(nb) + 1 + offset).astype(dtype), 12: rng.integers(0, 2557, nb).astype(np.int32),
+            21: (rng.integers(1, nb + 3, np_rows) + offset).astype(dtype), 22: rng.integers(0, 2557, np_rows).astype(np.int32),
+            23: rng.integers(90000, 10495001, np_rows) / 100.0, 24: rng.integers(0, 11, np_rows) / 100.0}
+    f1 = [["bd#12", "<", "1170"]] if filters else None
+    f2 = [["pd#22", ">", "1170"]] if filters else None
+    d = {c: torch.from_numpy(a).cuda() for c, a in cols.items()}
+    p = JoinAggTopK(d[11], int(cols[11].min()), int(cols[11].max()), d[21], {12: d[12]}, f1,
+                    {22: d[22], 23: d[23], 24: d[24]}, f2, [["p#23", "*", ["1.0", "-", "d#24"]]], k=k)
+    for _ in range(2):              # reruns reuse the workspace
+        p.run()
+        keys, vals, groups = p.result()
+    ek, ev, eg = _oracle_join(cols, f1, f2, k)
+    assert groups == eg
+    np.testing.assert_array_equal(keys, ek)
+    assert_f64_close(vals, ev)
+
+
+def test_join_pipeline_repeated_build_key_raises():
+    from tqpk.pipeline import JoinAggTopK
+    bk = torch.tensor([1, 2, 2, 3], dtype=torch.int32, device="cuda")
+    pk = torch.tensor([1, 2, 3], dtype=torch.int32, device="cuda")
+    v = torch.ones(3, dtype=torch.float64, device="cuda")
+    p = JoinAggTopK(bk, 1, 3, pk, {}, None, {23: v}, None, ["p#23"], k=2)
+    p.run()
+    with pytest.raises(NotImplementedError):
+        p.result()
+
+
+@pytest.mark.parametrize("scale,k", [(0.05, 100), (0.01, 7), (0.002, 256)])
+def test_star_pipeline_vs_oracle(scale, k):
+    import bench
+    from tqpk.pipeline import StarAggTopK
+    w = bench.StarJoin(scale=scale)
+    w.targs = dict(w.targs, limit=k)
+    ek, ev, ec = w.oracle()
+    d = {c: torch.from_numpy(a).cuda() for c, a in w.cols.items()}
+    dom = lambda a: (int(a.min()), int(a.max()))  # noqa: E731
+    p = StarAggTopK(d[41], d[42], {43: d[43], 44: d[44]}, None, w.value_tree, d[31], {32: d[32]},
+                    w.fa["filter tree"], dom(w.cols[31]), d[51], d[52], dom(w.cols[51]), d[61], dom(w.cols[61]), k=k)
+    p.run()
+    keys, vals, cnts, groups = p.result()
+    np.testing.assert_array_equal(keys, ek)
+    assert_f64_close(vals, ev)
+    np.testing.assert_array_equal(cnts, ec)
+
+
+@pytest.mark.parametrize("k", [200, 256, 257, 1000])
+def test_topk_stable_large_k(k):
+    from tqpk.ops import topk_stable
+    rng = np.random.default_rng(k)
+    x = rng.integers(-1000, 1000, 300_001).astype(np.int64)
+    got = topk_stable(torch.from_numpy(x).cuda(), k, True).cpu().numpy()
+    np.testing.assert_array_equal(got, O._stable_order(x, True)[:k])

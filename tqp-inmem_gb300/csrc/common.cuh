@@ -101,6 +101,24 @@ __device__ __forceinline__ double f64_from_ordered(uint64_t o) {
   return u2d(u);
 }
 
+// Order-preserving uint64 image of a key of any dtype for sorting: signed ints
+// flip the sign bit; float64 flips sign-magnitude with -0.0 -> +0.0 and every
+// NaN mapped to the largest value (torch.sort's order); descending = bitwise
+// complement, which keeps equal keys in input order under a stable sort.
+__device__ __forceinline__ uint64_t sort_key_bits(uint64_t raw, int is_f64, int desc) {
+  uint64_t u;
+  if (is_f64) {
+    double d = __longlong_as_double(static_cast<long long>(raw));
+    if (d == 0.0) d = 0.0;
+    uint64_t b = static_cast<uint64_t>(__double_as_longlong(d));
+    if (d != d) b = 0x7ff8000000000000ull;
+    u = (b & (1ull << 63)) ? ~b : (b | (1ull << 63));
+  } else {
+    u = raw ^ (1ull << 63);
+  }
+  return desc ? ~u : u;
+}
+
 // ---- column loads -----------------------------------------------------------
 __device__ __forceinline__ int64_t ld_int(const void* p, int dt, int64_t i) {
   switch (dt) {
@@ -116,6 +134,11 @@ __device__ __forceinline__ int64_t ld_int(const void* p, int dt, int64_t i) {
 __device__ __forceinline__ double ld_f64(const void* p, int dt, int64_t i) {
   if (dt == TQPK_F64) return static_cast<const double*>(p)[i];
   return static_cast<double>(ld_int(p, dt, i));
+}
+__device__ __forceinline__ uint64_t sort_key(const void* keys, int dt, int64_t i, int desc) {
+  const uint64_t raw = dt == TQPK_F64 ? static_cast<uint64_t>(__double_as_longlong(static_cast<const double*>(keys)[i]))
+                                      : static_cast<uint64_t>(ld_int(keys, dt, i));
+  return sort_key_bits(raw, dt == TQPK_F64, desc);
 }
 
 // Loads four consecutive rows r0..r0+3 (r0 % 4 == 0); rows >= n read as 0.
@@ -165,6 +188,88 @@ __device__ __forceinline__ void ld4_f64(const void* p, int64_t r0, int64_t n, bo
   }
 #pragma unroll
   for (int j = 0; j < 4; ++j) x[j] = (r0 + j < n) ? static_cast<const double*>(p)[r0 + j] : 0.0;
+}
+
+// ---- row expressions ---------------------------------------------------------
+// Straight-line expression program (tqpk_expr_insn) evaluated for one row.
+// Programs of up to NR instructions run fully unrolled with operands picked
+// by compile-time selects, so the register file stays in registers; longer
+// programs use the generic loop (a small local-memory array).
+__device__ __forceinline__ uint64_t expr_apply(const tqpk_expr_insn& X, uint64_t a, uint64_t b, const void* const* cols,
+                                              const int* dts, int64_t row) {
+  const bool f = X.type == TQPK_F64;
+  switch (X.op) {
+    case TQPK_X_COL:
+      return f ? static_cast<uint64_t>(__double_as_longlong(ld_f64(cols[X.col], dts[X.col], row)))
+               : static_cast<uint64_t>(ld_int(cols[X.col], dts[X.col], row));
+    case TQPK_X_CONST: return f ? static_cast<uint64_t>(__double_as_longlong(X.cf)) : static_cast<uint64_t>(X.ci);
+    case TQPK_X_TOF64:
+      return static_cast<uint64_t>(__double_as_longlong(static_cast<double>(static_cast<int64_t>(a))));
+    case TQPK_X_ADD:
+      return f ? static_cast<uint64_t>(__double_as_longlong(__dadd_rn(__longlong_as_double(a), __longlong_as_double(b))))
+               : a + b;
+    case TQPK_X_SUB:
+      return f ? static_cast<uint64_t>(__double_as_longlong(__dsub_rn(__longlong_as_double(a), __longlong_as_double(b))))
+               : a - b;
+    case TQPK_X_MUL:
+      return f ? static_cast<uint64_t>(__double_as_longlong(__dmul_rn(__longlong_as_double(a), __longlong_as_double(b))))
+               : static_cast<uint64_t>(static_cast<int64_t>(a) * static_cast<int64_t>(b));
+    case TQPK_X_DIV:
+      return static_cast<uint64_t>(__double_as_longlong(__ddiv_rn(__longlong_as_double(a), __longlong_as_double(b))));
+  }
+  return 0;
+}
+
+template <int NR>
+__device__ __forceinline__ void expr_eval_small(const tqpk_expr_insn* E, int n, const void* const* cols,
+                                                const int* dts, int64_t row, uint64_t (&r)[NR]) {
+#pragma unroll
+  for (int i = 0; i < NR; ++i) {
+    r[i] = 0;
+    if (i < n) {
+      const tqpk_expr_insn& X = E[i];
+      uint64_t a = 0, b = 0;
+#pragma unroll
+      for (int j = 0; j < i; ++j) {
+        a = (X.a == j) ? r[j] : a;
+        b = (X.b == j) ? r[j] : b;
+      }
+      r[i] = expr_apply(X, a, b, cols, dts, row);
+    }
+  }
+}
+
+template <int NR>
+__device__ __forceinline__ uint64_t reg_pick(const uint64_t (&r)[NR], int idx) {
+  uint64_t v = 0;
+#pragma unroll
+  for (int j = 0; j < NR; ++j) v = (idx == j) ? r[j] : v;
+  return v;
+}
+
+__device__ __forceinline__ void expr_eval_generic(const tqpk_expr_insn* E, int n, const void* const* cols,
+                                                  const int* dts, int64_t row, uint64_t* r) {
+  for (int i = 0; i < n; ++i) {
+    const tqpk_expr_insn& X = E[i];
+    r[i] = expr_apply(X, (X.op >= TQPK_X_ADD) ? r[X.a] : 0, (X.op >= TQPK_X_ADD && X.op <= TQPK_X_DIV) ? r[X.b] : 0,
+                      cols, dts, row);
+  }
+}
+
+// Value of register `out` for one row as a double (integers converted).
+__device__ __forceinline__ double expr_value(const tqpk_groupby_spec& S, int64_t row, int out) {
+  const bool f = S.expr[out].type == TQPK_F64;
+  uint64_t v;
+  if (out < 8) {
+    uint64_t r[8];
+    expr_eval_small<8>(S.expr, out + 1, S.cols, S.col_dtypes, row, r);
+    v = reg_pick<8>(r, out);
+  } else {
+    uint64_t r[TQPK_MAX_EXPR];
+    expr_eval_generic(S.expr, out + 1, S.cols, S.col_dtypes, row, r);
+    v = r[out];
+  }
+  return f ? __longlong_as_double(static_cast<long long>(v)) : static_cast<double>(static_cast<int64_t>(v));
 }
 
 // ---- predicate interpreter (filter.py:14-162) -------------------------------
@@ -225,6 +330,11 @@ __device__ __forceinline__ uint32_t pred_leaf4(const tqpk_predicate& P, const tq
 
 // Evaluates the predicate for rows r0..r0+3 -> 4-bit mask (rows >= n are 0).
 __device__ __forceinline__ uint32_t eval_pred4(const tqpk_predicate& P, int64_t r0, int64_t n, bool vec) {
+  if (P.n_insn == 1 && P.insn[0].op == TQPK_P_CMP) {  // one comparison: no stack
+    const int64_t valid = n - r0;
+    const uint32_t vm = valid >= 4 ? 0xfu : (valid <= 0 ? 0u : ((1u << valid) - 1));
+    return pred_leaf4(P, P.insn[0], r0, n, vec) & vm;
+  }
   uint32_t st[TQPK_MAX_PRED];
   int sp = 0;
   for (int k = 0; k < P.n_insn; ++k) {

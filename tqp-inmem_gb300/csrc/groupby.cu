@@ -42,54 +42,26 @@ __device__ __forceinline__ uint64_t acc_init(const tqpk_acc& a) {
   return 0ull;
 }
 
-// Evaluates the expression program for one row into reg[] (int64 or f64 bits).
-__device__ __forceinline__ void eval_expr(const tqpk_groupby_spec& S, int64_t row, uint64_t* reg) {
-  for (int i = 0; i < S.n_expr; ++i) {
-    const tqpk_expr_insn& X = S.expr[i];
-    uint64_t r = 0;
-    const bool f = X.type == TQPK_F64;
-    switch (X.op) {
-      case TQPK_X_COL:
-        r = f ? d2u(ld_f64(S.cols[X.col], S.col_dtypes[X.col], row))
-              : static_cast<uint64_t>(ld_int(S.cols[X.col], S.col_dtypes[X.col], row));
-        break;
-      case TQPK_X_CONST: r = f ? d2u(X.cf) : static_cast<uint64_t>(X.ci); break;
-      case TQPK_X_TOF64: r = d2u(static_cast<double>(static_cast<int64_t>(reg[X.a]))); break;
-      case TQPK_X_ADD:
-        r = f ? d2u(__dadd_rn(u2d(reg[X.a]), u2d(reg[X.b]))) : reg[X.a] + reg[X.b];
-        break;
-      case TQPK_X_SUB:
-        r = f ? d2u(__dsub_rn(u2d(reg[X.a]), u2d(reg[X.b]))) : reg[X.a] - reg[X.b];
-        break;
-      case TQPK_X_MUL:
-        r = f ? d2u(__dmul_rn(u2d(reg[X.a]), u2d(reg[X.b])))
-              : static_cast<uint64_t>(static_cast<int64_t>(reg[X.a]) * static_cast<int64_t>(reg[X.b]));
-        break;
-      case TQPK_X_DIV: r = d2u(__ddiv_rn(u2d(reg[X.a]), u2d(reg[X.b]))); break;
-    }
-    reg[i] = r;
-  }
-}
-
 // Plain (owner-only) update of one accumulator cell.
-__device__ __forceinline__ void acc_plain(uint64_t* p, const tqpk_acc& a, const uint64_t* reg) {
+// x is the raw register value (float64 or int64 bits) of the accumulated expression.
+__device__ __forceinline__ void acc_plain(uint64_t* p, const tqpk_acc& a, uint64_t x) {
   switch (a.kind) {
     case TQPK_ACC_SUM:
-      if (a.type == TQPK_F64) *p = d2u(__dadd_rn(u2d(*p), u2d(reg[a.reg])));
-      else *p += reg[a.reg];
+      if (a.type == TQPK_F64) *p = d2u(__dadd_rn(u2d(*p), u2d(x)));
+      else *p += x;
       break;
     case TQPK_ACC_COUNT_ROWS: *p += 1; break;
     case TQPK_ACC_COUNT_NOTNULL:
-      if (a.type == TQPK_F64) *p += (u2d(reg[a.reg]) != (double)TQPK_NULL_INDEX);
-      else *p += (static_cast<int64_t>(reg[a.reg]) != TQPK_NULL_INDEX);
+      if (a.type == TQPK_F64) *p += (u2d(x) != (double)TQPK_NULL_INDEX);
+      else *p += (static_cast<int64_t>(x) != TQPK_NULL_INDEX);
       break;
     case TQPK_ACC_MIN:
-      if (a.type == TQPK_F64) *p = min(*p, f64_ordered(u2d(reg[a.reg])));
-      else *p = static_cast<uint64_t>(min(static_cast<int64_t>(*p), static_cast<int64_t>(reg[a.reg])));
+      if (a.type == TQPK_F64) *p = min(*p, f64_ordered(u2d(x)));
+      else *p = static_cast<uint64_t>(min(static_cast<int64_t>(*p), static_cast<int64_t>(x)));
       break;
     case TQPK_ACC_MAX:
-      if (a.type == TQPK_F64) *p = max(*p, f64_ordered(u2d(reg[a.reg])));
-      else *p = static_cast<uint64_t>(max(static_cast<int64_t>(*p), static_cast<int64_t>(reg[a.reg])));
+      if (a.type == TQPK_F64) *p = max(*p, f64_ordered(u2d(x)));
+      else *p = static_cast<uint64_t>(max(static_cast<int64_t>(*p), static_cast<int64_t>(x)));
       break;
   }
 }
@@ -115,14 +87,25 @@ __device__ __forceinline__ void acc_merge_atomic(uint64_t* p, const tqpk_acc& a,
 }
 
 // Accumulator encoding of one row's contribution.
-__device__ __forceinline__ uint64_t acc_value(const tqpk_acc& a, const uint64_t* reg) {
+__device__ __forceinline__ uint64_t acc_value(const tqpk_acc& a, uint64_t x) {
   switch (a.kind) {
-    case TQPK_ACC_SUM: return reg[a.reg];
+    case TQPK_ACC_SUM: return x;
     case TQPK_ACC_COUNT_ROWS: return 1ull;
     case TQPK_ACC_COUNT_NOTNULL:
-      return a.type == TQPK_F64 ? (u2d(reg[a.reg]) != (double)TQPK_NULL_INDEX)
-                                : (static_cast<int64_t>(reg[a.reg]) != TQPK_NULL_INDEX);
-    default: return a.type == TQPK_F64 ? f64_ordered(u2d(reg[a.reg])) : reg[a.reg];
+      return a.type == TQPK_F64 ? (u2d(x) != (double)TQPK_NULL_INDEX) : (static_cast<int64_t>(x) != TQPK_NULL_INDEX);
+    default: return a.type == TQPK_F64 ? f64_ordered(u2d(x)) : x;
+  }
+}
+
+template <int MODE>
+__device__ __forceinline__ void acc_row(const tqpk_groupby_spec& S, uint64_t* sm, uint64_t* gacc, int64_t K,
+                                        int64_t slot, int a, uint64_t x) {
+  if (MODE == 1) {
+    acc_plain(&sm[(slot * S.n_accs + a) * blockDim.x + threadIdx.x], S.accs[a], x);
+  } else if (MODE == 2) {
+    acc_merge_atomic(&sm[slot * S.n_accs + a], S.accs[a], acc_value(S.accs[a], x));
+  } else {
+    acc_merge_atomic(&gacc[(int64_t)a * K + slot], S.accs[a], acc_value(S.accs[a], x));
   }
 }
 
@@ -154,8 +137,8 @@ __global__ void __launch_bounds__(256) k_groupby_dense(const __grid_constant__ t
     for (int64_t i = threadIdx.x; i < K * A; i += T) sm[i] = acc_init(S.accs[i % A]);
   }
   __syncthreads();
-  uint64_t reg[TQPK_MAX_EXPR];
   const int64_t groups = (n + 3) >> 2;
+  const bool small = S.n_expr <= 8;
   for (int64_t g = blockIdx.x * (int64_t)T + threadIdx.x; g < groups; g += (int64_t)gridDim.x * T) {
     const int64_t r0 = g << 2;
     const uint32_t b = filter4(F, P, r0, n);
@@ -170,15 +153,14 @@ __global__ void __launch_bounds__(256) k_groupby_dense(const __grid_constant__ t
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       if (!((b >> j) & 1u)) continue;
-      eval_expr(S, r0 + j, reg);
-      for (int a = 0; a < A; ++a) {
-        if (MODE == MODE_PRIVATE) {
-          acc_plain(&sm[(slot[j] * A + a) * T + threadIdx.x], S.accs[a], reg);
-        } else if (MODE == MODE_SHARED) {
-          acc_merge_atomic(&sm[slot[j] * A + a], S.accs[a], acc_value(S.accs[a], reg));
-        } else {
-          acc_merge_atomic(&gacc[(int64_t)a * K + slot[j]], S.accs[a], acc_value(S.accs[a], reg));
-        }
+      if (small) {
+        uint64_t r[8];
+        expr_eval_small<8>(S.expr, S.n_expr, S.cols, S.col_dtypes, r0 + j, r);
+        for (int a = 0; a < A; ++a) acc_row<MODE>(S, sm, gacc, K, slot[j], a, reg_pick<8>(r, S.accs[a].reg));
+      } else {
+        uint64_t r[TQPK_MAX_EXPR];
+        expr_eval_generic(S.expr, S.n_expr, S.cols, S.col_dtypes, r0 + j, r);
+        for (int a = 0; a < A; ++a) acc_row<MODE>(S, sm, gacc, K, slot[j], a, r[S.accs[a].reg]);
       }
     }
   }

@@ -27,20 +27,6 @@ namespace tqpk {
 constexpr int kRadix = 256;
 constexpr int kPasses = 8;
 
-__device__ __forceinline__ uint64_t sort_key(const void* keys, int dt, int64_t i, int desc) {
-  uint64_t u;
-  if (dt == TQPK_F64) {
-    double d = static_cast<const double*>(keys)[i];
-    if (d == 0.0) d = 0.0;                               // -0.0 sorts equal to +0.0
-    uint64_t b = d2u(d);
-    if (isnan(d)) b = 0x7ff8000000000000ull;             // every NaN is the largest value
-    u = (b & (1ull << 63)) ? ~b : (b | (1ull << 63));
-  } else {
-    u = static_cast<uint64_t>(ld_int(keys, dt, i)) ^ (1ull << 63);
-  }
-  return desc ? ~u : u;
-}
-
 __global__ void __launch_bounds__(kBlock) k_sort_prepare(const void* keys, int dt, int desc, const int64_t* perm_in,
                                                          int64_t n, uint64_t* kout, int64_t* vout,
                                                          unsigned* hist /*[8][256]*/) {
@@ -210,22 +196,3 @@ extern "C" int tqpk_argsort_stable(const void* d_keys, int32_t dt, int32_t desc,
   return TQPK_OK;
 }
 
-extern "C" size_t tqpk_topk_workspace_bytes(int64_t n, int64_t k) {
-  (void)k;
-  return sort_ws_bytes(n < 0 ? 0 : n);
-}
-
-extern "C" int tqpk_topk_stable(const void* d_keys, int32_t dt, int32_t desc, const int64_t* d_perm_in, int64_t n,
-                                int64_t k, int64_t* d_perm_out, void* ws, size_t ws_bytes, tqpk_stream stream) {
-  if (n < 0 || k < 0 || (n > 0 && k > 0 && (!d_keys || !d_perm_out || !ws))) return TQPK_EINVAL;
-  if (!dtype_size(dt)) return TQPK_EDTYPE;
-  const int64_t m = std::min(n, k);
-  if (m == 0) return TQPK_OK;
-  if (ws_bytes < sort_ws_bytes(n)) return TQPK_ENOMEM;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int64_t* res = nullptr;
-  int rc = sort_pairs(d_keys, dt, desc ? 1 : 0, d_perm_in, n, ws, ws_bytes, s, &res);
-  if (rc) return rc;
-  TQPK_CUDA(cudaMemcpyAsync(d_perm_out, res, m * sizeof(int64_t), cudaMemcpyDeviceToDevice, s));
-  return TQPK_OK;
-}

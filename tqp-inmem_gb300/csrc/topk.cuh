@@ -1,0 +1,232 @@
+// topk.cuh - kernel (e): stable top-k with warp-resident sorted lists.
+//
+// Reference: operators/sort.py:41-42 sorts everything (stable) and keeps
+// perm[:limit].  The stable top-k order is lexicographic on
+// (order-preserving key, position), smaller first, so ties keep input order.
+//
+// Each warp keeps its best k entries as a sorted list striped over the warp
+// (entry p = row p/32 of lane p%32, R rows per lane, k <= 32*R).  A batch of 32
+// candidates is compared against the current k-th entry and the survivors
+// are inserted one by one (rank by ballot/popc, shift by shuffles).  A CTA
+// merges its warps' lists in shared memory, writes them out, and the last CTA
+// to finish (an atomic ticket, no waiting) merges the per-CTA lists.
+#pragma once
+
+#include "common.cuh"
+
+namespace tqpk {
+
+__device__ __forceinline__ bool tk_better(uint64_t ka, int64_t ia, uint64_t kb, int64_t ib) {
+  return ka < kb || (ka == kb && ia < ib);
+}
+
+template <int R>
+struct WarpList {
+  uint64_t key[R];
+  int64_t idx[R];  // -1 = empty
+  __device__ __forceinline__ void init() {
+#pragma unroll
+    for (int r = 0; r < R; ++r) { key[r] = ~0ull; idx[r] = -1; }
+  }
+  // entry at position p (warp-uniform p)
+  __device__ __forceinline__ void at(int p, uint64_t& k, int64_t& i) const {
+    const int rr = p >> 5, ll = p & 31;
+    k = ~0ull;
+    i = -1;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const uint64_t kk = __shfl_sync(0xffffffffu, key[r], ll);
+      const int64_t ii = __shfl_sync(0xffffffffu, idx[r], ll);
+      if (r == rr) { k = kk; i = ii; }
+    }
+  }
+  __device__ __forceinline__ void insert(int k, uint64_t ck, int64_t ci) {
+    const int lane = threadIdx.x & 31;
+    int pos = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const bool b = (r * 32 + lane < k) && idx[r] >= 0 && tk_better(key[r], idx[r], ck, ci);
+      pos += __popc(__ballot_sync(0xffffffffu, b));
+    }
+    if (pos >= k) return;
+#pragma unroll
+    for (int r = R - 1; r >= 0; --r) {
+      uint64_t uk = __shfl_up_sync(0xffffffffu, key[r], 1);
+      int64_t ui = __shfl_up_sync(0xffffffffu, idx[r], 1);
+      if (r > 0) {
+        const uint64_t pk = __shfl_sync(0xffffffffu, key[r - 1], 31);
+        const int64_t pi = __shfl_sync(0xffffffffu, idx[r - 1], 31);
+        if (lane == 0) { uk = pk; ui = pi; }
+      }
+      const int p = r * 32 + lane;
+      if (p > pos && p < k) { key[r] = uk; idx[r] = ui; }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      if (r * 32 + lane == pos) { key[r] = ck; idx[r] = ci; }
+  }
+  // Inserts the valid lanes' candidates that beat the current k-th entry.
+  __device__ __forceinline__ void offer(int k, uint64_t ck, int64_t ci, bool valid) {
+    uint64_t tk;
+    int64_t ti;
+    at(k - 1, tk, ti);
+    const bool cand = valid && (ti < 0 || tk_better(ck, ci, tk, ti));
+    uint32_t pending = __ballot_sync(0xffffffffu, cand);
+    while (pending) {
+      const int src = __ffs(pending) - 1;
+      pending &= pending - 1;
+      const uint64_t k0 = __shfl_sync(0xffffffffu, ck, src);
+      const int64_t i0 = __shfl_sync(0xffffffffu, ci, src);
+      insert(k, k0, i0);
+    }
+  }
+};
+
+// Candidate sources -----------------------------------------------------------
+// Occupied slots of a dense group table, keyed by their float64 sum.
+struct DenseSumSource {
+  const double* sum;
+  const unsigned* cnt;   // occupancy: non-zero for groups that received a row
+  int64_t n;
+  int desc;
+  __device__ __forceinline__ bool get(int64_t i, uint64_t& k) const {
+    if (i >= n || cnt[i] == 0) return false;
+    double v = sum[i];
+    if (v == 0.0) v = 0.0;
+    uint64_t b = d2u(v);
+    if (isnan(v)) b = 0x7ff8000000000000ull;
+    const uint64_t u = (b & (1ull << 63)) ? ~b : (b | (1ull << 63));
+    k = desc ? ~u : u;
+    return true;
+  }
+};
+
+// keys[perm_in[i]] (perm_in may be null) of any dtype, position i.
+struct ArraySource {
+  const void* keys;
+  int dt;
+  const int64_t* perm;
+  int64_t n;
+  int desc;
+  __device__ __forceinline__ bool get(int64_t i, uint64_t& k) const;
+};
+
+struct TopkOut {
+  int64_t* out_idx;     // positions (or slots) of the best entries
+  int64_t* out_count;   // min(k, valid items)
+  uint64_t* cand_key;   // [grid][k]
+  int64_t* cand_idx;
+  unsigned* ticket;
+  unsigned long long* valid_total;  // number of valid items seen (may be null)
+};
+
+template <int R, class Src>
+__global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
+  extern __shared__ unsigned char tk_smem[];
+  uint64_t* sk = reinterpret_cast<uint64_t*>(tk_smem);            // [8][32R]
+  int64_t* si = reinterpret_cast<int64_t*>(sk + 8 * 32 * R);
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpList<R> L;
+  L.init();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned valid = 0;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + warp * 32; base < src.n; base += stride) {
+    const int64_t i = base + lane;
+    uint64_t key = ~0ull;
+    const bool ok = src.get(i, key);
+    valid += ok;
+    L.offer(k, key, i, ok);
+  }
+  valid = __reduce_add_sync(0xffffffffu, valid);
+  if (lane == 0 && valid && O.valid_total) atomicAdd(O.valid_total, (unsigned long long)valid);
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    sk[warp * 32 * R + r * 32 + lane] = L.key[r];
+    si[warp * 32 * R + r * 32 + lane] = L.idx[r];
+  }
+  __syncthreads();
+  if (warp == 0) {
+    WarpList<R> M;
+    M.init();
+    for (int w = 0; w < 8; ++w)
+      for (int r = 0; r < R; ++r) {
+        const int p = r * 32 + lane;
+        const int64_t ii = si[w * 32 * R + p];
+        M.offer(k, sk[w * 32 * R + p], ii, p < k && ii >= 0);
+      }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int p = r * 32 + lane;
+      if (p < k) {
+        O.cand_key[(int64_t)blockIdx.x * k + p] = M.key[r];
+        O.cand_idx[(int64_t)blockIdx.x * k + p] = M.idx[r];
+      }
+    }
+    __threadfence();
+    unsigned prev = 0;
+    if (lane == 0) prev = atomicAdd(O.ticket, 1u);
+    prev = __shfl_sync(0xffffffffu, prev, 0);
+    if (lane == 0) last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // The last CTA: stage the per-CTA lists through shared memory (all threads,
+  // coalesced L2 loads) and let every warp merge its share, then warp 0
+  // merges the eight warp lists.
+  constexpr int CHUNK = 8 * 32 * R;
+  WarpList<R> F;
+  F.init();
+  const int64_t total = (int64_t)gridDim.x * k;
+  for (int64_t base = 0; base < total; base += CHUNK) {
+    for (int j = threadIdx.x; j < CHUNK; j += blockDim.x) {
+      const int64_t g = base + j;
+      sk[j] = g < total ? __ldcg(&O.cand_key[g]) : ~0ull;
+      si[j] = g < total ? __ldcg(&O.cand_idx[g]) : -1;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int p = warp * 32 * R + r * 32 + lane;
+      F.offer(k, sk[p], si[p], si[p] >= 0);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    sk[warp * 32 * R + r * 32 + lane] = F.key[r];
+    si[warp * 32 * R + r * 32 + lane] = F.idx[r];
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  WarpList<R> M;
+  M.init();
+  for (int w = 0; w < 8; ++w)
+    for (int r = 0; r < R; ++r) {
+      const int p = r * 32 + lane;
+      const int64_t ii = si[w * 32 * R + p];
+      M.offer(k, sk[w * 32 * R + p], ii, p < k && ii >= 0);
+    }
+  int cnt = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int p = r * 32 + lane;
+    const bool v = p < k && M.idx[r] >= 0;
+    cnt += __popc(__ballot_sync(0xffffffffu, v));
+    if (v) O.out_idx[p] = M.idx[r];
+  }
+  if (lane == 0) {
+    *O.out_count = cnt;
+    *O.ticket = 0;
+  }
+}
+
+// Host launcher: k <= 256.  cand arrays hold grid*k entries each.
+int topk_warp_launch(int kind, const void* src, int k, int grid, TopkOut O, cudaStream_t s);
+inline int topk_grid_size() { return num_sms() * 2; }
+inline size_t topk_scratch_bytes(int k) {
+  return 2 * align_up((size_t)topk_grid_size() * k * 8, 256) + 512;
+}
+
+}  // namespace tqpk

@@ -100,6 +100,12 @@ SIGNATURES = {
                                               _P(Predicate), _P(GroupbySpec), _I32, _I32, _I32, _VP, _SZ, _VP, _VP,
                                               _VP, _VP, _VP]),
     "tqpk_pipeline_error": (C.c_int, [_VP, _P(C.c_int), _VP]),
+    "tqpk_pipeline_star_workspace_bytes": (_SZ, [_I64, _I64, _I64]),
+    "tqpk_pipeline_star_agg_topk": (C.c_int, [_VP, _I32, _VP, _I32, _I64, _P(Predicate), _P(GroupbySpec), _I32,
+                                              _VP, _I32, _I64, _P(Predicate), _I64, _I64,
+                                              _VP, _I32, _VP, _I32, _I64, _I64, _I64,
+                                              _VP, _I32, _I64, _I64, _I64, _I32, _I32, _VP, _SZ,
+                                              _VP, _VP, _VP, _VP, _VP, _VP]),
 }
 
 KID_FILTER_MASK, KID_GROUPBY, KID_JOIN_PROBE, KID_PIPE_PROBE, KID_PIPE_BUILD, KID_PIPE_TOPK = 1, 3, 5, 6, 7, 8

@@ -38,8 +38,8 @@ class JoinAggTopK:
                                  probe_cols)
         self.prog = prog
         self.value_reg = prog.spec.accs[prog.outputs[0][2]].reg
-        if not 1 <= k <= 32:
-            raise NotImplementedError("the fused top-k handles k <= 32")
+        if not 1 <= k <= 256:
+            raise NotImplementedError("the fused top-k handles k <= 256")
         self.k, self.desc = int(k), bool(descending)
         nbytes = self.lib.tqpk_pipeline_join_agg_topk_workspace_bytes(self.key_min, self.key_max)
         self.ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.dev)
@@ -75,3 +75,62 @@ class JoinAggTopK:
         self.check_error()
         m = int(self.out_count.item())
         return (self.out_keys[:m].cpu().numpy(), self.out_vals[:m].cpu().numpy(), int(self.groups.item()))
+
+
+class StarAggTopK:
+    """Fact -> A (filtered) -> B -> C star join, sum(expr) and count(*) by the C key, top-k.
+
+    Dimension key domains are table statistics ([min, max] of each primary
+    key, computed once when the tables are loaded)."""
+
+    def __init__(self, f_fka, f_fkb, fact_cols: Dict[int, torch.Tensor], fact_filter, value_tree,
+                 a_key, a_cols: Dict[int, torch.Tensor], a_filter, a_dom, b_key, b_fkc, b_dom, c_key, c_dom,
+                 k: int = 100, descending: bool = True):
+        self.lib = L.load()
+        self.dev = f_fka.device
+        self.t = [x.contiguous() for x in (f_fka, f_fkb, a_key, b_key, b_fkc, c_key)]
+        self.fpred = compile_filter(fact_filter, fact_cols) if fact_filter is not None else None
+        self.apred = compile_filter(a_filter, a_cols) if a_filter is not None else None
+        self.prog = compile_aggregate({"keys": None, "results": [[[["sum", value_tree], "#", "1"], "AS", "v#1"]]},
+                                      fact_cols)
+        self.value_reg = self.prog.spec.accs[self.prog.outputs[0][2]].reg
+        if not 1 <= k <= 256:
+            raise NotImplementedError("the fused top-k handles k <= 256")
+        self.k, self.desc = int(k), bool(descending)
+        self.doms = [tuple(map(int, d)) for d in (a_dom, b_dom, c_dom)]
+        (amn, amx), (bmn, bmx), (cmn, cmx) = self.doms
+        nbytes = self.lib.tqpk_pipeline_star_workspace_bytes(amx - amn + 1, bmx - bmn + 1, cmx - cmn + 1)
+        self.ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.dev)
+        self.out_keys = torch.empty(self.k, dtype=torch.int64, device=self.dev)
+        self.out_vals = torch.empty(self.k, dtype=torch.float64, device=self.dev)
+        self.out_cnts = torch.empty(self.k, dtype=torch.int64, device=self.dev)
+        self.out_count = torch.zeros(1, dtype=torch.int64, device=self.dev)
+        self.groups = torch.zeros(1, dtype=torch.int64, device=self.dev)
+
+    @property
+    def workspace_bytes(self) -> int:
+        return int(self.ws.numel())
+
+    def run(self, stream=None):
+        s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
+        fa, fb, ak, bk, bc, ck = self.t
+        (amn, amx), (bmn, bmx), (cmn, cmx) = self.doms
+        L.check(self.lib.tqpk_pipeline_star_agg_topk(
+            fa.data_ptr(), code_of(fa.dtype), fb.data_ptr(), code_of(fb.dtype), fa.numel(),
+            C.byref(self.fpred.struct) if self.fpred else None, C.byref(self.prog.spec), self.value_reg,
+            ak.data_ptr(), code_of(ak.dtype), ak.numel(), C.byref(self.apred.struct) if self.apred else None, amn, amx,
+            bk.data_ptr(), code_of(bk.dtype), bc.data_ptr(), code_of(bc.dtype), bk.numel(), bmn, bmx,
+            ck.data_ptr(), code_of(ck.dtype), ck.numel(), cmn, cmx, self.k, int(self.desc),
+            self.ws.data_ptr(), self.ws.numel(), self.out_keys.data_ptr(), self.out_vals.data_ptr(),
+            self.out_cnts.data_ptr(), self.out_count.data_ptr(), self.groups.data_ptr(), s),
+            "tqpk_pipeline_star_agg_topk")
+
+    def result(self):
+        s = torch.cuda.current_stream(self.dev).cuda_stream
+        err = C.c_int(0)
+        L.check(self.lib.tqpk_pipeline_error(self.ws.data_ptr(), C.byref(err), s), "tqpk_pipeline_error")
+        if err.value:
+            L.check(err.value, "star pipeline (repeated or out-of-domain dimension key)")
+        m = int(self.out_count.item())
+        return (self.out_keys[:m].cpu().numpy(), self.out_vals[:m].cpu().numpy(),
+                self.out_cnts[:m].cpu().numpy(), int(self.groups.item()))

@@ -322,6 +322,170 @@ class StarJoin:
         return r[61].reshape(-1), r[72], r[74]
 
 
+class Batched:
+    """64 uneven instances (half filter+group-by, half join+aggregate+top-10; rows log-uniform in
+    [1e4, 1e7], group cardinality log-uniform in [4, 1e6]) as one persistent launch replayed from a
+    CUDA graph, against the same instances run one at a time through the drop-in operators."""
+    name = "batched"
+    AGG = ["flag#5", "status#6",
+           [[["sum", ["quantity#1"]], "#", "101"], "AS", "a#201"],
+           [[["sum", ["price#2"]], "#", "102"], "AS", "b#202"],
+           [[["sum", [["price#2", "*", ["1.0", "-", "discount#3"]]]], "#", "103"], "AS", "c#203"],
+           [[["sum", [[["price#2", "*", ["1.0", "-", "discount#3"]], "*", ["1.0", "+", "tax#4"]]]], "#", "104"],
+            "AS", "d#204"],
+           [[["avg", ["quantity#1"]], "#", "105"], "AS", "e#205"],
+           [[["avg", ["price#2"]], "#", "106"], "AS", "f#206"],
+           [[["avg", ["discount#3"]], "#", "107"], "AS", "g#207"],
+           [[["count", ["1"]], "#", "108L"], "AS", "h#208"]]
+    AGG_IDS = [201, 202, 203, 204, 205, 206, 207, 208]
+
+    def __init__(self, n_instances=64):
+        from tqpk import datagen
+        self.dg = datagen
+        self.specs = datagen.batch_specs(n_instances, seed=3)
+        self.fact_rows = sum(s["rows"] for s in self.specs)
+        self.config = {"workload": "64 uneven instances: filter+group-by and join+aggregate+top-10, one persistent "
+                                   "launch (CUDA graph) vs per-instance drop-in operators",
+                       "instances": n_instances, "total_rows": self.fact_rows,
+                       "rows_range": [10_000, 10_000_000], "group_range": [4, 1_000_000]}
+
+    def setup_device(self, dev):
+        import torch
+        from tqpk.batch import Autotuner, Batch, GroupByInstance, JoinInstance
+        self.dev = dev
+        self.insts, self.plain_args = [], []
+        for sp in self.specs:
+            if sp["kind"] == "groupby":
+                t, (a, b) = self.dg.groupby_instance_tables(sp["rows"], sp["groups"], sp["seed"])
+                ids = {"quantity": 1, "price": 2, "discount": 3, "tax": 4, "flag": 5, "status": 6, "ship_date": 7}
+                d = {ids[k]: torch.from_numpy(v).to(dev) for k, v in t.items()}
+                args = {"is partial": False, "keys": ["flag#5", "status#6"], "input ids": [1, 2, 3, 4, 5, 6],
+                        "results": self.AGG, "out agg ids": self.AGG_IDS}
+                self.insts.append(GroupByInstance(args=args, columns={c: d[c] for c in range(1, 7)},
+                                                  filter_tree=[["ship_date#7", "<=", "2470"]], filter_cols={7: d[7]},
+                                                  key_domains=[(0, a - 1), (0, b - 1)]))
+                self.plain_args.append(("groupby", d))
+            else:
+                t = self.dg.join_tables(sp["groups"], sp["rows"], sp["seed"])
+                d = {k: torch.from_numpy(v).to(dev) for k, v in t.items()}
+                self.insts.append(JoinInstance(d["b_key"], (1, sp["groups"]), d["p_fk"], {12: d["b_date"]},
+                                               [["bd#12", "<", "1170"]],
+                                               {22: d["p_date"], 23: d["p_price"], 24: d["p_discount"]},
+                                               [["pd#22", ">", "1170"]], [["p#23", "*", ["1.0", "-", "d#24"]]], k=10))
+                self.plain_args.append(("join", d))
+        self.batch = Batch(self.insts, Autotuner())
+        self.batch.capture()
+
+    def run_batched(self):
+        self.batch.replay()
+
+    def run_plain(self):
+        """Every instance alone through the drop-in operators (the reference's per-operator path)."""
+        import torch
+        from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
+        from tqpk.variable import Variable
+        out = []
+        for kind, d in self.plain_args:
+            if kind == "groupby":
+                tg = {c: Variable(d[c], "float" if c <= 4 else ("date" if c == 7 else "int")) for c in d}
+                tqp_filter(True, tg, {"filter tree": [["ship_date#7", "<=", "2470"]], "materialized in": [7],
+                                      "out mask id": 900}, None, None, None, "f")
+                tqp_hash_aggregate(True, tg, {"is partial": False, "keys": ["flag#5", "status#6"],
+                                              "input ids": [1, 2, 3, 4, 5, 6], "results": self.AGG,
+                                              "out agg ids": self.AGG_IDS,
+                                              "mask map": {c: 900 for c in range(1, 7)}}, None, None, "a")
+                out.append(({o: tg[o].tensor for o in self.AGG_IDS}, [tg[5].tensor, tg[6].tensor]))
+            else:
+                tg = {11: Variable(d["b_key"], "int"), 12: Variable(d["b_date"], "date"),
+                      21: Variable(d["p_fk"], "int"), 22: Variable(d["p_date"], "date"),
+                      23: Variable(d["p_price"], "float"), 24: Variable(d["p_discount"], "float")}
+                tqp_filter(True, tg, {"filter tree": [["bd#12", "<", "1170"]], "materialized in": [12],
+                                      "out mask id": 901}, None, None, None, "f")
+                tqp_filter(True, tg, {"filter tree": [["pd#22", ">", "1170"]], "materialized in": [22],
+                                      "out mask id": 902}, None, None, None, "f")
+                join_vortex(True, tg, {"left group": [11, 12], "right group": [21, 22, 23, 24],
+                                       "materialized in": [11, 21, 23, 24],
+                                       "mask map": {11: 901, 21: 902, 23: 902, 24: 902}}, 11, 21, [], "inner",
+                            None, None, "j")
+                tqp_hash_aggregate(True, tg, {"is partial": False, "keys": ["k#11"], "input ids": [11, 23, 24],
+                                              "results": ["k#11", [[["sum", [["p#23", "*", ["1.0", "-", "d#24"]]]],
+                                                                    "#", "1"], "AS", "r#302"]],
+                                              "out agg ids": [302]}, None, None, "a")
+                tqp_sort(True, tg, {"limit": 10, "input ids": [11, 302], "key ids": [302], "key orders": [True]},
+                         True, "t")
+                out.append((tg[11].tensor, tg[302].tensor))
+        torch.cuda.synchronize()
+        return out
+
+    def compare(self, plain, batched):
+        for (kind, _), p, b in zip(self.plain_args, plain, batched):
+            if kind == "join":
+                assert np.array_equal(p[0].cpu().numpy().reshape(-1), b[0])
+                pv = p[1].cpu().numpy()
+                assert np.all(np.abs(pv - b[1]) <= 1e-12 * np.abs(pv))
+            else:
+                outs, keys, g = b
+                assert np.array_equal(p[1][0].cpu().numpy().reshape(-1), keys[0])
+                assert np.array_equal(p[1][1].cpu().numpy().reshape(-1), keys[1])
+                for o in self.AGG_IDS:
+                    pv = p[0][o].cpu().numpy()
+                    if pv.dtype == np.float64:
+                        assert np.all(np.abs(pv - outs[o]) <= 1e-12 * np.abs(pv)), o
+                    else:
+                        assert np.array_equal(pv, outs[o]), o
+
+
+def run_batched_bench(args):
+    import torch
+    from tqpk import _lib as L
+    import __graft_entry__ as G
+    G.build()
+    lib = L.load()
+    dev = torch.device("cuda", 0)
+    w = Batched()
+    w.setup_device(dev)
+    w.run_batched()
+    torch.cuda.synchronize()
+    batched_res = w.batch.results()
+    plain_res = w.run_plain()
+    w.compare(plain_res, batched_res)
+    for _ in range(args.warmup):
+        w.run_batched()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    L.check(lib.tqpk_timing_begin(L.KID_BATCH), "tqpk_timing_begin")
+    launches0 = lib.tqpk_launch_count()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for s, e in evs:
+        s.record()
+        w.run_batched()
+        e.record()
+    torch.cuda.synchronize()
+    launches = lib.tqpk_launch_count() - launches0
+    import ctypes as C
+    kms, kn = C.c_double(0), C.c_int32(0)
+    L.check(lib.tqpk_timing_end(C.byref(kms), C.byref(kn)), "tqpk_timing_end")
+    batched_ms = statistics.median([s.elapsed_time(e) for s, e in evs])
+    clocks = sampler.stop()
+    plain_times = []
+    for _ in range(max(2, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        w.run_plain()
+        plain_times.append(time.perf_counter() - t0)
+    plain_s = statistics.median(plain_times)
+    n = len(w.specs)
+    line = {"metric": "queries/s", "value": n / (batched_ms / 1000.0), "unit": "queries/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": dict(w.config, plain_queries_per_s=n / plain_s, speedup_vs_plain=(n / (batched_ms / 1000.0)) /
+                           (n / plain_s), batched_rows_per_s=w.fact_rows / (batched_ms / 1000.0),
+                           kernel_ms=kms.value / max(kn.value, 1)),
+            "clocks": clocks, "gpu_launches": launches}
+    print(json.dumps(line))
+
+
 WORKLOADS = {c.name: c for c in (JoinAggTop10, FilterGroupBy, StarJoin)}
 
 
@@ -584,11 +748,17 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="join_agg_top10")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batched"], default="join_agg_top10")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world = dist_setup(args.gpus)
+    if args.workload == "batched":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the batched form has no reference counterpart"}))
+        elif rank == 0:
+            run_batched_bench(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:

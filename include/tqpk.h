@@ -300,6 +300,42 @@ int tqpk_pipeline_star_agg_topk(const void* d_f_fka, int32_t f_fka_dtype, const 
                                 int64_t c_min, int64_t c_max, int32_t k, int32_t descending, void* d_ws,
                                 size_t ws_bytes, int64_t* d_out_keys, double* d_out_vals, int64_t* d_out_counts,
                                 int64_t* d_out_count, int64_t* d_groups_out, tqpk_stream stream);
+/* ---- batched instances (one persistent launch) -----------------------------
+ * Many independent JOIN-shaped (as tqpk_pipeline_join_agg_topk, k <= 32) and
+ * GROUPBY-shaped (filter + dense group-by + ordered emit) instances run as
+ * phase-major work items of one persistent kernel fed by an atomic ticket.
+ * Each instance is described into an opaque host record of
+ * tqpk_batch_record_bytes() bytes (the records are then copied to the device
+ * by the caller); rows_per_item / slots_per_item size its work items.  An item
+ * of phase p waits (bounded) for the instance's phase p-1 items.  Reset +
+ * run only enqueue memsets and kernels on the stream (capturable in a CUDA
+ * graph).  Group-by keys use caller-provided domains (table statistics).  */
+size_t tqpk_batch_record_bytes(void);
+size_t tqpk_batch_join_workspace_bytes(int64_t key_min, int64_t key_max);
+int tqpk_batch_describe_join(void* h_rec, const void* d_build_keys, int32_t build_dtype, int64_t nb,
+                             const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max,
+                             const void* d_probe_fk, int32_t probe_dtype, int64_t np,
+                             const tqpk_predicate* h_probe_pred, const tqpk_groupby_spec* h_values,
+                             int32_t value_reg, int32_t k, int32_t descending, void* d_ws, size_t ws_bytes,
+                             int64_t* d_out_keys, double* d_out_vals, int64_t* d_out_count,
+                             int64_t* d_groups_out, int64_t build_rows_per_item, int64_t probe_rows_per_item);
+size_t tqpk_batch_groupby_workspace_bytes(const tqpk_groupby_spec* h_spec, const int64_t* key_min,
+                                          const int64_t* key_max, int64_t slots_per_item);
+int tqpk_batch_describe_groupby(void* h_rec, const tqpk_groupby_spec* h_spec, const tqpk_predicate* h_pred,
+                                int64_t n, const int64_t* key_min, const int64_t* key_max, void* d_ws,
+                                size_t ws_bytes, void* const* h_out_keys, int32_t n_out, const int32_t* h_out_ops,
+                                void* const* h_out_cols, int64_t* d_groups_out, int64_t rows_per_item,
+                                int64_t slots_per_item, int32_t prefer_private);
+/* Writes the phase-major work items (24 bytes each) of n_inst host records;
+ * returns the item count (the required count when it exceeds cap).        */
+int64_t tqpk_batch_items(const void* h_recs, int32_t n_inst, void* h_items, int64_t cap);
+size_t tqpk_batch_ctl_bytes(int32_t n_inst);
+int tqpk_batch_reset(const void* h_recs, const void* d_recs, int32_t n_inst, void* d_ctl, tqpk_stream stream);
+int tqpk_batch_run(const void* d_recs, int32_t n_inst, const void* d_items, int32_t n_items, void* d_ctl,
+                   int32_t grid, tqpk_stream stream);
+int tqpk_batch_error(const void* d_ctl, int* h_err, tqpk_stream stream);
+int32_t tqpk_batch_grid(void);
+
 /* Reads (synchronising) the error word a fused pipeline left in its workspace. */
 int tqpk_pipeline_error(const void* d_ws, int* h_err, tqpk_stream stream);
 

@@ -323,9 +323,9 @@ def eval_agg_expr(tree, cols: Dict[int, np.ndarray]):
 def group_rows(key_cols: Sequence[np.ndarray]) -> Tuple[List[np.ndarray], np.ndarray]:
     """Group ids of key tuples (aggregate.py:298-333), ordered by key tuple."""
     n = key_cols[0].shape[0]
-    flat = [k.reshape(n, -1) for k in key_cols]
     if n == 0:
-        return [k.reshape(0, -1)[:0] for k in key_cols], np.zeros(0, np.int64)
+        return [k.reshape(0, k.shape[1] if k.ndim == 2 else 1) for k in key_cols], np.zeros(0, np.int64)
+    flat = [k.reshape(n, -1) for k in key_cols]
     order = np.lexsort([f[:, j] for f in reversed(flat) for j in reversed(range(f.shape[1]))])
     stacked = [f[order] for f in flat]
     change = np.zeros(n, dtype=bool)
@@ -383,7 +383,7 @@ def reduce_groups(fn: str, v, inverse: np.ndarray, G: int, n: int) -> np.ndarray
     if fn == "count":                                               # :184-185
         v = (v != NULL).astype(np.int64)
         is_int = True
-    s = np.bincount(inverse, weights=v.astype(np.float64), minlength=G)   # :187-190
+    s = np.bincount(inverse, weights=v.astype(np.float64), minlength=G).astype(np.float64)   # :187-190
     if is_int:                                                      # :192-193
         return np.round(s).astype(np.int64)
     return s
@@ -449,7 +449,8 @@ def tqp_hash_aggregate(cols: Dict[int, np.ndarray], args: dict):
         oid = get_id(_right_most(tree))
         if _is_key(tree):
             kid = get_id(tree if isinstance(tree, str) else tree[0])
-            out[oid] = ukeys[key_ids.index(kid)].reshape(G, -1).astype(m[kid].dtype)
+            uk = ukeys[key_ids.index(kid)]
+            out[oid] = uk.reshape(G, uk.shape[1] if uk.ndim == 2 else 1).astype(m[kid].dtype)
         else:
             fn, arg = _agg_fn_and_arg(tree)
             out[oid] = reduce_groups(fn, eval_agg_expr(arg, m), inverse, G, n)

@@ -195,6 +195,10 @@ __device__ __forceinline__ void ld4_f64(const void* p, int64_t r0, int64_t n, bo
 // Programs of up to NR instructions run fully unrolled with operands picked
 // by compile-time selects, so the register file stays in registers; longer
 // programs use the generic loop (a small local-memory array).
+static __device__ __noinline__ uint64_t expr_div(uint64_t a, uint64_t b) {
+  return static_cast<uint64_t>(__double_as_longlong(__ddiv_rn(__longlong_as_double(a), __longlong_as_double(b))));
+}
+
 __device__ __forceinline__ uint64_t expr_apply(const tqpk_expr_insn& X, uint64_t a, uint64_t b, const void* const* cols,
                                               const int* dts, int64_t row) {
   const bool f = X.type == TQPK_F64;
@@ -214,8 +218,7 @@ __device__ __forceinline__ uint64_t expr_apply(const tqpk_expr_insn& X, uint64_t
     case TQPK_X_MUL:
       return f ? static_cast<uint64_t>(__double_as_longlong(__dmul_rn(__longlong_as_double(a), __longlong_as_double(b))))
                : static_cast<uint64_t>(static_cast<int64_t>(a) * static_cast<int64_t>(b));
-    case TQPK_X_DIV:
-      return static_cast<uint64_t>(__double_as_longlong(__ddiv_rn(__longlong_as_double(a), __longlong_as_double(b))));
+    case TQPK_X_DIV: return expr_div(a, b);
   }
   return 0;
 }
@@ -256,14 +259,75 @@ __device__ __forceinline__ void expr_eval_generic(const tqpk_expr_insn* E, int n
   }
 }
 
+// Column preloading for 4-row groups: the first kPreCols columns of a program
+// are loaded with 128-bit loads for four rows at once (all loads issued
+// before any use), and X_COL instructions read them from registers.
+constexpr int kPreCols = 4;
+
+struct ColTile4 {
+  uint64_t v[kPreCols][4];
+};
+
+__device__ __forceinline__ void load_cols4(const tqpk_groupby_spec& S, int64_t r0, int64_t n, bool vec, ColTile4& T) {
+#pragma unroll
+  for (int c = 0; c < kPreCols; ++c) {
+    if (c < S.n_cols) {
+      if (S.col_dtypes[c] == TQPK_F64) {
+        double x[4];
+        ld4_f64(S.cols[c], r0, n, vec, x);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) T.v[c][j] = static_cast<uint64_t>(__double_as_longlong(x[j]));
+      } else {
+        int64_t x[4];
+        ld4_int(S.cols[c], S.col_dtypes[c], r0, n, vec, x);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) T.v[c][j] = static_cast<uint64_t>(x[j]);
+      }
+    }
+  }
+}
+
+// Evaluates registers 0..n-1 for row j of a preloaded tile (n <= NR; every
+// X_COL must name a preloaded column).
+template <int NR>
+__device__ __forceinline__ void expr_eval_tile(const tqpk_expr_insn* E, int n, const int* dts, const ColTile4& T, int j,
+                                               uint64_t (&r)[NR]) {
+#pragma unroll
+  for (int i = 0; i < NR; ++i) {
+    r[i] = 0;
+    if (i < n) {
+      const tqpk_expr_insn& X = E[i];
+      if (X.op == TQPK_X_COL) {
+        uint64_t raw = 0;
+#pragma unroll
+        for (int cc = 0; cc < kPreCols; ++cc) raw = (X.col == cc) ? T.v[cc][j] : raw;
+        if (X.type == TQPK_F64 && dts[X.col] != TQPK_F64)
+          raw = static_cast<uint64_t>(__double_as_longlong(static_cast<double>(static_cast<int64_t>(raw))));
+        r[i] = raw;
+      } else {
+        uint64_t a = 0, b = 0;
+#pragma unroll
+        for (int q = 0; q < i; ++q) {
+          a = (X.a == q) ? r[q] : a;
+          b = (X.b == q) ? r[q] : b;
+        }
+        r[i] = expr_apply(X, a, b, nullptr, dts, 0);
+      }
+    }
+  }
+}
+
+// True when the program's columns are all preloadable (and it fits NR=16 registers).
+__device__ __forceinline__ bool tile_ok(const tqpk_groupby_spec& S) { return S.n_cols <= kPreCols && S.n_expr <= 16; }
+
 // Value of register `out` for one row as a double (integers converted).
 __device__ __forceinline__ double expr_value(const tqpk_groupby_spec& S, int64_t row, int out) {
   const bool f = S.expr[out].type == TQPK_F64;
   uint64_t v;
-  if (out < 8) {
-    uint64_t r[8];
-    expr_eval_small<8>(S.expr, out + 1, S.cols, S.col_dtypes, row, r);
-    v = reg_pick<8>(r, out);
+  if (out < 16) {
+    uint64_t r[16];
+    expr_eval_small<16>(S.expr, out + 1, S.cols, S.col_dtypes, row, r);
+    v = reg_pick<16>(r, out);
   } else {
     uint64_t r[TQPK_MAX_EXPR];
     expr_eval_generic(S.expr, out + 1, S.cols, S.col_dtypes, row, r);
@@ -540,6 +604,22 @@ size_t compact_status_bytes(int64_t n);
 int compact_launch(const tqpk_predicate* pred, const uint8_t* mask, int64_t n, const ColSet& C, int64_t* d_count,
                    void* ws, size_t ws_bytes, cudaStream_t s);
 size_t sort_ws_bytes(int64_t n);
+bool spec_cols_vec(const tqpk_groupby_spec* S);   // all spec columns 16-byte aligned
+
+// Grid of one full wave: resident CTAs per SM (occupancy API) x SMs, capped by
+// the work (one thread per work unit).
+template <class K>
+inline int occ_grid(K kernel, int64_t work_units, size_t smem = 0) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, smem) != cudaSuccess || per_sm < 1) {
+    (void)cudaGetLastError();
+    per_sm = 2;
+  }
+  int64_t g = (work_units + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)per_sm * num_sms();
+  if (g > cap) g = cap;
+  return (int)(g < 1 ? 1 : g);
+}
 int sort_pairs(const void* keys, int dt, int desc, const int64_t* perm_in, int64_t n, void* ws, size_t ws_bytes,
                cudaStream_t s, const int64_t** result);
 

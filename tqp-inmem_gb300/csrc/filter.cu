@@ -221,6 +221,13 @@ int check_pred(const tqpk_predicate* p) {
   return (p->n_insn == 0 || depth == 1) ? TQPK_OK : TQPK_EINVAL;
 }
 
+bool spec_cols_vec(const tqpk_groupby_spec* S) {
+  if (!S) return true;
+  for (int c = 0; c < S->n_cols; ++c)
+    if (!aligned16(S->cols[c])) return false;
+  return true;
+}
+
 RowFilter make_filter(const tqpk_predicate* pred, const uint8_t* mask) {
   RowFilter F;
   F.mask = mask;

@@ -126,7 +126,7 @@ template <int MODE>
 __global__ void __launch_bounds__(256) k_groupby_dense(const __grid_constant__ tqpk_groupby_spec S,
                                                        const __grid_constant__ tqpk_predicate P, RowFilter F,
                                                        int64_t n, GbDev G, uint64_t* __restrict__ gacc,
-                                                       int keys_vec) {
+                                                       int keys_vec, int cols_vec) {
   extern __shared__ uint64_t sm[];
   const int A = S.n_accs;
   const int T = blockDim.x;
@@ -138,7 +138,8 @@ __global__ void __launch_bounds__(256) k_groupby_dense(const __grid_constant__ t
   }
   __syncthreads();
   const int64_t groups = (n + 3) >> 2;
-  const bool small = S.n_expr <= 8;
+  const bool small = S.n_expr <= 16;
+  const bool tile = tile_ok(S);
   for (int64_t g = blockIdx.x * (int64_t)T + threadIdx.x; g < groups; g += (int64_t)gridDim.x * T) {
     const int64_t r0 = g << 2;
     const uint32_t b = filter4(F, P, r0, n);
@@ -150,13 +151,25 @@ __global__ void __launch_bounds__(256) k_groupby_dense(const __grid_constant__ t
 #pragma unroll
       for (int j = 0; j < 4; ++j) slot[j] += (x[j] - G.kmin[k]) * G.kstride[k];
     }
+    if (tile) {
+      ColTile4 T;
+      load_cols4(S, r0, n, cols_vec, T);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (!((b >> j) & 1u)) continue;
+        uint64_t r[16];
+        expr_eval_tile<16>(S.expr, S.n_expr, S.col_dtypes, T, j, r);
+        for (int a = 0; a < A; ++a) acc_row<MODE>(S, sm, gacc, K, slot[j], a, reg_pick<16>(r, S.accs[a].reg));
+      }
+      continue;
+    }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       if (!((b >> j) & 1u)) continue;
       if (small) {
-        uint64_t r[8];
-        expr_eval_small<8>(S.expr, S.n_expr, S.cols, S.col_dtypes, r0 + j, r);
-        for (int a = 0; a < A; ++a) acc_row<MODE>(S, sm, gacc, K, slot[j], a, reg_pick<8>(r, S.accs[a].reg));
+        uint64_t r[16];
+        expr_eval_small<16>(S.expr, S.n_expr, S.cols, S.col_dtypes, r0 + j, r);
+        for (int a = 0; a < A; ++a) acc_row<MODE>(S, sm, gacc, K, slot[j], a, reg_pick<16>(r, S.accs[a].reg));
       } else {
         uint64_t r[TQPK_MAX_EXPR];
         expr_eval_generic(S.expr, S.n_expr, S.cols, S.col_dtypes, r0 + j, r);
@@ -401,7 +414,7 @@ extern "C" int tqpk_groupby_run(const tqpk_groupby_spec* S, const tqpk_gb_plan* 
                                      (int)smem));
       int g = (int)std::min<int64_t>((groups4 + T - 1) / T, (int64_t)num_sms() * 2);
       timing_before(KID_GROUPBY, s);
-      k_groupby_dense<MODE_PRIVATE><<<std::max(g, 1), T, smem, s>>>(*S, P, F, n, G, gacc, kvec);
+      k_groupby_dense<MODE_PRIVATE><<<std::max(g, 1), T, smem, s>>>(*S, P, F, n, G, gacc, kvec, spec_cols_vec(S) ? 1 : 0);
       timing_after(KID_GROUPBY, s);
     } else if (plan->mode == TQPK_GB_DENSE_SHARED) {
       const size_t smem = (size_t)(K * A * 8);
@@ -409,12 +422,12 @@ extern "C" int tqpk_groupby_run(const tqpk_groupby_spec* S, const tqpk_gb_plan* 
                                      (int)smem));
       int g = (int)std::min<int64_t>((groups4 + 255) / 256, (int64_t)num_sms() * 2);
       timing_before(KID_GROUPBY, s);
-      k_groupby_dense<MODE_SHARED><<<std::max(g, 1), 256, smem, s>>>(*S, P, F, n, G, gacc, kvec);
+      k_groupby_dense<MODE_SHARED><<<std::max(g, 1), 256, smem, s>>>(*S, P, F, n, G, gacc, kvec, spec_cols_vec(S) ? 1 : 0);
       timing_after(KID_GROUPBY, s);
     } else {
       int g = grid_for(groups4, 8);
       timing_before(KID_GROUPBY, s);
-      k_groupby_dense<MODE_GLOBAL><<<g, 256, 0, s>>>(*S, P, F, n, G, gacc, kvec);
+      k_groupby_dense<MODE_GLOBAL><<<g, 256, 0, s>>>(*S, P, F, n, G, gacc, kvec, spec_cols_vec(S) ? 1 : 0);
       timing_after(KID_GROUPBY, s);
     }
     TQPK_CHECK_LAUNCH();

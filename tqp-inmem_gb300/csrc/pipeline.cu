@@ -41,6 +41,7 @@ struct PipeJoinArgs {
   int desc;
   int b_pvec;  // build predicate columns are 16-byte aligned
   int p_pvec;  // probe predicate columns are 16-byte aligned
+  int v_pvec;  // value columns are 16-byte aligned
 };
 
 __global__ void __launch_bounds__(kBlock) k_pl_build(const __grid_constant__ tqpk_predicate P, PipeJoinArgs A,
@@ -70,23 +71,58 @@ __global__ void __launch_bounds__(kBlock) k_pl_probe_agg(const __grid_constant__
                                                          const int* __restrict__ dir, double* __restrict__ sum,
                                                          unsigned* __restrict__ cnt,
                                                          unsigned long long* __restrict__ groups) {
-  const int64_t ngroups4 = (A.np + 3) >> 2;
+  // Two 4-row groups per thread per iteration: every load of the 8 rows
+  // (filter column, fk, directory, value columns) is issued before the
+  // atomics, so each thread keeps several independent misses in flight.
+  constexpr int U = 2;
+  const int64_t n8 = (A.np + 4 * U - 1) / (4 * U);
   const bool vec = ((reinterpret_cast<uintptr_t>(A.p_fk) & 15u) == 0);
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ngroups4;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r0 = g << 2;
-    uint32_t b = P.n_insn ? eval_pred4(P, r0, A.np, A.p_pvec != 0) : (A.np - r0 >= 4 ? 0xfu : ((1u << (A.np - r0)) - 1));
-    if (!b) continue;
-    int64_t x[4];
-    ld4_int(A.p_fk, A.p_dt, r0, A.np, vec, x);
+  const bool tile = tile_ok(S);
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n8; g += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t m[U];
+    int64_t x[U][4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (!((b >> j) & 1u)) continue;
-      const int64_t slot = x[j] - A.key_min;
-      if (slot < 0 || slot >= A.slots) continue;
-      if (__ldg(&dir[slot]) < 0) continue;
-      atomicAdd(&sum[slot], expr_value(S, r0 + j, A.val_reg));
-      cnt[slot] = 1u;  // occupancy (the top-k pass counts the groups)
+    for (int u = 0; u < U; ++u) {
+      const int64_t r0 = (g * U + u) << 2;
+      m[u] = P.n_insn ? eval_pred4(P, r0, A.np, A.p_pvec != 0)
+                      : (A.np - r0 >= 4 ? 0xfu : (A.np - r0 <= 0 ? 0u : ((1u << (A.np - r0)) - 1)));
+      if (m[u]) ld4_int(A.p_fk, A.p_dt, r0, A.np, vec, x[u]);
+    }
+    int64_t slot[U][4];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        slot[u][j] = x[u][j] - A.key_min;
+        const bool ok = ((m[u] >> j) & 1u) && slot[u][j] >= 0 && slot[u][j] < A.slots;
+        if (!ok || __ldg(&dir[slot[u][j]]) < 0) m[u] &= ~(1u << j);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!m[u]) continue;
+      const int64_t r0 = (g * U + u) << 2;
+      double v[4];
+      if (tile) {
+        ColTile4 T;
+        load_cols4(S, r0, A.np, A.v_pvec != 0, T);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          uint64_t r[16];
+          expr_eval_tile<16>(S.expr, A.val_reg + 1, S.col_dtypes, T, j, r);
+          const uint64_t raw = reg_pick<16>(r, A.val_reg);
+          v[j] = S.expr[A.val_reg].type == TQPK_F64 ? u2d(raw) : (double)(int64_t)raw;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = ((m[u] >> j) & 1u) ? expr_value(S, r0 + j, A.val_reg) : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (!((m[u] >> j) & 1u)) continue;
+        atomicAdd(&sum[slot[u][j]], v[j]);
+        cnt[slot[u][j]] = 1u;  // occupancy (the top-k pass counts the groups)
+      }
     }
   }
 }
@@ -165,8 +201,9 @@ extern "C" int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t bui
   if (!is_int_dtype(build_dtype) || !is_int_dtype(probe_dtype)) return TQPK_EDTYPE;
   if (key_max < key_min || key_max - key_min + 1 > (int64_t(1) << 31)) return TQPK_EUNSUPPORTED;
   if (value_reg < 0 || value_reg >= h_values->n_expr) return TQPK_EINVAL;
-  int rc = check_pred(h_build_pred);
-  if (!rc) rc = check_pred(h_probe_pred);
+  // a side with no rows never evaluates its predicate (its columns may be empty, null tensors)
+  int rc = nb > 0 ? check_pred(h_build_pred) : TQPK_OK;
+  if (!rc && np > 0) rc = check_pred(h_probe_pred);
   if (rc) return rc;
   const int64_t slots = key_max - key_min + 1;
   const int grid = topk_grid();
@@ -188,6 +225,7 @@ extern "C" int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t bui
   A.desc = descending ? 1 : 0;
   A.b_pvec = pred_vec_ok(h_build_pred) ? 1 : 0;
   A.p_pvec = pred_vec_ok(h_probe_pred) ? 1 : 0;
+  A.v_pvec = spec_cols_vec(h_values) ? 1 : 0;
   TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 32, s));
   TQPK_CUDA(cudaMemsetAsync(L.dir, 0xff, slots * 4, s));
   TQPK_CUDA(cudaMemsetAsync(L.sum, 0, slots * 8, s));
@@ -200,8 +238,8 @@ extern "C" int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t bui
   }
   if (np > 0) {
     timing_before(KID_PIPE_PROBE, s);
-    k_pl_probe_agg<<<grid_for((np + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_probe_pred), *h_values, A, L.dir,
-                                                               L.sum, L.cnt, L.groups);
+    k_pl_probe_agg<<<occ_grid(k_pl_probe_agg, (np + 7) / 8), kBlock, 0, s>>>(*pred_or_empty(h_probe_pred), *h_values,
+                                                                           A, L.dir, L.sum, L.cnt, L.groups);
     timing_after(KID_PIPE_PROBE, s);
     TQPK_CHECK_LAUNCH();
   }

@@ -31,7 +31,7 @@ struct StarArgs {
   const void* b_key; int b_dt; const void* b_fkc; int b_fkc_dt; int64_t nb; int64_t b_min, b_slots;
   const void* c_key; int c_dt; int64_t nc; int64_t c_min, c_slots;
   int val_reg;
-  int a_pvec, f_pvec;
+  int a_pvec, f_pvec, v_pvec;
 };
 
 // Dimension builds: mode 0 = A (predicate -> 1), 1 = B (payload fkc), 2 = C (existence).
@@ -70,35 +70,77 @@ __global__ void __launch_bounds__(kBlock) k_star_probe(const __grid_constant__ t
                                                        const int* __restrict__ dir_c, double* __restrict__ sum,
                                                        unsigned* __restrict__ cnt,
                                                        unsigned long long* __restrict__ groups) {
-  const int64_t g4 = (A.nf + 3) >> 2;
+  // Two 4-row groups per thread per iteration; each hop (A, B, C) issues the
+  // lookups of all surviving rows before the next hop uses them.
+  constexpr int U = 2;
+  const int64_t n8 = (A.nf + 4 * U - 1) / (4 * U);
   const bool va = ((reinterpret_cast<uintptr_t>(A.f_fka) & 15u) == 0);
   const bool vb = ((reinterpret_cast<uintptr_t>(A.f_fkb) & 15u) == 0);
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < g4; g += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r0 = g << 2;
-    uint32_t b = P.n_insn ? eval_pred4(P, r0, A.nf, A.f_pvec) : (A.nf - r0 >= 4 ? 0xfu : ((1u << (A.nf - r0)) - 1));
-    if (!b) continue;
-    int64_t fa[4];
-    ld4_int(A.f_fka, A.f_fka_dt, r0, A.nf, va, fa);
+  const bool tile = tile_ok(S);
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n8; g += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t m[U];
+    int64_t k[U][4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (!((b >> j) & 1u)) continue;
-      const int64_t sa = fa[j] - A.a_min;
-      if (sa < 0 || sa >= A.a_slots || __ldg(&dir_a[sa]) <= 0) b &= ~(1u << j);
+    for (int u = 0; u < U; ++u) {
+      const int64_t r0 = (g * U + u) << 2;
+      m[u] = P.n_insn ? eval_pred4(P, r0, A.nf, A.f_pvec)
+                      : (A.nf - r0 >= 4 ? 0xfu : (A.nf - r0 <= 0 ? 0u : ((1u << (A.nf - r0)) - 1)));
+      if (m[u]) ld4_int(A.f_fka, A.f_fka_dt, r0, A.nf, va, k[u]);
     }
-    if (!b) continue;
-    int64_t fb[4];
-    ld4_int(A.f_fkb, A.f_fkb_dt, r0, A.nf, vb, fb);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (!((b >> j) & 1u)) continue;
-      const int64_t sb = fb[j] - A.b_min;
-      if (sb < 0 || sb >= A.b_slots) continue;
-      const int fkc = __ldg(&dir_b[sb]);
-      if (fkc == INT32_MIN) continue;
-      const int64_t sc = (int64_t)fkc - A.c_min;
-      if (sc < 0 || sc >= A.c_slots || __ldg(&dir_c[sc]) == INT32_MIN) continue;
-      atomicAdd(&sum[sc], expr_value(S, r0 + j, A.val_reg));
-      atomicAdd(&cnt[sc], 1u);
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t sa = k[u][j] - A.a_min;
+        const bool ok = ((m[u] >> j) & 1u) && sa >= 0 && sa < A.a_slots;
+        if (!ok || __ldg(&dir_a[sa]) <= 0) m[u] &= ~(1u << j);
+      }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (m[u]) ld4_int(A.f_fkb, A.f_fkb_dt, (g * U + u) << 2, A.nf, vb, k[u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t sb = k[u][j] - A.b_min;
+        const bool ok = ((m[u] >> j) & 1u) && sb >= 0 && sb < A.b_slots;
+        const int fkc = ok ? __ldg(&dir_b[sb]) : INT32_MIN;
+        if (fkc == INT32_MIN) m[u] &= ~(1u << j);
+        k[u][j] = (int64_t)fkc - A.c_min;
+      }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t sc = k[u][j];
+        const bool ok = ((m[u] >> j) & 1u) && sc >= 0 && sc < A.c_slots;
+        if (!ok || __ldg(&dir_c[sc]) == INT32_MIN) m[u] &= ~(1u << j);
+      }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (!m[u]) continue;
+      const int64_t r0 = (g * U + u) << 2;
+      double v[4];
+      if (tile) {
+        ColTile4 T;
+        load_cols4(S, r0, A.nf, A.v_pvec != 0, T);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          uint64_t r[16];
+          expr_eval_tile<16>(S.expr, A.val_reg + 1, S.col_dtypes, T, j, r);
+          const uint64_t raw = reg_pick<16>(r, A.val_reg);
+          v[j] = S.expr[A.val_reg].type == TQPK_F64 ? u2d(raw) : (double)(int64_t)raw;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = ((m[u] >> j) & 1u) ? expr_value(S, r0 + j, A.val_reg) : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (!((m[u] >> j) & 1u)) continue;
+        atomicAdd(&sum[k[u][j]], v[j]);
+        atomicAdd(&cnt[k[u][j]], 1u);
+      }
     }
   }
 }
@@ -189,8 +231,8 @@ extern "C" int tqpk_pipeline_star_agg_topk(
   const int64_t as = a_max - a_min + 1, bs = b_max - b_min + 1, cs = c_max - c_min + 1;
   if (as > (int64_t(1) << 31) || bs > (int64_t(1) << 31) || cs > (int64_t(1) << 31)) return TQPK_EUNSUPPORTED;
   if (value_reg < 0 || value_reg >= h_values->n_expr) return TQPK_EINVAL;
-  int rc = check_pred(h_fact_pred);
-  if (!rc) rc = check_pred(h_a_pred);
+  int rc = nf > 0 ? check_pred(h_fact_pred) : TQPK_OK;   // empty sides never evaluate their predicate
+  if (!rc && na > 0) rc = check_pred(h_a_pred);
   if (rc) return rc;
   const int grid = topk_grid_size();
   if (ws_bytes < star_bytes(as, bs, cs, grid)) return TQPK_ENOMEM;
@@ -199,7 +241,8 @@ extern "C" int tqpk_pipeline_star_agg_topk(
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   StarArgs A{d_f_fka, f_fka_dtype, d_f_fkb, f_fkb_dtype, nf, d_a_key, a_dtype, na, a_min, as,
              d_b_key, b_dtype, d_b_fkc, b_fkc_dtype, nb, b_min, bs, d_c_key, c_dtype, nc, c_min, cs,
-             value_reg, pred_vec_ok(h_a_pred) ? 1 : 0, pred_vec_ok(h_fact_pred) ? 1 : 0};
+             value_reg, pred_vec_ok(h_a_pred) ? 1 : 0, pred_vec_ok(h_fact_pred) ? 1 : 0,
+             spec_cols_vec(h_values) ? 1 : 0};
   TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 64, s));
   k_fill_i32<<<grid_for(as, 4), kBlock, 0, s>>>(L.dir_a, as, INT32_MIN);
   TQPK_CHECK_LAUNCH();
@@ -227,8 +270,9 @@ extern "C" int tqpk_pipeline_star_agg_topk(
   }
   if (nf) {
     timing_before(KID_STAR_PROBE, s);
-    k_star_probe<<<grid_for((nf + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_fact_pred), *h_values, A, L.dir_a,
-                                                             L.dir_b, L.dir_c, L.sum, L.cnt, L.groups);
+    k_star_probe<<<occ_grid(k_star_probe, (nf + 7) / 8), kBlock, 0, s>>>(*pred_or_empty(h_fact_pred), *h_values, A,
+                                                                       L.dir_a, L.dir_b, L.dir_c, L.sum, L.cnt,
+                                                                       L.groups);
     timing_after(KID_STAR_PROBE, s);
     TQPK_CHECK_LAUNCH();
   }

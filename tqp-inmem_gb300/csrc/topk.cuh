@@ -90,8 +90,8 @@ struct DenseSumSource {
   int64_t n;
   int desc;
   __device__ __forceinline__ bool get(int64_t i, uint64_t& k) const {
-    if (i >= n || cnt[i] == 0) return false;
-    double v = sum[i];
+    if (i >= n || __ldcg(&cnt[i]) == 0) return false;   // L2 loads: the table may have been written
+    double v = __ldcg(&sum[i]);                          // earlier in the same launch by other CTAs
     if (v == 0.0) v = 0.0;
     uint64_t b = d2u(v);
     if (isnan(v)) b = 0x7ff8000000000000ull;
@@ -226,7 +226,8 @@ __global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
 int topk_warp_launch(int kind, const void* src, int k, int grid, TopkOut O, cudaStream_t s);
 inline int topk_grid_size() { return num_sms() * 2; }
 inline size_t topk_scratch_bytes(int k) {
-  return 2 * align_up((size_t)topk_grid_size() * k * 8, 256) + 512;
+  // ticket block + count + k indices + two [grid][k] candidate arrays, each 256-byte aligned
+  return 2 * align_up((size_t)topk_grid_size() * k * 8, 256) + align_up((size_t)k * 8, 256) + 1024;
 }
 
 }  // namespace tqpk

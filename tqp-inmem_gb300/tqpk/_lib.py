@@ -93,6 +93,20 @@ SIGNATURES = {
     "tqpk_join_probe": (C.c_int, [_P(JoinPlan), _VP, _VP, _I32, _VP, _I64, _I32, _VP, _VP, _I64, _P(_I64), _VP,
                                   _SZ, _VP]),
     "tqpk_gather": (C.c_int, [_I32, _P(_VP), _P(_I32), _VP, _I64, _I32, _P(_VP), _VP]),
+    "tqpk_batch_record_bytes": (_SZ, []),
+    "tqpk_batch_join_workspace_bytes": (_SZ, [_I64, _I64]),
+    "tqpk_batch_describe_join": (C.c_int, [_VP, _VP, _I32, _I64, _P(Predicate), _I64, _I64, _VP, _I32, _I64,
+                                           _P(Predicate), _P(GroupbySpec), _I32, _I32, _I32, _VP, _SZ, _VP, _VP,
+                                           _VP, _VP, _I64, _I64]),
+    "tqpk_batch_groupby_workspace_bytes": (_SZ, [_P(GroupbySpec), _P(_I64), _P(_I64), _I64]),
+    "tqpk_batch_describe_groupby": (C.c_int, [_VP, _P(GroupbySpec), _P(Predicate), _I64, _P(_I64), _P(_I64), _VP,
+                                              _SZ, _P(_VP), _I32, _P(_I32), _P(_VP), _VP, _I64, _I64, _I32]),
+    "tqpk_batch_items": (_I64, [_VP, _I32, _VP, _I64]),
+    "tqpk_batch_ctl_bytes": (_SZ, [_I32]),
+    "tqpk_batch_reset": (C.c_int, [_VP, _VP, _I32, _VP, _VP]),
+    "tqpk_batch_run": (C.c_int, [_VP, _I32, _VP, _I32, _VP, _I32, _VP]),
+    "tqpk_batch_error": (C.c_int, [_VP, _P(C.c_int), _VP]),
+    "tqpk_batch_grid": (_I32, []),
     "tqpk_timing_begin": (C.c_int, [_I32]),
     "tqpk_timing_end": (C.c_int, [_P(C.c_double), _P(_I32)]),
     "tqpk_pipeline_join_agg_topk_workspace_bytes": (_SZ, [_I64, _I64]),

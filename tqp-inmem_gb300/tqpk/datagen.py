@@ -66,3 +66,27 @@ SHIP_DATE_MAX = 2470      # lineitem: ship_date <= 2470 (~97% pass)
 BUILD_DATE_LT = 1170      # join build: date < 1170 (~45%)
 PROBE_DATE_GT = 1170      # join probe: date > 1170 (~54%)
 STAR_CATEGORY = 1         # star: dim A category == 1 (~20%)
+
+
+def batch_specs(n_instances: int = 64, seed: int = 0, rows=(10_000, 10_000_000), card=(4, 1_000_000)):
+    """Uneven instance shapes: half filter+group-by, half join+aggregate+top-10;
+    rows and group cardinality log-uniform over the given ranges."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_instances):
+        n = int(np.exp(rng.uniform(np.log(rows[0]), np.log(rows[1]))))
+        g = int(np.exp(rng.uniform(np.log(card[0]), np.log(card[1]))))
+        specs.append({"kind": "groupby" if i % 2 == 0 else "join", "rows": n, "groups": max(1, g), "seed": seed * 1000 + i})
+    return specs
+
+
+def groupby_instance_tables(rows: int, groups: int, seed: int):
+    """lineitem-like table whose (flag, status) key domain has about `groups` tuples."""
+    t = lineitem(rows, seed)
+    a = int(np.ceil(np.sqrt(groups)))
+    b = int(np.ceil(groups / a))
+    rng = np.random.default_rng(seed + 1)
+    kd = np.uint8 if max(a, b) <= 255 else np.int32
+    t["flag"] = rng.integers(0, a, rows).astype(kd)
+    t["status"] = rng.integers(0, b, rows).astype(kd)
+    return t, (a, b)

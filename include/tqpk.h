@@ -180,6 +180,20 @@ int tqpk_compact(const tqpk_predicate* h_pred, const uint8_t* d_mask, int64_t n,
                  const void* const* h_cols_in, const int32_t* h_dtypes, void* const* h_cols_out,
                  int64_t* d_count, void* d_ws, size_t ws_bytes, tqpk_stream stream);
 
+/* Stream compaction for callers that cannot allocate device memory when
+ * they call (no counterpart in the reference, which always allocates through
+ * torch): same arguments and results as tqpk_compact, minus the workspace.
+ * Its scratch is a 1 MiB array inside the library, resident on every device
+ * that loads it.  Inputs longer than tqpk_compact_noalloc_max_rows() rows
+ * return TQPK_ENOMEM.  All calls on a device share that array, so calls that
+ * overlap on the GPU race and must be ordered by the caller.  The first call
+ * on a device looks up the array's address; make it before any stream
+ * capture on that device.                                                 */
+int64_t tqpk_compact_noalloc_max_rows(void);
+int tqpk_compact_noalloc(const tqpk_predicate* h_pred, const uint8_t* d_mask, int64_t n, int32_t ncols,
+                         const void* const* h_cols_in, const int32_t* h_dtypes, void* const* h_cols_out,
+                         int64_t* d_count, tqpk_stream stream);
+
 /* ---- (d) group-by aggregation ----------------------------------------- */
 /* Computes the key ranges of the rows passing the filter (d_mask or h_pred,
  * either may be NULL) and picks the kernel.  Synchronises.                */

@@ -350,6 +350,36 @@ int tqpk_batch_run(const void* d_recs, int32_t n_inst, const void* d_items, int3
 int tqpk_batch_error(const void* d_ctl, int* h_err, tqpk_stream stream);
 int32_t tqpk_batch_grid(void);
 
+/* ---- runtime-compiled query kernels (NVRTC, opened with dlopen) ----------
+ * The host generates CUDA C++ for one query's hot loop (predicate, expression
+ * and accumulators as straight-line code); these compile it for sm_103a,
+ * load it and launch it.  tqpk_jit_available() is 0 when NVRTC cannot be
+ * opened; the interpreting kernels then run instead.                        */
+int tqpk_jit_available(void);
+int tqpk_jit_check(const char* src, char* log, size_t log_len);
+int tqpk_jit_compile(const char* src, const char* name, void** h_handle, char* log, size_t log_len);
+int tqpk_jit_occupancy(void* handle, int32_t block, size_t smem);
+int tqpk_jit_launch(void* handle, int32_t grid, int32_t block, size_t smem, void** args, int32_t timing_kid,
+                    tqpk_stream stream);
+int32_t tqpk_num_sms(void);
+/* Stages of tqpk_groupby_run around a caller-launched accumulation kernel. */
+int tqpk_groupby_prepare(const tqpk_groupby_spec* h_spec, const tqpk_gb_plan* h_plan, void* d_ws, size_t ws_bytes,
+                         tqpk_stream stream);
+int tqpk_groupby_count(const tqpk_groupby_spec* h_spec, const tqpk_gb_plan* h_plan, void* d_ws, int64_t* h_groups,
+                       tqpk_stream stream);
+void* tqpk_groupby_table(void* d_ws);
+/* The fused join pipeline run stage by stage (bit 0 reset + build, bit 1
+ * probe, bit 2 top-k + emit), and the addresses of its tables.             */
+int tqpk_pipeline_join_agg_topk_stages(int32_t stages, const void* d_build_keys, int32_t build_dtype, int64_t nb,
+                                       const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max,
+                                       const void* d_probe_fk, int32_t probe_dtype, int64_t np,
+                                       const tqpk_predicate* h_probe_pred, const tqpk_groupby_spec* h_values,
+                                       int32_t value_reg, int32_t k, int32_t descending, void* d_ws, size_t ws_bytes,
+                                       int64_t* d_out_keys, double* d_out_vals, int64_t* d_out_count,
+                                       int64_t* d_groups_out, tqpk_stream stream);
+int tqpk_pipeline_join_tables(void* d_ws, size_t ws_bytes, int64_t key_min, int64_t key_max, void** dir, void** sum,
+                              void** occ);
+
 /* Reads (synchronising) the error word a fused pipeline left in its workspace. */
 int tqpk_pipeline_error(const void* d_ws, int* h_err, tqpk_stream stream);
 

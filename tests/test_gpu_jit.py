@@ -1,0 +1,111 @@
+"""Query-specialised (runtime-compiled) kernels against the interpreting kernels and the oracle."""
+import copy
+
+import numpy as np
+import pytest
+import torch
+
+from golden_io import assert_f64_close, load
+from oracle import tqp_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    from tqpk import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def test_nvrtc_available_on_the_gpu_box():
+    from tqpk import jit
+    assert jit.available(), "NVRTC could not be opened; the hot loops would run interpreted"
+
+
+@pytest.mark.parametrize("jit_on", ["1", "0"])
+def test_lineitem_groupby_both_paths(monkeypatch, jit_on):
+    monkeypatch.setenv("TQPK_JIT", jit_on)
+    from tqpk import datagen
+    from tqpk.operators import tqp_filter, tqp_hash_aggregate
+    from tqpk.variable import Variable
+    _, _, args = load("filter_agg_sort_lineitem")
+    t = datagen.lineitem(1_000_003, seed=4)
+    ids = {"quantity": 1, "price": 2, "discount": 3, "tax": 4, "flag": 5, "status": 6, "ship_date": 7}
+    cols = {ids[k]: v for k, v in t.items()}
+    tg = {c: Variable(torch.from_numpy(a).cuda(), args["types"][str(c)]) for c, a in cols.items()}
+    tqp_filter(True, tg, copy.deepcopy(args["filter"]), None, None, None, "f")
+    aargs = copy.deepcopy(args["aggregate"])
+    aargs["mask map"] = {int(k): v for k, v in aargs["mask map"].items()}
+    tqp_hash_aggregate(True, tg, copy.deepcopy(aargs), None, None, "a")
+    oc = dict(cols)
+    oc[900] = cols[7] <= 2470
+    ref = O.tqp_hash_aggregate(oc, aargs)
+    for c in (5, 6):
+        np.testing.assert_array_equal(tg[c].tensor.cpu().numpy(), ref[c])
+    for a in aargs["out agg ids"]:
+        got = tg[a].tensor.cpu().numpy()
+        (assert_f64_close if ref[a].dtype == np.float64 else np.testing.assert_array_equal)(got, ref[a])
+
+
+@pytest.mark.parametrize("jit_on", ["1", "0"])
+def test_groupby_predicate_fused_both_paths(monkeypatch, jit_on):
+    """The fused predicate form (no mask) with min/max/count-not-null and int sums."""
+    monkeypatch.setenv("TQPK_JIT", jit_on)
+    from tqpk.expr import compile_aggregate
+    from tqpk.ops import groupby
+    from tqpk.predicate import compile_filter
+    rng = np.random.default_rng(17)
+    n = 500_001
+    cols = {1: rng.integers(-3, 4, n).astype(np.int32), 2: rng.integers(0, 300, n).astype(np.int64),
+            3: rng.normal(10, 50, n), 4: rng.integers(-100, 1000, n).astype(np.int64),
+            5: rng.integers(0, 2557, n).astype(np.int32)}
+    d = {c: torch.from_numpy(a).cuda() for c, a in cols.items()}
+    results = ["k1#1", "k2#2",
+               [[["sum", ["v#3"]], "#", "1"], "AS", "s#501"], [[["min", ["v#3"]], "#", "2"], "AS", "a#502"],
+               [[["max", ["w#4"]], "#", "3"], "AS", "b#503"], [[["sum", ["w#4"]], "#", "4"], "AS", "c#504"],
+               [[["count", ["w#4"]], "#", "5L"], "AS", "d#505"], [[["avg", [["v#3", "*", "2.5"]]], "#", "6"], "AS", "e#506"]]
+    args = {"is partial": False, "keys": ["k1#1", "k2#2"], "input ids": [1, 2, 3, 4], "results": results,
+            "out agg ids": [501, 502, 503, 504, 505, 506]}
+    tree = [[["d#5", ">=", "300"], "AND", ["d#5", "<", "2000"]], "OR", ["v#3", "<=", "0.5"]]
+    prog = compile_aggregate(args, d)
+    pred = compile_filter(tree, {5: d[5], 3: d[3]})
+    keys, outs, G, _ = groupby(prog, n, d[1].device, pred=pred)
+    mask = O.eval_filter(tree, cols)
+    oc = dict(cols)
+    oc[99] = mask
+    ref = O.tqp_hash_aggregate(oc, dict(args, **{"mask map": {1: 99, 2: 99, 3: 99, 4: 99}}))
+    np.testing.assert_array_equal(keys[0].cpu().numpy(), ref[1].reshape(-1))
+    np.testing.assert_array_equal(keys[1].cpu().numpy(), ref[2].reshape(-1))
+    for a in args["out agg ids"]:
+        got = outs[a].cpu().numpy()
+        (assert_f64_close if ref[a].dtype == np.float64 else np.testing.assert_array_equal)(got, ref[a])
+
+
+@pytest.mark.parametrize("jit_on", ["1", "0"])
+def test_join_pipeline_both_paths(monkeypatch, jit_on):
+    monkeypatch.setenv("TQPK_JIT", jit_on)
+    from tqpk import datagen
+    from tqpk.pipeline import JoinAggTopK
+    t = datagen.join_tables(200_000, 900_001, seed=21)
+    d = {k: torch.from_numpy(v).cuda() for k, v in t.items()}
+    p = JoinAggTopK(d["b_key"], 1, 200_000, d["p_fk"], {12: d["b_date"]}, [["bd#12", "<", "1170"]],
+                    {22: d["p_date"], 23: d["p_price"], 24: d["p_discount"]}, [["pd#22", ">", "1170"]],
+                    [["p#23", "*", ["1.0", "-", "d#24"]]], k=10)
+    p.run()
+    keys, vals, groups = p.result()
+    cols = {11: t["b_key"], 12: t["b_date"], 21: t["p_fk"], 22: t["p_date"], 23: t["p_price"], 24: t["p_discount"]}
+    oc = dict(cols)
+    oc[901] = cols[12] < 1170
+    oc[902] = cols[22] > 1170
+    res, _ = O.join_vortex(oc, {"left group": [11, 12], "right group": [21, 22, 23, 24],
+                                "materialized in": [11, 21, 23, 24],
+                                "mask map": {11: 901, 21: 902, 23: 902, 24: 902}}, 11, 21, "inner")
+    agg = O.tqp_hash_aggregate(res, {"is partial": False, "keys": ["k#11"], "input ids": [11, 23, 24],
+                                     "results": ["k#11", [[["sum", [["p#23", "*", ["1.0", "-", "d#24"]]]], "#", "1"],
+                                                          "AS", "r#302"]], "out agg ids": [302]})
+    top = O.tqp_sort({11: agg[11], 302: agg[302]}, {"limit": 10, "input ids": [11, 302], "key ids": [302],
+                                                    "key orders": [True]}, True)
+    assert groups == agg[11].shape[0]
+    np.testing.assert_array_equal(keys, top[11].reshape(-1))
+    assert_f64_close(vals, top[302])

@@ -492,3 +492,45 @@ extern "C" int tqpk_groupby_emit(const tqpk_groupby_spec* S, const tqpk_gb_plan*
   TQPK_CUDA(cudaStreamSynchronize(s));
   return err ? err : TQPK_OK;
 }
+
+// Stages of tqpk_groupby_run for callers that launch their own accumulation
+// kernel (the runtime-compiled one): prepare zeroes/initialises the table,
+// count counts the occupied slots (synchronises).
+extern "C" int tqpk_groupby_prepare(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, void* ws, size_t ws_bytes,
+                                    tqpk_stream stream) {
+  int rc = check_spec(S);
+  if (rc) return rc;
+  if (!plan || !ws) return TQPK_EINVAL;
+  if (ws_bytes < plan->ws_bytes) return TQPK_ENOMEM;
+  if (plan->mode == TQPK_GB_HASH) return TQPK_EUNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* base = static_cast<char*>(ws);
+  TQPK_CUDA(cudaMemsetAsync(base, 0, 8, s));
+  k_init_accs<<<grid_for(plan->slots * S->n_accs, 4), kBlock, 0, s>>>(*S, reinterpret_cast<uint64_t*>(base + 512),
+                                                                       plan->slots);
+  TQPK_CHECK_LAUNCH();
+  return TQPK_OK;
+}
+
+extern "C" int tqpk_groupby_count(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, void* ws, int64_t* h_groups,
+                                  tqpk_stream stream) {
+  if (!S || !plan || !ws || !h_groups) return TQPK_EINVAL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* base = static_cast<char*>(ws);
+  if (S->n_keys == 0) {
+    *h_groups = 1;
+    return TQPK_OK;
+  }
+  unsigned long long* d_groups = reinterpret_cast<unsigned long long*>(base);
+  k_count_groups<<<grid_for(plan->slots, 4), kBlock, 0, s>>>(reinterpret_cast<const uint64_t*>(base + 512),
+                                                            plan->slots, d_groups);
+  TQPK_CHECK_LAUNCH();
+  unsigned long long h = 0;
+  TQPK_CUDA(cudaMemcpyAsync(&h, d_groups, 8, cudaMemcpyDeviceToHost, s));
+  TQPK_CUDA(cudaStreamSynchronize(s));
+  *h_groups = (int64_t)h;
+  return TQPK_OK;
+}
+
+// Device address of the accumulator table inside a plan's workspace ([n_accs][slots], 8 bytes each).
+extern "C" void* tqpk_groupby_table(void* ws) { return ws ? static_cast<char*>(ws) + 512 : nullptr; }

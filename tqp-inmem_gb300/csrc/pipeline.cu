@@ -188,13 +188,12 @@ extern "C" size_t tqpk_pipeline_join_agg_topk_workspace_bytes(int64_t key_min, i
   return pipe_bytes(key_max - key_min + 1, topk_grid());
 }
 
-extern "C" int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t build_dtype, int64_t nb,
-                                           const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max,
-                                           const void* d_probe_fk, int32_t probe_dtype, int64_t np,
-                                           const tqpk_predicate* h_probe_pred, const tqpk_groupby_spec* h_values,
-                                           int32_t value_reg, int32_t k, int32_t descending, void* d_ws,
-                                           size_t ws_bytes, int64_t* d_out_keys, double* d_out_vals,
-                                           int64_t* d_out_count, int64_t* d_groups_out, tqpk_stream stream) {
+static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dtype, int64_t nb,
+                         const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max, const void* d_probe_fk,
+                         int32_t probe_dtype, int64_t np, const tqpk_predicate* h_probe_pred,
+                         const tqpk_groupby_spec* h_values, int32_t value_reg, int32_t k, int32_t descending,
+                         void* d_ws, size_t ws_bytes, int64_t* d_out_keys, double* d_out_vals, int64_t* d_out_count,
+                         int64_t* d_groups_out, tqpk_stream stream) {
   if (nb < 0 || np < 0 || k < 1 || k > kPipeMaxK || !h_values || !d_ws || !d_out_keys || !d_out_vals || !d_out_count)
     return TQPK_EINVAL;
   if ((nb > 0 && !d_build_keys) || (np > 0 && !d_probe_fk)) return TQPK_EINVAL;
@@ -226,6 +225,7 @@ extern "C" int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t bui
   A.b_pvec = pred_vec_ok(h_build_pred) ? 1 : 0;
   A.p_pvec = pred_vec_ok(h_probe_pred) ? 1 : 0;
   A.v_pvec = spec_cols_vec(h_values) ? 1 : 0;
+  if (stages & 1) {
   TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 32, s));
   TQPK_CUDA(cudaMemsetAsync(L.dir, 0xff, slots * 4, s));
   TQPK_CUDA(cudaMemsetAsync(L.sum, 0, slots * 8, s));
@@ -236,14 +236,15 @@ extern "C" int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t bui
     timing_after(KID_PIPE_BUILD, s);
     TQPK_CHECK_LAUNCH();
   }
-  if (np > 0) {
+  }
+  if ((stages & 2) && np > 0) {
     timing_before(KID_PIPE_PROBE, s);
     k_pl_probe_agg<<<occ_grid(k_pl_probe_agg, (np + 7) / 8), kBlock, 0, s>>>(*pred_or_empty(h_probe_pred), *h_values,
                                                                            A, L.dir, L.sum, L.cnt, L.groups);
     timing_after(KID_PIPE_PROBE, s);
     TQPK_CHECK_LAUNCH();
   }
-  {
+  if (stages & 4) {
     DenseSumSource src{L.sum, L.cnt, slots, A.desc};
     TopkOut O{L.top_idx, L.top_count, L.cand_key, L.cand_slot, L.done, L.groups};
     timing_before(KID_PIPE_TOPK, s);
@@ -253,7 +254,47 @@ extern "C" int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t bui
     k_pl_emit<<<1, 256, 0, s>>>(L.top_idx, L.top_count, L.sum, key_min, k, d_out_keys, d_out_vals, d_out_count);
     TQPK_CHECK_LAUNCH();
   }
-  if (d_groups_out) TQPK_CUDA(cudaMemcpyAsync(d_groups_out, L.groups, 8, cudaMemcpyDeviceToDevice, s));
+  if ((stages & 4) && d_groups_out) TQPK_CUDA(cudaMemcpyAsync(d_groups_out, L.groups, 8, cudaMemcpyDeviceToDevice, s));
+  return TQPK_OK;
+}
+
+extern "C" int tqpk_pipeline_join_agg_topk(const void* d_build_keys, int32_t build_dtype, int64_t nb,
+                                           const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max,
+                                           const void* d_probe_fk, int32_t probe_dtype, int64_t np,
+                                           const tqpk_predicate* h_probe_pred, const tqpk_groupby_spec* h_values,
+                                           int32_t value_reg, int32_t k, int32_t descending, void* d_ws,
+                                           size_t ws_bytes, int64_t* d_out_keys, double* d_out_vals,
+                                           int64_t* d_out_count, int64_t* d_groups_out, tqpk_stream stream) {
+  return pipeline_join(7, d_build_keys, build_dtype, nb, h_build_pred, key_min, key_max, d_probe_fk, probe_dtype, np,
+                       h_probe_pred, h_values, value_reg, k, descending, d_ws, ws_bytes, d_out_keys, d_out_vals,
+                       d_out_count, d_groups_out, stream);
+}
+
+// Same pipeline, run stage by stage: bit 0 = reset + build, bit 1 = probe +
+// aggregate, bit 2 = top-k + emit.  A caller with its own probe kernel runs
+// stages 1 and 4 around it (tqpk_pipeline_join_tables gives the tables).
+extern "C" int tqpk_pipeline_join_agg_topk_stages(int32_t stages, const void* d_build_keys, int32_t build_dtype,
+                                                  int64_t nb, const tqpk_predicate* h_build_pred, int64_t key_min,
+                                                  int64_t key_max, const void* d_probe_fk, int32_t probe_dtype,
+                                                  int64_t np, const tqpk_predicate* h_probe_pred,
+                                                  const tqpk_groupby_spec* h_values, int32_t value_reg, int32_t k,
+                                                  int32_t descending, void* d_ws, size_t ws_bytes,
+                                                  int64_t* d_out_keys, double* d_out_vals, int64_t* d_out_count,
+                                                  int64_t* d_groups_out, tqpk_stream stream) {
+  return pipeline_join(stages, d_build_keys, build_dtype, nb, h_build_pred, key_min, key_max, d_probe_fk, probe_dtype,
+                       np, h_probe_pred, h_values, value_reg, k, descending, d_ws, ws_bytes, d_out_keys, d_out_vals,
+                       d_out_count, d_groups_out, stream);
+}
+
+// Device addresses of the directory (int32), sums (f64) and occupancy (u32) in the workspace.
+extern "C" int tqpk_pipeline_join_tables(void* d_ws, size_t ws_bytes, int64_t key_min, int64_t key_max, void** dir,
+                                         void** sum, void** occ) {
+  PipeLayout L;
+  if (!d_ws || key_max < key_min || !pipe_layout(d_ws, ws_bytes, key_max - key_min + 1, topk_grid(), L))
+    return TQPK_EINVAL;
+  *dir = L.dir;
+  *sum = L.sum;
+  *occ = L.cnt;
   return TQPK_OK;
 }
 

@@ -107,6 +107,19 @@ SIGNATURES = {
     "tqpk_batch_run": (C.c_int, [_VP, _I32, _VP, _I32, _VP, _I32, _VP]),
     "tqpk_batch_error": (C.c_int, [_VP, _P(C.c_int), _VP]),
     "tqpk_batch_grid": (_I32, []),
+    "tqpk_jit_available": (C.c_int, []),
+    "tqpk_jit_check": (C.c_int, [C.c_char_p, C.c_char_p, _SZ]),
+    "tqpk_jit_compile": (C.c_int, [C.c_char_p, C.c_char_p, _P(_VP), C.c_char_p, _SZ]),
+    "tqpk_jit_occupancy": (C.c_int, [_VP, _I32, _SZ]),
+    "tqpk_jit_launch": (C.c_int, [_VP, _I32, _I32, _SZ, _P(_VP), _I32, _VP]),
+    "tqpk_num_sms": (_I32, []),
+    "tqpk_groupby_prepare": (C.c_int, [_P(GroupbySpec), _P(GbPlan), _VP, _SZ, _VP]),
+    "tqpk_groupby_count": (C.c_int, [_P(GroupbySpec), _P(GbPlan), _VP, _P(_I64), _VP]),
+    "tqpk_groupby_table": (_VP, [_VP]),
+    "tqpk_pipeline_join_agg_topk_stages": (C.c_int, [_I32, _VP, _I32, _I64, _P(Predicate), _I64, _I64, _VP, _I32, _I64,
+                                                     _P(Predicate), _P(GroupbySpec), _I32, _I32, _I32, _VP, _SZ, _VP,
+                                                     _VP, _VP, _VP, _VP]),
+    "tqpk_pipeline_join_tables": (C.c_int, [_VP, _SZ, _I64, _I64, _P(_VP), _P(_VP), _P(_VP)]),
     "tqpk_compact_noalloc_max_rows": (_I64, []),
     "tqpk_compact_noalloc": (C.c_int, [_P(Predicate), _VP, _I64, _I32, _P(_VP), _P(_I32), _P(_VP), _VP, _VP]),
     "tqpk_timing_begin": (C.c_int, [_I32]),

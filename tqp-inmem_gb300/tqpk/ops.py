@@ -115,8 +115,20 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
             "tqpk_groupby_plan")
     ws = _ws(plan.ws_bytes, device)
     groups = C.c_int64(0)
-    L.check(lib.tqpk_groupby_run(C.byref(prog.spec), C.byref(plan), pp, mp, n, ws.data_ptr(), ws.numel(),
-                                 C.byref(groups), s), "tqpk_groupby_run")
+    from . import jit
+    if jit.available() and mask is not None and pred is None and plan.n_rows > 0 and n > 0:
+        pred = _mask_predicate(mask)              # the mask as a one-instruction predicate
+    if jit.available() and (mask is None or pred is not None) and plan.n_rows > 0 and n > 0:
+        # query-specialised accumulation kernel between the library's prepare and count stages
+        L.check(lib.tqpk_groupby_prepare(C.byref(prog.spec), C.byref(plan), ws.data_ptr(), ws.numel(), s),
+                "tqpk_groupby_prepare")
+        jit.run_groupby(prog.spec, pred, plan, ws, n, s, pred.tensors if pred is not None else (),
+                        [t for t in prog.tensors[:prog.spec.n_keys]], prog.tensors[prog.spec.n_keys:])
+        L.check(lib.tqpk_groupby_count(C.byref(prog.spec), C.byref(plan), ws.data_ptr(), C.byref(groups), s),
+                "tqpk_groupby_count")
+    else:
+        L.check(lib.tqpk_groupby_run(C.byref(prog.spec), C.byref(plan), pp, mp, n, ws.data_ptr(), ws.numel(),
+                                     C.byref(groups), s), "tqpk_groupby_run")
     G = groups.value
     keys = [torch.empty(G, dtype=dtype_of(prog.spec.key_dtypes[k]), device=device) for k in range(prog.spec.n_keys)]
     outs = [torch.empty(G, dtype=dt, device=device) for (_, _, _, _, dt) in prog.outputs]
@@ -127,6 +139,16 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
                                   _vp_array([k.data_ptr() for k in keys]), len(outs), _i32_array(ops),
                                   _vp_array([o.data_ptr() for o in outs]), s), "tqpk_groupby_emit")
     return keys, {oid: o for (oid, *_), o in zip(prog.outputs, outs)}, G, plan
+
+
+def _mask_predicate(mask: torch.Tensor) -> CompiledPredicate:
+    p = L.Predicate()
+    p.n_insn, p.n_cols = 1, 1
+    m = mask.contiguous()
+    p.cols[0] = m.data_ptr()
+    p.dtypes[0] = L.BOOL
+    p.insn[0] = L.PredInsn(L.P_MASK, 0, 0, 0, 0, 0.0, 0.0)
+    return CompiledPredicate(p, [m], [-1])
 
 
 # ---------------------------------------------------------------- (b) sort / (e) top-k

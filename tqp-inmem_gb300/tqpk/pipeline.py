@@ -52,16 +52,57 @@ class JoinAggTopK:
     def workspace_bytes(self) -> int:
         return int(self.ws.numel())
 
-    def run(self, stream=None):
-        s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
-        L.check(self.lib.tqpk_pipeline_join_agg_topk(
-            self.bk.data_ptr(), code_of(self.bk.dtype), self.bk.numel(),
+    def _stages(self, stages, s):
+        L.check(self.lib.tqpk_pipeline_join_agg_topk_stages(
+            stages, self.bk.data_ptr() if self.bk.numel() else None, code_of(self.bk.dtype), self.bk.numel(),
             C.byref(self.bpred.struct) if self.bpred else None, self.key_min, self.key_max,
-            self.pk.data_ptr(), code_of(self.pk.dtype), self.pk.numel(),
+            self.pk.data_ptr() if self.pk.numel() else None, code_of(self.pk.dtype), self.pk.numel(),
             C.byref(self.ppred.struct) if self.ppred else None, C.byref(self.prog.spec), self.value_reg,
             self.k, int(self.desc), self.ws.data_ptr(), self.ws.numel(), self.out_keys.data_ptr(),
             self.out_vals.data_ptr(), self.out_count.data_ptr(), self.groups.data_ptr(), s),
             "tqpk_pipeline_join_agg_topk")
+
+    def _jit_probe(self, s):
+        """The probe + aggregate pass as a query-specialised kernel."""
+        from . import jit
+        if not hasattr(self, "_probe_handle"):
+            src, name = jit.join_probe_source(self.prog.spec, self.value_reg,
+                                              self.ppred.struct if self.ppred else None)
+            self._probe_handle = jit.compile_kernel(src, name)
+            d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
+            L.check(self.lib.tqpk_pipeline_join_tables(self.ws.data_ptr(), self.ws.numel(), self.key_min,
+                                                       self.key_max, C.byref(d), C.byref(su), C.byref(oc)),
+                    "tqpk_pipeline_join_tables")
+            a = jit._Args()
+            if self.ppred:
+                for c in range(self.ppred.struct.n_cols):
+                    a.ptr(self.ppred.struct.cols[c])
+            for c in range(self.prog.spec.n_cols):
+                a.ptr(self.prog.spec.cols[c])
+            a.ptr(self.pk.data_ptr())
+            a.i32(code_of(self.pk.dtype))
+            a.i64(self.pk.numel())
+            a.i64(self.key_min)
+            a.i64(self.key_max - self.key_min + 1)
+            a.ptr(d.value)
+            a.ptr(su.value)
+            a.ptr(oc.value)
+            a.i32(jit._aligned(*self.ppred.tensors) if self.ppred else 1)
+            a.i32(jit._aligned(*self.prog.tensors))
+            a.i32(jit._aligned(self.pk))
+            self._probe_args = a
+            self._probe_grid = jit.occupancy_grid(self._probe_handle, 256, 0, (self.pk.numel() + 7) // 8)
+        jit.launch(self._probe_handle, self._probe_grid, 256, 0, self._probe_args, s, L.KID_PIPE_PROBE)
+
+    def run(self, stream=None):
+        from . import jit
+        s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
+        if jit.available() and jit.probe_supported(code_of(self.pk.dtype)) and self.pk.numel() > 0:
+            self._stages(1, s)
+            self._jit_probe(s)
+            self._stages(4, s)
+        else:
+            self._stages(7, s)
 
     def check_error(self, stream=None):
         s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream

@@ -486,6 +486,75 @@ def run_batched_bench(args):
     print(json.dumps(line))
 
 
+def run_serving_bench(args):
+    """Poisson arrivals (2000/s) of the three query shapes over resident 60M-row tables, HBM budget
+    150 GB: continuous batching (8 slots) beside one-at-a-time on the same trace, plus the
+    closed-loop (all requests queued at t=0) throughput of both."""
+    import dataclasses
+    import torch
+    import __graft_entry__ as G
+    G.build()
+    from tqpk import _lib as L
+    from tqpk.serve import DeviceArena, GpuExecutor, ResidentTables, Scheduler, latency_summary, poisson_trace
+    lib = L.load()
+    dev = torch.device("cuda", 0)
+    n_fact, rate, slots, budget = 60_000_000, 2000.0, 8, 150 << 30
+    t_setup = time.perf_counter()
+    tables = ResidentTables(dev, n_fact=n_fact)
+    ex = GpuExecutor(tables, slots)
+    arena = DeviceArena(budget, tables.nbytes, dev, slab_cap=8 << 30)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    warm = poisson_trace(max(30, 10 * args.warmup), rate, n_fact, seed=100)
+    Scheduler(ex, arena, slots).run(warm)
+    Scheduler(ex, arena, 1).run(warm[:10])
+    n_req = max(400, 100 * args.steps)
+    trace = poisson_trace(n_req, rate, n_fact, seed=1)
+    sampler = ClockSampler(0)
+    sampler.start()
+    launches0 = lib.tqpk_launch_count()
+    sched = Scheduler(ex, arena, slots)
+    cont = sched.run(trace)
+    launches = lib.tqpk_launch_count() - launches0
+    serial = Scheduler(ex, arena, 1).run(trace)
+    burst = [dataclasses.replace(r, arrival=0.0) for r in trace[: max(200, n_req // 4)]]
+    cont_sat = Scheduler(ex, arena, slots).run(burst)
+    serial_sat = Scheduler(ex, arena, 1).run(burst)
+    clocks = sampler.stop()
+    sc, ss = latency_summary(cont), latency_summary(serial)
+    by_shape = {}
+    for shape in ("filter_groupby", "join", "star"):
+        sub = [c for c in cont if c.req.shape == shape]
+        if sub:
+            lat = np.array([c.latency for c in sub]) * 1e3
+            by_shape[shape] = {"requests": len(sub), "p50_ms": float(np.percentile(lat, 50)),
+                               "p99_ms": float(np.percentile(lat, 99))}
+    def result_bytes(r):
+        parts = []
+        for v in r.values():
+            parts += list(v.values()) if isinstance(v, dict) else (v if isinstance(v, list) else [v])
+        return sum(np.asarray(x).nbytes for x in parts)
+    d2h = sum(result_bytes(c.result) for c in cont)
+    line = {"metric": "requests/s", "value": sc["requests_per_s"], "unit": "requests/s", "n_gpus": 1,
+            "steps": n_req, "warmup": len(warm), "ms_per_step": 1e3 / sc["requests_per_s"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded), Poisson arrivals",
+            "config": {"workload": "serving: Poisson arrivals of filter+group-by / join+agg+top-10 / star join+top-100 "
+                                   "over resident tables, continuous batching vs one-at-a-time",
+                       "arrival_rate_per_s": rate, "requests": n_req, "fact_rows_range": [1_000_000, n_fact],
+                       "slots": slots, "hbm_budget_bytes": budget, "resident_bytes": tables.nbytes,
+                       "setup_s": setup_s, "l2": "inputs (GBs per shape) larger than L2"},
+            "serving": {"continuous": sc, "one_at_a_time": ss, "continuous_by_shape": by_shape,
+                        "closed_loop_requests_per_s": {"continuous": latency_summary(cont_sat)["requests_per_s"],
+                                                       "one_at_a_time": latency_summary(serial_sat)["requests_per_s"],
+                                                       "requests": len(burst)},
+                        "max_inflight": sched.max_inflight},
+            "e2e": {"value": sc["requests_per_s"], "unit": "requests/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": d2h / max(len(cont), 1),
+                    "path": "arrival on the host to result in pinned host memory; tables resident"},
+            "clocks": clocks, "gpu_launches": launches}
+    print(json.dumps(line))
+
+
 WORKLOADS = {c.name: c for c in (JoinAggTop10, FilterGroupBy, StarJoin)}
 
 
@@ -748,11 +817,18 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batched"], default="join_agg_top10")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batched", "serving"], default="join_agg_top10")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world = dist_setup(args.gpus)
+    if args.workload == "serving":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference answers one query at a time; its "
+                              "per-query CPU time is the other workloads' reference lines"}))
+        elif rank == 0:
+            run_serving_bench(args)
+        return
     if args.workload == "batched":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the batched form has no reference counterpart"}))

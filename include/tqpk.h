@@ -349,6 +349,10 @@ int tqpk_batch_run(const void* d_recs, int32_t n_inst, const void* d_items, int3
                    int32_t grid, tqpk_stream stream);
 int tqpk_batch_error(const void* d_ctl, int* h_err, tqpk_stream stream);
 int32_t tqpk_batch_grid(void);
+/* Per-item timeline (32 bytes per work item: dequeue, dependency met and
+ * completion times in ns, SM id) written by later tqpk_batch_run launches
+ * while d_trace is set; NULL turns it off.                                  */
+int tqpk_batch_set_trace(void* d_trace);
 
 /* ---- runtime-compiled query kernels (NVRTC, opened with dlopen) ----------
  * The host generates CUDA C++ for one query's hot loop (predicate, expression
@@ -379,6 +383,34 @@ int tqpk_pipeline_join_agg_topk_stages(int32_t stages, const void* d_build_keys,
                                        int64_t* d_groups_out, tqpk_stream stream);
 int tqpk_pipeline_join_tables(void* d_ws, size_t ws_bytes, int64_t key_min, int64_t key_max, void** dir, void** sum,
                               void** occ);
+
+/* ---- resident directories and dense slot tables (dense.cu) ---------------
+ * Replaces the per-call build of operators/hashjoin.py:24-177 (torch.sort of
+ * the build keys, then searchsorted) for a join on a unique key: a
+ * direct-address directory built once per loaded table and kept in HBM.
+ * dir[key - key_min] = payload (the row index when d_payload is NULL) for
+ * rows passing h_pred (NULL = all), fail_value for the others, `empty` where
+ * no row has the key; a payload outside int32 or equal to `empty` is stored
+ * as fail_value.  A key outside [key_min, key_min + slots) sets TQPK_EINVAL
+ * in *d_err, a repeated key TQPK_EUNSUPPORTED.                              */
+int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64_t n, const tqpk_predicate* h_pred,
+                         const void* d_payload, int32_t payload_dtype, int64_t key_min, int64_t slots, int32_t empty,
+                         int32_t fail_value, int32_t* d_dir, int32_t* d_err, tqpk_stream stream);
+/* The k (<= 256) best groups of a dense slot table (sum[s], count[s] != 0
+ * marks a group) ordered by sum (descending when `descending`), ties to the
+ * smaller key: the "sort by aggregate + limit" of operators/sort.py:6-58 over
+ * a group-by result in ascending key order (aggregate.py:325 unique order).
+ * Keys are key_min + slot.  No host synchronisation.                       */
+size_t tqpk_dense_topk_workspace_bytes(int32_t k);
+int tqpk_dense_topk(const double* d_sum, const uint32_t* d_cnt, int64_t slots, int64_t key_min, int32_t k,
+                    int32_t descending, void* d_ws, size_t ws_bytes, int64_t* d_out_keys, double* d_out_vals,
+                    int64_t* d_out_counts, int64_t* d_out_count, int64_t* d_out_groups, tqpk_stream stream);
+/* tqpk_groupby_emit without the host synchronisation: outputs hold
+ * h_plan->slots rows; *d_groups_out receives the group count (or a negative
+ * status).                                                                   */
+int tqpk_groupby_emit_async(const tqpk_groupby_spec* h_spec, const tqpk_gb_plan* h_plan, void* d_ws,
+                            void* const* h_out_keys, int32_t n_out, const int32_t* h_out_ops,
+                            void* const* h_out_cols, int64_t* d_groups_out, tqpk_stream stream);
 
 /* Reads (synchronising) the error word a fused pipeline left in its workspace. */
 int tqpk_pipeline_error(const void* d_ws, int* h_err, tqpk_stream stream);

@@ -14,12 +14,17 @@ def load(name):
     return ins, outs, json.loads(str(z["args"]))
 
 
-def assert_f64_close(a, b, rel=1e-12):
+def assert_f64_close(a, b, rel=1e-12, magnitude=None):
+    """|a - b| <= rel * max(|a|, |b|), or rel * magnitude where given: for sums with
+    cancellation the error bound of any summation order scales with sum(|x|), so
+    tests pass that per element (the sum of absolute values of the summed terms)."""
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     assert a.shape == b.shape, (a.shape, b.shape)
     same_nan = np.isnan(a) & np.isnan(b)
     scale = np.maximum(np.abs(a), np.abs(b))
+    if magnitude is not None:
+        scale = np.maximum(scale, np.asarray(magnitude, np.float64))
     ok = (np.abs(a - b) <= rel * scale) | same_nan | (a == b)
     assert np.all(ok), (a[~ok][:5], b[~ok][:5])
 

@@ -74,8 +74,10 @@ def test_join_pipeline_repeated_build_key_raises():
         p.result()
 
 
+@pytest.mark.parametrize("jit_on", ["1", "0"])
 @pytest.mark.parametrize("scale,k", [(0.05, 100), (0.01, 7), (0.002, 256)])
-def test_star_pipeline_vs_oracle(scale, k):
+def test_star_pipeline_vs_oracle(monkeypatch, jit_on, scale, k):
+    monkeypatch.setenv("TQPK_JIT", jit_on)
     import bench
     from tqpk.pipeline import StarAggTopK
     w = bench.StarJoin(scale=scale)

@@ -31,7 +31,7 @@ constexpr int kBatchSmem = 96 * 1024;   // dynamic shared memory of the batch ke
 struct BatchInst {
   int type;
   int k, desc;
-  int gb_mode;            // GROUPBY: 1 = per-thread private tables in shared memory, 3 = global atomics
+  int gb_mode;            // GROUPBY: 1 = per-thread private tables, 2 = one shared-memory table per item, 3 = global atomics
   int64_t n_items[3];
   // JOIN
   const void* b_keys; int b_dt; int64_t nb;
@@ -196,8 +196,12 @@ __device__ void gb_agg_item(const BatchInst& I, int64_t b, int64_t e, uint64_t* 
   const int T = blockDim.x;
   const int64_t K = I.gslots;
   const bool priv = I.gb_mode == 1;
+  const bool shared = I.gb_mode == 2;   // one table per CTA (per item), shared-memory atomics
   if (priv) {
     for (int64_t i = threadIdx.x; i < K * A * T; i += T) sm[i] = b_acc_init(S.accs[(i / T) % A]);
+    __syncthreads();
+  } else if (shared) {
+    for (int64_t i = threadIdx.x; i < K * A; i += T) sm[i] = b_acc_init(S.accs[i % A]);
     __syncthreads();
   }
   const bool small = S.n_expr <= 16;
@@ -224,11 +228,23 @@ __device__ void gb_agg_item(const BatchInst& I, int64_t b, int64_t e, uint64_t* 
         if (priv) {
           uint64_t* p = &sm[(slot[j] * A + a) * T + threadIdx.x];
           *p = b_combine(ac, *p, b_acc_value(ac, x));
+        } else if (shared) {
+          b_merge_atomic(&sm[slot[j] * A + a], ac, b_acc_value(ac, x));
         } else {
           b_merge_atomic(&I.gacc[(int64_t)a * K + slot[j]], ac, b_acc_value(ac, x));
         }
       }
     }
+  }
+  if (shared) {
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < K * A; c += T) {
+      const tqpk_acc& a = S.accs[c % A];
+      const uint64_t v = sm[c];
+      if (v != b_acc_init(a)) b_merge_atomic(&I.gacc[(c % A) * K + c / A], a, v);
+    }
+    __syncthreads();
+    return;
   }
   if (!priv) return;
   __syncthreads();
@@ -305,9 +321,16 @@ __device__ void gb_emit_item(const BatchInst& I, int64_t item, int64_t b, int64_
   }
 }
 
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 __global__ void __launch_bounds__(kBlock) k_batch(const BatchInst* __restrict__ insts,
                                                   const WorkItem* __restrict__ items, int n_items,
-                                                  unsigned* ticket, unsigned* done, int* err) {
+                                                  unsigned* ticket, unsigned* done, int* err,
+                                                  uint64_t* __restrict__ trace) {
   extern __shared__ uint64_t bsm[];
   __shared__ int s_item;
   __shared__ uint64_t tk_k[kBlock];
@@ -319,6 +342,8 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchInst* __restrict__ 
     if (it >= n_items) return;
     const WorkItem W = items[it];
     const BatchInst& I = insts[W.inst];
+    uint64_t t0 = 0, t1 = 0;
+    if (trace && threadIdx.x == 0) t0 = global_ns();
     if (W.phase > 0 && threadIdx.x == 0) {
       const unsigned need = (unsigned)I.n_items[W.phase - 1];
       const uint64_t* flag = reinterpret_cast<const uint64_t*>(&done[(W.inst * 4 + W.phase - 1) * 2]);
@@ -329,6 +354,7 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchInst* __restrict__ 
       }
     }
     __syncthreads();
+    if (trace && threadIdx.x == 0) t1 = global_ns();
     if (I.type == BT_JOIN) {
       if (W.phase == 0) join_build_item(I, W.begin, W.end, err);
       else if (W.phase == 1) join_probe_item(I, W.begin, W.end);
@@ -342,9 +368,19 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchInst* __restrict__ 
     if (threadIdx.x == 0) {
       __threadfence();
       atomicAdd(reinterpret_cast<unsigned long long*>(&done[(W.inst * 4 + W.phase) * 2]), 1ull);
+      if (trace) {
+        unsigned sm;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+        trace[4 * it + 0] = t0;
+        trace[4 * it + 1] = t1;
+        trace[4 * it + 2] = global_ns();
+        trace[4 * it + 3] = sm;
+      }
     }
   }
 }
+
+static uint64_t* g_batch_trace = nullptr;
 
 __global__ void k_batch_init_gacc(const BatchInst* insts, int n_inst) {
   for (int i = blockIdx.y; i < n_inst; i += gridDim.y) {
@@ -466,7 +502,8 @@ extern "C" int tqpk_batch_describe_groupby(void* h_rec, const tqpk_groupby_spec*
   WsCursor c(d_ws, ws_bytes);
   I.gacc = c.take<uint64_t>((size_t)K * S->n_accs);
   I.range_count = c.take<int64_t>(ranges);
-  I.gb_mode = (prefer_private && K * S->n_accs * 8 * kBlock <= kBatchSmem) ? 1 : 3;
+  I.gb_mode = (prefer_private && K * S->n_accs * 8 * kBlock <= kBatchSmem) ? 1
+              : (K * S->n_accs * 8 <= kBatchSmem ? 2 : 3);
   I.n_out = n_out;
   for (int o = 0; o < n_out; ++o) {
     I.out_op[o] = h_out_ops[4 * o];
@@ -553,7 +590,7 @@ extern "C" int tqpk_batch_run(const void* d_insts, int32_t n_inst, const void* d
   timing_before(KID_BATCH, s);
   k_batch<<<grid, kBlock, kBatchSmem, s>>>(static_cast<const BatchInst*>(d_insts),
                                            static_cast<const WorkItem*>(d_items), n_items, ctl, ctl + 16,
-                                           reinterpret_cast<int*>(ctl + 1));
+                                           reinterpret_cast<int*>(ctl + 1), g_batch_trace);
   timing_after(KID_BATCH, s);
   TQPK_CHECK_LAUNCH();
   return TQPK_OK;
@@ -569,3 +606,12 @@ extern "C" int tqpk_batch_error(const void* d_ctl, int* h_err, tqpk_stream strea
 }
 
 extern "C" int32_t tqpk_batch_grid(void) { return num_sms() * 2; }
+
+// Per-item timeline for tuning: when d_trace is set (32 bytes per work item),
+// later tqpk_batch_run launches record for item i the global timer (ns) at
+// dequeue, after its dependency wait and at completion, and the SM id.
+// NULL turns it off.  A launch captured in a graph keeps the setting it had.
+extern "C" int tqpk_batch_set_trace(void* d_trace) {
+  g_batch_trace = static_cast<uint64_t*>(d_trace);
+  return TQPK_OK;
+}

@@ -1,0 +1,141 @@
+// dense.cu - resident key directories and dense slot tables.
+//
+// A dimension table joined on its primary key becomes a direct-address
+// directory over the key domain [key_min, key_min + slots): dir[key - min]
+// holds the row index (or a payload column such as the next hop's foreign
+// key).  Built once when the table is loaded, it stays in HBM and serves every
+// later join against that table: the per-query build predicate is evaluated
+// through the row index at probe time instead of being baked into the
+// directory.  This is the "built join table" of the reference's sort-based
+// join (operators/hashjoin.py:24-177 sorts the build keys on every call); the
+// directory replaces the sort + searchsorted for a unique key.
+//
+// The group tables these probes fill are dense too (one FP64 sum and one
+// count per directory slot), and tqpk_dense_topk turns such a table into the
+// k best groups without a host round trip: the warp-list top-k of topk.cuh,
+// ties to the smaller key, plus a device-side group count.
+//
+// tqpk_groupby_emit_async is the group-by emit stage without its host
+// synchronisation, for callers (the serving loop) that keep many queries in
+// flight and read the group count later from device memory.
+#include <algorithm>
+
+#include "topk.cuh"
+
+namespace tqpk {
+
+__global__ void __launch_bounds__(kBlock) k_dir_build(const __grid_constant__ tqpk_predicate P, const void* keys,
+                                                      int dt, const void* payload, int pdt, int64_t n, int64_t kmin,
+                                                      int64_t slots, int empty, int fail_value, int pvec,
+                                                      int* __restrict__ dir, int* err) {
+  const int64_t groups = (n + 3) >> 2;
+  const bool kvec = ((reinterpret_cast<uintptr_t>(keys) & 15u) == 0);
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r0 = g << 2;
+    const uint32_t live = n - r0 >= 4 ? 0xfu : ((1u << (n - r0)) - 1);
+    const uint32_t pass = P.n_insn ? eval_pred4(P, r0, n, pvec) : live;
+    int64_t x[4];
+    ld4_int(keys, dt, r0, n, kvec, x);
+    int64_t pl[4] = {r0, r0 + 1, r0 + 2, r0 + 3};
+    if (payload) ld4_int(payload, pdt, r0, n, false, pl);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (!((live >> j) & 1u)) break;
+      const int64_t slot = x[j] - kmin;
+      if (slot < 0 || slot >= slots) { set_error(err, TQPK_EINVAL); continue; }
+      // a payload outside int32, or equal to the empty marker, cannot name a key of the
+      // next (int32) domain: the row stays in the directory as a non-matching entry
+      const bool pl_ok = pl[j] >= (int64_t)INT32_MIN && pl[j] <= (int64_t)INT32_MAX && pl[j] != (int64_t)empty;
+      const int v = (((pass >> j) & 1u) && pl_ok) ? (int)pl[j] : fail_value;
+      if (atomicCAS(&dir[slot], empty, v) != empty) set_error(err, TQPK_EUNSUPPORTED);  // repeated key
+    }
+  }
+}
+
+__global__ void k_dir_fill(int* p, int64_t n, int v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+__global__ void k_dense_emit(const int64_t* idx, const int64_t* count, const double* sum, const unsigned* cnt,
+                             int64_t key_min, int k, int64_t* out_keys, double* out_vals, int64_t* out_cnts,
+                             int64_t* out_count, const unsigned long long* groups, int64_t* out_groups) {
+  const int64_t m = *count;
+  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+    if (j < m) {
+      out_keys[j] = key_min + idx[j];
+      out_vals[j] = __ldcg(&sum[idx[j]]);
+      if (out_cnts) out_cnts[j] = __ldcg(&cnt[idx[j]]);
+    }
+  }
+  if (threadIdx.x == 0) {
+    *out_count = m;
+    if (out_groups) *out_groups = (int64_t)*groups;
+  }
+}
+
+constexpr int kDenseMaxK = 256;
+
+}  // namespace tqpk
+
+using namespace tqpk;
+
+extern "C" int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64_t n, const tqpk_predicate* h_pred,
+                                    const void* d_payload, int32_t payload_dtype, int64_t key_min, int64_t slots,
+                                    int32_t empty, int32_t fail_value, int32_t* d_dir, int32_t* d_err,
+                                    tqpk_stream stream) {
+  if (n < 0 || slots < 1 || slots > (int64_t(1) << 31) || !d_dir || !d_err || (n > 0 && !d_keys)) return TQPK_EINVAL;
+  if (!is_int_dtype(key_dtype) || (d_payload && !is_int_dtype(payload_dtype))) return TQPK_EDTYPE;
+  if (!d_payload && n > (int64_t)INT32_MAX) return TQPK_EUNSUPPORTED;  // row indices travel as int32
+  if (fail_value == empty) return TQPK_EINVAL;
+  int rc = n > 0 ? check_pred(h_pred) : TQPK_OK;
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  TQPK_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int32_t), s));
+  k_dir_fill<<<grid_for(slots, 4), kBlock, 0, s>>>(d_dir, slots, empty);
+  TQPK_CHECK_LAUNCH();
+  if (n > 0) {
+    k_dir_build<<<grid_for((n + 3) / 4, 4), kBlock, 0, s>>>(*pred_or_empty(h_pred), d_keys, key_dtype, d_payload,
+                                                           payload_dtype, n, key_min, slots, empty, fail_value,
+                                                           pred_vec_ok(h_pred) ? 1 : 0, d_dir, d_err);
+    TQPK_CHECK_LAUNCH();
+  }
+  return TQPK_OK;
+}
+
+extern "C" size_t tqpk_dense_topk_workspace_bytes(int32_t k) {
+  k = std::max(1, std::min(k, kDenseMaxK));
+  return 1024 + align_up((size_t)k * 8, 256) + 2 * align_up((size_t)topk_grid_size() * k * 8, 256) + 1024;
+}
+
+extern "C" int tqpk_dense_topk(const double* d_sum, const uint32_t* d_cnt, int64_t slots, int64_t key_min, int32_t k,
+                               int32_t descending, void* d_ws, size_t ws_bytes, int64_t* d_out_keys,
+                               double* d_out_vals, int64_t* d_out_counts, int64_t* d_out_count,
+                               int64_t* d_out_groups, tqpk_stream stream) {
+  if (slots < 0 || k < 1 || k > kDenseMaxK || !d_ws || !d_out_keys || !d_out_vals || !d_out_count) return TQPK_EINVAL;
+  if (slots > 0 && (!d_sum || !d_cnt)) return TQPK_EINVAL;
+  if (ws_bytes < tqpk_dense_topk_workspace_bytes(k)) return TQPK_ENOMEM;
+  const int grid = topk_grid_size();
+  WsCursor c(d_ws, ws_bytes);
+  unsigned* hdr = c.take<unsigned>(64);
+  int64_t* top_idx = c.take<int64_t>(k);
+  uint64_t* cand_key = c.take<uint64_t>((size_t)grid * k);
+  int64_t* cand_idx = c.take<int64_t>((size_t)grid * k);
+  if (!cand_idx) return TQPK_ENOMEM;
+  unsigned* ticket = hdr;
+  unsigned long long* groups = reinterpret_cast<unsigned long long*>(hdr + 2);
+  int64_t* count = reinterpret_cast<int64_t*>(hdr + 4);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  TQPK_CUDA(cudaMemsetAsync(hdr, 0, 256, s));
+  DenseSumSource src{d_sum, reinterpret_cast<const unsigned*>(d_cnt), slots, descending ? 1 : 0};
+  TopkOut O{top_idx, count, cand_key, cand_idx, ticket, groups};
+  timing_before(KID_PIPE_TOPK, s);
+  int rc = topk_warp_launch(0, &src, k, grid, O, s);
+  timing_after(KID_PIPE_TOPK, s);
+  if (rc) return rc;
+  k_dense_emit<<<1, 256, 0, s>>>(top_idx, count, d_sum, reinterpret_cast<const unsigned*>(d_cnt), key_min, k,
+                                 d_out_keys, d_out_vals, d_out_counts, d_out_count, groups, d_out_groups);
+  TQPK_CHECK_LAUNCH();
+  return TQPK_OK;
+}

@@ -214,6 +214,12 @@ __global__ void k_count_groups(const uint64_t* cnt, int64_t K, unsigned long lon
   if ((threadIdx.x & 31) == 0 && local) atomicAdd(groups, (unsigned long long)local);
 }
 
+__global__ void k_count_one(unsigned long long* groups) { *groups = 1; }
+
+__global__ void k_groups_or_error(const int* err, const unsigned long long* groups, int64_t* out) {
+  *out = *err ? (int64_t)*err : (int64_t)*groups;
+}
+
 struct EmitOut {
   int n;
   int op[TQPK_MAX_ACCS];
@@ -491,6 +497,60 @@ extern "C" int tqpk_groupby_emit(const tqpk_groupby_spec* S, const tqpk_gb_plan*
   TQPK_CUDA(cudaMemcpyAsync(&err, ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
   TQPK_CUDA(cudaStreamSynchronize(s));
   return err ? err : TQPK_OK;
+}
+
+// tqpk_groupby_emit without a host synchronisation: the group count is
+// counted on the device and written to *d_groups_out (a negative status
+// there if the emit's look-back failed).  The output columns must hold
+// plan->slots rows (the largest possible group count).
+extern "C" int tqpk_groupby_emit_async(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, void* ws,
+                                       void* const* out_keys, int32_t n_out, const int32_t* ops,
+                                       void* const* out_cols, int64_t* d_groups_out, tqpk_stream stream) {
+  int rc = check_spec(S);
+  if (rc) return rc;
+  if (!plan || !ws || !d_groups_out || n_out < 0 || n_out > TQPK_MAX_ACCS) return TQPK_EINVAL;
+  if (plan->mode == TQPK_GB_HASH) return TQPK_EUNSUPPORTED;
+  EmitOut E;
+  E.n = n_out;
+  for (int o = 0; o < n_out; ++o) {
+    E.op[o] = ops[4 * o];
+    E.a[o] = ops[4 * o + 1];
+    E.b[o] = ops[4 * o + 2];
+    E.dt[o] = ops[4 * o + 3];
+    E.col[o] = out_cols[o];
+    if (E.a[o] < 0 || E.a[o] >= S->n_accs || !E.col[o] || !dtype_size(E.dt[o])) return TQPK_EINVAL;
+    if (E.op[o] == TQPK_OUT_AVG && (E.b[o] < 0 || E.b[o] >= S->n_accs)) return TQPK_EINVAL;
+  }
+  for (int k = 0; k < S->n_keys; ++k) {
+    if (!out_keys[k]) return TQPK_EINVAL;
+    E.key[k] = out_keys[k];
+    E.key_dt[k] = S->key_dtypes[k];
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int64_t K = plan->slots, A = S->n_accs;
+  char* base = static_cast<char*>(ws);
+  unsigned long long* d_groups = reinterpret_cast<unsigned long long*>(base);
+  uint64_t* gacc = reinterpret_cast<uint64_t*>(base + 512);
+  void* cws = base + 512 + align_up((size_t)(K * A * 8), 256);
+  const int64_t tiles = (K + kTile - 1) / kTile;
+  WsCursor cur(cws, compact_status_bytes(K));
+  int* ctl = cur.take<int>(64);
+  uint64_t* status = cur.take<uint64_t>(tiles);
+  if (!ctl || !status) return TQPK_ENOMEM;
+  TQPK_CUDA(cudaMemsetAsync(cws, 0, cur.off, s));
+  TQPK_CUDA(cudaMemsetAsync(d_groups, 0, 8, s));
+  if (S->n_keys == 0) {
+    k_count_one<<<1, 1, 0, s>>>(d_groups);
+  } else {
+    k_count_groups<<<grid_for(K, 4), kBlock, 0, s>>>(gacc, K, d_groups);
+  }
+  TQPK_CHECK_LAUNCH();
+  const GbDev G = to_dev(*plan, S->n_keys);
+  k_emit_dense<<<(int)tiles, kBlock, 0, s>>>(*S, G, gacc, S->n_keys == 0 ? 1 : 0, E, status, ctl, ctl + 1);
+  TQPK_CHECK_LAUNCH();
+  k_groups_or_error<<<1, 1, 0, s>>>(ctl + 1, d_groups, d_groups_out);
+  TQPK_CHECK_LAUNCH();
+  return TQPK_OK;
 }
 
 // Stages of tqpk_groupby_run for callers that launch their own accumulation

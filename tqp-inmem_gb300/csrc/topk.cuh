@@ -89,15 +89,44 @@ struct DenseSumSource {
   const unsigned* cnt;   // occupancy: non-zero for groups that received a row
   int64_t n;
   int desc;
-  __device__ __forceinline__ bool get(int64_t i, uint64_t& k) const {
-    if (i >= n || __ldcg(&cnt[i]) == 0) return false;   // L2 loads: the table may have been written
-    double v = __ldcg(&sum[i]);                          // earlier in the same launch by other CTAs
+  __device__ __forceinline__ uint64_t order_key(double v) const {
     if (v == 0.0) v = 0.0;
     uint64_t b = d2u(v);
     if (isnan(v)) b = 0x7ff8000000000000ull;
     const uint64_t u = (b & (1ull << 63)) ? ~b : (b | (1ull << 63));
-    k = desc ? ~u : u;
+    return desc ? ~u : u;
+  }
+  __device__ __forceinline__ bool get(int64_t i, uint64_t& k) const {
+    if (i >= n || __ldcg(&cnt[i]) == 0) return false;   // L2 loads: the table may have been written
+    k = order_key(__ldcg(&sum[i]));                      // earlier in the same launch by other CTAs
     return true;
+  }
+  // Slots i0..i0+3 (i0 % 4 == 0): the occupancy and sum loads are issued
+  // together (16-byte vectors when aligned), so a warp keeps 3 independent
+  // loads per lane in flight instead of two dependent ones per slot.
+  __device__ __forceinline__ unsigned get4(int64_t i0, uint64_t* k) const {
+    unsigned c[4];
+    double v[4];
+    if (i0 + 4 <= n && ((reinterpret_cast<uintptr_t>(cnt) | reinterpret_cast<uintptr_t>(sum)) & 15u) == 0) {
+      const uint4 cc = __ldcg(reinterpret_cast<const uint4*>(cnt + i0));
+      const double2 a = __ldcg(reinterpret_cast<const double2*>(sum + i0));
+      const double2 b = __ldcg(reinterpret_cast<const double2*>(sum + i0 + 2));
+      c[0] = cc.x; c[1] = cc.y; c[2] = cc.z; c[3] = cc.w;
+      v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        c[q] = (i0 + q < n) ? __ldcg(&cnt[i0 + q]) : 0u;
+        v[q] = (i0 + q < n) ? __ldcg(&sum[i0 + q]) : 0.0;
+      }
+    }
+    unsigned ok = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      k[q] = order_key(v[q]);
+      ok |= (c[q] != 0u ? 1u : 0u) << q;
+    }
+    return ok;
   }
 };
 
@@ -109,6 +138,12 @@ struct ArraySource {
   int64_t n;
   int desc;
   __device__ __forceinline__ bool get(int64_t i, uint64_t& k) const;
+  __device__ __forceinline__ unsigned get4(int64_t i0, uint64_t* k) const {
+    unsigned ok = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ok |= (get(i0 + q, k[q]) ? 1u : 0u) << q;
+    return ok;
+  }
 };
 
 struct TopkOut {
@@ -129,14 +164,16 @@ __global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   WarpList<R> L;
   L.init();
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
   unsigned valid = 0;
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + warp * 32; base < src.n; base += stride) {
-    const int64_t i = base + lane;
-    uint64_t key = ~0ull;
-    const bool ok = src.get(i, key);
-    valid += ok;
-    L.offer(k, key, i, ok);
+  // four consecutive items per lane per step; the warp offers them in four rounds
+  for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + warp * 32) * 4; base < src.n; base += stride) {
+    const int64_t i0 = base + lane * 4;
+    uint64_t key[4];
+    const unsigned ok = src.get4(i0, key);
+    valid += __popc(ok);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) L.offer(k, key[q], i0 + q, (ok >> q) & 1u);
   }
   valid = __reduce_add_sync(0xffffffffu, valid);
   if (lane == 0 && valid && O.valid_total) atomicAdd(O.valid_total, (unsigned long long)valid);

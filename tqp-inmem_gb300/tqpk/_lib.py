@@ -107,6 +107,7 @@ SIGNATURES = {
     "tqpk_batch_run": (C.c_int, [_VP, _I32, _VP, _I32, _VP, _I32, _VP]),
     "tqpk_batch_error": (C.c_int, [_VP, _P(C.c_int), _VP]),
     "tqpk_batch_grid": (_I32, []),
+    "tqpk_batch_set_trace": (C.c_int, [_VP]),
     "tqpk_jit_available": (C.c_int, []),
     "tqpk_jit_check": (C.c_int, [C.c_char_p, C.c_char_p, _SZ]),
     "tqpk_jit_compile": (C.c_int, [C.c_char_p, C.c_char_p, _P(_VP), C.c_char_p, _SZ]),
@@ -120,6 +121,12 @@ SIGNATURES = {
                                                      _P(Predicate), _P(GroupbySpec), _I32, _I32, _I32, _VP, _SZ, _VP,
                                                      _VP, _VP, _VP, _VP]),
     "tqpk_pipeline_join_tables": (C.c_int, [_VP, _SZ, _I64, _I64, _P(_VP), _P(_VP), _P(_VP)]),
+    "tqpk_directory_build": (C.c_int, [_VP, _I32, _I64, _P(Predicate), _VP, _I32, _I64, _I64, _I32, _I32, _VP, _VP,
+                                       _VP]),
+    "tqpk_dense_topk_workspace_bytes": (_SZ, [_I32]),
+    "tqpk_dense_topk": (C.c_int, [_VP, _VP, _I64, _I64, _I32, _I32, _VP, _SZ, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "tqpk_groupby_emit_async": (C.c_int, [_P(GroupbySpec), _P(GbPlan), _VP, _P(_VP), _I32, _P(_I32), _P(_VP), _VP,
+                                          _VP]),
     "tqpk_compact_noalloc_max_rows": (_I64, []),
     "tqpk_compact_noalloc": (C.c_int, [_P(Predicate), _VP, _I64, _I32, _P(_VP), _P(_I32), _P(_VP), _VP, _VP]),
     "tqpk_timing_begin": (C.c_int, [_I32]),

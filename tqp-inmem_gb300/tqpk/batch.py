@@ -139,6 +139,7 @@ class Batch:
         got = self.lib.tqpk_batch_items(C.addressof(self.h_recs), n, C.addressof(h_items), need)
         assert got == need
         self.n_items = int(need)
+        self.h_items = bytes(h_items)
         self.d_recs = torch.frombuffer(bytearray(self.h_recs), dtype=torch.uint8).to(self.dev)
         self.d_items = torch.frombuffer(bytearray(h_items), dtype=torch.uint8).to(self.dev)
         self.ctl = torch.zeros(self.lib.tqpk_batch_ctl_bytes(n), dtype=torch.uint8, device=self.dev)
@@ -222,6 +223,30 @@ class Batch:
 
     def replay(self):
         self.graph.replay()
+
+    def item_timeline(self) -> np.ndarray:
+        """Runs the batch once (outside any graph) with the per-item timeline on.
+
+        Returns a structured array, one row per work item: inst, phase, begin, end
+        (rows or slots), and dequeue / dependency-met / completion times in
+        microseconds from the first dequeue, plus the SM id."""
+        tr = torch.zeros(self.n_items * 4, dtype=torch.int64, device=self.dev)
+        L.check(self.lib.tqpk_batch_set_trace(tr.data_ptr()), "tqpk_batch_set_trace")
+        try:
+            self.run()
+            torch.cuda.synchronize()
+        finally:
+            self.lib.tqpk_batch_set_trace(None)
+        t = tr.cpu().numpy().reshape(-1, 4)
+        it = np.frombuffer(self.h_items, dtype=[("inst", "<i4"), ("phase", "<i4"), ("begin", "<i8"), ("end", "<i8")])
+        out = np.zeros(self.n_items, dtype=[("inst", "i4"), ("phase", "i4"), ("begin", "i8"), ("end", "i8"),
+                                            ("t_deq", "f8"), ("t_ready", "f8"), ("t_done", "f8"), ("sm", "i4")])
+        for f in ("inst", "phase", "begin", "end"):
+            out[f] = it[f]
+        t0 = t[:, 0].min()
+        out["t_deq"], out["t_ready"], out["t_done"] = (t[:, 0] - t0) / 1e3, (t[:, 1] - t0) / 1e3, (t[:, 2] - t0) / 1e3
+        out["sm"] = t[:, 3]
+        return out
 
     def check_error(self):
         err = C.c_int(0)

@@ -43,6 +43,8 @@ __device__ __forceinline__ bool iscl(double x, double lit, double allowed) {
   double e = fabs(__dsub_rn(x, lit));
   return (x == lit) || (isfinite(e) && e <= allowed);
 }
+// predicate literals, bound at launch (one compiled kernel serves every constant)
+struct PL { long long i[32]; double f[32]; double a[32]; };
 template <class T> struct V4 { T v[4]; };
 // four consecutive rows r0..r0+3 (r0 % 4 == 0); rows >= n read as 0
 __device__ __forceinline__ V4<double> ld4(const double* p, i64 r0, i64 n, bool vec) {
@@ -117,6 +119,7 @@ def run_groupby(spec, pred, plan, ws, n: int, stream: int, pred_tensors=(), key_
     if pred is not None:
         for c in range(pred.struct.n_cols):
             a.ptr(pred.struct.cols[c])
+    a.blob(pred_lits(pred.struct if pred is not None else None))
     for k in range(spec.n_keys):
         a.ptr(spec.keys[k])
     for c in range(spec.n_cols):
@@ -137,11 +140,6 @@ def probe_supported(fk_dtype_code: int) -> bool:
 def _hexf(x: float) -> str:
     return f"({float(x).hex()})" if x == x and abs(x) != float("inf") else (
         "__longlong_as_double(0x%016xLL)" % struct.unpack("<Q", struct.pack("<d", x))[0])
-
-
-def _hexf32(x: float) -> str:
-    import numpy as np
-    return "__int_as_float(0x%08x)" % struct.unpack("<I", struct.pack("<f", np.float32(x)))[0]
 
 
 def check_compiles(src: str) -> Tuple[bool, str]:
@@ -166,11 +164,28 @@ def compile_kernel(src: str, name: str) -> int:
         return handle.value
 
 
+class PredLits(C.Structure):
+    """The literals of a predicate program (struct PL of the generated code)."""
+    _fields_ = [("i", C.c_int64 * 32), ("f", C.c_double * 32), ("a", C.c_double * 32)]
+
+
+def pred_lits(P) -> PredLits:
+    out = PredLits()
+    if P is not None:
+        for k in range(P.n_insn):
+            out.i[k], out.f[k], out.a[k] = P.insn[k].lit_i, P.insn[k].lit_f, P.insn[k].lit_aux
+    return out
+
+
 class _Args:
     """Kernel parameters for cudaLaunchKernel (keeps the ctypes values alive)."""
 
     def __init__(self):
         self.vals: List = []
+
+    def blob(self, v):
+        """A by-value struct parameter (a ctypes Structure)."""
+        self.vals.append(v)
 
     def ptr(self, p):
         self.vals.append(C.c_void_p(p))
@@ -201,8 +216,12 @@ def occupancy_grid(handle: int, block: int, smem: int, work_units: int) -> int:
 
 
 # ---------------------------------------------------------------------------- code pieces
-def _pred_code(P, prefix: str) -> Tuple[List[int], str]:
-    """Boolean C++ expression of row j for a tqpk_predicate; returns (column slots used, code)."""
+def _pred_code(P, prefix: str, lits: str = "lp") -> Tuple[List[int], str]:
+    """Boolean C++ expression of row j for a tqpk_predicate; returns (column slots used, code).
+
+    Comparison literals are read from the kernel's PL parameter `lits`
+    (instruction k's literal at index k), so the compiled kernel depends on
+    the predicate's shape only and each launch binds its own constants."""
     st: List[str] = []
     used = set()
     for k in range(P.n_insn):
@@ -212,14 +231,14 @@ def _pred_code(P, prefix: str) -> Tuple[List[int], str]:
             x = f"{prefix}{I.col}.v[j]"
             dt = P.dtypes[I.col]
             if I.cmp == L.ISCLOSE:
-                st.append(f"iscl({x}, {_hexf(I.lit_f)}, {_hexf(I.lit_aux)})")
+                st.append(f"iscl({x}, {lits}.f[{k}], {lits}.a[{k}])")
             elif I.domain == L.DOM_F64:
                 xx = x if dt == L.F64 else f"(double){x}"
-                st.append(f"({xx} {_CMP_OP[I.cmp]} {_hexf(I.lit_f)})")
+                st.append(f"({xx} {_CMP_OP[I.cmp]} {lits}.f[{k}])")
             elif I.domain == L.DOM_F32:
-                st.append(f"((float){x} {_CMP_OP[I.cmp]} {_hexf32(I.lit_f)})")
+                st.append(f"((float){x} {_CMP_OP[I.cmp]} __double2float_rn({lits}.f[{k}]))")
             else:
-                st.append(f"((i64){x} {_CMP_OP[I.cmp]} ({I.lit_i}LL))")
+                st.append(f"((i64){x} {_CMP_OP[I.cmp]} {lits}.i[{k}])")
         elif I.op == L.P_CMPCOL:
             used.add(I.col)
             used.add(int(I.lit_i))
@@ -324,23 +343,29 @@ def groupby_source(spec, pred, plan) -> Tuple[str, str, int, int]:
     S = spec
     A, K = S.n_accs, int(plan.slots)
     private = plan.mode in (L.GB_DENSE_PRIVATE, L.GB_GLOBAL_ONE)
+    shared = plan.mode == L.GB_DENSE_SHARED          # one table per CTA, shared-memory atomics
     T = int(plan.threads) if private else 256
-    smem = K * A * 8 * T if private else 0
+    smem = K * A * 8 * T if private else (K * A * 8 if shared else 0)
     pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
     ecols, elines = _expr_code(S, S.n_expr, "c")
     kcols = list(range(S.n_keys))
     name = "tqpk_q_groupby"
     src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__({T}) {name}(']
     params = [f"const void* __restrict__ pp{c}" for c in range(pred.n_cols if pred is not None else 0)]
+    params += ["const PL lp"]
     params += [f"const void* __restrict__ kp{k}" for k in kcols]
     params += [f"const void* __restrict__ cp{c}" for c in range(S.n_cols)]
     params += ["i64 n", "u64* __restrict__ gacc", "int vp", "int vk", "int vc"]
     src.append("    " + ",\n    ".join(params) + ") {")
     src.append(f"  constexpr int T = {T}; constexpr int A = {A}; constexpr i64 K = {K}LL;")
+    inits = " : ".join(f"(a == {i}) ? {_acc_init(S.accs[i])}" for i in range(A)) + " : 0ull"
     if private:
         src.append("  extern __shared__ u64 sm[];")
-        inits = " : ".join(f"(a == {i}) ? {_acc_init(S.accs[i])}" for i in range(A)) + " : 0ull"
         src.append(f"  for (i64 i = threadIdx.x; i < K * A * T; i += T) {{ const int a = (int)((i / T) % A); sm[i] = {inits}; }}")
+        src.append("  __syncthreads();")
+    elif shared:
+        src.append("  extern __shared__ u64 sm[];")
+        src.append(f"  for (i64 i = threadIdx.x; i < K * A; i += T) {{ const int a = (int)(i % A); sm[i] = {inits}; }}")
         src.append("  __syncthreads();")
     src.append("  const i64 groups = (n + 3) >> 2;")
     src.append("  for (i64 g = blockIdx.x * (i64)T + threadIdx.x; g < groups; g += (i64)gridDim.x * T) {")
@@ -362,6 +387,8 @@ def groupby_source(spec, pred, plan) -> Tuple[str, str, int, int]:
         if private:
             cell = f"sm[(slot * A + {a}) * T + threadIdx.x]"
             src.append(f"      {cell} = {_combine(acc, cell, v)};")
+        elif shared:
+            src.append("      " + _merge_atomic(acc, f"&sm[slot * A + {a}]", v))
         else:
             src.append("      " + _merge_atomic(acc, f"&gacc[{a} * K + slot]", v))
     src.append("    }")
@@ -384,6 +411,16 @@ def groupby_source(spec, pred, plan) -> Tuple[str, str, int, int]:
             src.append("      break; }")
         src.append("    }")
         src.append("  }")
+    elif shared:
+        src.append("  __syncthreads();")
+        src.append("  for (i64 c = threadIdx.x; c < K * A; c += T) {")
+        src.append("    const int a = (int)(c % A); const i64 s = c / A; const u64 v = sm[c];")
+        src.append("    switch (a) {")
+        for a in range(A):
+            acc = S.accs[a]
+            src.append(f"    case {a}: if (v != {_acc_init(acc)}) {_merge_atomic(acc, f'&gacc[{a} * K + s]', 'v')} break;")
+        src.append("    }")
+        src.append("  }")
     src.append("}")
     return "\n".join(src), name, T, smem
 
@@ -395,14 +432,71 @@ def _rename(code: str, old_prefix: str, new_prefix: str) -> str:
 
 
 # ---------------------------------------------------------------------------- fused join probe
-def join_probe_source(spec, val_reg: int, pred) -> Tuple[str, str]:
-    """CUDA source of the fused probe + aggregate (directory lookup, value, FP64 sum, occupancy)."""
+def _gather_pred(pred, prefix: str, lits: str, ptr_pfx: str, row: str, live: str) -> Tuple[List[str], str]:
+    """A predicate over dimension columns read through a row index (row[j], j live):
+    (statements declaring the V4 tiles, boolean expression of row j)."""
+    cols, expr = _pred_code(pred, prefix, lits)
+    lines = []
+    for c in cols:
+        t = _CTYPE[pred.dtypes[c]]
+        lines.append(f"V4<{t}> G{prefix}{c};")
+        lines.append(f"for (int j = 0; j < 4; ++j) G{prefix}{c}.v[j] = (({live} >> j) & 1u) ? "
+                     f"__ldg((const {t}*){ptr_pfx}{c} + {row}[j]) : ({t})0;")
+    return lines, _rename(expr, prefix, "G" + prefix)
+
+
+def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[str]) -> List[str]:
+    """Warp-dense value pass: the warp's matched rows (queued as row offsets and
+    slots in shared memory) are spread over all 32 lanes, so each FP64
+    instruction and atomic runs with full lanes instead of the ~1 in 4 a
+    row-per-lane loop leaves active after the predicate and the lookups."""
+    import re
+    lines = ["    const unsigned nm = __popc(m[0]) + __popc(m[1]);",
+             "    unsigned incl = nm;",
+             "#pragma unroll",
+             "    for (int o = 1; o < 32; o <<= 1) { const unsigned t = __shfl_up_sync(0xffffffffu, incl, o); "
+             "if (lane >= o) incl += t; }",
+             "    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);",
+             "    unsigned pos = incl - nm;",
+             "#pragma unroll",
+             "    for (int u = 0; u < 2; ++u)",
+             "#pragma unroll",
+             "      for (int j = 0; j < 4; ++j)",
+             f"        if ((m[u] >> j) & 1u) {{ q_off[wid][pos] = (unsigned char)(lane * 8 + u * 4 + j); "
+             f"q_slot[wid][pos] = (int){key}[u][j]; ++pos; }}",
+             "    __syncwarp();",
+             "    for (unsigned i = lane; i < total; i += 32) {",
+             "      const i64 row = wrow + q_off[wid][i];",
+             "      const i64 slot = q_slot[wid][i];"]
+    for c in ecols:
+        t = _CTYPE[S.col_dtypes[c]]
+        lines.append(f"      const {t} Cs{c} = __ldg((const {t}*)cp{c} + row);")
+    for l in elines:
+        lines.append("      " + re.sub(r"\bc(\d+)\.v\[j\]", r"Cs\1", l))
+    lines.append(f"      atomicAdd(&sum[slot], (double)r{val_reg});")
+    lines += ["      " + x for x in extra]
+    lines += ["    }", "    __syncwarp();"]
+    return lines
+
+
+def join_probe_source(spec, val_reg: int, pred, bpred=None) -> Tuple[str, str]:
+    """CUDA source of the fused probe + aggregate (directory lookup, value, FP64 sum, occupancy).
+
+    The directory holds build row indices (negative = no row).  `bpred`, when
+    given, is a predicate over build-side columns evaluated through the row
+    index (a resident directory serving queries with their own build filter).
+    Each lane filters and looks up 8 consecutive rows (4-row vector loads); the
+    warp then computes the value and updates the group of its matched rows
+    densely (_dense_tail)."""
     S = spec
     pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
     ecols, elines = _expr_code(S, val_reg + 1, "c")
-    vt = "double" if S.expr[val_reg].type == L.F64 else "i64"
     name = "tqpk_q_join_probe"
     params = [f"const void* __restrict__ pp{c}" for c in range(pred.n_cols if pred is not None else 0)]
+    params += ["const PL lp"]
+    if bpred is not None:
+        params += [f"const void* __restrict__ bp{c}" for c in range(bpred.n_cols)]
+        params += ["const PL lb"]
     params += [f"const void* __restrict__ cp{c}" for c in range(S.n_cols)]
     params += ["const void* __restrict__ fk", "int fk_dt", "i64 np", "i64 key_min", "i64 slots",
                "const int* __restrict__ dir", "double* __restrict__ sum", "u32* __restrict__ occ",
@@ -411,9 +505,14 @@ def join_probe_source(spec, val_reg: int, pred) -> Tuple[str, str]:
                "[&]{ V4<int> t = ld4((const int*)fk, r0, np, vf != 0); V4<i64> o; "
                "for (int q = 0; q < 4; ++q) o.v[q] = t.v[q]; return o; }();")
     src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__(256) {name}(', "    " + ",\n    ".join(params) + ") {",
+           "  __shared__ unsigned char q_off[8][256];",
+           "  __shared__ int q_slot[8][256];",
+           "  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;",
            "  const i64 n8 = (np + 7) >> 3;",
-           "  for (i64 g = blockIdx.x * (i64)blockDim.x + threadIdx.x; g < n8; g += (i64)gridDim.x * blockDim.x) {",
-           "    i64 sl[2][4]; unsigned m[2];",
+           "  const i64 stride = (i64)gridDim.x * blockDim.x;",
+           "  for (i64 w0 = blockIdx.x * (i64)blockDim.x + (threadIdx.x & ~31); w0 < n8; w0 += stride) {",
+           "    const i64 g = w0 + lane, wrow = w0 << 3;",
+           "    i64 sl[2][4]; int rw[2][4]; unsigned m[2];",
            "#pragma unroll",
            "    for (int u = 0; u < 2; ++u) {",
            "      const i64 r0 = ((g << 1) + u) << 2;",
@@ -431,15 +530,125 @@ def join_probe_source(spec, val_reg: int, pred) -> Tuple[str, str]:
             "#pragma unroll",
             "    for (int u = 0; u < 2; ++u)",
             "#pragma unroll",
-            "      for (int j = 0; j < 4; ++j)",
-            "        if (((m[u] >> j) & 1u) && __ldg(&dir[sl[u][j]]) < 0) m[u] &= ~(1u << j);",
+            "      for (int j = 0; j < 4; ++j) {",
+            "        rw[u][j] = ((m[u] >> j) & 1u) ? __ldg(&dir[sl[u][j]]) : -1;",
+            "        if (rw[u][j] < 0) m[u] &= ~(1u << j);",
+            "      }"]
+    if bpred is not None:
+        glines, gexpr = _gather_pred(bpred, "b", "lb", "bp", "rw[u]", "m[u]")
+        src += ["#pragma unroll", "    for (int u = 0; u < 2; ++u) {", "      if (!m[u]) continue;"]
+        src += ["      " + l for l in glines]
+        src += ["#pragma unroll", "      for (int j = 0; j < 4; ++j)",
+                f"        if (((m[u] >> j) & 1u) && !({gexpr})) m[u] &= ~(1u << j);", "    }"]
+    src += _dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"])
+    src += ["  }", "}"]
+    return "\n".join(src), name
+
+
+def join_probe_args(a: "_Args", spec, pred, bpred, fk, np_: int, key_min: int, slots: int, dir_ptr: int,
+                    sum_ptr: int, occ_ptr: int, pred_tensors=(), bpred_tensors=(), col_tensors=()):
+    """Parameters of join_probe_source's kernel, in order."""
+    if pred is not None:
+        for c in range(pred.n_cols):
+            a.ptr(pred.cols[c])
+    a.blob(pred_lits(pred))
+    if bpred is not None:
+        for c in range(bpred.n_cols):
+            a.ptr(bpred.cols[c])
+        a.blob(pred_lits(bpred))
+    for c in range(spec.n_cols):
+        a.ptr(spec.cols[c])
+    a.ptr(fk.data_ptr())
+    a.i32(L.I64 if fk.dtype.itemsize == 8 else L.I32)
+    a.i64(np_)
+    a.i64(key_min)
+    a.i64(slots)
+    a.ptr(dir_ptr)
+    a.ptr(sum_ptr)
+    a.ptr(occ_ptr)
+    a.i32(_aligned(*pred_tensors) if pred is not None else 1)
+    a.i32(_aligned(*col_tensors))
+    a.i32(_aligned(fk))
+    return a
+
+
+# ---------------------------------------------------------------------------- star probe
+def star_probe_source(spec, val_reg: int, fpred, apred) -> Tuple[str, str]:
+    """CUDA source of the star probe: fact -> A (row directory, A predicate through the
+    row) -> B (directory of the C foreign key) -> C (row directory), then FP64 sum and
+    count per C slot, computed warp-densely over the matched rows (_dense_tail).
+    Directories: A and C hold row indices (negative = none), B holds the C key
+    (INT_MIN = none)."""
+    S = spec
+    pcols, pexpr = _pred_code(fpred, "p") if fpred is not None else ([], "true")
+    ecols, elines = _expr_code(S, val_reg + 1, "c")
+    name = "tqpk_q_star_probe"
+    params = [f"const void* __restrict__ pp{c}" for c in range(fpred.n_cols if fpred is not None else 0)]
+    params += ["const PL lp"]
+    if apred is not None:
+        params += [f"const void* __restrict__ ap{c}" for c in range(apred.n_cols)]
+        params += ["const PL la"]
+    params += [f"const void* __restrict__ cp{c}" for c in range(S.n_cols)]
+    params += ["const int* __restrict__ fka", "const int* __restrict__ fkb", "i64 nf",
+               "i64 a_min", "i64 a_slots", "const int* __restrict__ dir_a",
+               "i64 b_min", "i64 b_slots", "const int* __restrict__ dir_b",
+               "i64 c_min", "i64 c_slots", "const int* __restrict__ dir_c",
+               "double* __restrict__ sum", "u32* __restrict__ cnt", "int vp", "int vc", "int vf"]
+    src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__(256) {name}(', "    " + ",\n    ".join(params) + ") {",
+           "  __shared__ unsigned char q_off[8][256];",
+           "  __shared__ int q_slot[8][256];",
+           "  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;",
+           "  const i64 n8 = (nf + 7) >> 3;",
+           "  const i64 stride = (i64)gridDim.x * blockDim.x;",
+           "  for (i64 w0 = blockIdx.x * (i64)blockDim.x + (threadIdx.x & ~31); w0 < n8; w0 += stride) {",
+           "    const i64 g = w0 + lane, wrow = w0 << 3;",
+           "    i64 k[2][4]; int rw[2][4]; unsigned m[2];",
+           "#pragma unroll",
+           "    for (int u = 0; u < 2; ++u) {",
+           "      const i64 r0 = ((g << 1) + u) << 2;",
+           "      m[u] = 0;",
+           "      if (r0 >= nf) continue;"]
+    src += ["      " + l for l in _load_lines(pcols, fpred.dtypes, "P", "pp", "nf", "vp != 0")] if fpred is not None else []
+    src += ["      const V4<int> FA = ld4(fka, r0, nf, vf != 0);",
             "#pragma unroll",
+            "      for (int j = 0; j < 4; ++j) {",
+            "        k[u][j] = (i64)FA.v[j] - a_min;",
+            f"        const bool ok = (r0 + j < nf) && ({_rename(pexpr, 'p', 'P')}) && k[u][j] >= 0 && k[u][j] < a_slots;",
+            "        m[u] |= (unsigned)ok << j;",
+            "      }",
+            "    }",
+            "#pragma unroll",
+            "    for (int u = 0; u < 2; ++u)",
+            "#pragma unroll",
+            "      for (int j = 0; j < 4; ++j) {",
+            "        rw[u][j] = ((m[u] >> j) & 1u) ? __ldg(&dir_a[k[u][j]]) : -1;",
+            "        if (rw[u][j] < 0) m[u] &= ~(1u << j);",
+            "      }"]
+    if apred is not None:
+        glines, gexpr = _gather_pred(apred, "a", "la", "ap", "rw[u]", "m[u]")
+        src += ["#pragma unroll", "    for (int u = 0; u < 2; ++u) {", "      if (!m[u]) continue;"]
+        src += ["      " + l for l in glines]
+        src += ["#pragma unroll", "      for (int j = 0; j < 4; ++j)",
+                f"        if (((m[u] >> j) & 1u) && !({gexpr})) m[u] &= ~(1u << j);", "    }"]
+    src += ["#pragma unroll",
             "    for (int u = 0; u < 2; ++u) {",
             "      if (!m[u]) continue;",
-            "      const i64 r0 = ((g << 1) + u) << 2;"]
-    src += ["      " + l for l in _load_lines(ecols, S.col_dtypes, "Cv", "cp", "np", "vc != 0")]
-    src += ["#pragma unroll", "      for (int j = 0; j < 4; ++j) {", "        if (!((m[u] >> j) & 1u)) continue;"]
-    src += ["        " + _rename(l, "c", "Cv") for l in elines]
-    src += [f"        atomicAdd(&sum[sl[u][j]], (double)r{val_reg});", "        occ[sl[u][j]] = 1u;",
-            "      }", "    }", "  }", "}"]
+            "      const i64 r0 = ((g << 1) + u) << 2;",
+            "      const V4<int> FB = ld4(fkb, r0, nf, vf != 0);",
+            "#pragma unroll",
+            "      for (int j = 0; j < 4; ++j) {",
+            "        const i64 sb = (i64)FB.v[j] - b_min;",
+            "        const bool ok = ((m[u] >> j) & 1u) && sb >= 0 && sb < b_slots;",
+            "        const int fc = ok ? __ldg(&dir_b[sb]) : (int)0x80000000;",
+            "        k[u][j] = (i64)fc - c_min;",
+            "        if (fc == (int)0x80000000 || k[u][j] < 0 || k[u][j] >= c_slots) m[u] &= ~(1u << j);",
+            "      }",
+            "    }",
+            "#pragma unroll",
+            "    for (int u = 0; u < 2; ++u)",
+            "#pragma unroll",
+            "      for (int j = 0; j < 4; ++j)",
+            "        if (((m[u] >> j) & 1u) && __ldg(&dir_c[k[u][j]]) < 0) m[u] &= ~(1u << j);"]
+    src += _dense_tail(S, val_reg, ecols, elines, "nf", "k", ["atomicAdd(&cnt[slot], 1u);"])
+    src += ["  }", "}"]
     return "\n".join(src), name

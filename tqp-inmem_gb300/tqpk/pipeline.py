@@ -73,24 +73,10 @@ class JoinAggTopK:
             L.check(self.lib.tqpk_pipeline_join_tables(self.ws.data_ptr(), self.ws.numel(), self.key_min,
                                                        self.key_max, C.byref(d), C.byref(su), C.byref(oc)),
                     "tqpk_pipeline_join_tables")
-            a = jit._Args()
-            if self.ppred:
-                for c in range(self.ppred.struct.n_cols):
-                    a.ptr(self.ppred.struct.cols[c])
-            for c in range(self.prog.spec.n_cols):
-                a.ptr(self.prog.spec.cols[c])
-            a.ptr(self.pk.data_ptr())
-            a.i32(code_of(self.pk.dtype))
-            a.i64(self.pk.numel())
-            a.i64(self.key_min)
-            a.i64(self.key_max - self.key_min + 1)
-            a.ptr(d.value)
-            a.ptr(su.value)
-            a.ptr(oc.value)
-            a.i32(jit._aligned(*self.ppred.tensors) if self.ppred else 1)
-            a.i32(jit._aligned(*self.prog.tensors))
-            a.i32(jit._aligned(self.pk))
-            self._probe_args = a
+            self._probe_args = jit.join_probe_args(
+                jit._Args(), self.prog.spec, self.ppred.struct if self.ppred else None, None, self.pk,
+                self.pk.numel(), self.key_min, self.key_max - self.key_min + 1, d.value, su.value, oc.value,
+                pred_tensors=self.ppred.tensors if self.ppred else (), col_tensors=self.prog.tensors)
             self._probe_grid = jit.occupancy_grid(self._probe_handle, 256, 0, (self.pk.numel() + 7) // 8)
         jit.launch(self._probe_handle, self._probe_grid, 256, 0, self._probe_args, s, L.KID_PIPE_PROBE)
 
@@ -152,8 +138,83 @@ class StarAggTopK:
     def workspace_bytes(self) -> int:
         return int(self.ws.numel())
 
+    def _jit_ok(self) -> bool:
+        from . import jit
+        fa, fb, ak, bk, bc, ck = self.t
+        cmn, cmx = self.doms[2]
+        return (jit.available() and fa.numel() > 0 and fa.dtype == torch.int32 and fb.dtype == torch.int32
+                and all(x.numel() > 0 for x in (ak, bk, ck)) and cmn > -(1 << 31) + 1 and cmx < (1 << 31))
+
+    def _jit_setup(self):
+        """Tables of the generated-probe path: row directories for A (its filter applied
+        at build) and C, the C-key directory for B, the slot table and top-k scratch."""
+        from . import jit
+        (amn, amx), (bmn, bmx), (cmn, cmx) = self.doms
+        dev = self.dev
+        self.dir_a = torch.empty(amx - amn + 1, dtype=torch.int32, device=dev)
+        self.dir_b = torch.empty(bmx - bmn + 1, dtype=torch.int32, device=dev)
+        self.dir_c = torch.empty(cmx - cmn + 1, dtype=torch.int32, device=dev)
+        self.sum = torch.empty(cmx - cmn + 1, dtype=torch.float64, device=dev)
+        self.cnt = torch.empty(cmx - cmn + 1, dtype=torch.int32, device=dev)
+        self.err = torch.zeros(3, dtype=torch.int32, device=dev)
+        self.tws = torch.empty(self.lib.tqpk_dense_topk_workspace_bytes(self.k), dtype=torch.uint8, device=dev)
+        src, name = jit.star_probe_source(self.prog.spec, self.value_reg, self.fpred.struct if self.fpred else None,
+                                          None)
+        self._probe = jit.compile_kernel(src, name)
+        fa, fb = self.t[0], self.t[1]
+        a = jit._Args()
+        if self.fpred:
+            for c in range(self.fpred.struct.n_cols):
+                a.ptr(self.fpred.struct.cols[c])
+        a.blob(jit.pred_lits(self.fpred.struct if self.fpred else None))
+        for c in range(self.prog.spec.n_cols):
+            a.ptr(self.prog.spec.cols[c])
+        for v in (fa.data_ptr(), fb.data_ptr()):
+            a.ptr(v)
+        a.i64(fa.numel())
+        for mn, mx, d in ((amn, amx, self.dir_a), (bmn, bmx, self.dir_b), (cmn, cmx, self.dir_c)):
+            a.i64(mn)
+            a.i64(mx - mn + 1)
+            a.ptr(d.data_ptr())
+        a.ptr(self.sum.data_ptr())
+        a.ptr(self.cnt.data_ptr())
+        a.i32(jit._aligned(*self.fpred.tensors) if self.fpred else 1)
+        a.i32(jit._aligned(*self.prog.tensors))
+        a.i32(jit._aligned(fa, fb))
+        self._probe_args = a
+        self._probe_grid = jit.occupancy_grid(self._probe, 256, 0, (fa.numel() + 7) // 8)
+
+    def _run_jit(self, s):
+        from . import jit
+        if not hasattr(self, "_probe"):
+            self._jit_setup()
+        fa, fb, ak, bk, bc, ck = self.t
+        (amn, amx), (bmn, bmx), (cmn, cmx) = self.doms
+        INT_MIN = -(1 << 31)
+        build = self.lib.tqpk_directory_build
+        ap = C.byref(self.apred.struct) if self.apred else None
+        e = self.err.data_ptr()
+        L.check(build(ak.data_ptr(), code_of(ak.dtype), ak.numel(), ap, None, 0, amn, amx - amn + 1, -1, -2,
+                      self.dir_a.data_ptr(), e, s), "tqpk_directory_build")
+        L.check(build(bk.data_ptr(), code_of(bk.dtype), bk.numel(), None, bc.data_ptr(), code_of(bc.dtype), bmn,
+                      bmx - bmn + 1, INT_MIN, INT_MIN + 1, self.dir_b.data_ptr(), e + 4, s), "tqpk_directory_build")
+        L.check(build(ck.data_ptr(), code_of(ck.dtype), ck.numel(), None, None, 0, cmn, cmx - cmn + 1, -1, -2,
+                      self.dir_c.data_ptr(), e + 8, s), "tqpk_directory_build")
+        self.sum.zero_()
+        self.cnt.zero_()
+        jit.launch(self._probe, self._probe_grid, 256, 0, self._probe_args, s, L.KID_STAR_PROBE)
+        L.check(self.lib.tqpk_dense_topk(self.sum.data_ptr(), self.cnt.data_ptr(), self.sum.numel(), cmn, self.k,
+                                         int(self.desc), self.tws.data_ptr(), self.tws.numel(),
+                                         self.out_keys.data_ptr(), self.out_vals.data_ptr(), self.out_cnts.data_ptr(),
+                                         self.out_count.data_ptr(), self.groups.data_ptr(), s), "tqpk_dense_topk")
+
     def run(self, stream=None):
         s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
+        self._jit_path = self._jit_ok()
+        if self._jit_path:
+            with torch.cuda.stream(stream or torch.cuda.current_stream(self.dev)):
+                self._run_jit(s)
+            return
         fa, fb, ak, bk, bc, ck = self.t
         (amn, amx), (bmn, bmx), (cmn, cmx) = self.doms
         L.check(self.lib.tqpk_pipeline_star_agg_topk(
@@ -169,7 +230,11 @@ class StarAggTopK:
     def result(self):
         s = torch.cuda.current_stream(self.dev).cuda_stream
         err = C.c_int(0)
-        L.check(self.lib.tqpk_pipeline_error(self.ws.data_ptr(), C.byref(err), s), "tqpk_pipeline_error")
+        if getattr(self, "_jit_path", False):
+            errs = [int(x) for x in self.err.cpu().tolist() if x]
+            err.value = errs[0] if errs else 0
+        else:
+            L.check(self.lib.tqpk_pipeline_error(self.ws.data_ptr(), C.byref(err), s), "tqpk_pipeline_error")
         if err.value:
             L.check(err.value, "star pipeline (repeated or out-of-domain dimension key)")
         m = int(self.out_count.item())

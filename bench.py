@@ -22,6 +22,7 @@ numpy restatement in oracle/) on the host cores, one process per core.
 from __future__ import annotations
 
 import argparse
+from typing import Optional
 import copy
 import json
 import os
@@ -78,8 +79,9 @@ class JoinAggTop10:
 
     def dominant(self):
         from tqpk import _lib as L
+        from tqpk import jit
         # probe + aggregate: reads fk, date, price, discount of every probe row once
-        return L.KID_PIPE_PROBE, "k_pl_probe_agg", self.NP * 24
+        return L.KID_PIPE_PROBE, "tqpk_q_join_probe" if jit.available() else "k_pl_probe_agg", self.NP * 24
 
     def setup_device(self, dev):
         import torch
@@ -163,9 +165,23 @@ class FilterGroupBy:
     def algorithmic_bytes(self):
         return self.N * 38
 
+    def fp64_ops(self):
+        """FP64 operations per launch of the accumulation kernel: the float arithmetic of the
+        expression program and one add per float sum accumulator, for every row that
+        passes the filter."""
+        from tqpk import _lib as L
+        S = self.prog.spec
+        arith = sum(1 for i in range(S.n_expr) if S.expr[i].type == L.F64 and S.expr[i].op in
+                    (L.X_ADD, L.X_SUB, L.X_MUL, L.X_DIV))
+        sums = sum(1 for a in range(S.n_accs) if S.accs[a].kind == L.ACC_SUM and S.accs[a].type == L.F64)
+        passing = int((self.t["ship_date"] <= 2470).sum())
+        return (arith + sums) * passing, arith + sums
+
     def dominant(self):
         from tqpk import _lib as L
-        return L.KID_GROUPBY, "k_groupby_dense", self.N * 38
+        from tqpk import jit
+        # filter + group-by: ship_date (4 B), quantity/price/discount/tax (4 x 8 B), flag, status (1 B each)
+        return L.KID_GROUPBY, "tqpk_q_groupby" if jit.available() else "k_groupby_dense", self.N * 38
 
     def setup_device(self, dev):
         import torch
@@ -248,7 +264,9 @@ class StarJoin:
 
     def dominant(self):
         from tqpk import _lib as L
-        return L.KID_STAR_PROBE, "k_star_probe", self.n[0] * 24
+        from tqpk import jit
+        # fact fkA, fkB (4 B each), price, discount (8 B each)
+        return L.KID_STAR_PROBE, "tqpk_q_star_probe" if jit.available() else "k_star_probe", self.n[0] * 24
 
     def setup_device(self, dev):
         import torch
@@ -373,7 +391,12 @@ class Batched:
                                                {22: d["p_date"], 23: d["p_price"], 24: d["p_discount"]},
                                                [["pd#22", ">", "1170"]], [["p#23", "*", ["1.0", "-", "d#24"]]], k=10))
                 self.plain_args.append(("join", d))
-        self.batch = Batch(self.insts, Autotuner())
+        from tqpk import jit
+        if jit.available():
+            from tqpk.jitbatch import QueryBatch
+            self.batch = QueryBatch(self.insts, Autotuner())      # the generated persistent kernel
+        else:
+            self.batch = Batch(self.insts, Autotuner())
         self.batch.capture()
 
     def run_batched(self):
@@ -454,20 +477,22 @@ def run_batched_bench(args):
     torch.cuda.synchronize()
     sampler = ClockSampler(0)
     sampler.start()
-    L.check(lib.tqpk_timing_begin(L.KID_BATCH), "tqpk_timing_begin")
-    launches0 = lib.tqpk_launch_count()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for s, e in evs:
         s.record()
-        w.run_batched()
+        w.run_batched()          # one CUDA graph: control reset, table reset kernel, persistent kernel
         e.record()
     torch.cuda.synchronize()
-    launches = lib.tqpk_launch_count() - launches0
-    import ctypes as C
-    kms, kn = C.c_double(0), C.c_int32(0)
-    L.check(lib.tqpk_timing_end(C.byref(kms), C.byref(kn)), "tqpk_timing_end")
+    launches = 2 * args.steps    # our kernels inside each replayed graph
     batched_ms = statistics.median([s.elapsed_time(e) for s, e in evs])
     clocks = sampler.stop()
+    # the persistent kernel alone (direct launches, CUDA events around it)
+    import ctypes as C
+    L.check(lib.tqpk_timing_begin(L.KID_BATCH), "tqpk_timing_begin")
+    for _ in range(3):
+        w.batch.run()
+    kms, kn = C.c_double(0), C.c_int32(0)
+    L.check(lib.tqpk_timing_end(C.byref(kms), C.byref(kn)), "tqpk_timing_end")
     plain_times = []
     for _ in range(max(2, min(args.steps, 3))):
         torch.cuda.synchronize()
@@ -567,6 +592,40 @@ def peak_gbs():
         except Exception:
             pass
     return PEAK_FALLBACK_GBS, "fallback"
+
+
+def fp64_peak_gops() -> Optional[float]:
+    """Measured FP64 add throughput of this GPU (Gop/s): four independent __dadd_rn chains
+    per thread over a full grid, timed with CUDA events."""
+    import torch
+    from tqpk import jit
+    if not jit.available():
+        return None
+    src = r"""
+extern "C" __global__ void fp64_add_rate(double* out, int iters) {
+  double a = threadIdx.x * 1e-3, b = blockIdx.x * 1e-6, c = 0.5, d = 0.25;
+  const double x = 1.0000001, y = 0.9999999;
+  for (int i = 0; i < iters; ++i) {
+    a = __dadd_rn(a, x); b = __dadd_rn(b, y); c = __dadd_rn(c, x); d = __dadd_rn(d, y);
+  }
+  if (a + b + c + d == 12345.678) out[0] = a;
+}"""
+    h = jit.compile_kernel(src, "fp64_add_rate")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    sms, blocks, iters = torch.cuda.get_device_properties(0).multi_processor_count, 8, 4096
+    a = jit._Args()
+    a.ptr(out.data_ptr())
+    a.i32(iters)
+    s = torch.cuda.current_stream().cuda_stream
+    jit.launch(h, sms * blocks, 256, 0, a, s)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        jit.launch(h, sms * blocks, 256, 0, a, s)
+    e1.record()
+    torch.cuda.synchronize()
+    ops = 5 * sms * blocks * 256 * iters * 4
+    return ops / (e0.elapsed_time(e1) / 1e3) / 1e9
 
 
 def traffic_per_launch(kernel: str, workload: str):
@@ -807,6 +866,14 @@ def run_ours(args, rank, world):
         "clocks": clocks,
         "gpu_launches": launches,
     }
+    if hasattr(w, "fp64_ops") and kn.value:
+        # the accumulation kernel is bound by the FP64 pipe (1/64 rate on this part), not by HBM
+        ops, per_row = w.fp64_ops()
+        fpk = fp64_peak_gops()
+        got = ops / k_avg_s / 1e9
+        line["roofline"]["fp64"] = {"ops_per_launch": ops, "ops_per_passing_row": per_row, "achieved": got,
+                                    "peak": fpk, "unit": "Gop/s", "frac": got / fpk if fpk else None,
+                                    "peak_source": "measured in this run (four independent __dadd_rn chains per thread, full grid)"}
     if rank == 0:
         print(json.dumps(line))
 

@@ -1,0 +1,100 @@
+"""Generated query kernels compile for sm_103a (NVRTC runs without a GPU) and keep
+their launch-bound literals out of the code."""
+import numpy as np
+import pytest
+import torch
+
+from tqpk import _lib as L
+from tqpk.expr import compile_aggregate
+from tqpk.predicate import compile_filter
+
+jit = pytest.importorskip("tqpk.jit")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def nvrtc():
+    from tqpk import build
+    build.build()
+    if not L.load().tqpk_jit_available():
+        pytest.skip("NVRTC is not available")
+
+
+LINEITEM_AGG = ["flag#5", "status#6",
+                [[["sum", ["quantity#1"]], "#", "101"], "AS", "a#201"],
+                [[["sum", [["price#2", "*", ["1.0", "-", "discount#3"]]]], "#", "103"], "AS", "c#203"],
+                [[["avg", ["discount#3"]], "#", "107"], "AS", "g#207"],
+                [[["min", ["price#2"]], "#", "109"], "AS", "m#209"],
+                [[["max", ["status#6"]], "#", "110"], "AS", "x#210"],
+                [[["count", ["1"]], "#", "108L"], "AS", "h#208"]]
+
+
+def _lineitem(n=64):
+    from tqpk import datagen
+    t = datagen.lineitem(n, 1)
+    ids = {"quantity": 1, "price": 2, "discount": 3, "tax": 4, "flag": 5, "status": 6, "ship_date": 7}
+    return {ids[k]: torch.from_numpy(v) for k, v in t.items()}
+
+
+def _join_cols(n=64):
+    from tqpk import datagen
+    return {k: torch.from_numpy(v) for k, v in datagen.join_tables(16, n, 1).items()}
+
+
+def test_groupby_kernel_compiles_for_each_table_mode():
+    d = _lineitem()
+    prog = compile_aggregate({"is partial": False, "keys": ["flag#5", "status#6"], "input ids": [1, 2, 3, 5, 6],
+                              "results": LINEITEM_AGG, "out agg ids": [201, 203, 207, 209, 210, 208]}, d)
+    pred = compile_filter([[["ship_date#7", "<=", "2470"], "AND", ["price#2", ">=", "1000.5"]], "OR",
+                           ["discount#3", "=", "0.05"]], {7: d[7], 2: d[2], 3: d[3]})
+    for mode in (L.GB_DENSE_PRIVATE, L.GB_DENSE_SHARED, L.GB_DENSE_GLOBAL):
+        plan = L.GbPlan()
+        plan.mode, plan.threads, plan.slots = mode, 256, 6
+        plan.key_stride[0], plan.key_stride[1] = 2, 1
+        src, name, T, smem = jit.groupby_source(prog.spec, pred.struct, plan)
+        ok, log = jit.check_compiles(src)
+        assert ok, log[:2000]
+        assert "2470" not in src and "1000.5" not in src    # literals are bound at launch
+
+
+def test_probe_kernels_compile_with_and_without_build_filter():
+    j = _join_cols()
+    pcols = {22: j["p_date"], 23: j["p_price"], 24: j["p_discount"]}
+    prog = compile_aggregate({"keys": None, "results": [[[["sum", [["p#23", "*", ["1.0", "-", "d#24"]]]], "#", "1"],
+                                                         "AS", "v#1"]]}, pcols)
+    vreg = prog.spec.accs[prog.outputs[0][2]].reg
+    pp = compile_filter([["pd#22", ">", "1170"]], {22: j["p_date"]})
+    bp = compile_filter([["bd#12", "<", "1170"]], {12: j["b_date"]})
+    for p, b in ((pp, None), (pp, bp), (None, bp), (None, None)):
+        src, _ = jit.join_probe_source(prog.spec, vreg, p.struct if p else None, b.struct if b else None)
+        ok, log = jit.check_compiles(src)
+        assert ok, log[:2000]
+    cat = compile_filter([["cat#32", "=", "1"]], {32: torch.zeros(8, dtype=torch.uint8)})
+    for f, a in ((None, cat), (pp, cat), (None, None)):
+        src, _ = jit.star_probe_source(prog.spec, vreg, f.struct if f else None, a.struct if a else None)
+        ok, log = jit.check_compiles(src)
+        assert ok, log[:2000]
+
+
+def test_generated_batch_kernel_compiles_and_record_layout_matches():
+    from tqpk import jitbatch as QB
+    d = _lineitem()
+    prog = compile_aggregate({"is partial": False, "keys": ["flag#5", "status#6"], "input ids": [1, 2, 3, 5, 6],
+                              "results": LINEITEM_AGG, "out agg ids": [201, 203, 207, 209, 210, 208]}, d)
+    pred = compile_filter([["ship_date#7", "<=", "2470"]], {7: d[7]})
+    j = _join_cols()
+    pcols = {22: j["p_date"], 23: j["p_price"], 24: j["p_discount"]}
+    jprog = compile_aggregate({"keys": None, "results": [[[["sum", [["p#23", "*", ["1.0", "-", "d#24"]]]], "#", "1"],
+                                                          "AS", "v#1"]]}, pcols)
+    vreg = jprog.spec.accs[jprog.outputs[0][2]].reg
+    pp = compile_filter([["pd#22", ">", "1170"]], {22: j["p_date"]})
+    bp = compile_filter([["bd#12", "<", "1170"]], {12: j["b_date"]})
+    src = QB.batch_source([(prog.spec, pred.struct, prog.outputs), (prog.spec, None, prog.outputs)],
+                          [(jprog.spec, vreg, pp.struct, bp.struct), (jprog.spec, vreg, None, None)])
+    probe = src + "\nstatic_assert(sizeof(QInst) == %d, \"record size\");\n" % C_sizeof(QB.QInst)
+    ok, log = jit.check_compiles(probe)
+    assert ok, log[:3000]
+
+
+def C_sizeof(t):
+    import ctypes
+    return ctypes.sizeof(t)

@@ -86,8 +86,17 @@ def check(results, expected):
                 (assert_f64_close if e.dtype == np.float64 else np.testing.assert_array_equal)(outs[oid], e)
 
 
-def test_batch_uneven_instances_vs_oracle():
-    from tqpk.batch import Batch
+def batch_class(impl):
+    if impl == "library":
+        from tqpk.batch import Batch
+        return Batch
+    from tqpk.jitbatch import QueryBatch
+    return QueryBatch
+
+
+@pytest.mark.parametrize("impl", ["library", "generated"])
+def test_batch_uneven_instances_vs_oracle(impl):
+    Batch = batch_class(impl)
     shapes = [("groupby", 1000, 4), ("join", 5000, 300), ("groupby", 250_000, 5000), ("join", 300_000, 20_000),
               ("groupby", 40_000, 60), ("join", 1000, 7), ("groupby", 3, 2), ("join", 120_000, 100_000),
               ("groupby", 700_001, 1), ("join", 64, 1000), ("groupby", 90_000, 40_000), ("join", 2_000_000, 500)]
@@ -105,8 +114,10 @@ def test_batch_uneven_instances_vs_oracle():
         check(b.results(), expected)
 
 
-def test_batch_item_sizes_do_not_change_results():
-    from tqpk.batch import Autotuner, Batch
+@pytest.mark.parametrize("impl", ["library", "generated"])
+def test_batch_item_sizes_do_not_change_results(impl):
+    from tqpk.batch import Autotuner
+    Batch = batch_class(impl)
     insts, expected = [], []
     for i, (kind, rows, g) in enumerate([("groupby", 300_000, 12), ("join", 400_000, 50_000)]):
         inst, exp = (make_groupby if kind == "groupby" else make_join)(rows, g, 7 + i)
@@ -117,3 +128,22 @@ def test_batch_item_sizes_do_not_change_results():
         b = Batch(insts, tuner)
         b.run()
         check(b.results(), expected)
+
+
+def test_generated_batch_table_modes_and_empty_instances():
+    """Group tables of every placement (per thread, several shared copies, one per CTA, global) and
+    instances with no rows, in one generated batch."""
+    from tqpk.jitbatch import QueryBatch, _mode
+    shapes = [("groupby", 200_000, 4), ("groupby", 200_000, 150), ("groupby", 200_000, 1400),
+              ("groupby", 200_000, 30_000), ("groupby", 0, 9), ("join", 0, 100), ("join", 50_000, 1)]
+    insts, expected = [], []
+    for i, (kind, rows, g) in enumerate(shapes):
+        inst, exp = (make_groupby if kind == "groupby" else make_join)(rows, g, 300 + i)
+        insts.append(inst)
+        expected.append((kind, exp))
+    b = QueryBatch(insts)
+    placements = {(int(b.recs[i].mode), int(b.recs[i].copies)) for i, (kind, _, _) in enumerate(shapes)
+                  if kind == "groupby"}
+    assert {(1, 256), (2, 8), (2, 1), (4, 1)} <= placements
+    b.run()
+    check(b.results(), expected)

@@ -79,7 +79,7 @@ extern "C" int tqpk_topk_stable(const void* d_keys, int32_t dt, int32_t desc, co
   if (!ci) return TQPK_ENOMEM;
   TQPK_CUDA(cudaMemsetAsync(ticket, 0, 256, s));
   ArraySource src{d_keys, dt, d_perm_in, n, desc ? 1 : 0};
-  TopkOut O{idx, count, ck, ci, ticket, nullptr};
+  TopkOut O{idx, count, ck, ci, ticket, nullptr, reinterpret_cast<unsigned long long*>(ticket + 8)};
   timing_before(KID_PIPE_TOPK, s);
   int rc = topk_warp_launch(1, &src, (int)k, grid, O, s);
   timing_after(KID_PIPE_TOPK, s);

@@ -66,11 +66,13 @@ struct WarpList {
       if (r * 32 + lane == pos) { key[r] = ck; idx[r] = ci; }
   }
   // Inserts the valid lanes' candidates that beat the current k-th entry.
-  __device__ __forceinline__ void offer(int k, uint64_t ck, int64_t ci, bool valid) {
+  // ext is a key bound known from elsewhere (some list already holds k keys
+  // <= ext): strictly larger keys cannot reach the top k and are skipped.
+  __device__ __forceinline__ void offer(int k, uint64_t ck, int64_t ci, bool valid, uint64_t ext = ~0ull) {
     uint64_t tk;
     int64_t ti;
     at(k - 1, tk, ti);
-    const bool cand = valid && (ti < 0 || tk_better(ck, ci, tk, ti));
+    const bool cand = valid && ck <= ext && (ti < 0 || tk_better(ck, ci, tk, ti));
     uint32_t pending = __ballot_sync(0xffffffffu, cand);
     while (pending) {
       const int src = __ffs(pending) - 1;
@@ -153,6 +155,7 @@ struct TopkOut {
   int64_t* cand_idx;
   unsigned* ticket;
   unsigned long long* valid_total;  // number of valid items seen (may be null)
+  unsigned long long* bound;        // ~(best known k-th key), raised with atomicMax; 0 = none (zeroed with the ticket)
 };
 
 template <int R, class Src>
@@ -166,14 +169,25 @@ __global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
   L.init();
   const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
   unsigned valid = 0;
-  // four consecutive items per lane per step; the warp offers them in four rounds
+  uint64_t published = ~0ull;
+  // four consecutive items per lane per step; the warp offers them in four rounds.
+  // Every full warp list publishes its k-th key to a grid-wide bound, so after the
+  // first lists fill, candidates that cannot reach the top k skip the insertion.
   for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + warp * 32) * 4; base < src.n; base += stride) {
     const int64_t i0 = base + lane * 4;
     uint64_t key[4];
     const unsigned ok = src.get4(i0, key);
+    const uint64_t ext = ~__ldcg(O.bound);
     valid += __popc(ok);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) L.offer(k, key[q], i0 + q, (ok >> q) & 1u);
+    for (int q = 0; q < 4; ++q) L.offer(k, key[q], i0 + q, (ok >> q) & 1u, ext);
+    uint64_t kk;
+    int64_t ki;
+    L.at(k - 1, kk, ki);
+    if (ki >= 0 && kk < published) {
+      if (lane == 0) atomicMax(O.bound, ~kk);
+      published = kk;
+    }
   }
   valid = __reduce_add_sync(0xffffffffu, valid);
   if (lane == 0 && valid && O.valid_total) atomicAdd(O.valid_total, (unsigned long long)valid);
@@ -186,11 +200,12 @@ __global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
   if (warp == 0) {
     WarpList<R> M;
     M.init();
+    const uint64_t ext = ~__ldcg(O.bound);
     for (int w = 0; w < 8; ++w)
       for (int r = 0; r < R; ++r) {
         const int p = r * 32 + lane;
         const int64_t ii = si[w * 32 * R + p];
-        M.offer(k, sk[w * 32 * R + p], ii, p < k && ii >= 0);
+        M.offer(k, sk[w * 32 * R + p], ii, p < k && ii >= 0, ext);
       }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -215,6 +230,7 @@ __global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
   constexpr int CHUNK = 8 * 32 * R;
   WarpList<R> F;
   F.init();
+  const uint64_t fext = ~__ldcg(O.bound);
   const int64_t total = (int64_t)gridDim.x * k;
   for (int64_t base = 0; base < total; base += CHUNK) {
     for (int j = threadIdx.x; j < CHUNK; j += blockDim.x) {
@@ -226,7 +242,7 @@ __global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int p = warp * 32 * R + r * 32 + lane;
-      F.offer(k, sk[p], si[p], si[p] >= 0);
+      F.offer(k, sk[p], si[p], si[p] >= 0, fext);
     }
     __syncthreads();
   }
@@ -261,7 +277,7 @@ __global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
 
 // Host launcher: k <= 256.  cand arrays hold grid*k entries each.
 int topk_warp_launch(int kind, const void* src, int k, int grid, TopkOut O, cudaStream_t s);
-inline int topk_grid_size() { return num_sms() * 2; }
+inline int topk_grid_size() { return num_sms(); }
 inline size_t topk_scratch_bytes(int k) {
   // ticket block + count + k indices + two [grid][k] candidate arrays, each 256-byte aligned
   return 2 * align_up((size_t)topk_grid_size() * k * 8, 256) + align_up((size_t)k * 8, 256) + 1024;

@@ -98,6 +98,12 @@ class JoinAggTop10:
     def step_device(self):
         self.pipe.run()
 
+    def capture(self):
+        self.pipe.capture()
+
+    def step_graph(self):
+        self.pipe.replay()
+
     def device_result(self):
         return self.pipe.result()[:2]
 
@@ -282,6 +288,12 @@ class StarJoin:
 
     def step_device(self):
         self.pipe.run()
+
+    def capture(self):
+        self.pipe.capture()
+
+    def step_graph(self):
+        self.pipe.replay()
 
     def device_result(self):
         k, v, c, _ = self.pipe.result()
@@ -796,21 +808,38 @@ def run_ours(args, rank, world):
             w.step_device()
         torch.cuda.synchronize()
     kid, kname, kbytes = w.dominant()
+    # a fused pipeline runs as one CUDA graph per step (its launches and memsets recorded once)
+    graph = hasattr(w, "capture")
+    if graph:
+        launches0 = lib.tqpk_launch_count()
+        w.capture()
+        launches_per_step = (lib.tqpk_launch_count() - launches0) // 2    # capture() runs once eagerly, once recorded
+        for _ in range(args.warmup):
+            w.step_graph()
+        torch.cuda.synchronize()
     barrier(world)
     torch.cuda.synchronize()
-    L.check(lib.tqpk_timing_begin(kid), "tqpk_timing_begin")
+    if not graph:
+        L.check(lib.tqpk_timing_begin(kid), "tqpk_timing_begin")
     launches0 = lib.tqpk_launch_count()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for s, e in evs:
         flush.zero_()
         s.record()
-        w.step_device()
+        w.step_graph() if graph else w.step_device()
         e.record()
     torch.cuda.synchronize()
-    launches = lib.tqpk_launch_count() - launches0
+    launches = launches_per_step * args.steps if graph else lib.tqpk_launch_count() - launches0
     barrier(world)
     import ctypes as C
     kms, kn = C.c_double(0), C.c_int32(0)
+    if graph:
+        # the dominant kernel's own duration: direct launches bracketed by CUDA events
+        L.check(lib.tqpk_timing_begin(kid), "tqpk_timing_begin")
+        for _ in range(args.steps):
+            flush.zero_()
+            w.step_device()
+        torch.cuda.synchronize()
     L.check(lib.tqpk_timing_end(C.byref(kms), C.byref(kn)), "tqpk_timing_end")
     step_ms = [s.elapsed_time(e) for s, e in evs]
     total_ms = max_over_ranks(sum(step_ms), world)
@@ -854,6 +883,7 @@ def run_ours(args, rank, world):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, TPC-H-like distributions)",
         "config": dict(w.config, parallelism="replicas" if world > 1 else "single GPU",
+                       step="one CUDA-graph replay of the fused pipeline" if graph else "direct launches",
                        pipeline_GBps=w.algorithmic_bytes() / (total_ms / args.steps / 1000.0) / 1e9),
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,

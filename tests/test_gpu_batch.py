@@ -147,3 +147,18 @@ def test_generated_batch_table_modes_and_empty_instances():
     assert {(1, 256), (2, 8), (2, 1), (4, 1)} <= placements
     b.run()
     check(b.results(), expected)
+
+
+def test_generated_batch_dependency_wait_times_out():
+    """A phase whose predecessor count can never be reached (one phase-0 item more than
+    the queue holds): the bounded wait gives up, the kernel still finishes every item and
+    the host reads TQPK_ETIMEOUT from the control block."""
+    from tqpk.jitbatch import QueryBatch
+    inst, _ = make_groupby(50_000, 12, 901)
+    b = QueryBatch([inst])
+    b.recs[0].ni[0] += 1
+    b.d_recs.copy_(torch.frombuffer(bytearray(bytes(b.recs)), dtype=torch.uint8))
+    b.run()
+    torch.cuda.synchronize()
+    with pytest.raises(TimeoutError):
+        b.check_error()

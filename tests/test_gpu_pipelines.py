@@ -63,6 +63,34 @@ def test_join_pipeline_vs_oracle(nb, np_rows, k, offset, dtype, filters):
     assert_f64_close(vals, ev)
 
 
+@pytest.mark.parametrize("tma", ["1", "0"])
+@pytest.mark.parametrize("nb,np_rows,dtype", [(100_000, 1_000_003, np.int32), (5_000, 2048, np.int32),
+                                              (70_000, 1_048_575, np.int64), (2_000, 1024, np.int64),
+                                              (9_000, 1023, np.int32), (300, 128, np.int32), (300, 127, np.int32),
+                                              (40_000, 9_000_001, np.int32)])
+def test_join_probe_staged_and_plain_paths(monkeypatch, tma, nb, np_rows, dtype):
+    """The TMA-staged probe (full 128-row chunks + a plain-load tail) and the register
+    probe give the oracle's result, with and without a whole number of chunks."""
+    monkeypatch.setenv("TQPK_TMA", tma)
+    from tqpk.pipeline import JoinAggTopK
+    rng = np.random.default_rng(nb ^ np_rows)
+    cols = {11: (rng.permutation(nb) + 1).astype(dtype), 12: rng.integers(0, 2557, nb).astype(np.int32),
+            21: rng.integers(1, nb + 3, np_rows).astype(dtype), 22: rng.integers(0, 2557, np_rows).astype(np.int32),
+            23: rng.integers(90000, 10495001, np_rows) / 100.0, 24: rng.integers(0, 11, np_rows) / 100.0}
+    f1, f2 = [["bd#12", "<", "1170"]], [["pd#22", ">", "1170"]]
+    d = {c: torch.from_numpy(a).cuda() for c, a in cols.items()}
+    p = JoinAggTopK(d[11], 1, nb, d[21], {12: d[12]}, f1, {22: d[22], 23: d[23], 24: d[24]}, f2,
+                    [["p#23", "*", ["1.0", "-", "d#24"]]], k=10)
+    p.run()
+    keys, vals, groups = p.result()
+    from tqpk import jit
+    assert bool(getattr(p, "_probe_smem", 0)) == (tma == "1" and np_rows >= jit.TMA_ROWS)
+    ek, ev, eg = _oracle_join(cols, f1, f2, 10)
+    assert groups == eg
+    np.testing.assert_array_equal(keys, ek)
+    assert_f64_close(vals, ev)
+
+
 def test_join_pipeline_repeated_build_key_raises():
     from tqpk.pipeline import JoinAggTopK
     bk = torch.tensor([1, 2, 2, 3], dtype=torch.int32, device="cuda")
@@ -101,3 +129,16 @@ def test_topk_stable_large_k(k):
     x = rng.integers(-1000, 1000, 300_001).astype(np.int64)
     got = topk_stable(torch.from_numpy(x).cuda(), k, True).cpu().numpy()
     np.testing.assert_array_equal(got, O._stable_order(x, True)[:k])
+
+
+@pytest.mark.parametrize("n,k,hi", [(100_003, 10, 1), (200_000, 100, 3), (5_000_000, 256, 1 << 40),
+                                    (3, 10, 5), (0, 10, 5), (4097, 1, 2)])
+@pytest.mark.parametrize("desc", [True, False])
+def test_topk_threshold_path_and_tie_fallback(n, k, hi, desc):
+    """Few distinct values put more items under the cut than the candidate list holds
+    (the warp-list fallback runs); many distinct values take the sorted-candidates path."""
+    from tqpk.ops import topk_stable
+    rng = np.random.default_rng(n + k)
+    x = rng.integers(0, hi, n).astype(np.int64)
+    got = topk_stable(torch.from_numpy(x).cuda(), k, desc).cpu().numpy()
+    np.testing.assert_array_equal(got, O._stable_order(x, desc)[:k])

@@ -106,7 +106,7 @@ extern "C" int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64
 
 extern "C" size_t tqpk_dense_topk_workspace_bytes(int32_t k) {
   k = std::max(1, std::min(k, kDenseMaxK));
-  return 1024 + align_up((size_t)k * 8, 256) + 2 * align_up((size_t)topk_grid_size() * k * 8, 256) + 1024;
+  return 1024 + align_up((size_t)k * 8, 256) + 2 * align_up(topk_cand_entries(k) * 8, 256) + 1024;
 }
 
 extern "C" int tqpk_dense_topk(const double* d_sum, const uint32_t* d_cnt, int64_t slots, int64_t key_min, int32_t k,
@@ -120,8 +120,8 @@ extern "C" int tqpk_dense_topk(const double* d_sum, const uint32_t* d_cnt, int64
   WsCursor c(d_ws, ws_bytes);
   unsigned* hdr = c.take<unsigned>(64);
   int64_t* top_idx = c.take<int64_t>(k);
-  uint64_t* cand_key = c.take<uint64_t>((size_t)grid * k);
-  int64_t* cand_idx = c.take<int64_t>((size_t)grid * k);
+  uint64_t* cand_key = c.take<uint64_t>(topk_cand_entries(k));
+  int64_t* cand_idx = c.take<int64_t>(topk_cand_entries(k));
   if (!cand_idx) return TQPK_ENOMEM;
   unsigned* ticket = hdr;
   unsigned long long* groups = reinterpret_cast<unsigned long long*>(hdr + 2);

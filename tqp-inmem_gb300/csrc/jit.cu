@@ -146,7 +146,7 @@ extern "C" int tqpk_jit_occupancy(void* handle, int32_t block, size_t smem) {
   if (!handle) return 0;
   JitKernel* k = static_cast<JitKernel*>(handle);
   int per_sm = 0;
-  if (smem > 48 * 1024)
+  if (smem > 0)   // dynamic + static shared memory may pass the 48 KB default even when smem alone does not
     cudaFuncSetAttribute(reinterpret_cast<const void*>(k->kernel), cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(k->kernel), block, smem) !=
@@ -166,7 +166,7 @@ extern "C" int tqpk_jit_launch(void* handle, int32_t grid, int32_t block, size_t
   if (!handle || grid < 1 || block < 1 || !args) return TQPK_EINVAL;
   JitKernel* k = static_cast<JitKernel*>(handle);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (smem > 48 * 1024)
+  if (smem > 0)
     TQPK_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(k->kernel),
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (timing_kid) timing_before(timing_kid, s);

@@ -157,7 +157,7 @@ struct PipeLayout {
 
 static size_t pipe_bytes(int64_t slots, int grid) {
   return 4096 + align_up(slots * 4, 256) + align_up(slots * 8, 256) + align_up(slots * 4, 256) +
-         align_up(kPipeMaxK * 8, 256) + 2 * align_up((size_t)grid * kPipeMaxK * 8, 256);
+         align_up(kPipeMaxK * 8, 256) + 2 * align_up(std::max<size_t>((size_t)grid * kPipeMaxK, kTopkCand) * 8, 256);
 }
 
 static bool pipe_layout(void* ws, size_t bytes, int64_t slots, int grid, PipeLayout& L) {
@@ -172,8 +172,8 @@ static bool pipe_layout(void* ws, size_t bytes, int64_t slots, int grid, PipeLay
   L.sum = c.take<double>(slots);
   L.cnt = c.take<unsigned>(slots);
   L.top_idx = c.take<int64_t>(kPipeMaxK);
-  L.cand_key = c.take<uint64_t>((size_t)grid * kPipeMaxK);
-  L.cand_slot = c.take<int64_t>((size_t)grid * kPipeMaxK);
+  L.cand_key = c.take<uint64_t>(std::max<size_t>((size_t)grid * kPipeMaxK, kTopkCand));
+  L.cand_slot = c.take<int64_t>(std::max<size_t>((size_t)grid * kPipeMaxK, kTopkCand));
   return L.cand_slot != nullptr;
 }
 
@@ -245,7 +245,8 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
     TQPK_CHECK_LAUNCH();
   }
   if (stages & 4) {
-    TQPK_CUDA(cudaMemsetAsync(L.top_count + 1, 0, 8, s));   // the top-k key bound of this run
+    TQPK_CUDA(cudaMemsetAsync(L.top_count + 1, 0, 8, s));   // the top-k cut of this run
+    TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 8, s));          // the group count the top-k pass accumulates
     DenseSumSource src{L.sum, L.cnt, slots, A.desc};
     TopkOut O{L.top_idx, L.top_count, L.cand_key, L.cand_slot, L.done, L.groups,
               reinterpret_cast<unsigned long long*>(L.top_count + 1)};   // hdr[6..7], zeroed with the header

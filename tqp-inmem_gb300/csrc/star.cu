@@ -180,7 +180,8 @@ struct StarLayout {
 
 static size_t star_bytes(int64_t as, int64_t bs, int64_t cs, int grid) {
   return 4096 + align_up(as * 4, 256) + align_up(bs * 4, 256) + align_up(cs * 4, 256) + align_up(cs * 8, 256) +
-         align_up(cs * 4, 256) + align_up(kStarMaxK * 8, 256) + 2 * align_up((size_t)grid * kStarMaxK * 8, 256);
+         align_up(cs * 4, 256) + align_up(kStarMaxK * 8, 256) +
+         2 * align_up(std::max<size_t>((size_t)grid * kStarMaxK, kTopkCand) * 8, 256);
 }
 
 static bool star_layout(void* ws, size_t bytes, int64_t as, int64_t bs, int64_t cs, int grid, StarLayout& L) {
@@ -197,8 +198,8 @@ static bool star_layout(void* ws, size_t bytes, int64_t as, int64_t bs, int64_t 
   L.sum = c.take<double>(cs);
   L.cnt = c.take<unsigned>(cs);
   L.top_idx = c.take<int64_t>(kStarMaxK);
-  L.cand_key = c.take<uint64_t>((size_t)grid * kStarMaxK);
-  L.cand_idx = c.take<int64_t>((size_t)grid * kStarMaxK);
+  L.cand_key = c.take<uint64_t>(std::max<size_t>((size_t)grid * kStarMaxK, kTopkCand));
+  L.cand_idx = c.take<int64_t>(std::max<size_t>((size_t)grid * kStarMaxK, kTopkCand));
   return L.cand_idx != nullptr;
 }
 

@@ -14,10 +14,21 @@ __device__ __forceinline__ bool ArraySource::get(int64_t i, uint64_t& k) const {
 
 template <int R, class Src>
 static int launch_r(const Src& src, int k, int grid, TopkOut O, cudaStream_t s) {
-  const size_t smem = (size_t)8 * 32 * R * 16;
-  if (smem > 48 * 1024)
-    TQPK_CUDA(cudaFuncSetAttribute(k_topk_warp<R, Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_topk_warp<R, Src><<<grid, 256, smem, s>>>(src, k, O);
+  (void)grid;
+  // groups of G items (a multiple of 4), at most kTopkGroups of them
+  int64_t G = 4;
+  while (G * kTopkGroups < src.n) G <<= 1;
+  const int ng = (int)std::max<int64_t>(1, (src.n + G - 1) / G);
+  k_tk_group_best<Src><<<ng, 256, 0, s>>>(src, G, O);
+  TQPK_CHECK_LAUNCH();
+  k_tk_cut<<<1, 1024, 0, s>>>(ng, k, O);
+  TQPK_CHECK_LAUNCH();
+  const int64_t units = (src.n + 1023) / 1024;
+  k_tk_filter<Src><<<(int)std::max<int64_t>(1, std::min<int64_t>(units, (int64_t)num_sms() * 8)), 256, 0, s>>>(src, O);
+  TQPK_CHECK_LAUNCH();
+  const size_t smem = (size_t)kTopkCap * 16;
+  TQPK_CUDA(cudaFuncSetAttribute(k_tk_final<R, Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_tk_final<R, Src><<<1, 256, smem, s>>>(src, k, O);
   TQPK_CHECK_LAUNCH();
   return TQPK_OK;
 }
@@ -74,8 +85,8 @@ extern "C" int tqpk_topk_stable(const void* d_keys, int32_t dt, int32_t desc, co
   unsigned* ticket = cur.take<unsigned>(64);
   int64_t* count = cur.take<int64_t>(4);
   int64_t* idx = cur.take<int64_t>(k);
-  uint64_t* ck = cur.take<uint64_t>((size_t)grid * k);
-  int64_t* ci = cur.take<int64_t>((size_t)grid * k);
+  uint64_t* ck = cur.take<uint64_t>(topk_cand_entries((int)k));
+  int64_t* ci = cur.take<int64_t>(topk_cand_entries((int)k));
   if (!ci) return TQPK_ENOMEM;
   TQPK_CUDA(cudaMemsetAsync(ticket, 0, 256, s));
   ArraySource src{d_keys, dt, d_perm_in, n, desc ? 1 : 0};

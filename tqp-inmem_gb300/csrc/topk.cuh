@@ -4,12 +4,13 @@
 // perm[:limit].  The stable top-k order is lexicographic on
 // (order-preserving key, position), smaller first, so ties keep input order.
 //
-// Each warp keeps its best k entries as a sorted list striped over the warp
-// (entry p = row p/32 of lane p%32, R rows per lane, k <= 32*R).  A batch of 32
-// candidates is compared against the current k-th entry and the survivors
-// are inserted one by one (rank by ballot/popc, shift by shuffles).  A CTA
-// merges its warps' lists in shared memory, writes them out, and the last CTA
-// to finish (an atomic ticket, no waiting) merges the per-CTA lists.
+// Items are cut by a threshold found from group bests, the few survivors are
+// sorted in one CTA (see k_tk_group_best below).  WarpList keeps a warp's best
+// k entries as a sorted list striped over the warp (entry p = row p/32 of lane
+// p%32, R rows per lane, k <= 32*R); a batch of 32 candidates is compared
+// against the current k-th entry and the survivors are inserted one by one
+// (rank by ballot/popc, shift by shuffles).  It serves the tie-heavy fallback
+// and the batched kernels.
 #pragma once
 
 #include "common.cuh"
@@ -158,98 +159,152 @@ struct TopkOut {
   unsigned long long* bound;        // ~(best known k-th key), raised with atomicMax; 0 = none (zeroed with the ticket)
 };
 
-template <int R, class Src>
-__global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
-  extern __shared__ unsigned char tk_smem[];
-  uint64_t* sk = reinterpret_cast<uint64_t*>(tk_smem);            // [8][32R]
-  int64_t* si = reinterpret_cast<int64_t*>(sk + 8 * 32 * R);
-  __shared__ bool last;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpList<R> L;
-  L.init();
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
+// ---------------------------------------------------------------------------
+// Threshold top-k (the default): one pass over the items cuts them into at
+// most kTopkGroups groups of G consecutive items and keeps each group's best
+// key; the k-th best of those group bests is a cut T with at least k items
+// at or below it (every one of those k groups holds one), so the top k are
+// all among the items with key <= T.  For independent keys only about k
+// items pass T.  A second pass appends them to a candidate list (at most
+// kTopkCap), and one CTA sorts the list bitonically by (key, index).  When
+// ties push more than kTopkCap items under the cut, that CTA falls back to
+// the warp lists over all items (same result, slower).
+constexpr int kTopkCap = 4096;
+constexpr int kTopkGroups = 2048;
+constexpr int kTopkCand = kTopkCap + kTopkGroups;   // cand_key entries used: candidates, then group bests
+
+__device__ __forceinline__ void block_min_u64(uint64_t& v, uint64_t* red) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const uint64_t w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < nw; ++w) v = red[w] < v ? red[w] : v;
+    red[0] = v;
+  }
+  __syncthreads();
+  v = red[0];
+}
+
+template <class Src>
+__global__ void __launch_bounds__(256) k_tk_group_best(Src src, int64_t G, TopkOut O) {
+  __shared__ uint64_t red[8];
+  const int64_t b0 = (int64_t)blockIdx.x * G, b1 = b0 + G < src.n ? b0 + G : src.n;
+  uint64_t best = ~0ull;
   unsigned valid = 0;
-  uint64_t published = ~0ull;
-  // four consecutive items per lane per step; the warp offers them in four rounds.
-  // Every full warp list publishes its k-th key to a grid-wide bound, so after the
-  // first lists fill, candidates that cannot reach the top k skip the insertion.
+  for (int64_t i0 = b0 + threadIdx.x * 4; i0 < b1; i0 += 4 * (int64_t)blockDim.x) {
+    uint64_t key[4];
+    const unsigned ok = src.get4(i0, key);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (((ok >> q) & 1u) && i0 + q < b1) {
+        best = key[q] < best ? key[q] : best;
+        ++valid;
+      }
+  }
+  valid = __reduce_add_sync(0xffffffffu, valid);
+  if ((threadIdx.x & 31) == 0 && valid && O.valid_total) atomicAdd(O.valid_total, (unsigned long long)valid);
+  block_min_u64(best, red);
+  if (threadIdx.x == 0) {
+    O.cand_key[kTopkCap + blockIdx.x] = best;
+    if (blockIdx.x == 0) *O.ticket = 0;          // the candidate counter of the next pass
+  }
+}
+
+// one CTA of 1024 threads: bitonic sort of the group bests, cut = the k-th
+static __global__ void __launch_bounds__(1024) k_tk_cut(int ng, int k, TopkOut O) {
+  __shared__ uint64_t v[kTopkGroups];
+  for (int i = threadIdx.x; i < kTopkGroups; i += blockDim.x) v[i] = i < ng ? __ldcg(&O.cand_key[kTopkCap + i]) : ~0ull;
+  __syncthreads();
+  for (int size = 2; size <= kTopkGroups; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < kTopkGroups / 2; t += blockDim.x) {
+        const int i = 2 * t - (t & (stride - 1)), j = i + stride;
+        const bool up = (i & size) == 0;
+        const uint64_t a = v[i], b = v[j];
+        if ((a > b) == up) { v[i] = b; v[j] = a; }
+      }
+      __syncthreads();
+    }
+  if (threadIdx.x == 0) *O.bound = v[(k <= kTopkGroups ? k : kTopkGroups) - 1];
+}
+
+template <class Src>
+__global__ void __launch_bounds__(256) k_tk_filter(Src src, TopkOut O) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t cut = __ldcg(O.bound);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
   for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + warp * 32) * 4; base < src.n; base += stride) {
     const int64_t i0 = base + lane * 4;
     uint64_t key[4];
     const unsigned ok = src.get4(i0, key);
-    const uint64_t ext = ~__ldcg(O.bound);
-    valid += __popc(ok);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) L.offer(k, key[q], i0 + q, (ok >> q) & 1u, ext);
-    uint64_t kk;
-    int64_t ki;
-    L.at(k - 1, kk, ki);
-    if (ki >= 0 && kk < published) {
-      if (lane == 0) atomicMax(O.bound, ~kk);
-      published = kk;
+    for (int q = 0; q < 4; ++q) {
+      const bool pass = ((ok >> q) & 1u) && key[q] <= cut;
+      const unsigned bal = __ballot_sync(0xffffffffu, pass);
+      if (!bal) continue;
+      unsigned at = 0;
+      if (lane == 0) at = atomicAdd(O.ticket, (unsigned)__popc(bal));
+      at = __shfl_sync(0xffffffffu, at, 0) + __popc(bal & ((1u << lane) - 1u));
+      if (pass && at < (unsigned)kTopkCap) {
+        O.cand_key[at] = key[q];
+        O.cand_idx[at] = i0 + q;
+      }
     }
   }
-  valid = __reduce_add_sync(0xffffffffu, valid);
-  if (lane == 0 && valid && O.valid_total) atomicAdd(O.valid_total, (unsigned long long)valid);
+}
+
+// one CTA of 256 threads: sort the candidates (or, past kTopkCap, rescan with warp lists)
+template <int R, class Src>
+__global__ void __launch_bounds__(256) k_tk_final(Src src, int k, TopkOut O) {
+  extern __shared__ unsigned char tk_smem[];
+  uint64_t* sk = reinterpret_cast<uint64_t*>(tk_smem);           // [kTopkCap]
+  int64_t* si = reinterpret_cast<int64_t*>(sk + kTopkCap);
+  const unsigned cnt = __ldcg(O.ticket);
+  if (cnt <= (unsigned)kTopkCap) {
+    int P = 2;
+    while (P < (int)cnt) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      const bool in = i < (int)cnt;
+      sk[i] = in ? __ldcg(&O.cand_key[i]) : ~0ull;
+      si[i] = in ? __ldcg(&O.cand_idx[i]) : INT64_MAX;
+    }
+    __syncthreads();
+    for (int size = 2; size <= P; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int t = threadIdx.x; t < P / 2; t += blockDim.x) {
+          const int i = 2 * t - (t & (stride - 1)), j = i + stride;
+          const bool up = (i & size) == 0;
+          const uint64_t ka = sk[i], kb = sk[j];
+          const int64_t ia = si[i], ib = si[j];
+          if (tk_better(kb, ib, ka, ia) == up) { sk[i] = kb; sk[j] = ka; si[i] = ib; si[j] = ia; }
+        }
+        __syncthreads();
+      }
+    const int m = (int)cnt < k ? (int)cnt : k;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) O.out_idx[j] = si[j];
+    if (threadIdx.x == 0) *O.out_count = m;
+    return;
+  }
+  // ties put more than kTopkCap items under the cut: warp lists over every item
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpList<R> L;
+  L.init();
+  for (int64_t base = warp * 128; base < src.n; base += 8 * 128) {
+    const int64_t i0 = base + lane * 4;
+    uint64_t key[4];
+    const unsigned ok = src.get4(i0, key);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) L.offer(k, key[q], i0 + q, (ok >> q) & 1u);
+  }
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     sk[warp * 32 * R + r * 32 + lane] = L.key[r];
     si[warp * 32 * R + r * 32 + lane] = L.idx[r];
-  }
-  __syncthreads();
-  if (warp == 0) {
-    WarpList<R> M;
-    M.init();
-    const uint64_t ext = ~__ldcg(O.bound);
-    for (int w = 0; w < 8; ++w)
-      for (int r = 0; r < R; ++r) {
-        const int p = r * 32 + lane;
-        const int64_t ii = si[w * 32 * R + p];
-        M.offer(k, sk[w * 32 * R + p], ii, p < k && ii >= 0, ext);
-      }
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int p = r * 32 + lane;
-      if (p < k) {
-        O.cand_key[(int64_t)blockIdx.x * k + p] = M.key[r];
-        O.cand_idx[(int64_t)blockIdx.x * k + p] = M.idx[r];
-      }
-    }
-    __threadfence();
-    unsigned prev = 0;
-    if (lane == 0) prev = atomicAdd(O.ticket, 1u);
-    prev = __shfl_sync(0xffffffffu, prev, 0);
-    if (lane == 0) last = (prev == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  // The last CTA: stage the per-CTA lists through shared memory (all threads,
-  // coalesced L2 loads) and let every warp merge its share, then warp 0
-  // merges the eight warp lists.
-  constexpr int CHUNK = 8 * 32 * R;
-  WarpList<R> F;
-  F.init();
-  const uint64_t fext = ~__ldcg(O.bound);
-  const int64_t total = (int64_t)gridDim.x * k;
-  for (int64_t base = 0; base < total; base += CHUNK) {
-    for (int j = threadIdx.x; j < CHUNK; j += blockDim.x) {
-      const int64_t g = base + j;
-      sk[j] = g < total ? __ldcg(&O.cand_key[g]) : ~0ull;
-      si[j] = g < total ? __ldcg(&O.cand_idx[g]) : -1;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int p = warp * 32 * R + r * 32 + lane;
-      F.offer(k, sk[p], si[p], si[p] >= 0, fext);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    sk[warp * 32 * R + r * 32 + lane] = F.key[r];
-    si[warp * 32 * R + r * 32 + lane] = F.idx[r];
   }
   __syncthreads();
   if (warp != 0) return;
@@ -261,26 +316,28 @@ __global__ void __launch_bounds__(256) k_topk_warp(Src src, int k, TopkOut O) {
       const int64_t ii = si[w * 32 * R + p];
       M.offer(k, sk[w * 32 * R + p], ii, p < k && ii >= 0);
     }
-  int cnt = 0;
+  int c = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int p = r * 32 + lane;
     const bool v = p < k && M.idx[r] >= 0;
-    cnt += __popc(__ballot_sync(0xffffffffu, v));
+    c += __popc(__ballot_sync(0xffffffffu, v));
     if (v) O.out_idx[p] = M.idx[r];
   }
-  if (lane == 0) {
-    *O.out_count = cnt;
-    *O.ticket = 0;
-  }
+  if (lane == 0) *O.out_count = c;
 }
 
-// Host launcher: k <= 256.  cand arrays hold grid*k entries each.
+// Host launcher: k <= 256.  The cand arrays hold topk_cand_entries(k) entries each;
+// O.ticket, O.bound and O.valid_total must be zero before the call.
 int topk_warp_launch(int kind, const void* src, int k, int grid, TopkOut O, cudaStream_t s);
 inline int topk_grid_size() { return num_sms(); }
+inline size_t topk_cand_entries(int k) {
+  const size_t a = (size_t)topk_grid_size() * k;
+  return a > (size_t)kTopkCand ? a : (size_t)kTopkCand;
+}
 inline size_t topk_scratch_bytes(int k) {
-  // ticket block + count + k indices + two [grid][k] candidate arrays, each 256-byte aligned
-  return 2 * align_up((size_t)topk_grid_size() * k * 8, 256) + align_up((size_t)k * 8, 256) + 1024;
+  // ticket block + count + k indices + two candidate arrays, each 256-byte aligned
+  return 2 * align_up(topk_cand_entries(k) * 8, 256) + align_up((size_t)k * 8, 256) + 1024;
 }
 
 }  // namespace tqpk

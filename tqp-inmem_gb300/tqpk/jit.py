@@ -43,6 +43,25 @@ __device__ __forceinline__ bool iscl(double x, double lit, double allowed) {
   double e = fabs(__dsub_rn(x, lit));
   return (x == lit) || (isfinite(e) && e <= allowed);
 }
+// bulk copies (TMA, 1-D) into shared memory, completed on an mbarrier
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(ok) : "r"(smem_u32(b)), "r"(parity) : "memory");
+  return ok != 0;
+}
 // predicate literals, bound at launch (one compiled kernel serves every constant)
 struct PL { long long i[32]; double f[32]; double a[32]; };
 template <class T> struct V4 { T v[4]; };
@@ -445,13 +464,17 @@ def _gather_pred(pred, prefix: str, lits: str, ptr_pfx: str, row: str, live: str
     return lines, _rename(expr, prefix, "G" + prefix)
 
 
-def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[str]) -> List[str]:
+def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[str], U: int = 2,
+                smem_vals: Optional[Dict[int, str]] = None) -> List[str]:
     """Warp-dense value pass: the warp's matched rows (queued as row offsets and
     slots in shared memory) are spread over all 32 lanes, so each FP64
     instruction and atomic runs with full lanes instead of the ~1 in 4 a
-    row-per-lane loop leaves active after the predicate and the lookups."""
+    row-per-lane loop leaves active after the predicate and the lookups.
+    Each lane holds U groups of 4 rows; value column c is read from global
+    memory, or from the shared-memory stage smem_vals[c] (indexed by the row's
+    offset in the warp's 128 * U rows)."""
     import re
-    lines = ["    const unsigned nm = __popc(m[0]) + __popc(m[1]);",
+    lines = [f"    const unsigned nm = {' + '.join(f'__popc(m[{u}])' for u in range(U))};",
              "    unsigned incl = nm;",
              "#pragma unroll",
              "    for (int o = 1; o < 32; o <<= 1) { const unsigned t = __shfl_up_sync(0xffffffffu, incl, o); "
@@ -459,18 +482,22 @@ def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[st
              "    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);",
              "    unsigned pos = incl - nm;",
              "#pragma unroll",
-             "    for (int u = 0; u < 2; ++u)",
+             f"    for (int u = 0; u < {U}; ++u)",
              "#pragma unroll",
              "      for (int j = 0; j < 4; ++j)",
-             f"        if ((m[u] >> j) & 1u) {{ q_off[wid][pos] = (unsigned char)(lane * 8 + u * 4 + j); "
+             f"        if ((m[u] >> j) & 1u) {{ q_off[wid][pos] = (unsigned char)(lane * {4 * U} + u * 4 + j); "
              f"q_slot[wid][pos] = (int){key}[u][j]; ++pos; }}",
              "    __syncwarp();",
              "    for (unsigned i = lane; i < total; i += 32) {",
-             "      const i64 row = wrow + q_off[wid][i];",
+             "      const int off = q_off[wid][i];",
+             "      const i64 row = wrow + off;",
              "      const i64 slot = q_slot[wid][i];"]
     for c in ecols:
         t = _CTYPE[S.col_dtypes[c]]
-        lines.append(f"      const {t} Cs{c} = __ldg((const {t}*)cp{c} + row);")
+        if smem_vals is not None:
+            lines.append(f"      const {t} Cs{c} = (({smem_vals[c]}))[off];")
+        else:
+            lines.append(f"      const {t} Cs{c} = __ldg((const {t}*)cp{c} + row);")
     for l in elines:
         lines.append("      " + re.sub(r"\bc(\d+)\.v\[j\]", r"Cs\1", l))
     lines.append(f"      atomicAdd(&sum[slot], (double)r{val_reg});")
@@ -543,6 +570,183 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None) -> Tuple[str, str]:
     src += _dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"])
     src += ["  }", "}"]
     return "\n".join(src), name
+
+
+TMA_ROWS = 128       # probe rows per staged chunk (one warp's rows: 4 per lane)
+
+
+def join_probe_tma_source(spec, val_reg: int, pred, bpred, fk_code: int, ST: int = 4) -> Tuple[str, str, int]:
+    """The fused probe + aggregate with its column streams staged by TMA, one ring per warp.
+
+    Every warp owns ST shared-memory stages and walks its own chunks of 128
+    probe rows (chunk c = global warp + i x all warps).  Its lane 0 copies a
+    chunk's column slices into a stage with 1-D bulk copies (cp.async.bulk,
+    completion counted on the stage's mbarrier) ST chunks ahead, so each warp
+    keeps ST x (24 B x 128) of HBM reads in flight while it filters, looks up
+    the directory and aggregates the chunk it has; no CTA-wide barrier is
+    involved after set-up.  The value pass is warp-dense and reads the values
+    from the stage.  The last warp of the grid handles the rows after the
+    last full chunk with plain loads.  Every stage wait is bounded: on expiry
+    the warp records TQPK_ETIMEOUT in *err, waits (bounded) for its copies in
+    flight and stops.  Returns (source, name, dynamic shared bytes)."""
+    S = spec
+    R = TMA_ROWS
+    pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
+    ecols, elines = _expr_code(S, val_reg + 1, "c")
+    name = "tqpk_q_join_probe_tma"
+    fkt = _CTYPE[fk_code]
+    size = {L.I8: 1, L.U8: 1, L.BOOL: 1, L.I32: 4, L.I64: 8, L.F64: 8}
+    cols = [("pp", c, pred.dtypes[c]) for c in pcols] + [("fk", 0, fk_code)] + \
+           [("cp", c, S.col_dtypes[c]) for c in ecols]
+    off, layout = 0, {}
+    for kind, c, dt in cols:
+        layout[(kind, c)] = (off, dt)
+        off += R * size[dt]
+    stage = off                                         # bytes of one stage (multiple of 128)
+    params = [f"const void* __restrict__ pp{c}" for c in range(pred.n_cols if pred is not None else 0)]
+    params += ["const PL lp"]
+    if bpred is not None:
+        params += [f"const void* __restrict__ bp{c}" for c in range(bpred.n_cols)]
+        params += ["const PL lb"]
+    params += [f"const void* __restrict__ cp{c}" for c in range(S.n_cols)]
+    params += ["const void* __restrict__ fk", "int fk_dt", "i64 np", "i64 key_min", "i64 slots",
+               "const int* __restrict__ dir", "double* __restrict__ sum", "u32* __restrict__ occ",
+               "int vp", "int vc", "int vf", "int* __restrict__ err"]
+
+    def issue(ind):
+        out = [f"{ind}mbar_expect_tx(&bar[wid][st], {stage}u);"]
+        for kind, c, dt in cols:
+            o, _ = layout[(kind, c)]
+            src = "fk" if kind == "fk" else f"{kind}{c}"
+            out.append(f"{ind}bulk_g2s(ring + st * {stage} + {o}, (const unsigned char*){src} + ch * "
+                       f"{R * size[dt]}ll, {R * size[dt]}u, &bar[wid][st]);")
+        return out
+
+    body = ["    const unsigned char* S0 = ring + st * " + str(stage) + ";",
+            f"    const i64 wrow = ch * {R};",
+            "    i64 sl[1][4]; int rw[1][4]; unsigned m[1];",
+            "    {",
+            "      const int u = 0;",
+            "      const int lr = lane * 4;"]
+    for c in pcols:
+        o, dt = layout[("pp", c)]
+        body.append(f"      const V4<{_CTYPE[dt]}> P{c} = ld4((const {_CTYPE[dt]}*)(S0 + {o}) + lr, 0, 4, true);")
+    o, _ = layout[("fk", 0)]
+    body += [f"      const V4<{fkt}> F = ld4((const {fkt}*)(S0 + {o}) + lr, 0, 4, true);",
+             "      m[0] = 0;",
+             "#pragma unroll",
+             "      for (int j = 0; j < 4; ++j) {",
+             "        sl[0][j] = (i64)F.v[j] - key_min;",
+             f"        const bool ok = ({_rename(pexpr, 'p', 'P')}) && sl[0][j] >= 0 && sl[0][j] < slots;",
+             "        m[0] |= (unsigned)ok << j;",
+             "      }",
+             "#pragma unroll",
+             "      for (int j = 0; j < 4; ++j) {",
+             "        rw[0][j] = ((m[0] >> j) & 1u) ? __ldg(&dir[sl[0][j]]) : -1;",
+             "        if (rw[0][j] < 0) m[0] &= ~(1u << j);",
+             "      }"]
+    if bpred is not None:
+        glines, gexpr = _gather_pred(bpred, "b", "lb", "bp", "rw[u]", "m[u]")
+        body += ["      if (m[0]) {"] + ["        " + l for l in glines]
+        body += ["#pragma unroll", "        for (int j = 0; j < 4; ++j)",
+                 f"          if (((m[u] >> j) & 1u) && !({gexpr})) m[u] &= ~(1u << j);", "      }"]
+    body += ["    }"]
+    smem_vals = {c: f"(const {_CTYPE[layout[('cp', c)][1]]}*)(S0 + {layout[('cp', c)][0]})" for c in ecols}
+    body += _dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"], U=1, smem_vals=smem_vals)
+    # rows after the last full chunk: the grid's last warp, plain loads
+    tail = ["  if (blockIdx.x == gridDim.x - 1 && wid == 7) {",
+            f"    for (i64 w0 = (nch * {R} >> 2); w0 < ((np + 3) >> 2); w0 += 32) {{",
+            "      const i64 g = w0 + lane, wrow = w0 << 2;",
+            "      i64 sl[1][4]; int rw[1][4]; unsigned m[1];",
+            "      {",
+            "        const int u = 0;",
+            "        const i64 r0 = g << 2;",
+            "        m[0] = 0;",
+            "        if (r0 < np) {"]
+    tail += ["          " + l for l in _load_lines(pcols, pred.dtypes, "P", "pp", "np", "false")] if pred is not None else []
+    tail += [f"          const V4<{fkt}> F = ld4((const {fkt}*)fk, r0, np, false);",
+             "#pragma unroll",
+             "          for (int j = 0; j < 4; ++j) {",
+             "            sl[0][j] = (i64)F.v[j] - key_min;",
+             f"            const bool ok = (r0 + j < np) && ({_rename(pexpr, 'p', 'P')}) && sl[0][j] >= 0 && sl[0][j] < slots;",
+             "            m[0] |= (unsigned)ok << j;",
+             "          }",
+             "        }",
+             "#pragma unroll",
+             "        for (int j = 0; j < 4; ++j) {",
+             "          rw[0][j] = ((m[0] >> j) & 1u) ? __ldg(&dir[sl[0][j]]) : -1;",
+             "          if (rw[0][j] < 0) m[0] &= ~(1u << j);",
+             "        }"]
+    if bpred is not None:
+        glines, gexpr = _gather_pred(bpred, "b", "lb", "bp", "rw[u]", "m[u]")
+        tail += ["        if (m[0]) {"] + ["          " + l for l in glines]
+        tail += ["#pragma unroll", "          for (int j = 0; j < 4; ++j)",
+                 f"            if (((m[u] >> j) & 1u) && !({gexpr})) m[u] &= ~(1u << j);", "        }"]
+    tail += ["      }"]
+    tail += ["  " + l for l in _dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"], U=1)]
+    tail += ["    }", "  }"]
+    src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__(256) {name}(',
+           "    " + ",\n    ".join(params) + ") {",
+           "  extern __shared__ __align__(1024) unsigned char stg[];",
+           f"  __shared__ __align__(8) unsigned long long bar[8][{ST}];",
+           f"  __shared__ unsigned char q_off[8][{R}];",
+           f"  __shared__ int q_slot[8][{R}];",
+           "  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;",
+           f"  unsigned char* ring = stg + wid * {ST * stage};",
+           f"  const i64 nch = np / {R};",
+           "  const i64 gw = (i64)blockIdx.x * 8 + wid, nw = (i64)gridDim.x * 8;",
+           "  if (threadIdx.x == 0) {",
+           f"    for (int w = 0; w < 8; ++w) for (int st = 0; st < {ST}; ++st) mbar_init(&bar[w][st], 1);",
+           "    mbar_fence_init();",
+           "  }",
+           "  __syncthreads();",
+           "  unsigned pend = 0, ppar = 0;      // lane 0: stages with a copy in flight and their phase parity",
+           "  if (lane == 0)",
+           f"    for (int st = 0; st < {ST}; ++st) {{",
+           "      const i64 ch = gw + st * nw;",
+           "      if (ch >= nch) break;"]
+    src += issue("      ")
+    src += ["      pend |= 1u << st;",
+            "    }",
+            "  int stop = 0;",
+            "  for (i64 it = 0;; ++it) {",
+            "    const i64 ch = gw + it * nw;",
+            "    if (ch >= nch) break;",
+            f"    const int st = (int)(it % {ST});",
+            f"    const unsigned par = (unsigned)((it / {ST}) & 1);",
+            "    if (lane == 0) {",
+            "      int spins = 0;",
+            "      while (!mbar_try_wait(&bar[wid][st], par))",
+            "        if (++spins > (1 << 20)) { atomicCAS(err, 0, -3); stop = 1; break; }",
+            "      if (!stop) pend &= ~(1u << st);",
+            "    }",
+            "    stop = __shfl_sync(0xffffffffu, stop, 0);",
+            "    if (stop) break;"]
+    src += body
+    src += ["    if (lane == 0) {                 // every lane is done with the stage (the tail's __syncwarp)",
+            f"      const i64 ch2 = ch + {ST} * nw;",
+            "      if (ch2 < nch) {",
+            "        const i64 ch = ch2;"]
+    src += issue("        ")
+    src += ["        pend |= 1u << st;",
+            f"        ppar = (ppar & ~(1u << st)) | ((unsigned)(((it + {ST}) / {ST}) & 1) << st);",
+            "      }",
+            "    }",
+            "  }",
+            "  if (stop) {",
+            "    // give this warp's copies still in flight a bounded time to land before it exits",
+            "    if (lane == 0)",
+            f"      for (int st = 0; st < {ST}; ++st) {{",
+            "        if (!((pend >> st) & 1u)) continue;",
+            "        int spins = 0;",
+            "        while (!mbar_try_wait(&bar[wid][st], (ppar >> st) & 1u) && ++spins < (1 << 16)) {}",
+            "      }",
+            "    __syncwarp();",
+            "    return;",
+            "  }"]
+    src += tail
+    src += ["}"]
+    return "\n".join(src), name, 8 * ST * stage
 
 
 def join_probe_args(a: "_Args", spec, pred, bpred, fk, np_: int, key_min: int, slots: int, dir_ptr: int,

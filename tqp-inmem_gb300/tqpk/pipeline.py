@@ -62,23 +62,46 @@ class JoinAggTopK:
             self.out_vals.data_ptr(), self.out_count.data_ptr(), self.groups.data_ptr(), s),
             "tqpk_pipeline_join_agg_topk")
 
+    def _tma_ok(self) -> bool:
+        """The TMA-staged probe: every staged column 16-byte aligned and at least one full chunk."""
+        import os
+        from . import jit
+        cols = [self.pk] + list(self.prog.tensors) + (list(self.ppred.tensors) if self.ppred else [])
+        return (os.environ.get("TQPK_TMA", "1") != "0" and self.pk.numel() >= jit.TMA_ROWS
+                and self.pk.dtype in (torch.int32, torch.int64) and all(t.data_ptr() % 16 == 0 for t in cols))
+
     def _jit_probe(self, s):
         """The probe + aggregate pass as a query-specialised kernel."""
         from . import jit
         if not hasattr(self, "_probe_handle"):
-            src, name = jit.join_probe_source(self.prog.spec, self.value_reg,
-                                              self.ppred.struct if self.ppred else None)
+            pp = self.ppred.struct if self.ppred else None
+            self._probe_smem = 0
+            if self._tma_ok():
+                import os
+                src, name, self._probe_smem = jit.join_probe_tma_source(
+                    self.prog.spec, self.value_reg, pp, None, code_of(self.pk.dtype),
+                    ST=int(os.environ.get("TQPK_TMA_STAGES", "4")))
+            else:
+                src, name = jit.join_probe_source(self.prog.spec, self.value_reg, pp)
             self._probe_handle = jit.compile_kernel(src, name)
             d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
             L.check(self.lib.tqpk_pipeline_join_tables(self.ws.data_ptr(), self.ws.numel(), self.key_min,
                                                        self.key_max, C.byref(d), C.byref(su), C.byref(oc)),
                     "tqpk_pipeline_join_tables")
             self._probe_args = jit.join_probe_args(
-                jit._Args(), self.prog.spec, self.ppred.struct if self.ppred else None, None, self.pk,
+                jit._Args(), self.prog.spec, pp, None, self.pk,
                 self.pk.numel(), self.key_min, self.key_max - self.key_min + 1, d.value, su.value, oc.value,
                 pred_tensors=self.ppred.tensors if self.ppred else (), col_tensors=self.prog.tensors)
-            self._probe_grid = jit.occupancy_grid(self._probe_handle, 256, 0, (self.pk.numel() + 7) // 8)
-        jit.launch(self._probe_handle, self._probe_grid, 256, 0, self._probe_args, s, L.KID_PIPE_PROBE)
+            if self._probe_smem:
+                self._probe_err = torch.zeros(1, dtype=torch.int32, device=self.dev)
+                self._probe_args.ptr(self._probe_err.data_ptr())
+                # one warp per 128-row chunk at a time: enough CTAs for every chunk, at most one wave
+                self._probe_grid = jit.occupancy_grid(self._probe_handle, 256, self._probe_smem,
+                                                      max(1, self.pk.numel() // jit.TMA_ROWS) * 32)
+            else:
+                self._probe_grid = jit.occupancy_grid(self._probe_handle, 256, 0, (self.pk.numel() + 7) // 8)
+        jit.launch(self._probe_handle, self._probe_grid, 256, self._probe_smem, self._probe_args, s,
+                   L.KID_PIPE_PROBE)
 
     def run(self, stream=None):
         from . import jit
@@ -90,8 +113,26 @@ class JoinAggTopK:
         else:
             self._stages(7, s)
 
+
+    def capture(self):
+        """Records one run (every memset and launch, no host synchronisation inside) in a CUDA
+        graph; replay() then re-runs the whole query with one graph launch."""
+        self.run()
+        torch.cuda.synchronize(self.dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.run()
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()
+
     def check_error(self, stream=None):
         s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
+        if getattr(self, "_probe_smem", 0):
+            e = int(self._probe_err.item())
+            if e:
+                L.check(e, "TMA-staged probe (a stage wait expired)")
         err = C.c_int(0)
         L.check(self.lib.tqpk_pipeline_error(self.ws.data_ptr(), C.byref(err), s), "tqpk_pipeline_error")
         if err.value:
@@ -226,6 +267,18 @@ class StarAggTopK:
             self.ws.data_ptr(), self.ws.numel(), self.out_keys.data_ptr(), self.out_vals.data_ptr(),
             self.out_cnts.data_ptr(), self.out_count.data_ptr(), self.groups.data_ptr(), s),
             "tqpk_pipeline_star_agg_topk")
+
+    def capture(self):
+        """Records one run in a CUDA graph (see JoinAggTopK.capture)."""
+        self.run()
+        torch.cuda.synchronize(self.dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.run()
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()
 
     def result(self):
         s = torch.cuda.current_stream(self.dev).cuda_stream

@@ -43,6 +43,41 @@ PEAK_FALLBACK_GBS = 6800.0
 
 
 # ---------------------------------------------------------------------------- workloads
+class StagedInputs:
+    """Host->device copies of one step's input columns on a copy stream, in the order the plan
+    reads them, with one event per column: each operator waits only for the columns it reads,
+    so the later columns' copies overlap the earlier operators."""
+
+    def __init__(self, host, dev, types, order):
+        import torch
+        self.host, self.dev, self.types, self.order = host, dev, types, list(order)
+        self.copy_stream = torch.cuda.Stream(dev)
+
+    def start(self):
+        import torch
+        from tqpk.variable import Variable
+        main = torch.cuda.current_stream(self.dev)
+        self.dst = {c: torch.empty(h.shape, dtype=h.dtype, device=self.dev) for c, h in self.host.items()}
+        self.copy_stream.wait_stream(main)          # the buffers are allocated on the main stream
+        self.ev = {}
+        with torch.cuda.stream(self.copy_stream):
+            for c in self.order:
+                self.dst[c].copy_(self.host[c], non_blocking=True)
+                self.ev[c] = torch.cuda.Event()
+                self.ev[c].record(self.copy_stream)
+        return {c: Variable(t, self.types[c]) for c, t in self.dst.items()}
+
+    def need(self, *cols):
+        import torch
+        main = torch.cuda.current_stream(self.dev)
+        for c in cols:
+            main.wait_event(self.ev[c])
+
+    @property
+    def bytes(self):
+        return sum(h.numel() * h.element_size() for h in self.host.values())
+
+
 class JoinAggTop10:
     name = "join_agg_top10"
     NB, NP = 1_500_000, 6_001_215
@@ -112,9 +147,14 @@ class JoinAggTop10:
         import torch
         from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
         from tqpk.variable import Variable
-        tg = {c: Variable(h.to(self.dev, non_blocking=True), self.types[c]) for c, h in self.host.items()}
+        if not hasattr(self, "staged"):
+            self.staged = StagedInputs(self.host, self.dev, self.types, (12, 22, 11, 21, 23, 24))
+        tg = self.staged.start()
+        self.staged.need(12)
         tqp_filter(True, tg, copy.deepcopy(self.f1), None, None, None, "f1")
+        self.staged.need(22)
         tqp_filter(True, tg, copy.deepcopy(self.f2), None, None, None, "f2")
+        self.staged.need(11, 21, 23, 24)
         join_vortex(True, tg, copy.deepcopy(self.jargs), 11, 21, [], "inner", None, None, "j")
         tqp_hash_aggregate(True, tg, copy.deepcopy(self.aargs), None, None, "a")
         tqp_sort(True, tg, copy.deepcopy(self.targs), True, "t")
@@ -213,8 +253,12 @@ class FilterGroupBy:
     def step_e2e(self):
         from tqpk.operators import tqp_filter, tqp_hash_aggregate, tqp_sort
         from tqpk.variable import Variable
-        tg = {c: Variable(h.to(self.dev, non_blocking=True), self.types[c]) for c, h in self.host.items()}
+        if not hasattr(self, "staged"):
+            self.staged = StagedInputs(self.host, self.dev, self.types, (7, 5, 6, 1, 2, 3, 4))
+        tg = self.staged.start()
+        self.staged.need(7)
         tqp_filter(True, tg, copy.deepcopy(self.fargs), None, None, None, "f")
+        self.staged.need(5, 6, 1, 2, 3, 4)
         tqp_hash_aggregate(True, tg, copy.deepcopy(self.aargs), None, None, "a")
         tqp_sort(True, tg, copy.deepcopy(self.sargs), False, "s")
         out = {c: tg[c].tensor.to("cpu").numpy() for c in self.sargs["input ids"]}
@@ -310,12 +354,16 @@ class StarJoin:
     def step_e2e(self):
         from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
         from tqpk.variable import Variable
-        tg = {c: Variable(h.to(self.dev, non_blocking=True), self.types[c]) for c, h in self.host.items()}
+        if not hasattr(self, "staged"):
+            self.staged = StagedInputs(self.host, self.dev, self.types, (32, 31, 41, 42, 43, 44, 51, 52, 61))
+        tg = self.staged.start()
 
         def f(tg, a):
+            self.staged.need(*a["materialized in"])
             tqp_filter(True, tg, a, None, None, None, "f")
 
         def j(tg, a, lk, rk):
+            self.staged.need(*[c for c in a["left group"] + a["right group"] if c in self.staged.ev])
             join_vortex(True, tg, a, lk, rk, [], "inner", None, None, "j")
             return tg
 
@@ -595,6 +643,12 @@ def run_serving_bench(args):
 WORKLOADS = {c.name: c for c in (JoinAggTop10, FilterGroupBy, StarJoin)}
 
 
+def make_workload(args):
+    if args.workload == "star_join":
+        return StarJoin(scale=args.scale)
+    return WORKLOADS[args.workload]()
+
+
 # ---------------------------------------------------------------------------- helpers
 def peak_gbs():
     p = ROOT / "MEASURED_PEAKS.json"
@@ -755,7 +809,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     import multiprocessing as mp
-    w = WORKLOADS[args.workload]()
+    w = make_workload(args)
     cores = os.cpu_count() or 1
     procs = max(1, min(cores, args.steps))
     ctx = mp.get_context("spawn")
@@ -789,7 +843,7 @@ def run_ours(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = WORKLOADS[args.workload]()
+    w = make_workload(args)
     w.setup_device(dev)
 
     # correctness gate (outside the timed region)
@@ -915,6 +969,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batched", "serving"], default="join_agg_top10")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="star_join only: table sizes x scale (a small case for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -21,7 +21,7 @@ static int launch_r(const Src& src, int k, int grid, TopkOut O, cudaStream_t s) 
   const int ng = (int)std::max<int64_t>(1, (src.n + G - 1) / G);
   k_tk_group_best<Src><<<ng, 256, 0, s>>>(src, G, O);
   TQPK_CHECK_LAUNCH();
-  k_tk_cut<<<1, 1024, 0, s>>>(ng, k, O);
+  k_tk_cut<<<1, 256, 0, s>>>(ng, k, O);
   TQPK_CHECK_LAUNCH();
   const int64_t units = (src.n + 1023) / 1024;
   k_tk_filter<Src><<<(int)std::max<int64_t>(1, std::min<int64_t>(units, (int64_t)num_sms() * 8)), 256, 0, s>>>(src, O);

@@ -170,7 +170,7 @@ struct TopkOut {
 // ties push more than kTopkCap items under the cut, that CTA falls back to
 // the warp lists over all items (same result, slower).
 constexpr int kTopkCap = 4096;
-constexpr int kTopkGroups = 2048;
+constexpr int kTopkGroups = 512;     // >= 2 x the largest k: the cut stays near the k-th item
 constexpr int kTopkCand = kTopkCap + kTopkGroups;   // cand_key entries used: candidates, then group bests
 
 __device__ __forceinline__ void block_min_u64(uint64_t& v, uint64_t* red) {
@@ -215,8 +215,8 @@ __global__ void __launch_bounds__(256) k_tk_group_best(Src src, int64_t G, TopkO
   }
 }
 
-// one CTA of 1024 threads: bitonic sort of the group bests, cut = the k-th
-static __global__ void __launch_bounds__(1024) k_tk_cut(int ng, int k, TopkOut O) {
+// one CTA of 256 threads: bitonic sort of the group bests, cut = the k-th
+static __global__ void __launch_bounds__(256) k_tk_cut(int ng, int k, TopkOut O) {
   __shared__ uint64_t v[kTopkGroups];
   for (int i = threadIdx.x; i < kTopkGroups; i += blockDim.x) v[i] = i < ng ? __ldcg(&O.cand_key[kTopkCap + i]) : ~0ull;
   __syncthreads();

@@ -485,7 +485,7 @@ def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[st
              f"    for (int u = 0; u < {U}; ++u)",
              "#pragma unroll",
              "      for (int j = 0; j < 4; ++j)",
-             f"        if ((m[u] >> j) & 1u) {{ q_off[wid][pos] = (unsigned char)(lane * {4 * U} + u * 4 + j); "
+             f"        if ((m[u] >> j) & 1u) {{ q_off[wid][pos] = (lane * {4 * U} + u * 4 + j); "
              f"q_slot[wid][pos] = (int){key}[u][j]; ++pos; }}",
              "    __syncwarp();",
              "    for (unsigned i = lane; i < total; i += 32) {",
@@ -506,15 +506,25 @@ def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[st
     return lines
 
 
-def join_probe_source(spec, val_reg: int, pred, bpred=None) -> Tuple[str, str]:
+PROBE_U = 1          # 4-row groups per lane in the register probe: 4 rows, 32 registers, full occupancy
+
+
+def probe_units(n: int) -> int:
+    """Threads the register probes need for n rows (4 * PROBE_U rows per thread)."""
+    return (int(n) + 4 * PROBE_U - 1) // (4 * PROBE_U)
+
+
+def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, min_blocks: int = 0
+                      ) -> Tuple[str, str]:
     """CUDA source of the fused probe + aggregate (directory lookup, value, FP64 sum, occupancy).
 
     The directory holds build row indices (negative = no row).  `bpred`, when
     given, is a predicate over build-side columns evaluated through the row
     index (a resident directory serving queries with their own build filter).
-    Each lane filters and looks up 8 consecutive rows (4-row vector loads); the
-    warp then computes the value and updates the group of its matched rows
-    densely (_dense_tail)."""
+    Each lane filters and looks up 4U consecutive rows (4-row vector loads);
+    the warp then computes the value and updates the group of its matched rows
+    densely (_dense_tail).  min_blocks > 0 asks the compiler for that many
+    resident CTAs per SM (__launch_bounds__ register cap)."""
     S = spec
     pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
     ecols, elines = _expr_code(S, val_reg + 1, "c")
@@ -531,18 +541,22 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None) -> Tuple[str, str]:
     fk_load = ("const V4<i64> F = (fk_dt == 4) ? ld4((const long long*)fk, r0, np, vf != 0) : "
                "[&]{ V4<int> t = ld4((const int*)fk, r0, np, vf != 0); V4<i64> o; "
                "for (int q = 0; q < 4; ++q) o.v[q] = t.v[q]; return o; }();")
-    src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__(256) {name}(', "    " + ",\n    ".join(params) + ") {",
-           "  __shared__ unsigned char q_off[8][256];",
-           "  __shared__ int q_slot[8][256];",
+    rows = 4 * U                                   # rows per lane
+    qt = "unsigned char" if 32 * rows <= 256 else "unsigned short"
+    lb = f"256, {min_blocks}" if min_blocks else "256"
+    src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__({lb}) {name}(',
+           "    " + ",\n    ".join(params) + ") {",
+           f"  __shared__ {qt} q_off[8][{32 * rows}];",
+           f"  __shared__ int q_slot[8][{32 * rows}];",
            "  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;",
-           "  const i64 n8 = (np + 7) >> 3;",
+           f"  const i64 nr = (np + {rows - 1}) / {rows};",
            "  const i64 stride = (i64)gridDim.x * blockDim.x;",
-           "  for (i64 w0 = blockIdx.x * (i64)blockDim.x + (threadIdx.x & ~31); w0 < n8; w0 += stride) {",
-           "    const i64 g = w0 + lane, wrow = w0 << 3;",
-           "    i64 sl[2][4]; int rw[2][4]; unsigned m[2];",
+           "  for (i64 w0 = blockIdx.x * (i64)blockDim.x + (threadIdx.x & ~31); w0 < nr; w0 += stride) {",
+           f"    const i64 g = w0 + lane, wrow = w0 * {rows};",
+           f"    i64 sl[{U}][4]; int rw[{U}][4]; unsigned m[{U}];",
            "#pragma unroll",
-           "    for (int u = 0; u < 2; ++u) {",
-           "      const i64 r0 = ((g << 1) + u) << 2;",
+           f"    for (int u = 0; u < {U}; ++u) {{",
+           f"      const i64 r0 = g * {rows} + u * 4;",
            "      m[u] = 0;",
            "      if (r0 >= np) continue;"]
     src += ["      " + l for l in _load_lines(pcols, pred.dtypes, "P", "pp", "np", "vp != 0")] if pred is not None else []
@@ -555,7 +569,7 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None) -> Tuple[str, str]:
             "      }",
             "    }",
             "#pragma unroll",
-            "    for (int u = 0; u < 2; ++u)",
+            f"    for (int u = 0; u < {U}; ++u)",
             "#pragma unroll",
             "      for (int j = 0; j < 4; ++j) {",
             "        rw[u][j] = ((m[u] >> j) & 1u) ? __ldg(&dir[sl[u][j]]) : -1;",
@@ -563,11 +577,11 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None) -> Tuple[str, str]:
             "      }"]
     if bpred is not None:
         glines, gexpr = _gather_pred(bpred, "b", "lb", "bp", "rw[u]", "m[u]")
-        src += ["#pragma unroll", "    for (int u = 0; u < 2; ++u) {", "      if (!m[u]) continue;"]
+        src += ["#pragma unroll", f"    for (int u = 0; u < {U}; ++u) {{", "      if (!m[u]) continue;"]
         src += ["      " + l for l in glines]
         src += ["#pragma unroll", "      for (int j = 0; j < 4; ++j)",
                 f"        if (((m[u] >> j) & 1u) && !({gexpr})) m[u] &= ~(1u << j);", "    }"]
-    src += _dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"])
+    src += _dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"], U=U)
     src += ["  }", "}"]
     return "\n".join(src), name
 
@@ -777,7 +791,8 @@ def join_probe_args(a: "_Args", spec, pred, bpred, fk, np_: int, key_min: int, s
 
 
 # ---------------------------------------------------------------------------- star probe
-def star_probe_source(spec, val_reg: int, fpred, apred) -> Tuple[str, str]:
+def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_blocks: int = 0
+                      ) -> Tuple[str, str]:
     """CUDA source of the star probe: fact -> A (row directory, A predicate through the
     row) -> B (directory of the C foreign key) -> C (row directory), then FP64 sum and
     count per C slot, computed warp-densely over the matched rows (_dense_tail).
@@ -798,18 +813,21 @@ def star_probe_source(spec, val_reg: int, fpred, apred) -> Tuple[str, str]:
                "i64 b_min", "i64 b_slots", "const int* __restrict__ dir_b",
                "i64 c_min", "i64 c_slots", "const int* __restrict__ dir_c",
                "double* __restrict__ sum", "u32* __restrict__ cnt", "int vp", "int vc", "int vf"]
-    src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__(256) {name}(', "    " + ",\n    ".join(params) + ") {",
-           "  __shared__ unsigned char q_off[8][256];",
-           "  __shared__ int q_slot[8][256];",
+    rows = 4 * U
+    qt = "unsigned char" if 32 * rows <= 256 else "unsigned short"
+    lb = f"256, {min_blocks}" if min_blocks else "256"
+    src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__({lb}) {name}(', "    " + ",\n    ".join(params) + ") {",
+           f"  __shared__ {qt} q_off[8][{32 * rows}];",
+           f"  __shared__ int q_slot[8][{32 * rows}];",
            "  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;",
-           "  const i64 n8 = (nf + 7) >> 3;",
+           f"  const i64 nr = (nf + {rows - 1}) / {rows};",
            "  const i64 stride = (i64)gridDim.x * blockDim.x;",
-           "  for (i64 w0 = blockIdx.x * (i64)blockDim.x + (threadIdx.x & ~31); w0 < n8; w0 += stride) {",
-           "    const i64 g = w0 + lane, wrow = w0 << 3;",
-           "    i64 k[2][4]; int rw[2][4]; unsigned m[2];",
+           "  for (i64 w0 = blockIdx.x * (i64)blockDim.x + (threadIdx.x & ~31); w0 < nr; w0 += stride) {",
+           f"    const i64 g = w0 + lane, wrow = w0 * {rows};",
+           f"    i64 k[{U}][4]; int rw[{U}][4]; unsigned m[{U}];",
            "#pragma unroll",
-           "    for (int u = 0; u < 2; ++u) {",
-           "      const i64 r0 = ((g << 1) + u) << 2;",
+           f"    for (int u = 0; u < {U}; ++u) {{",
+           f"      const i64 r0 = g * {rows} + u * 4;",
            "      m[u] = 0;",
            "      if (r0 >= nf) continue;"]
     src += ["      " + l for l in _load_lines(pcols, fpred.dtypes, "P", "pp", "nf", "vp != 0")] if fpred is not None else []
@@ -822,7 +840,7 @@ def star_probe_source(spec, val_reg: int, fpred, apred) -> Tuple[str, str]:
             "      }",
             "    }",
             "#pragma unroll",
-            "    for (int u = 0; u < 2; ++u)",
+            f"    for (int u = 0; u < {U}; ++u)",
             "#pragma unroll",
             "      for (int j = 0; j < 4; ++j) {",
             "        rw[u][j] = ((m[u] >> j) & 1u) ? __ldg(&dir_a[k[u][j]]) : -1;",
@@ -830,14 +848,14 @@ def star_probe_source(spec, val_reg: int, fpred, apred) -> Tuple[str, str]:
             "      }"]
     if apred is not None:
         glines, gexpr = _gather_pred(apred, "a", "la", "ap", "rw[u]", "m[u]")
-        src += ["#pragma unroll", "    for (int u = 0; u < 2; ++u) {", "      if (!m[u]) continue;"]
+        src += ["#pragma unroll", f"    for (int u = 0; u < {U}; ++u) {{", "      if (!m[u]) continue;"]
         src += ["      " + l for l in glines]
         src += ["#pragma unroll", "      for (int j = 0; j < 4; ++j)",
                 f"        if (((m[u] >> j) & 1u) && !({gexpr})) m[u] &= ~(1u << j);", "    }"]
     src += ["#pragma unroll",
-            "    for (int u = 0; u < 2; ++u) {",
+            f"    for (int u = 0; u < {U}; ++u) {{",
             "      if (!m[u]) continue;",
-            "      const i64 r0 = ((g << 1) + u) << 2;",
+            f"      const i64 r0 = g * {rows} + u * 4;",
             "      const V4<int> FB = ld4(fkb, r0, nf, vf != 0);",
             "#pragma unroll",
             "      for (int j = 0; j < 4; ++j) {",
@@ -849,10 +867,10 @@ def star_probe_source(spec, val_reg: int, fpred, apred) -> Tuple[str, str]:
             "      }",
             "    }",
             "#pragma unroll",
-            "    for (int u = 0; u < 2; ++u)",
+            f"    for (int u = 0; u < {U}; ++u)",
             "#pragma unroll",
             "      for (int j = 0; j < 4; ++j)",
             "        if (((m[u] >> j) & 1u) && __ldg(&dir_c[k[u][j]]) < 0) m[u] &= ~(1u << j);"]
-    src += _dense_tail(S, val_reg, ecols, elines, "nf", "k", ["atomicAdd(&cnt[slot], 1u);"])
+    src += _dense_tail(S, val_reg, ecols, elines, "nf", "k", ["atomicAdd(&cnt[slot], 1u);"], U=U)
     src += ["  }", "}"]
     return "\n".join(src), name

@@ -342,7 +342,7 @@ class GpuExecutor:
         self.j_bpred = compile_filter([["bd#12", "<", "1170"]], {12: jt["b_date"]})
         src, name = jit.join_probe_source(self.j_prog.spec, self.j_reg, self.j_ppred.struct, self.j_bpred.struct)
         self.j_kernel = jit.compile_kernel(src, name)
-        self.j_grid = jit.occupancy_grid(self.j_kernel, 256, 0, (tables.n_fact + 7) // 8)
+        self.j_grid = jit.occupancy_grid(self.j_kernel, 256, 0, jit.probe_units(tables.n_fact))
         # star: A's filter through A's row directory
         fcols = {33: st["f_price"], 34: st["f_discount"]}
         self.s_prog = compile_aggregate(
@@ -352,7 +352,7 @@ class GpuExecutor:
         self.s_apred = compile_filter([["cat#42", "=", "1"]], {42: st["a_cat"]})
         src, name = jit.star_probe_source(self.s_prog.spec, self.s_reg, None, self.s_apred.struct)
         self.s_kernel = jit.compile_kernel(src, name)
-        self.s_grid = jit.occupancy_grid(self.s_kernel, 256, 0, (tables.n_fact + 7) // 8)
+        self.s_grid = jit.occupancy_grid(self.s_kernel, 256, 0, jit.probe_units(tables.n_fact))
         self.topk_ws = {k: self.lib.tqpk_dense_topk_workspace_bytes(k) for k in (self.JOIN_K, self.STAR_K)}
 
     # -- literals, cached per (shape, constants)

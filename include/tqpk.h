@@ -67,7 +67,16 @@ enum { TQPK_ROWID = 0, TQPK_I8 = 1, TQPK_U8 = 2, TQPK_I32 = 3, TQPK_I64 = 4, TQP
  * Float literals for <= and >= arrive with the reference's +-eps already added
  * (filter.py:145-149).                                                      */
 enum { TQPK_P_CMP = 1, TQPK_P_AND = 2, TQPK_P_OR = 3, TQPK_P_NOT = 4, TQPK_P_TRUE = 5,
-       TQPK_P_FALSE = 6, TQPK_P_MASK = 7, TQPK_P_CMPCOL = 8 /* cols[col] <cmp> cols[lit_i] */ };
+       TQPK_P_FALSE = 6, TQPK_P_MASK = 7, TQPK_P_CMPCOL = 8 /* cols[col] <cmp> cols[lit_i] */,
+       /* string columns: int8 [N, w], w = widths[col]; literals are bytes of strpool.
+        * STRCMP: every byte of the row <cmp> the literal padded to w (lit_i = offset),
+        *         the reference's multi-character comparison (filter.py:151-158).
+        * PREFIX: the first len bytes equal the literal (StartsWith, filter.py:48-55).
+        * CONTAINS: the literal occurs at some position (Contains/EndsWith, like.py:3-11).
+        *         PREFIX/CONTAINS: lit_i = offset | len << 32.
+        * LIKE2:  '%a%b%': b starts at or after the end of an occurrence of a (like.py:13-22);
+        *         lit_i = off_a | len_a << 16 | off_b << 32 | len_b << 48.            */
+       TQPK_P_STRCMP = 9, TQPK_P_PREFIX = 10, TQPK_P_CONTAINS = 11, TQPK_P_LIKE2 = 12 };
 enum { TQPK_LT = 0, TQPK_LE = 1, TQPK_GT = 2, TQPK_GE = 3, TQPK_EQ = 4, TQPK_NE = 5, TQPK_ISCLOSE = 6 };
 enum { TQPK_DOM_I64 = 0, TQPK_DOM_F64 = 1, TQPK_DOM_F32 = 2 };
 
@@ -78,12 +87,16 @@ typedef struct {
   double lit_aux;
 } tqpk_pred_insn;
 
+#define TQPK_MAX_STRPOOL 512
+
 typedef struct {
   int32_t n_insn;
   int32_t n_cols;
   const void* cols[TQPK_MAX_COLS];
   int32_t dtypes[TQPK_MAX_COLS];
   tqpk_pred_insn insn[TQPK_MAX_PRED];
+  int32_t widths[TQPK_MAX_COLS];      /* bytes per row of an int8 [N, w] string column, else 0 */
+  uint8_t strpool[TQPK_MAX_STRPOOL];  /* literal bytes of the string instructions */
 } tqpk_predicate;
 
 /* ---- row expressions (aggregate.py:58-233, arithmetic part) --------------

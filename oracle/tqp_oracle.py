@@ -89,11 +89,39 @@ def _isclose(a: np.ndarray, b: float, rtol=1e-5, atol=EPS) -> np.ndarray:
     return (a == b) | (np.isfinite(err) & (err <= allowed))
 
 
+def _str_bytes(s: str, w: int) -> np.ndarray:
+    """conversion.py:36-37 (str_to_np): the characters' codes padded with zeros to w, as int8."""
+    return np.pad(np.array([ord(c) for c in s], np.int64), (0, w - len(s))).astype(np.int8)
+
+
+def _like_contains(a: np.ndarray, p: np.ndarray) -> np.ndarray:
+    """like.py:3-11: p occurs at some position of each row."""
+    n1, m = p.shape[0], a.shape[1]
+    out = np.zeros(a.shape[0], bool)
+    for pos in range(m - n1 + 1):
+        out |= (a[:, pos:pos + n1] == p).all(axis=1)
+    return out
+
+
+def _like_mask(a: np.ndarray, p1: np.ndarray, p2: np.ndarray) -> np.ndarray:
+    """like.py:13-22: p2 starts at or after the end of an earlier occurrence of p1."""
+    n1, n2, m = p1.shape[0], p2.shape[0], a.shape[1]
+    appear = np.zeros(a.shape[0], bool)
+    out = np.zeros(a.shape[0], bool)
+    for pos in range(m - n1 - n2 + 1):
+        appear |= (a[:, pos:pos + n1] == p1).all(axis=1)
+        out |= appear & (a[:, pos + n1:pos + n1 + n2] == p2).all(axis=1)
+    return out
+
+
 def eval_filter(tree, cols: Dict[int, np.ndarray], rows: int | None = None, subquery=None):
     """Evaluate a parsed filter tree into a bool mask (filter.py:14-162).
 
-    String predicates (StartsWith/Contains/LIKE, multi-char equality) are not
-    restated: they are outside the hot path.
+    String columns are int8 [N, w] tensors, zero padded (conversion.py:36-37):
+    StartsWith compares the first len(name) bytes (:48-55), Contains and
+    EndsWith search every position (:56-62, like.py:3-11), LIKE '%a%b%' finds
+    b after an occurrence of a (:121-127, like.py:13-22), and a multi-character
+    literal compares byte-wise against the literal padded to w (:151-158).
     """
     if rows is None:
         rows = next(iter(cols.values())).shape[0]
@@ -112,6 +140,13 @@ def eval_filter(tree, cols: Dict[int, np.ndarray], rows: int | None = None, subq
     if len(tree) == 3 and tree[1] == "#":                          # :40-44
         return cols[int(tree[-1])]
     if len(tree) == 2:                                             # :46-86
+        if tree[0] == "StartsWith":                                # :48-55
+            t = cols[get_id(tree[1][0])]
+            p = _str_bytes(tree[1][1], len(tree[1][1]))
+            assert t.shape[-1] >= len(p)
+            return (t[:, :len(p)] == p).all(axis=1)
+        if tree[0] in ("EndsWith", "Contains"):                    # :56-62
+            return _like_contains(cols[get_id(tree[1][0])], _str_bytes(tree[1][1], len(tree[1][1])))
         if tree[0] == "NOT":
             return ~eval_filter(tree[1], cols, rows, subquery)
         if tree[0] == "isnotnull":
@@ -122,11 +157,19 @@ def eval_filter(tree, cols: Dict[int, np.ndarray], rows: int | None = None, subq
                 return eval_filter(literal, cols, rows, subquery)
         raise NotImplementedError(f"filter function {tree[0]!r} is not on the oracle's path")
     op = tree[-2]
+    if op == "LIKE":                                               # :121-127
+        L = eval_filter(tree[0], cols, rows, subquery)
+        assert tree[-1].count("%") == 3
+        _, w1, w2, _ = tree[-1].split("%")
+        return _like_mask(L, _str_bytes(w1, len(w1)), _str_bytes(w2, len(w2)))
     if op == "IN":                                                 # :90-119
         L = eval_filter(tree[0], cols, rows, subquery)
         mask = np.zeros(rows, dtype=bool)
         for r in tree[-1]:
-            if _is_int(L):
+            if L.ndim == 2:                                        # :110-113
+                assert len(r) > 1
+                mask |= (L == _str_bytes(r, L.shape[-1])).all(axis=1)
+            elif _is_int(L):
                 if len(r) == 1 and not r.lstrip("-").isdigit():
                     mask |= L == ord(r)
                 else:
@@ -150,7 +193,9 @@ def eval_filter(tree, cols: Dict[int, np.ndarray], rows: int | None = None, subq
     if isinstance(R, str):                                         # :151-158
         if len(R) == 1:
             return _torch_compare(op, L, ord(R))
-        raise NotImplementedError("multi-character string compare is not on the oracle's path")
+        if L.ndim != 2:
+            raise NotImplementedError("multi-character literal against a one-dimensional column")
+        return _cmp(op, L, _str_bytes(R, L.shape[-1])).all(axis=1)
     if op == "=" and L.dtype == np.float64:                        # :160-161
         if not isinstance(R, float):
             raise TypeError("isclose against a non-float literal (the reference raises here too)")
@@ -285,7 +330,14 @@ def _promote(a, b):
         return np.float64
     if ("pf" in (ka, kb)):
         raise NotImplementedError("integer column with a float literal promotes to float32 in torch")
-    return np.int64
+    # integer tensors: the wider tensor dtype (a Python int does not widen it); bool counts as int64
+    order = [np.int8, np.uint8, np.int16, np.int32, np.int64]
+    ints = [x.dtype.type for x in (a, b) if isinstance(x, np.ndarray) and x.dtype != bool]
+    if not ints:
+        return np.int64
+    if len(ints) == 2 and {ints[0], ints[1]} == {np.int8, np.uint8}:
+        return np.int16
+    return max(ints, key=order.index)
 
 
 def eval_agg_expr(tree, cols: Dict[int, np.ndarray]):
@@ -486,3 +538,25 @@ def tqp_sort(cols: Dict[int, np.ndarray], args: dict, with_limit: bool):
     if with_limit:
         perm = perm[: args["limit"]]
     return {c: cols[c][perm] for c in args["input ids"]}
+
+
+def tqp_project(cols: Dict[int, np.ndarray], args: dict) -> Dict[int, np.ndarray]:
+    """operators/project.py:10-69: renames, then every computed expression of 'used expr'
+    (a bare column or `column AS name` is only renamed) evaluated row-wise
+    (aggregate.py:203-233 arithmetic), stored as float64 and cast back to the
+    expression's dtype, placed at 'materialized out' in order."""
+    out = dict(cols)
+    for orig, new in args["rename map"].items():           # :13-14
+        out[new] = out[orig]
+    results = []
+    for tree in args["used expr"]:                          # :23-40
+        while isinstance(tree, list) and len(tree) == 1:
+            tree = tree[0]
+        if isinstance(tree, str) or (tree[1] == "AS" and isinstance(tree[0], str)):
+            continue
+        r = eval_agg_expr(tree[0] if len(tree) > 1 and tree[1] == "AS" else tree,
+                          {k: out[k] for k in args["materialized in"]})
+        results.append(np.asarray(r).astype(np.float64).astype(np.asarray(r).dtype))   # :38, :58
+    for i, oid in enumerate(args["materialized out"]):     # :56-61
+        out[oid] = results[i]
+    return out

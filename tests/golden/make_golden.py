@@ -266,6 +266,52 @@ def filter_predicates(ref):
           {"trees": trees, "types": types_}, outs)
 
 
+@case
+def filter_strings(ref):
+    """String predicates on int8 [N, w] columns through tqp_filter: StartsWith, Contains,
+    EndsWith (the reference treats it as Contains), LIKE '%a%b%', multi-character =, IN,
+    combined with NOT/AND/OR and numeric comparisons."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(31)
+    n = 4099
+    words1 = ["STANDARD", "SMALL", "MEDIUM", "LARGE", "ECONOMY", "PROMO"]
+    words2 = ["ANODIZED", "BURNISHED", "PLATED", "POLISHED", "BRUSHED"]
+    words3 = ["TIN", "NICKEL", "BRASS", "STEEL", "COPPER"]
+    w = 25
+    types_col = np.zeros((n, w), np.int8)
+    for i in range(n):
+        s = " ".join([words1[rng.integers(0, 6)], words2[rng.integers(0, 5)], words3[rng.integers(0, 5)]])
+        types_col[i, :len(s)] = np.frombuffer(s.encode(), np.uint8).astype(np.int8)
+    cont = np.zeros((n, 10), np.int8)
+    conts = ["SM CASE", "SM BOX", "MED BAG", "LG PKG", "WRAP JAR", "JUMBO DRUM"]
+    for i in range(n):
+        s = conts[rng.integers(0, len(conts))]
+        cont[i, :len(s)] = np.frombuffer(s.encode(), np.uint8).astype(np.int8)
+    cols = {1: types_col, 2: cont, 3: rng.integers(0, 50, n).astype(np.int64)}
+    types_ = {1: "string", 2: "string", 3: "int"}
+    trees = [
+        ["StartsWith", ["t#1", "MEDIUM POLISHED"]],
+        ["StartsWith", ["t#1", "PROMO"]],
+        ["Contains", ["t#1", "BRASS"]],
+        ["EndsWith", ["t#1", "STEEL"]],
+        ["NOT", [["Contains", ["t#1", "NICKEL"]]]],
+        ["t#1", "LIKE", "%BURNISHED%COPPER%"],
+        ["t#1", "LIKE", "%SMALL%TIN%"],
+        ["c#2", "=", "SM BOX"],
+        ["c#2", "IN", ["SM CASE", "LG PKG", "JUMBO DRUM"]],
+        [["StartsWith", ["t#1", "LARGE"]], "AND", ["k#3", "<", "20"]],
+        [["c#2", "IN", ["MED BAG", "WRAP JAR"]], "OR", ["Contains", ["t#1", "PLATED"]]],
+    ]
+    outs = {}
+    for i, tree in enumerate(trees):
+        used = sorted({int(s.split("#")[1]) for s in _leaves(tree) if "#" in s})
+        tg = _tg(V.Variable, {c: cols[c] for c in used}, types_)
+        fa = {"name": "Filter", "filter tree": [tree], "materialized in": used, "out mask id": 999}
+        f.tqp_filter(False, tg, fa, None, None, _Pool(), "f")
+        outs[f"mask{i}"] = tg[999].tensor.numpy().astype(np.bool_)
+    _save("filter_strings", {str(k): v for k, v in cols.items()}, {"trees": trees, "types": types_}, outs)
+
+
 def _leaves(t):
     if isinstance(t, str):
         yield t

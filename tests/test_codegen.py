@@ -98,3 +98,15 @@ def test_generated_batch_kernel_compiles_and_record_layout_matches():
 def C_sizeof(t):
     import ctypes
     return ctypes.sizeof(t)
+
+
+def test_projection_kernel_compiles():
+    from tqpk.expr import compile_projection
+    d = _lineitem()
+    prog = compile_projection([[[["price#2", "*", ["1", "-", "discount#3"]], "AS", "a#11"]],
+                               [[["flag#5", "+", "status#6"], "AS", "b#12"]], "quantity#1"], d)
+    assert [dt for _, dt in prog.outputs] == [torch.float64, torch.uint8]
+    from tqpk.dtypes import code_of
+    src, _ = jit.project_source(prog.spec, [(r, code_of(dt)) for r, dt in prog.outputs])
+    ok, log = jit.check_compiles(src)
+    assert ok, log[:2000]

@@ -146,3 +146,89 @@ def test_shared_table_sums_stay_accurate(monkeypatch, jit_on):
     np.testing.assert_array_equal(keys[0].cpu().numpy(), np.arange(G))
     s = outs[601].cpu().numpy()
     assert np.max(np.abs(s - exact) / np.abs(exact)) <= 1e-13
+
+
+@pytest.mark.parametrize("n,spec", [
+    (1_000_003, "wide"),        # one key over [0, 1e12): far more slots than rows
+    (800_000, "q3"),            # three keys: order key x date x priority
+    (50_000, "neg"),            # negative keys, int8 + int64
+    (0, "wide"),
+])
+def test_sparse_key_space_groups_through_the_hash_table(n, spec):
+    from tqpk import _lib as L
+    from tqpk.expr import compile_aggregate
+    from tqpk.ops import groupby
+    from tqpk.predicate import compile_filter
+    rng = np.random.default_rng(n + len(spec))
+    if spec == "wide":
+        keys = {1: rng.integers(0, 10**12, n).astype(np.int64) // 997 * 997}
+    elif spec == "q3":
+        keys = {1: rng.integers(1, 6_000_000, n).astype(np.int64), 2: rng.integers(0, 2557, n).astype(np.int32),
+                3: np.zeros(n, np.int32)}
+    else:
+        keys = {1: rng.integers(-120, 120, n).astype(np.int8), 2: rng.integers(-10**10, 10**10, n).astype(np.int64)}
+    cols = dict(keys)
+    cols[8] = rng.integers(90000, 10495001, n) / 100.0
+    cols[9] = rng.integers(0, 11, n) / 100.0
+    cols[10] = rng.integers(0, 2557, n).astype(np.int32)
+    d = {c: torch.from_numpy(a).cuda() for c, a in cols.items()}
+    kn = [f"k{c}#{c}" for c in keys]
+    results = kn + [[[["sum", [["p#8", "*", ["1", "-", "d#9"]]]], "#", "1"], "AS", "r#501"],
+                    [[["count", ["p#8"]], "#", "2L"], "AS", "c#502"], [[["max", ["d#9"]], "#", "3"], "AS", "m#503"],
+                    [[["avg", ["p#8"]], "#", "4"], "AS", "a#504"]]
+    args = {"is partial": False, "keys": kn, "input ids": list(keys) + [8, 9], "results": results,
+            "out agg ids": [501, 502, 503, 504]}
+    tree = [["dt#10", "<", "2000"]]
+    prog = compile_aggregate(args, {c: d[c] for c in list(keys) + [8, 9]})
+    pred = compile_filter(tree, {10: d[10]})
+    out_keys, outs, G, plan = groupby(prog, n, d[8].device, pred=pred)
+    if n:
+        assert plan.mode == L.GB_HASH
+    oc = dict(cols)
+    oc[99] = O.eval_filter(tree, cols) if n else np.zeros(0, bool)
+    ref = O.tqp_hash_aggregate(oc, dict(args, **{"mask map": {c: 99 for c in list(keys) + [8, 9]}}))
+    assert G == (ref[501].shape[0] if n else 0)
+    for i, c in enumerate(keys):
+        np.testing.assert_array_equal(out_keys[i].cpu().numpy(), ref[c].reshape(-1))
+    for a in args["out agg ids"]:
+        got = outs[a].cpu().numpy()
+        (assert_f64_close if ref[a].dtype == np.float64 else np.testing.assert_array_equal)(got, ref[a])
+
+
+def test_key_space_beyond_62_bits_raises():
+    from tqpk.expr import compile_aggregate
+    from tqpk.ops import groupby
+    n = 1000
+    rng = np.random.default_rng(3)
+    cols = {c: rng.integers(-2**40, 2**40, n).astype(np.int64) for c in (1, 2)}
+    cols[8] = rng.random(n)
+    d = {c: torch.from_numpy(a).cuda() for c, a in cols.items()}
+    args = {"is partial": False, "keys": ["a#1", "b#2"], "input ids": [1, 2, 8],
+            "results": ["a#1", "b#2", [[["sum", ["v#8"]], "#", "1"], "AS", "s#501"]], "out agg ids": [501]}
+    prog = compile_aggregate(args, d)
+    with pytest.raises(NotImplementedError):
+        groupby(prog, n, d[8].device)
+
+
+def test_projection_operator_matches_the_oracle():
+    """Drop-in tqp_project: renames, float and integer expressions, int32/int64 promotion."""
+    from tqpk.operators import tqp_project
+    from tqpk.variable import Variable
+    rng = np.random.default_rng(12)
+    n = 300_007
+    cols = {1: rng.integers(90000, 10495001, n) / 100.0, 2: rng.integers(0, 11, n) / 100.0,
+            3: rng.integers(-50, 50, n).astype(np.int32), 4: rng.integers(0, 10**9, n).astype(np.int64),
+            5: rng.integers(0, 2557, n).astype(np.int32)}
+    args = {"rename map": {5: 55},
+            "used expr": ["p#1", [["p#1", "AS", "pp#11"]], [[["p#1", "*", ["1", "-", "d#2"]], "AS", "dp#12"]],
+                          [[["q#3", "+", "q#3"], "AS", "qq#13"]], [[["w#4", "*", "q#3"], "AS", "wq#14"]],
+                          [[["w#4", "-", "3"], "AS", "w3#15"]], [[["p#1", "/", ["q#3", "+", "100"]], "AS", "r#16"]]],
+            "materialized in": [1, 2, 3, 4], "materialized out": [12, 13, 14, 15, 16]}
+    tg = {c: Variable(torch.from_numpy(a).cuda(), "float" if a.dtype == np.float64 else "int") for c, a in cols.items()}
+    assert tqp_project(True, tg, args, None, None) == -1
+    ref = O.tqp_project(cols, args)
+    assert tg[55] is tg[5]
+    for oid in args["materialized out"]:
+        got = tg[oid].tensor.cpu().numpy()
+        assert got.dtype == ref[oid].dtype, (oid, got.dtype, ref[oid].dtype)
+        (assert_f64_close if ref[oid].dtype == np.float64 else np.testing.assert_array_equal)(got, ref[oid])

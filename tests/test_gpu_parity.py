@@ -49,6 +49,60 @@ def test_filter_predicates_golden():
         np.testing.assert_array_equal(np_(tg[999].tensor), outs[f"mask{i}"], err_msg=str(tree))
 
 
+def test_filter_strings_golden():
+    """StartsWith / Contains / EndsWith / LIKE / multi-character = / IN on int8 [N, w] columns."""
+    from tqpk.operators import tqp_filter
+    ins, outs, args = load("filter_strings")
+    for i, tree in enumerate(args["trees"]):
+        used = sorted({int(s.split("#")[1]) for s in _leaves(tree) if "#" in s})
+        tg = {c: V(ins[c], args["types"][str(c)]) for c in used}
+        tqp_filter(True, tg, {"filter tree": [tree], "materialized in": used, "out mask id": 999},
+                   None, None, None, "f")
+        np.testing.assert_array_equal(np_(tg[999].tensor), outs[f"mask{i}"], err_msg=str(tree))
+
+
+@pytest.mark.parametrize("n", [1, 4097, 500_001])
+def test_string_predicates_in_group_by_and_join_build(n):
+    """String filters fused into the group-by (library evaluator) and the join build side."""
+    from tqpk.expr import compile_aggregate
+    from tqpk.ops import groupby
+    from tqpk.pipeline import JoinAggTopK
+    from tqpk.predicate import compile_filter
+    ins, _, args = load("filter_strings")
+    rng = np.random.default_rng(n)
+    pick = rng.integers(0, ins[1].shape[0], n)
+    words = ins[1][pick]
+    key = rng.integers(0, 7, n).astype(np.int32)
+    val = rng.integers(100, 100000, n) / 100.0
+    d = {1: torch.from_numpy(words).cuda(), 2: torch.from_numpy(key).cuda(), 3: torch.from_numpy(val).cuda()}
+    tree = [["Contains", ["t#1", "BRASS"]], "OR", ["t#1", "LIKE", "%SMALL%TIN%"]]
+    aargs = {"is partial": False, "keys": ["k#2"], "input ids": [2, 3],
+             "results": ["k#2", [[["sum", ["v#3"]], "#", "1"], "AS", "s#501"], [[["count", ["v#3"]], "#", "2L"], "AS", "c#502"]],
+             "out agg ids": [501, 502]}
+    prog = compile_aggregate(aargs, {2: d[2], 3: d[3]})
+    keys, outs, G, _ = groupby(prog, n, d[2].device, pred=compile_filter(tree, {1: d[1]}))
+    oc = {1: words, 2: key, 3: val}
+    oc[99] = O.eval_filter(tree, {1: words})
+    ref = O.tqp_hash_aggregate(oc, dict(aargs, **{"mask map": {2: 99, 3: 99}}))
+    np.testing.assert_array_equal(np_(keys[0]), ref[2].reshape(-1))
+    assert_f64_close(np_(outs[501]), ref[501])
+    np.testing.assert_array_equal(np_(outs[502]), ref[502])
+    # the same filter on the build side of the fused join
+    bkey = torch.arange(1, n + 1, dtype=torch.int32, device="cuda")
+    fk = torch.from_numpy(rng.integers(1, n + 1, 3 * n).astype(np.int32)).cuda()
+    pv = torch.from_numpy(rng.integers(100, 100000, 3 * n) / 100.0).cuda()
+    p = JoinAggTopK(bkey, 1, n, fk, {1: d[1]}, tree, {23: pv}, None, ["p#23"], k=5)
+    p.run()
+    got_keys, got_vals, groups = p.result()
+    ok = O.eval_filter(tree, {1: words})
+    fkn = np_(fk)
+    sums = np.bincount(fkn - 1, weights=np_(pv) * ok[fkn - 1], minlength=n)
+    present = np.bincount(fkn - 1, weights=ok[fkn - 1].astype(np.float64), minlength=n) > 0
+    assert groups == int(present.sum())
+    order = O._stable_order(np.where(present, sums, -np.inf), True)[:min(5, int(present.sum()))]
+    np.testing.assert_array_equal(got_keys, order + 1)
+
+
 def _leaves(t):
     if isinstance(t, str):
         yield t

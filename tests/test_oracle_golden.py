@@ -38,6 +38,13 @@ def test_filter_predicates():
         np.testing.assert_array_equal(got.reshape(-1), outs[f"mask{i}"], err_msg=str(tree))
 
 
+def test_filter_strings():
+    ins, outs, args = load("filter_strings")
+    for i, tree in enumerate(args["trees"]):
+        got = O.eval_filter([tree], ins)
+        np.testing.assert_array_equal(got.reshape(-1), outs[f"mask{i}"], err_msg=str(tree))
+
+
 def test_filter_agg_sort_lineitem():
     ins, outs, args = load("filter_agg_sort_lineitem")
     mask = O.eval_filter(args["filter"]["filter tree"], {7: ins[7]})
@@ -139,3 +146,15 @@ def test_fsum_truth_close_to_bincount():
     v = rng.integers(90000, 10495001, 200000) / 100.0
     inv = rng.integers(0, 4, v.size)
     assert_f64_close(O.fsum_groups(v, inv, 4), np.bincount(inv, weights=v, minlength=4), rel=1e-13)
+
+
+def test_oracle_projection_dtypes_follow_torch():
+    import numpy as np
+    from oracle import tqp_oracle as O
+    cols = {1: np.array([1.5, 2.5]), 3: np.array([1, 2], np.int32), 4: np.array([10, 20], np.int64)}
+    args = {"rename map": {}, "used expr": [[[["q#3", "+", "q#3"], "AS", "a#13"]], [[["w#4", "*", "q#3"], "AS", "b#14"]],
+                                             [[["p#1", "*", "2"], "AS", "c#15"]]],
+            "materialized in": [1, 3, 4], "materialized out": [13, 14, 15]}
+    out = O.tqp_project(cols, args)
+    assert out[13].dtype == np.int32 and out[14].dtype == np.int64 and out[15].dtype == np.float64
+    np.testing.assert_array_equal(out[14], [10, 40])

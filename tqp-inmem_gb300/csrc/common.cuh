@@ -392,6 +392,53 @@ __device__ __forceinline__ uint32_t pred_leaf4(const tqpk_predicate& P, const tq
   return m;
 }
 
+// ---- string predicates on int8 [N, w] rows (w = P.widths[col]) ----
+__device__ __forceinline__ bool str_all_cmp(const int8_t* row, int w, const uint8_t* lit, int cmp) {
+  for (int j = 0; j < w; ++j)
+    if (!cmp_op<int64_t>(cmp, (int64_t)row[j], (int64_t)(int8_t)lit[j])) return false;
+  return true;
+}
+__device__ __forceinline__ bool str_at(const int8_t* row, const uint8_t* lit, int len) {
+  for (int j = 0; j < len; ++j)
+    if (row[j] != (int8_t)lit[j]) return false;
+  return true;
+}
+__device__ __forceinline__ bool str_contains(const int8_t* row, int w, const uint8_t* lit, int len) {
+  for (int pos = 0; pos + len <= w; ++pos)
+    if (str_at(row + pos, lit, len)) return true;
+  return false;
+}
+__device__ __forceinline__ bool str_like2(const int8_t* row, int w, const uint8_t* a, int na, const uint8_t* b,
+                                          int nb) {
+  bool seen = false;                        // an occurrence of a ends at or before pos + na
+  for (int pos = 0; pos + na + nb <= w; ++pos) {
+    seen = seen || str_at(row + pos, a, na);
+    if (seen && str_at(row + pos + na, b, nb)) return true;
+  }
+  return false;
+}
+static __device__ uint32_t str_leaf4(const tqpk_predicate& P, const tqpk_pred_insn& I, int64_t r0, int64_t n) {
+  const int w = P.widths[I.col];
+  const int8_t* base = static_cast<const int8_t*>(P.cols[I.col]);
+  const uint64_t L = (uint64_t)I.lit_i;
+  uint32_t m = 0;
+  for (int j = 0; j < 4; ++j) {
+    if (r0 + j >= n) break;
+    const int8_t* row = base + (r0 + j) * w;
+    bool ok;
+    switch (I.op) {
+      case TQPK_P_STRCMP: ok = str_all_cmp(row, w, P.strpool + (L & 0xffffffffu), I.cmp); break;
+      case TQPK_P_PREFIX: ok = str_at(row, P.strpool + (L & 0xffffffffu), (int)(L >> 32)); break;
+      case TQPK_P_CONTAINS: ok = str_contains(row, w, P.strpool + (L & 0xffffffffu), (int)(L >> 32)); break;
+      default:
+        ok = str_like2(row, w, P.strpool + (L & 0xffff), (int)((L >> 16) & 0xffff), P.strpool + ((L >> 32) & 0xffff),
+                       (int)(L >> 48));
+    }
+    m |= (uint32_t)ok << j;
+  }
+  return m;
+}
+
 // Evaluates the predicate for rows r0..r0+3 -> 4-bit mask (rows >= n are 0).
 __device__ __forceinline__ uint32_t eval_pred4(const tqpk_predicate& P, int64_t r0, int64_t n, bool vec) {
   if (P.n_insn == 1 && P.insn[0].op == TQPK_P_CMP) {  // one comparison: no stack
@@ -436,6 +483,10 @@ __device__ __forceinline__ uint32_t eval_pred4(const tqpk_predicate& P, int64_t 
         st[sp++] = (x[0] != 0) | ((x[1] != 0) << 1) | ((x[2] != 0) << 2) | ((x[3] != 0) << 3);
         break;
       }
+      case TQPK_P_STRCMP:
+      case TQPK_P_PREFIX:
+      case TQPK_P_CONTAINS:
+      case TQPK_P_LIKE2: st[sp++] = str_leaf4(P, I, r0, n); break;
     }
   }
   int64_t valid = n - r0;

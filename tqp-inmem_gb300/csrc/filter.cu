@@ -205,6 +205,28 @@ int check_pred(const tqpk_predicate* p) {
         if (!dtype_size(p->dtypes[I.col]) || !dtype_size(p->dtypes[I.lit_i])) return TQPK_EDTYPE;
         ++depth;
         break;
+      case TQPK_P_STRCMP:
+      case TQPK_P_PREFIX:
+      case TQPK_P_CONTAINS:
+      case TQPK_P_LIKE2: {
+        if (I.col < 0 || I.col >= p->n_cols || !p->cols[I.col]) return TQPK_EINVAL;
+        if (dtype_size(p->dtypes[I.col]) != 1) return TQPK_EDTYPE;
+        const int64_t w = p->widths[I.col];
+        const uint64_t L = (uint64_t)I.lit_i;
+        if (w <= 0) return TQPK_EINVAL;
+        bool ok;
+        if (I.op == TQPK_P_STRCMP) {
+          ok = (L & 0xffffffffu) + w <= TQPK_MAX_STRPOOL && I.cmp >= TQPK_LT && I.cmp <= TQPK_NE;
+        } else if (I.op == TQPK_P_LIKE2) {
+          ok = (L & 0xffff) + ((L >> 16) & 0xffff) <= TQPK_MAX_STRPOOL &&
+               ((L >> 32) & 0xffff) + (L >> 48) <= TQPK_MAX_STRPOOL;
+        } else {
+          ok = (L & 0xffffffffu) + (L >> 32) <= TQPK_MAX_STRPOOL && (I.op != TQPK_P_PREFIX || (int64_t)(L >> 32) <= w);
+        }
+        if (!ok) return TQPK_EINVAL;
+        ++depth;
+        break;
+      }
       case TQPK_P_TRUE:
       case TQPK_P_FALSE: ++depth; break;
       case TQPK_P_AND:

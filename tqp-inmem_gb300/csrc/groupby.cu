@@ -18,6 +18,9 @@
 //                  shared-memory f64 atomics serialise badly on GB300).
 //   DENSE_SHARED   up to ~12k slot*accs: one table per CTA, shared atomics.
 //   DENSE_GLOBAL   up to max(4*rows, 2^20) slots: global (L2) atomics.
+//   HASH           larger (sparse) key spaces: the packed mixed-radix key in an
+//                  open-addressing table of >= 2 x rows slots, groups sorted
+//                  by packed key at emit (the same ascending key-tuple order).
 //
 // FP64 work is the limit on GB300 (FP64 runs at 1/64 of the FP32 rate), so
 // the expression program is straight-line with shared subexpressions and no
@@ -199,6 +202,95 @@ __global__ void __launch_bounds__(256) k_groupby_dense(const __grid_constant__ t
   }
 }
 
+// ---------------------------------------------------------------- sparse key spaces
+// When the mixed-radix key space is far larger than the rows (several wide keys),
+// the packed key (the same mixed-radix number, < 2^62) is the key of an
+// open-addressing table of C = 2^k >= 2 x rows slots in global memory (linear
+// probing, atomicCAS claims an empty slot), and the accumulators live at the
+// claimed slot.  The groups are then sorted by packed key, which is the
+// ascending key-tuple order of the dense modes.
+constexpr uint64_t kHashEmpty = ~0ull;
+
+__device__ __forceinline__ int64_t hash_slot(uint64_t packed, int64_t C) {
+  return (int64_t)((packed * 0x9E3779B97F4A7C15ull) >> 20) & (C - 1);
+}
+
+__global__ void k_fill_u64(uint64_t* p, int64_t n, uint64_t v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+__global__ void __launch_bounds__(256) k_groupby_hash(const __grid_constant__ tqpk_groupby_spec S,
+                                                      const __grid_constant__ tqpk_predicate P, RowFilter F, int64_t n,
+                                                      GbDev G, uint64_t* __restrict__ gacc,
+                                                      unsigned long long* __restrict__ hkeys, int keys_vec,
+                                                      int cols_vec, int* err) {
+  const int A = S.n_accs;
+  const int64_t C = G.slots;
+  const int64_t groups = (n + 3) >> 2;
+  const bool small = S.n_expr <= 16;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r0 = g << 2;
+    const uint32_t b = filter4(F, P, r0, n);
+    if (!b) continue;
+    uint64_t packed[4] = {0, 0, 0, 0};
+    for (int k = 0; k < G.nk; ++k) {
+      int64_t x[4];
+      ld4_int(S.keys[k], S.key_dtypes[k], r0, n, keys_vec, x);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) packed[j] += (uint64_t)(x[j] - G.kmin[k]) * (uint64_t)G.kstride[k];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (!((b >> j) & 1u)) continue;
+      int64_t h = hash_slot(packed[j], C);
+      int64_t probes = 0;
+      while (true) {
+        const unsigned long long cur = __ldcg(&hkeys[h]);
+        if (cur == packed[j]) break;
+        if (cur == kHashEmpty) {
+          const unsigned long long prev = atomicCAS(&hkeys[h], kHashEmpty, (unsigned long long)packed[j]);
+          if (prev == kHashEmpty || prev == packed[j]) break;
+        }
+        h = (h + 1) & (C - 1);
+        if (++probes > C) { set_error(err, TQPK_ECAPACITY); h = -1; break; }   // table full: cannot happen (C >= 2 rows)
+      }
+      if (h < 0) continue;
+      if (small) {
+        uint64_t r[16];
+        expr_eval_small<16>(S.expr, S.n_expr, S.cols, S.col_dtypes, r0 + j, r);
+        for (int a = 0; a < A; ++a)
+          acc_merge_atomic(&gacc[(int64_t)a * C + h], S.accs[a], acc_value(S.accs[a], reg_pick<16>(r, S.accs[a].reg)));
+      } else {
+        uint64_t r[TQPK_MAX_EXPR];
+        expr_eval_generic(S.expr, S.n_expr, S.cols, S.col_dtypes, r0 + j, r);
+        for (int a = 0; a < A; ++a)
+          acc_merge_atomic(&gacc[(int64_t)a * C + h], S.accs[a], acc_value(S.accs[a], r[S.accs[a].reg]));
+      }
+    }
+  }
+}
+
+// Appends (packed key, slot) of every occupied slot (unordered).
+__global__ void k_hash_collect(const uint64_t* __restrict__ count0, const unsigned long long* __restrict__ hkeys,
+                               int64_t C, int64_t* __restrict__ pk, int64_t* __restrict__ cslot,
+                               unsigned long long* counter, int64_t cap) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < C;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = base + lane;
+    const bool occ = s < C && count0[s] != 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, occ);
+    if (!bal) continue;
+    unsigned long long at = 0;
+    if (lane == 0) at = atomicAdd(counter, (unsigned long long)__popc(bal));
+    at = __shfl_sync(0xffffffffu, at, 0) + __popc(bal & ((1u << lane) - 1u));
+    if (occ && (int64_t)at < cap) {
+      pk[at] = (int64_t)hkeys[s];
+      cslot[at] = s;
+    }
+  }
+}
+
 __global__ void k_init_accs(const __grid_constant__ tqpk_groupby_spec S, uint64_t* gacc, int64_t K) {
   const int64_t total = K * S.n_accs;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
@@ -294,6 +386,67 @@ __global__ void __launch_bounds__(kBlock) k_emit_dense(const __grid_constant__ t
   }
 }
 
+// Groups of a hash table in key order: position j holds slot cslot[perm[j]].
+__global__ void k_emit_hash(const __grid_constant__ tqpk_groupby_spec S, GbDev G, const uint64_t* __restrict__ gacc,
+                            int64_t groups, const int64_t* __restrict__ pk, const int64_t* __restrict__ cslot,
+                            const int64_t* __restrict__ perm, const __grid_constant__ EmitOut E) {
+  const int64_t C = G.slots;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < groups; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm[j];
+    const int64_t s = cslot[i];
+    const uint64_t packed = (uint64_t)pk[i];
+    for (int k = 0; k < G.nk; ++k) {
+      const int64_t key = G.kmin[k] + (int64_t)((packed / (uint64_t)G.kstride[k]) % (uint64_t)G.krange[k]);
+      store_as(E.key[k], E.key_dt[k], j, (uint64_t)key, false);
+    }
+    for (int o = 0; o < E.n; ++o) {
+      const tqpk_acc& a = S.accs[E.a[o]];
+      uint64_t v = gacc[(int64_t)E.a[o] * C + s];
+      bool f = a.type == TQPK_F64 && a.kind != TQPK_ACC_COUNT_ROWS && a.kind != TQPK_ACC_COUNT_NOTNULL;
+      if (f && (a.kind == TQPK_ACC_MIN || a.kind == TQPK_ACC_MAX)) v = d2u(f64_from_ordered(v));
+      if (E.op[o] == TQPK_OUT_AVG) {
+        const double num = f ? u2d(v) : (double)(int64_t)v;
+        const double den = (double)(int64_t)gacc[(int64_t)E.b[o] * C + s];
+        v = d2u(__ddiv_rn(num, den));
+        f = true;
+      } else if (a.kind == TQPK_ACC_COUNT_ROWS || a.kind == TQPK_ACC_COUNT_NOTNULL) {
+        f = false;
+      }
+      store_as(E.col[o], E.dt[o], j, v, f);
+    }
+  }
+}
+
+// Hash-mode workspace: [512 header][acc table A x C][keys C][packed keys C][slots C][sort workspace]
+struct HashLayout {
+  uint64_t* gacc;
+  unsigned long long* hkeys;
+  int64_t* pk;
+  int64_t* cslot;
+  void* sort_ws;
+  size_t sort_bytes;
+};
+
+static size_t hash_ws_bytes(int64_t C, int A) {
+  return 512 + align_up((size_t)C * A * 8, 256) + 3 * align_up((size_t)C * 8, 256) + sort_ws_bytes(C / 2 + 1) + 256;
+}
+
+static HashLayout hash_layout(void* ws, int64_t C, int A) {
+  HashLayout H;
+  char* p = static_cast<char*>(ws) + 512;
+  H.gacc = reinterpret_cast<uint64_t*>(p);
+  p += align_up((size_t)C * A * 8, 256);
+  H.hkeys = reinterpret_cast<unsigned long long*>(p);
+  p += align_up((size_t)C * 8, 256);
+  H.pk = reinterpret_cast<int64_t*>(p);
+  p += align_up((size_t)C * 8, 256);
+  H.cslot = reinterpret_cast<int64_t*>(p);
+  p += align_up((size_t)C * 8, 256);
+  H.sort_ws = p;
+  H.sort_bytes = sort_ws_bytes(C / 2 + 1);
+  return H;
+}
+
 // ---------------------------------------------------------------- host side
 static GbDev to_dev(const tqpk_gb_plan& p, int nk) {
   GbDev G;
@@ -307,16 +460,21 @@ static GbDev to_dev(const tqpk_gb_plan& p, int nk) {
   return G;
 }
 
-static int check_spec(const tqpk_groupby_spec* S) {
+// has_rows: the key and value columns are read (empty inputs may carry null column pointers)
+static int check_spec(const tqpk_groupby_spec* S, bool has_rows = true) {
   if (!S) return TQPK_EINVAL;
   if (S->n_keys < 0 || S->n_keys > TQPK_MAX_KEYS || S->n_cols < 0 || S->n_cols > TQPK_MAX_COLS ||
       S->n_expr < 0 || S->n_expr > TQPK_MAX_EXPR || S->n_accs < 1 || S->n_accs > TQPK_MAX_ACCS)
     return TQPK_EINVAL;
   if (S->accs[0].kind != TQPK_ACC_COUNT_ROWS) return TQPK_EINVAL;  // accumulator 0 marks occupied groups
-  for (int k = 0; k < S->n_keys; ++k)
-    if (!S->keys[k] || !is_int_dtype(S->key_dtypes[k])) return TQPK_EDTYPE;
-  for (int c = 0; c < S->n_cols; ++c)
-    if (!S->cols[c] || !dtype_size(S->col_dtypes[c])) return TQPK_EDTYPE;
+  for (int k = 0; k < S->n_keys; ++k) {
+    if (!is_int_dtype(S->key_dtypes[k])) return TQPK_EDTYPE;
+    if (has_rows && !S->keys[k]) return TQPK_EINVAL;
+  }
+  for (int c = 0; c < S->n_cols; ++c) {
+    if (!dtype_size(S->col_dtypes[c])) return TQPK_EDTYPE;
+    if (has_rows && !S->cols[c]) return TQPK_EINVAL;
+  }
   for (int i = 0; i < S->n_expr; ++i) {
     const tqpk_expr_insn& X = S->expr[i];
     if (X.type != TQPK_F64 && X.type != TQPK_I64) return TQPK_EDTYPE;
@@ -342,7 +500,7 @@ using namespace tqpk;
 
 extern "C" int tqpk_groupby_plan(const tqpk_groupby_spec* S, const tqpk_predicate* pred, const uint8_t* mask,
                                  int64_t n, tqpk_gb_plan* plan, void* scratch, tqpk_stream stream) {
-  int rc = check_spec(S);
+  int rc = check_spec(S, n > 0);
   if (rc) return rc;
   if ((rc = check_pred(pred))) return rc;
   if (!plan || n < 0) return TQPK_EINVAL;
@@ -383,8 +541,16 @@ extern "C" int tqpk_groupby_plan(const tqpk_groupby_spec* S, const tqpk_predicat
   if (plan->mode == TQPK_GB_GLOBAL_ONE) plan->threads = (K * A * 8 * 256 <= kPrivateBudget) ? 256 : 128;
   plan->slots = K;
   if (plan->mode == TQPK_GB_HASH) {
-    plan->ws_bytes = 0;
-    return TQPK_EUNSUPPORTED;
+    if (overflow) {            // the packed key would not fit 62 bits
+      plan->ws_bytes = 0;
+      return TQPK_EUNSUPPORTED;
+    }
+    int64_t C = 1024;
+    while (C < 2 * rows) C <<= 1;
+    plan->slots = C;
+    plan->threads = 256;
+    plan->ws_bytes = hash_ws_bytes(C, (int)A);
+    return TQPK_OK;
   }
   plan->ws_bytes = 512 + align_up((size_t)(K * A * 8), 256) + compact_status_bytes(K);
   return TQPK_OK;
@@ -393,12 +559,43 @@ extern "C" int tqpk_groupby_plan(const tqpk_groupby_spec* S, const tqpk_predicat
 extern "C" int tqpk_groupby_run(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, const tqpk_predicate* pred,
                                 const uint8_t* mask, int64_t n, void* ws, size_t ws_bytes, int64_t* h_groups,
                                 tqpk_stream stream) {
-  int rc = check_spec(S);
+  int rc = check_spec(S, n > 0);
   if (rc) return rc;
   if ((rc = check_pred(pred))) return rc;
   if (!plan || !ws || ws_bytes < plan->ws_bytes || !h_groups || n < 0) return !ws || ws_bytes < (plan ? plan->ws_bytes : 0) ? TQPK_ENOMEM : TQPK_EINVAL;
-  if (plan->mode == TQPK_GB_HASH) return TQPK_EUNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (plan->mode == TQPK_GB_HASH) {
+    if (!plan->ws_bytes) return TQPK_EUNSUPPORTED;
+    const int64_t C = plan->slots;
+    HashLayout H = hash_layout(ws, C, S->n_accs);
+    char* base = static_cast<char*>(ws);
+    unsigned long long* d_groups = reinterpret_cast<unsigned long long*>(base);
+    int* err = reinterpret_cast<int*>(base + 8);
+    TQPK_CUDA(cudaMemsetAsync(base, 0, 16, s));
+    k_init_accs<<<grid_for(C * S->n_accs, 4), kBlock, 0, s>>>(*S, H.gacc, C);
+    TQPK_CHECK_LAUNCH();
+    k_fill_u64<<<grid_for(C, 4), kBlock, 0, s>>>(reinterpret_cast<uint64_t*>(H.hkeys), C, kHashEmpty);
+    TQPK_CHECK_LAUNCH();
+    if (n > 0 && plan->n_rows > 0) {
+      bool kvec = true;
+      for (int k = 0; k < S->n_keys; ++k) kvec = kvec && aligned16(S->keys[k]);
+      const GbDev G = to_dev(*plan, S->n_keys);
+      timing_before(KID_GROUPBY, s);
+      k_groupby_hash<<<grid_for((n + 3) / 4, 8), 256, 0, s>>>(*S, *pred_or_empty(pred), make_filter(pred, mask), n, G,
+                                                               H.gacc, H.hkeys, kvec, spec_cols_vec(S) ? 1 : 0, err);
+      timing_after(KID_GROUPBY, s);
+      TQPK_CHECK_LAUNCH();
+      k_count_groups<<<grid_for(C, 4), kBlock, 0, s>>>(H.gacc, C, d_groups);
+      TQPK_CHECK_LAUNCH();
+    }
+    unsigned long long h[2] = {0, 0};
+    TQPK_CUDA(cudaMemcpyAsync(h, base, 16, cudaMemcpyDeviceToHost, s));
+    TQPK_CUDA(cudaStreamSynchronize(s));
+    const int e = (int)(h[1] & 0xffffffffu);
+    if (e) return e;
+    *h_groups = (int64_t)h[0];
+    return TQPK_OK;
+  }
   const int64_t K = plan->slots, A = S->n_accs;
   char* base = static_cast<char*>(ws);
   unsigned long long* d_groups = reinterpret_cast<unsigned long long*>(base);
@@ -458,10 +655,10 @@ extern "C" int tqpk_groupby_run(const tqpk_groupby_spec* S, const tqpk_gb_plan* 
 extern "C" int tqpk_groupby_emit(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, void* ws, int64_t groups,
                                  void* const* out_keys, int32_t n_out, const int32_t* ops, void* const* out_cols,
                                  tqpk_stream stream) {
-  int rc = check_spec(S);
+  int rc = check_spec(S, false);
   if (rc) return rc;
   if (!plan || !ws || n_out < 0 || n_out > TQPK_MAX_ACCS || groups < 0) return TQPK_EINVAL;
-  if (plan->mode == TQPK_GB_HASH) return TQPK_EUNSUPPORTED;
+  if (plan->mode == TQPK_GB_HASH && !plan->ws_bytes) return TQPK_EUNSUPPORTED;
   if (groups == 0) return TQPK_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   EmitOut E;
@@ -482,6 +679,22 @@ extern "C" int tqpk_groupby_emit(const tqpk_groupby_spec* S, const tqpk_gb_plan*
   }
   const int64_t K = plan->slots, A = S->n_accs;
   char* base = static_cast<char*>(ws);
+  if (plan->mode == TQPK_GB_HASH) {
+    // the occupied slots (unordered), sorted by packed key = ascending key tuple
+    HashLayout H = hash_layout(ws, K, (int)A);
+    unsigned long long* counter = reinterpret_cast<unsigned long long*>(base + 16);
+    TQPK_CUDA(cudaMemsetAsync(counter, 0, 8, s));
+    k_hash_collect<<<grid_for(K, 4), kBlock, 0, s>>>(H.gacc, H.hkeys, K, H.pk, H.cslot, counter, groups);
+    TQPK_CHECK_LAUNCH();
+    const int64_t* perm = nullptr;
+    int rc2 = sort_pairs(H.pk, TQPK_I64, 0, nullptr, groups, H.sort_ws, H.sort_bytes, s, &perm);
+    if (rc2) return rc2;
+    const GbDev G = to_dev(*plan, S->n_keys);
+    k_emit_hash<<<grid_for(groups, 4), kBlock, 0, s>>>(*S, G, H.gacc, groups, H.pk, H.cslot, perm, E);
+    TQPK_CHECK_LAUNCH();
+    TQPK_CUDA(cudaStreamSynchronize(s));
+    return TQPK_OK;
+  }
   uint64_t* gacc = reinterpret_cast<uint64_t*>(base + 512);
   void* cws = base + 512 + align_up((size_t)(K * A * 8), 256);
   const int64_t tiles = (K + kTile - 1) / kTile;
@@ -506,7 +719,7 @@ extern "C" int tqpk_groupby_emit(const tqpk_groupby_spec* S, const tqpk_gb_plan*
 extern "C" int tqpk_groupby_emit_async(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, void* ws,
                                        void* const* out_keys, int32_t n_out, const int32_t* ops,
                                        void* const* out_cols, int64_t* d_groups_out, tqpk_stream stream) {
-  int rc = check_spec(S);
+  int rc = check_spec(S, false);
   if (rc) return rc;
   if (!plan || !ws || !d_groups_out || n_out < 0 || n_out > TQPK_MAX_ACCS) return TQPK_EINVAL;
   if (plan->mode == TQPK_GB_HASH) return TQPK_EUNSUPPORTED;
@@ -558,7 +771,7 @@ extern "C" int tqpk_groupby_emit_async(const tqpk_groupby_spec* S, const tqpk_gb
 // count counts the occupied slots (synchronises).
 extern "C" int tqpk_groupby_prepare(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, void* ws, size_t ws_bytes,
                                     tqpk_stream stream) {
-  int rc = check_spec(S);
+  int rc = check_spec(S, false);
   if (rc) return rc;
   if (!plan || !ws) return TQPK_EINVAL;
   if (ws_bytes < plan->ws_bytes) return TQPK_ENOMEM;

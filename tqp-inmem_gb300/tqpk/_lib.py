@@ -20,6 +20,7 @@ MAX_COLS, MAX_PRED, MAX_KEYS, MAX_EXPR, MAX_ACCS = 16, 32, 4, 32, 16
 NULL_INDEX = -64
 
 P_CMP, P_AND, P_OR, P_NOT, P_TRUE, P_FALSE, P_MASK, P_CMPCOL = 1, 2, 3, 4, 5, 6, 7, 8
+P_STRCMP, P_PREFIX, P_CONTAINS, P_LIKE2 = 9, 10, 11, 12
 LT, LE, GT, GE, EQ, NE, ISCLOSE = 0, 1, 2, 3, 4, 5, 6
 DOM_I64, DOM_F64, DOM_F32 = 0, 1, 2
 X_COL, X_CONST, X_ADD, X_SUB, X_MUL, X_DIV, X_TOF64 = 1, 2, 3, 4, 5, 6, 7
@@ -35,9 +36,13 @@ class PredInsn(C.Structure):
                 ("lit_i", C.c_int64), ("lit_f", C.c_double), ("lit_aux", C.c_double)]
 
 
+MAX_STRPOOL = 512
+
+
 class Predicate(C.Structure):
     _fields_ = [("n_insn", C.c_int32), ("n_cols", C.c_int32), ("cols", C.c_void_p * MAX_COLS),
-                ("dtypes", C.c_int32 * MAX_COLS), ("insn", PredInsn * MAX_PRED)]
+                ("dtypes", C.c_int32 * MAX_COLS), ("insn", PredInsn * MAX_PRED),
+                ("widths", C.c_int32 * MAX_COLS), ("strpool", C.c_uint8 * MAX_STRPOOL)]
 
 
 class ExprInsn(C.Structure):

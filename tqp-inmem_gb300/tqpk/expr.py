@@ -248,3 +248,47 @@ def compile_aggregate(args: dict, columns: Dict[int, torch.Tensor]) -> Aggregate
         s.accs[i] = L.Acc(kind, ty, reg, 0, ii, ff)
     prog.spec = s
     return prog
+
+
+@dataclass
+class ProjectionProgram:
+    spec: Any                                   # expression program (no keys; accumulator 0 only)
+    tensors: List[torch.Tensor] = field(default_factory=list)
+    outputs: List[Tuple[int, torch.dtype]] = field(default_factory=list)   # (register, result dtype)
+
+
+def is_trivial_projection(tree) -> bool:
+    """A bare column or `column AS name` (project.py:27-31): renamed, not computed."""
+    while isinstance(tree, list) and len(tree) == 1:
+        tree = tree[0]
+    return isinstance(tree, str) or (tree[1] == "AS" and isinstance(tree[0], str))
+
+
+def compile_projection(trees, columns: Dict[int, torch.Tensor]) -> ProjectionProgram:
+    """The computed expressions of a projection (project.py:20-40) as one SSA program: each
+    output is a register with the dtype torch gives the expression (aggregate.py:203-233)."""
+    b = _Builder(columns)
+    outs = []
+    for tree in trees:
+        while isinstance(tree, list) and len(tree) == 1:
+            tree = tree[0]
+        if is_trivial_projection(tree):
+            continue
+        expr = tree[0] if len(tree) > 1 and tree[1] == "AS" else tree
+        v = b.value(expr)
+        if not isinstance(v, _Node):
+            raise NotImplementedError(f"projection of a literal {expr!r}")
+        outs.append((v.reg, v.dtype))
+    spec = L.GroupbySpec()
+    spec.n_keys = 0
+    spec.n_cols = len(b.col_tensors)
+    for i, t in enumerate(b.col_tensors):
+        spec.cols[i] = t.data_ptr()
+        spec.col_dtypes[i] = code_of(t.dtype)
+    spec.n_expr = len(b.expr)
+    for i, (op, ty, a, bb, col, ci, cf) in enumerate(b.expr):
+        X = spec.expr[i]
+        X.op, X.type, X.a, X.b, X.col, X.ci, X.cf = op, ty, a, bb, col, ci, cf
+    spec.n_accs = 1
+    spec.accs[0].kind, spec.accs[0].type = L.ACC_COUNT_ROWS, L.I64
+    return ProjectionProgram(spec=spec, tensors=list(b.col_tensors), outputs=outs)

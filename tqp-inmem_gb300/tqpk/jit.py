@@ -763,6 +763,33 @@ def join_probe_tma_source(spec, val_reg: int, pred, bpred, fk_code: int, ST: int
     return "\n".join(src), name, 8 * ST * stage
 
 
+def project_source(spec, outputs) -> Tuple[str, str]:
+    """CUDA source of a projection: every row's expression registers written to output
+    columns.  outputs: [(register, dtype code)].  Integer results pass through float64 on
+    the way out, as project.py:38-58 stores every result as float64 and casts it back."""
+    S = spec
+    upto = max(r for r, _ in outputs) + 1
+    ecols, elines = _expr_code(S, upto, "c")
+    name = "tqpk_q_project"
+    params = [f"const void* __restrict__ cp{c}" for c in range(S.n_cols)]
+    params += [f"void* __restrict__ op{o}" for o in range(len(outputs))]
+    params += ["i64 n", "int vc"]
+    src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__(256) {name}(', "    " + ",\n    ".join(params) + ") {",
+           "  for (i64 g = blockIdx.x * (i64)blockDim.x + threadIdx.x; g < ((n + 3) >> 2); g += (i64)gridDim.x * blockDim.x) {",
+           "    const i64 r0 = g << 2;"]
+    src += ["    " + l for l in _load_lines(ecols, S.col_dtypes, "Cv", "cp", "n", "vc != 0")]
+    src += ["#pragma unroll", "    for (int j = 0; j < 4; ++j) {", "      if (r0 + j >= n) break;",
+            "      const i64 row = r0 + j;            // r0.. below are expression registers"]
+    src += ["      " + _rename(l, "c", "Cv") for l in elines]
+    for o, (reg, dt) in enumerate(outputs):
+        t = _CTYPE[dt]
+        f64 = S.expr[reg].type == L.F64
+        val = f"r{reg}" if (f64 or dt == L.F64) else f"(double)r{reg}"
+        src.append(f"      (({t}*)op{o})[row] = ({t})({val});")
+    src += ["    }", "  }", "}"]
+    return "\n".join(src), name
+
+
 def join_probe_args(a: "_Args", spec, pred, bpred, fk, np_: int, key_min: int, slots: int, dir_ptr: int,
                     sum_ptr: int, occ_ptr: int, pred_tensors=(), bpred_tensors=(), col_tensors=()):
     """Parameters of join_probe_source's kernel, in order."""

@@ -548,6 +548,12 @@ extern "C" __global__ void tqpk_qb_reset(const QInst* __restrict__ insts, int n_
 
 
 # ---------------------------------------------------------------------------- host side
+def _no_strings(pred):
+    from .predicate import has_strings
+    if pred is not None and has_strings(pred.struct):
+        raise NotImplementedError("string predicates run on the operator path, not in the generated batch kernel")
+
+
 def _mode(K: int, A: int) -> Tuple[int, int]:
     """(mode, copies) of a group table of K slots x A accumulators: as many shared-memory
     copies as fit (a power of two, at most one per thread); with 32 or more, the lanes of a
@@ -628,6 +634,7 @@ class QueryBatch:
         self.dev = dev
         prog = compile_aggregate(inst.args, cols)
         pred = compile_filter(inst.filter_tree, inst.filter_cols) if inst.filter_tree is not None else None
+        _no_strings(pred)
         S = prog.spec
         nk = S.n_keys
         K = int(np.prod([int(d[1]) - int(d[0]) + 1 for d in inst.key_domains])) if nk else 1
@@ -682,6 +689,8 @@ class QueryBatch:
             raise TypeError("join keys must be int32 or int64")
         bpred = compile_filter(inst.build_filter, inst.build_cols) if inst.build_filter is not None else None
         ppred = compile_filter(inst.probe_filter, inst.probe_cols) if inst.probe_filter is not None else None
+        _no_strings(bpred)
+        _no_strings(ppred)
         prog = compile_aggregate({"keys": None, "results": [[[["sum", inst.value_tree], "#", "1"], "AS", "v#1"]]},
                                  inst.probe_cols)
         S = prog.spec

@@ -8,10 +8,12 @@ as the reference functions; the work runs in libtqpk.so:
   hashjoin.join_kernel_new      operators/hashjoin.py:24-177
   aggregate.tqp_hash_aggregate  operators/aggregate.py:236-393
   sort.tqp_sort                 operators/sort.py:6-58
+  project.tqp_project           operators/project.py:10-69
 """
 from .filter import tqp_filter
 from .hashjoin import join_vortex, join_kernel_new
 from .aggregate import tqp_hash_aggregate
 from .sort import tqp_sort
+from .project import tqp_project
 
-__all__ = ["tqp_filter", "join_vortex", "join_kernel_new", "tqp_hash_aggregate", "tqp_sort"]
+__all__ = ["tqp_filter", "join_vortex", "join_kernel_new", "tqp_hash_aggregate", "tqp_sort", "tqp_project"]

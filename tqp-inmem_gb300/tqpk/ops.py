@@ -116,9 +116,12 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
     ws = _ws(plan.ws_bytes, device)
     groups = C.c_int64(0)
     from . import jit
-    if jit.available() and mask is not None and pred is None and plan.n_rows > 0 and n > 0:
+    from .predicate import has_strings
+    use_jit = (jit.available() and plan.mode != L.GB_HASH and plan.n_rows > 0 and n > 0
+               and not has_strings(pred.struct if pred is not None else None))
+    if use_jit and mask is not None and pred is None:
         pred = _mask_predicate(mask)              # the mask as a one-instruction predicate
-    if jit.available() and (mask is None or pred is not None) and plan.n_rows > 0 and n > 0:
+    if use_jit and (mask is None or pred is not None):
         # query-specialised accumulation kernel between the library's prepare and count stages
         L.check(lib.tqpk_groupby_prepare(C.byref(prog.spec), C.byref(plan), ws.data_ptr(), ws.numel(), s),
                 "tqpk_groupby_prepare")
@@ -266,4 +269,27 @@ def gather(cols: Sequence[torch.Tensor], idx: torch.Tensor, null_aware: bool = F
                             _i32_array([code_of(c.dtype) for c in cols]), idx.contiguous().data_ptr(), n,
                             int(bool(null_aware)), _vp_array([o.data_ptr() for o in outs]), _stream(idx.device)),
             "tqpk_gather")
+    return outs
+
+
+def project(prog, n: int, device) -> List[torch.Tensor]:
+    """Evaluates a compiled projection over n rows: one output column per computed expression."""
+    from . import jit
+    from .dtypes import code_of
+    _check_cuda(*prog.tensors)
+    outs = [torch.empty(n, dtype=dt, device=device) for (_, dt) in prog.outputs]
+    if n == 0 or not outs:
+        return outs
+    if not jit.available():
+        raise NotImplementedError("projection needs the runtime compiler (NVRTC)")
+    src, name = jit.project_source(prog.spec, [(r, code_of(dt)) for (r, dt) in prog.outputs])
+    h = jit.compile_kernel(src, name)
+    a = jit._Args()
+    for c in range(prog.spec.n_cols):
+        a.ptr(prog.spec.cols[c])
+    for o in outs:
+        a.ptr(o.data_ptr())
+    a.i64(n)
+    a.i32(jit._aligned(*prog.tensors))
+    jit.launch(h, jit.occupancy_grid(h, 256, 0, (n + 3) // 4), 256, 0, a, _stream(device))
     return outs

@@ -108,7 +108,9 @@ class JoinAggTopK:
     def run(self, stream=None):
         from . import jit
         s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
-        if jit.available() and jit.probe_supported(code_of(self.pk.dtype)) and self.pk.numel() > 0:
+        from .predicate import has_strings
+        if (jit.available() and jit.probe_supported(code_of(self.pk.dtype)) and self.pk.numel() > 0
+                and not has_strings(self.ppred.struct if self.ppred else None)):
             self._stages(1, s)
             self._jit_probe(s)
             self._stages(4, s)
@@ -184,7 +186,10 @@ class StarAggTopK:
     def _jit_ok(self) -> bool:
         from . import jit
         fa, fb, ak, bk, bc, ck = self.t
+        from .predicate import has_strings
         cmn, cmx = self.doms[2]
+        if has_strings(self.fpred.struct if self.fpred else None):
+            return False
         return (jit.available() and fa.numel() > 0 and fa.dtype == torch.int32 and fb.dtype == torch.int32
                 and all(x.numel() > 0 for x in (ak, bk, ck)) and cmn > -(1 << 31) + 1 and cmx < (1 << 31))
 

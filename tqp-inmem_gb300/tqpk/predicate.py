@@ -16,8 +16,13 @@ reference's exact semantics:
 * ``isnotnull`` is all-true (``:67-69``), ``IN`` is an OR of equalities
   (``:90-119``), a one-character string literal compares with ``ord``.
 
-String predicates (StartsWith / Contains / LIKE / multi-character equality /
-substring) are not on the kernel path and raise ``NotImplementedError``.
+String columns are int8 ``[N, w]`` tensors (zero padded, conversion.py:36-37):
+``StartsWith`` (``:48-55``), ``Contains`` / ``EndsWith`` (``:56-62``, the
+reference treats both as a substring search), ``LIKE '%a%b%'`` (``:121-127``),
+a multi-character literal compared byte-wise against the literal padded to w
+(``:151-158``) and ``IN`` lists of such literals compile to the string
+instructions; their literal bytes go to the predicate's string pool.
+``substring`` is not on the kernel path and raises ``NotImplementedError``.
 """
 from __future__ import annotations
 
@@ -73,6 +78,8 @@ class _Compiler:
         self.subquery = subquery
         self.insn: List[tuple] = []
         self.slots: Dict[int, int] = {}
+        self.str_cols = set()
+        self.pool = b""
 
     # -- values -------------------------------------------------------------
     def value(self, tree):
@@ -112,8 +119,35 @@ class _Compiler:
         if t.dim() == 2 and t.shape[1] == 1:
             t = t.reshape(-1)
         if t.dim() != 1:
-            raise NotImplementedError("string (2-D) columns are not on the kernel path")
+            raise NotImplementedError("a string (2-D) column is compared only by the string predicates")
         return t
+
+    def str_tensor(self, cid: int):
+        t = self.columns[cid]
+        if t.dim() != 2 or t.dtype not in (torch_int8(), torch_uint8()):
+            raise NotImplementedError("string predicates take int8 [N, w] columns")
+        return t
+
+    def pool_add(self, data: bytes) -> int:
+        off = len(self.pool)
+        if off + len(data) > L.MAX_STRPOOL:
+            raise NotImplementedError(f"string literals exceed {L.MAX_STRPOOL} bytes")
+        self.pool += data
+        return off
+
+    def emit_str(self, op: int, cid: int, cmp: int, lit: int):
+        self.str_cols.add(cid)
+        self.insn.append((op, self.slot(cid), cmp, 0, lit, 0.0, 0.0))
+
+    @staticmethod
+    def _bytes(s: str, w: int) -> bytes:
+        """conversion.py:36-37: character codes padded with zeros to w (np.pad raises past w)."""
+        codes = [ord(c) for c in s]
+        if len(codes) > w:
+            raise ValueError(f"string literal {s!r} is longer than the column ({w} bytes)")
+        if any(c > 255 for c in codes):
+            raise NotImplementedError("non-byte characters in a string literal")
+        return bytes(codes) + bytes(w - len(codes))
 
     def dtype(self, cid: int) -> int:
         return code_of(self.col_tensor(cid).dtype)
@@ -149,14 +183,34 @@ class _Compiler:
             if head == "isnotnull":
                 self.insn.append((L.P_TRUE, 0, 0, 0, 0, 0.0, 0.0))
                 return
-            if head in ("StartsWith", "EndsWith", "Contains", "substring"):
-                raise NotImplementedError(f"string predicate {head} is not on the kernel path")
+            if head in ("StartsWith", "EndsWith", "Contains"):
+                cid, name = get_id(tree[1][0]), tree[1][1]
+                t = self.str_tensor(cid)
+                if head == "StartsWith":
+                    assert t.shape[-1] >= len(name)                       # filter.py:51
+                data = self._bytes(name, len(name))
+                off = self.pool_add(data)
+                self.emit_str(L.P_PREFIX if head == "StartsWith" else L.P_CONTAINS, cid, 0, off | (len(data) << 32))
+                return
+            if head == "substring":
+                raise NotImplementedError("substring is not on the kernel path")
             raise ValueError(f"Unsupported Function: {head}")
         op = tree[-2]
         if op == "IN":
             L_ = self.value(tree[0])
             if not isinstance(L_, _Col):
                 raise NotImplementedError("IN on a non-column operand")
+            if self.columns[L_.cid].dim() == 2 and self.columns[L_.cid].shape[1] != 1:   # filter.py:110-113
+                w = self.str_tensor(L_.cid).shape[-1]
+                if not tree[-1]:
+                    self.insn.append((L.P_FALSE, 0, 0, 0, 0, 0.0, 0.0))
+                    return
+                for i, r in enumerate(tree[-1]):
+                    assert len(r) != 1, "single characters against a string column (filter.py:111)"
+                    self.emit_str(L.P_STRCMP, L_.cid, L.EQ, self.pool_add(self._bytes(r, w)))
+                    if i:
+                        self.insn.append((L.P_OR, 0, 0, 0, 0, 0.0, 0.0))
+                return
             dt = self.dtype(L_.cid)
             if dt in (L.I64, L.I32):
                 vals = [int(r) for r in tree[-1]]
@@ -173,8 +227,17 @@ class _Compiler:
                 if i:
                     self.insn.append((L.P_OR, 0, 0, 0, 0, 0.0, 0.0))
             return
-        if op == "LIKE":
-            raise NotImplementedError("LIKE is not on the kernel path")
+        if op == "LIKE":                                   # filter.py:121-127
+            L_ = self.value(tree[0])
+            if not isinstance(L_, _Col):
+                raise NotImplementedError("LIKE on a non-column operand")
+            self.str_tensor(L_.cid)
+            assert tree[-1].count("%") == 3
+            _, w1, w2, _ = tree[-1].split("%")
+            a, b = self._bytes(w1, len(w1)), self._bytes(w2, len(w2))
+            oa, ob = self.pool_add(a), self.pool_add(b)
+            self.emit_str(L.P_LIKE2, L_.cid, 0, oa | (len(a) << 16) | (ob << 32) | (len(b) << 48))
+            return
         if op in ("AND", "OR"):
             self.emit(tree[0])
             self.emit(tree[-1])
@@ -202,7 +265,11 @@ class _Compiler:
         if isinstance(Rv, str):                            # filter.py:151-158
             if len(Rv) == 1:
                 return self.emit_cmp(Lv, op, ord(Rv))
-            raise NotImplementedError("multi-character string comparison is not on the kernel path")
+            t = self.columns[Lv.cid]
+            if t.dim() != 2:
+                raise NotImplementedError("multi-character literal against a one-dimensional column")
+            w = self.str_tensor(Lv.cid).shape[-1]
+            return self.emit_str(L.P_STRCMP, Lv.cid, _CMP[op], self.pool_add(self._bytes(Rv, w)))
         if op == "=" and self.dtype(Lv.cid) == L.F64:     # filter.py:160-161
             if not isinstance(Rv, float):
                 raise TypeError("isclose against a non-float literal (the reference raises here too)")
@@ -224,11 +291,33 @@ def compile_filter(tree, columns: Dict[int, Any], subquery=None) -> CompiledPred
     tensors = []
     ids = [None] * len(c.slots)
     for cid, s in c.slots.items():
-        t = c.col_tensor(cid).contiguous()
+        if cid in c.str_cols:
+            t = c.str_tensor(cid).contiguous()
+            p.widths[s] = int(t.shape[1])
+        else:
+            t = c.col_tensor(cid).contiguous()
         tensors.append(t)
         ids[s] = cid
         p.cols[s] = t.data_ptr()
         p.dtypes[s] = code_of(t.dtype)
     for i, (op, col, cmp, dom, li, lf, la) in enumerate(c.insn):
         p.insn[i] = L.PredInsn(op, col, cmp, dom, li, lf, la)
+    for i, b in enumerate(c.pool):
+        p.strpool[i] = b
     return CompiledPredicate(p, tensors, ids)
+
+
+def has_strings(P) -> bool:
+    """The predicate uses string instructions (only the library's evaluator runs them)."""
+    return P is not None and any(P.insn[k].op in (L.P_STRCMP, L.P_PREFIX, L.P_CONTAINS, L.P_LIKE2)
+                                 for k in range(P.n_insn))
+
+
+def torch_int8():
+    import torch
+    return torch.int8
+
+
+def torch_uint8():
+    import torch
+    return torch.uint8

@@ -428,6 +428,11 @@ int tqpk_groupby_emit_async(const tqpk_groupby_spec* h_spec, const tqpk_gb_plan*
 /* Reads (synchronising) the error word a fused pipeline left in its workspace. */
 int tqpk_pipeline_error(const void* d_ws, int* h_err, tqpk_stream stream);
 
+/* flags[idx[j]] = 1 for each j (indices outside [0, n) skipped): the probe rows
+ * that keep a pair after a join's extra conditions, from which the semi, anti
+ * and outer forms are compacted (hashjoin.py:110-151).                       */
+int tqpk_mark_rows(const int64_t* d_idx, int64_t n_idx, uint8_t* d_flags, int64_t n, tqpk_stream stream);
+
 /* Multi-column gather: out_c[j] = in_c[idx[j]]; with null_aware, an index
  * equal to TQPK_NULL_INDEX gives the value -64 (conversion.py:52-57).       */
 int tqpk_gather(int32_t ncols, const void* const* h_cols_in, const int32_t* h_dtypes,

@@ -223,11 +223,13 @@ def apply_mask_map(cols: Dict[int, np.ndarray], mask_map: Dict[int, int]) -> Dic
 # ---------------------------------------------------------------------------
 # Join: operators/hashjoin.py:24-177
 # ---------------------------------------------------------------------------
-def join_indices(left: np.ndarray, right: np.ndarray, jtype: str = "inner"):
+def join_indices(left: np.ndarray, right: np.ndarray, jtype: str = "inner", keep=None):
     """Sort-based equi-join of two key columns (hashjoin.py:24-151).
 
     Returns (left_idx, right_idx) as int64; for ``right-outer`` unmatched right
-    rows are appended with left index ``NULL`` (:135-158).
+    rows are appended with left index ``NULL`` (:135-158).  ``keep(cs, cr)``,
+    when given, is the extra join conditions' mask over the key-equal pairs
+    (:100-108); every join type is derived from the pairs it keeps.
     """
     left = left.reshape(-1)
     right = right.reshape(-1)
@@ -250,6 +252,9 @@ def join_indices(left: np.ndarray, right: np.ndarray, jtype: str = "inner"):
         cr = np.zeros(0, np.int64)
     cs = cs.astype(np.int64)
     cr = cr.astype(np.int64)
+    if keep is not None and cs.size:                               # :100-108
+        k = np.asarray(keep(cs, cr), bool).reshape(-1)
+        cs, cr = cs[k], cr[k]
     if jtype == "inner":                                           # :118-120
         return cs, cr
     matched = np.unique(cr)
@@ -267,6 +272,18 @@ def join_indices(left: np.ndarray, right: np.ndarray, jtype: str = "inner"):
     raise ValueError(jtype)
 
 
+def _cond_ids(tree, out):
+    if isinstance(tree, str):
+        if "#" in tree and not tree.startswith("Brand#"):
+            out[get_id(tree)] = True
+    elif isinstance(tree, list):
+        if len(tree) == 3 and tree[1] == "#":
+            out[int(tree[-1])] = True
+            return
+        for e in tree:
+            _cond_ids(e, out)
+
+
 def index_with_null(data: np.ndarray, idx: np.ndarray) -> np.ndarray:
     """conversion.py:52-57"""
     m = idx == NULL
@@ -276,11 +293,14 @@ def index_with_null(data: np.ndarray, idx: np.ndarray) -> np.ndarray:
     return out
 
 
-def join_vortex(cols: Dict[int, np.ndarray], args: dict, leftcol: int, rightcol: int, jtype: str):
+def join_vortex(cols: Dict[int, np.ndarray], args: dict, leftcol: int, rightcol: int, jtype: str,
+                conditions=()):
     """hashjoin.py:179-248: late-materialised inputs, join, gathered outputs.
 
     ``cols`` maps column id -> array (masks included).  Returns a new dict
     with the output columns replaced and the operator's row count.
+    ``conditions`` are filter trees over both sides' columns, evaluated on the
+    key-equal pairs (evaluate_join, :15-22, applied at :100-108).
     """
     mask_map = {int(k): v for k, v in args.get("mask map", {}).items()}
     groups = [args["left group"], args["right group"]]
@@ -294,7 +314,17 @@ def join_vortex(cols: Dict[int, np.ndarray], args: dict, leftcol: int, rightcol:
                     inp[mask_map[c]] = cols[mask_map[c]]
     used_masks = {c: mask_map[c] for c in out_ids if c in mask_map}
     m = apply_mask_map(inp, used_masks)
-    li, ri = join_indices(m[leftcol], m[rightcol], jtype)
+    left_ids = {c for c in out_ids if c in groups[0]}
+
+    def keep(cs, cr):
+        mask = np.ones(cs.size, bool)
+        for cond in conditions:
+            leaves = {}
+            _cond_ids(cond, leaves)
+            pair_cols = {c: (m[c][cs] if c in left_ids else m[c][cr]) for c in leaves}
+            mask &= np.asarray(eval_filter(cond, pair_cols, cs.size), bool).reshape(-1)
+        return mask
+    li, ri = join_indices(m[leftcol], m[rightcol], jtype, keep if conditions else None)
     sel = index_with_null if (jtype == "right-outer" and li.size > 0) else (lambda x, i: x[i])
     res = dict(cols)
     for c in out_ids:

@@ -390,8 +390,34 @@ def test_cpu_tensors_and_unsupported_shapes_raise():
         argsort_stable(torch.zeros(10, dtype=torch.int32))
     tg = {1: V(np.zeros(10, np.int8).reshape(5, 2))}
     with pytest.raises(NotImplementedError):
-        tqp_filter(True, tg, {"filter tree": [["s#1", "=", "AB"]], "materialized in": [1], "out mask id": 2},
-                   None, None, None, "f")
+        tqp_filter(True, tg, {"filter tree": [[["substring", ["s#1", "1", "2"]], "=", "AB"]], "materialized in": [1],
+                              "out mask id": 2}, None, None, None, "f")
     with pytest.raises(NotImplementedError):
         tqp_filter(False, tg, {"filter tree": [["s#1", "=", "A"]], "materialized in": [1], "out mask id": 2},
                    None, None, None, "f")
+
+
+@pytest.mark.parametrize("jtype", ["inner", "right-semi", "right-anti", "right-outer"])
+def test_join_conditions_every_join_type(jtype):
+    """Extra join conditions (a second key and a <> condition, hashjoin.py:100-108) with the
+    semi / anti / outer forms derived from the pairs they keep (hashjoin.py:110-151)."""
+    from tqpk.operators import join_vortex
+    from tqpk.variable import Variable
+    rng = np.random.default_rng(hash(jtype) % 1000)
+    nb, npr = 20_000, 90_001
+    cols = {11: rng.integers(0, 4000, nb).astype(np.int64), 12: rng.integers(0, 5, nb).astype(np.int32),
+            13: rng.integers(0, 100, nb).astype(np.int64),
+            21: rng.integers(0, 4500, npr).astype(np.int64), 22: rng.integers(0, 5, npr).astype(np.int32),
+            23: rng.integers(0, 100, npr).astype(np.int64), 24: rng.integers(0, 2557, npr).astype(np.int32)}
+    cols[902] = cols[24] > 1000
+    conds = [["#12", "=", "#22"], ["s#13", "<", "t#23"]]
+    args = {"left group": [11, 12, 13], "right group": [21, 22, 23, 24], "materialized in": [11, 12, 13, 21, 22, 23],
+            "mask map": {21: 902, 22: 902, 23: 902}}
+    tg = {c: Variable(torch.from_numpy(a).cuda(), "int") for c, a in cols.items() if c != 902}
+    tg[902] = Variable(torch.from_numpy(cols[902]).cuda(), "bool")
+    rows = join_vortex(True, tg, copy.deepcopy(args), 11, 21, copy.deepcopy(conds), jtype, None, None, "j")
+    ref, ref_rows = O.join_vortex(cols, copy.deepcopy(args), 11, 21, jtype, conds)
+    assert rows == ref_rows
+    for c in (11, 12, 13, 21, 22, 23):
+        got = np_(tg[c].tensor).reshape(-1)
+        np.testing.assert_array_equal(got, np.asarray(ref[c]).reshape(-1), err_msg=str(c))

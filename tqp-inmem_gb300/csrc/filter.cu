@@ -434,3 +434,22 @@ extern "C" int tqpk_compact(const tqpk_predicate* h_pred, const uint8_t* d_mask,
   return compact_launch(d_mask ? nullptr : h_pred, d_mask, n, C, d_count, d_ws, ws_bytes,
                         static_cast<cudaStream_t>(stream));
 }
+
+namespace tqpk {
+__global__ void k_mark_rows(const int64_t* __restrict__ idx, int64_t n_idx, uint8_t* __restrict__ flags, int64_t n) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n_idx; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx[j];
+    if (i >= 0 && i < n) flags[i] = 1;
+  }
+}
+}  // namespace tqpk
+
+// flags[idx[j]] = 1 for every j (indices outside [0, n) are skipped): the rows a set of
+// join pairs touches, for the semi / anti / outer forms of a join with extra conditions.
+extern "C" int tqpk_mark_rows(const int64_t* d_idx, int64_t n_idx, uint8_t* d_flags, int64_t n, tqpk_stream stream) {
+  if (n_idx < 0 || n < 0 || (n_idx > 0 && (!d_idx || !d_flags))) return TQPK_EINVAL;
+  if (n_idx == 0) return TQPK_OK;
+  k_mark_rows<<<grid_for(n_idx, 4), kBlock, 0, static_cast<cudaStream_t>(stream)>>>(d_idx, n_idx, d_flags, n);
+  TQPK_CHECK_LAUNCH();
+  return TQPK_OK;
+}

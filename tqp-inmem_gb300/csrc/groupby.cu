@@ -502,7 +502,7 @@ extern "C" int tqpk_groupby_plan(const tqpk_groupby_spec* S, const tqpk_predicat
                                  int64_t n, tqpk_gb_plan* plan, void* scratch, tqpk_stream stream) {
   int rc = check_spec(S, n > 0);
   if (rc) return rc;
-  if ((rc = check_pred(pred))) return rc;
+  if (n > 0 && (rc = check_pred(pred))) return rc;   // an empty input never evaluates its predicate
   if (!plan || n < 0) return TQPK_EINVAL;
   *plan = tqpk_gb_plan{};
   int64_t mn[TQPK_MAX_KEYS], mx[TQPK_MAX_KEYS], rows = 0;
@@ -561,7 +561,7 @@ extern "C" int tqpk_groupby_run(const tqpk_groupby_spec* S, const tqpk_gb_plan* 
                                 tqpk_stream stream) {
   int rc = check_spec(S, n > 0);
   if (rc) return rc;
-  if ((rc = check_pred(pred))) return rc;
+  if (n > 0 && (rc = check_pred(pred))) return rc;   // an empty input never evaluates its predicate
   if (!plan || !ws || ws_bytes < plan->ws_bytes || !h_groups || n < 0) return !ws || ws_bytes < (plan ? plan->ws_bytes : 0) ? TQPK_ENOMEM : TQPK_EINVAL;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (plan->mode == TQPK_GB_HASH) {

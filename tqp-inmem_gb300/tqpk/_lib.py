@@ -98,6 +98,7 @@ SIGNATURES = {
     "tqpk_join_probe": (C.c_int, [_P(JoinPlan), _VP, _VP, _I32, _VP, _I64, _I32, _VP, _VP, _I64, _P(_I64), _VP,
                                   _SZ, _VP]),
     "tqpk_gather": (C.c_int, [_I32, _P(_VP), _P(_I32), _VP, _I64, _I32, _P(_VP), _VP]),
+    "tqpk_mark_rows": (C.c_int, [_VP, _I64, _VP, _I64, _VP]),
     "tqpk_batch_record_bytes": (_SZ, []),
     "tqpk_batch_join_workspace_bytes": (_SZ, [_I64, _I64]),
     "tqpk_batch_describe_join": (C.c_int, [_VP, _VP, _I32, _I64, _P(Predicate), _I64, _I64, _VP, _I32, _I64,

@@ -15,7 +15,8 @@ which changes a result:
 
 Extra join conditions (:100-108, e.g. the second key of a two-key join,
 main.py:208-217) are evaluated on the gathered pair columns with the
-predicate kernel and the pairs compacted; they are supported for inner joins.
+predicate kernel and the pairs compacted; the semi, anti and outer forms are
+then derived from the probe rows that keep a pair (:110-151).
 """
 from __future__ import annotations
 
@@ -24,7 +25,7 @@ from typing import Dict, List
 import torch
 
 from .. import _lib as L
-from ..ops import compact, filter_mask, gather, join_build, join_probe
+from ..ops import compact, filter_mask, gather, join_build, join_probe, mark_rows
 from ..predicate import compile_filter
 from ..variable import make_like
 from .filter import _require_gpu
@@ -53,10 +54,9 @@ def _side_mask(tensor_group, cols: List[int], mask_map: Dict[int, int], key: int
 def _pairs(tensors_left, tensors_right, left_key, right_key, condition_list, jtype, left_mask, right_mask):
     lk = tensors_left[left_key].tensor
     rk = tensors_right[right_key].tensor
-    if condition_list and jtype != "inner":
-        raise NotImplementedError("join conditions are supported for inner joins only")
     b = join_build(lk, left_mask)
-    bi, pi = join_probe(b, rk, right_mask, jtype)
+    # with extra conditions every form starts from the key-equal pairs (hashjoin.py:100-108)
+    bi, pi = join_probe(b, rk, right_mask, "inner" if condition_list else jtype)
     for cond in condition_list:                       # hashjoin.py:100-108
         ids = set()
         _collect_ids(cond, ids)
@@ -69,7 +69,29 @@ def _pairs(tensors_left, tensors_right, left_key, right_key, condition_list, jty
         pred = compile_filter(cond, cols)
         keep, _ = filter_mask(pred, int(bi.numel()), bi.device)
         (bi, pi), _ = compact([bi, pi], mask=keep)
+    if condition_list and jtype != "inner":
+        bi, pi = _non_inner(bi, pi, rk, right_mask, jtype)
     return bi, pi, b.plan.nb_rows
+
+
+def _non_inner(bi, pi, rk, right_mask, jtype):
+    """hashjoin.py:110-151 from the pairs left after the conditions: semi = probe rows with
+    a pair (ascending), anti = probe rows (passing their mask) without one, outer = the
+    pairs followed by the anti rows with a null build index."""
+    n = int(rk.numel())
+    hit = mark_rows(pi, n)
+    dev = rk.device
+    if jtype == "right-semi":
+        (rows,), _ = compact([], mask=hit, with_row_ids=True)
+        return torch.empty(0, dtype=torch.int64, device=dev), rows
+    tree = ["NOT", ["h#2"]] if right_mask is None else [["m#1"], "AND", ["NOT", ["h#2"]]]
+    cols = {2: hit} if right_mask is None else {1: right_mask.to(torch.bool), 2: hit}
+    lone, _ = filter_mask(compile_filter(tree, cols), n, dev)
+    (rows,), _ = compact([], mask=lone, with_row_ids=True)
+    if jtype == "right-anti":
+        return torch.empty(0, dtype=torch.int64, device=dev), rows
+    nulls = torch.full((rows.numel(),), L.NULL_INDEX, dtype=torch.int64, device=dev)
+    return torch.cat([bi, nulls]), torch.cat([pi, rows])
 
 
 def _collect_ids(tree, out):

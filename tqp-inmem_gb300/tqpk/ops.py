@@ -293,3 +293,14 @@ def project(prog, n: int, device) -> List[torch.Tensor]:
     a.i32(jit._aligned(*prog.tensors))
     jit.launch(h, jit.occupancy_grid(h, 256, 0, (n + 3) // 4), 256, 0, a, _stream(device))
     return outs
+
+
+def mark_rows(idx: torch.Tensor, n: int) -> torch.Tensor:
+    """Bool flags over n rows: True at every index in idx."""
+    lib = L.load()
+    flags = torch.zeros(n, dtype=torch.bool, device=idx.device)
+    _check_cuda(idx)
+    idx = idx.contiguous()
+    L.check(lib.tqpk_mark_rows(idx.data_ptr() if idx.numel() else None, idx.numel(),
+                               flags.data_ptr() if n else None, n, _stream(idx.device)), "tqpk_mark_rows")
+    return flags

@@ -379,6 +379,11 @@ int tqpk_jit_occupancy(void* handle, int32_t block, size_t smem);
 int tqpk_jit_launch(void* handle, int32_t grid, int32_t block, size_t smem, void** args, int32_t timing_kid,
                     tqpk_stream stream);
 int32_t tqpk_num_sms(void);
+/* A group-by plan from key domains known ahead (table statistics [key_min, key_max]
+ * per key), with no pass over the data and no host synchronisation; n_rows sizes
+ * the hash mode.  The groups still come out only for occupied slots.          */
+int tqpk_groupby_plan_domains(const tqpk_groupby_spec* h_spec, const int64_t* h_key_min, const int64_t* h_key_max,
+                              int64_t n_rows, tqpk_gb_plan* h_plan);
 /* Stages of tqpk_groupby_run around a caller-launched accumulation kernel. */
 int tqpk_groupby_prepare(const tqpk_groupby_spec* h_spec, const tqpk_gb_plan* h_plan, void* d_ws, size_t ws_bytes,
                          tqpk_stream stream);

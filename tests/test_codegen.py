@@ -73,6 +73,14 @@ def test_probe_kernels_compile_with_and_without_build_filter():
         src, _ = jit.star_probe_source(prog.spec, vreg, f.struct if f else None, a.struct if a else None)
         ok, log = jit.check_compiles(src)
         assert ok, log[:2000]
+    for early, cs in ((True, False), (True, True), (False, True)):
+        src, _ = jit.star_probe_source(prog.spec, vreg, pp.struct, cat.struct, early_fb=early, stream_cs=cs)
+        ok, log = jit.check_compiles(src)
+        assert ok, log[:2000]
+        assert ("#define TQPK_LD(p) __ldcs" in src) == cs
+    src, _ = jit.join_probe_source(prog.spec, vreg, pp.struct, None, stream_cs=True)
+    ok, log = jit.check_compiles(src)
+    assert ok, log[:2000]
 
 
 def test_generated_batch_kernel_compiles_and_record_layout_matches():

@@ -142,3 +142,34 @@ def test_topk_threshold_path_and_tie_fallback(n, k, hi, desc):
     x = rng.integers(0, hi, n).astype(np.int64)
     got = topk_stable(torch.from_numpy(x).cuda(), k, desc).cpu().numpy()
     np.testing.assert_array_equal(got, O._stable_order(x, desc)[:k])
+
+
+@pytest.mark.parametrize("n,groups", [(1_000_003, 6), (200_000, 1400), (50_000, 30_000), (3, 4)])
+def test_groupby_pipeline_domains_and_graph_replay(n, groups):
+    """Filter + group-by over table-statistic key domains, no host synchronisation inside;
+    graph replays give the oracle's groups in key order."""
+    from tqpk import datagen
+    from tqpk.pipeline import GroupByPipeline
+    t, (a, b) = datagen.groupby_instance_tables(n, groups, 17)
+    ids = {"quantity": 1, "price": 2, "discount": 3, "tax": 4, "flag": 5, "status": 6, "ship_date": 7}
+    cols = {ids[k]: v for k, v in t.items()}
+    d = {c: torch.from_numpy(x).cuda() for c, x in cols.items()}
+    results = ["flag#5", "status#6", [[["sum", [["price#2", "*", ["1.0", "-", "discount#3"]]]], "#", "1"], "AS", "c#203"],
+               [[["avg", ["discount#3"]], "#", "2"], "AS", "g#207"], [[["min", ["price#2"]], "#", "3"], "AS", "m#209"],
+               [[["count", ["1"]], "#", "4L"], "AS", "h#208"]]
+    args = {"is partial": False, "keys": ["flag#5", "status#6"], "input ids": [1, 2, 3, 4, 5, 6], "results": results,
+            "out agg ids": [203, 207, 209, 208]}
+    tree = [["ship_date#7", "<=", "2000"]]
+    p = GroupByPipeline(args, {c: d[c] for c in range(1, 7)}, tree, {7: d[7]}, [(0, a - 1), (0, b - 1)])
+    oc = dict(cols)
+    oc[900] = O.eval_filter(tree, {7: cols[7]})
+    ref = O.tqp_hash_aggregate(oc, dict(copy.deepcopy(args), **{"mask map": {c: 900 for c in range(1, 7)}}))
+    p.capture()
+    for _ in range(2):
+        p.replay()
+        keys, outs, G = p.result()
+        np.testing.assert_array_equal(keys[0].cpu().numpy(), ref[5].reshape(-1))
+        np.testing.assert_array_equal(keys[1].cpu().numpy(), ref[6].reshape(-1))
+        for oid in args["out agg ids"]:
+            e = ref[oid]
+            (assert_f64_close if e.dtype == np.float64 else np.testing.assert_array_equal)(outs[oid].cpu().numpy(), e)

@@ -494,21 +494,9 @@ static int check_spec(const tqpk_groupby_spec* S, bool has_rows = true) {
 
 constexpr int64_t kPrivateBudget = 96 * 1024;  // bytes of shared memory per CTA for private tables
 
-}  // namespace tqpk
-
-using namespace tqpk;
-
-extern "C" int tqpk_groupby_plan(const tqpk_groupby_spec* S, const tqpk_predicate* pred, const uint8_t* mask,
-                                 int64_t n, tqpk_gb_plan* plan, void* scratch, tqpk_stream stream) {
-  int rc = check_spec(S, n > 0);
-  if (rc) return rc;
-  if (n > 0 && (rc = check_pred(pred))) return rc;   // an empty input never evaluates its predicate
-  if (!plan || n < 0) return TQPK_EINVAL;
-  *plan = tqpk_gb_plan{};
-  int64_t mn[TQPK_MAX_KEYS], mx[TQPK_MAX_KEYS], rows = 0;
-  rc = key_ranges(pred, mask, n, S->n_keys, S->keys, S->key_dtypes, mn, mx, &rows, scratch,
-                  static_cast<cudaStream_t>(stream));
-  if (rc) return rc;
+// Slots, table placement and workspace of a plan from the key ranges and the row count.
+static int plan_from_ranges(const tqpk_groupby_spec* S, const int64_t* mn, const int64_t* mx, int64_t rows,
+                            tqpk_gb_plan* plan) {
   plan->n_rows = rows;
   int64_t K = 1;
   bool overflow = false;
@@ -554,6 +542,39 @@ extern "C" int tqpk_groupby_plan(const tqpk_groupby_spec* S, const tqpk_predicat
   }
   plan->ws_bytes = 512 + align_up((size_t)(K * A * 8), 256) + compact_status_bytes(K);
   return TQPK_OK;
+}
+
+}  // namespace tqpk
+
+using namespace tqpk;
+
+extern "C" int tqpk_groupby_plan(const tqpk_groupby_spec* S, const tqpk_predicate* pred, const uint8_t* mask,
+                                 int64_t n, tqpk_gb_plan* plan, void* scratch, tqpk_stream stream) {
+  int rc = check_spec(S, n > 0);
+  if (rc) return rc;
+  if (n > 0 && (rc = check_pred(pred))) return rc;   // an empty input never evaluates its predicate
+  if (!plan || n < 0) return TQPK_EINVAL;
+  *plan = tqpk_gb_plan{};
+  int64_t mn[TQPK_MAX_KEYS], mx[TQPK_MAX_KEYS], rows = 0;
+  rc = key_ranges(pred, mask, n, S->n_keys, S->keys, S->key_dtypes, mn, mx, &rows, scratch,
+                  static_cast<cudaStream_t>(stream));
+  if (rc) return rc;
+  return plan_from_ranges(S, mn, mx, rows, plan);
+}
+
+// The plan of a key domain known without a pass over the data (table statistics:
+// [key_min[k], key_max[k]] per key), for callers that run the group-by with no host
+// synchronisation (a captured graph, a serving loop).  n_rows is the row count the
+// hash-mode sizing assumes (the input's rows); dense modes do not depend on it.
+extern "C" int tqpk_groupby_plan_domains(const tqpk_groupby_spec* S, const int64_t* key_min, const int64_t* key_max,
+                                         int64_t n_rows, tqpk_gb_plan* plan) {
+  int rc = check_spec(S, false);
+  if (rc) return rc;
+  if (!plan || n_rows < 0 || (S->n_keys > 0 && (!key_min || !key_max))) return TQPK_EINVAL;
+  for (int k = 0; k < S->n_keys; ++k)
+    if (key_max[k] < key_min[k]) return TQPK_EINVAL;
+  *plan = tqpk_gb_plan{};
+  return plan_from_ranges(S, key_min, key_max, std::max<int64_t>(n_rows, 1), plan);
 }
 
 extern "C" int tqpk_groupby_run(const tqpk_groupby_spec* S, const tqpk_gb_plan* plan, const tqpk_predicate* pred,

@@ -121,6 +121,7 @@ SIGNATURES = {
     "tqpk_jit_launch": (C.c_int, [_VP, _I32, _I32, _SZ, _P(_VP), _I32, _VP]),
     "tqpk_num_sms": (_I32, []),
     "tqpk_groupby_prepare": (C.c_int, [_P(GroupbySpec), _P(GbPlan), _VP, _SZ, _VP]),
+    "tqpk_groupby_plan_domains": (C.c_int, [_P(GroupbySpec), _P(_I64), _P(_I64), _I64, _P(GbPlan)]),
     "tqpk_groupby_count": (C.c_int, [_P(GroupbySpec), _P(GbPlan), _VP, _P(_I64), _VP]),
     "tqpk_groupby_table": (_VP, [_VP]),
     "tqpk_pipeline_join_agg_topk_stages": (C.c_int, [_I32, _VP, _I32, _I64, _P(Predicate), _I64, _I64, _VP, _I32, _I64,

@@ -65,12 +65,17 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
 // predicate literals, bound at launch (one compiled kernel serves every constant)
 struct PL { long long i[32]; double f[32]; double a[32]; };
 template <class T> struct V4 { T v[4]; };
+// column stream loads; a kernel source may define TQPK_LD as __ldcs (evict-first) so the
+// streamed columns do not push directories and group tables out of L2
+#ifndef TQPK_LD
+#define TQPK_LD(p) (*(p))
+#endif
 // four consecutive rows r0..r0+3 (r0 % 4 == 0); rows >= n read as 0
 __device__ __forceinline__ V4<double> ld4(const double* p, i64 r0, i64 n, bool vec) {
   V4<double> o;
   if (vec && r0 + 4 <= n) {
     const double2* q = reinterpret_cast<const double2*>(p + r0);
-    double2 a = q[0], b = q[1];
+    double2 a = TQPK_LD(q), b = TQPK_LD(q + 1);
     o.v[0] = a.x; o.v[1] = a.y; o.v[2] = b.x; o.v[3] = b.y;
   } else {
     for (int j = 0; j < 4; ++j) o.v[j] = (r0 + j < n) ? p[r0 + j] : 0.0;
@@ -81,7 +86,7 @@ __device__ __forceinline__ V4<long long> ld4(const long long* p, i64 r0, i64 n, 
   V4<long long> o;
   if (vec && r0 + 4 <= n) {
     const longlong2* q = reinterpret_cast<const longlong2*>(p + r0);
-    longlong2 a = q[0], b = q[1];
+    longlong2 a = TQPK_LD(q), b = TQPK_LD(q + 1);
     o.v[0] = a.x; o.v[1] = a.y; o.v[2] = b.x; o.v[3] = b.y;
   } else {
     for (int j = 0; j < 4; ++j) o.v[j] = (r0 + j < n) ? p[r0 + j] : 0;
@@ -91,7 +96,7 @@ __device__ __forceinline__ V4<long long> ld4(const long long* p, i64 r0, i64 n, 
 __device__ __forceinline__ V4<int> ld4(const int* p, i64 r0, i64 n, bool vec) {
   V4<int> o;
   if (vec && r0 + 4 <= n) {
-    int4 a = *reinterpret_cast<const int4*>(p + r0);
+    int4 a = TQPK_LD(reinterpret_cast<const int4*>(p + r0));
     o.v[0] = a.x; o.v[1] = a.y; o.v[2] = a.z; o.v[3] = a.w;
   } else {
     for (int j = 0; j < 4; ++j) o.v[j] = (r0 + j < n) ? p[r0 + j] : 0;
@@ -102,7 +107,7 @@ template <class B>
 __device__ __forceinline__ V4<B> ld4b(const B* p, i64 r0, i64 n, bool vec) {
   V4<B> o;
   if (vec && r0 + 4 <= n) {
-    unsigned w = *reinterpret_cast<const unsigned*>(p + r0);
+    unsigned w = TQPK_LD(reinterpret_cast<const unsigned*>(p + r0));
     for (int j = 0; j < 4; ++j) o.v[j] = (B)((w >> (8 * j)) & 0xff);
   } else {
     for (int j = 0; j < 4; ++j) o.v[j] = (r0 + j < n) ? p[r0 + j] : (B)0;
@@ -514,8 +519,8 @@ def probe_units(n: int) -> int:
     return (int(n) + 4 * PROBE_U - 1) // (4 * PROBE_U)
 
 
-def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, min_blocks: int = 0
-                      ) -> Tuple[str, str]:
+def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, min_blocks: int = 0,
+                      stream_cs: bool = False) -> Tuple[str, str]:
     """CUDA source of the fused probe + aggregate (directory lookup, value, FP64 sum, occupancy).
 
     The directory holds build row indices (negative = no row).  `bpred`, when
@@ -524,7 +529,8 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
     Each lane filters and looks up 4U consecutive rows (4-row vector loads);
     the warp then computes the value and updates the group of its matched rows
     densely (_dense_tail).  min_blocks > 0 asks the compiler for that many
-    resident CTAs per SM (__launch_bounds__ register cap)."""
+    resident CTAs per SM (__launch_bounds__ register cap); stream_cs loads the
+    probe columns with evict-first hints."""
     S = spec
     pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
     ecols, elines = _expr_code(S, val_reg + 1, "c")
@@ -544,7 +550,8 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
     rows = 4 * U                                   # rows per lane
     qt = "unsigned char" if 32 * rows <= 256 else "unsigned short"
     lb = f"256, {min_blocks}" if min_blocks else "256"
-    src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__({lb}) {name}(',
+    hint = "#define TQPK_LD(p) __ldcs(p)\n" if stream_cs else ""
+    src = [hint + PRELUDE, f'extern "C" __global__ void __launch_bounds__({lb}) {name}(',
            "    " + ",\n    ".join(params) + ") {",
            f"  __shared__ {qt} q_off[8][{32 * rows}];",
            f"  __shared__ int q_slot[8][{32 * rows}];",
@@ -818,13 +825,15 @@ def join_probe_args(a: "_Args", spec, pred, bpred, fk, np_: int, key_min: int, s
 
 
 # ---------------------------------------------------------------------------- star probe
-def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_blocks: int = 0
-                      ) -> Tuple[str, str]:
+def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_blocks: int = 0,
+                      early_fb: bool = False, stream_cs: bool = False) -> Tuple[str, str]:
     """CUDA source of the star probe: fact -> A (row directory, A predicate through the
     row) -> B (directory of the C foreign key) -> C (row directory), then FP64 sum and
     count per C slot, computed warp-densely over the matched rows (_dense_tail).
     Directories: A and C hold row indices (negative = none), B holds the C key
-    (INT_MIN = none)."""
+    (INT_MIN = none).  early_fb loads the fkB column together with fkA, so the
+    B lookup does not wait for a second column round trip after the A lookup;
+    stream_cs loads the fact columns with evict-first hints."""
     S = spec
     pcols, pexpr = _pred_code(fpred, "p") if fpred is not None else ([], "true")
     ecols, elines = _expr_code(S, val_reg + 1, "c")
@@ -843,7 +852,8 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
     rows = 4 * U
     qt = "unsigned char" if 32 * rows <= 256 else "unsigned short"
     lb = f"256, {min_blocks}" if min_blocks else "256"
-    src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__({lb}) {name}(', "    " + ",\n    ".join(params) + ") {",
+    hint = "#define TQPK_LD(p) __ldcs(p)\n" if stream_cs else ""
+    src = [hint + PRELUDE, f'extern "C" __global__ void __launch_bounds__({lb}) {name}(', "    " + ",\n    ".join(params) + ") {",
            f"  __shared__ {qt} q_off[8][{32 * rows}];",
            f"  __shared__ int q_slot[8][{32 * rows}];",
            "  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;",
@@ -851,15 +861,19 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
            "  const i64 stride = (i64)gridDim.x * blockDim.x;",
            "  for (i64 w0 = blockIdx.x * (i64)blockDim.x + (threadIdx.x & ~31); w0 < nr; w0 += stride) {",
            f"    const i64 g = w0 + lane, wrow = w0 * {rows};",
-           f"    i64 k[{U}][4]; int rw[{U}][4]; unsigned m[{U}];",
+           f"    i64 k[{U}][4]; int rw[{U}][4]; unsigned m[{U}];"]
+    if early_fb:
+        src += [f"    V4<int> FBs[{U}];"]
+    src += [
            "#pragma unroll",
            f"    for (int u = 0; u < {U}; ++u) {{",
            f"      const i64 r0 = g * {rows} + u * 4;",
            "      m[u] = 0;",
            "      if (r0 >= nf) continue;"]
     src += ["      " + l for l in _load_lines(pcols, fpred.dtypes, "P", "pp", "nf", "vp != 0")] if fpred is not None else []
-    src += ["      const V4<int> FA = ld4(fka, r0, nf, vf != 0);",
-            "#pragma unroll",
+    src += ["      const V4<int> FA = ld4(fka, r0, nf, vf != 0);"]
+    src += ["      FBs[u] = ld4(fkb, r0, nf, vf != 0);"] if early_fb else []
+    src += ["#pragma unroll",
             "      for (int j = 0; j < 4; ++j) {",
             "        k[u][j] = (i64)FA.v[j] - a_min;",
             f"        const bool ok = (r0 + j < nf) && ({_rename(pexpr, 'p', 'P')}) && k[u][j] >= 0 && k[u][j] < a_slots;",
@@ -883,7 +897,7 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
             f"    for (int u = 0; u < {U}; ++u) {{",
             "      if (!m[u]) continue;",
             f"      const i64 r0 = g * {rows} + u * 4;",
-            "      const V4<int> FB = ld4(fkb, r0, nf, vf != 0);",
+            "      const V4<int> FB = FBs[u];" if early_fb else "      const V4<int> FB = ld4(fkb, r0, nf, vf != 0);",
             "#pragma unroll",
             "      for (int j = 0; j < 4; ++j) {",
             "        const i64 sb = (i64)FB.v[j] - b_min;",

@@ -300,3 +300,96 @@ class StarAggTopK:
         m = int(self.out_count.item())
         return (self.out_keys[:m].cpu().numpy(), self.out_vals[:m].cpu().numpy(),
                 self.out_cnts[:m].cpu().numpy(), int(self.groups.item()))
+
+
+class GroupByPipeline:
+    """Filter + group-by whose key domains are known ahead (table statistics), with no
+    host synchronisation: the accumulator table is reset, the generated filter +
+    accumulation kernel runs, and the occupied groups are counted and written on the
+    device (tqpk_groupby_emit_async).  The same groups, in the same key order, as
+    tqp_hash_aggregate over the filtered rows; capture()/replay() as a CUDA graph."""
+
+    def __init__(self, args: dict, columns: Dict[int, torch.Tensor], filter_tree, filter_cols: Dict[int, torch.Tensor],
+                 key_domains):
+        from . import jit
+        from .dtypes import dtype_of
+        from .predicate import has_strings
+        if not jit.available():
+            raise NotImplementedError("the group-by pipeline needs the runtime compiler (NVRTC)")
+        self.lib = L.load()
+        first = next(iter(columns.values()))
+        self.dev, self.n = first.device, int(first.shape[0])
+        a = dict(args)
+        a.pop("mask map", None)
+        self.prog = compile_aggregate(a, columns)
+        self.pred = compile_filter(filter_tree, filter_cols) if filter_tree is not None else None
+        if self.pred is not None and has_strings(self.pred.struct):
+            raise NotImplementedError("string predicates run on the operator path")
+        S = self.prog.spec
+        nk = S.n_keys
+        kmin = (C.c_int64 * max(nk, 1))(*[int(d[0]) for d in key_domains])
+        kmax = (C.c_int64 * max(nk, 1))(*[int(d[1]) for d in key_domains])
+        self.plan = L.GbPlan()
+        L.check(self.lib.tqpk_groupby_plan_domains(C.byref(S), kmin, kmax, self.n, C.byref(self.plan)),
+                "tqpk_groupby_plan_domains")
+        if self.plan.mode == L.GB_HASH:
+            raise NotImplementedError("a sparse key domain takes the operator path (hash group-by)")
+        K = int(self.plan.slots)
+        self.ws = torch.empty(max(int(self.plan.ws_bytes), 256), dtype=torch.uint8, device=self.dev)
+        self.keys = [torch.empty(K, dtype=dtype_of(S.key_dtypes[k]), device=self.dev) for k in range(nk)]
+        self.outs = [torch.empty(K, dtype=dt, device=self.dev) for (_, _, _, _, dt) in self.prog.outputs]
+        self.groups = torch.zeros(1, dtype=torch.int64, device=self.dev)
+        ops = []
+        for (_, op, a_, b_, dt) in self.prog.outputs:
+            ops += [op, a_, b_, code_of(dt)]
+        self._ops = (C.c_int32 * max(len(ops), 1))(*ops)
+        self._kp = (C.c_void_p * max(nk, 1))(*[k.data_ptr() for k in self.keys])
+        self._oc = (C.c_void_p * max(len(self.outs), 1))(*[o.data_ptr() for o in self.outs])
+        P = self.pred.struct if self.pred is not None else None
+        src, name, self.T, self.smem = jit.groupby_source(S, P, self.plan)
+        self.kernel = jit.compile_kernel(src, name)
+        self.args = jit._Args()
+        if P is not None:
+            for c in range(P.n_cols):
+                self.args.ptr(P.cols[c])
+        self.args.blob(jit.pred_lits(P))
+        for k in range(nk):
+            self.args.ptr(S.keys[k])
+        for c in range(S.n_cols):
+            self.args.ptr(S.cols[c])
+        self.args.i64(self.n)
+        self.args.ptr(self.lib.tqpk_groupby_table(self.ws.data_ptr()))
+        self.args.i32(jit._aligned(*self.pred.tensors) if self.pred is not None else 1)
+        self.args.i32(jit._aligned(*self.prog.tensors[:nk]))
+        self.args.i32(jit._aligned(*self.prog.tensors[nk:]))
+        self.grid = jit.occupancy_grid(self.kernel, self.T, self.smem, (self.n + 3) // 4)
+
+    def run(self, stream=None):
+        from . import jit
+        s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
+        S = self.prog.spec
+        L.check(self.lib.tqpk_groupby_prepare(C.byref(S), C.byref(self.plan), self.ws.data_ptr(), self.ws.numel(), s),
+                "tqpk_groupby_prepare")
+        if self.n > 0:
+            jit.launch(self.kernel, self.grid, self.T, self.smem, self.args, s, L.KID_GROUPBY)
+        L.check(self.lib.tqpk_groupby_emit_async(C.byref(S), C.byref(self.plan), self.ws.data_ptr(), self._kp,
+                                                 len(self.outs), self._ops, self._oc, self.groups.data_ptr(), s),
+                "tqpk_groupby_emit_async")
+
+    def capture(self):
+        self.run()
+        torch.cuda.synchronize(self.dev)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.run()
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()
+
+    def result(self):
+        """(key columns [G], {out id: column [G]}, G) after the last run (synchronises)."""
+        G = int(self.groups.item())
+        if G < 0:
+            L.check(G, "group-by emit")
+        return ([k[:G] for k in self.keys], {oid: o[:G] for (oid, *_), o in zip(self.prog.outputs, self.outs)}, G)

@@ -97,20 +97,28 @@ typedef struct {
   tqpk_pred_insn insn[TQPK_MAX_PRED];
   int32_t widths[TQPK_MAX_COLS];      /* bytes per row of an int8 [N, w] string column, else 0 */
   uint8_t strpool[TQPK_MAX_STRPOOL];  /* literal bytes of the string instructions */
+  int32_t strides[TQPK_MAX_COLS];     /* row stride of a string column view (substring, filter.py:71-76):
+                                         bytes between rows; 0 = the width */
 } tqpk_predicate;
 
-/* ---- row expressions (aggregate.py:58-233, arithmetic part) --------------
+/* ---- row expressions (aggregate.py:58-233) --------------------------------
  * Straight-line SSA program: instruction i writes register i.  Operands a, b
  * are earlier register numbers.  Arithmetic follows torch's promotion:
  * registers are float64 or int64 (`type`); float64 arithmetic is IEEE
- * round-to-nearest per operation (no contraction), as torch evaluates it.   */
+ * round-to-nearest per operation (no contraction), as torch evaluates it.
+ * TQPK_X_SELECT is torch.where(a != 0, b, col) (CASE WHEN, aggregate.py:76-87;
+ * register `col` holds the ELSE value, the condition is a 0/1 register, e.g.
+ * a bool column).  TQPK_X_YEAR maps int64 days since 1990-01-01 to the year
+ * (aggregate.py:100-101: bucketize over the cumulative year lengths of
+ * 1990-1999; days before 1990 give 1990, days from 2000 on the calendar year,
+ * where the reference's year table has no entry).                         */
 enum { TQPK_X_COL = 1, TQPK_X_CONST = 2, TQPK_X_ADD = 3, TQPK_X_SUB = 4, TQPK_X_MUL = 5,
-       TQPK_X_DIV = 6, TQPK_X_TOF64 = 7 };
+       TQPK_X_DIV = 6, TQPK_X_TOF64 = 7, TQPK_X_SELECT = 8, TQPK_X_YEAR = 9 };
 
 typedef struct {
   int32_t op, type; /* type: TQPK_I64 or TQPK_F64 */
   int32_t a, b;     /* operand registers */
-  int32_t col;      /* TQPK_X_COL: column slot */
+  int32_t col;      /* TQPK_X_COL: column slot; TQPK_X_SELECT: ELSE register */
   int32_t pad;
   int64_t ci;       /* TQPK_X_CONST integer value */
   double cf;        /* TQPK_X_CONST float value */
@@ -443,6 +451,25 @@ int tqpk_mark_rows(const int64_t* d_idx, int64_t n_idx, uint8_t* d_flags, int64_
 int tqpk_gather(int32_t ncols, const void* const* h_cols_in, const int32_t* h_dtypes,
                 const int64_t* d_idx, int64_t n_idx, int32_t null_aware, void* const* h_cols_out,
                 tqpk_stream stream);
+
+/* ---- group codes of arbitrary key tuples (aggregate.py:291-333) ----------
+ * Key tuples of up to TQPK_MAX_COLS columns: 1-D integer or float64 keys
+ * (h_widths[k] = 0) and int8/uint8 [N, w] string keys (h_widths[k] = w), the
+ * columns the reference stacks side by side before numbering the distinct
+ * rows.  Rows passing d_mask (NULL = all) get d_codes[r] in [0, G), ordered by
+ * key tuple ascending (numbers by value, float64 -0.0 == +0.0, strings byte by
+ * byte as int8); masked rows get 0.  d_reps[g] (room for n) is a row of group
+ * g.  Synchronises once (for G).                                            */
+size_t tqpk_key_encode_workspace_bytes(int64_t n);
+int tqpk_key_encode(int32_t n_keys, const void* const* h_keys, const int32_t* h_dtypes, const int32_t* h_widths,
+                    const uint8_t* d_mask, int64_t n, int32_t* d_codes, int64_t* d_reps, int64_t* h_groups,
+                    void* d_ws, size_t ws_bytes, tqpk_stream stream);
+
+/* Row gather of fixed-width rows (a 2-D [N, w] column): dst[j] = src[idx[j]],
+ * row_bytes bytes each (hashjoin.py:153-175 and aggregate.py:323-325 for
+ * string columns).  Indices outside [0, n_src) give zero rows.               */
+int tqpk_gather_rows(const void* d_src, int64_t n_src, int64_t row_bytes, const int64_t* d_idx, int64_t n_idx,
+                     void* d_dst, tqpk_stream stream);
 
 #ifdef __cplusplus
 }

@@ -151,6 +151,11 @@ def eval_filter(tree, cols: Dict[int, np.ndarray], rows: int | None = None, subq
             return ~eval_filter(tree[1], cols, rows, subquery)
         if tree[0] == "isnotnull":
             return np.ones(rows, dtype=bool)
+        if tree[0] == "substring":                                 # :71-76: a column slice [:, l-1:l-1+w]
+            assert len(tree[1]) == 3
+            sub, l, w = tree[1]
+            l, w = int(l) - 1, int(w)
+            return eval_filter(sub, cols, rows, subquery)[:, l:l + w]
         if tree[0] == "cast":
             literal, _, cast_type = tree[1][0].split(" ")
             if cast_type == "double":
@@ -195,7 +200,7 @@ def eval_filter(tree, cols: Dict[int, np.ndarray], rows: int | None = None, subq
             return _torch_compare(op, L, ord(R))
         if L.ndim != 2:
             raise NotImplementedError("multi-character literal against a one-dimensional column")
-        return _cmp(op, L, _str_bytes(R, L.shape[-1])).all(axis=1)
+        return (L == _str_bytes(R, L.shape[-1])).all(axis=1)       # equality whatever the operator
     if op == "=" and L.dtype == np.float64:                        # :160-161
         if not isinstance(R, float):
             raise TypeError("isclose against a non-float literal (the reference raises here too)")
@@ -370,8 +375,50 @@ def _promote(a, b):
     return max(ints, key=order.index)
 
 
-def eval_agg_expr(tree, cols: Dict[int, np.ndarray]):
-    """Row-wise expression part of aggregate.py:58-233 (arithmetic only)."""
+_YEAR_RANGE = np.arange(1990, 2000, dtype=np.int64)                            # conversion.py:14
+_YEAR_EDGES = np.cumsum([365 if y % 4 else 366 for y in range(1990, 2000)])     # conversion.py:15
+_AGG_CALLS = ("sum", "avg", "count", "min", "max")
+
+
+def _where(mask, a, b):
+    """torch.where(mask, a, b) with torch's promotion of arrays and Python scalars
+    (aggregate.py:87).  A float literal with integers (or two float literals) is
+    float32 in torch and is rejected, as it is by the product."""
+    arrs = [x for x in (a, b) if isinstance(x, np.ndarray)]
+    pys = [x for x in (a, b) if not isinstance(x, np.ndarray)]
+    if any(x.dtype.kind == "f" for x in arrs):
+        dt = np.float64
+    elif any(isinstance(x, float) for x in pys):
+        raise NotImplementedError("CASE mixing a float literal with integers is float32 in torch")
+    elif not arrs:
+        dt = np.int64
+    else:
+        order = [np.bool_, np.int8, np.uint8, np.int16, np.int32, np.int64]
+        kinds = [x.dtype.type for x in arrs]
+        if len(kinds) == 2 and {kinds[0], kinds[1]} == {np.int8, np.uint8}:
+            raise NotImplementedError("uint8 with int8 promotes to int16 in torch")
+        dt = max(kinds, key=order.index)
+        if dt == np.bool_ and pys:
+            dt = np.int64
+    return np.where(mask, a, b).astype(dt)
+
+
+def _agg_compare(op: str, L, R):
+    """ops[op](L, R) of aggregate.py:224-233 for arrays and Python numbers."""
+    if isinstance(L, np.ndarray) and isinstance(R, np.ndarray):
+        return _cmp(op, L, R)
+    if isinstance(L, np.ndarray):
+        return _torch_compare(op, L, R)
+    if isinstance(R, np.ndarray):
+        flip = {"<": ">", "<=": ">=", ">": "<", ">=": "<=", "=": "=", "<>": "<>"}[op]
+        return _torch_compare(flip, R, L)
+    return _cmp(op, L, R)
+
+
+def eval_agg_expr(tree, cols: Dict[int, np.ndarray], ctx=None):
+    """evaluate() of aggregate.py:58-233.  Row-wise expressions give arrays over the
+    rows; an aggregate call (only with ctx = (inverse, G, n)) gives an array over
+    the groups, so arithmetic around calls is per-group (:197-233)."""
     if isinstance(tree, str):                                      # :59-67
         if tree.isdigit():
             return int(tree)
@@ -380,17 +427,60 @@ def eval_agg_expr(tree, cols: Dict[int, np.ndarray]):
         if "#" in tree and tree.split("#")[-1].replace("L", "").isdigit():
             return cols[get_id(tree)]
         return tree
-    if len(tree) == 1:
-        return eval_agg_expr(tree[0], cols)
-    if len(tree) == 3 and tree[1] == "#":
-        return eval_agg_expr(tree[0], cols)
+    if len(tree) == 1:                                             # :69-70
+        return eval_agg_expr(tree[0], cols, ctx)
+    if len(tree) == 3 and tree[1] == "#":                          # :72-74
+        return eval_agg_expr(tree[0], cols, ctx)
+    if len(tree) == 8:                                             # :76-87 CASE WHEN c THEN a ELSE b END
+        assert tree[0] == "CASE" and tree[1] == "WHEN" and tree[3] == "THEN" and tree[5] == "ELSE" and tree[7] == "END"
+        mask = eval_agg_expr(tree[2], cols, ctx)
+        return _where(mask, eval_agg_expr(tree[4], cols, ctx), eval_agg_expr(tree[6], cols, ctx))
+    if len(tree) == 2:
+        head = tree[0]
+        if head == "StartsWith":                                   # :89-99
+            t = cols[get_id(tree[1][0])]
+            name = tree[1][1]
+            assert t.shape[-1] >= len(name)
+            return (t[:, :len(name)] == _str_bytes(name, len(name))).all(axis=1)
+        if head == "year":                                         # :100-101
+            R = eval_agg_expr(tree[1], cols, ctx)
+            idx = np.searchsorted(_YEAR_EDGES, R, side="right")
+            if np.any(idx >= _YEAR_RANGE.size):
+                raise IndexError("year() of a day past the reference's 1990-1999 table")
+            return _YEAR_RANGE[idx]
+        if head == "NOT":                                          # :103-104
+            return ~eval_agg_expr(tree[1], cols, ctx)
+        if head == "cast":                                         # :106-113
+            literal, _, cast_type = tree[1][0].split(" ")
+            if cast_type == "double":
+                return eval_agg_expr(literal, cols, ctx)
+            raise ValueError(f"Unsupported cast type: {cast_type}")
+        if head == "substring":
+            raise NotImplementedError("substring is not on the oracle's path")
+        if head not in _AGG_CALLS:                                 # :122-123
+            raise ValueError(f"Unsupported aggregation function: {head}")
+        if ctx is None:
+            raise ValueError("aggregate call outside an aggregation")
+        inverse, G, n = ctx
+        return reduce_groups(head, eval_agg_expr(tree[1], cols, ctx), inverse, G, n)
     op = tree[-2]
-    if op == "AS":
-        return eval_agg_expr(tree[0], cols)
-    if op not in "+-*/":
-        raise NotImplementedError(f"aggregate expression operation {op!r}")
-    L = eval_agg_expr(tree[0], cols)
-    R = eval_agg_expr(tree[-1], cols)
+    if op == "AS":                                                 # :199-200
+        return eval_agg_expr(tree[0], cols, ctx)
+    if op not in ("+", "-", "*", "/", "<=", ">=", "<", ">", "=", "<>", "AND", "OR"):
+        raise ValueError(f"Unsupported Operation: {op}")
+    L = eval_agg_expr(tree[0], cols, ctx)
+    R = eval_agg_expr(tree[-1], cols, ctx)
+    if isinstance(R, str):                                         # :224-231
+        if isinstance(L, int):
+            assert op == "-"
+            return "".join(tree)
+        if len(R) == 1:
+            return _agg_compare(op, L, ord(R))
+        return (L == _str_bytes(R, L.shape[-1])).all(axis=1)
+    if op in ("AND", "OR"):
+        return (np.logical_and if op == "AND" else np.logical_or)(L, R)
+    if op not in ("+", "-", "*", "/"):
+        return _agg_compare(op, L, R)
     if op == "/":
         t = np.float64 if _promote(L, R) == np.float64 else None
         if t is None:
@@ -448,13 +538,13 @@ def reduce_groups(fn: str, v, inverse: np.ndarray, G: int, n: int) -> np.ndarray
             with np.errstate(all="ignore"):
                 return s / _sum_2steps(inverse, np.ones(n), G, S)
         return np.round(s).astype(np.int64) if (is_int or fn == "count") else s
-    if fn == "min":                                                 # :154-160
-        init = np.iinfo(np.int64).max if is_int else np.finfo(np.float64).max
-        out = np.full(G, init, dtype=np.int64 if is_int else np.float64)
+    if fn == "min":                                                 # :154-160 (the value's own dtype)
+        init = np.iinfo(v.dtype).max if is_int else np.finfo(v.dtype).max
+        out = np.full(G, init, dtype=v.dtype)
         np.minimum.at(out, inverse, v)
         return out
     if fn == "max":                                                 # :161-167 (initial value 0)
-        out = np.zeros(G, dtype=np.int64 if is_int else np.float64)
+        out = np.zeros(G, dtype=v.dtype)
         np.maximum.at(out, inverse, v)
         return out
     if fn == "avg":                                                 # :168-177
@@ -534,8 +624,7 @@ def tqp_hash_aggregate(cols: Dict[int, np.ndarray], args: dict):
             uk = ukeys[key_ids.index(kid)]
             out[oid] = uk.reshape(G, uk.shape[1] if uk.ndim == 2 else 1).astype(m[kid].dtype)
         else:
-            fn, arg = _agg_fn_and_arg(tree)
-            out[oid] = reduce_groups(fn, eval_agg_expr(arg, m), inverse, G, n)
+            out[oid] = eval_agg_expr(tree, m, (inverse, G, n))     # :276-281: evaluate(tree)
     return out
 
 

@@ -312,6 +312,41 @@ def filter_strings(ref):
     _save("filter_strings", {str(k): v for k, v in cols.items()}, {"trees": trees, "types": types_}, outs)
 
 
+@case
+def filter_substring(ref):
+    """substring(col, start, width) in filters (filter.py:71-76): IN over a 2-byte prefix (the
+    customer phone country code), = on a leading slice, a slice clipped at the row's end, and a
+    multi-character literal under '>' (the reference compares for equality whatever the
+    operator, filter.py:151-158)."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(37)
+    n = 5003
+    phone = np.zeros((n, 15), np.int8)
+    for i in range(n):
+        s = f"{rng.integers(10, 35)}-{rng.integers(100, 1000)}-{rng.integers(100, 1000)}-{rng.integers(1000, 10000)}"
+        phone[i, :len(s)] = np.frombuffer(s.encode(), np.uint8).astype(np.int8)
+    nation = _strings(rng, ["CANADA", "BRAZIL", "PERU", "CHINA"], n, 25)
+    cols = {1: phone, 2: nation, 3: rng.normal(4000.0, 3000.0, n)}
+    types_ = {1: "string", 2: "string", 3: "float"}
+    trees = [
+        [["substring", ["p#1", "1", "2"]], "IN", ["13", "31", "23", "29", "30", "18", "17"]],
+        [[["isnotnull", ["b#3"]], "AND", [["substring", ["p#1", "1", "2"]], "IN", ["13", "31", "23", "29", "30"]]],
+         "AND", ["b#3", ">", "0.0"]],
+        [["substring", ["n#2", "1", "3"]], "=", "CAN"],
+        [["substring", ["p#1", "14", "5"]], "IN", ["12", "34", "56"]],
+        ["n#2", ">", "CANADA"],
+        ["NOT", [[["substring", ["n#2", "2", "3"]], "=", "ERU"]]],
+    ]
+    outs = {}
+    for i, tree in enumerate(trees):
+        used = sorted({int(s.split("#")[1]) for s in _leaves(tree) if "#" in s})
+        tg = _tg(V.Variable, {c: cols[c] for c in used}, types_)
+        fa = {"name": "Filter", "filter tree": [tree], "materialized in": used, "out mask id": 999}
+        f.tqp_filter(False, tg, fa, None, None, _Pool(), "f")
+        outs[f"mask{i}"] = tg[999].tensor.numpy().astype(np.bool_)
+    _save("filter_substring", {str(k): v for k, v in cols.items()}, {"trees": trees, "types": types_}, outs)
+
+
 def _leaves(t):
     if isinstance(t, str):
         yield t
@@ -461,6 +496,141 @@ def aggregate_ops(ref):
         outs[str(c)] = tg2[c].tensor.numpy()
     _save("aggregate_ops", {str(k): v for k, v in cols.items()},
           {"aggregate": aargs, "global": gargs, "types": types_}, outs)
+
+
+def _strings(rng, words, n, w):
+    """An int8 [n, w] string column of the given words (conversion.py:36-37 layout)."""
+    pick = rng.integers(0, len(words), n)
+    out = np.zeros((n, w), np.int8)
+    for i, wd in enumerate(words):
+        b = np.frombuffer(wd.encode(), np.uint8).astype(np.int8)
+        out[pick == i, :len(b)] = b
+    return out
+
+
+@case
+def aggregate_expressions(ref):
+    """tqp_project (year(), CASE WHEN over a string condition, arithmetic, a comparison as a
+    value) feeding tqp_hash_aggregate with CASE WHEN conditions (string equality with the
+    split '1-URGENT' literal, OR/AND/NOT, StartsWith, numeric comparisons without the
+    filter's eps), year(), and arithmetic over aggregates (100 * sum / sum, sum / sum)."""
+    f, hj, ag, so, V = ref
+    from operators import project as pj
+    rng = np.random.default_rng(23)
+    n = 20000
+    cols = {
+        1: rng.integers(1, 51, n).astype(np.float64),
+        2: rng.integers(90000, 10495001, n).astype(np.float64) / 100.0,
+        3: rng.integers(0, 11, n).astype(np.float64) / 100.0,
+        6: _strings(rng, ["1-URGENT", "2-HIGH", "3-MEDIUM", "4-NOT SPECIFIED", "5-LOW"], n, 15),
+        7: rng.integers(0, 3652, n).astype(np.int32),
+        8: _strings(rng, ["PROMO BRUSHED COPPER", "STANDARD POLISHED TIN", "PROMO ANODIZED STEEL",
+                          "ECONOMY BURNISHED NICKEL", "MEDIUM PLATED BRASS"], n, 25),
+        9: _strings(rng, ["BRAZIL", "CANADA", "PERU", "ARGENTINA", "BRAZILIA"], n, 25),
+        10: rng.integers(0, 3, n).astype(np.uint8),
+    }
+    types_ = {1: "float", 2: "float", 3: "float", 6: "string", 7: "date", 8: "string", 9: "string", 10: "int"}
+    tg = _tg(V.Variable, cols, types_)
+    pargs = {"name": "Project", "rename map": {}, "materialized in": [1, 2, 3, 7, 9],
+             "used expr": [[["year", ["ship_date#7"]], "AS", "y#20"],
+                           [["CASE", "WHEN", ["nation#9", "=", "BRAZIL"], "THEN", "price#2", "ELSE", "0.0", "END"],
+                            "AS", "v#21"],
+                           [[["price#2", "*", ["1.0", "-", "discount#3"]]], "AS", "w#22"],
+                           [["quantity#1", "<", "10"], "AS", "b#23"]],
+             "materialized out": [20, 21, 22, 23]}
+    pj.tqp_project(False, tg, copy.deepcopy(pargs), None, _Pool(), "p")
+    proj = {str(c): tg[c].tensor.numpy().copy() for c in (20, 21, 22, 23)}
+    disc_price = [["price#2", "*", ["1.0", "-", "discount#3"]]]
+    urgent = [[["prio#6", "=", ["1", "-", "URGENT"]]], "OR", [["prio#6", "=", ["2", "-", "HIGH"]]]]
+    not_urgent = [["NOT", [["prio#6", "=", ["1", "-", "URGENT"]]]], "AND", ["NOT", [["prio#6", "=", ["2", "-", "HIGH"]]]]]
+    results = [
+        "flag#10", "y#20",
+        [[["sum", ["CASE", "WHEN", urgent, "THEN", "1", "ELSE", "0", "END"]], "#", "301L"], "AS", "high#401L"],
+        [[["sum", ["CASE", "WHEN", not_urgent, "THEN", "1", "ELSE", "0", "END"]], "#", "302L"], "AS", "low#402L"],
+        [[["100.0", "*", [["sum", ["CASE", "WHEN", ["StartsWith", ["p_type#8", "PROMO"]], "THEN", disc_price,
+                                   "ELSE", "0.0", "END"]], "#", "303"]], "/", [["sum", disc_price], "#", "304"]],
+         "AS", "promo#403"],
+        [[[["sum", ["CASE", "WHEN", ["nation#9", "=", "BRAZIL"], "THEN", "price#2", "ELSE", "0.0", "END"]], "#", "305"],
+          "/", [["sum", "price#2"], "#", "306"]], "AS", "share#404"],
+        [[["sum", ["CASE", "WHEN", ["quantity#1", "<", "10"], "THEN", "price#2", "ELSE", "0.0", "END"]], "#", "307"],
+         "AS", "small#405"],
+        [[["avg", ["CASE", "WHEN", ["discount#3", ">=", "0.05"], "THEN", "quantity#1", "ELSE", "0.0", "END"]], "#",
+          "308"], "AS", "avgq#406"],
+        [[["max", ["CASE", "WHEN", ["quantity#1", "<>", "25.0"], "THEN", "ship_date#7", "ELSE", "0", "END"]], "#",
+          "309"], "AS", "mx#407"],
+        [[["min", [["year", ["ship_date#7"]]]], "#", "310"], "AS", "miny#408"],
+        [[["count", ["CASE", "WHEN", ["price#2", ">", "50000.5"], "THEN", "quantity#1", "ELSE", "-64.0", "END"]],
+          "#", "311L"], "AS", "cnt#409L"],
+        [[["sum", [["year", ["ship_date#7"]]]], "#", "312L"], "AS", "sumy#410L"],
+    ]
+    aargs = {"name": "Aggregate", "is partial": False, "keys": ["flag#10", "y#20"],
+             "input ids": [1, 2, 3, 6, 7, 8, 9, 10, 20], "results": results,
+             "out agg ids": [401, 402, 403, 404, 405, 406, 407, 408, 409, 410]}
+    torch.manual_seed(5)
+    ag.tqp_hash_aggregate(False, tg, copy.deepcopy(aargs), _Pool(), None, "a")
+    outs = {str(c): tg[c].tensor.numpy() for c in [10, 20] + aargs["out agg ids"]}
+    outs.update({f"p{k}": v for k, v in proj.items()})
+    _save("aggregate_expressions", {str(k): v for k, v in cols.items()},
+          {"project": pargs, "aggregate": aargs, "types": types_}, outs)
+
+
+@case
+def aggregate_string_keys(ref):
+    """Group keys the reference stacks as 2-D (aggregate.py:291-311): a string key alone, five
+    keys mixing int, string, float and uint8 (more than four), and a float key with -0.0 and
+    +0.0 rows; under a late-materialisation mask."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(41)
+    n = 30011
+    cust = rng.integers(0, 60, n).astype(np.int64)
+    phone = np.zeros((n, 15), np.int8)
+    for c in range(60):
+        s_ = f"{10 + c % 25}-{100 + c}-{200 + 3 * c}-{1000 + 7 * c}"
+        phone[cust == c, :len(s_)] = np.frombuffer(s_.encode(), np.uint8).astype(np.int8)
+    acct = (cust - 10).astype(np.float64) * 1.5
+    acct[rng.integers(0, n, 500)] = -0.0
+    cols = {
+        1: _strings(rng, ["MAIL", "SHIP", "AIR", "REG AIR", "TRUCK", "RAIL", "FOB"], n, 10),
+        2: _strings(rng, ["BRAZIL", "CANADA", "PERU", "CHINA"], n, 25),
+        3: cust, 4: acct,
+        5: rng.integers(90000, 10495001, n).astype(np.float64) / 100.0,
+        6: rng.integers(0, 3, n).astype(np.uint8),
+        7: phone,
+        8: rng.integers(0, 2570, n).astype(np.int32),
+    }
+    types_ = {1: "string", 2: "string", 3: "int", 4: "float", 5: "float", 6: "int", 7: "string", 8: "date"}
+    fargs = {"name": "Filter", "filter tree": [["d#8", "<", "2400"]], "materialized in": [8], "out mask id": 900}
+    tg = _tg(V.Variable, cols, types_)
+    f.tqp_filter(False, tg, copy.deepcopy(fargs), None, None, _Pool(), "f")
+    mask = tg[900].tensor.numpy().copy()
+    sets = {
+        "a": {"keys": ["mode#1"], "input ids": [1, 5],
+              "results": ["mode#1", [[["sum", ["p#5"]], "#", "11"], "AS", "s#111"],
+                          [[["count", ["1"]], "#", "12L"], "AS", "c#112L"], [[["min", ["p#5"]], "#", "13"], "AS", "m#113"]],
+              "out agg ids": [111, 112, 113]},
+        "b": {"keys": ["ck#3", "nat#2", "bal#4", "ph#7", "fl#6"], "input ids": [2, 3, 4, 5, 6, 7],
+              "results": ["ck#3", "nat#2", "bal#4", "ph#7", "fl#6", [[["sum", ["p#5"]], "#", "21"], "AS", "s#121"],
+                          [[["avg", ["p#5"]], "#", "22"], "AS", "a#122"]],
+              "out agg ids": [121, 122]},
+        "c": {"keys": ["bal#4"], "input ids": [4, 5],
+              "results": ["bal#4", [[["count", ["1"]], "#", "31L"], "AS", "c#131L"],
+                          [[["max", ["p#5"]], "#", "32"], "AS", "x#132"]],
+              "out agg ids": [131, 132]},
+    }
+    outs = {"mask": mask}
+    for name, a_ in sets.items():
+        aargs = dict(a_, **{"name": "Aggregate", "is partial": False,
+                            "mask map": {c: 900 for c in a_["input ids"]}})
+        tgi = _tg(V.Variable, cols, types_)
+        tgi[900] = tg[900]
+        torch.manual_seed(7)
+        ag.tqp_hash_aggregate(False, tgi, copy.deepcopy(aargs), _Pool(), None, "a")
+        key_ids = [int(k.split("#")[-1]) for k in a_["keys"]]
+        for c in key_ids + a_["out agg ids"]:
+            outs[f"{name}_{c}"] = tgi[c].tensor.numpy()
+        sets[name] = _jsonable(aargs)
+    _save("aggregate_string_keys", {str(k): v for k, v in cols.items()},
+          {"filter": fargs, "sets": sets, "types": types_}, outs)
 
 
 @case

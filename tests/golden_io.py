@@ -32,3 +32,14 @@ def assert_f64_close(a, b, rel=1e-12, magnitude=None):
 def rows_sorted(*cols):
     m = np.stack([np.asarray(c).reshape(-1).astype(np.float64) for c in cols], 1)
     return m[np.lexsort(m.T[::-1])] if m.size else m
+
+
+def key_tuple_order(keys):
+    """Row order of groups by key tuple ascending: each key compared by value, a 2-D
+    (string) key byte column by byte column, the first key most significant."""
+    cols = []
+    for k in keys:
+        k = np.asarray(k)
+        k2 = k.reshape(k.shape[0], -1)
+        cols.extend(k2[:, j] for j in range(k2.shape[1]))
+    return np.lexsort(cols[::-1])

@@ -118,3 +118,34 @@ def test_projection_kernel_compiles():
     src, _ = jit.project_source(prog.spec, [(r, code_of(dt)) for r, dt in prog.outputs])
     ok, log = jit.check_compiles(src)
     assert ok, log[:2000]
+
+
+def test_expression_forms_compile_case_year_and_post_arithmetic():
+    """CASE WHEN / conditions / year() / arithmetic over aggregates compile (the golden
+    aggregate_expressions trees): conditions become bool mask columns, calls inside a
+    result expression become hidden outputs, the generated kernels compile."""
+    import json
+    from pathlib import Path
+    from tqpk.expr import compile_projection
+    z = np.load(Path(__file__).parent / "golden" / "aggregate_expressions.npz")
+    args = json.loads(str(z["args"]))
+    cols = {int(k[3:]): torch.from_numpy(z[k]) for k in z.files if k.startswith("in_")}
+    pp = compile_projection(args["project"]["used expr"], cols, derived=True)
+    assert [dt for _, dt in pp.outputs] == [torch.int64, torch.float64, torch.float64, torch.bool]
+    assert len(pp.masks) == 2
+    src, name = jit.project_source(pp.spec, [(r, L.I64 if dt != torch.float64 else L.F64) for r, dt in pp.outputs])
+    ok, log = jit.check_compiles(src)
+    assert ok, log[:2000]
+    cols[20] = torch.from_numpy(z["out_p20"])
+    prog = compile_aggregate(args["aggregate"], cols, derived=True)
+    assert [(o, dt) for o, _, dt in prog.post] == [(403, torch.float64), (404, torch.float64)]
+    assert len({o[0] for o in prog.outputs}) == len(prog.outputs)
+    plan = L.GbPlan()
+    plan.mode, plan.threads, plan.slots = L.GB_DENSE_SHARED, 256, 30
+    plan.key_stride[0], plan.key_stride[1] = 10, 1
+    src, name, T, smem = jit.groupby_source(prog.spec, None, plan)
+    assert "tqpk_year(" in src and " ? " in src
+    ok, log = jit.check_compiles(src)
+    assert ok, log[:2000]
+    with pytest.raises(NotImplementedError):          # fused pipelines keep to plain calls
+        compile_aggregate(args["aggregate"], cols)

@@ -61,6 +61,19 @@ def test_filter_strings_golden():
         np.testing.assert_array_equal(np_(tg[999].tensor), outs[f"mask{i}"], err_msg=str(tree))
 
 
+def test_filter_substring_golden():
+    """substring(col, start, width) views: IN over a prefix, = on a slice, a slice clipped at
+    the row's end, NOT; a multi-character literal under '>' compares for equality."""
+    from tqpk.operators import tqp_filter
+    ins, outs, args = load("filter_substring")
+    for i, tree in enumerate(args["trees"]):
+        used = sorted({int(s.split("#")[1]) for s in _leaves(tree) if "#" in s})
+        tg = {c: V(ins[c], args["types"][str(c)]) for c in used}
+        tqp_filter(True, tg, {"filter tree": [tree], "materialized in": used, "out mask id": 999},
+                   None, None, None, "f")
+        np.testing.assert_array_equal(np_(tg[999].tensor), outs[f"mask{i}"], err_msg=str(tree))
+
+
 @pytest.mark.parametrize("n", [1, 4097, 500_001])
 def test_string_predicates_in_group_by_and_join_build(n):
     """String filters fused into the group-by (library evaluator) and the join build side."""
@@ -300,6 +313,116 @@ def test_aggregate_ops_golden():
         assert_f64_close(o, g) if g.dtype == np.float64 else np.testing.assert_array_equal(o, g)
 
 
+def test_aggregate_expressions_golden():
+    """tqp_project (year, CASE over a string condition, a comparison as a value) then
+    tqp_hash_aggregate with CASE conditions, year() and arithmetic over aggregates."""
+    from tqpk.operators import tqp_hash_aggregate, tqp_project
+    ins, outs, args = load("aggregate_expressions")
+    tg = tg_from(ins, args["types"])
+    tqp_project(True, tg, copy.deepcopy(args["project"]), None, None, "p")
+    for c in args["project"]["materialized out"]:
+        o, g = np_(tg[c].tensor), outs[f"p{c}"]
+        assert o.dtype == g.dtype, (c, o.dtype, g.dtype)
+        np.testing.assert_array_equal(o, g)
+    tqp_hash_aggregate(True, tg, copy.deepcopy(args["aggregate"]), None, None, "a")
+    order = np.lexsort([outs["20"].reshape(-1), outs["10"].reshape(-1)])
+    np.testing.assert_array_equal(np_(tg[10].tensor), outs["10"][order])
+    np.testing.assert_array_equal(np_(tg[20].tensor), outs["20"][order])
+    for i in args["aggregate"]["out agg ids"]:
+        g, o = outs[str(i)][order], np_(tg[i].tensor)
+        assert o.dtype == g.dtype, (i, o.dtype, g.dtype)
+        assert_f64_close(o, g) if g.dtype == np.float64 else np.testing.assert_array_equal(o, g)
+
+
+def test_case_conditions_vs_oracle_at_size():
+    """CASE WHEN at 3M rows (generated accumulation kernel, shared-table mode) against the oracle."""
+    from tqpk.operators import tqp_hash_aggregate
+    rng = np.random.default_rng(31)
+    n = 3_000_000
+    cols = {1: rng.integers(1, 51, n).astype(np.float64), 2: rng.integers(90000, 10495001, n) / 100.0,
+            3: rng.integers(0, 11, n) / 100.0, 4: rng.integers(0, 3652, n).astype(np.int32),
+            5: rng.integers(0, 700, n).astype(np.int32)}
+    res = ["k#5",
+           [[["sum", ["CASE", "WHEN", [["q#1", "<", "24"], "AND", ["d#3", ">=", "0.05"]], "THEN",
+                      [["p#2", "*", ["1.0", "-", "d#3"]]], "ELSE", "0.0", "END"]], "#", "1"], "AS", "a#11"],
+           [[["sum", ["CASE", "WHEN", ["NOT", ["q#1", "=", "1"]], "THEN", "1", "ELSE", "0", "END"]], "#", "2L"], "AS",
+            "b#12L"],
+           [[[["sum", ["CASE", "WHEN", ["y#4", ">", "1000"], "THEN", "p#2", "ELSE", "0.0", "END"]], "#", "3"], "/",
+             [["sum", "p#2"], "#", "4"]], "AS", "c#13"],
+           [[["max", [["year", ["y#4"]]]], "#", "5"], "AS", "d#14"]]
+    args = {"is partial": False, "keys": ["k#5"], "input ids": [1, 2, 3, 4, 5], "results": res,
+            "out agg ids": [11, 12, 13, 14]}
+    tg = {1: V(cols[1], "float"), 2: V(cols[2], "float"), 3: V(cols[3], "float"), 4: V(cols[4], "date"), 5: V(cols[5])}
+    tqp_hash_aggregate(True, tg, copy.deepcopy(args), None, None, "a")
+    ref = O.tqp_hash_aggregate(cols, copy.deepcopy(args))
+    np.testing.assert_array_equal(np_(tg[5].tensor), ref[5])
+    for i in (11, 13):
+        assert_f64_close(np_(tg[i].tensor), ref[i])
+    for i in (12, 14):
+        np.testing.assert_array_equal(np_(tg[i].tensor), ref[i])
+
+
+def test_aggregate_string_keys_golden():
+    """String (2-D) keys, five mixed keys (int, string, float, uint8), a float key with -0.0
+    and +0.0 rows, under a late-materialisation mask: numbered by the key-encoding pass,
+    grouped by code, key outputs gathered as [G, w] / [G, 1]."""
+    from golden_io import key_tuple_order
+    from tqpk.operators import tqp_filter, tqp_hash_aggregate
+    ins, outs, args = load("aggregate_string_keys")
+    for name, a in args["sets"].items():
+        tg = tg_from(ins, args["types"])
+        tqp_filter(True, tg, copy.deepcopy(args["filter"]), None, None, None, "f")
+        a = copy.deepcopy(a)
+        a["mask map"] = {int(k): v for k, v in a["mask map"].items()}
+        tqp_hash_aggregate(True, tg, a, None, None, "a")
+        kids = [O.get_id(k) for k in a["keys"]]
+        order = key_tuple_order([outs[f"{name}_{k}"] for k in kids])
+        for k in kids:
+            g, o = outs[f"{name}_{k}"][order], np_(tg[k].tensor)
+            assert o.dtype == g.dtype and o.shape == g.shape, (name, k, o.dtype, o.shape, g.shape)
+            np.testing.assert_array_equal(o, g)
+        for i in a["out agg ids"]:
+            g, o = outs[f"{name}_{i}"][order], np_(tg[i].tensor)
+            assert o.dtype == g.dtype, (name, i)
+            assert_f64_close(o, g) if g.dtype == np.float64 else np.testing.assert_array_equal(o, g)
+
+
+@pytest.mark.parametrize("n", [1, 1000, 2_000_003])
+def test_key_encode_vs_oracle_at_size(n):
+    """Key encoding at size: a 10-byte string key and an int key, ~n/3 groups at the top size."""
+    from tqpk.ops import encode_keys
+    rng = np.random.default_rng(n)
+    s = rng.integers(65, 70, (n, 10)).astype(np.int8)
+    s[:, 6:] = 0
+    k = rng.integers(0, max(1, n // 1000), n).astype(np.int32)
+    codes, reps, G = encode_keys([torch.from_numpy(s).cuda(), torch.from_numpy(k).cuda()])
+    ukeys, inverse = O.group_rows([s, k])
+    assert G == ukeys[0].shape[0]
+    np.testing.assert_array_equal(np_(codes), inverse)
+    r = np_(reps)
+    np.testing.assert_array_equal(s[r], ukeys[0])
+    np.testing.assert_array_equal(k[r], ukeys[1].reshape(-1))
+
+
+def test_join_gathers_string_payloads():
+    """join_vortex materialises a 2-D string column of each side (row gather)."""
+    from tqpk.operators import join_vortex
+    from tqpk.variable import Variable
+    rng = np.random.default_rng(3)
+    nb, npr = 5000, 40_000
+    bk = rng.permutation(nb).astype(np.int64)
+    bs = rng.integers(65, 91, (nb, 25)).astype(np.int8)
+    pk = rng.integers(0, nb + 500, npr).astype(np.int64)
+    ps = rng.integers(65, 91, (npr, 15)).astype(np.int8)
+    tg = {1: V(bk), 2: Variable(torch.from_numpy(bs).cuda(), "string"), 3: V(pk),
+          4: Variable(torch.from_numpy(ps).cuda(), "string")}
+    join_vortex(True, tg, {"left group": [1, 2], "right group": [3, 4], "materialized in": [1, 2, 3, 4]},
+                1, 3, [], "inner", None, None, "j")
+    bi, pi = O.join_indices(bk, pk, "inner")
+    np.testing.assert_array_equal(np_(tg[2].tensor), bs[bi])
+    np.testing.assert_array_equal(np_(tg[4].tensor), ps[pi])
+
+
 def test_aggregate_two_step_golden():
     from tqpk.operators import tqp_hash_aggregate
     ins, outs, args = load("aggregate_two_step")
@@ -389,8 +512,8 @@ def test_cpu_tensors_and_unsupported_shapes_raise():
     with pytest.raises(ValueError):
         argsort_stable(torch.zeros(10, dtype=torch.int32))
     tg = {1: V(np.zeros(10, np.int8).reshape(5, 2))}
-    with pytest.raises(NotImplementedError):
-        tqp_filter(True, tg, {"filter tree": [[["substring", ["s#1", "1", "2"]], "=", "AB"]], "materialized in": [1],
+    with pytest.raises(NotImplementedError):       # a numeric literal against a string slice
+        tqp_filter(True, tg, {"filter tree": [[["substring", ["s#1", "1", "2"]], "=", "12"]], "materialized in": [1],
                               "out mask id": 2}, None, None, None, "f")
     with pytest.raises(NotImplementedError):
         tqp_filter(False, tg, {"filter tree": [["s#1", "=", "A"]], "materialized in": [1], "out mask id": 2},

@@ -45,6 +45,13 @@ def test_filter_strings():
         np.testing.assert_array_equal(got.reshape(-1), outs[f"mask{i}"], err_msg=str(tree))
 
 
+def test_filter_substring():
+    ins, outs, args = load("filter_substring")
+    for i, tree in enumerate(args["trees"]):
+        got = O.eval_filter([tree], ins)
+        np.testing.assert_array_equal(got.reshape(-1), outs[f"mask{i}"], err_msg=str(tree))
+
+
 def test_filter_agg_sort_lineitem():
     ins, outs, args = load("filter_agg_sort_lineitem")
     mask = O.eval_filter(args["filter"]["filter tree"], {7: ins[7]})
@@ -131,6 +138,51 @@ def test_aggregate_two_step():
     for i, g in zip(ids, vals):
         assert agg[i].dtype == g.dtype
         assert_f64_close(agg[i], g) if g.dtype == np.float64 else np.testing.assert_array_equal(agg[i], g)
+
+
+def test_aggregate_expressions():
+    """CASE WHEN / conditions / year() / arithmetic over aggregates, after a projection."""
+    ins, outs, args = load("aggregate_expressions")
+    proj = O.tqp_project(dict(ins), args["project"])
+    for c in args["project"]["materialized out"]:
+        g = outs[f"p{c}"]
+        assert proj[c].dtype == g.dtype, c
+        np.testing.assert_array_equal(proj[c], g)
+    agg = O.tqp_hash_aggregate(proj, args["aggregate"])
+    ids = args["aggregate"]["out agg ids"]
+    keys_g, vals_g = _by_key([outs["10"], outs["20"]], *[outs[str(i)] for i in ids])
+    np.testing.assert_array_equal(agg[10].reshape(-1), keys_g[0])
+    np.testing.assert_array_equal(agg[20].reshape(-1), keys_g[1])
+    for i, g in zip(ids, vals_g):
+        assert agg[i].dtype == g.dtype, i
+        assert_f64_close(agg[i], g) if g.dtype == np.float64 else np.testing.assert_array_equal(agg[i], g)
+
+
+def test_aggregate_string_keys():
+    """String keys, five mixed keys, a float key with -0.0 / +0.0, under a mask."""
+    from golden_io import key_tuple_order
+    ins, outs, args = load("aggregate_string_keys")
+    mask = O.eval_filter(args["filter"]["filter tree"], {8: ins[8]})
+    np.testing.assert_array_equal(mask, outs["mask"])
+    cols = dict(ins)
+    cols[900] = mask
+    for name, a in args["sets"].items():
+        agg = O.tqp_hash_aggregate(cols, a)
+        kids = [O.get_id(k) for k in a["keys"]]
+        order = key_tuple_order([outs[f"{name}_{k}"] for k in kids])
+        for k in kids:
+            g = outs[f"{name}_{k}"][order]
+            assert agg[k].dtype == g.dtype and agg[k].shape == g.shape, (name, k)
+            np.testing.assert_array_equal(agg[k], g)
+        for i in a["out agg ids"]:
+            g = outs[f"{name}_{i}"][order]
+            assert agg[i].dtype == g.dtype, (name, i)
+            assert_f64_close(agg[i], g) if g.dtype == np.float64 else np.testing.assert_array_equal(agg[i], g)
+
+
+def test_oracle_year_past_the_table_raises():
+    with pytest.raises(IndexError):
+        O.eval_agg_expr(["year", ["d#1"]], {1: np.array([3651, 3652], np.int32)})
 
 
 def test_sort_multikey():

@@ -199,10 +199,28 @@ static __device__ __noinline__ uint64_t expr_div(uint64_t a, uint64_t b) {
   return static_cast<uint64_t>(__double_as_longlong(__ddiv_rn(__longlong_as_double(a), __longlong_as_double(b))));
 }
 
-__device__ __forceinline__ uint64_t expr_apply(const tqpk_expr_insn& X, uint64_t a, uint64_t b, const void* const* cols,
-                                              const int* dts, int64_t row) {
+// Year of day d (days since 1990-01-01).  Days before 1990 fall in the first
+// bucket (1990), as torch.bucketize over the year edges puts them.  Otherwise
+// the proleptic Gregorian year, by H. Hinnant's civil_from_days method: days
+// since 0000-03-01 split into 400-year eras of 146097 days, the year of the era
+// from the day of the era, and January/February counted in the next year.
+__host__ __device__ __forceinline__ int64_t expr_year(int64_t d) {
+  if (d < 0) return 1990;
+  const int64_t z = d + 7305 + 719468;           // 1970-01-01 is day 719468 after 0000-03-01
+  const int64_t era = z / 146097;
+  const int64_t doe = z - era * 146097;
+  const int64_t yoe = (doe - doe / 1460 + doe / 36524 - doe / 146096) / 365;
+  const int64_t doy = doe - (365 * yoe + yoe / 4 - yoe / 100);
+  const int64_t mp = (5 * doy + 2) / 153;
+  return yoe + era * 400 + (mp >= 10 ? 1 : 0);
+}
+
+__device__ __forceinline__ uint64_t expr_apply(const tqpk_expr_insn& X, uint64_t a, uint64_t b, uint64_t c,
+                                              const void* const* cols, const int* dts, int64_t row) {
   const bool f = X.type == TQPK_F64;
   switch (X.op) {
+    case TQPK_X_SELECT: return a != 0 ? b : c;
+    case TQPK_X_YEAR: return static_cast<uint64_t>(expr_year(static_cast<int64_t>(a)));
     case TQPK_X_COL:
       return f ? static_cast<uint64_t>(__double_as_longlong(ld_f64(cols[X.col], dts[X.col], row)))
                : static_cast<uint64_t>(ld_int(cols[X.col], dts[X.col], row));
@@ -231,13 +249,14 @@ __device__ __forceinline__ void expr_eval_small(const tqpk_expr_insn* E, int n, 
     r[i] = 0;
     if (i < n) {
       const tqpk_expr_insn& X = E[i];
-      uint64_t a = 0, b = 0;
+      uint64_t a = 0, b = 0, c = 0;
 #pragma unroll
       for (int j = 0; j < i; ++j) {
         a = (X.a == j) ? r[j] : a;
         b = (X.b == j) ? r[j] : b;
+        c = (X.col == j) ? r[j] : c;
       }
-      r[i] = expr_apply(X, a, b, cols, dts, row);
+      r[i] = expr_apply(X, a, b, c, cols, dts, row);
     }
   }
 }
@@ -254,7 +273,8 @@ __device__ __forceinline__ void expr_eval_generic(const tqpk_expr_insn* E, int n
                                                   const int* dts, int64_t row, uint64_t* r) {
   for (int i = 0; i < n; ++i) {
     const tqpk_expr_insn& X = E[i];
-    r[i] = expr_apply(X, (X.op >= TQPK_X_ADD) ? r[X.a] : 0, (X.op >= TQPK_X_ADD && X.op <= TQPK_X_DIV) ? r[X.b] : 0,
+    const bool two = (X.op >= TQPK_X_ADD && X.op <= TQPK_X_DIV) || X.op == TQPK_X_SELECT;
+    r[i] = expr_apply(X, (X.op >= TQPK_X_ADD) ? r[X.a] : 0, two ? r[X.b] : 0, X.op == TQPK_X_SELECT ? r[X.col] : 0,
                       cols, dts, row);
   }
 }
@@ -305,13 +325,14 @@ __device__ __forceinline__ void expr_eval_tile(const tqpk_expr_insn* E, int n, c
           raw = static_cast<uint64_t>(__double_as_longlong(static_cast<double>(static_cast<int64_t>(raw))));
         r[i] = raw;
       } else {
-        uint64_t a = 0, b = 0;
+        uint64_t a = 0, b = 0, c = 0;
 #pragma unroll
         for (int q = 0; q < i; ++q) {
           a = (X.a == q) ? r[q] : a;
           b = (X.b == q) ? r[q] : b;
+          c = (X.col == q) ? r[q] : c;
         }
-        r[i] = expr_apply(X, a, b, nullptr, dts, 0);
+        r[i] = expr_apply(X, a, b, c, nullptr, dts, 0);
       }
     }
   }
@@ -419,12 +440,13 @@ __device__ __forceinline__ bool str_like2(const int8_t* row, int w, const uint8_
 }
 static __device__ uint32_t str_leaf4(const tqpk_predicate& P, const tqpk_pred_insn& I, int64_t r0, int64_t n) {
   const int w = P.widths[I.col];
+  const int64_t stride = P.strides[I.col] > 0 ? P.strides[I.col] : w;
   const int8_t* base = static_cast<const int8_t*>(P.cols[I.col]);
   const uint64_t L = (uint64_t)I.lit_i;
   uint32_t m = 0;
   for (int j = 0; j < 4; ++j) {
     if (r0 + j >= n) break;
-    const int8_t* row = base + (r0 + j) * w;
+    const int8_t* row = base + (r0 + j) * stride;
     bool ok;
     switch (I.op) {
       case TQPK_P_STRCMP: ok = str_all_cmp(row, w, P.strpool + (L & 0xffffffffu), I.cmp); break;

@@ -213,7 +213,7 @@ int check_pred(const tqpk_predicate* p) {
         if (dtype_size(p->dtypes[I.col]) != 1) return TQPK_EDTYPE;
         const int64_t w = p->widths[I.col];
         const uint64_t L = (uint64_t)I.lit_i;
-        if (w <= 0) return TQPK_EINVAL;
+        if (w <= 0 || p->strides[I.col] < 0 || (p->strides[I.col] > 0 && p->strides[I.col] < w)) return TQPK_EINVAL;
         bool ok;
         if (I.op == TQPK_P_STRCMP) {
           ok = (L & 0xffffffffu) + w <= TQPK_MAX_STRPOOL && I.cmp >= TQPK_LT && I.cmp <= TQPK_NE;

@@ -482,7 +482,14 @@ static int check_spec(const tqpk_groupby_spec* S, bool has_rows = true) {
     if (X.op >= TQPK_X_ADD && X.op <= TQPK_X_DIV && (X.a < 0 || X.a >= i || X.b < 0 || X.b >= i)) return TQPK_EINVAL;
     if (X.op == TQPK_X_TOF64 && (X.a < 0 || X.a >= i)) return TQPK_EINVAL;
     if (X.op == TQPK_X_DIV && X.type != TQPK_F64) return TQPK_EUNSUPPORTED;
-    if (X.op < TQPK_X_COL || X.op > TQPK_X_TOF64) return TQPK_EINVAL;
+    if (X.op == TQPK_X_SELECT) {
+      if (X.a < 0 || X.a >= i || X.b < 0 || X.b >= i || X.col < 0 || X.col >= i) return TQPK_EINVAL;
+      if (S->expr[X.a].type != TQPK_I64 || S->expr[X.b].type != X.type || S->expr[X.col].type != X.type)
+        return TQPK_EDTYPE;
+    }
+    if (X.op == TQPK_X_YEAR && (X.a < 0 || X.a >= i || X.type != TQPK_I64 || S->expr[X.a].type != TQPK_I64))
+      return TQPK_EINVAL;
+    if (X.op < TQPK_X_COL || X.op > TQPK_X_YEAR) return TQPK_EINVAL;
   }
   for (int a = 0; a < S->n_accs; ++a) {
     const tqpk_acc& A = S->accs[a];

@@ -23,7 +23,7 @@ P_CMP, P_AND, P_OR, P_NOT, P_TRUE, P_FALSE, P_MASK, P_CMPCOL = 1, 2, 3, 4, 5, 6,
 P_STRCMP, P_PREFIX, P_CONTAINS, P_LIKE2 = 9, 10, 11, 12
 LT, LE, GT, GE, EQ, NE, ISCLOSE = 0, 1, 2, 3, 4, 5, 6
 DOM_I64, DOM_F64, DOM_F32 = 0, 1, 2
-X_COL, X_CONST, X_ADD, X_SUB, X_MUL, X_DIV, X_TOF64 = 1, 2, 3, 4, 5, 6, 7
+X_COL, X_CONST, X_ADD, X_SUB, X_MUL, X_DIV, X_TOF64, X_SELECT, X_YEAR = 1, 2, 3, 4, 5, 6, 7, 8, 9
 ACC_SUM, ACC_COUNT_NOTNULL, ACC_COUNT_ROWS, ACC_MIN, ACC_MAX = 1, 2, 3, 4, 5
 GB_GLOBAL_ONE, GB_DENSE_PRIVATE, GB_DENSE_SHARED, GB_DENSE_GLOBAL, GB_HASH = 0, 1, 2, 3, 4
 OUT_ACC, OUT_AVG = 0, 1
@@ -42,7 +42,8 @@ MAX_STRPOOL = 512
 class Predicate(C.Structure):
     _fields_ = [("n_insn", C.c_int32), ("n_cols", C.c_int32), ("cols", C.c_void_p * MAX_COLS),
                 ("dtypes", C.c_int32 * MAX_COLS), ("insn", PredInsn * MAX_PRED),
-                ("widths", C.c_int32 * MAX_COLS), ("strpool", C.c_uint8 * MAX_STRPOOL)]
+                ("widths", C.c_int32 * MAX_COLS), ("strpool", C.c_uint8 * MAX_STRPOOL),
+                ("strides", C.c_int32 * MAX_COLS)]
 
 
 class ExprInsn(C.Structure):
@@ -99,6 +100,9 @@ SIGNATURES = {
                                   _SZ, _VP]),
     "tqpk_gather": (C.c_int, [_I32, _P(_VP), _P(_I32), _VP, _I64, _I32, _P(_VP), _VP]),
     "tqpk_mark_rows": (C.c_int, [_VP, _I64, _VP, _I64, _VP]),
+    "tqpk_key_encode_workspace_bytes": (_SZ, [_I64]),
+    "tqpk_key_encode": (C.c_int, [_I32, _P(_VP), _P(_I32), _P(_I32), _VP, _I64, _VP, _VP, _P(_I64), _VP, _SZ, _VP]),
+    "tqpk_gather_rows": (C.c_int, [_VP, _I64, _I64, _VP, _I64, _VP, _VP]),
     "tqpk_batch_record_bytes": (_SZ, []),
     "tqpk_batch_join_workspace_bytes": (_SZ, [_I64, _I64]),
     "tqpk_batch_describe_join": (C.c_int, [_VP, _VP, _I32, _I64, _P(Predicate), _I64, _I64, _VP, _I32, _I64,

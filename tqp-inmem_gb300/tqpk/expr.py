@@ -18,6 +18,21 @@ torch.add/sub/mul/div to tensors and Python numbers): float64 wins; integer
 tensors with Python ints stay integer.  An integer tensor combined with a
 Python float, or an integer true division, is float32 in torch; those are
 rejected with NotImplementedError rather than computed differently.
+
+With ``derived=True`` (the operator path) the rest of the reference's
+expression language compiles too:
+
+* a condition (comparisons, AND/OR, NOT, StartsWith, string equality,
+  ``aggregate.py:89-99, 203-233``) becomes a bool column: the condition is a
+  predicate program (aggregate comparison rules, no eps) that the filter
+  kernel evaluates into a 1-byte mask before the accumulation kernel reads it;
+* ``CASE WHEN c THEN x ELSE y END`` (``:76-87``) is a SELECT instruction with
+  torch.where's promotion;
+* ``year(d)`` (``:100-101``) is a YEAR instruction;
+* a result that combines aggregates arithmetically (``sum(a) / sum(b)``,
+  ``100.0 * sum(..) / sum(..)``; ``:197-233`` evaluates each call, then the
+  arithmetic on the per-group tensors) computes its calls as hidden
+  accumulator outputs and the arithmetic as a projection over the groups.
 """
 from __future__ import annotations
 
@@ -32,6 +47,8 @@ from .predicate import get_id, _is_float
 
 _AGG_FNS = ("sum", "avg", "count", "min", "max")
 _INT_ORDER = {torch.bool: 0, torch.uint8: 1, torch.int8: 1, torch.int32: 3, torch.int64: 4}
+_COND_OPS = ("<=", ">=", "<", ">", "=", "<>", "AND", "OR")
+_HIDDEN_ID = 1 << 40          # ids of hidden per-group columns (aggregate calls inside a result expression)
 
 
 def _strip(t):
@@ -64,11 +81,30 @@ class AggregateProgram:
     key_ids: List[int] = field(default_factory=list)        # grouping columns (args['keys'])
     key_outputs: List[Tuple[int, int]] = field(default_factory=list)   # (out id, input key id)
     outputs: List[Tuple[int, int, int, int, torch.dtype]] = field(default_factory=list)  # (out id, op, a, b, dtype)
+    masks: List[Tuple[Any, torch.Tensor]] = field(default_factory=list)   # (condition predicate, its bool column)
+    post: List[Tuple[int, Any, torch.dtype]] = field(default_factory=list)  # (out id, arithmetic over hidden ids, dtype)
+    encoded: bool = False     # the kernel groups by one int32 code column standing for the key tuple
+
+
+def needs_key_codes(args: dict, columns: Dict[int, torch.Tensor]) -> bool:
+    """Key tuples the dense / packed-hash slots cannot take: a 2-D (string) key, a float
+    key, or more than TQPK_MAX_KEYS keys (aggregate.py:291-311 stacks any of these)."""
+    keys = [get_id(k) for k in (args.get("keys") or [])]
+    if len(keys) > L.MAX_KEYS:
+        return True
+    for kid in keys:
+        t = columns[kid]
+        if (t.dim() == 2 and t.shape[1] != 1) or t.dtype not in _INT_ORDER:
+            return True
+    return False
 
 
 class _Builder:
-    def __init__(self, columns: Dict[int, torch.Tensor]):
-        self.columns = columns
+    def __init__(self, columns: Dict[int, torch.Tensor], derived: bool = False):
+        self.columns = dict(columns)
+        self.derived = derived
+        self.masks: List[Tuple[Any, torch.Tensor]] = []
+        self.mask_memo: Dict[str, int] = {}
         self.expr: List[tuple] = []
         self.memo: Dict[tuple, int] = {}
         self.col_slot: Dict[int, int] = {}
@@ -126,13 +162,66 @@ class _Builder:
             return self.value(tree)
         if len(tree) == 3 and tree[1] in ("#", "AS"):
             return self.value(tree[0])
-        if len(tree) == 3 and tree[1] in "+-*/":
+        if len(tree) == 3 and tree[1] in ("+", "-", "*", "/"):
             return self.binary(tree[1], self.value(tree[0]), self.value(tree[2]))
         if len(tree) == 2 and tree[0] == "cast":
             literal, _, cast_type = tree[1][0].split(" ")
             if cast_type == "double":
                 return self.value(literal)
+        if self.derived:
+            if len(tree) == 8 and tree[0] == "CASE":
+                assert tree[1] == "WHEN" and tree[3] == "THEN" and tree[5] == "ELSE" and tree[7] == "END"
+                return self.select(self.value(tree[2]), self.value(tree[4]), self.value(tree[6]))
+            if len(tree) == 2 and tree[0] == "year":
+                d = self.value(tree[1])
+                if not isinstance(d, _Node) or d.f64:
+                    raise NotImplementedError("year() of a non-integer operand is not on the kernel path")
+                return _Node(self._insn(("year", d.reg), L.X_YEAR, False, a=d.reg), False, torch.int64)
+            if (len(tree) == 2 and tree[0] in ("NOT", "StartsWith")) or (len(tree) == 3 and tree[1] in _COND_OPS):
+                return self.condition(tree)
         raise NotImplementedError(f"aggregate expression {tree!r} is not on the kernel path")
+
+    def condition(self, tree) -> _Node:
+        """A boolean sub-expression as a bool column, filled by the filter kernel before the
+        program runs (aggregate comparison rules)."""
+        from .predicate import compile_filter
+        key = repr(tree)
+        if key not in self.mask_memo:
+            pred = compile_filter(tree, {c: t for c, t in self.columns.items() if c < _HIDDEN_ID}, agg=True)
+            t0 = pred.tensors[0]
+            mask = torch.empty(t0.shape[0], dtype=torch.bool, device=t0.device)
+            cid = _HIDDEN_ID * 2 + len(self.masks)
+            self.columns[cid] = mask
+            self.masks.append((pred, mask))
+            self.mask_memo[key] = cid
+        return self.column(self.mask_memo[key])
+
+    def select(self, c, t, e) -> _Node:
+        """torch.where(c, t, e) with torch's promotion of the two branches."""
+        if not isinstance(c, _Node) or c.dtype != torch.bool:
+            raise NotImplementedError("CASE WHEN needs a boolean condition")
+        nodes = [x for x in (t, e) if isinstance(x, _Node)]
+        pys = [x for x in (t, e) if not isinstance(x, _Node)]
+        if any(n.f64 for n in nodes):
+            f64, dtype = True, torch.float64
+        elif any(isinstance(x, float) for x in pys):
+            raise NotImplementedError("CASE mixing a float literal with integers is float32 in torch")
+        elif not nodes:
+            f64, dtype = False, torch.int64
+        else:
+            ints = [n.dtype for n in nodes]
+            if len(ints) == 2 and {ints[0], ints[1]} == {torch.uint8, torch.int8}:
+                raise NotImplementedError("uint8 with int8 promotes to int16 in torch")
+            dtype = max(ints, key=lambda d: _INT_ORDER[d])
+            if dtype == torch.bool and pys:
+                dtype = torch.int64
+            f64 = False
+        regs = []
+        for x in (t, e):
+            n = x if isinstance(x, _Node) else self.const(float(x) if f64 else int(x))
+            regs.append(self.to_f64(n) if f64 else n.reg)
+        reg = self._insn(("sel", c.reg, regs[0], regs[1], f64), L.X_SELECT, f64, a=c.reg, b=regs[0], col=regs[1])
+        return _Node(reg, f64, dtype)
 
     def binary(self, op: str, a, b):
         op_code = {"+": L.X_ADD, "-": L.X_SUB, "*": L.X_MUL, "/": L.X_DIV}[op]
@@ -173,6 +262,16 @@ class _Builder:
         return self.acc_memo[key]
 
 
+def _call_of(t):
+    """(fn, arg) when t is an aggregate call, possibly wrapped as [[fn, arg], '#', id]."""
+    t = _strip(t)
+    while isinstance(t, list) and len(t) == 3 and t[1] == "#":
+        t = _strip(t[0])
+    if isinstance(t, list) and len(t) == 2 and isinstance(t[0], str) and t[0] in _AGG_FNS:
+        return t[0], t[1]
+    return None
+
+
 def _agg_call(tree):
     """Walks [[fn, arg], '#', id] / [.., 'AS', name] down to (fn, arg)."""
     t = _strip(tree)
@@ -183,11 +282,57 @@ def _agg_call(tree):
     raise NotImplementedError(f"aggregate result {tree!r}: only plain sum/avg/count/min/max calls run on the kernels")
 
 
-def compile_aggregate(args: dict, columns: Dict[int, torch.Tensor]) -> AggregateProgram:
-    b = _Builder(columns)
+def _lift_calls(t, calls: list, base: int):
+    """Replaces each aggregate call inside a result expression by a hidden column name
+    (ids base, base + 1, ...)."""
+    c = _call_of(t)
+    if c is not None:
+        hid = base + len(calls)
+        calls.append((hid, c[0], c[1]))
+        return f"agg#{hid}"
+    if isinstance(t, list):
+        return [_lift_calls(x, calls, base) for x in t]
+    return t
+
+
+def _add_output(b: _Builder, prog: AggregateProgram, oid: int, fn: str, arg):
+    v = b.value(arg)
+    scalar = not isinstance(v, _Node)
+    if fn == "count" and scalar and v != L.NULL_INDEX:      # count(1): every row counts
+        prog.outputs.append((oid, L.OUT_ACC, 0, 0, torch.int64))
+        return
+    if scalar:                                              # aggregate.py:149-152: full(cnt_rows, v)
+        v = b.const(v)
+    if fn == "sum":
+        a = b.acc(L.ACC_SUM, v)
+        prog.outputs.append((oid, L.OUT_ACC, a, 0, torch.float64 if v.f64 else torch.int64))
+    elif fn == "avg":
+        a = b.acc(L.ACC_SUM, v)
+        prog.outputs.append((oid, L.OUT_AVG, a, 0, torch.float64))
+    elif fn == "count":
+        a = b.acc(L.ACC_COUNT_NOTNULL, v)
+        prog.outputs.append((oid, L.OUT_ACC, a, 0, torch.int64))
+    elif fn == "min":
+        if v.f64:
+            a = b.acc(L.ACC_MIN, v, init_f=float(torch.finfo(torch.float64).max))
+        else:
+            a = b.acc(L.ACC_MIN, v, init_i=int(torch.iinfo(v.dtype if v.dtype != torch.bool else torch.int64).max))
+        prog.outputs.append((oid, L.OUT_ACC, a, 0, v.dtype))
+    else:  # max starts from zero, as the reference's zeros() initial tensor
+        a = b.acc(L.ACC_MAX, v)
+        prog.outputs.append((oid, L.OUT_ACC, a, 0, v.dtype))
+
+
+def compile_aggregate(args: dict, columns: Dict[int, torch.Tensor], derived: bool = False,
+                      key_codes: torch.Tensor = None) -> AggregateProgram:
+    """derived=False keeps to plain calls over arithmetic (every fused pipeline);
+    derived=True adds conditions, CASE, year() and arithmetic over aggregates.
+    key_codes (int32 [n], from ops.encode_keys) replaces the key tuple in the kernel."""
+    b = _Builder(columns, derived)
     prog = AggregateProgram(spec=None)
     prog.key_ids = [get_id(k) for k in (args.get("keys") or [])]
-    if len(prog.key_ids) > L.MAX_KEYS:
+    prog.encoded = key_codes is not None
+    if len(prog.key_ids) > L.MAX_KEYS and not prog.encoded:
         raise NotImplementedError(f"more than {L.MAX_KEYS} group keys")
     for tree in args["results"]:
         tree = _strip(tree)
@@ -195,37 +340,34 @@ def compile_aggregate(args: dict, columns: Dict[int, torch.Tensor]) -> Aggregate
         if is_key_result(tree):
             prog.key_outputs.append((oid, get_id(tree if isinstance(tree, str) else tree[0])))
             continue
-        fn, arg = _agg_call(tree)
-        v = b.value(arg)
-        scalar = not isinstance(v, _Node)
-        if fn == "count" and scalar and v != L.NULL_INDEX:  # count(1): every row counts
-            prog.outputs.append((oid, L.OUT_ACC, 0, 0, torch.int64))
+        body = tree[0] if isinstance(tree, list) and len(tree) == 3 and tree[1] == "AS" else tree
+        call = _call_of(body)
+        if call is not None:
+            _add_output(b, prog, oid, *call)
             continue
-        if scalar:                                          # aggregate.py:149-152: full(cnt_rows, v)
-            v = b.const(v)
-        if fn == "sum":
-            a = b.acc(L.ACC_SUM, v)
-            prog.outputs.append((oid, L.OUT_ACC, a, 0, torch.float64 if v.f64 else torch.int64))
-        elif fn == "avg":
-            a = b.acc(L.ACC_SUM, v)
-            prog.outputs.append((oid, L.OUT_AVG, a, 0, torch.float64))
-        elif fn == "count":
-            a = b.acc(L.ACC_COUNT_NOTNULL, v)
-            prog.outputs.append((oid, L.OUT_ACC, a, 0, torch.int64))
-        elif fn == "min":
-            if v.f64:
-                a = b.acc(L.ACC_MIN, v, init_f=float(torch.finfo(torch.float64).max))
-            else:
-                a = b.acc(L.ACC_MIN, v, init_i=int(torch.iinfo(v.dtype if v.dtype != torch.bool else torch.int64).max))
-            prog.outputs.append((oid, L.OUT_ACC, a, 0, v.dtype))
-        else:  # max starts from zero, as the reference's zeros() initial tensor
-            a = b.acc(L.ACC_MAX, v)
-            prog.outputs.append((oid, L.OUT_ACC, a, 0, v.dtype))
+        if not derived:
+            _agg_call(tree)                                 # raises NotImplementedError
+        calls: list = []
+        lifted = _lift_calls(body, calls, _HIDDEN_ID + sum(1 for o in prog.outputs if o[0] >= _HIDDEN_ID))
+        if not calls:
+            raise NotImplementedError(f"aggregate result {tree!r} has no aggregate call")
+        for hid, fn, arg in calls:
+            _add_output(b, prog, hid, fn, arg)
+        dts = {hid: dt for (hid, _, _, _, dt) in prog.outputs if hid in {c[0] for c in calls}}
+        trial = compile_projection([lifted], {h: torch.empty(0, dtype=dt) for h, dt in dts.items()})
+        prog.post.append((oid, lifted, trial.outputs[0][1]))
     if len(prog.outputs) > L.MAX_ACCS:
         raise NotImplementedError(f"more than {L.MAX_ACCS} aggregate outputs")
     s = L.GroupbySpec()
-    s.n_keys = len(prog.key_ids)
-    for k, kid in enumerate(prog.key_ids):
+    if prog.encoded:
+        t = key_codes.contiguous()
+        s.n_keys = 1
+        prog.tensors.append(t)
+        s.keys[0] = t.data_ptr()
+        s.key_dtypes[0] = code_of(t.dtype)
+    else:
+        s.n_keys = len(prog.key_ids)
+    for k, kid in enumerate([] if prog.encoded else prog.key_ids):
         t = columns[kid]
         if t.dim() == 2 and t.shape[1] == 1:
             t = t.reshape(-1)
@@ -247,6 +389,7 @@ def compile_aggregate(args: dict, columns: Dict[int, torch.Tensor]) -> Aggregate
     for i, (kind, ty, reg, ii, ff) in enumerate(b.accs):
         s.accs[i] = L.Acc(kind, ty, reg, 0, ii, ff)
     prog.spec = s
+    prog.masks = b.masks
     return prog
 
 
@@ -255,6 +398,7 @@ class ProjectionProgram:
     spec: Any                                   # expression program (no keys; accumulator 0 only)
     tensors: List[torch.Tensor] = field(default_factory=list)
     outputs: List[Tuple[int, torch.dtype]] = field(default_factory=list)   # (register, result dtype)
+    masks: List[Tuple[Any, torch.Tensor]] = field(default_factory=list)   # (condition predicate, its bool column)
 
 
 def is_trivial_projection(tree) -> bool:
@@ -264,10 +408,11 @@ def is_trivial_projection(tree) -> bool:
     return isinstance(tree, str) or (tree[1] == "AS" and isinstance(tree[0], str))
 
 
-def compile_projection(trees, columns: Dict[int, torch.Tensor]) -> ProjectionProgram:
+def compile_projection(trees, columns: Dict[int, torch.Tensor], derived: bool = False) -> ProjectionProgram:
     """The computed expressions of a projection (project.py:20-40) as one SSA program: each
-    output is a register with the dtype torch gives the expression (aggregate.py:203-233)."""
-    b = _Builder(columns)
+    output is a register with the dtype torch gives the expression (aggregate.py:203-233).
+    derived=True adds conditions, CASE and year() (bool columns filled before the launch)."""
+    b = _Builder(columns, derived)
     outs = []
     for tree in trees:
         while isinstance(tree, list) and len(tree) == 1:
@@ -291,4 +436,4 @@ def compile_projection(trees, columns: Dict[int, torch.Tensor]) -> ProjectionPro
         X.op, X.type, X.a, X.b, X.col, X.ci, X.cf = op, ty, a, bb, col, ci, cf
     spec.n_accs = 1
     spec.accs[0].kind, spec.accs[0].type = L.ACC_COUNT_ROWS, L.I64
-    return ProjectionProgram(spec=spec, tensors=list(b.col_tensors), outputs=outs)
+    return ProjectionProgram(spec=spec, tensors=list(b.col_tensors), outputs=outs, masks=b.masks)

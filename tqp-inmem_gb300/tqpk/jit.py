@@ -62,6 +62,15 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
                : "=r"(ok) : "r"(smem_u32(b)), "r"(parity) : "memory");
   return ok != 0;
 }
+// Year of day d (days since 1990-01-01): 1990 before that day, else the proleptic
+// Gregorian year by H. Hinnant's civil_from_days (400-year eras of 146097 days).
+__device__ __forceinline__ i64 tqpk_year(i64 d) {
+  if (d < 0) return 1990;
+  const i64 z = d + 7305 + 719468, era = z / 146097, doe = z - era * 146097;
+  const i64 yoe = (doe - doe / 1460 + doe / 36524 - doe / 146096) / 365;
+  const i64 doy = doe - (365 * yoe + yoe / 4 - yoe / 100), mp = (5 * doy + 2) / 153;
+  return yoe + era * 400 + (mp >= 10 ? 1 : 0);
+}
 // predicate literals, bound at launch (one compiled kernel serves every constant)
 struct PL { long long i[32]; double f[32]; double a[32]; };
 template <class T> struct V4 { T v[4]; };
@@ -299,6 +308,10 @@ def _expr_code(S, upto: int, colpfx: str) -> Tuple[List[int], List[str]]:
             lines.append(f"const {t} r{i} = {_hexf(X.cf) if f else str(int(X.ci)) + 'LL'};")
         elif X.op == L.X_TOF64:
             lines.append(f"const double r{i} = (double)r{X.a};")
+        elif X.op == L.X_SELECT:
+            lines.append(f"const {t} r{i} = r{X.a} != 0 ? r{X.b} : r{X.col};")
+        elif X.op == L.X_YEAR:
+            lines.append(f"const i64 r{i} = tqpk_year(r{X.a});")
         else:
             if f:
                 fn = {L.X_ADD: "__dadd_rn", L.X_SUB: "__dsub_rn", L.X_MUL: "__dmul_rn", L.X_DIV: "__ddiv_rn"}[X.op]

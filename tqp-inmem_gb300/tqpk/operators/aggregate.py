@@ -9,14 +9,16 @@ The filter mask is applied inside the aggregation kernel (the reference
 compacts every input column first, vortex_pipeline.py:58), every aggregate is
 computed in the same pass, and groups come out in ascending key order (the
 reference's order is the ascending order of a random linear hash of the key
-tuple, :320-327; for one non-negative key the two coincide).
+tuple, :320-327; for one non-negative key the two coincide).  Key tuples with a
+string (2-D) key, a float key or more than four keys are first numbered by
+ops.encode_keys (codes in key-tuple order) and grouped by that code.
 """
 from __future__ import annotations
 
 import torch
 
-from ..expr import compile_aggregate
-from ..ops import groupby
+from ..expr import compile_aggregate, needs_key_codes
+from ..ops import encode_keys, gather, groupby
 from ..variable import make_like, torch_to_type
 from .filter import _require_gpu
 
@@ -60,8 +62,19 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
         keys_out = {k: torch.tensor([], device=device) for k in range(len(key_ids))}
         vals_out = {a: torch.tensor([], device=device) for a in agg_ids}
         prog = None
+    elif needs_key_codes(args, cols):
+        # string / float / many keys: number the key tuples first, group by the code
+        kids = [int(k.split("#")[-1].replace("L", "")) for k in args["keys"]]
+        codes, reps, G0 = encode_keys([cols[k] for k in kids], mask)
+        prog = compile_aggregate(args, cols, derived=True, key_codes=codes)
+        _, vals_out, G, _ = groupby(prog, n, device, mask=mask)
+        assert G == G0, (G, G0)
+        keys_out = {}
+        for i, (oid, kid) in enumerate(prog.key_outputs):
+            k = gather([cols[kid]], reps)[0]
+            keys_out[i] = k if k.dim() == 2 else k.reshape(G, 1)     # unique_key_cols[:, pos_l:pos_r]
     else:
-        prog = compile_aggregate(args, cols)
+        prog = compile_aggregate(args, cols, derived=True)
         keys, vals_out, G, _ = groupby(prog, n, device, mask=mask)
         keys_out = {}
         for i, (oid, kid) in enumerate(prog.key_outputs):

@@ -22,7 +22,7 @@ def tqp_project(gpu_enable, tensor_group, args, cpu_mem_pool, gpu_mem_pool, name
         inputs = {k: tensor_group[k] for k in args["materialized in"]}
         first = next(iter(inputs.values()))
         rows = first.tensor.size(0)
-        prog = compile_projection(args["used expr"], {k: v.tensor for k, v in inputs.items()})
+        prog = compile_projection(args["used expr"], {k: v.tensor for k, v in inputs.items()}, derived=True)
         outs = project(prog, rows, first.tensor.device)
         for i, out_id in enumerate(args["materialized out"]):
             tensor_group[out_id] = make_like(first, outs[i], torch_to_type(outs[i].dtype))

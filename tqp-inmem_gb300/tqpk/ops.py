@@ -67,6 +67,17 @@ def filter_mask(pred: CompiledPredicate, n: int, device) -> Tuple[torch.Tensor, 
     return mask, count
 
 
+def fill_masks(masks, device) -> None:
+    """Evaluates the conditions of a compiled aggregate/projection (CASE WHEN, comparisons
+    used as values) into their preallocated bool columns."""
+    lib = L.load()
+    for pred, out in masks:
+        _check_cuda(out, *pred.tensors)
+        n = int(out.numel())
+        L.check(lib.tqpk_filter_mask(C.byref(pred.struct), n, out.data_ptr() if n else None, None,
+                                     _stream(device)), "tqpk_filter_mask")
+
+
 def compact(cols: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = None,
             pred: Optional[CompiledPredicate] = None, with_row_ids: bool = False) -> Tuple[List[torch.Tensor], int]:
     """Stable compaction of columns by a mask (or a predicate): tensor[mask]."""
@@ -107,6 +118,7 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
     lib = L.load()
     _check_cuda(mask, *prog.tensors)
     s = _stream(device)
+    fill_masks(prog.masks, device)
     plan = L.GbPlan()
     scratch = _ws(256, device)
     pp = C.byref(pred.struct) if pred is not None else None
@@ -141,7 +153,16 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
     L.check(lib.tqpk_groupby_emit(C.byref(prog.spec), C.byref(plan), ws.data_ptr(), G,
                                   _vp_array([k.data_ptr() for k in keys]), len(outs), _i32_array(ops),
                                   _vp_array([o.data_ptr() for o in outs]), s), "tqpk_groupby_emit")
-    return keys, {oid: o for (oid, *_), o in zip(prog.outputs, outs)}, G, plan
+    res = {oid: o for (oid, *_), o in zip(prog.outputs, outs)}
+    if prog.post:
+        # arithmetic over aggregates (aggregate.py:197-233): a projection over the group columns
+        from .expr import _HIDDEN_ID, compile_projection
+        hidden = {oid: res.pop(oid) for oid in list(res) if oid >= _HIDDEN_ID}
+        for oid, tree, dt in prog.post:
+            pp = compile_projection([tree], hidden)
+            res[oid] = project(pp, G, device)[0]
+            assert res[oid].dtype == dt
+    return keys, res, G, plan
 
 
 def _mask_predicate(mask: torch.Tensor) -> CompiledPredicate:
@@ -254,9 +275,70 @@ def join_probe(build: JoinBuild, probe_keys: torch.Tensor, probe_mask: Optional[
     raise RuntimeError("tqpk_join_probe: output size changed between calls")
 
 
-def gather(cols: Sequence[torch.Tensor], idx: torch.Tensor, null_aware: bool = False) -> List[torch.Tensor]:
-    """out_c = col_c[idx]; with null_aware an index of -64 yields -64 (index_with_null)."""
+def gather_rows(col: torch.Tensor, idx: torch.Tensor) -> torch.Tensor:
+    """col[idx] for a 2-D [N, w] column (string rows of w bytes)."""
     lib = L.load()
+    _check_cuda(col, idx)
+    c = col.contiguous()
+    n = int(idx.numel())
+    out = torch.empty((n,) + tuple(c.shape[1:]), dtype=c.dtype, device=c.device)
+    if n == 0:
+        return out
+    rb = c.element_size() * (c[0].numel() if c.shape[0] else 1)
+    L.check(lib.tqpk_gather_rows(c.data_ptr(), int(c.shape[0]), rb, idx.contiguous().data_ptr(), n, out.data_ptr(),
+                                 _stream(c.device)), "tqpk_gather_rows")
+    return out
+
+
+def encode_keys(keys: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = None):
+    """Dense group codes of key tuples (string, float and any number of keys):
+    (codes int32 [n], reps int64 [G] with groups in ascending key-tuple order, G)."""
+    lib = L.load()
+    ks, dts, ws = [], [], []
+    for k in keys:
+        if k.dim() == 2 and k.shape[1] == 1:
+            k = k.reshape(-1)
+        k = k.contiguous()
+        if k.dim() == 2:
+            if k.dtype not in (torch.int8, torch.uint8):
+                raise NotImplementedError(f"2-D group key of dtype {k.dtype}")
+            ws.append(int(k.shape[1]))
+        else:
+            ws.append(0)
+        ks.append(k)
+        dts.append(code_of(k.dtype))
+    _check_cuda(mask, *ks)
+    if len(ks) > L.MAX_COLS:
+        raise NotImplementedError(f"more than {L.MAX_COLS} group keys")
+    n = int(ks[0].shape[0])
+    device = ks[0].device
+    codes = torch.empty(n, dtype=torch.int32, device=device)
+    reps = torch.empty(max(n, 1), dtype=torch.int64, device=device)
+    ws_t = _ws(lib.tqpk_key_encode_workspace_bytes(n), device)
+    G = C.c_int64(0)
+    L.check(lib.tqpk_key_encode(len(ks), _vp_array([k.data_ptr() for k in ks]), _i32_array(dts), _i32_array(ws),
+                                mask.data_ptr() if mask is not None else None, n, codes.data_ptr() if n else None,
+                                reps.data_ptr(), C.byref(G), ws_t.data_ptr(), ws_t.numel(), _stream(device)),
+            "tqpk_key_encode")
+    return codes, reps[:G.value], G.value
+
+
+def gather(cols: Sequence[torch.Tensor], idx: torch.Tensor, null_aware: bool = False) -> List[torch.Tensor]:
+    """out_c = col_c[idx]; with null_aware an index of -64 yields -64 (index_with_null).
+    2-D (string) columns are gathered row by row."""
+    lib = L.load()
+    if any(c.dim() == 2 and c.shape[1] != 1 for c in cols):
+        if null_aware:
+            raise NotImplementedError("null-filled rows of a 2-D column (right-outer join payload)")
+        out = [None] * len(cols)
+        flat = [(i, c) for i, c in enumerate(cols) if not (c.dim() == 2 and c.shape[1] != 1)]
+        for i, c in enumerate(cols):
+            if c.dim() == 2 and c.shape[1] != 1:
+                out[i] = gather_rows(c, idx)
+        if flat:
+            for (i, _), o in zip(flat, gather([c for _, c in flat], idx)):
+                out[i] = o
+        return out
     cols = [_col1d(c) for c in cols]
     _check_cuda(idx, *cols)
     n = int(idx.numel())
@@ -280,6 +362,7 @@ def project(prog, n: int, device) -> List[torch.Tensor]:
     outs = [torch.empty(n, dtype=dt, device=device) for (_, dt) in prog.outputs]
     if n == 0 or not outs:
         return outs
+    fill_masks(prog.masks, device)
     if not jit.available():
         raise NotImplementedError("projection needs the runtime compiler (NVRTC)")
     src, name = jit.project_source(prog.spec, [(r, code_of(dt)) for (r, dt) in prog.outputs])

@@ -22,7 +22,8 @@ reference treats both as a substring search), ``LIKE '%a%b%'`` (``:121-127``),
 a multi-character literal compared byte-wise against the literal padded to w
 (``:151-158``) and ``IN`` lists of such literals compile to the string
 instructions; their literal bytes go to the predicate's string pool.
-``substring`` is not on the kernel path and raises ``NotImplementedError``.
+``substring(col, start, width)`` is a view of a string column (pointer offset,
+its own width, the column's row stride), usable wherever a string column is.
 """
 from __future__ import annotations
 
@@ -62,6 +63,19 @@ class _Col:
 
 
 @dataclass
+class _Sub:
+    """substring(col, start, width): the byte columns [start-1, start-1+width) of a string
+    column (filter.py:71-76, a strided view; Python slicing clips at the row's end)."""
+    cid: int
+    start: int
+    width: int
+
+    @property
+    def key(self):
+        return ("sub", self.cid, self.start, self.width)
+
+
+@dataclass
 class CompiledPredicate:
     """A predicate program plus the column tensors it reads (kept alive)."""
     struct: Any
@@ -73,9 +87,10 @@ class CompiledPredicate:
 
 
 class _Compiler:
-    def __init__(self, columns: Dict[int, Any], subquery=None):
+    def __init__(self, columns: Dict[int, Any], subquery=None, agg: bool = False):
         self.columns = columns
         self.subquery = subquery
+        self.agg = agg          # the comparison rules of aggregate.py:203-233 instead of filter.py's
         self.insn: List[tuple] = []
         self.slots: Dict[int, int] = {}
         self.str_cols = set()
@@ -83,6 +98,8 @@ class _Compiler:
 
     # -- values -------------------------------------------------------------
     def value(self, tree):
+        if self.agg:
+            return self._agg_value(tree)
         if isinstance(tree, str):
             if tree == "Subquery":
                 if self.subquery is None:
@@ -103,11 +120,49 @@ class _Compiler:
             literal, _, cast_type = tree[1][0].split(" ")
             if cast_type == "double":
                 return self.value(literal)
+        if len(tree) == 2 and tree[0] == "substring":
+            assert len(tree[1]) == 3
+            col, start, width = tree[1]
+            base = self.value(col)
+            if not isinstance(base, _Col):
+                raise NotImplementedError("substring of a non-column operand")
+            W = self.str_tensor(base.cid).shape[-1]
+            l0, w = int(start) - 1, int(width)
+            if l0 < 0 or w <= 0 or l0 >= W:
+                raise NotImplementedError(f"substring({start}, {width}) of a {W}-byte column")
+            return _Sub(base.cid, l0, min(W, l0 + w) - l0)
         return None  # a boolean sub-expression
 
-    def slot(self, cid: int) -> int:
+    def _agg_value(self, tree):
+        """Operands as aggregate.py:58-67 and :203-233 read them: digits are ints, other
+        numbers floats, `1 - URGENT` (a literal the plan parser split at '-') joins back
+        into the string '1-URGENT' (:224-227)."""
+        if isinstance(tree, str):
+            if tree.isdigit():
+                return int(tree)
+            if _is_float(tree):
+                return float(tree)               # a date literal raises here, as float() does there
+            if "#" in tree and tree.split("#")[-1].replace("L", "").isdigit():
+                return _Col(get_id(tree))
+            return tree
+        if len(tree) == 1:
+            return self._agg_value(tree[0])
+        if len(tree) == 3 and tree[1] == "#":
+            return self._agg_value(tree[0])
+        if len(tree) == 2 and tree[0] == "cast":
+            literal, _, cast_type = tree[1][0].split(" ")
+            if cast_type == "double":
+                return self._agg_value(literal)
+        if len(tree) == 3 and tree[1] == "-":
+            lv, rv = self._agg_value(tree[0]), self._agg_value(tree[2])
+            if isinstance(lv, int) and isinstance(rv, str):
+                return "".join(tree)
+        return None
+
+    def slot(self, cid) -> int:
+        """Slot of a column id, or of a substring view key ('sub', id, start, width)."""
         if cid not in self.slots:
-            if cid not in self.columns:
+            if (cid[1] if isinstance(cid, tuple) else cid) not in self.columns:
                 raise KeyError(f"filter column {cid} is not among the operator's inputs")
             if len(self.slots) >= L.MAX_COLS:
                 raise NotImplementedError(f"predicate reads more than {L.MAX_COLS} columns")
@@ -180,6 +235,8 @@ class _Compiler:
                 self.emit(tree[1])
                 self.insn.append((L.P_NOT, 0, 0, 0, 0, 0.0, 0.0))
                 return
+            if self.agg and head not in ("StartsWith",):        # aggregate.py:89-122
+                raise ValueError(f"Unsupported aggregation function: {head}")
             if head == "isnotnull":
                 self.insn.append((L.P_TRUE, 0, 0, 0, 0, 0.0, 0.0))
                 return
@@ -193,11 +250,23 @@ class _Compiler:
                 self.emit_str(L.P_PREFIX if head == "StartsWith" else L.P_CONTAINS, cid, 0, off | (len(data) << 32))
                 return
             if head == "substring":
-                raise NotImplementedError("substring is not on the kernel path")
+                raise NotImplementedError(f"filter leaf {tree!r} is not a boolean")
             raise ValueError(f"Unsupported Function: {head}")
         op = tree[-2]
+        if self.agg and op in ("IN", "LIKE"):                  # aggregate.py:206-222
+            raise ValueError(f"Unsupported Operation: {op}")
         if op == "IN":
             L_ = self.value(tree[0])
+            if isinstance(L_, _Sub):                             # filter.py:110-113 on a [N, w] slice
+                if not tree[-1]:
+                    self.insn.append((L.P_FALSE, 0, 0, 0, 0, 0.0, 0.0))
+                    return
+                for i, r in enumerate(tree[-1]):
+                    assert len(r) != 1, "single characters against a string column (filter.py:111)"
+                    self.emit_str(L.P_STRCMP, L_.key, L.EQ, self.pool_add(self._bytes(r, L_.width)))
+                    if i:
+                        self.insn.append((L.P_OR, 0, 0, 0, 0, 0.0, 0.0))
+                return
             if not isinstance(L_, _Col):
                 raise NotImplementedError("IN on a non-column operand")
             if self.columns[L_.cid].dim() == 2 and self.columns[L_.cid].shape[1] != 1:   # filter.py:110-113
@@ -243,15 +312,19 @@ class _Compiler:
             self.emit(tree[-1])
             self.insn.append((L.P_AND if op == "AND" else L.P_OR, 0, 0, 0, 0, 0.0, 0.0))
             return
-        if op not in ("<=", ">=", "<", ">", "="):
+        if op not in ("<=", ">=", "<", ">", "=") + (("<>",) if self.agg else ()):
             raise ValueError(f"Unsupported Operation: {op}")
         Lv = self.value(tree[0])
         Rv = self.value(tree[-1])
+        if self.agg:
+            return self._agg_cmp(tree, op, Lv, Rv)
         if isinstance(Lv, _Col) and isinstance(Rv, _Col):
             da, db = self.dtype(Lv.cid), self.dtype(Rv.cid)
             dom = L.DOM_F64 if L.F64 in (da, db) else L.DOM_I64
             self.insn.append((L.P_CMPCOL, self.slot(Lv.cid), _CMP[op], dom, self.slot(Rv.cid), 0.0, 0.0))
             return
+        if isinstance(Lv, _Sub) and isinstance(Rv, str) and len(Rv) > 1:      # filter.py:151-158 on a slice
+            return self.emit_str(L.P_STRCMP, Lv.key, L.EQ, self.pool_add(self._bytes(Rv, Lv.width)))
         if not isinstance(Lv, _Col):
             if isinstance(Rv, _Col):      # literal <op> column: same comparison mirrored
                 Lv, Rv, op = Rv, Lv, _FLIP[op]
@@ -269,7 +342,8 @@ class _Compiler:
             if t.dim() != 2:
                 raise NotImplementedError("multi-character literal against a one-dimensional column")
             w = self.str_tensor(Lv.cid).shape[-1]
-            return self.emit_str(L.P_STRCMP, Lv.cid, _CMP[op], self.pool_add(self._bytes(Rv, w)))
+            # (L == R).all(dim=1) whatever the operator (filter.py:158)
+            return self.emit_str(L.P_STRCMP, Lv.cid, L.EQ, self.pool_add(self._bytes(Rv, w)))
         if op == "=" and self.dtype(Lv.cid) == L.F64:     # filter.py:160-161
             if not isinstance(Rv, float):
                 raise TypeError("isclose against a non-float literal (the reference raises here too)")
@@ -278,10 +352,37 @@ class _Compiler:
             return
         return self.emit_cmp(Lv, op, Rv)
 
+    def _agg_cmp(self, tree, op, Lv, Rv):
+        """aggregate.py:224-233: ops[op](L, R) on tensors and Python numbers."""
+        if isinstance(Lv, _Col) and isinstance(Rv, _Col):
+            da, db = self.dtype(Lv.cid), self.dtype(Rv.cid)
+            dom = L.DOM_F64 if L.F64 in (da, db) else L.DOM_I64
+            self.insn.append((L.P_CMPCOL, self.slot(Lv.cid), _CMP[op], dom, self.slot(Rv.cid), 0.0, 0.0))
+            return
+        if isinstance(Rv, str):
+            if not isinstance(Lv, _Col):
+                raise NotImplementedError(f"string comparison without a column operand: {tree!r}")
+            if len(Rv) == 1:
+                return self.emit_cmp(Lv, op, ord(Rv))
+            w = self.str_tensor(Lv.cid).shape[-1]
+            return self.emit_str(L.P_STRCMP, Lv.cid, L.EQ, self.pool_add(self._bytes(Rv, w)))
+        if not isinstance(Lv, _Col):
+            if isinstance(Rv, _Col) and isinstance(Lv, (int, float)):
+                Lv, Rv, op = Rv, Lv, _FLIP[op]
+            else:
+                raise NotImplementedError(f"comparison without a column operand: {tree!r}")
+        if not isinstance(Rv, (int, float)):
+            raise NotImplementedError(f"comparison operand {tree[-1]!r} is not on the kernel path")
+        return self.emit_cmp(Lv, op, Rv)
 
-def compile_filter(tree, columns: Dict[int, Any], subquery=None) -> CompiledPredicate:
-    """Compiles a filter tree over ``columns`` (id -> 1-D device tensor)."""
-    c = _Compiler(columns, subquery)
+
+def compile_filter(tree, columns: Dict[int, Any], subquery=None, agg: bool = False) -> CompiledPredicate:
+    """Compiles a filter tree over ``columns`` (id -> 1-D device tensor).  With agg the
+    tree is a condition inside an aggregate or projection expression and compares as
+    aggregate.py:203-233 does: torch.le/ge/eq/ne without the filter's eps and isclose,
+    `<>` allowed, a multi-character string literal tested for equality whatever the
+    operator (:229-231), IN/LIKE and functions other than NOT/StartsWith rejected."""
+    c = _Compiler(columns, subquery, agg)
     c.emit(tree)
     if len(c.insn) > L.MAX_PRED:
         raise NotImplementedError(f"predicate longer than {L.MAX_PRED} instructions")
@@ -291,6 +392,16 @@ def compile_filter(tree, columns: Dict[int, Any], subquery=None) -> CompiledPred
     tensors = []
     ids = [None] * len(c.slots)
     for cid, s in c.slots.items():
+        if isinstance(cid, tuple):                     # substring view: offset pointer, own width, row stride
+            _, base_id, start, width = cid
+            t = c.str_tensor(base_id).contiguous()
+            tensors.append(t)
+            ids[s] = base_id
+            p.cols[s] = t.data_ptr() + start
+            p.widths[s] = width
+            p.strides[s] = int(t.shape[1])
+            p.dtypes[s] = code_of(t.dtype)
+            continue
         if cid in c.str_cols:
             t = c.str_tensor(cid).contiguous()
             p.widths[s] = int(t.shape[1])

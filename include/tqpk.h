@@ -471,6 +471,12 @@ int tqpk_key_encode(int32_t n_keys, const void* const* h_keys, const int32_t* h_
 int tqpk_gather_rows(const void* d_src, int64_t n_src, int64_t row_bytes, const int64_t* d_idx, int64_t n_idx,
                      void* d_dst, tqpk_stream stream);
 
+/* Sort keys of a string column for tqpk_argsort_stable (dtype int64): d_out[r]
+ * = bytes word*8 .. word*8+7 of row r, so ceil(w/8) stable passes, last word
+ * first, order the rows as the reference's unique(dim=0) ranks of the int8
+ * rows do (sort.py:31-35).                                                   */
+int tqpk_string_words(const void* d_src, int64_t n, int32_t width, int32_t word, int64_t* d_out, tqpk_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -423,6 +423,30 @@ def test_join_gathers_string_payloads():
     np.testing.assert_array_equal(np_(tg[4].tensor), ps[pi])
 
 
+@pytest.mark.parametrize("desc,limit", [(False, None), (True, None), (True, 7), (False, 100)])
+def test_sort_string_keys_vs_oracle(desc, limit):
+    """tqp_sort on a 19-byte string key (three word passes) then an int key, with and
+    without a limit; string payloads gathered row by row."""
+    from tqpk.operators import tqp_sort
+    from tqpk.variable import Variable
+    rng = np.random.default_rng(17)
+    n = 50_003
+    sk = rng.integers(60, 68, (n, 19)).astype(np.int8)
+    sk[:, 3:] = 0
+    sk[rng.integers(0, n, 300), 10] = -5          # a negative byte deep in the row
+    ik = rng.integers(0, 50, n).astype(np.int32)
+    pay = rng.integers(65, 91, (n, 11)).astype(np.int8)
+    tg = {1: Variable(torch.from_numpy(sk).cuda(), "string"), 2: V(ik),
+          3: Variable(torch.from_numpy(pay).cuda(), "string")}
+    args = {"input ids": [1, 2, 3], "key ids": [1, 2], "key orders": [desc, False]}
+    if limit is not None:
+        args["limit"] = limit
+    tqp_sort(True, tg, copy.deepcopy(args), limit is not None, "s")
+    ref = O.tqp_sort({1: sk, 2: ik, 3: pay}, args, limit is not None)
+    for c in (1, 2, 3):
+        np.testing.assert_array_equal(np_(tg[c].tensor), ref[c], err_msg=str(c))
+
+
 def test_aggregate_two_step_golden():
     from tqpk.operators import tqp_hash_aggregate
     ins, outs, args = load("aggregate_two_step")

@@ -165,6 +165,22 @@ __global__ void k_key_codes(const int64_t* __restrict__ entry_of_row, int64_t n,
   }
 }
 
+// Word `word` of each row of an int8 [n, w] column as a sort key: bytes
+// word*8 .. word*8+7 big-endian with the sign bit of each byte flipped (zero
+// past w), stored as int64 with its top bit flipped, so the library's int64
+// sort orders rows as the int8 byte columns compare, most significant first.
+__global__ void k_string_words(const uint8_t* __restrict__ src, int64_t n, int w, int word, int64_t* __restrict__ out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t* s = src + r * w;
+    uint64_t v = 0;
+    for (int i = 0; i < 8; ++i) {
+      const int c = word * 8 + i;
+      v = (v << 8) | (c < w ? static_cast<uint64_t>(s[c] ^ 0x80u) : 0ull);
+    }
+    out[r] = static_cast<int64_t>(v ^ (1ull << 63));
+  }
+}
+
 __global__ void k_gather_rows(const uint8_t* __restrict__ src, int64_t row_bytes, const int64_t* __restrict__ idx,
                               int64_t n_idx, int64_t n_src, uint8_t* __restrict__ dst, int* err) {
   const int64_t total = n_idx * row_bytes;
@@ -276,6 +292,17 @@ extern "C" int tqpk_gather_rows(const void* d_src, int64_t n_src, int64_t row_by
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   k_gather_rows<<<grid_for(n_idx * row_bytes, 8), kBlock, 0, s>>>(static_cast<const uint8_t*>(d_src), row_bytes, d_idx,
                                                                   n_idx, n_src, static_cast<uint8_t*>(d_dst), nullptr);
+  TQPK_CHECK_LAUNCH();
+  return TQPK_OK;
+}
+
+extern "C" int tqpk_string_words(const void* d_src, int64_t n, int32_t width, int32_t word, int64_t* d_out,
+                                 tqpk_stream stream) {
+  if (n < 0 || width <= 0 || word < 0 || word * 8 >= width) return TQPK_EINVAL;
+  if (n == 0) return TQPK_OK;
+  if (!d_src || !d_out) return TQPK_EINVAL;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  k_string_words<<<grid_for(n, 8), kBlock, 0, s>>>(static_cast<const uint8_t*>(d_src), n, width, word, d_out);
   TQPK_CHECK_LAUNCH();
   return TQPK_OK;
 }

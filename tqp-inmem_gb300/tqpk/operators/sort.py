@@ -6,14 +6,15 @@ gathering the key through ``perm`` (:26-35), then slices ``perm[:limit]``
 tqpk_argsort_stable call that sorts keys[perm] and permutes perm in the same
 kernels; with a limit the first key uses the stable top-k, which returns the
 same rows as the full sort followed by the slice.  A [N, w] key (the
-reference ranks its rows with unique(dim=0)) is sorted as w stable passes,
-last byte column first, which gives the same lexicographic order and ties.
+reference ranks its rows with unique(dim=0)) is sorted as ceil(w/8) stable
+passes over 8-byte words of the rows, last word first, which gives the same
+lexicographic order and ties; [N, w] columns are gathered row by row.
 """
 from __future__ import annotations
 
 import torch
 
-from ..ops import argsort_stable, gather, topk_stable
+from ..ops import argsort_stable, gather, gather_rows, string_words, topk_stable
 from ..variable import make_like
 from .filter import _require_gpu
 
@@ -33,7 +34,9 @@ def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
     for key_id, desc in zip(reversed(key_ids), reversed(key_descs)):
         col = tensor_group[key_id].tensor
         if col.dim() == 2 and col.shape[1] > 1:
-            steps += [(col[:, c].contiguous(), desc) for c in reversed(range(col.shape[1]))]
+            if col.dtype not in (torch.int8, torch.uint8):
+                raise NotImplementedError(f"2-D sort key of dtype {col.dtype}")
+            steps += [(string_words(col, wd), desc) for wd in reversed(range((col.shape[1] + 7) // 8))]
         else:
             steps.append((col.reshape(-1), desc))
     for i, (key, desc) in enumerate(steps):
@@ -51,7 +54,7 @@ def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
         if t.dim() == 2 and t.shape[1] == 1:
             out = gather([t.reshape(-1)], perm)[0].reshape(-1, 1)
         elif t.dim() == 2:
-            out = t.index_select(0, perm)    # multi-byte string rows: not on the kernel path
+            out = gather_rows(t, perm)
         else:
             out = gather([t], perm)[0]
         tensor_group[key_id] = make_like(tensor_group[key_id], out, tensor_group[key_id].tensor_type)

@@ -290,6 +290,18 @@ def gather_rows(col: torch.Tensor, idx: torch.Tensor) -> torch.Tensor:
     return out
 
 
+def string_words(col: torch.Tensor, word: int) -> torch.Tensor:
+    """Sort keys (int64) of 8-byte word `word` of an int8/uint8 [N, w] column."""
+    lib = L.load()
+    _check_cuda(col)
+    c = col.contiguous()
+    n, w = int(c.shape[0]), int(c.shape[1])
+    out = torch.empty(n, dtype=torch.int64, device=c.device)
+    L.check(lib.tqpk_string_words(c.data_ptr() if n else None, n, w, word, out.data_ptr() if n else None,
+                                  _stream(c.device)), "tqpk_string_words")
+    return out
+
+
 def encode_keys(keys: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = None):
     """Dense group codes of key tuples (string, float and any number of keys):
     (codes int32 [n], reps int64 [G] with groups in ascending key-tuple order, G)."""

@@ -636,9 +636,9 @@ def _stable_order(x: np.ndarray, desc: bool) -> np.ndarray:
         _, inv = np.unique(x, axis=0, return_inverse=True)
         x = inv.reshape(-1)
     if not desc:
-        return np.argsort(x, kind="stable")
+        return np.argsort(x, kind="stable")                         # NaN sorts last, as torch puts it
     if x.dtype.kind == "f":
-        return np.argsort(-x, kind="stable")
+        return np.lexsort((-x, ~np.isnan(x)))                       # torch: NaN is the largest, first when descending
     return np.argsort(~x.astype(np.int64), kind="stable")
 
 

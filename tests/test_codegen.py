@@ -78,9 +78,11 @@ def test_probe_kernels_compile_with_and_without_build_filter():
         ok, log = jit.check_compiles(src)
         assert ok, log[:2000]
         assert ("#define TQPK_LD(p) __ldcs" in src) == cs
-    src, _ = jit.join_probe_source(prog.spec, vreg, pp.struct, None, stream_cs=True)
-    ok, log = jit.check_compiles(src)
-    assert ok, log[:2000]
+    for cs, st in ((True, False), (False, True), (True, True)):
+        src, _ = jit.join_probe_source(prog.spec, vreg, pp.struct, None, stream_cs=cs, stage_vals=st)
+        ok, log = jit.check_compiles(src)
+        assert ok, log[:2000]
+        assert ("cp_async16(&q_v" in src) == st
 
 
 def test_generated_batch_kernel_compiles_and_record_layout_matches():

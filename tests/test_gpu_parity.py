@@ -505,6 +505,23 @@ def test_sort_multikey_golden():
             np.testing.assert_array_equal(np_(tg[c].tensor), outs[f"s{i}_{c}"], err_msg=f"spec {i} col {c}")
 
 
+@pytest.mark.parametrize("n", [1, 6, 1000, 2048, 2049])
+@pytest.mark.parametrize("desc", [False, True])
+def test_argsort_small_single_cta_path(n, desc):
+    """n <= 2048 sorts in one CTA (bitonic on key, position); 2049 takes the radix path."""
+    from tqpk.ops import argsort_stable
+    rng = np.random.default_rng(n)
+    for dtype in (np.int32, np.float64, np.uint8):
+        k = (rng.integers(-5, 5, n) * 0.5).astype(dtype) if dtype == np.float64 else rng.integers(0, 7, n).astype(dtype)
+        if dtype == np.float64 and n > 3:
+            k[:3] = [-0.0, 0.0, np.nan]
+        perm_in = rng.permutation(n)
+        got = np_(argsort_stable(torch.from_numpy(k).cuda(), desc, torch.from_numpy(perm_in).cuda()))
+        np.testing.assert_array_equal(got, perm_in[O._stable_order(k[perm_in], desc)])
+        got = np_(argsort_stable(torch.from_numpy(k).cuda(), desc))
+        np.testing.assert_array_equal(got, O._stable_order(k, desc))
+
+
 @pytest.mark.parametrize("dtype", [np.int32, np.int64, np.float64, np.uint8, np.int8])
 @pytest.mark.parametrize("desc", [False, True])
 def test_argsort_stable_vs_numpy(dtype, desc):

@@ -333,11 +333,13 @@ extern "C" int tqpk_join_build(tqpk_join_plan* plan, const void* keys, int32_t d
                                                                       L.hdr);
       TQPK_CHECK_LAUNCH();
     }
-    int dup = 0;
-    TQPK_CUDA(cudaMemcpyAsync(&dup, L.hdr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int h[2] = {0, 0};   // [0] a repeated key, [1] error word: one read
+    TQPK_CUDA(cudaMemcpyAsync(h, L.hdr, sizeof(h), cudaMemcpyDeviceToHost, s));
     TQPK_CUDA(cudaStreamSynchronize(s));
-    plan->unique = dup ? 0 : 1;
-    need_sort = dup != 0;
+    if (h[1]) return h[1];
+    plan->unique = h[0] ? 0 : 1;
+    need_sort = h[0] != 0;
+    if (!need_sort) return TQPK_OK;
   }
   if (need_sort && plan->nb_rows > 0) {
     plan->unique = 0;

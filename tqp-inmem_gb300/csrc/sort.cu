@@ -121,6 +121,52 @@ __global__ void __launch_bounds__(kBlock) k_sort_pass(const uint64_t* __restrict
   }
 }
 
+// Small sorts (n <= kSmallSort, e.g. the groups of an aggregate result): one
+// CTA sorts (key, position) pairs with a bitonic network in shared memory.
+// Ties fall to the smaller position, so the result is the stable order, and
+// the host never waits (no trivial-pass flags, no look-back error word).
+constexpr int kSmallSort = 2048;
+
+__global__ void __launch_bounds__(1024) k_sort_small(const void* keys, int dt, int desc, const int64_t* perm_in,
+                                                     int n, int64_t* perm_out) {
+  __shared__ uint64_t sk[kSmallSort];
+  __shared__ uint16_t si[kSmallSort];
+  __shared__ int64_t pin[kSmallSort];
+  int P = 1;
+  while (P < n) P <<= 1;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    if (i < n) {
+      const int64_t row = perm_in ? perm_in[i] : i;
+      pin[i] = row;
+      sk[i] = sort_key(keys, dt, row, desc);
+      si[i] = static_cast<uint16_t>(i);
+    } else {
+      sk[i] = ~0ull;
+      si[i] = 0xffffu;
+    }
+  }
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const bool up = (i & k) == 0;
+          const uint64_t ka = sk[i], kb = sk[ixj];
+          const uint16_t ia = si[i], ib = si[ixj];
+          const bool greater = ka > kb || (ka == kb && ia > ib);
+          if (greater == up) {
+            sk[i] = kb; sk[ixj] = ka;
+            si[i] = ib; si[ixj] = ia;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm_out[i] = pin[si[i]];
+}
+
 size_t sort_ws_bytes(int64_t n) {
   const int64_t tiles = (n + kSortTile - 1) / kSortTile;
   size_t b = 0;
@@ -189,6 +235,11 @@ extern "C" int tqpk_argsort_stable(const void* d_keys, int32_t dt, int32_t desc,
   if (ws_bytes < sort_ws_bytes(n)) return TQPK_ENOMEM;
   if ((n + kSortTile - 1) / kSortTile > INT32_MAX) return TQPK_EUNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (n <= kSmallSort) {
+    k_sort_small<<<1, 1024, 0, s>>>(d_keys, dt, desc ? 1 : 0, d_perm_in, (int)n, d_perm_out);
+    TQPK_CHECK_LAUNCH();
+    return TQPK_OK;
+  }
   const int64_t* res = nullptr;
   int rc = sort_pairs(d_keys, dt, desc ? 1 : 0, d_perm_in, n, ws, ws_bytes, s, &res);
   if (rc) return rc;

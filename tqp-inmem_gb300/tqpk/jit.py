@@ -71,6 +71,13 @@ __device__ __forceinline__ i64 tqpk_year(i64 d) {
   const i64 doy = doe - (365 * yoe + yoe / 4 - yoe / 100), mp = (5 * doy + 2) / 153;
   return yoe + era * 400 + (mp >= 10 ? 1 : 0);
 }
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
 // predicate literals, bound at launch (one compiled kernel serves every constant)
 struct PL { long long i[32]; double f[32]; double a[32]; };
 template <class T> struct V4 { T v[4]; };
@@ -143,11 +150,41 @@ def _aligned(*ts) -> int:
     return int(all(t.data_ptr() % 16 == 0 for t in ts if t is not None))
 
 
+_gb_memo: Dict[bytes, Tuple[int, int, int]] = {}
+
+
+def _shape_key(*structs) -> bytes:
+    """The bytes of ctypes structs with their pointer arrays cleared: what a generated
+    kernel's source depends on (pointers and literals are launch arguments)."""
+    out = []
+    for st in structs:
+        if st is None:
+            out.append(b"-")
+            continue
+        c = type(st).from_buffer_copy(st)
+        for fname, ftype in type(st)._fields_:
+            if fname in ("cols", "keys", "n_rows", "ws_bytes", "key_range"):   # pointers, plan sizes
+                setattr(c, fname, ftype())
+            elif fname == "insn" and isinstance(st, L.Predicate):  # comparison literals are bound at launch
+                for i in range(c.n_insn):
+                    if c.insn[i].op == L.P_CMP:
+                        c.insn[i].lit_i, c.insn[i].lit_f, c.insn[i].lit_aux = 0, 0.0, 0.0
+        out.append(bytes(c))
+    return b"|".join(out)
+
+
 def run_groupby(spec, pred, plan, ws, n: int, stream: int, pred_tensors=(), key_tensors=(), col_tensors=()):
-    """Accumulation pass of ops.groupby as a query-specialised kernel (table in ws)."""
+    """Accumulation pass of ops.groupby as a query-specialised kernel (table in ws).  The
+    generated kernel is looked up by the shape of the spec, predicate and plan, so a
+    repeated query shape skips the source generation."""
     lib = L.load()
-    src, name, T, smem = groupby_source(spec, pred.struct if pred is not None else None, plan)
-    h = compile_kernel(src, name)
+    key = _shape_key(spec, pred.struct if pred is not None else None, plan)
+    hit = _gb_memo.get(key)
+    if hit is None:
+        src, name, T, smem = groupby_source(spec, pred.struct if pred is not None else None, plan)
+        hit = (compile_kernel(src, name), T, smem)
+        _gb_memo[key] = hit
+    h, T, smem = hit
     a = _Args()
     if pred is not None:
         for c in range(pred.struct.n_cols):
@@ -532,8 +569,33 @@ def probe_units(n: int) -> int:
     return (int(n) + 4 * PROBE_U - 1) // (4 * PROBE_U)
 
 
+def _stage_values(S, ecols, rows: int, n: str) -> Tuple[List[str], List[str], Dict[int, str]]:
+    """Shared-memory stages of the value columns filled by cp.async (global -> shared,
+    16-byte pieces, no registers held while the lookups are in flight): declarations,
+    per-u copy statements (r0 = the 4-row group, sidx = its offset in the warp's rows),
+    and the _dense_tail smem_vals map."""
+    decl, copy, sv = [], [], {}
+    for c in ecols:
+        t = _CTYPE[S.col_dtypes[c]]
+        es = {L.F64: 8, L.I64: 8, L.I32: 4}.get(S.col_dtypes[c])
+        decl.append(f"  __shared__ __align__(16) {t} q_v{c}[8][{32 * rows}];")
+        sv[c] = f"q_v{c}[wid]"
+        if es is None:
+            copy.append(f"for (int j = 0; j < 4; ++j) q_v{c}[wid][sidx + j] = (r0 + j < {n}) ? "
+                        f"((const {t}*)cp{c})[r0 + j] : ({t})0;")
+            continue
+        pieces = 4 * es // 16
+        copy.append(f"if (vc != 0 && r0 + 4 <= {n}) {{")
+        for q in range(pieces):
+            copy.append(f"  cp_async16(&q_v{c}[wid][sidx + {q * 16 // es}], (const {t}*)cp{c} + r0 + {q * 16 // es});")
+        copy.append("} else {")
+        copy.append(f"  for (int j = 0; j < 4; ++j) q_v{c}[wid][sidx + j] = (r0 + j < {n}) ? ((const {t}*)cp{c})[r0 + j] : ({t})0;")
+        copy.append("}")
+    return decl, copy, sv
+
+
 def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, min_blocks: int = 0,
-                      stream_cs: bool = False) -> Tuple[str, str]:
+                      stream_cs: bool = False, stage_vals: bool = False) -> Tuple[str, str]:
     """CUDA source of the fused probe + aggregate (directory lookup, value, FP64 sum, occupancy).
 
     The directory holds build row indices (negative = no row).  `bpred`, when
@@ -543,7 +605,9 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
     the warp then computes the value and updates the group of its matched rows
     densely (_dense_tail).  min_blocks > 0 asks the compiler for that many
     resident CTAs per SM (__launch_bounds__ register cap); stream_cs loads the
-    probe columns with evict-first hints."""
+    probe columns with evict-first hints; stage_vals copies the value columns of
+    every row to shared memory with cp.async at the top of the iteration (the
+    value gather after the lookup leaves the dependent chain)."""
     S = spec
     pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
     ecols, elines = _expr_code(S, val_reg + 1, "c")
@@ -564,10 +628,11 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
     qt = "unsigned char" if 32 * rows <= 256 else "unsigned short"
     lb = f"256, {min_blocks}" if min_blocks else "256"
     hint = "#define TQPK_LD(p) __ldcs(p)\n" if stream_cs else ""
+    sdecl, scopy, smem_vals = _stage_values(S, ecols, rows, "np") if stage_vals else ([], [], None)
     src = [hint + PRELUDE, f'extern "C" __global__ void __launch_bounds__({lb}) {name}(',
            "    " + ",\n    ".join(params) + ") {",
            f"  __shared__ {qt} q_off[8][{32 * rows}];",
-           f"  __shared__ int q_slot[8][{32 * rows}];",
+           f"  __shared__ int q_slot[8][{32 * rows}];"] + sdecl + [
            "  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;",
            f"  const i64 nr = (np + {rows - 1}) / {rows};",
            "  const i64 stride = (i64)gridDim.x * blockDim.x;",
@@ -579,6 +644,8 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
            f"      const i64 r0 = g * {rows} + u * 4;",
            "      m[u] = 0;",
            "      if (r0 >= np) continue;"]
+    if stage_vals:
+        src += [f"      const int sidx = lane * {rows} + u * 4;"] + ["      " + l for l in scopy]
     src += ["      " + l for l in _load_lines(pcols, pred.dtypes, "P", "pp", "np", "vp != 0")] if pred is not None else []
     src += ["      " + fk_load,
             "#pragma unroll",
@@ -601,7 +668,9 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
         src += ["      " + l for l in glines]
         src += ["#pragma unroll", "      for (int j = 0; j < 4; ++j)",
                 f"        if (((m[u] >> j) & 1u) && !({gexpr})) m[u] &= ~(1u << j);", "    }"]
-    src += _dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"], U=U)
+    if stage_vals:
+        src += ["    cp_async_wait_all();", "    __syncwarp();"]
+    src += _dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"], U=U, smem_vals=smem_vals)
     src += ["  }", "}"]
     return "\n".join(src), name
 

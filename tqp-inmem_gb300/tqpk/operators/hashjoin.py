@@ -167,7 +167,11 @@ def join_vortex(gpu_enable, tensor_group, args, leftcol, rightcol, condition_lis
     if leftcol not in tl or rightcol not in tr:
         raise KeyError("join key is not in its side's group")
     bi, pi, nb_rows = _pairs(tl, tr, leftcol, rightcol, condition_list, type, masks[LEFT], masks[RIGHT])
-    np_rows = int(masks[RIGHT].sum().item()) if masks[RIGHT] is not None else tr[rightcol].tensor.shape[0]
+    # only "does the probe side have rows" matters (hashjoin.py:161-172); any output row answers it
+    if pi.numel() > 0:
+        np_rows = int(pi.numel())
+    else:
+        np_rows = int(masks[RIGHT].sum().item()) if masks[RIGHT] is not None else tr[rightcol].tensor.shape[0]
     outs = _outputs(tl, tr, join_output, type, bi, pi, left_rows=nb_rows, right_rows=np_rows)
     for i, k in enumerate(join_output):                # hashjoin.py:234-238
         tensor_group[k] = make_like(tensor_group[k], outs[i], tensor_group[k].tensor_type)

@@ -56,14 +56,16 @@ def _i32_array(vals: Sequence[int]):
 
 
 # ---------------------------------------------------------------- (a) filter
-def filter_mask(pred: CompiledPredicate, n: int, device) -> Tuple[torch.Tensor, torch.Tensor]:
-    """Bool mask of the predicate over n rows and a device count of true rows."""
+def filter_mask(pred: CompiledPredicate, n: int, device, with_count: bool = False):
+    """Bool mask of the predicate over n rows and, with_count, a device count of true rows
+    (else None)."""
     lib = L.load()
     mask = torch.empty(n, dtype=torch.bool, device=device)
-    count = torch.zeros(1, dtype=torch.int64, device=device)
+    count = torch.zeros(1, dtype=torch.int64, device=device) if with_count else None
     _check_cuda(*pred.tensors)
-    L.check(lib.tqpk_filter_mask(C.byref(pred.struct), n, mask.data_ptr() if n else None, count.data_ptr(),
-                                 _stream(device)), "tqpk_filter_mask")
+    L.check(lib.tqpk_filter_mask(C.byref(pred.struct), n, mask.data_ptr() if n else None,
+                                 count.data_ptr() if count is not None else None, _stream(device)),
+            "tqpk_filter_mask")
     return mask, count
 
 
@@ -139,20 +141,35 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
                 "tqpk_groupby_prepare")
         jit.run_groupby(prog.spec, pred, plan, ws, n, s, pred.tensors if pred is not None else (),
                         [t for t in prog.tensors[:prog.spec.n_keys]], prog.tensors[prog.spec.n_keys:])
-        L.check(lib.tqpk_groupby_count(C.byref(prog.spec), C.byref(plan), ws.data_ptr(), C.byref(groups), s),
-                "tqpk_groupby_count")
-    else:
-        L.check(lib.tqpk_groupby_run(C.byref(prog.spec), C.byref(plan), pp, mp, n, ws.data_ptr(), ws.numel(),
-                                     C.byref(groups), s), "tqpk_groupby_run")
-    G = groups.value
-    keys = [torch.empty(G, dtype=dtype_of(prog.spec.key_dtypes[k]), device=device) for k in range(prog.spec.n_keys)]
-    outs = [torch.empty(G, dtype=dt, device=device) for (_, _, _, _, dt) in prog.outputs]
     ops = []
     for (_, op, a, b, dt) in prog.outputs:
         ops += [op, a, b, code_of(dt)]
-    L.check(lib.tqpk_groupby_emit(C.byref(prog.spec), C.byref(plan), ws.data_ptr(), G,
-                                  _vp_array([k.data_ptr() for k in keys]), len(outs), _i32_array(ops),
-                                  _vp_array([o.data_ptr() for o in outs]), s), "tqpk_groupby_emit")
+    if use_jit and (mask is None or pred is not None):
+        # count and emit with one host read: outputs sized for every slot, the device count
+        # (or a negative status) read once, then views of the first G rows
+        K = int(plan.slots)
+        keys = [torch.empty(K, dtype=dtype_of(prog.spec.key_dtypes[k]), device=device) for k in range(prog.spec.n_keys)]
+        outs = [torch.empty(K, dtype=dt, device=device) for (_, _, _, _, dt) in prog.outputs]
+        gdev = torch.empty(1, dtype=torch.int64, device=device)
+        L.check(lib.tqpk_groupby_emit_async(C.byref(prog.spec), C.byref(plan), ws.data_ptr(),
+                                            _vp_array([k.data_ptr() for k in keys]), len(outs), _i32_array(ops),
+                                            _vp_array([o.data_ptr() for o in outs]), gdev.data_ptr(), s),
+                "tqpk_groupby_emit_async")
+        G = int(gdev.item())
+        if G < 0:
+            L.check(G, "tqpk_groupby_emit_async")
+        keys = [k[:G] for k in keys]
+        outs = [o[:G] for o in outs]
+    else:
+        L.check(lib.tqpk_groupby_run(C.byref(prog.spec), C.byref(plan), pp, mp, n, ws.data_ptr(), ws.numel(),
+                                     C.byref(groups), s), "tqpk_groupby_run")
+        G = groups.value
+        keys = [torch.empty(G, dtype=dtype_of(prog.spec.key_dtypes[k]), device=device)
+                for k in range(prog.spec.n_keys)]
+        outs = [torch.empty(G, dtype=dt, device=device) for (_, _, _, _, dt) in prog.outputs]
+        L.check(lib.tqpk_groupby_emit(C.byref(prog.spec), C.byref(plan), ws.data_ptr(), G,
+                                      _vp_array([k.data_ptr() for k in keys]), len(outs), _i32_array(ops),
+                                      _vp_array([o.data_ptr() for o in outs]), s), "tqpk_groupby_emit")
     res = {oid: o for (oid, *_), o in zip(prog.outputs, outs)}
     if prog.post:
         # arithmetic over aggregates (aggregate.py:197-233): a projection over the group columns

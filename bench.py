@@ -43,10 +43,23 @@ PEAK_FALLBACK_GBS = 6800.0
 
 
 # ---------------------------------------------------------------------------- workloads
+def d2h_all(tensors):
+    """Results to pinned host memory: every copy queued, then one synchronisation."""
+    import torch
+    out = {}
+    for c, t in tensors.items():
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        out[c] = h
+    torch.cuda.current_stream().synchronize()
+    return out
+
+
 class StagedInputs:
     """Host->device copies of one step's input columns on a copy stream, in the order the plan
-    reads them, with one event per column: each operator waits only for the columns it reads,
-    so the later columns' copies overlap the earlier operators."""
+    reads them, with one event per column carried by the column's Variable (`ready`): each
+    operator waits for a column right before its first kernel that reads it, so the later
+    columns' copies overlap the earlier operators (and the earlier stages of an operator)."""
 
     def __init__(self, host, dev, types, order):
         import torch
@@ -63,15 +76,10 @@ class StagedInputs:
         with torch.cuda.stream(self.copy_stream):
             for c in self.order:
                 self.dst[c].copy_(self.host[c], non_blocking=True)
+                self.dst[c].record_stream(self.copy_stream)
                 self.ev[c] = torch.cuda.Event()
                 self.ev[c].record(self.copy_stream)
-        return {c: Variable(t, self.types[c]) for c, t in self.dst.items()}
-
-    def need(self, *cols):
-        import torch
-        main = torch.cuda.current_stream(self.dev)
-        for c in cols:
-            main.wait_event(self.ev[c])
+        return {c: Variable(t, self.types[c], ready=self.ev[c]) for c, t in self.dst.items()}
 
     @property
     def bytes(self):
@@ -150,16 +158,13 @@ class JoinAggTop10:
         if not hasattr(self, "staged"):
             self.staged = StagedInputs(self.host, self.dev, self.types, (12, 22, 11, 21, 23, 24))
         tg = self.staged.start()
-        self.staged.need(12)
         tqp_filter(True, tg, copy.deepcopy(self.f1), None, None, None, "f1")
-        self.staged.need(22)
         tqp_filter(True, tg, copy.deepcopy(self.f2), None, None, None, "f2")
-        self.staged.need(11, 21, 23, 24)
         join_vortex(True, tg, copy.deepcopy(self.jargs), 11, 21, [], "inner", None, None, "j")
         tqp_hash_aggregate(True, tg, copy.deepcopy(self.aargs), None, None, "a")
         tqp_sort(True, tg, copy.deepcopy(self.targs), True, "t")
-        keys = tg[11].tensor.to("cpu")
-        vals = tg[302].tensor.to("cpu")
+        res = d2h_all({11: tg[11].tensor, 302: tg[302].tensor})
+        keys, vals = res[11], res[302]
         h2d = sum(h.numel() * h.element_size() for h in self.host.values())
         d2h = keys.numel() * keys.element_size() + vals.numel() * vals.element_size()
         return (keys.numpy().reshape(-1), vals.numpy()), h2d, d2h
@@ -274,12 +279,10 @@ class FilterGroupBy:
         if not hasattr(self, "staged"):
             self.staged = StagedInputs(self.host, self.dev, self.types, (7, 5, 6, 1, 2, 3, 4))
         tg = self.staged.start()
-        self.staged.need(7)
         tqp_filter(True, tg, copy.deepcopy(self.fargs), None, None, None, "f")
-        self.staged.need(5, 6, 1, 2, 3, 4)
         tqp_hash_aggregate(True, tg, copy.deepcopy(self.aargs), None, None, "a")
         tqp_sort(True, tg, copy.deepcopy(self.sargs), False, "s")
-        out = {c: tg[c].tensor.to("cpu").numpy() for c in self.sargs["input ids"]}
+        out = {c: v.numpy() for c, v in d2h_all({c: tg[c].tensor for c in self.sargs["input ids"]}).items()}
         h2d = sum(h.numel() * h.element_size() for h in self.host.values())
         d2h = sum(v.nbytes for v in out.values())
         return out, h2d, d2h
@@ -377,11 +380,9 @@ class StarJoin:
         tg = self.staged.start()
 
         def f(tg, a):
-            self.staged.need(*a["materialized in"])
             tqp_filter(True, tg, a, None, None, None, "f")
 
         def j(tg, a, lk, rk):
-            self.staged.need(*[c for c in a["left group"] + a["right group"] if c in self.staged.ev])
             join_vortex(True, tg, a, lk, rk, [], "inner", None, None, "j")
             return tg
 
@@ -393,7 +394,8 @@ class StarJoin:
             tqp_sort(True, tg, a, True, "t")
             return tg
         tg = self._plan(tg, (f, j, ag, so))
-        out = [tg[c].tensor.to("cpu").numpy().reshape(-1) for c in (61, 72, 74)]
+        res = d2h_all({c: tg[c].tensor for c in (61, 72, 74)})
+        out = [res[c].numpy().reshape(-1) for c in (61, 72, 74)]
         h2d = sum(h.numel() * h.element_size() for h in self.host.values())
         return tuple(out), h2d, sum(o.nbytes for o in out)
 

@@ -585,3 +585,49 @@ def test_join_conditions_every_join_type(jtype):
     for c in (11, 12, 13, 21, 22, 23):
         got = np_(tg[c].tensor).reshape(-1)
         np.testing.assert_array_equal(got, np.asarray(ref[c]).reshape(-1), err_msg=str(c))
+
+
+def test_operators_wait_for_columns_still_copying():
+    """Columns copied from pinned host memory on a side stream, each Variable carrying the
+    copy's event: every operator waits for a column right before its first kernel reads it,
+    and the chained filter -> join -> aggregate -> top-10 matches the oracle."""
+    from tqpk import datagen
+    from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
+    from tqpk.variable import Variable
+    t = datagen.join_tables(300_000, 2_000_003, seed=5)
+    cols = {11: t["b_key"], 12: t["b_date"], 21: t["p_fk"], 22: t["p_date"], 23: t["p_price"], 24: t["p_discount"]}
+    types = {11: "int", 12: "date", 21: "int", 22: "date", 23: "float", 24: "float"}
+    host = {c: torch.from_numpy(a).pin_memory() for c, a in cols.items()}
+    side = torch.cuda.Stream()
+    main = torch.cuda.current_stream()
+    dst = {c: torch.empty(h.shape, dtype=h.dtype, device="cuda") for c, h in host.items()}
+    side.wait_stream(main)
+    tg = {}
+    with torch.cuda.stream(side):
+        for c in (12, 22, 11, 21, 23, 24):
+            dst[c].copy_(host[c], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(side)
+            tg[c] = Variable(dst[c], types[c], ready=ev)
+    f1 = {"filter tree": [["bd#12", "<", "1170"]], "materialized in": [12], "out mask id": 901}
+    f2 = {"filter tree": [["pd#22", ">", "1170"]], "materialized in": [22], "out mask id": 902}
+    jargs = {"left group": [11, 12], "right group": [21, 22, 23, 24], "materialized in": [11, 21, 23, 24],
+             "mask map": {11: 901, 21: 902, 23: 902, 24: 902}}
+    aargs = {"is partial": False, "keys": ["k#11"], "input ids": [11, 23, 24],
+             "results": ["k#11", [[["sum", [["p#23", "*", ["1.0", "-", "d#24"]]]], "#", "301"], "AS", "rev#302"]],
+             "out agg ids": [302]}
+    targs = {"limit": 10, "input ids": [11, 302], "key ids": [302], "key orders": [True]}
+    tqp_filter(True, tg, copy.deepcopy(f1), None, None, None, "f1")
+    tqp_filter(True, tg, copy.deepcopy(f2), None, None, None, "f2")
+    join_vortex(True, tg, copy.deepcopy(jargs), 11, 21, [], "inner", None, None, "j")
+    tqp_hash_aggregate(True, tg, copy.deepcopy(aargs), None, None, "a")
+    tqp_sort(True, tg, copy.deepcopy(targs), True, "t")
+    got_k, got_v = np_(tg[11].tensor).reshape(-1), np_(tg[302].tensor)
+    oc = dict(cols)
+    oc[901] = O.eval_filter(f1["filter tree"], {12: cols[12]})
+    oc[902] = O.eval_filter(f2["filter tree"], {22: cols[22]})
+    j = O.join_vortex(oc, copy.deepcopy(jargs), 11, 21, "inner")[0]
+    agg = O.tqp_hash_aggregate(j, copy.deepcopy(aargs))
+    top = O.tqp_sort(agg, targs, True)
+    np.testing.assert_array_equal(got_k, top[11].reshape(-1))
+    assert_f64_close(got_v, top[302])

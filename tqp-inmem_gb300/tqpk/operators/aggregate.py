@@ -19,7 +19,7 @@ import torch
 
 from ..expr import compile_aggregate, needs_key_codes
 from ..ops import encode_keys, gather, groupby
-from ..variable import make_like, torch_to_type
+from ..variable import make_like, torch_to_type, wait_ready
 from .filter import _require_gpu
 
 
@@ -54,6 +54,11 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
     agg_ids = args["out agg ids"]
 
     cols = {c: tensor_group[c].tensor for c in data_ids}
+    key_set = {int(k.split("#")[-1].replace("L", "")) for k in (args.get("keys") or [])}
+    wait_ready(*[tensor_group[c] for c in transfer_set if c in key_set or c in mask_ids])   # the plan's inputs
+
+    def values_ready():
+        wait_ready(*[tensor_group[c] for c in transfer_set if c not in key_set and c not in mask_ids])
     proto = tensor_group[data_ids[0]] if data_ids else None
     n = next(iter(cols.values())).shape[0] if cols else 0
     device = next(iter(cols.values())).device if cols else torch.device("cuda")
@@ -67,7 +72,7 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
         kids = [int(k.split("#")[-1].replace("L", "")) for k in args["keys"]]
         codes, reps, G0 = encode_keys([cols[k] for k in kids], mask)
         prog = compile_aggregate(args, cols, derived=True, key_codes=codes)
-        _, vals_out, G, _ = groupby(prog, n, device, mask=mask)
+        _, vals_out, G, _ = groupby(prog, n, device, mask=mask, before_values=values_ready)
         assert G == G0, (G, G0)
         keys_out = {}
         for i, (oid, kid) in enumerate(prog.key_outputs):
@@ -75,7 +80,7 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
             keys_out[i] = k if k.dim() == 2 else k.reshape(G, 1)     # unique_key_cols[:, pos_l:pos_r]
     else:
         prog = compile_aggregate(args, cols, derived=True)
-        keys, vals_out, G, _ = groupby(prog, n, device, mask=mask)
+        keys, vals_out, G, _ = groupby(prog, n, device, mask=mask, before_values=values_ready)
         keys_out = {}
         for i, (oid, kid) in enumerate(prog.key_outputs):
             keys_out[i] = keys[prog.key_ids.index(kid)].reshape(G, 1)

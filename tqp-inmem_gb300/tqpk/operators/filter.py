@@ -8,7 +8,7 @@ from __future__ import annotations
 
 from ..ops import filter_mask
 from ..predicate import compile_filter
-from ..variable import make_like
+from ..variable import make_like, wait_ready
 
 
 def _require_gpu(gpu_enable):
@@ -26,6 +26,7 @@ def tqp_filter(gpu_enable, tensor_group, args, subquery_result, cpu_mem_pool, gp
     rows = first.tensor.size(0)
     cols = {k: v.tensor for k, v in input_columns.items()}
     pred = compile_filter(args["filter tree"], cols, subquery_result)
+    wait_ready(*input_columns.values())
     mask, _ = filter_mask(pred, rows, first.tensor.device)
     tensor_group[args["out mask id"]] = make_like(first, mask, "bool")
     return -1

@@ -27,7 +27,7 @@ import torch
 from .. import _lib as L
 from ..ops import compact, filter_mask, gather, join_build, join_probe, mark_rows
 from ..predicate import compile_filter
-from ..variable import make_like
+from ..variable import make_like, wait_ready
 from .filter import _require_gpu
 
 LEFT, RIGHT = 0, 1
@@ -54,7 +54,9 @@ def _side_mask(tensor_group, cols: List[int], mask_map: Dict[int, int], key: int
 def _pairs(tensors_left, tensors_right, left_key, right_key, condition_list, jtype, left_mask, right_mask):
     lk = tensors_left[left_key].tensor
     rk = tensors_right[right_key].tensor
+    wait_ready(tensors_left[left_key])
     b = join_build(lk, left_mask)
+    wait_ready(tensors_right[right_key])
     # with extra conditions every form starts from the key-equal pairs (hashjoin.py:100-108)
     bi, pi = join_probe(b, rk, right_mask, "inner" if condition_list else jtype)
     for cond in condition_list:                       # hashjoin.py:100-108
@@ -63,8 +65,10 @@ def _pairs(tensors_left, tensors_right, left_key, right_key, condition_list, jty
         cols = {}
         for cid in ids:
             if cid in tensors_left:
+                wait_ready(tensors_left[cid])
                 cols[cid] = gather([tensors_left[cid].tensor], bi)[0]
             else:
+                wait_ready(tensors_right[cid])
                 cols[cid] = gather([tensors_right[cid].tensor], pi)[0]
         pred = compile_filter(cond, cols)
         keep, _ = filter_mask(pred, int(bi.numel()), bi.device)
@@ -130,6 +134,7 @@ def _outputs(tensors_left, tensors_right, keys, jtype, bi, pi, return_global_ind
         bi = torch.empty(0, dtype=torch.int64, device=pi.device)
     lcols = [k for k in keys if k in tensors_left]
     rcols = [k for k in keys if k not in tensors_left]
+    wait_ready(*[tensors_left[k] for k in lcols], *[tensors_right[k] for k in rcols])
     lout = gather([tensors_left[k].tensor for k in lcols], bi, null_aware) if lcols else []
     rout = gather([tensors_right[k].tensor for k in rcols], pi) if rcols else []
     res, li, ri = [], iter(lout), iter(rout)

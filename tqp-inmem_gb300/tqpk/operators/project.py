@@ -9,7 +9,7 @@ from __future__ import annotations
 
 from ..expr import compile_projection, is_trivial_projection
 from ..ops import project
-from ..variable import make_like, torch_to_type
+from ..variable import make_like, torch_to_type, wait_ready
 from .filter import _require_gpu
 
 
@@ -23,6 +23,7 @@ def tqp_project(gpu_enable, tensor_group, args, cpu_mem_pool, gpu_mem_pool, name
         first = next(iter(inputs.values()))
         rows = first.tensor.size(0)
         prog = compile_projection(args["used expr"], {k: v.tensor for k, v in inputs.items()}, derived=True)
+        wait_ready(*inputs.values())
         outs = project(prog, rows, first.tensor.device)
         for i, out_id in enumerate(args["materialized out"]):
             tensor_group[out_id] = make_like(first, outs[i], torch_to_type(outs[i].dtype))

@@ -15,7 +15,7 @@ from __future__ import annotations
 import torch
 
 from ..ops import argsort_stable, gather, gather_rows, string_words, topk_stable
-from ..variable import make_like
+from ..variable import make_like, wait_ready
 from .filter import _require_gpu
 
 
@@ -29,6 +29,7 @@ def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
     if k0.numel() * k0.element_size() >= 8_000_000_000:   # sort.py:22-23, 38-39
         raise RuntimeError("sort input exceeds in-memory limit")
     device = k0.device
+    wait_ready(*[tensor_group[k] for k in key_ids])
     perm = torch.arange(rows, device=device, dtype=torch.int64)
     steps = []
     for key_id, desc in zip(reversed(key_ids), reversed(key_descs)):
@@ -47,15 +48,22 @@ def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
             perm = argsort_stable(key, desc, perm)
     if limit is not None:
         perm = perm[:limit]
+    wait_ready(*[tensor_group[k] for k in input_ids])
+    flat, shapes = [], []
     for key_id in input_ids:                              # sort.py:44-54
         t = tensor_group[key_id].tensor
         if not t.is_cuda:
             t = t.to(device)
-        if t.dim() == 2 and t.shape[1] == 1:
-            out = gather([t.reshape(-1)], perm)[0].reshape(-1, 1)
-        elif t.dim() == 2:
-            out = gather_rows(t, perm)
-        else:
-            out = gather([t], perm)[0]
+        flat.append(t)
+    # every 1-D (or [N, 1]) column in one multi-column gather launch; [N, w] rows by row gather
+    one_d = [i for i, t in enumerate(flat) if t.dim() == 1 or (t.dim() == 2 and t.shape[1] == 1)]
+    outs = [None] * len(flat)
+    if one_d:
+        for i, o in zip(one_d, gather([flat[i].reshape(-1) for i in one_d], perm)):
+            outs[i] = o.reshape(-1, 1) if flat[i].dim() == 2 else o
+    for i, t in enumerate(flat):
+        if outs[i] is None:
+            outs[i] = gather_rows(t, perm)
+    for key_id, out in zip(input_ids, outs):
         tensor_group[key_id] = make_like(tensor_group[key_id], out, tensor_group[key_id].tensor_type)
     return rows

@@ -115,12 +115,13 @@ def compact(cols: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = None,
 
 # ---------------------------------------------------------------- (d) group-by
 def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor] = None,
-            pred: Optional[CompiledPredicate] = None):
-    """Runs the compiled aggregate; returns (key columns [G], {out id: column}, G)."""
+            pred: Optional[CompiledPredicate] = None, before_values=None):
+    """Runs the compiled aggregate; returns (key columns [G], {out id: column}, G).
+    before_values, when given, is called after the plan (which reads only the keys and
+    the mask) and before the first kernel that reads the value columns."""
     lib = L.load()
     _check_cuda(mask, *prog.tensors)
     s = _stream(device)
-    fill_masks(prog.masks, device)
     plan = L.GbPlan()
     scratch = _ws(256, device)
     pp = C.byref(pred.struct) if pred is not None else None
@@ -129,6 +130,9 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
             "tqpk_groupby_plan")
     ws = _ws(plan.ws_bytes, device)
     groups = C.c_int64(0)
+    if before_values is not None:
+        before_values()
+    fill_masks(prog.masks, device)
     from . import jit
     from .predicate import has_strings
     use_jit = (jit.available() and plan.mode != L.GB_HASH and plan.n_rows > 0 and n > 0

@@ -20,12 +20,13 @@ class Variable:
     """variable.py:9-43"""
 
     def __init__(self, tensor, tensor_type: str, backing_mem_ptr=None, var_state="cpu resident",
-                 is_sorted: bool = False):
+                 is_sorted: bool = False, ready=None):
         self.tensor = tensor
         self.tensor_type = tensor_type
         self.state = var_state
         self.backing_mem_ptr = backing_mem_ptr
         self.is_sorted = is_sorted
+        self.ready = ready      # CUDA event after which the tensor's data is on the device (None: already)
 
     def __repr__(self):
         return f"Variable (tensor size = {self.tensor.shape} ({self.tensor.dtype}), tensor type = '{self.tensor_type}')"
@@ -40,6 +41,18 @@ class Variable:
         if self.tensor.dim() == 0:
             self.tensor = self.tensor.unsqueeze(0)
         assert self.tensor.dim() == 1
+
+
+def wait_ready(*variables) -> None:
+    """Orders the current stream after the copies that fill these columns: a column still
+    arriving from the host (a Variable with a `ready` event, e.g. one copied on a side
+    stream) is waited for right before the first kernel that reads it, so the operators
+    before it overlap the copy.  Columns without the attribute (the reference's Variable)
+    are ready."""
+    for v in variables:
+        ev = getattr(v, "ready", None) if v is not None else None
+        if ev is not None:
+            torch.cuda.current_stream(v.tensor.device).wait_event(ev)
 
 
 def torch_to_type(dtype) -> str:

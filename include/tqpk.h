@@ -242,7 +242,9 @@ int tqpk_groupby_emit(const tqpk_groupby_spec* h_spec, const tqpk_gb_plan* h_pla
  * payload perm_in[i]; writes the sorted permutation (int64) to d_perm_out.
  * One call is one iteration of sort.py:26-35's key loop.  descending keeps
  * ties in input order (torch.sort(stable=True, descending=True)).
- * Float keys: -0.0 sorts equal to +0.0 and NaN sorts as the largest value. */
+ * Float keys: -0.0 sorts equal to +0.0 and NaN sorts as the largest value.
+ * n <= 2048 sorts in one CTA without a workspace (d_ws may be NULL) and
+ * without a host synchronisation; larger sorts synchronise twice.          */
 size_t tqpk_sort_workspace_bytes(int64_t n);
 int tqpk_argsort_stable(const void* d_keys, int32_t key_dtype, int32_t descending,
                         const int64_t* d_perm_in, int64_t n, int64_t* d_perm_out, void* d_ws,

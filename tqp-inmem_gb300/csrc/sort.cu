@@ -229,17 +229,18 @@ extern "C" size_t tqpk_sort_workspace_bytes(int64_t n) { return sort_ws_bytes(n 
 
 extern "C" int tqpk_argsort_stable(const void* d_keys, int32_t dt, int32_t desc, const int64_t* d_perm_in, int64_t n,
                                    int64_t* d_perm_out, void* ws, size_t ws_bytes, tqpk_stream stream) {
-  if (n < 0 || (n > 0 && (!d_keys || !d_perm_out || !ws))) return TQPK_EINVAL;
+  if (n < 0 || (n > 0 && (!d_keys || !d_perm_out))) return TQPK_EINVAL;
   if (!dtype_size(dt)) return TQPK_EDTYPE;
   if (n == 0) return TQPK_OK;
-  if (ws_bytes < sort_ws_bytes(n)) return TQPK_ENOMEM;
-  if ((n + kSortTile - 1) / kSortTile > INT32_MAX) return TQPK_EUNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (n <= kSmallSort) {
+  if (n <= kSmallSort) {   // no workspace needed
     k_sort_small<<<1, 1024, 0, s>>>(d_keys, dt, desc ? 1 : 0, d_perm_in, (int)n, d_perm_out);
     TQPK_CHECK_LAUNCH();
     return TQPK_OK;
   }
+  if (!ws) return TQPK_EINVAL;
+  if (ws_bytes < sort_ws_bytes(n)) return TQPK_ENOMEM;
+  if ((n + kSortTile - 1) / kSortTile > INT32_MAX) return TQPK_EUNSUPPORTED;
   const int64_t* res = nullptr;
   int rc = sort_pairs(d_keys, dt, desc ? 1 : 0, d_perm_in, n, ws, ws_bytes, s, &res);
   if (rc) return rc;

@@ -30,7 +30,7 @@ def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
         raise RuntimeError("sort input exceeds in-memory limit")
     device = k0.device
     wait_ready(*[tensor_group[k] for k in key_ids])
-    perm = torch.arange(rows, device=device, dtype=torch.int64)
+    perm = None                                           # identity until the first pass
     steps = []
     for key_id, desc in zip(reversed(key_ids), reversed(key_descs)):
         col = tensor_group[key_id].tensor
@@ -46,6 +46,8 @@ def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
             perm = topk_stable(key, limit, desc, perm)
         else:
             perm = argsort_stable(key, desc, perm)
+    if perm is None:                                      # no key columns
+        perm = torch.arange(rows, device=device, dtype=torch.int64)
     if limit is not None:
         perm = perm[:limit]
     wait_ready(*[tensor_group[k] for k in input_ids])

@@ -207,10 +207,11 @@ def argsort_stable(keys: torch.Tensor, descending: bool = False,
     out = torch.empty(n, dtype=torch.int64, device=keys.device)
     if n == 0:
         return out
-    ws = _ws(lib.tqpk_sort_workspace_bytes(n), keys.device)
+    ws = _ws(lib.tqpk_sort_workspace_bytes(n), keys.device) if n > 2048 else None   # small sorts: one CTA
     L.check(lib.tqpk_argsort_stable(keys.data_ptr(), code_of(keys.dtype), int(bool(descending)),
                                     perm_in.data_ptr() if perm_in is not None else None, n, out.data_ptr(),
-                                    ws.data_ptr(), ws.numel(), _stream(keys.device)), "tqpk_argsort_stable")
+                                    ws.data_ptr() if ws is not None else None, ws.numel() if ws is not None else 0,
+                                    _stream(keys.device)), "tqpk_argsort_stable")
     return out
 
 

@@ -151,3 +151,43 @@ def test_expression_forms_compile_case_year_and_post_arithmetic():
     assert ok, log[:2000]
     with pytest.raises(NotImplementedError):          # fused pipelines keep to plain calls
         compile_aggregate(args["aggregate"], cols)
+
+
+def test_fused_sum_of_product_and_kernel_shape_key():
+    """A float sum whose value is a product read nowhere else becomes one FMA in the private
+    group-by; the generated-kernel memo key ignores pointers and comparison literals but not
+    the predicate's shape or the expression constants."""
+    d = _lineitem()
+    prog = compile_aggregate({"is partial": False, "keys": ["flag#5", "status#6"], "input ids": [1, 2, 3, 4, 5, 6],
+                              "results": LINEITEM_AGG, "out agg ids": [201, 203, 207, 209, 210, 208]}, d)
+    fused = jit._fusable_products(prog.spec)
+    # sum(price * (1 - discount)) is fused; its product is not used by another accumulator
+    assert len(fused) == 1
+    (a, (x, y)), = fused.items()
+    assert prog.spec.expr[prog.spec.accs[a].reg].op == L.X_MUL
+    plan = L.GbPlan()
+    plan.mode, plan.threads, plan.slots = L.GB_DENSE_PRIVATE, 128, 6
+    plan.key_stride[0], plan.key_stride[1] = 2, 1
+    src, *_ = jit.groupby_source(prog.spec, None, plan)
+    assert src.count("__fma_rn(") == 1
+    p1 = compile_filter([["ship_date#7", "<=", "2470"]], {7: d[7]})
+    p2 = compile_filter([["ship_date#7", "<=", "100"]], {7: d[7]})
+    p3 = compile_filter([["ship_date#7", ">", "2470"]], {7: d[7]})
+    k1, k2, k3 = (jit._shape_key(prog.spec, p.struct, plan) for p in (p1, p2, p3))
+    assert k1 == k2 and k1 != k3
+    d2 = {c: t.clone() for c, t in d.items()}
+    prog2 = compile_aggregate({"is partial": False, "keys": ["flag#5", "status#6"], "input ids": [1, 2, 3, 4, 5, 6],
+                               "results": LINEITEM_AGG, "out agg ids": [201, 203, 207, 209, 210, 208]}, d2)
+    assert jit._shape_key(prog2.spec, p1.struct, plan) == k1          # other column buffers, same kernel
+    plan2 = L.GbPlan.from_buffer_copy(plan)
+    plan2.n_rows, plan2.ws_bytes = 12345, 999
+    assert jit._shape_key(prog.spec, p1.struct, plan2) == k1
+    plan2.slots = 7
+    assert jit._shape_key(prog.spec, p1.struct, plan2) != k1
+
+
+def test_wait_ready_without_events_is_a_no_op():
+    from tqpk.variable import Variable, wait_ready
+    v = Variable(torch.zeros(3), "float")
+    assert v.ready is None
+    wait_ready(v, None, type("RefVar", (), {"tensor": torch.zeros(1)})())

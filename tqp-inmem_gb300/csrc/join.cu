@@ -192,18 +192,39 @@ __global__ void __launch_bounds__(kBlock) k_join_probe(JoinDir D, const void* pk
   }
   __syncthreads();
   const int64_t base = (base_ptr ? *base_ptr : 0);
-  int64_t pos = base + (int64_t)s_excl + excl;
+  const bool one_per_row = JT != TQPK_JT_INNER || (D.mode == TQPK_JOIN_DIRECT && D.unique);   // block-uniform
+  if (one_per_row) {
+    // at most one output per row, so the tile's outputs fit kTile slots: each thread places its
+    // outputs at its block offset in shared memory, then the block writes them contiguously
+    // (coalesced) instead of every lane storing its own run
+    __shared__ int64_t s_out[kTile];
+    const int64_t gbase = base + (int64_t)s_excl;
+    int64_t lp = excl;
 #pragma unroll
-  for (int j = 0; j < kItems; ++j) {
-    const int64_t c = cnt[j];
-    for (int64_t t = 0; t < c; ++t, ++pos) {
-      if (pos >= capacity) continue;
-      out_p[pos] = r0 + j;
-      if (JT == TQPK_JT_INNER) {
-        const int64_t b = (D.mode == TQPK_JOIN_DIRECT && D.unique) ? first[j] : D.csr[first[j] + t];
-        out_b[pos] = b;
-      } else if (JT == TQPK_JT_ANTI && out_b) {
-        out_b[pos] = TQPK_NULL_INDEX;
+    for (int j = 0; j < kItems; ++j)
+      if (cnt[j]) s_out[lp++] = r0 + j;
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < total; i += kBlock)
+      if (gbase + i < capacity) out_p[gbase + i] = s_out[i];
+    if (JT == TQPK_JT_INNER || (JT == TQPK_JT_ANTI && out_b)) {
+      __syncthreads();
+      lp = excl;
+#pragma unroll
+      for (int j = 0; j < kItems; ++j)
+        if (cnt[j]) s_out[lp++] = (JT == TQPK_JT_INNER) ? first[j] : (int64_t)TQPK_NULL_INDEX;
+      __syncthreads();
+      for (int64_t i = threadIdx.x; i < total; i += kBlock)
+        if (gbase + i < capacity) out_b[gbase + i] = s_out[i];
+    }
+  } else {
+    int64_t pos = base + (int64_t)s_excl + excl;
+#pragma unroll
+    for (int j = 0; j < kItems; ++j) {
+      const int64_t c = cnt[j];
+      for (int64_t t = 0; t < c; ++t, ++pos) {
+        if (pos >= capacity) continue;
+        out_p[pos] = r0 + j;
+        if (JT == TQPK_JT_INNER) out_b[pos] = D.csr[first[j] + t];
       }
     }
   }

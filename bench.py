@@ -376,7 +376,8 @@ class StarJoin:
         from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
         from tqpk.variable import Variable
         if not hasattr(self, "staged"):
-            self.staged = StagedInputs(self.host, self.dev, self.types, (32, 31, 41, 42, 43, 44, 51, 52, 61))
+            # keys and dimension tables first, the fact value columns last: the joins run while they copy
+            self.staged = StagedInputs(self.host, self.dev, self.types, (32, 31, 41, 42, 51, 52, 61, 43, 44))
         tg = self.staged.start()
 
         def f(tg, a):

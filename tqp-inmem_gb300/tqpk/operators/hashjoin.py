@@ -121,8 +121,37 @@ def join_kernel_new(gpu_enable, tensors_left, tensors_right, left_key, right_key
                     left_global_idx, right_global_idx)
 
 
+_side = {}
+
+
+def _pending(v) -> bool:
+    """A column whose host copy has not finished yet (its `ready` event is not complete)."""
+    ev = getattr(v, "ready", None)
+    return ev is not None and not ev.query()
+
+
+def _gather_when_ready(v, idx, null_aware):
+    """col[idx] on a side stream after the column's copy and this stream's work so far (the
+    indices); returns the output and the event after the gather."""
+    dev = idx.device
+    side = _side.get(dev.index)
+    if side is None:
+        side = _side[dev.index] = torch.cuda.Stream(dev)
+    main = torch.cuda.current_stream(dev)
+    side.wait_stream(main)
+    side.wait_event(v.ready)
+    with torch.cuda.stream(side):
+        o = gather([v.tensor], idx, null_aware)[0]
+        ev = torch.cuda.Event()
+        ev.record(side)
+    o.record_stream(main)            # read on the caller's stream after the event
+    idx.record_stream(side)
+    v.tensor.record_stream(side)
+    return o, ev
+
+
 def _outputs(tensors_left, tensors_right, keys, jtype, bi, pi, return_global_index=False, lg=None, rg=None,
-             left_rows=None, right_rows=None):
+             left_rows=None, right_rows=None, ready_out=None):
     null_aware = False
     if jtype == "right-outer":
         n_pairs = int((bi != L.NULL_INDEX).sum().item()) if bi.numel() else 0
@@ -134,9 +163,27 @@ def _outputs(tensors_left, tensors_right, keys, jtype, bi, pi, return_global_ind
         bi = torch.empty(0, dtype=torch.int64, device=pi.device)
     lcols = [k for k in keys if k in tensors_left]
     rcols = [k for k in keys if k not in tensors_left]
-    wait_ready(*[tensors_left[k] for k in lcols], *[tensors_right[k] for k in rcols])
-    lout = gather([tensors_left[k].tensor for k in lcols], bi, null_aware) if lcols else []
-    rout = gather([tensors_right[k].tensor for k in rcols], pi) if rcols else []
+    # columns still arriving are gathered on a side stream once they land; their outputs carry
+    # the gather's event, so this join (and whatever the caller queues next) does not wait here
+    late_l = [k for k in lcols if _pending(tensors_left[k])]
+    late_r = [k for k in rcols if _pending(tensors_right[k])]
+    now_l = [k for k in lcols if k not in late_l]
+    now_r = [k for k in rcols if k not in late_r]
+    wait_ready(*[tensors_left[k] for k in now_l], *[tensors_right[k] for k in now_r])
+    out = {}
+    if now_l:
+        out.update(zip(now_l, gather([tensors_left[k].tensor for k in now_l], bi, null_aware)))
+    if now_r:
+        out.update(zip(now_r, gather([tensors_right[k].tensor for k in now_r], pi)))
+    events = {}
+    for k in late_l:
+        out[k], events[k] = _gather_when_ready(tensors_left[k], bi, null_aware)
+    for k in late_r:
+        out[k], events[k] = _gather_when_ready(tensors_right[k], pi, False)
+    if ready_out is not None:
+        ready_out.update(events)
+    lout = [out[k] for k in lcols]
+    rout = [out[k] for k in rcols]
     res, li, ri = [], iter(lout), iter(rout)
     for k in keys:                                     # hashjoin.py:161-172
         if k in tensors_left:
@@ -177,7 +224,10 @@ def join_vortex(gpu_enable, tensor_group, args, leftcol, rightcol, condition_lis
         np_rows = int(pi.numel())
     else:
         np_rows = int(masks[RIGHT].sum().item()) if masks[RIGHT] is not None else tr[rightcol].tensor.shape[0]
-    outs = _outputs(tl, tr, join_output, type, bi, pi, left_rows=nb_rows, right_rows=np_rows)
+    late = {}
+    outs = _outputs(tl, tr, join_output, type, bi, pi, left_rows=nb_rows, right_rows=np_rows, ready_out=late)
     for i, k in enumerate(join_output):                # hashjoin.py:234-238
         tensor_group[k] = make_like(tensor_group[k], outs[i], tensor_group[k].tensor_type)
+        if k in late:                                  # gathered on a side stream after a late input
+            tensor_group[k].ready = late[k]
     return next(iter(tensor_group.values())).tensor.size(0)

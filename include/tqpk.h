@@ -424,6 +424,13 @@ int tqpk_pipeline_join_tables(void* d_ws, size_t ws_bytes, int64_t key_min, int6
 int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64_t n, const tqpk_predicate* h_pred,
                          const void* d_payload, int32_t payload_dtype, int64_t key_min, int64_t slots, int32_t empty,
                          int32_t fail_value, int32_t* d_dir, int32_t* d_err, tqpk_stream stream);
+/* Snowflake chain B -> C: an entry of d_dir that names a key of the next
+ * table's domain (B's directory holding C keys) keeps it only when the next
+ * directory has a row at that key (d_next[v - next_min] >= 0, e.g. C's row
+ * directory with C's filter applied), else becomes fail_value; a probe through
+ * the composed directory then needs no lookup in the next one.              */
+int tqpk_directory_compose(int32_t* d_dir, int64_t slots, const int32_t* d_next, int64_t next_min,
+                           int64_t next_slots, int32_t empty, int32_t fail_value, tqpk_stream stream);
 /* The k (<= 256) best groups of a dense slot table (sum[s], count[s] != 0
  * marks a group) ordered by sum (descending when `descending`), ties to the
  * smaller key: the "sort by aggregate + limit" of operators/sort.py:6-58 over

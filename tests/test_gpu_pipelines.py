@@ -122,6 +122,32 @@ def test_star_pipeline_vs_oracle(monkeypatch, jit_on, scale, k):
     np.testing.assert_array_equal(cnts, ec)
 
 
+@pytest.mark.parametrize("jit_on", ["1", "0"])
+def test_star_pipeline_with_missing_dimension_rows(monkeypatch, jit_on):
+    """C holds only a third of the keys B points at, and B misses keys the fact table names:
+    the composed B -> C directory (generated path) and the three-hop probe (library path)
+    drop the same rows as the oracle's joins."""
+    monkeypatch.setenv("TQPK_JIT", jit_on)
+    import bench
+    from tqpk.pipeline import StarAggTopK
+    w = bench.StarJoin(scale=0.02)
+    rng = np.random.default_rng(3)
+    c_keys = w.cols[61]
+    w.cols[61] = c_keys[rng.random(c_keys.size) < 0.33]
+    b_keep = rng.random(w.cols[51].size) < 0.8
+    w.cols[51], w.cols[52] = w.cols[51][b_keep], w.cols[52][b_keep]
+    ek, ev, ec = w.oracle()
+    d = {c: torch.from_numpy(a).cuda() for c, a in w.cols.items()}
+    dom = lambda a: (int(a.min()), int(a.max()))  # noqa: E731
+    p = StarAggTopK(d[41], d[42], {43: d[43], 44: d[44]}, None, w.value_tree, d[31], {32: d[32]},
+                    w.fa["filter tree"], dom(w.cols[31]), d[51], d[52], dom(w.cols[51]), d[61], dom(w.cols[61]), k=100)
+    p.run()
+    keys, vals, cnts, groups = p.result()
+    np.testing.assert_array_equal(keys, ek)
+    assert_f64_close(vals, ev)
+    np.testing.assert_array_equal(cnts, ec)
+
+
 @pytest.mark.parametrize("k", [200, 256, 257, 1000])
 def test_topk_stable_large_k(k):
     from tqpk.ops import topk_stable

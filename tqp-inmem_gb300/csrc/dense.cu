@@ -104,6 +104,30 @@ extern "C" int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64
   return TQPK_OK;
 }
 
+// dir[i] (a key of the next table's domain) keeps its value only when the next
+// table's directory has a row there (next[v - next_min] >= 0); otherwise it
+// becomes fail_value.  `empty` and `fail_value` entries stay as they are.
+__global__ void k_dir_compose(int* __restrict__ dir, int64_t n, const int* __restrict__ next, int64_t next_min,
+                              int64_t next_slots, int empty, int fail_value) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int v = dir[i];
+    if (v == empty || v == fail_value) continue;
+    const int64_t k = (int64_t)v - next_min;
+    if (k < 0 || k >= next_slots || next[k] < 0) dir[i] = fail_value;
+  }
+}
+
+extern "C" int tqpk_directory_compose(int32_t* d_dir, int64_t slots, const int32_t* d_next, int64_t next_min,
+                                      int64_t next_slots, int32_t empty, int32_t fail_value, tqpk_stream stream) {
+  if (slots < 0 || next_slots < 0 || (slots > 0 && !d_dir) || (next_slots > 0 && !d_next)) return TQPK_EINVAL;
+  if (empty == fail_value) return TQPK_EINVAL;
+  if (slots == 0) return TQPK_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  k_dir_compose<<<grid_for(slots, 8), kBlock, 0, s>>>(d_dir, slots, d_next, next_min, next_slots, empty, fail_value);
+  TQPK_CHECK_LAUNCH();
+  return TQPK_OK;
+}
+
 extern "C" size_t tqpk_dense_topk_workspace_bytes(int32_t k) {
   k = std::max(1, std::min(k, kDenseMaxK));
   return 1024 + align_up((size_t)k * 8, 256) + 2 * align_up(topk_cand_entries(k) * 8, 256) + 1024;

@@ -942,14 +942,16 @@ def join_probe_args(a: "_Args", spec, pred, bpred, fk, np_: int, key_min: int, s
 
 # ---------------------------------------------------------------------------- star probe
 def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_blocks: int = 0,
-                      early_fb: bool = False, stream_cs: bool = False) -> Tuple[str, str]:
+                      early_fb: bool = False, stream_cs: bool = False, composed: bool = False) -> Tuple[str, str]:
     """CUDA source of the star probe: fact -> A (row directory, A predicate through the
     row) -> B (directory of the C foreign key) -> C (row directory), then FP64 sum and
     count per C slot, computed warp-densely over the matched rows (_dense_tail).
     Directories: A and C hold row indices (negative = none), B holds the C key
     (INT_MIN = none).  early_fb loads the fkB column together with fkA, so the
     B lookup does not wait for a second column round trip after the A lookup;
-    stream_cs loads the fact columns with evict-first hints."""
+    stream_cs loads the fact columns with evict-first hints; composed means B's directory
+    already holds only C keys that have a C row (tqpk_directory_compose), so the C lookup
+    is left out of the chain."""
     S = spec
     pcols, pexpr = _pred_code(fpred, "p") if fpred is not None else ([], "true")
     ecols, elines = _expr_code(S, val_reg + 1, "c")
@@ -1023,11 +1025,13 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
             "        if (fc == (int)0x80000000 || k[u][j] < 0 || k[u][j] >= c_slots) m[u] &= ~(1u << j);",
             "      }",
             "    }",
-            "#pragma unroll",
-            f"    for (int u = 0; u < {U}; ++u)",
-            "#pragma unroll",
-            "      for (int j = 0; j < 4; ++j)",
-            "        if (((m[u] >> j) & 1u) && __ldg(&dir_c[k[u][j]]) < 0) m[u] &= ~(1u << j);"]
+            ]
+    if not composed:
+        src += ["#pragma unroll",
+                f"    for (int u = 0; u < {U}; ++u)",
+                "#pragma unroll",
+                "      for (int j = 0; j < 4; ++j)",
+                "        if (((m[u] >> j) & 1u) && __ldg(&dir_c[k[u][j]]) < 0) m[u] &= ~(1u << j);"]
     src += _dense_tail(S, val_reg, ecols, elines, "nf", "k", ["atomicAdd(&cnt[slot], 1u);"], U=U)
     src += ["  }", "}"]
     return "\n".join(src), name

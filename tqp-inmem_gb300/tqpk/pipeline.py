@@ -201,6 +201,9 @@ class StarAggTopK:
         at build) and C, the C-key directory for B, the slot table and top-k scratch."""
         from . import jit
         (amn, amx), (bmn, bmx), (cmn, cmx) = self.doms
+        if cmn <= -(1 << 31) + 1:
+            # B's directory marks "no row" / "no C row" with the two smallest int32 values
+            raise NotImplementedError("C keys at the bottom of the int32 range are reserved as directory markers")
         dev = self.dev
         self.dir_a = torch.empty(amx - amn + 1, dtype=torch.int32, device=dev)
         self.dir_b = torch.empty(bmx - bmn + 1, dtype=torch.int32, device=dev)
@@ -210,8 +213,9 @@ class StarAggTopK:
         self.err = torch.zeros(3, dtype=torch.int32, device=dev)
         self.tws = torch.empty(self.lib.tqpk_dense_topk_workspace_bytes(self.k), dtype=torch.uint8, device=dev)
         # fkB loaded with fkA and evict-first column loads: 529 -> 507 us on the 59,986,052-row star join
+        # + B's directory composed with C's (no C lookup in the probe)
         src, name = jit.star_probe_source(self.prog.spec, self.value_reg, self.fpred.struct if self.fpred else None,
-                                          None, early_fb=True, stream_cs=True)
+                                          None, early_fb=True, stream_cs=True, composed=True)
         self._probe = jit.compile_kernel(src, name)
         fa, fb = self.t[0], self.t[1]
         a = jit._Args()
@@ -252,6 +256,8 @@ class StarAggTopK:
                       bmx - bmn + 1, INT_MIN, INT_MIN + 1, self.dir_b.data_ptr(), e + 4, s), "tqpk_directory_build")
         L.check(build(ck.data_ptr(), code_of(ck.dtype), ck.numel(), None, None, 0, cmn, cmx - cmn + 1, -1, -2,
                       self.dir_c.data_ptr(), e + 8, s), "tqpk_directory_build")
+        L.check(self.lib.tqpk_directory_compose(self.dir_b.data_ptr(), self.dir_b.numel(), self.dir_c.data_ptr(), cmn,
+                                                cmx - cmn + 1, INT_MIN, INT_MIN + 1, s), "tqpk_directory_compose")
         self.sum.zero_()
         self.cnt.zero_()
         jit.launch(self._probe, self._probe_grid, 256, 0, self._probe_args, s, L.KID_STAR_PROBE)

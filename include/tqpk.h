@@ -401,7 +401,10 @@ int tqpk_groupby_count(const tqpk_groupby_spec* h_spec, const tqpk_gb_plan* h_pl
                        tqpk_stream stream);
 void* tqpk_groupby_table(void* d_ws);
 /* The fused join pipeline run stage by stage (bit 0 reset + build, bit 1
- * probe, bit 2 top-k + emit), and the addresses of its tables.             */
+ * probe, bit 2 top-k + emit), and the addresses of its tables.  Bit 3 (with
+ * a caller-launched probe): the group sums start at -0.0 and carry the
+ * occupancy (the probe adds -0.0 values as +0.0 and writes no occupancy
+ * word); give it to the reset and the top-k stages alike.                  */
 int tqpk_pipeline_join_agg_topk_stages(int32_t stages, const void* d_build_keys, int32_t build_dtype, int64_t nb,
                                        const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max,
                                        const void* d_probe_fk, int32_t probe_dtype, int64_t np,

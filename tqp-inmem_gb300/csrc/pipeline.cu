@@ -188,6 +188,11 @@ extern "C" size_t tqpk_pipeline_join_agg_topk_workspace_bytes(int64_t key_min, i
   return pipe_bytes(key_max - key_min + 1, topk_grid());
 }
 
+__global__ void k_pl_fill_u64(uint64_t* p, int64_t n, uint64_t v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
 static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dtype, int64_t nb,
                          const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max, const void* d_probe_fk,
                          int32_t probe_dtype, int64_t np, const tqpk_predicate* h_probe_pred,
@@ -225,11 +230,18 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
   A.b_pvec = pred_vec_ok(h_build_pred) ? 1 : 0;
   A.p_pvec = pred_vec_ok(h_probe_pred) ? 1 : 0;
   A.v_pvec = spec_cols_vec(h_values) ? 1 : 0;
+  const bool sentinel = (stages & 8) != 0;   // occupancy carried by the sums (see DenseSumSource)
   if (stages & 1) {
   TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 32, s));
   TQPK_CUDA(cudaMemsetAsync(L.dir, 0xff, slots * 4, s));
-  TQPK_CUDA(cudaMemsetAsync(L.sum, 0, slots * 8, s));
-  TQPK_CUDA(cudaMemsetAsync(L.cnt, 0, slots * 4, s));
+  if (sentinel) {
+    k_pl_fill_u64<<<grid_for(slots, 4), kBlock, 0, s>>>(reinterpret_cast<uint64_t*>(L.sum), slots,
+                                                        DenseSumSource::kEmptySum);
+    TQPK_CHECK_LAUNCH();
+  } else {
+    TQPK_CUDA(cudaMemsetAsync(L.sum, 0, slots * 8, s));
+    TQPK_CUDA(cudaMemsetAsync(L.cnt, 0, slots * 4, s));
+  }
   if (nb > 0) {
     timing_before(KID_PIPE_BUILD, s);
     k_pl_build<<<grid_for((nb + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_build_pred), A, L.dir, L.err);
@@ -247,7 +259,7 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
   if (stages & 4) {
     TQPK_CUDA(cudaMemsetAsync(L.top_count + 1, 0, 8, s));   // the top-k cut of this run
     TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 8, s));          // the group count the top-k pass accumulates
-    DenseSumSource src{L.sum, L.cnt, slots, A.desc};
+    DenseSumSource src{L.sum, sentinel ? nullptr : L.cnt, slots, A.desc};
     TopkOut O{L.top_idx, L.top_count, L.cand_key, L.cand_slot, L.done, L.groups,
               reinterpret_cast<unsigned long long*>(L.top_count + 1)};   // hdr[6..7], zeroed with the header
     timing_before(KID_PIPE_TOPK, s);

@@ -89,9 +89,12 @@ struct WarpList {
 // Occupied slots of a dense group table, keyed by their float64 sum.
 struct DenseSumSource {
   const double* sum;
-  const unsigned* cnt;   // occupancy: non-zero for groups that received a row
+  const unsigned* cnt;   // occupancy: non-zero for groups that received a row; NULL: the sums
+                         // start at -0.0 and every added value is +0.0 or non-zero, so a slot is
+                         // occupied exactly when its bits are no longer those of -0.0
   int64_t n;
   int desc;
+  static constexpr uint64_t kEmptySum = 0x8000000000000000ull;
   __device__ __forceinline__ uint64_t order_key(double v) const {
     if (v == 0.0) v = 0.0;
     uint64_t b = d2u(v);
@@ -100,8 +103,15 @@ struct DenseSumSource {
     return desc ? ~u : u;
   }
   __device__ __forceinline__ bool get(int64_t i, uint64_t& k) const {
-    if (i >= n || __ldcg(&cnt[i]) == 0) return false;   // L2 loads: the table may have been written
-    k = order_key(__ldcg(&sum[i]));                      // earlier in the same launch by other CTAs
+    if (i >= n) return false;
+    if (!cnt) {
+      const double v = __ldcg(&sum[i]);
+      if (d2u(v) == kEmptySum) return false;
+      k = order_key(v);
+      return true;
+    }
+    if (__ldcg(&cnt[i]) == 0) return false;   // L2 loads: the table may have been written
+    k = order_key(__ldcg(&sum[i]));           // earlier in the same launch by other CTAs
     return true;
   }
   // Slots i0..i0+3 (i0 % 4 == 0): the occupancy and sum loads are issued
@@ -110,6 +120,23 @@ struct DenseSumSource {
   __device__ __forceinline__ unsigned get4(int64_t i0, uint64_t* k) const {
     unsigned c[4];
     double v[4];
+    if (!cnt) {
+      if (i0 + 4 <= n && (reinterpret_cast<uintptr_t>(sum) & 15u) == 0) {
+        const double2 a = __ldcg(reinterpret_cast<const double2*>(sum + i0));
+        const double2 b = __ldcg(reinterpret_cast<const double2*>(sum + i0 + 2));
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = (i0 + q < n) ? __ldcg(&sum[i0 + q]) : u2d(kEmptySum);
+      }
+      unsigned ok = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        k[q] = order_key(v[q]);
+        ok |= (d2u(v[q]) != kEmptySum ? 1u : 0u) << q;
+      }
+      return ok;
+    }
     if (i0 + 4 <= n && ((reinterpret_cast<uintptr_t>(cnt) | reinterpret_cast<uintptr_t>(sum)) & 15u) == 0) {
       const uint4 cc = __ldcg(reinterpret_cast<const uint4*>(cnt + i0));
       const double2 a = __ldcg(reinterpret_cast<const double2*>(sum + i0));

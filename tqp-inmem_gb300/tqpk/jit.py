@@ -554,7 +554,7 @@ def _gather_pred(pred, prefix: str, lits: str, ptr_pfx: str, row: str, live: str
 
 
 def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[str], U: int = 2,
-                smem_vals: Optional[Dict[int, str]] = None) -> List[str]:
+                smem_vals: Optional[Dict[int, str]] = None, neg_zero_as_zero: bool = False) -> List[str]:
     """Warp-dense value pass: the warp's matched rows (queued as row offsets and
     slots in shared memory) are spread over all 32 lanes, so each FP64
     instruction and atomic runs with full lanes instead of the ~1 in 4 a
@@ -589,7 +589,12 @@ def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[st
             lines.append(f"      const {t} Cs{c} = __ldg((const {t}*)cp{c} + row);")
     for l in elines:
         lines.append("      " + re.sub(r"\bc(\d+)\.v\[j\]", r"Cs\1", l))
-    lines.append(f"      atomicAdd(&sum[slot], (double)r{val_reg});")
+    if neg_zero_as_zero:     # the sums start at -0.0 (the empty marker); add a -0.0 value as +0.0
+        lines.append(f"      const double vz = (double)r{val_reg};")
+        lines.append("      atomicAdd(&sum[slot], __double_as_longlong(vz) == (long long)0x8000000000000000ull "
+                     "? 0.0 : vz);")
+    else:
+        lines.append(f"      atomicAdd(&sum[slot], (double)r{val_reg});")
     lines += ["      " + x for x in extra]
     lines += ["    }", "    __syncwarp();"]
     return lines
@@ -629,7 +634,8 @@ def _stage_values(S, ecols, rows: int, n: str) -> Tuple[List[str], List[str], Di
 
 
 def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, min_blocks: int = 0,
-                      stream_cs: bool = False, stage_vals: bool = False) -> Tuple[str, str]:
+                      stream_cs: bool = False, stage_vals: bool = False, occ_sentinel: bool = False
+                      ) -> Tuple[str, str]:
     """CUDA source of the fused probe + aggregate (directory lookup, value, FP64 sum, occupancy).
 
     The directory holds build row indices (negative = no row).  `bpred`, when
@@ -641,7 +647,8 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
     resident CTAs per SM (__launch_bounds__ register cap); stream_cs loads the
     probe columns with evict-first hints; stage_vals copies the value columns of
     every row to shared memory with cp.async at the top of the iteration (the
-    value gather after the lookup leaves the dependent chain)."""
+    value gather after the lookup leaves the dependent chain); occ_sentinel writes no
+    occupancy word (the sums start at -0.0 and carry it; pipeline stage bit 3)."""
     S = spec
     pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
     ecols, elines = _expr_code(S, val_reg + 1, "c")
@@ -704,7 +711,8 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
                 f"        if (((m[u] >> j) & 1u) && !({gexpr})) m[u] &= ~(1u << j);", "    }"]
     if stage_vals:
         src += ["    cp_async_wait_all();", "    __syncwarp();"]
-    src += _dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"], U=U, smem_vals=smem_vals)
+    src += _dense_tail(S, val_reg, ecols, elines, "np", "sl", [] if occ_sentinel else ["occ[slot] = 1u;"], U=U,
+                       smem_vals=smem_vals, neg_zero_as_zero=occ_sentinel)
     src += ["  }", "}"]
     return "\n".join(src), name
 

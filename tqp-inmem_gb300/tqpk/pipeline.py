@@ -87,7 +87,7 @@ class JoinAggTopK:
                 # value columns staged by cp.async + evict-first probe columns: 42.3-42.7 -> 41.4 us
                 # on the 6,001,215-row probe (measured through this pipeline's timing)
                 src, name = jit.join_probe_source(self.prog.spec, self.value_reg, pp, stream_cs=True,
-                                                  stage_vals=True)
+                                                  stage_vals=True, occ_sentinel=True)
             self._probe_handle = jit.compile_kernel(src, name)
             d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
             L.check(self.lib.tqpk_pipeline_join_tables(self.ws.data_ptr(), self.ws.numel(), self.key_min,
@@ -114,9 +114,10 @@ class JoinAggTopK:
         from .predicate import has_strings
         if (jit.available() and jit.probe_supported(code_of(self.pk.dtype)) and self.pk.numel() > 0
                 and not has_strings(self.ppred.struct if self.ppred else None)):
-            self._stages(1, s)
+            sent = 0 if self._tma_ok() else 8      # the generated register probe keeps occupancy in the sums
+            self._stages(1 | sent, s)
             self._jit_probe(s)
-            self._stages(4, s)
+            self._stages(4 | sent, s)
         else:
             self._stages(7, s)
 

@@ -91,6 +91,29 @@ def test_join_probe_staged_and_plain_paths(monkeypatch, tma, nb, np_rows, dtype)
     assert_f64_close(vals, ev)
 
 
+def test_join_pipeline_zero_sums_still_count_as_groups():
+    """Every value is +0.0 or -0.0, so every matched group sums to zero: the groups are told
+    apart from empty slots by occupancy alone (the sums start at -0.0 in the generated path and
+    a -0.0 value is added as +0.0), the count of groups and the top-10 (ties by key) match."""
+    from tqpk.pipeline import JoinAggTopK
+    rng = np.random.default_rng(8)
+    nb, np_rows = 5000, 40_000
+    cols = {11: (rng.permutation(nb) + 1).astype(np.int32), 12: rng.integers(0, 2557, nb).astype(np.int32),
+            21: rng.integers(1, nb + 3, np_rows).astype(np.int32), 22: rng.integers(0, 2557, np_rows).astype(np.int32),
+            23: np.where(rng.random(np_rows) < 0.5, -0.0, 0.0), 24: rng.integers(0, 11, np_rows) / 100.0}
+    f1, f2 = [["bd#12", "<", "1170"]], [["pd#22", ">", "1170"]]
+    d = {c: torch.from_numpy(a).cuda() for c, a in cols.items()}
+    p = JoinAggTopK(d[11], 1, nb, d[21], {12: d[12]}, f1, {22: d[22], 23: d[23], 24: d[24]}, f2,
+                    [["p#23", "*", ["1.0", "-", "d#24"]]], k=10)
+    p.run()
+    keys, vals, groups = p.result()
+    ek, ev, eg = _oracle_join(cols, f1, f2, 10)
+    assert groups == eg
+    np.testing.assert_array_equal(keys, ek)
+    np.testing.assert_array_equal(vals, ev)
+    assert not np.signbit(vals).any()                 # +0.0 sums, as the reference's bincount gives
+
+
 def test_join_pipeline_repeated_build_key_raises():
     from tqpk.pipeline import JoinAggTopK
     bk = torch.tensor([1, 2, 2, 3], dtype=torch.int32, device="cuda")

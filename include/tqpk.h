@@ -484,10 +484,11 @@ int tqpk_gather_rows(const void* d_src, int64_t n_src, int64_t row_bytes, const 
                      void* d_dst, tqpk_stream stream);
 
 /* Sort keys of a string column for tqpk_argsort_stable (dtype int64): d_out[r]
- * = bytes word*8 .. word*8+7 of row r, so ceil(w/8) stable passes, last word
- * first, order the rows as the reference's unique(dim=0) ranks of the int8
- * rows do (sort.py:31-35).                                                   */
-int tqpk_string_words(const void* d_src, int64_t n, int32_t width, int32_t word, int64_t* d_out, tqpk_stream stream);
+ * = bytes word*8 .. word*8+7 of row r (compared as int8 when signed_bytes,
+ * else as uint8), so ceil(w/8) stable passes, last word first, order the
+ * rows as the reference's unique(dim=0) ranks of the rows do (sort.py:31-35). */
+int tqpk_string_words(const void* d_src, int64_t n, int32_t width, int32_t word, int32_t signed_bytes,
+                      int64_t* d_out, tqpk_stream stream);
 
 #ifdef __cplusplus
 }

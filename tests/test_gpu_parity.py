@@ -631,3 +631,54 @@ def test_operators_wait_for_columns_still_copying():
     top = O.tqp_sort(agg, targs, True)
     np.testing.assert_array_equal(got_k, top[11].reshape(-1))
     assert_f64_close(got_v, top[302])
+
+
+def test_key_encode_edge_cases():
+    """Every row masked out (no groups), one row, a float key with -0.0 / +0.0, and string keys
+    with bytes >= 128 as uint8 (unsigned order) and as int8 (signed order)."""
+    from tqpk.ops import encode_keys
+    s = np.array([[1, 2], [3, 4], [1, 2]], np.int8)
+    codes, reps, G = encode_keys([torch.from_numpy(s).cuda()], torch.zeros(3, dtype=torch.bool, device="cuda"))
+    assert G == 0 and reps.numel() == 0
+    codes, reps, G = encode_keys([torch.from_numpy(s[:1]).cuda()])
+    assert G == 1 and np_(codes).tolist() == [0] and np_(reps).tolist() == [0]
+    f = np.array([0.0, -0.0, 1.5, -2.0, 1.5, 0.0], np.float64)
+    codes, reps, G = encode_keys([torch.from_numpy(f).cuda()])
+    assert G == 3 and np_(codes).tolist() == [1, 1, 2, 0, 2, 1]
+    u = np.array([[200, 1], [5, 1], [200, 0], [5, 1]], np.uint8)
+    codes, reps, G = encode_keys([torch.from_numpy(u).cuda()])
+    _, inv = O.group_rows([u])                       # uint8 bytes order unsigned, int8 bytes signed
+    np.testing.assert_array_equal(np_(codes), inv)
+    codes, reps, G = encode_keys([torch.from_numpy(u.view(np.int8)).cuda()])
+    _, inv = O.group_rows([u.view(np.int8)])
+    np.testing.assert_array_equal(np_(codes), inv)
+
+
+def test_project_case_over_a_string_condition_and_year_edges():
+    """tqp_project: CASE WHEN on a string equality, year() at the first and last day the
+    reference's table covers, and a comparison as a bool output."""
+    from tqpk.operators import tqp_project
+    from tqpk.variable import Variable
+    rng = np.random.default_rng(2)
+    n = 10_001
+    nat = np.zeros((n, 25), np.int8)
+    names = ["BRAZIL", "PERU"]
+    pick = rng.integers(0, 2, n)
+    for i, nm in enumerate(names):
+        nat[pick == i, :len(nm)] = np.frombuffer(nm.encode(), np.uint8).astype(np.int8)
+    days = rng.integers(0, 3652, n).astype(np.int32)
+    days[:4] = [0, 364, 365, 3651]
+    price = rng.integers(100, 10000, n) / 100.0
+    cols = {1: nat, 2: days, 3: price}
+    args = {"rename map": {}, "materialized in": [1, 2, 3],
+            "used expr": [[["CASE", "WHEN", ["n#1", "=", "BRAZIL"], "THEN", "p#3", "ELSE", "0.0", "END"], "AS", "v#10"],
+                          [["year", ["d#2"]], "AS", "y#11"], [["p#3", ">=", "50.0"], "AS", "b#12"]],
+            "materialized out": [10, 11, 12]}
+    tg = {1: Variable(torch.from_numpy(nat).cuda(), "string"), 2: V(days, "date"), 3: V(price, "float")}
+    tqp_project(True, tg, copy.deepcopy(args), None, None, "p")
+    ref = O.tqp_project(cols, args)
+    for c in (10, 11, 12):
+        o = np_(tg[c].tensor)
+        assert o.dtype == ref[c].dtype, c
+        np.testing.assert_array_equal(o, ref[c])
+    assert np_(tg[11].tensor)[:4].tolist() == [1990, 1990, 1991, 1999]

@@ -15,8 +15,8 @@
 //   2. k_key_collect: occupied entries are numbered (group ids in table order).
 //   3. The groups are ordered by key tuple with the library's stable radix sort,
 //      least significant key first: one pass per numeric key, one per 8 bytes
-//      of a string key (big-endian words of the bytes with the sign bit
-//      flipped, so unsigned word order is the int8 byte order of the
+//      of a string key (big-endian words of the bytes, an int8 column's with
+//      the sign bit flipped, so unsigned word order is the byte order of the
 //      reference's stacked columns).
 //   4. k_key_codes: every row gets the rank of its group; d_reps[rank] is the
 //      group's representative row.
@@ -134,10 +134,11 @@ __global__ void k_key_sortword(const __grid_constant__ KeyTuple K, int k, int wo
     const int64_t row = rep[g];
     if (K.width[k]) {
       const uint8_t* s = static_cast<const uint8_t*>(K.col[k]) + row * K.width[k];
+      const uint8_t flip = K.dt[k] == TQPK_I8 ? 0x80u : 0u;   // int8 bytes order as signed values
       uint64_t w = 0;
       for (int i = 0; i < 8; ++i) {
         const int c = word * 8 + i;
-        const uint64_t b = c < K.width[k] ? static_cast<uint64_t>(s[c] ^ 0x80u) : 0ull;
+        const uint64_t b = c < K.width[k] ? static_cast<uint64_t>(s[c] ^ flip) : 0ull;
         w = (w << 8) | b;
       }
       out[g] = static_cast<int64_t>(w ^ (1ull << 63));
@@ -165,17 +166,19 @@ __global__ void k_key_codes(const int64_t* __restrict__ entry_of_row, int64_t n,
   }
 }
 
-// Word `word` of each row of an int8 [n, w] column as a sort key: bytes
-// word*8 .. word*8+7 big-endian with the sign bit of each byte flipped (zero
-// past w), stored as int64 with its top bit flipped, so the library's int64
-// sort orders rows as the int8 byte columns compare, most significant first.
-__global__ void k_string_words(const uint8_t* __restrict__ src, int64_t n, int w, int word, int64_t* __restrict__ out) {
+// Word `word` of each row of an int8/uint8 [n, w] column as a sort key: bytes
+// word*8 .. word*8+7 big-endian (an int8 column's with the sign bit of each
+// byte flipped; zero past w), stored as int64 with its top bit flipped, so the
+// library's int64 sort orders rows as the byte columns compare, most
+// significant first.
+__global__ void k_string_words(const uint8_t* __restrict__ src, int64_t n, int w, int word, uint8_t flip,
+                               int64_t* __restrict__ out) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     const uint8_t* s = src + r * w;
     uint64_t v = 0;
     for (int i = 0; i < 8; ++i) {
       const int c = word * 8 + i;
-      v = (v << 8) | (c < w ? static_cast<uint64_t>(s[c] ^ 0x80u) : 0ull);
+      v = (v << 8) | (c < w ? static_cast<uint64_t>(s[c] ^ flip) : 0ull);
     }
     out[r] = static_cast<int64_t>(v ^ (1ull << 63));
   }
@@ -296,13 +299,14 @@ extern "C" int tqpk_gather_rows(const void* d_src, int64_t n_src, int64_t row_by
   return TQPK_OK;
 }
 
-extern "C" int tqpk_string_words(const void* d_src, int64_t n, int32_t width, int32_t word, int64_t* d_out,
-                                 tqpk_stream stream) {
+extern "C" int tqpk_string_words(const void* d_src, int64_t n, int32_t width, int32_t word, int32_t signed_bytes,
+                                 int64_t* d_out, tqpk_stream stream) {
   if (n < 0 || width <= 0 || word < 0 || word * 8 >= width) return TQPK_EINVAL;
   if (n == 0) return TQPK_OK;
   if (!d_src || !d_out) return TQPK_EINVAL;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  k_string_words<<<grid_for(n, 8), kBlock, 0, s>>>(static_cast<const uint8_t*>(d_src), n, width, word, d_out);
+  k_string_words<<<grid_for(n, 8), kBlock, 0, s>>>(static_cast<const uint8_t*>(d_src), n, width, word,
+                                                   signed_bytes ? 0x80u : 0u, d_out);
   TQPK_CHECK_LAUNCH();
   return TQPK_OK;
 }

@@ -103,7 +103,7 @@ SIGNATURES = {
     "tqpk_key_encode_workspace_bytes": (_SZ, [_I64]),
     "tqpk_key_encode": (C.c_int, [_I32, _P(_VP), _P(_I32), _P(_I32), _VP, _I64, _VP, _VP, _P(_I64), _VP, _SZ, _VP]),
     "tqpk_gather_rows": (C.c_int, [_VP, _I64, _I64, _VP, _I64, _VP, _VP]),
-    "tqpk_string_words": (C.c_int, [_VP, _I64, _I32, _I32, _VP, _VP]),
+    "tqpk_string_words": (C.c_int, [_VP, _I64, _I32, _I32, _I32, _VP, _VP]),
     "tqpk_directory_compose": (C.c_int, [_VP, _I64, _VP, _I64, _I64, _I32, _I32, _VP]),
     "tqpk_batch_record_bytes": (_SZ, []),
     "tqpk_batch_join_workspace_bytes": (_SZ, [_I64, _I64]),

@@ -319,8 +319,8 @@ def string_words(col: torch.Tensor, word: int) -> torch.Tensor:
     c = col.contiguous()
     n, w = int(c.shape[0]), int(c.shape[1])
     out = torch.empty(n, dtype=torch.int64, device=c.device)
-    L.check(lib.tqpk_string_words(c.data_ptr() if n else None, n, w, word, out.data_ptr() if n else None,
-                                  _stream(c.device)), "tqpk_string_words")
+    L.check(lib.tqpk_string_words(c.data_ptr() if n else None, n, w, word, int(c.dtype == torch.int8),
+                                  out.data_ptr() if n else None, _stream(c.device)), "tqpk_string_words")
     return out
 
 

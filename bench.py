@@ -55,37 +55,6 @@ def d2h_all(tensors):
     return out
 
 
-class StagedInputs:
-    """Host->device copies of one step's input columns on a copy stream, in the order the plan
-    reads them, with one event per column carried by the column's Variable (`ready`): each
-    operator waits for a column right before its first kernel that reads it, so the later
-    columns' copies overlap the earlier operators (and the earlier stages of an operator)."""
-
-    def __init__(self, host, dev, types, order):
-        import torch
-        self.host, self.dev, self.types, self.order = host, dev, types, list(order)
-        self.copy_stream = torch.cuda.Stream(dev)
-
-    def start(self):
-        import torch
-        from tqpk.variable import Variable
-        main = torch.cuda.current_stream(self.dev)
-        self.dst = {c: torch.empty(h.shape, dtype=h.dtype, device=self.dev) for c, h in self.host.items()}
-        self.copy_stream.wait_stream(main)          # the buffers are allocated on the main stream
-        self.ev = {}
-        with torch.cuda.stream(self.copy_stream):
-            for c in self.order:
-                self.dst[c].copy_(self.host[c], non_blocking=True)
-                self.dst[c].record_stream(self.copy_stream)
-                self.ev[c] = torch.cuda.Event()
-                self.ev[c].record(self.copy_stream)
-        return {c: Variable(t, self.types[c], ready=self.ev[c]) for c, t in self.dst.items()}
-
-    @property
-    def bytes(self):
-        return sum(h.numel() * h.element_size() for h in self.host.values())
-
-
 class JoinAggTop10:
     name = "join_agg_top10"
     NB, NP = 1_500_000, 6_001_215
@@ -156,8 +125,9 @@ class JoinAggTop10:
         from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
         from tqpk.variable import Variable
         if not hasattr(self, "staged"):
-            self.staged = StagedInputs(self.host, self.dev, self.types, (12, 22, 11, 21, 23, 24))
-        tg = self.staged.start()
+            from tqpk.ingress import ColumnStager
+            self.staged = ColumnStager(self.dev)
+        tg = self.staged.stage(self.host, self.types, (12, 22, 11, 21, 23, 24))
         tqp_filter(True, tg, copy.deepcopy(self.f1), None, None, None, "f1")
         tqp_filter(True, tg, copy.deepcopy(self.f2), None, None, None, "f2")
         join_vortex(True, tg, copy.deepcopy(self.jargs), 11, 21, [], "inner", None, None, "j")
@@ -277,8 +247,9 @@ class FilterGroupBy:
         from tqpk.operators import tqp_filter, tqp_hash_aggregate, tqp_sort
         from tqpk.variable import Variable
         if not hasattr(self, "staged"):
-            self.staged = StagedInputs(self.host, self.dev, self.types, (7, 5, 6, 1, 2, 3, 4))
-        tg = self.staged.start()
+            from tqpk.ingress import ColumnStager
+            self.staged = ColumnStager(self.dev)
+        tg = self.staged.stage(self.host, self.types, (7, 5, 6, 1, 2, 3, 4))
         tqp_filter(True, tg, copy.deepcopy(self.fargs), None, None, None, "f")
         tqp_hash_aggregate(True, tg, copy.deepcopy(self.aargs), None, None, "a")
         tqp_sort(True, tg, copy.deepcopy(self.sargs), False, "s")
@@ -376,9 +347,10 @@ class StarJoin:
         from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
         from tqpk.variable import Variable
         if not hasattr(self, "staged"):
-            # keys and dimension tables first, the fact value columns last: the joins run while they copy
-            self.staged = StagedInputs(self.host, self.dev, self.types, (32, 31, 41, 42, 51, 52, 61, 43, 44))
-        tg = self.staged.start()
+            from tqpk.ingress import ColumnStager
+            self.staged = ColumnStager(self.dev)
+        # keys and dimension tables first, the fact value columns last: the joins run while they copy
+        tg = self.staged.stage(self.host, self.types, (32, 31, 41, 42, 51, 52, 61, 43, 44))
 
         def f(tg, a):
             tqp_filter(True, tg, a, None, None, None, "f")

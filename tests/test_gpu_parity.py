@@ -682,3 +682,51 @@ def test_project_case_over_a_string_condition_and_year_edges():
         assert o.dtype == ref[c].dtype, c
         np.testing.assert_array_equal(o, ref[c])
     assert np_(tg[11].tensor)[:4].tolist() == [1990, 1990, 1991, 1999]
+
+
+def test_scan_staged_and_synchronous_paths_feed_the_operators(tmp_path):
+    """tqp_scan places the columns on the device synchronously (the reference's behaviour, in a
+    pool with malloc_like) or queues them on a ColumnStager; a filter and an aggregate over the
+    staged columns match the oracle."""
+    import torch.nn as nn
+    from tqpk.ingress import ColumnStager
+    from tqpk.operators import tqp_filter, tqp_hash_aggregate, tqp_scan
+
+    class Holder(nn.Module):
+        def __init__(self, t):
+            super().__init__()
+            self.p = nn.Parameter(t, requires_grad=False)
+
+        def forward(self):
+            return self.p
+
+    class Pool:
+        def __init__(self):
+            self.n = 0
+
+        def malloc_like(self, t):
+            self.n += 1
+            return self.n, torch.empty_like(t)
+
+    rng = np.random.default_rng(6)
+    n = 2_000_003
+    data = {"K": rng.integers(0, 7, n).astype(np.int32), "V": rng.integers(90000, 10495001, n) / 100.0,
+            "D": rng.integers(0, 2557, n).astype(np.int32)}
+    for name, a in data.items():
+        torch.jit.script(Holder(torch.from_numpy(a))).save(str(tmp_path / f"SF1-tensor-{name}.pth"))
+    schema = {"K": "integer", "V": "decimal", "D": "date"}
+    args = {"output names": ["k", "v", "d"], "output ids": [1, 2, 3]}
+    for stager, pool in ((None, Pool()), (ColumnStager(), None), (ColumnStager(), Pool())):
+        tg = {}
+        assert tqp_scan(True, tg, args, {"tensors path": str(tmp_path)}, schema, 1, pool, stager=stager) == n
+        assert (getattr(tg[2], "ready", None) is not None) == (stager is not None)
+        tqp_filter(True, tg, {"filter tree": [["d#3", "<=", "2000"]], "materialized in": [3], "out mask id": 900},
+                   None, None, None, "f")
+        aargs = {"is partial": False, "keys": ["k#1"], "input ids": [1, 2],
+                 "results": ["k#1", [[["sum", ["v#2"]], "#", "1"], "AS", "s#10"]], "out agg ids": [10],
+                 "mask map": {1: 900, 2: 900}}
+        tqp_hash_aggregate(True, tg, copy.deepcopy(aargs), None, None, "a")
+        oc = {1: data["K"].astype(np.int64), 2: data["V"], 900: data["D"] <= 2000}
+        ref = O.tqp_hash_aggregate(oc, copy.deepcopy(aargs))
+        np.testing.assert_array_equal(np_(tg[1].tensor), ref[1])
+        assert_f64_close(np_(tg[10].tensor), ref[10])

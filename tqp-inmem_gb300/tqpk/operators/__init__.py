@@ -9,11 +9,13 @@ as the reference functions; the work runs in libtqpk.so:
   aggregate.tqp_hash_aggregate  operators/aggregate.py:236-393
   sort.tqp_sort                 operators/sort.py:6-58
   project.tqp_project           operators/project.py:10-69
+  ingress.tqp_scan              operators/scan.py:8-54 (device placement; optionally asynchronous)
 """
 from .filter import tqp_filter
 from .hashjoin import join_vortex, join_kernel_new
 from .aggregate import tqp_hash_aggregate
 from .sort import tqp_sort
 from .project import tqp_project
+from ..ingress import tqp_scan
 
-__all__ = ["tqp_filter", "join_vortex", "join_kernel_new", "tqp_hash_aggregate", "tqp_sort", "tqp_project"]
+__all__ = ["tqp_filter", "join_vortex", "join_kernel_new", "tqp_hash_aggregate", "tqp_sort", "tqp_project", "tqp_scan"]

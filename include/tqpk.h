@@ -434,6 +434,15 @@ int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64_t n, const
  * the composed directory then needs no lookup in the next one.              */
 int tqpk_directory_compose(int32_t* d_dir, int64_t slots, const int32_t* d_next, int64_t next_min,
                            int64_t next_slots, int32_t empty, int32_t fail_value, tqpk_stream stream);
+/* Membership bitmap of a row directory: bit s of d_bits (word s / 32, bit
+ * s % 32) is set when d_dir[s] >= 0.  d_bits holds (slots + 31) / 32 words.
+ * A probe that only asks whether a dimension key has a row that passed the
+ * dimension's filter (the star join's A table, filtered at build) reads
+ * 1 bit per key instead of 4 bytes, so its lookups stay in L1/L2; the same
+ * membership test as the reference's inner join on a unique, pre-filtered
+ * build side (operators/hashjoin.py:24-177 with the filter of
+ * operators/filter.py:164-204 applied first).                               */
+int tqpk_directory_bits(const int32_t* d_dir, int64_t slots, uint32_t* d_bits, tqpk_stream stream);
 /* The k (<= 256) best groups of a dense slot table (sum[s], count[s] != 0
  * marks a group) ordered by sum (descending when `descending`), ties to the
  * smaller key: the "sort by aggregate + limit" of operators/sort.py:6-58 over

@@ -171,6 +171,52 @@ def test_star_pipeline_with_missing_dimension_rows(monkeypatch, jit_on):
     np.testing.assert_array_equal(cnts, ec)
 
 
+@pytest.mark.parametrize("slots", [1, 31, 32, 33, 1000, 2_000_003])
+def test_directory_bits(slots):
+    """Bit s of the membership bitmap is set exactly where the directory names a row."""
+    from tqpk import _lib as L
+    rng = np.random.default_rng(slots)
+    d = rng.integers(-2, 50, slots).astype(np.int32)
+    d[rng.random(slots) < 0.5] = -1
+    dd = torch.from_numpy(d).cuda()
+    words = (slots + 31) // 32
+    bits = torch.full((words + 1,), -7, dtype=torch.int32, device="cuda")      # one guard word
+    L.check(L.load().tqpk_directory_bits(dd.data_ptr(), slots, bits.data_ptr(),
+                                         torch.cuda.current_stream().cuda_stream), "tqpk_directory_bits")
+    got = bits.cpu().numpy().view(np.uint32)
+    assert got[words] == np.uint32(0xFFFFFFF9)                                  # untouched
+    want = np.packbits(np.concatenate([d >= 0, np.zeros(words * 32 - slots, bool)]).reshape(-1, 8)[:, ::-1]
+                       ).view(np.uint32)
+    np.testing.assert_array_equal(got[:words], want)
+
+
+@pytest.mark.parametrize("a_bits", ["1", "0"])
+def test_star_pipeline_a_bitmap_and_row_directory_agree(monkeypatch, a_bits):
+    """The generated star probe gives the oracle's result with A's membership bitmap and
+    with A's row directory, A having keys missing from its domain and a domain size
+    that is not a multiple of 32."""
+    monkeypatch.setenv("TQPK_JIT", "1")
+    monkeypatch.setenv("TQPK_STAR_ABITS", a_bits)
+    import bench
+    from tqpk.pipeline import StarAggTopK
+    w = bench.StarJoin(scale=0.01)
+    rng = np.random.default_rng(11)
+    keep = rng.random(w.cols[31].size) < 0.7
+    w.cols[31], w.cols[32] = w.cols[31][keep], w.cols[32][keep]
+    w.cols[31][-1] = int(w.cols[31].max()) + 45                  # the domain's last word half used
+    ek, ev, ec = w.oracle()
+    d = {c: torch.from_numpy(a).cuda() for c, a in w.cols.items()}
+    dom = lambda a: (int(a.min()), int(a.max()))  # noqa: E731
+    p = StarAggTopK(d[41], d[42], {43: d[43], 44: d[44]}, None, w.value_tree, d[31], {32: d[32]},
+                    w.fa["filter tree"], dom(w.cols[31]), d[51], d[52], dom(w.cols[51]), d[61], dom(w.cols[61]), k=100)
+    p.run()
+    keys, vals, cnts, groups = p.result()
+    assert p._a_bits == (a_bits == "1")
+    np.testing.assert_array_equal(keys, ek)
+    assert_f64_close(vals, ev)
+    np.testing.assert_array_equal(cnts, ec)
+
+
 @pytest.mark.parametrize("k", [200, 256, 257, 1000])
 def test_topk_stable_large_k(k):
     from tqpk.ops import topk_stable

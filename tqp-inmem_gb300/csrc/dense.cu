@@ -128,6 +128,28 @@ extern "C" int tqpk_directory_compose(int32_t* d_dir, int64_t slots, const int32
   return TQPK_OK;
 }
 
+// One bit per directory slot, set where the slot names a row (dir[s] >= 0): a warp
+// reads 32 consecutive slots and writes their ballot as one word.
+__global__ void k_dir_bits(const int* __restrict__ dir, int64_t n, uint32_t* __restrict__ bits) {
+  const int lane = threadIdx.x & 31;
+  const int64_t words = (n + 31) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < words; w += nwarps) {
+    const int64_t i = (w << 5) + lane;
+    const unsigned b = __ballot_sync(0xffffffffu, i < n && dir[i] >= 0);
+    if (lane == 0) bits[w] = b;
+  }
+}
+
+extern "C" int tqpk_directory_bits(const int32_t* d_dir, int64_t slots, uint32_t* d_bits, tqpk_stream stream) {
+  if (slots < 0 || (slots > 0 && (!d_dir || !d_bits))) return TQPK_EINVAL;
+  if (slots == 0) return TQPK_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  k_dir_bits<<<grid_for(((slots + 31) >> 5) * 32, 8), kBlock, 0, s>>>(d_dir, slots, d_bits);
+  TQPK_CHECK_LAUNCH();
+  return TQPK_OK;
+}
+
 extern "C" size_t tqpk_dense_topk_workspace_bytes(int32_t k) {
   k = std::max(1, std::min(k, kDenseMaxK));
   return 1024 + align_up((size_t)k * 8, 256) + 2 * align_up(topk_cand_entries(k) * 8, 256) + 1024;

@@ -105,6 +105,7 @@ SIGNATURES = {
     "tqpk_gather_rows": (C.c_int, [_VP, _I64, _I64, _VP, _I64, _VP, _VP]),
     "tqpk_string_words": (C.c_int, [_VP, _I64, _I32, _I32, _I32, _VP, _VP]),
     "tqpk_directory_compose": (C.c_int, [_VP, _I64, _VP, _I64, _I64, _I32, _I32, _VP]),
+    "tqpk_directory_bits": (C.c_int, [_VP, _I64, _VP, _VP]),
     "tqpk_batch_record_bytes": (_SZ, []),
     "tqpk_batch_join_workspace_bytes": (_SZ, [_I64, _I64]),
     "tqpk_batch_describe_join": (C.c_int, [_VP, _VP, _I32, _I64, _P(Predicate), _I64, _I64, _VP, _I32, _I64,

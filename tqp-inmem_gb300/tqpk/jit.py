@@ -950,7 +950,8 @@ def join_probe_args(a: "_Args", spec, pred, bpred, fk, np_: int, key_min: int, s
 
 # ---------------------------------------------------------------------------- star probe
 def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_blocks: int = 0,
-                      early_fb: bool = False, stream_cs: bool = False, composed: bool = False) -> Tuple[str, str]:
+                      early_fb: bool = False, stream_cs: bool = False, composed: bool = False,
+                      a_bits: bool = False) -> Tuple[str, str]:
     """CUDA source of the star probe: fact -> A (row directory, A predicate through the
     row) -> B (directory of the C foreign key) -> C (row directory), then FP64 sum and
     count per C slot, computed warp-densely over the matched rows (_dense_tail).
@@ -959,7 +960,11 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
     B lookup does not wait for a second column round trip after the A lookup;
     stream_cs loads the fact columns with evict-first hints; composed means B's directory
     already holds only C keys that have a C row (tqpk_directory_compose), so the C lookup
-    is left out of the chain."""
+    is left out of the chain; a_bits means dir_a is A's membership bitmap
+    (tqpk_directory_bits: 1 bit per key, 250 KB for 2 M keys, mostly L1-resident) in place
+    of its row directory, which needs A's filter applied at build (apred None)."""
+    if a_bits and apred is not None:
+        raise ValueError("a membership bitmap carries no A row for a probe-time A predicate")
     S = spec
     pcols, pexpr = _pred_code(fpred, "p") if fpred is not None else ([], "true")
     ecols, elines = _expr_code(S, val_reg + 1, "c")
@@ -971,7 +976,7 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
         params += ["const PL la"]
     params += [f"const void* __restrict__ cp{c}" for c in range(S.n_cols)]
     params += ["const int* __restrict__ fka", "const int* __restrict__ fkb", "i64 nf",
-               "i64 a_min", "i64 a_slots", "const int* __restrict__ dir_a",
+               "i64 a_min", "i64 a_slots", "const unsigned* __restrict__ dir_a" if a_bits else "const int* __restrict__ dir_a",
                "i64 b_min", "i64 b_slots", "const int* __restrict__ dir_b",
                "i64 c_min", "i64 c_slots", "const int* __restrict__ dir_c",
                "double* __restrict__ sum", "u32* __restrict__ cnt", "int vp", "int vc", "int vf"]
@@ -1010,7 +1015,8 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
             f"    for (int u = 0; u < {U}; ++u)",
             "#pragma unroll",
             "      for (int j = 0; j < 4; ++j) {",
-            "        rw[u][j] = ((m[u] >> j) & 1u) ? __ldg(&dir_a[k[u][j]]) : -1;",
+            ("        rw[u][j] = ((m[u] >> j) & 1u) ? (int)((__ldg(&dir_a[k[u][j] >> 5]) >> (k[u][j] & 31)) & 1u) - 1 : -1;"
+             if a_bits else "        rw[u][j] = ((m[u] >> j) & 1u) ? __ldg(&dir_a[k[u][j]]) : -1;"),
             "        if (rw[u][j] < 0) m[u] &= ~(1u << j);",
             "      }"]
     if apred is not None:

@@ -388,6 +388,11 @@ int tqpk_jit_compile(const char* src, const char* name, void** h_handle, char* l
 int tqpk_jit_occupancy(void* handle, int32_t block, size_t smem);
 int tqpk_jit_launch(void* handle, int32_t grid, int32_t block, size_t smem, void** args, int32_t timing_kid,
                     tqpk_stream stream);
+/* Preferred shared-memory share of the SM's unified L1/shared storage for a
+ * compiled kernel (percent of the maximum, 0-100; a hint the driver rounds
+ * to a supported split): a probe that keeps a small lookup structure in L1
+ * asks for no more shared memory than its CTAs use.                         */
+int tqpk_jit_prefer_shared(void* handle, int32_t percent);
 int32_t tqpk_num_sms(void);
 /* A group-by plan from key domains known ahead (table statistics [key_min, key_max]
  * per key), with no pass over the data and no host synchronisation; n_rows sizes

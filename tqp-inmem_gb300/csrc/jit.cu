@@ -157,6 +157,14 @@ extern "C" int tqpk_jit_occupancy(void* handle, int32_t block, size_t smem) {
   return per_sm;
 }
 
+extern "C" int tqpk_jit_prefer_shared(void* handle, int32_t percent) {
+  if (!handle || percent < 0 || percent > 100) return TQPK_EINVAL;
+  JitKernel* k = static_cast<JitKernel*>(handle);
+  TQPK_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(k->kernel),
+                                 cudaFuncAttributePreferredSharedMemoryCarveout, (int)percent));
+  return TQPK_OK;
+}
+
 extern "C" int32_t tqpk_num_sms(void) { return num_sms(); }
 
 // Launches a compiled kernel: args[i] points at the i-th kernel parameter.

@@ -126,6 +126,7 @@ SIGNATURES = {
     "tqpk_jit_compile": (C.c_int, [C.c_char_p, C.c_char_p, _P(_VP), C.c_char_p, _SZ]),
     "tqpk_jit_occupancy": (C.c_int, [_VP, _I32, _SZ]),
     "tqpk_jit_launch": (C.c_int, [_VP, _I32, _I32, _SZ, _P(_VP), _I32, _VP]),
+    "tqpk_jit_prefer_shared": (C.c_int, [_VP, _I32]),
     "tqpk_num_sms": (_I32, []),
     "tqpk_groupby_prepare": (C.c_int, [_P(GroupbySpec), _P(GbPlan), _VP, _SZ, _VP]),
     "tqpk_groupby_plan_domains": (C.c_int, [_P(GroupbySpec), _P(_I64), _P(_I64), _I64, _P(GbPlan)]),

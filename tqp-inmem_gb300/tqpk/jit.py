@@ -78,6 +78,16 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
+// read-only loads that leave L1 to other data (a lookup structure the kernel keeps there)
+__device__ __forceinline__ int ld_na(const int* p) {
+  int v; asm("ld.global.nc.L1::no_allocate.b32 %0, [%1];" : "=r"(v) : "l"(p)); return v;
+}
+__device__ __forceinline__ long long ld_na(const long long* p) {
+  long long v; asm("ld.global.nc.L1::no_allocate.b64 %0, [%1];" : "=l"(v) : "l"(p)); return v;
+}
+__device__ __forceinline__ double ld_na(const double* p) {
+  double v; asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p)); return v;
+}
 // predicate literals, bound at launch (one compiled kernel serves every constant)
 struct PL { long long i[32]; double f[32]; double a[32]; };
 template <class T> struct V4 { T v[4]; };
@@ -554,7 +564,8 @@ def _gather_pred(pred, prefix: str, lits: str, ptr_pfx: str, row: str, live: str
 
 
 def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[str], U: int = 2,
-                smem_vals: Optional[Dict[int, str]] = None, neg_zero_as_zero: bool = False) -> List[str]:
+                smem_vals: Optional[Dict[int, str]] = None, neg_zero_as_zero: bool = False,
+                l1_no_allocate: bool = False) -> List[str]:
     """Warp-dense value pass: the warp's matched rows (queued as row offsets and
     slots in shared memory) are spread over all 32 lanes, so each FP64
     instruction and atomic runs with full lanes instead of the ~1 in 4 a
@@ -585,6 +596,8 @@ def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[st
         t = _CTYPE[S.col_dtypes[c]]
         if smem_vals is not None:
             lines.append(f"      const {t} Cs{c} = (({smem_vals[c]}))[off];")
+        elif l1_no_allocate and S.col_dtypes[c] in (L.F64, L.I64, L.I32):
+            lines.append(f"      const {t} Cs{c} = ld_na((const {t}*)cp{c} + row);")
         else:
             lines.append(f"      const {t} Cs{c} = __ldg((const {t}*)cp{c} + row);")
     for l in elines:
@@ -962,7 +975,8 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
     already holds only C keys that have a C row (tqpk_directory_compose), so the C lookup
     is left out of the chain; a_bits means dir_a is A's membership bitmap
     (tqpk_directory_bits: 1 bit per key, 250 KB for 2 M keys, mostly L1-resident) in place
-    of its row directory, which needs A's filter applied at build (apred None)."""
+    of its row directory, which needs A's filter applied at build (apred None); the B lookups
+    and the value loads then bypass L1 so that the bitmap keeps it."""
     if a_bits and apred is not None:
         raise ValueError("a membership bitmap carries no A row for a probe-time A predicate")
     S = spec
@@ -1034,7 +1048,7 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
             "      for (int j = 0; j < 4; ++j) {",
             "        const i64 sb = (i64)FB.v[j] - b_min;",
             "        const bool ok = ((m[u] >> j) & 1u) && sb >= 0 && sb < b_slots;",
-            "        const int fc = ok ? __ldg(&dir_b[sb]) : (int)0x80000000;",
+            f"        const int fc = ok ? {'ld_na' if a_bits else '__ldg'}(&dir_b[sb]) : (int)0x80000000;",
             "        k[u][j] = (i64)fc - c_min;",
             "        if (fc == (int)0x80000000 || k[u][j] < 0 || k[u][j] >= c_slots) m[u] &= ~(1u << j);",
             "      }",
@@ -1046,6 +1060,7 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
                 "#pragma unroll",
                 "      for (int j = 0; j < 4; ++j)",
                 "        if (((m[u] >> j) & 1u) && __ldg(&dir_c[k[u][j]]) < 0) m[u] &= ~(1u << j);"]
-    src += _dense_tail(S, val_reg, ecols, elines, "nf", "k", ["atomicAdd(&cnt[slot], 1u);"], U=U)
+    src += _dense_tail(S, val_reg, ecols, elines, "nf", "k", ["atomicAdd(&cnt[slot], 1u);"], U=U,
+                       l1_no_allocate=a_bits)
     src += ["  }", "}"]
     return "\n".join(src), name

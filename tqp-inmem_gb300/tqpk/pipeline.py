@@ -153,7 +153,8 @@ class JoinAggTopK:
         return (self.out_keys[:m].cpu().numpy(), self.out_vals[:m].cpu().numpy(), int(self.groups.item()))
 
 
-STAR_A_BITS_MAX_BYTES = 64 << 10
+STAR_A_BITS_MAX_BYTES = 256 << 10
+STAR_SHARED_PERCENT = 20
 
 
 class StarAggTopK:
@@ -210,10 +211,11 @@ class StarAggTopK:
             raise NotImplementedError("C keys at the bottom of the int32 range are reserved as directory markers")
         dev = self.dev
         self.dir_a = torch.empty(amx - amn + 1, dtype=torch.int32, device=dev)
-        # A's membership bitmap in place of its row directory when the bitmap stays L1-resident
-        # (<= 64 KB): on GB300 the probe at 200 K A keys (25 KB) took 40.6 us against 53.5 us
-        # with the directory, at 2 M keys (250 KB) 467 us against 441 us.  TQPK_STAR_ABITS=1/0
-        # forces either form.
+        # A's membership bitmap in place of its row directory while it can stay in L1 (the B
+        # lookups and value loads bypass L1, and the kernel asks for a 20% shared-memory split).
+        # GB300, generated probe: 2 M A keys (250 KB) 424 us against 442 us with the directory,
+        # 600 K keys 117 against 140 us; without the L1 bypass 2 M keys took 467 us, and a 0% /
+        # 100% shared split 1585 / 889 us.  TQPK_STAR_ABITS=1/0 forces either form.
         import os
         words = (amx - amn + 32) // 32
         force = os.environ.get("TQPK_STAR_ABITS", "auto")
@@ -230,6 +232,8 @@ class StarAggTopK:
         src, name = jit.star_probe_source(self.prog.spec, self.value_reg, self.fpred.struct if self.fpred else None,
                                           None, early_fb=True, stream_cs=True, composed=True, a_bits=self._a_bits)
         self._probe = jit.compile_kernel(src, name)
+        if self._a_bits:      # the CTAs' 5 KB of queues per CTA; the rest of the SM's storage as L1
+            L.check(self.lib.tqpk_jit_prefer_shared(self._probe, STAR_SHARED_PERCENT), "tqpk_jit_prefer_shared")
         fa, fb = self.t[0], self.t[1]
         a = jit._Args()
         if self.fpred:

@@ -91,6 +91,33 @@ def test_join_probe_staged_and_plain_paths(monkeypatch, tma, nb, np_rows, dtype)
     assert_f64_close(vals, ev)
 
 
+@pytest.mark.parametrize("bits", [True, False])
+@pytest.mark.parametrize("nb,np_rows", [(1_500_000, 2_000_003), (33, 1000), (100_001, 777)])
+def test_join_probe_bitmap_and_row_directory(monkeypatch, bits, nb, np_rows):
+    """The generated probe over the build side's membership bitmap (the default while it fits
+    256 KB) and over its row directory give the oracle's groups, with build keys missing from
+    the key domain and a domain size that is not a multiple of 32."""
+    from tqpk import pipeline as P
+    monkeypatch.setattr(P, "JOIN_DIR_BITS", bits)
+    rng = np.random.default_rng(nb)
+    keys = rng.permutation(nb + nb // 3)[:nb] + 7
+    cols = {11: keys.astype(np.int32), 12: rng.integers(0, 2557, nb).astype(np.int32),
+            21: rng.integers(0, nb + nb // 3 + 20, np_rows).astype(np.int32),
+            22: rng.integers(0, 2557, np_rows).astype(np.int32),
+            23: rng.integers(90000, 10495001, np_rows) / 100.0, 24: rng.integers(0, 11, np_rows) / 100.0}
+    f1, f2 = [["bd#12", "<", "1170"]], [["pd#22", ">", "1170"]]
+    d = {c: torch.from_numpy(a).cuda() for c, a in cols.items()}
+    p = P.JoinAggTopK(d[11], int(cols[11].min()), int(cols[11].max()), d[21], {12: d[12]}, f1,
+                      {22: d[22], 23: d[23], 24: d[24]}, f2, [["p#23", "*", ["1.0", "-", "d#24"]]], k=10)
+    p.run()
+    keys_, vals, groups = p.result()
+    assert (p._bits is not None) == bits
+    ek, ev, eg = _oracle_join(cols, f1, f2, 10)
+    assert groups == eg
+    np.testing.assert_array_equal(keys_, ek)
+    assert_f64_close(vals, ev)
+
+
 def test_join_pipeline_zero_sums_still_count_as_groups():
     """Every value is +0.0 or -0.0, so every matched group sums to zero: the groups are told
     apart from empty slots by occupancy alone (the sums start at -0.0 in the generated path and

@@ -647,8 +647,8 @@ def _stage_values(S, ecols, rows: int, n: str) -> Tuple[List[str], List[str], Di
 
 
 def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, min_blocks: int = 0,
-                      stream_cs: bool = False, stage_vals: bool = False, occ_sentinel: bool = False
-                      ) -> Tuple[str, str]:
+                      stream_cs: bool = False, stage_vals: bool = False, occ_sentinel: bool = False,
+                      dir_bits: bool = False) -> Tuple[str, str]:
     """CUDA source of the fused probe + aggregate (directory lookup, value, FP64 sum, occupancy).
 
     The directory holds build row indices (negative = no row).  `bpred`, when
@@ -661,7 +661,12 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
     probe columns with evict-first hints; stage_vals copies the value columns of
     every row to shared memory with cp.async at the top of the iteration (the
     value gather after the lookup leaves the dependent chain); occ_sentinel writes no
-    occupancy word (the sums start at -0.0 and carry it; pipeline stage bit 3)."""
+    occupancy word (the sums start at -0.0 and carry it; pipeline stage bit 3); dir_bits
+    means `dir` is the build side's membership bitmap (tqpk_directory_bits; the group slot
+    is the key, so membership is all the probe asks) and the value loads that are not
+    staged bypass L1, which the bitmap keeps."""
+    if dir_bits and bpred is not None:
+        raise ValueError("a membership bitmap carries no build row for a probe-time build predicate")
     S = spec
     pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
     ecols, elines = _expr_code(S, val_reg + 1, "c")
@@ -673,8 +678,8 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
         params += ["const PL lb"]
     params += [f"const void* __restrict__ cp{c}" for c in range(S.n_cols)]
     params += ["const void* __restrict__ fk", "int fk_dt", "i64 np", "i64 key_min", "i64 slots",
-               "const int* __restrict__ dir", "double* __restrict__ sum", "u32* __restrict__ occ",
-               "int vp", "int vc", "int vf"]
+               "const unsigned* __restrict__ dir" if dir_bits else "const int* __restrict__ dir",
+               "double* __restrict__ sum", "u32* __restrict__ occ", "int vp", "int vc", "int vf"]
     fk_load = ("const V4<i64> F = (fk_dt == 4) ? ld4((const long long*)fk, r0, np, vf != 0) : "
                "[&]{ V4<int> t = ld4((const int*)fk, r0, np, vf != 0); V4<i64> o; "
                "for (int q = 0; q < 4; ++q) o.v[q] = t.v[q]; return o; }();")
@@ -713,7 +718,8 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
             f"    for (int u = 0; u < {U}; ++u)",
             "#pragma unroll",
             "      for (int j = 0; j < 4; ++j) {",
-            "        rw[u][j] = ((m[u] >> j) & 1u) ? __ldg(&dir[sl[u][j]]) : -1;",
+            ("        rw[u][j] = ((m[u] >> j) & 1u) ? (int)((__ldg(&dir[sl[u][j] >> 5]) >> (sl[u][j] & 31)) & 1u) - 1 : -1;"
+             if dir_bits else "        rw[u][j] = ((m[u] >> j) & 1u) ? __ldg(&dir[sl[u][j]]) : -1;"),
             "        if (rw[u][j] < 0) m[u] &= ~(1u << j);",
             "      }"]
     if bpred is not None:
@@ -725,7 +731,7 @@ def join_probe_source(spec, val_reg: int, pred, bpred=None, U: int = PROBE_U, mi
     if stage_vals:
         src += ["    cp_async_wait_all();", "    __syncwarp();"]
     src += _dense_tail(S, val_reg, ecols, elines, "np", "sl", [] if occ_sentinel else ["occ[slot] = 1u;"], U=U,
-                       smem_vals=smem_vals, neg_zero_as_zero=occ_sentinel)
+                       smem_vals=smem_vals, neg_zero_as_zero=occ_sentinel, l1_no_allocate=dir_bits)
     src += ["  }", "}"]
     return "\n".join(src), name
 

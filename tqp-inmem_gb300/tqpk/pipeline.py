@@ -23,6 +23,17 @@ from .expr import compile_aggregate
 from .predicate import compile_filter
 
 
+# The generated probe tests the build side's membership bitmap (1 bit per key; the group slot is
+# the key) instead of reading its row directory, while the bitmap can stay in L1, and then leaves
+# shared memory (no value stage) and L1 (value loads that bypass it) to the bitmap.  GB300,
+# 1.5 M build keys (188 KB), 6,001,215 probe rows: 34.9 us; with the value stage as well 39.4 us;
+# the row directory with the value stage 41.1-41.6 us; a 10% / 72% shared-memory split 37.6 /
+# 42.3 us.
+JOIN_DIR_BITS = True
+JOIN_BITS_MAX_BYTES = 256 << 10
+JOIN_SHARED_PERCENT = None
+
+
 class JoinAggTopK:
     def __init__(self, build_keys: torch.Tensor, key_min: int, key_max: int, probe_fk: torch.Tensor,
                  build_cols: Dict[int, torch.Tensor], build_filter, probe_cols: Dict[int, torch.Tensor],
@@ -77,6 +88,10 @@ class JoinAggTopK:
         from . import jit
         if not hasattr(self, "_probe_handle"):
             pp = self.ppred.struct if self.ppred else None
+            slots = self.key_max - self.key_min + 1
+            self._bits = (torch.empty((slots + 31) // 32, dtype=torch.int32, device=self.dev)
+                          if JOIN_DIR_BITS and not self._tma_ok() and (slots + 31) // 32 * 4 <= JOIN_BITS_MAX_BYTES
+                          else None)
             self._probe_smem = 0
             if self._tma_ok():
                 import os
@@ -84,15 +99,22 @@ class JoinAggTopK:
                     self.prog.spec, self.value_reg, pp, None, code_of(self.pk.dtype),
                     ST=int(os.environ.get("TQPK_TMA_STAGES", "2")))
             else:
-                # value columns staged by cp.async + evict-first probe columns: 42.3-42.7 -> 41.4 us
-                # on the 6,001,215-row probe (measured through this pipeline's timing)
+                # evict-first probe columns; with the row directory, value columns staged by cp.async
+                # (42.3-42.7 -> 41.4 us on the 6,001,215-row probe, this pipeline's timing)
                 src, name = jit.join_probe_source(self.prog.spec, self.value_reg, pp, stream_cs=True,
-                                                  stage_vals=True, occ_sentinel=True)
+                                                  stage_vals=self._bits is None, occ_sentinel=True,
+                                                  dir_bits=self._bits is not None)
             self._probe_handle = jit.compile_kernel(src, name)
+            if self._bits is not None and JOIN_SHARED_PERCENT is not None:
+                L.check(self.lib.tqpk_jit_prefer_shared(self._probe_handle, JOIN_SHARED_PERCENT),
+                        "tqpk_jit_prefer_shared")
             d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
             L.check(self.lib.tqpk_pipeline_join_tables(self.ws.data_ptr(), self.ws.numel(), self.key_min,
                                                        self.key_max, C.byref(d), C.byref(su), C.byref(oc)),
                     "tqpk_pipeline_join_tables")
+            self._dir_ptr = d.value
+            if self._bits is not None:
+                d = C.c_void_p(self._bits.data_ptr())
             self._probe_args = jit.join_probe_args(
                 jit._Args(), self.prog.spec, pp, None, self.pk,
                 self.pk.numel(), self.key_min, self.key_max - self.key_min + 1, d.value, su.value, oc.value,
@@ -105,6 +127,9 @@ class JoinAggTopK:
                                                       max(1, self.pk.numel() // jit.TMA_ROWS) * 32)
             else:
                 self._probe_grid = jit.occupancy_grid(self._probe_handle, 256, 0, jit.probe_units(self.pk.numel()))
+        if self._bits is not None:     # the build stage has just written the row directory
+            L.check(self.lib.tqpk_directory_bits(self._dir_ptr, self.key_max - self.key_min + 1,
+                                                 self._bits.data_ptr(), s), "tqpk_directory_bits")
         jit.launch(self._probe_handle, self._probe_grid, 256, self._probe_smem, self._probe_args, s,
                    L.KID_PIPE_PROBE)
 

@@ -409,7 +409,11 @@ void* tqpk_groupby_table(void* d_ws);
  * probe, bit 2 top-k + emit), and the addresses of its tables.  Bit 3 (with
  * a caller-launched probe): the group sums start at -0.0 and carry the
  * occupancy (the probe adds -0.0 values as +0.0 and writes no occupancy
- * word); give it to the reset and the top-k stages alike.                  */
+ * word); give it to the reset and the top-k stages alike.  Bit 4 (with a
+ * caller-launched probe, not with bit 1): the reset + build stage writes the
+ * build side's membership bitmap (bit s of word s / 32 for key key_min + s,
+ * (slots + 31) / 32 words at the directory's address) instead of its row
+ * directory; a repeated key still sets TQPK_EUNSUPPORTED.                   */
 int tqpk_pipeline_join_agg_topk_stages(int32_t stages, const void* d_build_keys, int32_t build_dtype, int64_t nb,
                                        const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max,
                                        const void* d_probe_fk, int32_t probe_dtype, int64_t np,

@@ -111,7 +111,7 @@ def test_join_probe_bitmap_and_row_directory(monkeypatch, bits, nb, np_rows):
                       {22: d[22], 23: d[23], 24: d[24]}, f2, [["p#23", "*", ["1.0", "-", "d#24"]]], k=10)
     p.run()
     keys_, vals, groups = p.result()
-    assert (p._bits is not None) == bits
+    assert p._bits == bits
     ek, ev, eg = _oracle_join(cols, f1, f2, 10)
     assert groups == eg
     np.testing.assert_array_equal(keys_, ek)

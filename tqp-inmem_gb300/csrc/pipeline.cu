@@ -66,6 +66,31 @@ __global__ void __launch_bounds__(kBlock) k_pl_build(const __grid_constant__ tqp
   }
 }
 
+// The build side's membership bitmap: one atomicOr per passing build row; a bit that was
+// already set is a repeated key.
+__global__ void __launch_bounds__(kBlock) k_pl_build_bits(const __grid_constant__ tqpk_predicate P, PipeJoinArgs A,
+                                                          unsigned* __restrict__ bits, int* err_dup) {
+  const int64_t groups = (A.nb + 3) >> 2;
+  const bool vec = ((reinterpret_cast<uintptr_t>(A.b_keys) & 15u) == 0);
+  const bool pvec = A.b_pvec != 0;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r0 = g << 2;
+    uint32_t b = P.n_insn ? eval_pred4(P, r0, A.nb, pvec) : (A.nb - r0 >= 4 ? 0xfu : ((1u << (A.nb - r0)) - 1));
+    if (!b) continue;
+    int64_t x[4];
+    ld4_int(A.b_keys, A.b_dt, r0, A.nb, vec, x);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (!((b >> j) & 1u)) continue;
+      const int64_t slot = x[j] - A.key_min;
+      if (slot < 0 || slot >= A.slots) { set_error(err_dup, TQPK_EINVAL); continue; }
+      const unsigned bit = 1u << (slot & 31);
+      if (atomicOr(&bits[slot >> 5], bit) & bit) set_error(err_dup, TQPK_EUNSUPPORTED);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) k_pl_probe_agg(const __grid_constant__ tqpk_predicate P,
                                                          const __grid_constant__ tqpk_groupby_spec S, PipeJoinArgs A,
                                                          const int* __restrict__ dir, double* __restrict__ sum,
@@ -231,9 +256,14 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
   A.p_pvec = pred_vec_ok(h_probe_pred) ? 1 : 0;
   A.v_pvec = spec_cols_vec(h_values) ? 1 : 0;
   const bool sentinel = (stages & 8) != 0;   // occupancy carried by the sums (see DenseSumSource)
+  const bool bits = (stages & 16) != 0;      // membership bitmap in place of the row directory
+  if (bits && (stages & 2)) return TQPK_EINVAL;
   if (stages & 1) {
   TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 32, s));
-  TQPK_CUDA(cudaMemsetAsync(L.dir, 0xff, slots * 4, s));
+  if (bits)
+    TQPK_CUDA(cudaMemsetAsync(L.dir, 0, ((slots + 31) / 32) * 4, s));
+  else
+    TQPK_CUDA(cudaMemsetAsync(L.dir, 0xff, slots * 4, s));
   if (sentinel) {
     k_pl_fill_u64<<<grid_for(slots, 4), kBlock, 0, s>>>(reinterpret_cast<uint64_t*>(L.sum), slots,
                                                         DenseSumSource::kEmptySum);
@@ -244,7 +274,11 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
   }
   if (nb > 0) {
     timing_before(KID_PIPE_BUILD, s);
-    k_pl_build<<<grid_for((nb + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_build_pred), A, L.dir, L.err);
+    if (bits)
+      k_pl_build_bits<<<grid_for((nb + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_build_pred), A,
+                                                                   reinterpret_cast<unsigned*>(L.dir), L.err);
+    else
+      k_pl_build<<<grid_for((nb + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_build_pred), A, L.dir, L.err);
     timing_after(KID_PIPE_BUILD, s);
     TQPK_CHECK_LAUNCH();
   }

@@ -24,11 +24,13 @@ from .predicate import compile_filter
 
 
 # The generated probe tests the build side's membership bitmap (1 bit per key; the group slot is
-# the key) instead of reading its row directory, while the bitmap can stay in L1, and then leaves
-# shared memory (no value stage) and L1 (value loads that bypass it) to the bitmap.  GB300,
-# 1.5 M build keys (188 KB), 6,001,215 probe rows: 34.9 us; with the value stage as well 39.4 us;
-# the row directory with the value stage 41.1-41.6 us; a 10% / 72% shared-memory split 37.6 /
-# 42.3 us.
+# the key), which the build stage writes directly (stage bit 4), instead of reading its row
+# directory, while the bitmap can stay in L1, and then leaves shared memory (no value stage) and
+# L1 (value loads that bypass it) to the bitmap.  GB300, 1.5 M build keys (188 KB), 6,001,215
+# probe rows: probe 34.9-37.3 us; with the value stage as well 39.4 us; the row directory with
+# the value stage 41.0-41.6 us; a 10% / 72% shared-memory split 37.6 / 42.3 us.  Whole step
+# (graph replay): 91.3-93.3 us, 93.4-96.4 us with the bitmap made from the row directory by a
+# second pass, 95.4-97.4 us with the row directory.
 JOIN_DIR_BITS = True
 JOIN_BITS_MAX_BYTES = 256 << 10
 JOIN_SHARED_PERCENT = None
@@ -83,15 +85,16 @@ class JoinAggTopK:
         return (os.environ.get("TQPK_TMA", "0") == "1" and self.pk.numel() >= jit.TMA_ROWS
                 and self.pk.dtype in (torch.int32, torch.int64) and all(t.data_ptr() % 16 == 0 for t in cols))
 
+    def _probe_uses_bits(self) -> bool:
+        slots = self.key_max - self.key_min + 1
+        return bool(JOIN_DIR_BITS and not self._tma_ok() and (slots + 31) // 32 * 4 <= JOIN_BITS_MAX_BYTES)
+
     def _jit_probe(self, s):
         """The probe + aggregate pass as a query-specialised kernel."""
         from . import jit
         if not hasattr(self, "_probe_handle"):
             pp = self.ppred.struct if self.ppred else None
-            slots = self.key_max - self.key_min + 1
-            self._bits = (torch.empty((slots + 31) // 32, dtype=torch.int32, device=self.dev)
-                          if JOIN_DIR_BITS and not self._tma_ok() and (slots + 31) // 32 * 4 <= JOIN_BITS_MAX_BYTES
-                          else None)
+            self._bits = self._probe_uses_bits()
             self._probe_smem = 0
             if self._tma_ok():
                 import os
@@ -102,19 +105,16 @@ class JoinAggTopK:
                 # evict-first probe columns; with the row directory, value columns staged by cp.async
                 # (42.3-42.7 -> 41.4 us on the 6,001,215-row probe, this pipeline's timing)
                 src, name = jit.join_probe_source(self.prog.spec, self.value_reg, pp, stream_cs=True,
-                                                  stage_vals=self._bits is None, occ_sentinel=True,
-                                                  dir_bits=self._bits is not None)
+                                                  stage_vals=not self._bits, occ_sentinel=True,
+                                                  dir_bits=self._bits)
             self._probe_handle = jit.compile_kernel(src, name)
-            if self._bits is not None and JOIN_SHARED_PERCENT is not None:
+            if self._bits and JOIN_SHARED_PERCENT is not None:
                 L.check(self.lib.tqpk_jit_prefer_shared(self._probe_handle, JOIN_SHARED_PERCENT),
                         "tqpk_jit_prefer_shared")
             d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
             L.check(self.lib.tqpk_pipeline_join_tables(self.ws.data_ptr(), self.ws.numel(), self.key_min,
                                                        self.key_max, C.byref(d), C.byref(su), C.byref(oc)),
                     "tqpk_pipeline_join_tables")
-            self._dir_ptr = d.value
-            if self._bits is not None:
-                d = C.c_void_p(self._bits.data_ptr())
             self._probe_args = jit.join_probe_args(
                 jit._Args(), self.prog.spec, pp, None, self.pk,
                 self.pk.numel(), self.key_min, self.key_max - self.key_min + 1, d.value, su.value, oc.value,
@@ -127,9 +127,6 @@ class JoinAggTopK:
                                                       max(1, self.pk.numel() // jit.TMA_ROWS) * 32)
             else:
                 self._probe_grid = jit.occupancy_grid(self._probe_handle, 256, 0, jit.probe_units(self.pk.numel()))
-        if self._bits is not None:     # the build stage has just written the row directory
-            L.check(self.lib.tqpk_directory_bits(self._dir_ptr, self.key_max - self.key_min + 1,
-                                                 self._bits.data_ptr(), s), "tqpk_directory_bits")
         jit.launch(self._probe_handle, self._probe_grid, 256, self._probe_smem, self._probe_args, s,
                    L.KID_PIPE_PROBE)
 
@@ -140,7 +137,8 @@ class JoinAggTopK:
         if (jit.available() and jit.probe_supported(code_of(self.pk.dtype)) and self.pk.numel() > 0
                 and not has_strings(self.ppred.struct if self.ppred else None)):
             sent = 0 if self._tma_ok() else 8      # the generated register probe keeps occupancy in the sums
-            self._stages(1 | sent, s)
+            bits = 16 if self._probe_uses_bits() else 0   # the build stage writes the membership bitmap
+            self._stages(1 | sent | bits, s)
             self._jit_probe(s)
             self._stages(4 | sent, s)
         else:

@@ -55,6 +55,13 @@ def d2h_all(tensors):
     return out
 
 
+def plan_args(args):
+    """A fresh copy of an operator's argument dict, as a plan executor hands each operator its
+    own: the top-level lists and dicts are copied (the operators append to 'input ids' and pop
+    from 'mask map'); the parsed trees inside them are only read and stay shared."""
+    return {k: (list(v) if isinstance(v, list) else dict(v) if isinstance(v, dict) else v) for k, v in args.items()}
+
+
 class JoinAggTop10:
     name = "join_agg_top10"
     NB, NP = 1_500_000, 6_001_215
@@ -128,11 +135,11 @@ class JoinAggTop10:
             from tqpk.ingress import ColumnStager
             self.staged = ColumnStager(self.dev)
         tg = self.staged.stage(self.host, self.types, (12, 22, 11, 21, 23, 24))
-        tqp_filter(True, tg, copy.deepcopy(self.f1), None, None, None, "f1")
-        tqp_filter(True, tg, copy.deepcopy(self.f2), None, None, None, "f2")
-        join_vortex(True, tg, copy.deepcopy(self.jargs), 11, 21, [], "inner", None, None, "j")
-        tqp_hash_aggregate(True, tg, copy.deepcopy(self.aargs), None, None, "a")
-        tqp_sort(True, tg, copy.deepcopy(self.targs), True, "t")
+        tqp_filter(True, tg, plan_args(self.f1), None, None, None, "f1")
+        tqp_filter(True, tg, plan_args(self.f2), None, None, None, "f2")
+        join_vortex(True, tg, plan_args(self.jargs), 11, 21, [], "inner", None, None, "j")
+        tqp_hash_aggregate(True, tg, plan_args(self.aargs), None, None, "a")
+        tqp_sort(True, tg, plan_args(self.targs), True, "t")
         res = d2h_all({11: tg[11].tensor, 302: tg[302].tensor})
         keys, vals = res[11], res[302]
         h2d = sum(h.numel() * h.element_size() for h in self.host.values())
@@ -250,9 +257,9 @@ class FilterGroupBy:
             from tqpk.ingress import ColumnStager
             self.staged = ColumnStager(self.dev)
         tg = self.staged.stage(self.host, self.types, (7, 5, 6, 1, 2, 3, 4))
-        tqp_filter(True, tg, copy.deepcopy(self.fargs), None, None, None, "f")
-        tqp_hash_aggregate(True, tg, copy.deepcopy(self.aargs), None, None, "a")
-        tqp_sort(True, tg, copy.deepcopy(self.sargs), False, "s")
+        tqp_filter(True, tg, plan_args(self.fargs), None, None, None, "f")
+        tqp_hash_aggregate(True, tg, plan_args(self.aargs), None, None, "a")
+        tqp_sort(True, tg, plan_args(self.sargs), False, "s")
         out = {c: v.numpy() for c, v in d2h_all({c: tg[c].tensor for c in self.sargs["input ids"]}).items()}
         h2d = sum(h.numel() * h.element_size() for h in self.host.values())
         d2h = sum(v.nbytes for v in out.values())
@@ -337,11 +344,11 @@ class StarJoin:
 
     def _plan(self, tg, ops):
         f, j, a, s = ops
-        f(tg, copy.deepcopy(self.fa))
+        f(tg, plan_args(self.fa))
         for args, lk, rk in (self.j1, self.j2, self.j3):
-            tg = j(tg, copy.deepcopy(args), lk, rk)
-        tg = a(tg, copy.deepcopy(self.aargs))
-        return s(tg, copy.deepcopy(self.targs))
+            tg = j(tg, plan_args(args), lk, rk)
+        tg = a(tg, plan_args(self.aargs))
+        return s(tg, plan_args(self.targs))
 
     def step_e2e(self):
         from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort

@@ -730,3 +730,44 @@ def test_scan_staged_and_synchronous_paths_feed_the_operators(tmp_path):
         ref = O.tqp_hash_aggregate(oc, copy.deepcopy(aargs))
         np.testing.assert_array_equal(np_(tg[1].tensor), ref[1])
         assert_f64_close(np_(tg[10].tensor), ref[10])
+
+
+@pytest.mark.parametrize("spread", [1, 1_000_003])
+def test_join_key_range_feeds_the_groupby_plan(spread):
+    """An inner join's key outputs carry the filtered build-key range; the group-by that
+    follows plans from it (dense keys) or falls back to reading the keys (a range too
+    sparse for a slot table), and both give the oracle's groups."""
+    import copy
+    from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate
+    from tqpk.variable import Variable
+    rng = np.random.default_rng(spread)
+    nb, np_ = 20_000, 90_001
+    bkey = (rng.permutation(nb).astype(np.int64) * spread + 5).astype(np.int64)
+    cols = {11: bkey, 12: rng.integers(0, 2557, nb).astype(np.int32),
+            21: bkey[rng.integers(0, nb, np_)], 22: rng.integers(0, 2557, np_).astype(np.int32),
+            23: rng.integers(90000, 10495001, np_) / 100.0, 24: rng.integers(0, 11, np_) / 100.0}
+    types = {11: "int", 12: "date", 21: "int", 22: "date", 23: "float", 24: "float"}
+    tg = {c: Variable(torch.from_numpy(a).cuda(), types[c]) for c, a in cols.items()}
+    f1 = {"filter tree": [["bd#12", "<", "1170"]], "materialized in": [12], "out mask id": 901}
+    f2 = {"filter tree": [["pd#22", ">", "1170"]], "materialized in": [22], "out mask id": 902}
+    jargs = {"left group": [11, 12], "right group": [21, 22, 23, 24], "materialized in": [11, 21, 23, 24],
+             "mask map": {11: 901, 21: 902, 23: 902, 24: 902}}
+    aargs = {"is partial": False, "keys": ["k#11"], "input ids": [11, 23, 24],
+             "results": ["k#11", [[["sum", [["p#23", "*", ["1.0", "-", "d#24"]]]], "#", "301"], "AS", "rev#302"],
+                         [[["count", ["1"]], "#", "303L"], "AS", "c#304"]],
+             "out agg ids": [302, 304]}
+    tqp_filter(True, tg, copy.deepcopy(f1), None, None, None, "f1")
+    tqp_filter(True, tg, copy.deepcopy(f2), None, None, None, "f2")
+    join_vortex(True, tg, copy.deepcopy(jargs), 11, 21, [], "inner", None, None, "j")
+    kr = tg[11].key_range
+    passing = cols[11][cols[12] < 1170]
+    assert kr == (int(passing.min()), int(passing.max()))
+    tqp_hash_aggregate(True, tg, copy.deepcopy(aargs), None, None, "a")
+    oc = dict(cols)
+    oc[901] = O.eval_filter(f1["filter tree"], {12: cols[12]})
+    oc[902] = O.eval_filter(f2["filter tree"], {22: cols[22]})
+    res, _ = O.join_vortex(oc, copy.deepcopy(jargs), 11, 21, "inner")
+    agg = O.tqp_hash_aggregate(res, copy.deepcopy(aargs))
+    np.testing.assert_array_equal(tg[11].tensor.cpu().numpy().reshape(-1), agg[11].reshape(-1))
+    np.testing.assert_array_equal(tg[304].tensor.cpu().numpy().reshape(-1), agg[304].reshape(-1))
+    assert_f64_close(tg[302].tensor.cpu().numpy().reshape(-1), agg[302].reshape(-1))

@@ -9,6 +9,7 @@
 // launches it on the caller's stream.  NVRTC is opened with dlopen, so the
 // library has no link-time dependency on it; without it the interpreting
 // kernels run instead (the same results, more instructions per row).
+#include <atomic>
 #include <dlfcn.h>
 #include <stdio.h>
 #include <string.h>
@@ -71,7 +72,18 @@ bool nvrtc_open() {
 struct JitKernel {
   cudaLibrary_t lib;
   cudaKernel_t kernel;
+  std::atomic<size_t> smem_allowed{0};   // dynamic shared memory the kernel has been opened up to
 };
+
+// Raises the kernel's dynamic shared-memory limit once per new maximum: the attribute call
+// costs tens of microseconds of host time, too much to repeat on every launch.
+static cudaError_t allow_smem(JitKernel* k, size_t smem) {
+  if (smem <= k->smem_allowed.load(std::memory_order_relaxed)) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k->kernel),
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) k->smem_allowed.store(smem, std::memory_order_relaxed);
+  return e;
+}
 
 }  // namespace
 }  // namespace tqpk
@@ -147,8 +159,7 @@ extern "C" int tqpk_jit_occupancy(void* handle, int32_t block, size_t smem) {
   JitKernel* k = static_cast<JitKernel*>(handle);
   int per_sm = 0;
   if (smem > 0)   // dynamic + static shared memory may pass the 48 KB default even when smem alone does not
-    cudaFuncSetAttribute(reinterpret_cast<const void*>(k->kernel), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
+    (void)allow_smem(k, smem);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(k->kernel), block, smem) !=
       cudaSuccess) {
     (void)cudaGetLastError();
@@ -174,9 +185,7 @@ extern "C" int tqpk_jit_launch(void* handle, int32_t grid, int32_t block, size_t
   if (!handle || grid < 1 || block < 1 || !args) return TQPK_EINVAL;
   JitKernel* k = static_cast<JitKernel*>(handle);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (smem > 0)
-    TQPK_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(k->kernel),
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (smem > 0) TQPK_CUDA(allow_smem(k, smem));
   if (timing_kid) timing_before(timing_kid, s);
   const cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(k->kernel), dim3(grid), dim3(block), args,
                                          smem, s);

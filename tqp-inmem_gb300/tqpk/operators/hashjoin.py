@@ -75,7 +75,8 @@ def _pairs(tensors_left, tensors_right, left_key, right_key, condition_list, jty
         (bi, pi), _ = compact([bi, pi], mask=keep)
     if condition_list and jtype != "inner":
         bi, pi = _non_inner(bi, pi, rk, right_mask, jtype)
-    return bi, pi, b.plan.nb_rows
+    key_range = (int(b.plan.key_min), int(b.plan.key_max)) if b.plan.key_max >= b.plan.key_min else None
+    return bi, pi, b.plan.nb_rows, key_range
 
 
 def _non_inner(bi, pi, rk, right_mask, jtype):
@@ -116,7 +117,8 @@ def join_kernel_new(gpu_enable, tensors_left, tensors_right, left_key, right_key
     assert type in {"inner", "right-semi", "right-anti", "right-outer"}, "Invalid Join type."
     _normalize(tensors_left[left_key])
     _normalize(tensors_right[right_key])
-    bi, pi, _ = _pairs(tensors_left, tensors_right, left_key, right_key, condition_list, type, left_mask, right_mask)
+    bi, pi, _, _ = _pairs(tensors_left, tensors_right, left_key, right_key, condition_list, type, left_mask,
+                          right_mask)
     return _outputs(tensors_left, tensors_right, join_output_keys, type, bi, pi, return_global_index,
                     left_global_idx, right_global_idx)
 
@@ -218,7 +220,8 @@ def join_vortex(gpu_enable, tensor_group, args, leftcol, rightcol, condition_lis
     tr = {k: tensor_group[k] for k in groupings[RIGHT] if k in tensor_group}
     if leftcol not in tl or rightcol not in tr:
         raise KeyError("join key is not in its side's group")
-    bi, pi, nb_rows = _pairs(tl, tr, leftcol, rightcol, condition_list, type, masks[LEFT], masks[RIGHT])
+    bi, pi, nb_rows, key_range = _pairs(tl, tr, leftcol, rightcol, condition_list, type, masks[LEFT],
+                                        masks[RIGHT])
     # only "does the probe side have rows" matters (hashjoin.py:161-172); any output row answers it
     if pi.numel() > 0:
         np_rows = int(pi.numel())
@@ -230,4 +233,6 @@ def join_vortex(gpu_enable, tensor_group, args, leftcol, rightcol, condition_lis
         tensor_group[k] = make_like(tensor_group[k], outs[i], tensor_group[k].tensor_type)
         if k in late:                                  # gathered on a side stream after a late input
             tensor_group[k].ready = late[k]
+        if type == "inner" and key_range is not None and k in (leftcol, rightcol):
+            tensor_group[k].key_range = key_range      # every output key equals a filtered build key
     return next(iter(tensor_group.values())).tensor.size(0)

@@ -115,19 +115,32 @@ def compact(cols: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = None,
 
 # ---------------------------------------------------------------- (d) group-by
 def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor] = None,
-            pred: Optional[CompiledPredicate] = None, before_values=None):
+            pred: Optional[CompiledPredicate] = None, before_values=None, key_ranges=None):
     """Runs the compiled aggregate; returns (key columns [G], {out id: column}, G).
     before_values, when given, is called after the plan (which reads only the keys and
-    the mask) and before the first kernel that reads the value columns."""
+    the mask) and before the first kernel that reads the value columns.  key_ranges, when
+    given, bounds each key column ((min, max) per key, in spec order): the plan is made from
+    them without reading the keys (no host synchronisation), unless they call for the hash
+    table of sparse key spaces."""
     lib = L.load()
     _check_cuda(mask, *prog.tensors)
     s = _stream(device)
     plan = L.GbPlan()
-    scratch = _ws(256, device)
     pp = C.byref(pred.struct) if pred is not None else None
     mp = mask.data_ptr() if mask is not None else None
-    L.check(lib.tqpk_groupby_plan(C.byref(prog.spec), pp, mp, n, C.byref(plan), scratch.data_ptr(), s),
-            "tqpk_groupby_plan")
+    planned = False
+    if key_ranges is not None and len(key_ranges) == prog.spec.n_keys and n > 0:
+        nk = prog.spec.n_keys
+        kmin = (C.c_int64 * max(nk, 1))(*[int(r[0]) for r in key_ranges])
+        kmax = (C.c_int64 * max(nk, 1))(*[int(r[1]) for r in key_ranges])
+        planned = (lib.tqpk_groupby_plan_domains(C.byref(prog.spec), kmin, kmax, n, C.byref(plan)) == 0
+                   and plan.mode != L.GB_HASH)
+        if not planned:
+            plan = L.GbPlan()
+    if not planned:
+        scratch = _ws(256, device)
+        L.check(lib.tqpk_groupby_plan(C.byref(prog.spec), pp, mp, n, C.byref(plan), scratch.data_ptr(), s),
+                "tqpk_groupby_plan")
     ws = _ws(plan.ws_bytes, device)
     groups = C.c_int64(0)
     if before_values is not None:

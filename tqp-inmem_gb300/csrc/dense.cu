@@ -175,7 +175,8 @@ extern "C" int tqpk_dense_topk(const double* d_sum, const uint32_t* d_cnt, int64
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   TQPK_CUDA(cudaMemsetAsync(hdr, 0, 256, s));
   DenseSumSource src{d_sum, reinterpret_cast<const unsigned*>(d_cnt), slots, descending ? 1 : 0};
-  TopkOut O{top_idx, count, cand_key, cand_idx, ticket, groups, reinterpret_cast<unsigned long long*>(hdr + 6)};
+  TopkOut O{top_idx, count, cand_key, cand_idx, ticket, groups, reinterpret_cast<unsigned long long*>(hdr + 6),
+            hdr + 8};
   timing_before(KID_PIPE_TOPK, s);
   int rc = topk_warp_launch(0, &src, k, grid, O, s);
   timing_after(KID_PIPE_TOPK, s);

@@ -291,11 +291,11 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
     TQPK_CHECK_LAUNCH();
   }
   if (stages & 4) {
-    TQPK_CUDA(cudaMemsetAsync(L.top_count + 1, 0, 8, s));   // the top-k cut of this run
+    TQPK_CUDA(cudaMemsetAsync(L.top_count + 1, 0, 16, s));  // the top-k cut and arrival counters of this run
     TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 8, s));          // the group count the top-k pass accumulates
     DenseSumSource src{L.sum, sentinel ? nullptr : L.cnt, slots, A.desc};
     TopkOut O{L.top_idx, L.top_count, L.cand_key, L.cand_slot, L.done, L.groups,
-              reinterpret_cast<unsigned long long*>(L.top_count + 1)};   // hdr[6..7], zeroed with the header
+              reinterpret_cast<unsigned long long*>(L.top_count + 1), reinterpret_cast<unsigned*>(L.top_count + 2)};   // hdr[6..7], zeroed with the header
     timing_before(KID_PIPE_TOPK, s);
     int trc = topk_warp_launch(0, &src, k, grid, O, s);
     timing_after(KID_PIPE_TOPK, s);

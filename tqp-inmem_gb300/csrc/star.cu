@@ -279,7 +279,8 @@ extern "C" int tqpk_pipeline_star_agg_topk(
   }
   DenseSumSource src{L.sum, L.cnt, cs, descending ? 1 : 0};
   TopkOut O{L.top_idx, L.top_count, L.cand_key, L.cand_idx, L.ticket, L.groups,
-            reinterpret_cast<unsigned long long*>(L.top_count + 1)};   // zeroed with the header
+            reinterpret_cast<unsigned long long*>(L.top_count + 1),    // zeroed with the header
+            reinterpret_cast<unsigned*>(L.top_count + 2)};
   rc = topk_warp_launch(0, &src, k, grid, O, s);
   if (rc) return rc;
   k_star_emit<<<1, 256, 0, s>>>(L.top_idx, L.top_count, L.sum, L.cnt, c_min, k, d_out_keys, d_out_vals, d_out_counts,

@@ -19,16 +19,12 @@ static int launch_r(const Src& src, int k, int grid, TopkOut O, cudaStream_t s) 
   int64_t G = 4;
   while (G * kTopkGroups < src.n) G <<= 1;
   const int ng = (int)std::max<int64_t>(1, (src.n + G - 1) / G);
-  k_tk_group_best<Src><<<ng, 256, 0, s>>>(src, G, O);
+  k_tk_group_best<Src><<<ng, 256, 0, s>>>(src, G, k, O);
   TQPK_CHECK_LAUNCH();
-  k_tk_cut<<<1, 256, 0, s>>>(ng, k, O);
-  TQPK_CHECK_LAUNCH();
+  // the filter CTAs hold tk_final's 32 KB sort buffer: 4 per SM keeps them in one wave
   const int64_t units = (src.n + 1023) / 1024;
-  k_tk_filter<Src><<<(int)std::max<int64_t>(1, std::min<int64_t>(units, (int64_t)num_sms() * 8)), 256, 0, s>>>(src, O);
-  TQPK_CHECK_LAUNCH();
-  const size_t smem = (size_t)kTopkCap * 16;
-  TQPK_CUDA(cudaFuncSetAttribute(k_tk_final<R, Src>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_tk_final<R, Src><<<1, 256, smem, s>>>(src, k, O);
+  k_tk_filter<R, Src><<<(int)std::max<int64_t>(1, std::min<int64_t>(units, (int64_t)num_sms() * 4)), 256, 0, s>>>(
+      src, k, O);
   TQPK_CHECK_LAUNCH();
   return TQPK_OK;
 }
@@ -90,7 +86,7 @@ extern "C" int tqpk_topk_stable(const void* d_keys, int32_t dt, int32_t desc, co
   if (!ci) return TQPK_ENOMEM;
   TQPK_CUDA(cudaMemsetAsync(ticket, 0, 256, s));
   ArraySource src{d_keys, dt, d_perm_in, n, desc ? 1 : 0};
-  TopkOut O{idx, count, ck, ci, ticket, nullptr, reinterpret_cast<unsigned long long*>(ticket + 8)};
+  TopkOut O{idx, count, ck, ci, ticket, nullptr, reinterpret_cast<unsigned long long*>(ticket + 8), ticket + 16};
   timing_before(KID_PIPE_TOPK, s);
   int rc = topk_warp_launch(1, &src, (int)k, grid, O, s);
   timing_after(KID_PIPE_TOPK, s);

@@ -184,6 +184,7 @@ struct TopkOut {
   unsigned* ticket;
   unsigned long long* valid_total;  // number of valid items seen (may be null)
   unsigned long long* bound;        // ~(best known k-th key), raised with atomicMax; 0 = none (zeroed with the ticket)
+  unsigned* arrive;                 // [2] CTAs done with the group-best and the filter pass (zeroed before the launch)
 };
 
 // ---------------------------------------------------------------------------
@@ -193,9 +194,11 @@ struct TopkOut {
 // at or below it (every one of those k groups holds one), so the top k are
 // all among the items with key <= T.  For independent keys only about k
 // items pass T.  A second pass appends them to a candidate list (at most
-// kTopkCap), and one CTA sorts the list bitonically by (key, index).  When
-// ties push more than kTopkCap items under the cut, that CTA falls back to
-// the warp lists over all items (same result, slower).
+// kTopkCap), and the last CTA of that pass sorts the list bitonically by
+// (key, index) in shared memory.  When ties push more than kTopkSortCap items
+// under the cut, that CTA falls back to the warp lists over all items (same
+// result, slower).  The cut itself is computed by the last CTA of the first
+// pass, so the whole top-k is two launches.
 constexpr int kTopkCap = 4096;
 constexpr int kTopkGroups = 512;     // >= 2 x the largest k: the cut stays near the k-th item
 constexpr int kTopkCand = kTopkCap + kTopkGroups;   // cand_key entries used: candidates, then group bests
@@ -217,8 +220,41 @@ __device__ __forceinline__ void block_min_u64(uint64_t& v, uint64_t* red) {
   v = red[0];
 }
 
+// True in the last CTA of the grid to get here, after every other CTA has made its
+// writes visible; all threads of every CTA call it once, at the end of the kernel.  No CTA
+// waits for another: the others have finished.
+__device__ __forceinline__ bool tk_last_cta(unsigned* arrive) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(arrive, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+// The cut: the k-th best of the ng group bests (bitonic sort of the bests in one CTA).
+__device__ __forceinline__ void tk_cut(int ng, int k, TopkOut O) {
+  __shared__ uint64_t v[kTopkGroups];
+  for (int i = threadIdx.x; i < kTopkGroups; i += blockDim.x) v[i] = i < ng ? __ldcg(&O.cand_key[kTopkCap + i]) : ~0ull;
+  __syncthreads();
+  for (int size = 2; size <= kTopkGroups; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < kTopkGroups / 2; t += blockDim.x) {
+        const int i = 2 * t - (t & (stride - 1)), j = i + stride;
+        const bool up = (i & size) == 0;
+        const uint64_t a = v[i], b = v[j];
+        if ((a > b) == up) { v[i] = b; v[j] = a; }
+      }
+      __syncthreads();
+    }
+  if (threadIdx.x == 0) *O.bound = v[(k <= kTopkGroups ? k : kTopkGroups) - 1];
+}
+
+// Pass 1: each CTA keeps the best key of its group of G items; the last CTA to finish
+// computes the cut from all groups' bests.
 template <class Src>
-__global__ void __launch_bounds__(256) k_tk_group_best(Src src, int64_t G, TopkOut O) {
+__global__ void __launch_bounds__(256) k_tk_group_best(Src src, int64_t G, int k, TopkOut O) {
   __shared__ uint64_t red[8];
   const int64_t b0 = (int64_t)blockIdx.x * G, b1 = b0 + G < src.n ? b0 + G : src.n;
   uint64_t best = ~0ull;
@@ -240,59 +276,19 @@ __global__ void __launch_bounds__(256) k_tk_group_best(Src src, int64_t G, TopkO
     O.cand_key[kTopkCap + blockIdx.x] = best;
     if (blockIdx.x == 0) *O.ticket = 0;          // the candidate counter of the next pass
   }
+  if (tk_last_cta(O.arrive)) tk_cut((int)gridDim.x, k, O);
 }
 
-// one CTA of 256 threads: bitonic sort of the group bests, cut = the k-th
-static __global__ void __launch_bounds__(256) k_tk_cut(int ng, int k, TopkOut O) {
-  __shared__ uint64_t v[kTopkGroups];
-  for (int i = threadIdx.x; i < kTopkGroups; i += blockDim.x) v[i] = i < ng ? __ldcg(&O.cand_key[kTopkCap + i]) : ~0ull;
-  __syncthreads();
-  for (int size = 2; size <= kTopkGroups; size <<= 1)
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int t = threadIdx.x; t < kTopkGroups / 2; t += blockDim.x) {
-        const int i = 2 * t - (t & (stride - 1)), j = i + stride;
-        const bool up = (i & size) == 0;
-        const uint64_t a = v[i], b = v[j];
-        if ((a > b) == up) { v[i] = b; v[j] = a; }
-      }
-      __syncthreads();
-    }
-  if (threadIdx.x == 0) *O.bound = v[(k <= kTopkGroups ? k : kTopkGroups) - 1];
-}
+constexpr int kTopkSortCap = 2048;   // candidates the final CTA sorts in shared memory
 
-template <class Src>
-__global__ void __launch_bounds__(256) k_tk_filter(Src src, TopkOut O) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint64_t cut = __ldcg(O.bound);
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
-  for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + warp * 32) * 4; base < src.n; base += stride) {
-    const int64_t i0 = base + lane * 4;
-    uint64_t key[4];
-    const unsigned ok = src.get4(i0, key);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const bool pass = ((ok >> q) & 1u) && key[q] <= cut;
-      const unsigned bal = __ballot_sync(0xffffffffu, pass);
-      if (!bal) continue;
-      unsigned at = 0;
-      if (lane == 0) at = atomicAdd(O.ticket, (unsigned)__popc(bal));
-      at = __shfl_sync(0xffffffffu, at, 0) + __popc(bal & ((1u << lane) - 1u));
-      if (pass && at < (unsigned)kTopkCap) {
-        O.cand_key[at] = key[q];
-        O.cand_idx[at] = i0 + q;
-      }
-    }
-  }
-}
-
-// one CTA of 256 threads: sort the candidates (or, past kTopkCap, rescan with warp lists)
+// The final step, in one CTA: sort the candidates under the cut by (key, index), or, when
+// ties put more than kTopkSortCap items under it, warp lists over every item.
 template <int R, class Src>
-__global__ void __launch_bounds__(256) k_tk_final(Src src, int k, TopkOut O) {
-  extern __shared__ unsigned char tk_smem[];
-  uint64_t* sk = reinterpret_cast<uint64_t*>(tk_smem);           // [kTopkCap]
-  int64_t* si = reinterpret_cast<int64_t*>(sk + kTopkCap);
+__device__ __forceinline__ void tk_final(const Src& src, int k, TopkOut O) {
+  __shared__ uint64_t sk[kTopkSortCap];
+  __shared__ int64_t si[kTopkSortCap];
   const unsigned cnt = __ldcg(O.ticket);
-  if (cnt <= (unsigned)kTopkCap) {
+  if (cnt <= (unsigned)kTopkSortCap) {
     int P = 2;
     while (P < (int)cnt) P <<= 1;
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -317,7 +313,6 @@ __global__ void __launch_bounds__(256) k_tk_final(Src src, int k, TopkOut O) {
     if (threadIdx.x == 0) *O.out_count = m;
     return;
   }
-  // ties put more than kTopkCap items under the cut: warp lists over every item
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   WarpList<R> L;
   L.init();
@@ -354,8 +349,36 @@ __global__ void __launch_bounds__(256) k_tk_final(Src src, int k, TopkOut O) {
   if (lane == 0) *O.out_count = c;
 }
 
+// Pass 2: the items at or under the cut are appended to the candidate list; the last CTA
+// to finish sorts them (tk_final).  Blocks of 256 threads (tk_final's 8 warps).
+template <int R, class Src>
+__global__ void __launch_bounds__(256) k_tk_filter(Src src, int k, TopkOut O) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t cut = __ldcg(O.bound);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
+  for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + warp * 32) * 4; base < src.n; base += stride) {
+    const int64_t i0 = base + lane * 4;
+    uint64_t key[4];
+    const unsigned ok = src.get4(i0, key);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const bool pass = ((ok >> q) & 1u) && key[q] <= cut;
+      const unsigned bal = __ballot_sync(0xffffffffu, pass);
+      if (!bal) continue;
+      unsigned at = 0;
+      if (lane == 0) at = atomicAdd(O.ticket, (unsigned)__popc(bal));
+      at = __shfl_sync(0xffffffffu, at, 0) + __popc(bal & ((1u << lane) - 1u));
+      if (pass && at < (unsigned)kTopkCap) {
+        O.cand_key[at] = key[q];
+        O.cand_idx[at] = i0 + q;
+      }
+    }
+  }
+  if (tk_last_cta(O.arrive + 1)) tk_final<R>(src, k, O);
+}
+
 // Host launcher: k <= 256.  The cand arrays hold topk_cand_entries(k) entries each;
-// O.ticket, O.bound and O.valid_total must be zero before the call.
+// O.ticket, O.bound, O.arrive[0..1] and O.valid_total must be zero before the call.
 int topk_warp_launch(int kind, const void* src, int k, int grid, TopkOut O, cudaStream_t s);
 inline int topk_grid_size() { return num_sms(); }
 inline size_t topk_cand_entries(int k) {

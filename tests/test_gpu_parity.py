@@ -759,7 +759,7 @@ def test_join_key_range_feeds_the_groupby_plan(spread):
     tqp_filter(True, tg, copy.deepcopy(f1), None, None, None, "f1")
     tqp_filter(True, tg, copy.deepcopy(f2), None, None, None, "f2")
     join_vortex(True, tg, copy.deepcopy(jargs), 11, 21, [], "inner", None, None, "j")
-    kr = tg[11].key_range
+    kr = tg[11]._key_range
     passing = cols[11][cols[12] < 1170]
     assert kr == (int(passing.min()), int(passing.max()))
     tqp_hash_aggregate(True, tg, copy.deepcopy(aargs), None, None, "a")

@@ -80,7 +80,7 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
             keys_out[i] = k if k.dim() == 2 else k.reshape(G, 1)     # unique_key_cols[:, pos_l:pos_r]
     else:
         prog = compile_aggregate(args, cols, derived=True)
-        ranges = [getattr(tensor_group[kid], "key_range", None) for kid in prog.key_ids]
+        ranges = [getattr(tensor_group[kid], "_key_range", None) for kid in prog.key_ids]
         keys, vals_out, G, _ = groupby(prog, n, device, mask=mask, before_values=values_ready,
                                        key_ranges=ranges if ranges and all(r is not None for r in ranges) else None)
         keys_out = {}

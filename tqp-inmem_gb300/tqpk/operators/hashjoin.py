@@ -234,5 +234,5 @@ def join_vortex(gpu_enable, tensor_group, args, leftcol, rightcol, condition_lis
         if k in late:                                  # gathered on a side stream after a late input
             tensor_group[k].ready = late[k]
         if type == "inner" and key_range is not None and k in (leftcol, rightcol):
-            tensor_group[k].key_range = key_range      # every output key equals a filtered build key
+            tensor_group[k]._key_range = key_range     # every output key equals a filtered build key
     return next(iter(tensor_group.values())).tensor.size(0)

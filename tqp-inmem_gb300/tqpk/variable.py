@@ -27,10 +27,11 @@ class Variable:
         self.backing_mem_ptr = backing_mem_ptr
         self.is_sorted = is_sorted
         self.ready = ready      # CUDA event after which the tensor's data is on the device (None: already)
-        # inclusive (min, max) bound on the values, known to whoever made the column (a table
-        # statistic, or an inner join's build-key range for its key columns); a group-by over
-        # columns that carry one plans its slot table from it without a key-range pass
-        self.key_range = None
+        # inclusive (min, max) bound on the values, set by join_vortex only (an inner join's key
+        # outputs all lie in the filtered build side's key range); a group-by over columns that
+        # carry one plans its slot table from it without a key-range pass.  The group-by indexes
+        # its table with this bound, so nothing else sets it.
+        self._key_range = None
 
     def __repr__(self):
         return f"Variable (tensor size = {self.tensor.shape} ({self.tensor.dtype}), tensor type = '{self.tensor_type}')"

@@ -24,7 +24,7 @@ def _ws(nbytes: int, device) -> torch.Tensor:
 
 
 def _stream(device) -> int:
-    return torch.cuda.current_stream(device).cuda_stream
+    return L.stream_handle(device)
 
 
 def _col1d(t: torch.Tensor) -> torch.Tensor:

@@ -443,6 +443,15 @@ int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64_t n, const
  * the composed directory then needs no lookup in the next one.              */
 int tqpk_directory_compose(int32_t* d_dir, int64_t slots, const int32_t* d_next, int64_t next_min,
                            int64_t next_slots, int32_t empty, int32_t fail_value, tqpk_stream stream);
+/* tqpk_directory_build with the composition built in: a payload (a key of
+ * the next table's domain) is kept only when d_next[payload - next_min] >= 0,
+ * else the entry becomes fail_value; the same directory as build followed by
+ * tqpk_directory_compose, without the second pass over it.  d_next is built
+ * first (the snowflake chain's last table first).                          */
+int tqpk_directory_build_next(const void* d_keys, int32_t key_dtype, int64_t n, const tqpk_predicate* h_pred,
+                              const void* d_payload, int32_t payload_dtype, int64_t key_min, int64_t slots,
+                              int32_t empty, int32_t fail_value, const int32_t* d_next, int64_t next_min,
+                              int64_t next_slots, int32_t* d_dir, int32_t* d_err, tqpk_stream stream);
 /* Membership bitmap of a row directory: bit s of d_bits (word s / 32, bit
  * s % 32) is set when d_dir[s] >= 0.  d_bits holds (slots + 31) / 32 words.
  * A probe that only asks whether a dimension key has a row that passed the

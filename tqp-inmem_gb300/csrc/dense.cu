@@ -27,9 +27,11 @@ namespace tqpk {
 __global__ void __launch_bounds__(kBlock) k_dir_build(const __grid_constant__ tqpk_predicate P, const void* keys,
                                                       int dt, const void* payload, int pdt, int64_t n, int64_t kmin,
                                                       int64_t slots, int empty, int fail_value, int pvec,
-                                                      int* __restrict__ dir, int* err) {
+                                                      const int* __restrict__ next, int64_t next_min,
+                                                      int64_t next_slots, int* __restrict__ dir, int* err) {
   const int64_t groups = (n + 3) >> 2;
   const bool kvec = ((reinterpret_cast<uintptr_t>(keys) & 15u) == 0);
+  const bool plvec = ((reinterpret_cast<uintptr_t>(payload) & 15u) == 0);
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups;
        g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r0 = g << 2;
@@ -38,7 +40,7 @@ __global__ void __launch_bounds__(kBlock) k_dir_build(const __grid_constant__ tq
     int64_t x[4];
     ld4_int(keys, dt, r0, n, kvec, x);
     int64_t pl[4] = {r0, r0 + 1, r0 + 2, r0 + 3};
-    if (payload) ld4_int(payload, pdt, r0, n, false, pl);
+    if (payload) ld4_int(payload, pdt, r0, n, plvec, pl);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       if (!((live >> j) & 1u)) break;
@@ -46,8 +48,13 @@ __global__ void __launch_bounds__(kBlock) k_dir_build(const __grid_constant__ tq
       if (slot < 0 || slot >= slots) { set_error(err, TQPK_EINVAL); continue; }
       // a payload outside int32, or equal to the empty marker, cannot name a key of the
       // next (int32) domain: the row stays in the directory as a non-matching entry
-      const bool pl_ok = pl[j] >= (int64_t)INT32_MIN && pl[j] <= (int64_t)INT32_MAX && pl[j] != (int64_t)empty;
-      const int v = (((pass >> j) & 1u) && pl_ok) ? (int)pl[j] : fail_value;
+      bool ok = ((pass >> j) & 1u) && pl[j] >= (int64_t)INT32_MIN && pl[j] <= (int64_t)INT32_MAX &&
+                pl[j] != (int64_t)empty;
+      if (ok && next) {        // composed with the next table: keep a payload key that has a row there
+        const int64_t q = pl[j] - next_min;
+        ok = q >= 0 && q < next_slots && __ldg(&next[q]) >= 0;
+      }
+      const int v = ok ? (int)pl[j] : fail_value;
       if (atomicCAS(&dir[slot], empty, v) != empty) set_error(err, TQPK_EUNSUPPORTED);  // repeated key
     }
   }
@@ -81,11 +88,12 @@ constexpr int kDenseMaxK = 256;
 
 using namespace tqpk;
 
-extern "C" int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64_t n, const tqpk_predicate* h_pred,
-                                    const void* d_payload, int32_t payload_dtype, int64_t key_min, int64_t slots,
-                                    int32_t empty, int32_t fail_value, int32_t* d_dir, int32_t* d_err,
-                                    tqpk_stream stream) {
+static int directory_build(const void* d_keys, int32_t key_dtype, int64_t n, const tqpk_predicate* h_pred,
+                           const void* d_payload, int32_t payload_dtype, int64_t key_min, int64_t slots,
+                           int32_t empty, int32_t fail_value, const int32_t* d_next, int64_t next_min,
+                           int64_t next_slots, int32_t* d_dir, int32_t* d_err, tqpk_stream stream) {
   if (n < 0 || slots < 1 || slots > (int64_t(1) << 31) || !d_dir || !d_err || (n > 0 && !d_keys)) return TQPK_EINVAL;
+  if (d_next && (!d_payload || next_slots < 1)) return TQPK_EINVAL;
   if (!is_int_dtype(key_dtype) || (d_payload && !is_int_dtype(payload_dtype))) return TQPK_EDTYPE;
   if (!d_payload && n > (int64_t)INT32_MAX) return TQPK_EUNSUPPORTED;  // row indices travel as int32
   if (fail_value == empty) return TQPK_EINVAL;
@@ -96,12 +104,31 @@ extern "C" int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64
   k_dir_fill<<<grid_for(slots, 4), kBlock, 0, s>>>(d_dir, slots, empty);
   TQPK_CHECK_LAUNCH();
   if (n > 0) {
-    k_dir_build<<<grid_for((n + 3) / 4, 4), kBlock, 0, s>>>(*pred_or_empty(h_pred), d_keys, key_dtype, d_payload,
+    k_dir_build<<<grid_for((n + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_pred), d_keys, key_dtype, d_payload,
                                                            payload_dtype, n, key_min, slots, empty, fail_value,
-                                                           pred_vec_ok(h_pred) ? 1 : 0, d_dir, d_err);
+                                                           pred_vec_ok(h_pred) ? 1 : 0, d_next, next_min, next_slots,
+                                                           d_dir, d_err);
     TQPK_CHECK_LAUNCH();
   }
   return TQPK_OK;
+}
+
+extern "C" int tqpk_directory_build(const void* d_keys, int32_t key_dtype, int64_t n, const tqpk_predicate* h_pred,
+                                    const void* d_payload, int32_t payload_dtype, int64_t key_min, int64_t slots,
+                                    int32_t empty, int32_t fail_value, int32_t* d_dir, int32_t* d_err,
+                                    tqpk_stream stream) {
+  return directory_build(d_keys, key_dtype, n, h_pred, d_payload, payload_dtype, key_min, slots, empty, fail_value,
+                         nullptr, 0, 0, d_dir, d_err, stream);
+}
+
+extern "C" int tqpk_directory_build_next(const void* d_keys, int32_t key_dtype, int64_t n,
+                                         const tqpk_predicate* h_pred, const void* d_payload, int32_t payload_dtype,
+                                         int64_t key_min, int64_t slots, int32_t empty, int32_t fail_value,
+                                         const int32_t* d_next, int64_t next_min, int64_t next_slots,
+                                         int32_t* d_dir, int32_t* d_err, tqpk_stream stream) {
+  if (!d_next) return TQPK_EINVAL;
+  return directory_build(d_keys, key_dtype, n, h_pred, d_payload, payload_dtype, key_min, slots, empty, fail_value,
+                         d_next, next_min, next_slots, d_dir, d_err, stream);
 }
 
 // dir[i] (a key of the next table's domain) keeps its value only when the next

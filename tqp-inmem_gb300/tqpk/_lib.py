@@ -138,6 +138,8 @@ SIGNATURES = {
     "tqpk_pipeline_join_tables": (C.c_int, [_VP, _SZ, _I64, _I64, _P(_VP), _P(_VP), _P(_VP)]),
     "tqpk_directory_build": (C.c_int, [_VP, _I32, _I64, _P(Predicate), _VP, _I32, _I64, _I64, _I32, _I32, _VP, _VP,
                                        _VP]),
+    "tqpk_directory_build_next": (C.c_int, [_VP, _I32, _I64, _P(Predicate), _VP, _I32, _I64, _I64, _I32, _I32,
+                                            _VP, _I64, _I64, _VP, _VP, _VP]),
     "tqpk_dense_topk_workspace_bytes": (_SZ, [_I32]),
     "tqpk_dense_topk": (C.c_int, [_VP, _VP, _I64, _I64, _I32, _I32, _VP, _SZ, _VP, _VP, _VP, _VP, _VP, _VP]),
     "tqpk_groupby_emit_async": (C.c_int, [_P(GroupbySpec), _P(GbPlan), _VP, _P(_VP), _I32, _P(_I32), _P(_VP), _VP,

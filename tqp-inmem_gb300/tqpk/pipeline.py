@@ -293,12 +293,13 @@ class StarAggTopK:
         e = self.err.data_ptr()
         L.check(build(ak.data_ptr(), code_of(ak.dtype), ak.numel(), ap, None, 0, amn, amx - amn + 1, -1, -2,
                       self.dir_a.data_ptr(), e, s), "tqpk_directory_build")
-        L.check(build(bk.data_ptr(), code_of(bk.dtype), bk.numel(), None, bc.data_ptr(), code_of(bc.dtype), bmn,
-                      bmx - bmn + 1, INT_MIN, INT_MIN + 1, self.dir_b.data_ptr(), e + 4, s), "tqpk_directory_build")
         L.check(build(ck.data_ptr(), code_of(ck.dtype), ck.numel(), None, None, 0, cmn, cmx - cmn + 1, -1, -2,
                       self.dir_c.data_ptr(), e + 8, s), "tqpk_directory_build")
-        L.check(self.lib.tqpk_directory_compose(self.dir_b.data_ptr(), self.dir_b.numel(), self.dir_c.data_ptr(), cmn,
-                                                cmx - cmn + 1, INT_MIN, INT_MIN + 1, s), "tqpk_directory_compose")
+        # B's directory of C keys, composed with C's as it is built (a C key without a C row fails)
+        L.check(self.lib.tqpk_directory_build_next(
+            bk.data_ptr(), code_of(bk.dtype), bk.numel(), None, bc.data_ptr(), code_of(bc.dtype), bmn, bmx - bmn + 1,
+            INT_MIN, INT_MIN + 1, self.dir_c.data_ptr(), cmn, cmx - cmn + 1, self.dir_b.data_ptr(), e + 4, s),
+            "tqpk_directory_build_next")
         if self._a_bits:
             L.check(self.lib.tqpk_directory_bits(self.dir_a.data_ptr(), self.dir_a.numel(), self.bits_a.data_ptr(), s),
                     "tqpk_directory_bits")

@@ -266,6 +266,22 @@ def test_topk_threshold_path_and_tie_fallback(n, k, hi, desc):
     np.testing.assert_array_equal(got, O._stable_order(x, desc)[:k])
 
 
+@pytest.mark.parametrize("ties", [1500, 3000, 5000])
+@pytest.mark.parametrize("desc", [True, False])
+def test_topk_tied_candidates_around_the_sort_capacity(ties, desc):
+    """A block of equal best keys puts `ties` items under the cut: up to 2048 the last filter
+    CTA sorts them in shared memory, above that it takes the warp lists; both keep the
+    stable order (smaller position first among equal keys)."""
+    from tqpk.ops import topk_stable
+    rng = np.random.default_rng(ties)
+    n = 300_007
+    x = rng.integers(1000, 1 << 40, n).astype(np.int64)
+    x[rng.choice(n, ties, replace=False)] = (1 << 41) if desc else 5
+    for k in (10, 100):
+        got = topk_stable(torch.from_numpy(x).cuda(), k, desc).cpu().numpy()
+        np.testing.assert_array_equal(got, O._stable_order(x, desc)[:k])
+
+
 @pytest.mark.parametrize("n,groups", [(1_000_003, 6), (200_000, 1400), (50_000, 30_000), (3, 4)])
 def test_groupby_pipeline_domains_and_graph_replay(n, groups):
     """Filter + group-by over table-statistic key domains, no host synchronisation inside;

@@ -266,6 +266,45 @@ def test_topk_threshold_path_and_tie_fallback(n, k, hi, desc):
     np.testing.assert_array_equal(got, O._stable_order(x, desc)[:k])
 
 
+@pytest.mark.parametrize("repeat", [False, True])
+@pytest.mark.parametrize("n,slots", [(15_000, 20_011), (1_000_003, 1_000_003), (5, 7)])
+def test_directory_build_next_matches_build_then_compose(repeat, n, slots):
+    """tqpk_directory_build_next (composition with the next directory while building) writes
+    the same directory as tqpk_directory_build + tqpk_directory_compose, and reports a
+    repeated key the same way."""
+    import ctypes as C
+    from tqpk import _lib as L
+    from tqpk.predicate import compile_filter
+    lib = L.load()
+    rng = np.random.default_rng(n + int(repeat))
+    keys = (rng.permutation(slots)[:n] + 3).astype(np.int32)
+    if repeat and n > 1:
+        keys[-1] = keys[0]
+    nxt_slots = 997
+    payload = rng.integers(-5, nxt_slots + 10, n).astype(np.int32)
+    cat = rng.integers(0, 3, n).astype(np.int32)
+    nxt = np.where(rng.random(nxt_slots) < 0.6, np.arange(nxt_slots), -1).astype(np.int32)
+    d = {k: torch.from_numpy(v).cuda() for k, v in (("k", keys), ("p", payload), ("c", cat), ("x", nxt))}
+    pred = compile_filter([["c#1", "<", "2"]], {1: d["c"]})
+    s = torch.cuda.current_stream().cuda_stream
+    INT_MIN = -(1 << 31)
+    a = torch.empty(slots, dtype=torch.int32, device="cuda")
+    b = torch.empty(slots, dtype=torch.int32, device="cuda")
+    err = torch.zeros(2, dtype=torch.int32, device="cuda")
+    L.check(lib.tqpk_directory_build(d["k"].data_ptr(), L.I32, n, C.byref(pred.struct), d["p"].data_ptr(), L.I32, 3,
+                                     slots, INT_MIN, INT_MIN + 1, a.data_ptr(), err.data_ptr(), s), "build")
+    L.check(lib.tqpk_directory_compose(a.data_ptr(), slots, d["x"].data_ptr(), 0, nxt_slots, INT_MIN, INT_MIN + 1, s),
+            "compose")
+    L.check(lib.tqpk_directory_build_next(d["k"].data_ptr(), L.I32, n, C.byref(pred.struct), d["p"].data_ptr(), L.I32,
+                                          3, slots, INT_MIN, INT_MIN + 1, d["x"].data_ptr(), 0, nxt_slots,
+                                          b.data_ptr(), err.data_ptr() + 4, s), "build_next")
+    e = err.cpu().numpy()
+    assert (e[0] == L.EUNSUPPORTED) == (repeat and n > 1)
+    assert e[1] == e[0]
+    if not (repeat and n > 1):
+        np.testing.assert_array_equal(b.cpu().numpy(), a.cpu().numpy())
+
+
 @pytest.mark.parametrize("ties", [1500, 3000, 5000])
 @pytest.mark.parametrize("desc", [True, False])
 def test_topk_tied_candidates_around_the_sort_capacity(ties, desc):

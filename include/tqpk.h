@@ -391,7 +391,8 @@ int tqpk_jit_launch(void* handle, int32_t grid, int32_t block, size_t smem, void
 /* Preferred shared-memory share of the SM's unified L1/shared storage for a
  * compiled kernel (percent of the maximum, 0-100; a hint the driver rounds
  * to a supported split): a probe that keeps a small lookup structure in L1
- * asks for no more shared memory than its CTAs use.                         */
+ * asks for no more shared memory than its CTAs use.  A launch setting with
+ * no counterpart in the reference (its joins run as ATen calls).            */
 int tqpk_jit_prefer_shared(void* handle, int32_t percent);
 int32_t tqpk_num_sms(void);
 /* A group-by plan from key domains known ahead (table statistics [key_min, key_max]
@@ -447,7 +448,9 @@ int tqpk_directory_compose(int32_t* d_dir, int64_t slots, const int32_t* d_next,
  * the next table's domain) is kept only when d_next[payload - next_min] >= 0,
  * else the entry becomes fail_value; the same directory as build followed by
  * tqpk_directory_compose, without the second pass over it.  d_next is built
- * first (the snowflake chain's last table first).                          */
+ * first (the snowflake chain's last table first).  Replaces, for a chain of
+ * inner joins on primary keys, the build side of two successive join_vortex
+ * calls (operators/hashjoin.py:179-248, main.py:198-244).                  */
 int tqpk_directory_build_next(const void* d_keys, int32_t key_dtype, int64_t n, const tqpk_predicate* h_pred,
                               const void* d_payload, int32_t payload_dtype, int64_t key_min, int64_t slots,
                               int32_t empty, int32_t fail_value, const int32_t* d_next, int64_t next_min,

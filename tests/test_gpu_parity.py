@@ -771,3 +771,43 @@ def test_join_key_range_feeds_the_groupby_plan(spread):
     np.testing.assert_array_equal(tg[11].tensor.cpu().numpy().reshape(-1), agg[11].reshape(-1))
     np.testing.assert_array_equal(tg[304].tensor.cpu().numpy().reshape(-1), agg[304].reshape(-1))
     assert_f64_close(tg[302].tensor.cpu().numpy().reshape(-1), agg[302].reshape(-1))
+
+
+@pytest.mark.parametrize("keys,orders,limit", [([5, 6], [False, False], None), ([5], [False], 3),
+                                               ([6, 5], [False, False], None), ([5, 6], [True, False], None),
+                                               ([5, 6], [False, False], 4)])
+def test_sort_after_groupby_on_its_keys(keys, orders, limit):
+    """A sort on an ascending prefix of the group keys returns the group-by's own order (the
+    sort is elided); other key lists and orders sort; all match the oracle."""
+    import copy
+    from tqpk import datagen
+    from tqpk.operators import tqp_hash_aggregate, tqp_sort
+    from tqpk.variable import Variable
+    t = datagen.lineitem(200_003, seed=12)
+    ids = {"quantity": 1, "price": 2, "discount": 3, "tax": 4, "flag": 5, "status": 6, "ship_date": 7}
+    cols = {ids[k]: v for k, v in t.items()}
+    types = {1: "float", 2: "float", 3: "float", 4: "float", 5: "int", 6: "int", 7: "date"}
+    tg = {c: Variable(torch.from_numpy(a).cuda(), types[c]) for c, a in cols.items()}
+    aargs = {"is partial": False, "keys": ["flag#5", "status#6"], "input ids": [1, 2, 5, 6],
+             "results": ["flag#5", "status#6", [[["sum", ["quantity#1"]], "#", "101"], "AS", "a#201"],
+                         [[["count", ["1"]], "#", "108L"], "AS", "h#208"]],
+             "out agg ids": [201, 208]}
+    sargs = {"input ids": [5, 6, 201, 208], "key ids": keys, "key orders": orders}
+    if limit is not None:
+        sargs["limit"] = limit
+    tqp_hash_aggregate(True, tg, copy.deepcopy(aargs), None, None, "a")
+    elided = orders == [False] * len(orders) and keys == [5, 6][:len(keys)]
+    assert all(getattr(tg[c], "_row_order", None) is tg[5]._row_order for c in sargs["input ids"])
+    tqp_sort(True, tg, copy.deepcopy(sargs), limit is not None, "s")
+    agg = O.tqp_hash_aggregate(dict(cols), copy.deepcopy(aargs))
+    ref = O.tqp_sort({c: agg[c] for c in sargs["input ids"]}, sargs, limit is not None)
+    for c in sargs["input ids"]:
+        got = tg[c].tensor.cpu().numpy()
+        assert got.shape == np.asarray(ref[c]).shape, (c, got.shape, np.asarray(ref[c]).shape)
+        if got.dtype == np.float64:
+            assert_f64_close(got.reshape(-1), np.asarray(ref[c]).reshape(-1))
+        else:
+            np.testing.assert_array_equal(got, ref[c])
+    # an elided sort without a limit leaves the group-by's columns in place (still tagged);
+    # a sort that ran, or a limit, makes new columns
+    assert (getattr(tg[201], "_row_order", None) is not None) == (elided and limit is None)

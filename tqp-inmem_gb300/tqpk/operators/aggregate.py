@@ -93,6 +93,19 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
         tensor_group[a] = make_like(proto, v, torch_to_type(v.dtype))
     for i, oid in enumerate(key_out_ids):
         tensor_group[oid] = make_like(proto, keys_out[i], key_types_name[i])
+    if prog is not None and not prog.encoded:
+        # the groups come out in ascending key-tuple order (mixed-radix slots, or the packed key
+        # for sparse spaces): tqp_sort on a prefix of these keys, ascending, keeps this order
+        by = []
+        for kid in prog.key_ids:
+            oid = next((o for (o, k) in prog.key_outputs if k == kid), None)
+            if oid is None:
+                break
+            by.append(oid)
+        if by:
+            order = (object(), tuple(by))
+            for oid in list(agg_ids) + list(key_out_ids):
+                tensor_group[oid]._row_order = order
     return list(tensor_group.values())[0].tensor.size(0)
 
 

@@ -9,6 +9,9 @@ same rows as the full sort followed by the slice.  A [N, w] key (the
 reference ranks its rows with unique(dim=0)) is sorted as ceil(w/8) stable
 passes over 8-byte words of the rows, last word first, which gives the same
 lexicographic order and ties; [N, w] columns are gathered row by row.
+When every input column comes from one tqp_hash_aggregate call, whose groups are
+in ascending key-tuple order, and the sort keys are a prefix of those group keys,
+all ascending, the stable sort is the identity: only the limit is applied.
 """
 from __future__ import annotations
 
@@ -29,6 +32,16 @@ def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
     if k0.numel() * k0.element_size() >= 8_000_000_000:   # sort.py:22-23, 38-39
         raise RuntimeError("sort input exceeds in-memory limit")
     device = k0.device
+    order = getattr(tensor_group[input_ids[0]], "_row_order", None)
+    if (order is not None and not any(key_descs) and tuple(key_ids) == order[1][:len(key_ids)]
+            and all(getattr(tensor_group[c], "_row_order", None) is order for c in input_ids)):
+        # every input column holds one group-by's output, whose rows are already in ascending
+        # order of these keys: the stable sort is the identity, only the limit is left
+        if limit is not None:
+            for c in input_ids:
+                v = tensor_group[c]
+                tensor_group[c] = make_like(v, v.tensor[:limit], v.tensor_type)
+        return rows
     wait_ready(*[tensor_group[k] for k in key_ids])
     perm = None                                           # identity until the first pass
     steps = []

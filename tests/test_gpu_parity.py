@@ -811,3 +811,44 @@ def test_sort_after_groupby_on_its_keys(keys, orders, limit):
     # an elided sort without a limit leaves the group-by's columns in place (still tagged);
     # a sort that ran, or a limit, makes new columns
     assert (getattr(tg[201], "_row_order", None) is not None) == (elided and limit is None)
+
+
+@pytest.mark.parametrize("nb,np_", [(20_000, 400_003), (3_000, 2_000_001)])
+def test_staged_join_aggregate_topk_counts_groups_before_the_values(nb, np_):
+    """Columns copied from pinned host memory on a side stream, value columns last: the join
+    gathers them late, the aggregate counts its groups from the keys while they are still in
+    flight, and the result equals the oracle's."""
+    import copy
+    from tqpk import datagen
+    from tqpk.ingress import ColumnStager
+    from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
+    t = datagen.join_tables(nb, np_, seed=nb)
+    cols = {11: t["b_key"], 12: t["b_date"], 21: t["p_fk"], 22: t["p_date"], 23: t["p_price"], 24: t["p_discount"]}
+    types = {11: "int", 12: "date", 21: "int", 22: "date", 23: "float", 24: "float"}
+    host = {c: torch.from_numpy(a).pin_memory() for c, a in cols.items()}
+    f1 = {"filter tree": [["bd#12", "<", "1170"]], "materialized in": [12], "out mask id": 901}
+    f2 = {"filter tree": [["pd#22", ">", "1170"]], "materialized in": [22], "out mask id": 902}
+    jargs = {"left group": [11, 12], "right group": [21, 22, 23, 24], "materialized in": [11, 21, 23, 24],
+             "mask map": {11: 901, 21: 902, 23: 902, 24: 902}}
+    aargs = {"is partial": False, "keys": ["k#11"], "input ids": [11, 23, 24],
+             "results": ["k#11", [[["sum", [["p#23", "*", ["1.0", "-", "d#24"]]]], "#", "301"], "AS", "rev#302"]],
+             "out agg ids": [302]}
+    targs = {"limit": 10, "input ids": [11, 302], "key ids": [302], "key orders": [True]}
+    stager = ColumnStager()
+    for _ in range(2):
+        tg = stager.stage(host, types, (12, 22, 11, 21, 23, 24))
+        tqp_filter(True, tg, copy.deepcopy(f1), None, None, None, "f1")
+        tqp_filter(True, tg, copy.deepcopy(f2), None, None, None, "f2")
+        join_vortex(True, tg, copy.deepcopy(jargs), 11, 21, [], "inner", None, None, "j")
+        tqp_hash_aggregate(True, tg, copy.deepcopy(aargs), None, None, "a")
+        tqp_sort(True, tg, copy.deepcopy(targs), True, "t")
+        got_k = tg[11].tensor.cpu().numpy().reshape(-1)
+        got_v = tg[302].tensor.cpu().numpy().reshape(-1)
+        oc = dict(cols)
+        oc[901] = O.eval_filter(f1["filter tree"], {12: cols[12]})
+        oc[902] = O.eval_filter(f2["filter tree"], {22: cols[22]})
+        res, _ = O.join_vortex(oc, copy.deepcopy(jargs), 11, 21, "inner")
+        agg = O.tqp_hash_aggregate(res, copy.deepcopy(aargs))
+        top = O.tqp_sort({11: agg[11], 302: agg[302]}, targs, True)
+        np.testing.assert_array_equal(got_k, top[11].reshape(-1))
+        assert_f64_close(got_v, top[302].reshape(-1))

@@ -59,6 +59,12 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
 
     def values_ready():
         wait_ready(*[tensor_group[c] for c in transfer_set if c not in key_set and c not in mask_ids])
+
+    def _pending(v):
+        ev = getattr(v, "ready", None)
+        return ev is not None and not ev.query()
+    # value columns still in flight (a host copy or a late gather): count the groups from the keys
+    values_late = any(_pending(tensor_group[c]) for c in transfer_set if c not in key_set and c not in mask_ids)
     proto = tensor_group[data_ids[0]] if data_ids else None
     n = next(iter(cols.values())).shape[0] if cols else 0
     device = next(iter(cols.values())).device if cols else torch.device("cuda")
@@ -82,7 +88,8 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
         prog = compile_aggregate(args, cols, derived=True)
         ranges = [getattr(tensor_group[kid], "_key_range", None) for kid in prog.key_ids]
         keys, vals_out, G, _ = groupby(prog, n, device, mask=mask, before_values=values_ready,
-                                       key_ranges=ranges if ranges and all(r is not None for r in ranges) else None)
+                                       key_ranges=ranges if ranges and all(r is not None for r in ranges) else None,
+                                       values_late=values_late)
         keys_out = {}
         for i, (oid, kid) in enumerate(prog.key_outputs):
             keys_out[i] = keys[prog.key_ids.index(kid)].reshape(G, 1)

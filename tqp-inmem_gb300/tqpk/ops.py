@@ -114,14 +114,36 @@ def compact(cols: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = None,
 
 
 # ---------------------------------------------------------------- (d) group-by
+def _count_groups_from_keys(prog: AggregateProgram, plan, pred, n: int, device, s: int) -> int:
+    """Occupied slots of the group table, from the key columns (and the mask) alone: a
+    count-only pass of the generated kernel into a table of its own, then one host read.
+    Lets the group count come back while the value columns are still being copied."""
+    from . import jit
+    lib = L.load()
+    cs = L.GroupbySpec.from_buffer_copy(prog.spec)
+    cs.n_cols, cs.n_expr, cs.n_accs = 0, 0, 1            # accumulator 0 counts the rows of a group
+    cplan = L.GbPlan.from_buffer_copy(plan)
+    ws = _ws(cplan.ws_bytes, device)
+    L.check(lib.tqpk_groupby_prepare(C.byref(cs), C.byref(cplan), ws.data_ptr(), ws.numel(), s),
+            "tqpk_groupby_prepare")
+    jit.run_groupby(cs, pred, cplan, ws, n, s, pred.tensors if pred is not None else (),
+                    [t for t in prog.tensors[:prog.spec.n_keys]], ())
+    g = C.c_int64(0)
+    L.check(lib.tqpk_groupby_count(C.byref(cs), C.byref(cplan), ws.data_ptr(), C.byref(g), s), "tqpk_groupby_count")
+    return int(g.value)
+
+
 def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor] = None,
-            pred: Optional[CompiledPredicate] = None, before_values=None, key_ranges=None):
+            pred: Optional[CompiledPredicate] = None, before_values=None, key_ranges=None,
+            values_late: bool = False):
     """Runs the compiled aggregate; returns (key columns [G], {out id: column}, G).
     before_values, when given, is called after the plan (which reads only the keys and
     the mask) and before the first kernel that reads the value columns.  key_ranges, when
     given, bounds each key column ((min, max) per key, in spec order): the plan is made from
     them without reading the keys (no host synchronisation), unless they call for the hash
-    table of sparse key spaces."""
+    table of sparse key spaces.  values_late: the value columns are still arriving; the group
+    count is then taken from the keys first, and the accumulation and emission are queued
+    behind the values without another host synchronisation."""
     lib = L.load()
     _check_cuda(mask, *prog.tensors)
     s = _stream(device)
@@ -143,15 +165,18 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
                 "tqpk_groupby_plan")
     ws = _ws(plan.ws_bytes, device)
     groups = C.c_int64(0)
-    if before_values is not None:
-        before_values()
-    fill_masks(prog.masks, device)
     from . import jit
     from .predicate import has_strings
     use_jit = (jit.available() and plan.mode != L.GB_HASH and plan.n_rows > 0 and n > 0
                and not has_strings(pred.struct if pred is not None else None))
     if use_jit and mask is not None and pred is None:
         pred = _mask_predicate(mask)              # the mask as a one-instruction predicate
+    g_early = None
+    if use_jit and values_late and not prog.masks:
+        g_early = _count_groups_from_keys(prog, plan, pred, n, device, s)
+    if before_values is not None:
+        before_values()
+    fill_masks(prog.masks, device)
     if use_jit and (mask is None or pred is not None):
         # query-specialised accumulation kernel between the library's prepare and count stages
         L.check(lib.tqpk_groupby_prepare(C.byref(prog.spec), C.byref(plan), ws.data_ptr(), ws.numel(), s),
@@ -172,7 +197,7 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
                                             _vp_array([k.data_ptr() for k in keys]), len(outs), _i32_array(ops),
                                             _vp_array([o.data_ptr() for o in outs]), gdev.data_ptr(), s),
                 "tqpk_groupby_emit_async")
-        G = int(gdev.item())
+        G = g_early if g_early is not None else int(gdev.item())
         if G < 0:
             L.check(G, "tqpk_groupby_emit_async")
         keys = [k[:G] for k in keys]

@@ -202,8 +202,11 @@ int tqpk_compact(const tqpk_predicate* h_pred, const uint8_t* d_mask, int64_t n,
                  int64_t* d_count, void* d_ws, size_t ws_bytes, tqpk_stream stream);
 
 /* Stream compaction for callers that cannot allocate device memory when
- * they call (no counterpart in the reference, which always allocates through
- * torch): same arguments and results as tqpk_compact, minus the workspace.
+ * they call: an engine that owns all device memory through its own arena, or
+ * a serving loop that allows no cudaMalloc after start-up (it can stall the
+ * device and can fail mid-request).  No counterpart in the reference, which
+ * always allocates through torch.  Same arguments and results as
+ * tqpk_compact, minus the workspace.
  * Its scratch is a 1 MiB array inside the library, resident on every device
  * that loads it.  Inputs longer than tqpk_compact_noalloc_max_rows() rows
  * return TQPK_ENOMEM.  All calls on a device share that array, so calls that

@@ -852,3 +852,28 @@ def test_staged_join_aggregate_topk_counts_groups_before_the_values(nb, np_):
         top = O.tqp_sort({11: agg[11], 302: agg[302]}, targs, True)
         np.testing.assert_array_equal(got_k, top[11].reshape(-1))
         assert_f64_close(got_v, top[302].reshape(-1))
+
+
+def test_sort_after_groupby_sorts_a_replaced_column():
+    """A group-by output column whose tensor was replaced afterwards is no longer known to be in
+    key order: the sort runs (and matches the oracle on the replaced data)."""
+    import copy
+    from tqpk import datagen
+    from tqpk.operators import tqp_hash_aggregate, tqp_sort
+    from tqpk.variable import Variable
+    t = datagen.lineitem(50_001, seed=13)
+    cols = {1: t["quantity"], 5: t["flag"], 6: t["status"]}
+    types = {1: "float", 5: "int", 6: "int"}
+    tg = {c: Variable(torch.from_numpy(a).cuda(), types[c]) for c, a in cols.items()}
+    aargs = {"is partial": False, "keys": ["flag#5", "status#6"], "input ids": [1, 5, 6],
+             "results": ["flag#5", "status#6", [[["sum", ["quantity#1"]], "#", "101"], "AS", "a#201"]],
+             "out agg ids": [201]}
+    tqp_hash_aggregate(True, tg, copy.deepcopy(aargs), None, None, "a")
+    flipped = torch.flip(tg[5].tensor, dims=[0]).contiguous()
+    tg[5].tensor = flipped                           # same Variable, other rows
+    sargs = {"input ids": [5, 6, 201], "key ids": [5, 6], "key orders": [False, False]}
+    host = {c: tg[c].tensor.cpu().numpy() for c in sargs["input ids"]}
+    tqp_sort(True, tg, copy.deepcopy(sargs), False, "s")
+    ref = O.tqp_sort(host, sargs, False)
+    for c in sargs["input ids"]:
+        np.testing.assert_array_equal(tg[c].tensor.cpu().numpy(), ref[c])

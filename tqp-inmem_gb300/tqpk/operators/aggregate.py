@@ -110,8 +110,10 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
                 break
             by.append(oid)
         if by:
-            order = (object(), tuple(by))
-            for oid in list(agg_ids) + list(key_out_ids):
+            out_ids = list(agg_ids) + list(key_out_ids)
+            # the tag holds each column's storage, so a column whose tensor was replaced no longer matches
+            order = (object(), tuple(by), {oid: tensor_group[oid].tensor.data_ptr() for oid in out_ids})
+            for oid in out_ids:
                 tensor_group[oid]._row_order = order
     return list(tensor_group.values())[0].tensor.size(0)
 

@@ -34,7 +34,8 @@ def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
     device = k0.device
     order = getattr(tensor_group[input_ids[0]], "_row_order", None)
     if (order is not None and not any(key_descs) and tuple(key_ids) == order[1][:len(key_ids)]
-            and all(getattr(tensor_group[c], "_row_order", None) is order for c in input_ids)):
+            and all(getattr(tensor_group[c], "_row_order", None) is order
+                    and order[2].get(c) == tensor_group[c].tensor.data_ptr() for c in input_ids)):
         # every input column holds one group-by's output, whose rows are already in ascending
         # order of these keys: the stable sort is the identity, only the limit is left
         if limit is not None:

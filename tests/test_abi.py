@@ -69,3 +69,18 @@ def test_invalid_arguments_rejected_without_gpu(lib):
     assert lib.tqpk_filter_mask(None, 10, 1 << 20, None, None) == _lib.EINVAL
     assert lib.tqpk_argsort_stable(1 << 20, 77, 0, None, 10, 1 << 20, 1 << 20, 1 << 30, None) == _lib.EDTYPE
     assert lib.tqpk_gather(1, None, None, None, -1, 0, None, None) == _lib.EINVAL
+
+
+def test_membership_and_directory_entry_points_check_arguments_without_gpu(lib):
+    from tqpk import _lib
+    # tqpk_directory_bits: negative slot count, missing buffers
+    assert lib.tqpk_directory_bits(None, -1, None, None) == _lib.EINVAL
+    assert lib.tqpk_directory_bits(None, 10, 1 << 20, None) == _lib.EINVAL
+    assert lib.tqpk_directory_bits(None, 0, None, None) == _lib.OK          # nothing to do
+    # tqpk_directory_build_next: the next directory is required
+    assert lib.tqpk_directory_build_next(1 << 20, _lib.I32, 10, None, 1 << 20, _lib.I32, 0, 16, -1, -2,
+                                         None, 0, 8, 1 << 20, 1 << 20, None) == _lib.EINVAL
+    # tqpk_jit_prefer_shared: a kernel handle and a percentage
+    assert lib.tqpk_jit_prefer_shared(None, 20) == _lib.EINVAL
+    assert lib.tqpk_jit_prefer_shared(1 << 20, 101) == _lib.EINVAL
+    assert lib.tqpk_jit_prefer_shared(1 << 20, -1) == _lib.EINVAL

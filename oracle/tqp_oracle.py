@@ -455,8 +455,10 @@ def eval_agg_expr(tree, cols: Dict[int, np.ndarray], ctx=None):
             if cast_type == "double":
                 return eval_agg_expr(literal, cols, ctx)
             raise ValueError(f"Unsupported cast type: {cast_type}")
-        if head == "substring":
-            raise NotImplementedError("substring is not on the oracle's path")
+        if head == "substring":                                    # :114-119: a slice of the string rows
+            sub, l, w = tree[1]
+            l, w = int(l) - 1, int(w)
+            return np.asarray(eval_agg_expr(sub, cols, ctx))[:, l:l + w]
         if head not in _AGG_CALLS:                                 # :122-123
             raise ValueError(f"Unsupported aggregation function: {head}")
         if ctx is None:

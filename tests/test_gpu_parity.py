@@ -877,3 +877,42 @@ def test_sort_after_groupby_sorts_a_replaced_column():
     ref = O.tqp_sort(host, sargs, False)
     for c in sargs["input ids"]:
         np.testing.assert_array_equal(tg[c].tensor.cpu().numpy(), ref[c])
+
+
+def test_project_substring_then_group_by_it():
+    """tqp_project of substring(phone, 1, 2) gives the int8 [N, 2] slice the reference's
+    evaluate returns (aggregate.py:114-119); a group-by over that string key (with a numeric
+    projection beside it) matches the oracle."""
+    import copy
+    from tqpk.operators import tqp_hash_aggregate, tqp_project
+    from tqpk.variable import Variable
+    rng = np.random.default_rng(22)
+    n = 100_003
+    code = rng.integers(10, 35, n)
+    phone = rng.integers(ord("0"), ord("9") + 1, (n, 15)).astype(np.int8)
+    phone[:, 0] = ord("0") + code // 10
+    phone[:, 1] = ord("0") + code % 10
+    phone[:, 2] = ord("-")
+    bal = rng.integers(-99999, 999999, n) / 100.0
+    cols = {317: phone, 318: bal}
+    tg = {317: Variable(torch.from_numpy(phone).cuda(), "string"), 318: Variable(torch.from_numpy(bal).cuda(), "float")}
+    pargs = {"rename map": {}, "materialized in": [317, 318],
+             "used expr": [[["substring", ["c_phone#317", "1", "2"]], "AS", "cntrycode#400"],
+                           [["c_acctbal#318", "*", "2.0"], "AS", "dbl#401"]],
+             "materialized out": [400, 401]}
+    tqp_project(True, tg, copy.deepcopy(pargs), None, None, "p")
+    ref = O.tqp_project(dict(cols), copy.deepcopy(pargs))
+    got = tg[400].tensor.cpu().numpy()
+    assert got.dtype == np.int8 and got.shape == (n, 2) and tg[400].tensor_type == "string"
+    np.testing.assert_array_equal(got, ref[400])
+    np.testing.assert_array_equal(tg[401].tensor.cpu().numpy(), ref[401])
+    aargs = {"is partial": False, "keys": ["cntrycode#400"], "input ids": [400, 401],
+             "results": ["cntrycode#400", [[["count", ["1"]], "#", "500L"], "AS", "n#501"],
+                         [[["sum", ["dbl#401"]], "#", "502"], "AS", "s#503"]],
+             "out agg ids": [501, 503]}
+    tqp_hash_aggregate(True, tg, copy.deepcopy(aargs), None, None, "a")
+    agg = O.tqp_hash_aggregate({400: ref[400], 401: ref[401]}, copy.deepcopy(aargs))
+    np.testing.assert_array_equal(tg[400].tensor.cpu().numpy(), agg[400])
+    np.testing.assert_array_equal(tg[501].tensor.cpu().numpy().reshape(-1), agg[501].reshape(-1))
+    assert_f64_close(tg[503].tensor.cpu().numpy().reshape(-1), agg[503].reshape(-1),
+                     magnitude=np.abs(ref[401]).sum())

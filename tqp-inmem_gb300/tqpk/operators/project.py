@@ -3,14 +3,33 @@
 Renames columns (``args['rename map']``) and evaluates the computed expressions of
 ``args['used expr']`` in one generated kernel over the ``materialized in`` columns; the
 results land at ``args['materialized out']`` with the dtype torch gives each expression
-(integer results pass through float64, as the reference stores them).
+(integer results pass through float64, as the reference stores them).  A
+``substring(col, l, w)`` result is the int8 [N, w] slice of the string rows, as the
+reference's evaluate returns it (aggregate.py:114-119).
 """
 from __future__ import annotations
 
+import torch
+
 from ..expr import compile_projection, is_trivial_projection
+from ..predicate import get_id
 from ..ops import project
 from ..variable import make_like, torch_to_type, wait_ready
 from .filter import _require_gpu
+
+
+def _substring_of(tree):
+    """(column id, start, width) of a `substring(col, l, w)` result (aggregate.py:114-119), else None."""
+    while isinstance(tree, list) and len(tree) == 1:
+        tree = tree[0]
+    if isinstance(tree, list) and len(tree) == 3 and tree[1] == "AS":
+        tree = tree[0]
+    while isinstance(tree, list) and len(tree) == 1:
+        tree = tree[0]
+    if isinstance(tree, list) and len(tree) == 2 and tree[0] == "substring":
+        sub, l, w = tree[1]
+        return get_id(sub), int(l) - 1, int(w)
+    return None
 
 
 def tqp_project(gpu_enable, tensor_group, args, cpu_mem_pool, gpu_mem_pool, name="project"):
@@ -22,9 +41,24 @@ def tqp_project(gpu_enable, tensor_group, args, cpu_mem_pool, gpu_mem_pool, name
         inputs = {k: tensor_group[k] for k in args["materialized in"]}
         first = next(iter(inputs.values()))
         rows = first.tensor.size(0)
-        prog = compile_projection(args["used expr"], {k: v.tensor for k, v in inputs.items()}, derived=True)
+        computed = [t for t in args["used expr"] if not is_trivial_projection(t)]
+        subs = [_substring_of(t) for t in computed]
+        numeric = [t for t, sub in zip(computed, subs) if sub is None]
         wait_ready(*inputs.values())
-        outs = project(prog, rows, first.tensor.device)
+        nums = iter([])
+        if numeric:
+            prog = compile_projection(numeric, {k: v.tensor for k, v in inputs.items()}, derived=True)
+            nums = iter(project(prog, rows, first.tensor.device))
+        outs = []
+        for sub in subs:
+            if sub is None:
+                outs.append(next(nums))
+                continue
+            cid, l, w = sub          # the byte columns [l, l + w) of each string row, stored densely
+            col = inputs[cid].tensor
+            if col.dim() != 2 or col.dtype not in (torch.int8, torch.uint8):
+                raise NotImplementedError(f"substring of a {tuple(col.shape)} {col.dtype} column")
+            outs.append(col[:, l:l + w].contiguous())
         for i, out_id in enumerate(args["materialized out"]):
             tensor_group[out_id] = make_like(first, outs[i], torch_to_type(outs[i].dtype))
     return -1

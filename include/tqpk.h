@@ -193,7 +193,9 @@ int tqpk_filter_mask(const tqpk_predicate* h_pred, int64_t n, uint8_t* d_mask,
                      unsigned long long* d_count, tqpk_stream stream);
 
 /* Stream compaction, stable: keeps rows where d_mask[i] != 0 (or, when
- * d_mask is NULL, where the predicate holds).  Writes *d_count (int64).
+ * d_mask is NULL, where the predicate holds).  Writes *d_count (int64): the
+ * number of rows kept, or a negative status (TQPK_ETIMEOUT) when a bounded
+ * device-side wait gave up, in which case the outputs are not valid.
  * Replaces vortex_pipeline.py:58 (tensor[mask]) for up to TQPK_MAX_COLS
  * columns in one pass.                                                    */
 size_t tqpk_compact_workspace_bytes(int64_t n);
@@ -217,6 +219,13 @@ int64_t tqpk_compact_noalloc_max_rows(void);
 int tqpk_compact_noalloc(const tqpk_predicate* h_pred, const uint8_t* d_mask, int64_t n, int32_t ncols,
                          const void* const* h_cols_in, const int32_t* h_dtypes, void* const* h_cols_out,
                          int64_t* d_count, tqpk_stream stream);
+
+/* Test hook, no counterpart in the reference: the poll limit of the
+ * compaction's look-back (<= its default) and a tile whose CTA publishes
+ * nothing (-1: none).  With a tile stalled, its successors' bounded waits run
+ * out and the next compactions report TQPK_ETIMEOUT in *d_count.  (2097152, -1)
+ * restores the defaults.  Process-wide and not thread-safe.              */
+int tqpk_debug_compact_wait(int32_t spin_limit, int64_t stall_tile);
 
 /* ---- (d) group-by aggregation ----------------------------------------- */
 /* Computes the key ranges of the rows passing the filter (d_mask or h_pred,

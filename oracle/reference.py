@@ -1,0 +1,190 @@
+"""TQP-Inmem's own operator modules, compiled once and loaded for timing and pinning.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/golden/make_golden.py (to generate the golden
+vectors), by bench.py (the reference arm and the reference's torch CUDA path beside the kernels)
+and by nothing in the product.
+
+build() compiles the reference's operator path -- ``operators/{filter,like,hashjoin,aggregate,
+sort,project}.py``, ``IO/vortex_pipeline.py``, ``IO/pinned_mem.py``, ``variable.py``,
+``constants.py``, ``conversion.py``, ``utility/{logger,tensor_utils}.py`` and four functions of
+``parsing.py`` -- from a TQP-Inmem source tree (``TQP_REFERENCE``) into sourceless bytecode under
+``oracle/_ref/`` (git-ignored).  The bytecode travels with a copy of this repository to a GPU
+machine, where the source tree is absent, and load() imports it there unchanged.
+
+Three adaptations make the modules import without pandas, pyspark and pyparsing, and none of them
+touches the operators' arithmetic:
+
+1. ``pandas``/``pyspark``/``pyparsing``/``expression`` are empty stand-in modules (only
+   ``pd.Timestamp`` is evaluated at import time, by ``conversion.py``).
+2. ``parsing`` is compiled from the reference's own ``get_id``/``get_name``/``get_literals``/
+   ``right_most`` function bodies alone (the rest of that file drives Spark).
+3. ``IO/vortex_pipeline.py`` is compiled with assertions off: its two asserts check that the
+   input columns are CUDA tensors and that a mask column was passed, and the reference's CPU
+   path (``gpu_enable=False``) puts CPU tensors through the same class.
+
+On the CPU, cpu_mode() additionally maps the hard-coded ``device='cuda'`` arguments of
+``operators/aggregate.py:100,101,171,320,326`` to the CPU and makes ``torch.cuda.synchronize``
+(``operators/sort.py:37``) a no-op, for the duration of a ``with`` block.
+"""
+from __future__ import annotations
+
+import ast
+import contextlib
+import importlib.util
+import json
+import marshal
+import os
+import sys
+import types
+from pathlib import Path
+
+OUT = Path(__file__).resolve().parent / "_ref"
+
+# (module path relative to the TQP-Inmem tree, optimisation level)
+MODULES = [
+    ("constants.py", 0), ("variable.py", 0), ("conversion.py", 0),
+    ("utility/__init__.py", 0), ("utility/logger.py", 0), ("utility/tensor_utils.py", 0),
+    ("IO/__init__.py", 0), ("IO/vortex_pipeline.py", 1), ("IO/pinned_mem.py", 0),
+    ("operators/like.py", 0), ("operators/filter.py", 0), ("operators/hashjoin.py", 0),
+    ("operators/aggregate.py", 0), ("operators/sort.py", 0), ("operators/project.py", 0),
+]
+PARSING_FUNCTIONS = {"get_id", "get_name", "get_literals", "right_most"}
+
+
+class ReferenceUnavailable(RuntimeError):
+    """The compiled reference modules are missing or were built for another Python."""
+
+
+def _pyc(code: types.CodeType) -> bytes:
+    # header: magic, flags 0, and zero source mtime/size (a sourceless import checks only the magic)
+    return bytes(importlib.util.MAGIC_NUMBER) + bytes(12) + marshal.dumps(code)
+
+
+def build(src=None) -> Path | None:
+    """Compiles the reference's operator path into oracle/_ref/ when its source tree is present
+    (``src``, else ``TQP_REFERENCE``); returns oracle/_ref/, or None when neither the source nor a
+    previous build exists."""
+    src = Path(src or os.environ.get("TQP_REFERENCE", "")) if (src or os.environ.get("TQP_REFERENCE")) else None
+    if src is None or not (src / "operators" / "aggregate.py").exists():
+        return OUT if (OUT / "manifest.json").exists() else None
+    OUT.mkdir(parents=True, exist_ok=True)
+    built = []
+    for rel, opt in MODULES:
+        path = src / rel
+        code = compile(path.read_text(), f"TQP-Inmem/{rel}", "exec", optimize=opt, dont_inherit=True)
+        dst = OUT / (rel[:-3] + ".pyc")
+        dst.parent.mkdir(parents=True, exist_ok=True)
+        dst.write_bytes(_pyc(code))
+        built.append(rel)
+    tree = ast.parse((src / "parsing.py").read_text())
+    body = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in PARSING_FUNCTIONS]
+    imp = ast.parse("import re").body
+    code = compile(ast.Module(body=imp + body, type_ignores=[]), "TQP-Inmem/parsing.py", "exec", dont_inherit=True)
+    (OUT / "parsing.pyc").write_bytes(_pyc(code))
+    built.append("parsing.py (get_id, get_name, get_literals, right_most)")
+    (OUT / "manifest.json").write_text(json.dumps({"magic": importlib.util.MAGIC_NUMBER.hex(),
+                                                   "python": sys.version.split()[0], "modules": built}, indent=1))
+    return OUT
+
+
+def _stub(name: str, **attrs) -> types.ModuleType:
+    m = sys.modules.get(name)
+    if m is None:
+        m = types.ModuleType(name)
+        sys.modules[name] = m
+    for k, v in attrs.items():
+        setattr(m, k, v)
+    return m
+
+
+_LOADED = None
+
+
+def available() -> tuple[bool, str]:
+    """(True, '') when load() can import the compiled reference, else (False, why)."""
+    man = OUT / "manifest.json"
+    if not man.exists():
+        return False, "oracle/_ref was not built (the TQP-Inmem source tree was absent when build() ran)"
+    magic = json.loads(man.read_text()).get("magic")
+    if magic != importlib.util.MAGIC_NUMBER.hex():
+        return False, f"oracle/_ref holds bytecode of another Python ({magic})"
+    return True, ""
+
+
+def load() -> types.SimpleNamespace:
+    """The reference's modules, imported from oracle/_ref/: filter, hashjoin, aggregate, sort,
+    project, variable, pinned_mem."""
+    global _LOADED
+    if _LOADED is not None:
+        return _LOADED
+    ok, why = available()
+    if not ok:
+        raise ReferenceUnavailable(why)
+
+    class _Timestamp:                         # conversion.py computes one epoch at import time
+        def __init__(self, *a, **k):
+            pass
+
+    _stub("pandas", Timestamp=_Timestamp, Timedelta=None, DataFrame=None)
+    _stub("pyspark")
+    _stub("pyspark.sql", SparkSession=None)
+    _stub("pyspark.sql.types", StructType=None, DateType=None, StructField=None, IntegerType=None, StringType=None,
+          DoubleType=None)
+    _stub("pyparsing")
+    _stub("expression", parse=None)
+    if str(OUT) not in sys.path:
+        sys.path.insert(0, str(OUT))
+    import importlib
+    mods = {}
+    for name in ("constants", "variable", "conversion", "parsing", "utility.logger", "IO.vortex_pipeline",
+                 "IO.pinned_mem", "operators.filter", "operators.hashjoin", "operators.aggregate", "operators.sort",
+                 "operators.project"):
+        mods[name] = importlib.import_module(name)
+    for name, m in mods.items():
+        f = getattr(m, "__file__", "") or ""
+        if not f.startswith(str(OUT)):
+            raise ReferenceUnavailable(f"module {name} resolved outside oracle/_ref ({f})")
+    lg = mods["utility.logger"]
+    lg.set_perf_logger(None, False)           # as main.py does before running queries
+    lg.set_message_logger(None, False)
+    _LOADED = types.SimpleNamespace(filter=mods["operators.filter"], hashjoin=mods["operators.hashjoin"],
+                                    aggregate=mods["operators.aggregate"], sort=mods["operators.sort"],
+                                    project=mods["operators.project"], variable=mods["variable"],
+                                    pinned_mem=mods["IO.pinned_mem"])
+    return _LOADED
+
+
+class CpuPool:
+    """Stands in for IO/pinned_mem.GPUMemory on the CPU path: plain allocations."""
+
+    def malloc_like(self, t):
+        import torch
+        return 0, torch.empty_like(t)
+
+    def free_all(self):
+        pass
+
+
+@contextlib.contextmanager
+def cpu_mode():
+    """Runs the reference's CPU path (gpu_enable=False): device='cuda' keyword arguments become
+    the CPU and torch.cuda.synchronize is a no-op, inside the block only."""
+    import torch
+    from torch.overrides import TorchFunctionMode
+
+    class _CudaToCpu(TorchFunctionMode):
+        def __torch_function__(self, func, types_, args=(), kwargs=None):
+            kwargs = dict(kwargs or {})
+            dev = kwargs.get("device")
+            if dev is not None and ((isinstance(dev, str) and dev.startswith("cuda"))
+                                    or (isinstance(dev, torch.device) and dev.type == "cuda")):
+                kwargs["device"] = "cpu"
+            return func(*args, **kwargs)
+
+    sync = torch.cuda.synchronize
+    torch.cuda.synchronize = lambda *a, **k: None
+    try:
+        with _CudaToCpu():
+            yield
+    finally:
+        torch.cuda.synchronize = sync

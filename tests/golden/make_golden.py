@@ -1,122 +1,44 @@
 """Generate golden input/output vectors by running TQP-Inmem's own operators.
 
-This script is run by hand in a container where the TQP-Inmem source tree is
-mounted (default ``/root/reference``; override with ``TQP_REFERENCE``).  It
-imports the reference's operator modules unmodified and calls them through
-their public API on CPU torch:
+Run by hand after the reference's operator path has been compiled into oracle/_ref/ (the
+recipe ``python oracle/build_ref.py SOURCE_TREE``; __graft_entry__.build() runs it where the
+TQP-Inmem source tree is present).  The operators are called unmodified, through their public
+API, on their CPU path (``gpu_enable=False``, CPU torch):
 
 * ``operators/filter.py``    ``tqp_filter``
 * ``operators/hashjoin.py``  ``join_vortex`` / ``join_kernel_new``
 * ``operators/aggregate.py`` ``tqp_hash_aggregate``
 * ``operators/sort.py``      ``tqp_sort``
+* ``operators/project.py``   ``tqp_project``
 
-Three adaptations make them run on a machine without CUDA, pandas, pyspark
-and pyparsing, and none of them touches the operators' arithmetic:
+oracle/reference.py lists the adaptations that make them import without pandas, pyspark and
+pyparsing (none touches the operators' arithmetic); oracle.reference.cpu_mode() maps their
+hard-coded ``device='cuda'`` arguments to the CPU.
 
-1. ``pandas``/``pyspark``/``pyparsing`` are replaced by empty stand-in modules
-   (only ``pd.Timestamp`` is evaluated at import time, by ``conversion.py``).
-   ``parsing`` is replaced by a module built from the reference's own
-   ``get_id``/``get_name``/``get_literals``/``right_most`` function bodies,
-   extracted from ``parsing.py`` with ``ast`` (the rest of that file needs
-   Spark).
-2. ``IO/vortex_pipeline.py`` is compiled from its own source with the
-   ``assert ...is_cuda`` statements removed (the operators put CPU tensors
-   through it here).
-3. A ``TorchFunctionMode`` rewrites ``device='cuda'`` arguments to ``cpu`` and
-   ``torch.cuda.synchronize`` becomes a no-op.
-
-Each case is written to ``tests/golden/<case>.npz`` with its inputs, the
-operator arguments (JSON) and the outputs.  The fixtures are small (a few
-thousand to ~150k rows) so the tests that read them run in seconds.
+Each case is written to ``tests/golden/<case>.npz`` with its inputs, the operator arguments
+(JSON) and the outputs.  The fixtures are small (a few thousand to ~150k rows) so the tests that
+read them run in seconds.
 """
 from __future__ import annotations
 
-import ast
 import copy
 import json
-import os
 import sys
-import types
 from pathlib import Path
 
 import numpy as np
 import torch
-from torch.overrides import TorchFunctionMode
 
-REF = Path(os.environ.get("TQP_REFERENCE", "/root/reference"))
+ROOT = Path(__file__).resolve().parents[2]
 OUT = Path(__file__).resolve().parent
 
 
-# --------------------------------------------------------------------------
-# Loading the reference on CPU
-# --------------------------------------------------------------------------
-class _CudaToCpu(TorchFunctionMode):
-    """Rewrites device='cuda...' keyword arguments to the CPU."""
-
-    def __torch_function__(self, func, types_, args=(), kwargs=None):
-        kwargs = dict(kwargs or {})
-        dev = kwargs.get("device")
-        if dev is not None:
-            if (isinstance(dev, str) and dev.startswith("cuda")) or (
-                isinstance(dev, torch.device) and dev.type == "cuda"
-            ):
-                kwargs["device"] = "cpu"
-        return func(*args, **kwargs)
-
-
-def _stub(name: str, **attrs) -> types.ModuleType:
-    m = types.ModuleType(name)
-    for k, v in attrs.items():
-        setattr(m, k, v)
-    sys.modules[name] = m
-    return m
-
-
-def _module_from_functions(name: str, path: Path, fnames: set[str]) -> types.ModuleType:
-    tree = ast.parse(path.read_text())
-    body = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in fnames]
-    mod = types.ModuleType(name)
-    exec(compile(ast.Module(body=body, type_ignores=[]), str(path), "exec"), mod.__dict__)
-    mod.__dict__["re"] = __import__("re")
-    sys.modules[name] = mod
-    return mod
-
-
-class _StripCudaAsserts(ast.NodeTransformer):
-    def visit_Assert(self, node):
-        return None if "is_cuda" in ast.unparse(node) else node
-
-
 def load_reference():
-    class _Timestamp:  # conversion.py computes one epoch at import time
-        def __init__(self, *a, **k):
-            pass
-
-    _stub("pandas", Timestamp=_Timestamp, Timedelta=None, DataFrame=None)
-    _stub("pyspark")
-    _stub("pyspark.sql", SparkSession=None)
-    _stub("pyspark.sql.types", StructType=None, DateType=None, StructField=None,
-          IntegerType=None, StringType=None, DoubleType=None)
-    _stub("pyparsing")
-    _stub("expression", parse=None)
-    sys.path.insert(0, str(REF))
-    _module_from_functions("parsing", REF / "parsing.py",
-                           {"get_id", "get_name", "get_literals", "right_most"})
-    import IO  # noqa: F401  (package)
-    src = (REF / "IO" / "vortex_pipeline.py").read_text()
-    tree = _StripCudaAsserts().visit(ast.parse(src))
-    ast.fix_missing_locations(tree)
-    vp = types.ModuleType("IO.vortex_pipeline")
-    vp.__file__ = str(REF / "IO" / "vortex_pipeline.py")
-    sys.modules["IO.vortex_pipeline"] = vp
-    exec(compile(tree, vp.__file__, "exec"), vp.__dict__)
-    torch.cuda.synchronize = lambda *a, **k: None
-    from utility import logger
-    logger.set_perf_logger(None, False)      # as main.py does before running queries
-    logger.set_message_logger(None, False)
-    from operators import filter as f, hashjoin as hj, aggregate as ag, sort as so
-    import variable
-    return f, hj, ag, so, variable
+    if str(ROOT) not in sys.path:
+        sys.path.insert(0, str(ROOT))
+    from oracle import reference
+    R = reference.load()            # raises ReferenceUnavailable when oracle/_ref was not built
+    return R.filter, R.hashjoin, R.aggregate, R.sort, R.variable
 
 
 class _Pool:
@@ -691,7 +613,8 @@ def sort_multikey(ref):
 
 def main(argv):
     ref = load_reference()
-    with _CudaToCpu():
+    from oracle import reference
+    with reference.cpu_mode():
         for name, fn in CASES.items():
             if len(argv) > 1 and name not in argv[1:]:
                 continue

@@ -84,3 +84,22 @@ def test_membership_and_directory_entry_points_check_arguments_without_gpu(lib):
     assert lib.tqpk_jit_prefer_shared(None, 20) == _lib.EINVAL
     assert lib.tqpk_jit_prefer_shared(1 << 20, 101) == _lib.EINVAL
     assert lib.tqpk_jit_prefer_shared(1 << 20, -1) == _lib.EINVAL
+
+
+def test_compaction_workspace_and_noalloc_limit_agree(lib):
+    # the allocation-free compaction's row limit is the largest input whose workspace (control
+    # block + one status word per 4096-row tile) fits its 1 MiB array
+    cap = 1 << 20
+    rows = lib.tqpk_compact_noalloc_max_rows()
+    assert rows > 0 and rows % 4096 == 0
+    assert lib.tqpk_compact_workspace_bytes(rows) <= cap
+    assert lib.tqpk_compact_workspace_bytes(rows + 4096) > cap
+    assert lib.tqpk_compact_workspace_bytes(0) >= 256
+
+
+def test_compaction_wait_hook_checks_arguments(lib):
+    from tqpk import _lib
+    assert lib.tqpk_debug_compact_wait(-1, -1) == _lib.EINVAL
+    assert lib.tqpk_debug_compact_wait(1 << 22, -1) == _lib.EINVAL
+    assert lib.tqpk_debug_compact_wait(16, -2) == _lib.EINVAL
+    assert lib.tqpk_debug_compact_wait(1 << 21, -1) == _lib.OK          # the defaults

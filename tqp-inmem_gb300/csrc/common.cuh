@@ -575,7 +575,8 @@ __device__ __forceinline__ T block_excl_scan(T v, T& total, T* sw) {
 // Decoupled look-back (single-pass prefix over tiles in tile order).  Called
 // by all 32 lanes of one warp; returns the exclusive prefix of `tile` and
 // publishes its inclusive prefix.  status[] must start zeroed.
-__device__ __forceinline__ uint64_t lookback_warp(uint64_t* status, int64_t tile, uint64_t aggregate, int* err) {
+__device__ __forceinline__ uint64_t lookback_warp(uint64_t* status, int64_t tile, uint64_t aggregate, int* err,
+                                                  int spin_limit = kSpinLimit) {
   const int lane = threadIdx.x & 31;
   if (tile == 0) {
     if (lane == 0) st_release(&status[0], kFlagInc | aggregate);
@@ -592,7 +593,7 @@ __device__ __forceinline__ uint64_t lookback_warp(uint64_t* status, int64_t tile
     const uint32_t zero = __ballot_sync(0xffffffffu, (s >> 62) == 0);
     const uint32_t need = inc ? (((inc & (0u - inc)) << 1) - 1u) : 0xffffffffu;
     if (zero & need) {
-      if (++spins > kSpinLimit) {
+      if (++spins > spin_limit) {
         if (lane == 0) set_error(err, TQPK_ETIMEOUT);
         break;
       }

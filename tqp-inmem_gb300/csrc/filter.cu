@@ -71,15 +71,27 @@ __global__ void __launch_bounds__(kBlock) k_filter_mask(const __grid_constant__ 
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_compact(const __grid_constant__ tqpk_predicate P, RowFilter F, int64_t n,
-                                                    const __grid_constant__ ColSet C, int64_t* count,
-                                                    uint64_t* status, int* tile_ctr, int* err) {
-  __shared__ int s_tile;
-  __shared__ uint64_t s_excl;
-  __shared__ int sw[kBlock / 32 + 1];
-  if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1);
-  __syncthreads();
-  const int64_t tile = s_tile;
+// Control block of one compaction (zeroed before the launch).
+struct CompactCtl {
+  int tile_ctr;      // next tile to take
+  int err;           // first error status of any CTA
+  int finished;      // CTAs done
+  int pad;
+  int64_t kept;      // rows kept, written by the CTA of the last tile
+};
+constexpr size_t kCompactCtlBytes = 256;   // one WsCursor piece
+static_assert(sizeof(CompactCtl) <= kCompactCtlBytes, "control block");
+
+// Test hook (tqpk_debug_compact_wait): the poll limit of the look-back, and a tile whose CTA
+// publishes nothing, so that its successors' waits run out.  Defaults: kSpinLimit, none.
+static int g_dbg_spin_limit = kSpinLimit;
+static int64_t g_dbg_stall_tile = -1;
+
+// One 4096-row tile of k_compact: the tile's mask bits, its block scan, the look-back for its
+// output offset, then the kept rows of every column in row order.
+__device__ __forceinline__ void compact_tile(const tqpk_predicate& P, const RowFilter& F, int64_t n, const ColSet& C,
+                                             uint64_t* status, CompactCtl* ctl, int spin_limit, int64_t tile,
+                                             uint64_t& s_excl, int* sw) {
   const int64_t r0 = tile * kTile + threadIdx.x * kItems;
   uint32_t bits = 0;
 #pragma unroll
@@ -87,7 +99,7 @@ __global__ void __launch_bounds__(kBlock) k_compact(const __grid_constant__ tqpk
   int total;
   const int excl = block_excl_scan<kBlock, int>(__popc(bits), total, sw);
   if (threadIdx.x < 32) {
-    uint64_t e = lookback_warp(status, tile, (uint64_t)total, err);
+    uint64_t e = lookback_warp(status, tile, (uint64_t)total, &ctl->err, spin_limit);
     if (threadIdx.x == 0) s_excl = e;
   }
   __syncthreads();
@@ -121,7 +133,32 @@ __global__ void __launch_bounds__(kBlock) k_compact(const __grid_constant__ tqpk
       }
     }
   }
-  if (tile == (int64_t)gridDim.x - 1 && threadIdx.x == 0) *count = (int64_t)(s_excl + total);
+  if (tile == (int64_t)gridDim.x - 1 && threadIdx.x == 0) ctl->kept = (int64_t)(s_excl + total);
+}
+
+__global__ void __launch_bounds__(kBlock) k_compact(const __grid_constant__ tqpk_predicate P, RowFilter F, int64_t n,
+                                                    const __grid_constant__ ColSet C, int64_t* count,
+                                                    uint64_t* status, CompactCtl* ctl, int spin_limit,
+                                                    int64_t stall_tile) {
+  __shared__ int s_tile;
+  __shared__ uint64_t s_excl;
+  __shared__ int sw[kBlock / 32 + 1];
+  if (threadIdx.x == 0) s_tile = atomicAdd(&ctl->tile_ctr, 1);
+  __syncthreads();
+  const int64_t tile = s_tile;
+  if (tile != stall_tile) compact_tile(P, F, n, C, status, ctl, spin_limit, tile, s_excl, sw);
+  // The last CTA to finish writes the result: the kept-row count, or the error status (negative)
+  // when any look-back gave up.  Every CTA's error write precedes its fence and its increment.
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ctl->finished, 1) == (int)gridDim.x - 1) {
+      __threadfence();
+      const int e = *reinterpret_cast<volatile int*>(&ctl->err);
+      const int64_t kept = *reinterpret_cast<volatile int64_t*>(&ctl->kept);
+      *count = e ? (int64_t)e : kept;
+    }
+  }
 }
 
 // Min/max of up to four integer key columns over the rows passing a filter,
@@ -315,13 +352,15 @@ int key_ranges(const tqpk_predicate* pred, const uint8_t* mask, int64_t n, int n
 }
 
 // Stable compaction used inside the library (groups, join rows).
-size_t compact_status_bytes(int64_t n) { return align_up(((n + kTile - 1) / kTile) * 8 + 256, 256) + 256; }
+// Workspace of one compaction: the control block, then one status word per tile (both
+// 256-byte aligned pieces, as compact_launch takes them).
+size_t compact_status_bytes(int64_t n) { return kCompactCtlBytes + align_up(((n + kTile - 1) / kTile) * 8, 256); }
 
 int compact_launch(const tqpk_predicate* pred, const uint8_t* mask, int64_t n, const ColSet& C, int64_t* d_count,
                    void* ws, size_t ws_bytes, cudaStream_t s) {
   const int64_t tiles = (n + kTile - 1) / kTile;
   WsCursor cur(ws, ws_bytes);
-  int* ctl = cur.take<int>(64);  // [0] tile counter, [1] error word
+  CompactCtl* ctl = reinterpret_cast<CompactCtl*>(cur.take<unsigned char>(kCompactCtlBytes));
   uint64_t* status = cur.take<uint64_t>(tiles > 0 ? tiles : 1);
   if (!ctl || !status) return TQPK_ENOMEM;
   TQPK_CUDA(cudaMemsetAsync(ws, 0, cur.off, s));
@@ -331,7 +370,8 @@ int compact_launch(const tqpk_predicate* pred, const uint8_t* mask, int64_t n, c
   }
   if (tiles > INT32_MAX) return TQPK_EUNSUPPORTED;
   RowFilter F = make_filter(pred, mask);
-  k_compact<<<(int)tiles, kBlock, 0, s>>>(*pred_or_empty(pred), F, n, C, d_count, status, ctl, ctl + 1);
+  k_compact<<<(int)tiles, kBlock, 0, s>>>(*pred_or_empty(pred), F, n, C, d_count, status, ctl, g_dbg_spin_limit,
+                                          g_dbg_stall_tile);
   TQPK_CHECK_LAUNCH();
   return TQPK_OK;
 }
@@ -405,6 +445,16 @@ extern "C" int tqpk_filter_mask(const tqpk_predicate* h_pred, int64_t n, uint8_t
                                                           mask_vec);
   timing_after(KID_FILTER_MASK, s);
   TQPK_CHECK_LAUNCH();
+  return TQPK_OK;
+}
+
+// Test hook: the poll limit of the compaction's look-back, and a tile whose CTA publishes nothing
+// (its successors' bounded waits then run out and the call's count becomes TQPK_ETIMEOUT).
+// (kSpinLimit or less, -1) restores the defaults.  Not thread-safe; for tests only.
+extern "C" int tqpk_debug_compact_wait(int32_t spin_limit, int64_t stall_tile) {
+  if (spin_limit < 0 || spin_limit > kSpinLimit || stall_tile < -1) return TQPK_EINVAL;
+  g_dbg_spin_limit = spin_limit;
+  g_dbg_stall_tile = stall_tile;
   return TQPK_OK;
 }
 

@@ -36,6 +36,11 @@ struct JoinDir {
   const int64_t* ustart;    // SORTED: run starts (n_unique + 1 entries)
 };
 
+// A compaction leaves a negative status in its count when a look-back gave up.
+__global__ void k_count_status(const int64_t* count, int* err) {
+  if (*count < 0) set_error(err, (int)*count);
+}
+
 __global__ void k_join_init_dir(int64_t* dir, int* cnt, int64_t slots) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < slots; i += (int64_t)gridDim.x * blockDim.x) {
     dir[i] = -1;
@@ -376,6 +381,8 @@ extern "C" int tqpk_join_build(tqpk_join_plan* plan, const void* keys, int32_t d
     int64_t* d_m = L.nu + 1;
     int rc = compact_launch(nullptr, mask, nb, C, d_m, L.sort_ws, L.sort_bytes, s);  // no mask: all rows
     if (rc) return rc;
+    k_count_status<<<1, 1, 0, s>>>(d_m, L.hdr + 1);   // a failed compaction's status joins the error word
+    TQPK_CHECK_LAUNCH();
     const int64_t* sorted = nullptr;
     rc = sort_pairs(keys, dt, 0, L.csr, plan->nb_rows, L.sort_ws, L.sort_bytes, s, &sorted);
     if (rc) return rc;

@@ -12,9 +12,11 @@
 // device array below, so a call only needs the inputs and outputs.
 //
 // Limits and sharing:
-//  * the array is 1 MiB, which holds the status words of at most
-//    tqpk_compact_noalloc_max_rows() rows; larger inputs are rejected with
-//    TQPK_ENOMEM before anything is launched;
+//  * the array is 1 MiB: a 256-byte control block and the look-back status
+//    words of at most tqpk_compact_noalloc_max_rows() rows (536,739,840);
+//    larger inputs are rejected with TQPK_ENOMEM before anything is launched;
+//  * a look-back wait that runs out leaves the negative status TQPK_ETIMEOUT
+//    in *d_count instead of a row count, as tqpk_compact does;
 //  * every GPU that loads this library keeps the array resident until the
 //    process exits;
 //  * all calls on a device share the one array and it keeps whatever the
@@ -66,8 +68,11 @@ static int noalloc_scratch(void** out) {
 using namespace tqpk;
 
 extern "C" int64_t tqpk_compact_noalloc_max_rows(void) {
-  // 256 bytes of control words, then one 8-byte status word per tile
-  return (int64_t)((kNoAllocScratchBytes - 512) / 8) * kTile;
+  // The compaction's workspace (compact_status_bytes) is a 256-byte control block followed by one
+  // 8-byte look-back status word per 4096-row tile, rounded up to 256 bytes: the array holds
+  // (1 MiB - 256) / 8 = 131,040 tiles.
+  const int64_t rows = (int64_t)((kNoAllocScratchBytes - 256) / 8) * kTile;
+  return compact_status_bytes(rows) <= kNoAllocScratchBytes ? rows : 0;
 }
 
 extern "C" int tqpk_compact_noalloc(const tqpk_predicate* h_pred, const uint8_t* d_mask, int64_t n, int32_t ncols,

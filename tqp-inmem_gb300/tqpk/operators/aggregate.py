@@ -18,13 +18,14 @@ from __future__ import annotations
 import torch
 
 from ..expr import compile_aggregate, needs_key_codes
-from ..ops import encode_keys, gather, groupby
+from ..ops import check_deferred, encode_keys, gather, groupby
 from ..variable import make_like, torch_to_type, wait_ready
 from .filter import _require_gpu
 
 
 def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_pool, name="aggregation"):
     _require_gpu(gpu_enable)
+    check_deferred()
     assert not args["is partial"]
     transfer_set = args["input ids"]
     agg_mask_map = {}

@@ -6,7 +6,7 @@ reference does; the rows are compacted (or skipped) by the consumer.
 """
 from __future__ import annotations
 
-from ..ops import filter_mask
+from ..ops import check_deferred, filter_mask
 from ..predicate import compile_filter
 from ..variable import make_like, wait_ready
 
@@ -18,6 +18,7 @@ def _require_gpu(gpu_enable):
 
 def tqp_filter(gpu_enable, tensor_group, args, subquery_result, cpu_mem_pool, gpu_mem_pool, name):
     _require_gpu(gpu_enable)
+    check_deferred()
     assert "mask map" not in args, "Filter not accepting masks"
     input_columns = {k: tensor_group[k] for k in args["materialized in"]}
     if len(input_columns) == 0:

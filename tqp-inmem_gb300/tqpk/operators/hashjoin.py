@@ -25,7 +25,7 @@ from typing import Dict, List
 import torch
 
 from .. import _lib as L
-from ..ops import compact, filter_mask, gather, join_build, join_probe, mark_rows
+from ..ops import check_deferred, compact, filter_mask, gather, join_build, join_probe, mark_rows
 from ..predicate import compile_filter
 from ..variable import make_like, wait_ready
 from .filter import _require_gpu
@@ -202,6 +202,7 @@ def _outputs(tensors_left, tensors_right, keys, jtype, bi, pi, return_global_ind
 def join_vortex(gpu_enable, tensor_group, args, leftcol, rightcol, condition_list, type, cpu_mem_pool,
                 gpu_mem_pool, name):
     _require_gpu(gpu_enable)
+    check_deferred()
     join_key_index = [leftcol, rightcol]
     groupings = [args["left group"], args["right group"]]
     join_mask_map, join_output = {}, []

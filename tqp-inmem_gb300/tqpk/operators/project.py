@@ -13,7 +13,7 @@ import torch
 
 from ..expr import compile_projection, is_trivial_projection
 from ..predicate import get_id
-from ..ops import project
+from ..ops import check_deferred, project
 from ..variable import make_like, torch_to_type, wait_ready
 from .filter import _require_gpu
 
@@ -34,6 +34,7 @@ def _substring_of(tree):
 
 def tqp_project(gpu_enable, tensor_group, args, cpu_mem_pool, gpu_mem_pool, name="project"):
     _require_gpu(gpu_enable)
+    check_deferred()
     for orig, new in args["rename map"].items():
         tensor_group[new] = tensor_group[orig]
     if len(args["used expr"]) > 0:

@@ -17,13 +17,14 @@ from __future__ import annotations
 
 import torch
 
-from ..ops import argsort_stable, gather, gather_rows, string_words, topk_stable
+from ..ops import argsort_stable, check_deferred, gather, gather_rows, string_words, topk_stable
 from ..variable import make_like, wait_ready
 from .filter import _require_gpu
 
 
 def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
     _require_gpu(gpu_enable)
+    check_deferred()
     limit = args["limit"] if with_limit else None
     input_ids = args["input ids"]
     rows = tensor_group[input_ids[0]].tensor.shape[0]
@@ -35,7 +36,7 @@ def tqp_sort(gpu_enable, tensor_group, args, with_limit, name="sort"):
     order = getattr(tensor_group[input_ids[0]], "_row_order", None)
     if (order is not None and not any(key_descs) and tuple(key_ids) == order[1][:len(key_ids)]
             and all(getattr(tensor_group[c], "_row_order", None) is order
-                    and order[2].get(c) == tensor_group[c].tensor.data_ptr() for c in input_ids)):
+                    and order[2].get(c) == tensor_group[c].tensor.data_ptr() for c in {*input_ids, *key_ids})):
         # every input column holds one group-by's output, whose rows are already in ascending
         # order of these keys: the stable sort is the identity, only the limit is left
         if limit is not None:

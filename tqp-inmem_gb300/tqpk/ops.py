@@ -110,6 +110,8 @@ def compact(cols: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = None,
                              _vp_array(optr), cnt.data_ptr(), ws.data_ptr(), ws.numel(), _stream(device)),
             "tqpk_compact")
     m = int(cnt.item())
+    if m < 0:                                 # a bounded device wait gave up: the count is its status
+        L.check(m, "tqpk_compact")
     return [o[:m] for o in outs], m
 
 
@@ -197,7 +199,11 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
                                             _vp_array([k.data_ptr() for k in keys]), len(outs), _i32_array(ops),
                                             _vp_array([o.data_ptr() for o in outs]), gdev.data_ptr(), s),
                 "tqpk_groupby_emit_async")
-        G = g_early if g_early is not None else int(gdev.item())
+        if g_early is not None:
+            G = g_early                      # the emit's own count (or status) is checked once it lands
+            _defer_count_check(gdev, G, "tqpk_groupby_emit_async")
+        else:
+            G = int(gdev.item())
         if G < 0:
             L.check(G, "tqpk_groupby_emit_async")
         keys = [k[:G] for k in keys]
@@ -222,6 +228,43 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
             res[oid] = project(pp, G, device)[0]
             assert res[oid].dtype == dt
     return keys, res, G, plan
+
+
+# Counts written on the device by calls that did not wait for them (the group count of an emission
+# whose size was known beforehand): each is copied to pinned host memory behind its kernel and
+# compared with the size used, once its event has completed.  Every drop-in operator checks them
+# on entry, so a failure (a negative status, or a count that disagrees) raises at the latest in
+# the next operator call after the one that made it; check_deferred(wait=True) waits for them.
+_DEFERRED: list = []
+
+
+def _defer_count_check(d_count: torch.Tensor, expected: int, what: str) -> None:
+    h = torch.empty(1, dtype=torch.int64, pin_memory=True)
+    h.copy_(d_count, non_blocking=True)
+    ev = torch.cuda.Event()
+    ev.record()
+    _DEFERRED.append((h, ev, int(expected), what))
+
+
+def check_deferred(wait: bool = False) -> None:
+    """Raises for any deferred device count that came back as an error status or differs from
+    the size its call used; entries whose kernels have not finished stay queued (unless wait)."""
+    pending, failed = [], None
+    for h, ev, expected, what in _DEFERRED:
+        if wait:
+            ev.synchronize()
+        elif not ev.query():
+            pending.append((h, ev, expected, what))
+            continue
+        got = int(h[0])
+        if failed is None and got != expected:
+            failed = (got, expected, what)
+    _DEFERRED[:] = pending
+    if failed is not None:
+        got, expected, what = failed
+        if got < 0:
+            L.check(got, what)
+        raise RuntimeError(f"{what}: the device counted {got} rows where {expected} were sized")
 
 
 def _mask_predicate(mask: torch.Tensor) -> CompiledPredicate:

@@ -1,23 +1,26 @@
 #!/usr/bin/env python3
 """Benchmark of the TQP-Inmem relational hot path on GB300.
 
-Default workload (``--workload join_agg_top10``): the filtered equi-join +
-aggregate + top-10 query -- build side 1,500,000 rows (key = permutation of
-1..1.5M, date), filter date < 1170; probe side 6,001,215 rows (fk uniform
-over the build keys, date, price, discount), filter date > 1170;
-sum(price * (1 - discount)) grouped by build key; top 10 by the sum,
-descending.  Synthetic seeded data with the TPC-H-like distributions of
-tqpk.datagen (TPC-H itself is not available).
+The default run (``--workload all``) measures every workload and prints one JSON line: the
+headline is the filtered equi-join + aggregate + top-10 query -- build side 1,500,000 rows
+(key = permutation of 1..1.5M, date), filter date < 1170; probe side 6,001,215 rows (fk uniform
+over the build keys, date, price, discount), filter date > 1170; sum(price * (1 - discount))
+grouped by build key; top 10 by the sum, descending -- and ``workloads`` holds one record each
+for the filter + group-by query (6,001,215 rows), the star join (59,986,052 fact rows), the 64
+uneven instances of the batched form and the serving loop.  ``--workload NAME`` runs one.
 
-One step = one run of the whole query over inputs resident in HBM, through
-the fused pipeline (tqpk_pipeline_join_agg_topk: build, probe+aggregate,
-top-k).  ``e2e`` = the same query through the drop-in operators
-(tqp_filter x2, join_vortex, tqp_hash_aggregate, tqp_sort with limit) with
-the input columns copied from pinned host memory and the result copied back
-inside the timed region.  Metric: rows/s = probe (fact) rows / step time.
+Synthetic seeded data with the TPC-H-like distributions of tqpk.datagen (TPC-H itself is not
+available).  One step = one run of the whole query over inputs resident in HBM, through the fused
+pipeline (one CUDA-graph replay).  ``e2e`` = the same query through the drop-in operators
+(tqp_filter, join_vortex, tqp_hash_aggregate, tqp_sort) with the input columns copied from pinned
+host memory and the result copied back inside the timed region; ``dropin`` = the drop-in
+operators over resident columns.  Metric: rows/s = probe (fact) rows / step time.
 
-``--impl reference`` times the reference algorithm's CPU implementation (the
-numpy restatement in oracle/) on the host cores, one process per core.
+Beside them: ``reference_cuda`` = TQP-Inmem's own operators (compiled from its source into
+oracle/_ref, run unmodified through their public API, main.py's plan order, a synchronisation
+after every operator as main.py:273-274) on torch CUDA on the same GPU, resident and end to end;
+``cpu_baseline`` = the same operators on their CPU path (torch CPU, every host core), a bounded
+sample.  ``--impl reference`` is that CPU path alone, on the workload's full-size query.
 """
 from __future__ import annotations
 
@@ -92,7 +95,7 @@ class JoinAggTop10:
                      23: self.t["p_price"], 24: self.t["p_discount"]}
         self.types = {11: "int", 12: "date", 21: "int", 22: "date", 23: "float", 24: "float"}
 
-    # algorithmic bytes: every input column read once (SURVEY 8d convention)
+    # algorithmic bytes: every input column read once, the outputs written once
     def algorithmic_bytes(self):
         return self.NB * 8 + self.NP * 24
 
@@ -140,6 +143,68 @@ class JoinAggTop10:
         join_vortex(True, tg, plan_args(self.jargs), 11, 21, [], "inner", None, None, "j")
         tqp_hash_aggregate(True, tg, plan_args(self.aargs), None, None, "a")
         tqp_sort(True, tg, plan_args(self.targs), True, "t")
+        res = d2h_all({11: tg[11].tensor, 302: tg[302].tensor})
+        keys, vals = res[11], res[302]
+        h2d = sum(h.numel() * h.element_size() for h in self.host.values())
+        d2h = keys.numel() * keys.element_size() + vals.numel() * vals.element_size()
+        return (keys.numpy().reshape(-1), vals.numpy()), h2d, d2h
+
+    def ref_plan(self, R, tg, pool, ge, sync):
+        """main.py's plan over TQP-Inmem's own operators: Filter, Filter, Join, Aggregate,
+        take ordered (main.py:152-253), synchronising after each operator (main.py:273-274)."""
+        R.filter.tqp_filter(ge, tg, plan_args(self.f1), None, None, pool, "f1"); sync()
+        R.filter.tqp_filter(ge, tg, plan_args(self.f2), None, None, pool, "f2"); sync()
+        R.hashjoin.join_vortex(ge, tg, plan_args(self.jargs), 11, 21, [], "inner", None, pool, "j"); sync()
+        R.aggregate.tqp_hash_aggregate(ge, tg, plan_args(self.aargs), pool, None, "a"); sync()
+        groups = int(tg[11].tensor.shape[0])
+        R.sort.tqp_sort(ge, tg, plan_args(self.targs), True, "t"); sync()
+        return (tg[11].tensor.cpu().numpy().reshape(-1), tg[302].tensor.cpu().numpy()), groups
+
+    def step_dropin(self, tg):
+        """The drop-in operators over resident columns (no copies)."""
+        from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
+        tqp_filter(True, tg, plan_args(self.f1), None, None, None, "f1")
+        tqp_filter(True, tg, plan_args(self.f2), None, None, None, "f2")
+        join_vortex(True, tg, plan_args(self.jargs), 11, 21, [], "inner", None, None, "j")
+        tqp_hash_aggregate(True, tg, plan_args(self.aargs), None, None, "a")
+        tqp_sort(True, tg, plan_args(self.targs), True, "t")
+        return tg[302].tensor
+
+    def plan(self):
+        """The query as a plan executor holds it (main.py:123-130): the operators in order and
+        each one's argument dict, keyed by operator id."""
+        ops = [3, 4, 5, 6, 7]
+        args = {3: dict(plan_args(self.f1), name="Filter"), 4: dict(plan_args(self.f2), name="Filter"),
+                5: dict(plan_args(self.jargs), name="Join", **{"left keys": [11], "right keys": [21],
+                                                                "join type": "Inner"}),
+                6: dict(plan_args(self.aargs), name="Aggregate"), 7: dict(plan_args(self.targs), name="take ordered")}
+        return ops, args
+
+    def step_e2e_fused(self):
+        """A plan executor that offers each run of operators to try_fused before dispatching them one
+        by one (main.py:123-253 with the loop of tqpk.operators.fused); host buffers as step_e2e."""
+        from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort, try_fused
+        if not hasattr(self, "staged"):
+            from tqpk.ingress import ColumnStager
+            self.staged = ColumnStager(self.dev)
+        tg = self.staged.stage(self.host, self.types, (12, 22, 11, 21, 23, 24))
+        ops, args = self.plan()
+        i = 0
+        while i < len(ops):
+            m = try_fused(True, tg, ops, args, i)
+            if m:
+                i += m
+                continue
+            a = args[ops[i]]
+            if a["name"] == "Filter":
+                tqp_filter(True, tg, a, None, None, None, "f")
+            elif a["name"] == "Join":
+                join_vortex(True, tg, a, a["left keys"][0], a["right keys"][0], [], "inner", None, None, "j")
+            elif a["name"] == "Aggregate":
+                tqp_hash_aggregate(True, tg, a, None, None, "a")
+            else:
+                tqp_sort(True, tg, a, True, "t")
+            i += 1
         res = d2h_all({11: tg[11].tensor, 302: tg[302].tensor})
         keys, vals = res[11], res[302]
         h2d = sum(h.numel() * h.element_size() for h in self.host.values())
@@ -265,6 +330,21 @@ class FilterGroupBy:
         d2h = sum(v.nbytes for v in out.values())
         return out, h2d, d2h
 
+    def ref_plan(self, R, tg, pool, ge, sync):
+        """main.py's plan over TQP-Inmem's own operators: Filter, Aggregate, Sort."""
+        R.filter.tqp_filter(ge, tg, plan_args(self.fargs), None, None, pool, "f"); sync()
+        R.aggregate.tqp_hash_aggregate(ge, tg, plan_args(self.aargs), pool, None, "a"); sync()
+        R.sort.tqp_sort(ge, tg, plan_args(self.sargs), False, "s"); sync()
+        out = {c: tg[c].tensor.cpu().numpy() for c in self.sargs["input ids"]}
+        return out, int(out[5].shape[0])          # the oracle's form: column id -> array
+
+    def step_dropin(self, tg):
+        from tqpk.operators import tqp_filter, tqp_hash_aggregate, tqp_sort
+        tqp_filter(True, tg, plan_args(self.fargs), None, None, None, "f")
+        tqp_hash_aggregate(True, tg, plan_args(self.aargs), None, None, "a")
+        tqp_sort(True, tg, plan_args(self.sargs), False, "s")
+        return tg[201].tensor
+
     def oracle(self, cols=None):
         from oracle import tqp_oracle as O
         cols = dict(self.cols if cols is None else cols)
@@ -378,6 +458,52 @@ class StarJoin:
         out = [res[c].numpy().reshape(-1) for c in (61, 72, 74)]
         h2d = sum(h.numel() * h.element_size() for h in self.host.values())
         return tuple(out), h2d, sum(o.nbytes for o in out)
+
+    def cpu_sample(self):
+        """The bounded CPU sample: the same star at a tenth of the size."""
+        return StarJoin(scale=0.1)
+
+    def ref_plan(self, R, tg, pool, ge, sync):
+        """main.py's plan over TQP-Inmem's own operators: Filter(A), three Joins, Aggregate,
+        take ordered."""
+        groups = []
+
+        def f(tg, a):
+            R.filter.tqp_filter(ge, tg, a, None, None, pool, "f"); sync()
+
+        def j(tg, a, lk, rk):
+            R.hashjoin.join_vortex(ge, tg, a, lk, rk, [], "inner", None, pool, "j"); sync()
+            return tg
+
+        def ag(tg, a):
+            R.aggregate.tqp_hash_aggregate(ge, tg, a, pool, None, "a"); sync()
+            groups.append(int(tg[61].tensor.shape[0]))
+            return tg
+
+        def so(tg, a):
+            R.sort.tqp_sort(ge, tg, a, True, "t"); sync()
+            return tg
+        tg = self._plan(tg, (f, j, ag, so))
+        return tuple(tg[c].tensor.cpu().numpy().reshape(-1) for c in (61, 72, 74)), groups[0]
+
+    def step_dropin(self, tg):
+        from tqpk.operators import join_vortex, tqp_filter, tqp_hash_aggregate, tqp_sort
+
+        def f(tg, a):
+            tqp_filter(True, tg, a, None, None, None, "f")
+
+        def j(tg, a, lk, rk):
+            join_vortex(True, tg, a, lk, rk, [], "inner", None, None, "j")
+            return tg
+
+        def ag(tg, a):
+            tqp_hash_aggregate(True, tg, a, None, None, "a")
+            return tg
+
+        def so(tg, a):
+            tqp_sort(True, tg, a, True, "t")
+            return tg
+        return self._plan(tg, (f, j, ag, so))[72].tensor
 
     def oracle(self, cols=None):
         from oracle import tqp_oracle as O
@@ -568,7 +694,7 @@ def run_batched_bench(args):
                            (n / plain_s), batched_rows_per_s=w.fact_rows / (batched_ms / 1000.0),
                            kernel_ms=kms.value / max(kn.value, 1)),
             "clocks": clocks, "gpu_launches": launches}
-    print(json.dumps(line))
+    return line
 
 
 def run_serving_bench(args):
@@ -637,7 +763,7 @@ def run_serving_bench(args):
                     "d2h_bytes_per_step": d2h / max(len(cont), 1),
                     "path": "arrival on the host to result in pinned host memory; tables resident"},
             "clocks": clocks, "gpu_launches": launches}
-    print(json.dumps(line))
+    return line
 
 
 WORKLOADS = {c.name: c for c in (JoinAggTop10, FilterGroupBy, StarJoin)}
@@ -793,67 +919,178 @@ def compare(workload, got, exp):
                 assert np.array_equal(v, e), (oid, v, e)
 
 
-# ---------------------------------------------------------------------------- reference arm
-def _ref_worker_init(name):
-    global _REF_W
-    _REF_W = WORKLOADS[name]()
+# ---------------------------------------------------------------------------- the reference's operators
+def reference_modules():
+    """TQP-Inmem's own operator modules (oracle/_ref), or (None, why) when they are unavailable."""
+    try:
+        from oracle import reference
+        return reference.load(), ""
+    except Exception as e:                    # missing build, other Python, import failure
+        return None, f"{type(e).__name__}: {e}"
 
 
-def _ref_worker_step(_):
-    t0 = time.perf_counter()
-    _REF_W.oracle()
-    return time.perf_counter() - t0
+def _ref_tensor_group(R, cols, types, device=None):
+    import torch
+    V = R.variable.Variable
+    tg = {}
+    for c, a in cols.items():
+        t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
+        if device is not None:
+            t = t.to(device, non_blocking=True)
+        tg[c] = V(t, types[c])
+    return tg
+
+
+def reference_cpu(w, budget_s: float, max_runs: int = 3):
+    """TQP-Inmem's operators on their CPU path (gpu_enable=False, torch CPU on every host core)
+    over the workload's full-size tables, bounded: runs until max_runs or budget_s; returns
+    (cpu_baseline record, last result) or (None, why)."""
+    import torch
+    R, why = reference_modules()
+    if R is None:
+        return None, why
+    from oracle import reference
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    pool = reference.CpuPool()
+    ts, res = [], None
+    t_end = time.perf_counter() + budget_s
+    with reference.cpu_mode():
+        while len(ts) < max_runs and (not ts or time.perf_counter() + statistics.median(ts) < t_end):
+            tg = _ref_tensor_group(R, w.cols, w.types)
+            torch.manual_seed(0)
+            t0 = time.perf_counter()
+            res = w.ref_plan(R, tg, pool, False, lambda: None)
+            ts.append(time.perf_counter() - t0)
+    med = statistics.median(ts)
+    rec = {"value": w.fact_rows / med, "unit": "rows/s", "cores": torch.get_num_threads(), "kind": "reference",
+           "sample": f"{type(w).__name__} full-size query ({w.fact_rows} fact rows) x{len(ts)}, median {med:.3f} s: "
+                     f"TQP-Inmem's operators (oracle/_ref), gpu_enable=False, torch {torch.__version__} CPU"}
+    return rec, res
+
+
+def reference_cuda(w, dev, steps: int, warmup: int = 2):
+    """TQP-Inmem's operators on torch CUDA on this GPU, through main.py's plan with a
+    synchronisation after every operator and the reference's own device pool
+    (IO/pinned_mem.GPUMemory(40 GB, 40 MB blocks), main.py:56, freed per query, main.py:293-294).
+    Resident: the input columns already on the device; e2e: copied from pinned host memory inside
+    the timed region and the result read back.  Returns (record, result) or (None, why)."""
+    import torch
+    R, why = reference_modules()
+    if R is None:
+        return None, why
+    pool = R.pinned_mem.GPUMemory(capacity_gb=40, block_size_mb=40)
+    dcols = {c: torch.from_numpy(np.ascontiguousarray(a)).to(dev) for c, a in w.cols.items()}
+    hcols = {c: torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for c, a in w.cols.items()}
+    sync = torch.cuda.synchronize
+
+    def one(cols, copy_in):
+        tg = _ref_tensor_group(R, cols, w.types, device=dev if copy_in else None)
+        out = w.ref_plan(R, tg, pool, True, sync)
+        pool.free_all()
+        return out
+
+    res = None
+    for _ in range(warmup):
+        res = one(dcols, False)
+    sync()
+    ts = []
+    for _ in range(steps):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        one(dcols, False)
+        s1.record()
+        sync()
+        ts.append(s0.elapsed_time(s1))
+    e2e = []
+    for _ in range(max(2, steps // 2)):
+        sync()
+        t0 = time.perf_counter()
+        one(hcols, True)
+        sync()
+        e2e.append(time.perf_counter() - t0)
+    ms, e2e_s = statistics.median(ts), statistics.median(e2e)
+    h2d = sum(h.numel() * h.element_size() for h in hcols.values())
+    rec = {"value": w.fact_rows / (ms / 1e3), "unit": "rows/s", "ms_per_step": ms, "steps": steps,
+           "e2e": {"value": w.fact_rows / e2e_s, "unit": "rows/s", "ms_per_step": e2e_s * 1e3, "h2d_bytes_per_step": h2d},
+           "path": f"TQP-Inmem's operators (oracle/_ref) on torch {torch.__version__} CUDA, main.py's plan order"}
+    del dcols, hcols, pool
+    torch.cuda.empty_cache()
+    return rec, res
 
 
 def run_reference(args, rank, world):
+    """The reference arm: TQP-Inmem's own operators on their CPU path (torch CPU, every host
+    core), each step one full-size query of the workload.  Falls back to the numpy
+    restatement of the same algorithm (oracle/tqp_oracle.py) when the compiled reference is
+    unavailable, and says so."""
     if rank != 0:
         return
-    import multiprocessing as mp
-    w = make_workload(args)
+    import torch
+    name = args.workload if args.workload in WORKLOADS else JoinAggTop10.name
+    w = make_workload(argparse.Namespace(workload=name, scale=args.scale))
+    R, why = reference_modules()
     cores = os.cpu_count() or 1
-    procs = max(1, min(cores, args.steps))
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(procs, initializer=_ref_worker_init, initargs=(args.workload,)) as pool:
-        pool.map(_ref_worker_step, range(min(args.warmup, procs)))
-        t0 = time.perf_counter()
-        times = pool.map(_ref_worker_step, range(args.steps))
-        wall = time.perf_counter() - t0
+    if R is not None:
+        from oracle import reference
+        torch.set_num_threads(cores)
+        pool = reference.CpuPool()
+
+        def step():
+            tg = _ref_tensor_group(R, w.cols, w.types)
+            torch.manual_seed(0)
+            w.ref_plan(R, tg, pool, False, lambda: None)
+        kind, how = "reference", (f"TQP-Inmem's operators (oracle/_ref), gpu_enable=False, torch {torch.__version__} "
+                                  f"CPU, {torch.get_num_threads()} threads")
+        ctx = reference.cpu_mode()
+    else:
+        def step():
+            w.oracle()
+        kind, how = "port", f"numpy restatement (oracle/tqp_oracle.py), 1 thread; the compiled reference: {why}"
+        import contextlib
+        ctx = contextlib.nullcontext()
+    with ctx:
+        for _ in range(args.warmup):
+            step()
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            step()
+            times.append(time.perf_counter() - t0)
+    wall = sum(times)
     value = args.steps * w.fact_rows / wall
+    threads = torch.get_num_threads() if R is not None else 1
     line = {
         "impl": "reference", "metric": "rows/s", "value": value, "unit": "rows/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(w.config, parallelism=f"{procs} host processes"),
-        "cpu_baseline": {"value": value, "unit": "rows/s", "cores": procs, "kind": "port",
-                         "sample": f"{args.steps} full-size queries on {procs} processes "
-                                   f"(median single-query {statistics.median(times):.3f} s)"},
+        "config": dict(w.config, parallelism=f"host CPU, {threads} threads"),
+        "cpu_baseline": {"value": value, "unit": "rows/s", "cores": threads, "kind": kind,
+                         "sample": f"{args.steps} full-size queries, one after another (median "
+                                   f"{statistics.median(times):.3f} s): {how}"},
         "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
 
 # ---------------------------------------------------------------------------- our arm
-def run_ours(args, rank, world):
+def measure_ours(args, w, rank, world, dev, cpu_budget_s=20.0, with_reference=True):
+    """One workload on this GPU: correctness gate, the fused step (CUDA-graph replay) timed with
+    CUDA events, the dominant kernel's own launches, the drop-in operators resident and end to end,
+    the reference's operators on torch CUDA and on the CPU.  Returns the JSON record."""
     import torch
     from tqpk import _lib as L
-    import __graft_entry__ as G
-
-    G.build()
     lib = L.load()
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    w = make_workload(args)
     w.setup_device(dev)
 
-    # correctness gate (outside the timed region)
+    # correctness gate (outside the timed region): the fused step against the oracle
     exp = w.oracle()
     w.step_device()
     torch.cuda.synchronize()
     compare(w, w.device_result(), exp)
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    sampler = ClockSampler(local)
+    sampler = ClockSampler(dev.index or 0)
     sampler.start()
     # keep the GPU loaded ~1 s so clocks settle and are sampled around the timed steps
     t_end = time.perf_counter() + 1.0
@@ -877,11 +1114,11 @@ def run_ours(args, rank, world):
         L.check(lib.tqpk_timing_begin(kid), "tqpk_timing_begin")
     launches0 = lib.tqpk_launch_count()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    for s, e in evs:
+    for s0, e0 in evs:
         flush.zero_()
-        s.record()
+        s0.record()
         w.step_graph() if graph else w.step_device()
-        e.record()
+        e0.record()
     torch.cuda.synchronize()
     launches = launches_per_step * args.steps if graph else lib.tqpk_launch_count() - launches0
     barrier(world)
@@ -895,37 +1132,77 @@ def run_ours(args, rank, world):
             w.step_device()
         torch.cuda.synchronize()
     L.check(lib.tqpk_timing_end(C.byref(kms), C.byref(kn)), "tqpk_timing_end")
-    step_ms = [s.elapsed_time(e) for s, e in evs]
+    step_ms = [s0.elapsed_time(e0) for s0, e0 in evs]
     total_ms = max_over_ranks(sum(step_ms), world)
     clocks = sampler.stop()
 
-    # end to end through the drop-in operators with host buffers
-    for _ in range(2):
-        w.step_e2e()
-    torch.cuda.synchronize()
-    e2e_times, h2d, d2h = [], 0, 0
-    e2e_steps = max(3, min(args.steps, 10))
-    for _ in range(e2e_steps):
+    # the drop-in operators over resident columns (the reference-facing path, no copies)
+    from tqpk.variable import Variable
+    dropin = []
+    for i in range(2 + max(3, min(args.steps, 10))):
+        tg = {c: Variable(w.d[c], w.types[c]) for c in w.cols}
+        flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        res, h2d, d2h = w.step_e2e()
+        w.step_dropin(tg)
         torch.cuda.synchronize()
-        e2e_times.append(time.perf_counter() - t0)
-    compare(w, res if not isinstance(w, FilterGroupBy) else
-            ([res[5].reshape(-1), res[6].reshape(-1)], {o: res[o] for o in w.aargs["out agg ids"]}), exp)
-    e2e_s = max_over_ranks(statistics.median(e2e_times), world)
+        if i >= 2:
+            dropin.append(time.perf_counter() - t0)
+    dropin_s = statistics.median(dropin)
 
-    # CPU baseline: the oracle on the host cores (rank 0, N=1 only), bounded sample
+    # end to end with host buffers: the drop-in operators one by one, and (where the workload has
+    # one) the executor that hands the whole run to try_fused
+    def timed_e2e(step):
+        for _ in range(2):
+            step()
+        torch.cuda.synchronize()
+        ts, out = [], None
+        for _ in range(max(3, min(args.steps, 10))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = step()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return max_over_ranks(statistics.median(ts), world), out
+
+    ops_s, (res, h2d, d2h) = timed_e2e(w.step_e2e)
+    got_e2e = res if not isinstance(w, FilterGroupBy) else \
+        ([res[5].reshape(-1), res[6].reshape(-1)], {o: res[o] for o in w.aargs["out agg ids"]})
+    compare(w, got_e2e, exp)
+    e2e_s, e2e_path = ops_s, "drop-in operators, pinned host inputs"
+    if hasattr(w, "step_e2e_fused"):
+        e2e_s, (res_f, h2d, d2h) = timed_e2e(w.step_e2e_fused)
+        compare(w, res_f, exp)
+        e2e_path = "plan executor with try_fused (one fused pipeline for the filter-join-aggregate-top-k run), pinned host inputs"
+
+    # TQP-Inmem's own operators on torch CUDA on this GPU, and their result against ours
+    ref_cuda = None
+    if with_reference and rank == 0:
+        rec, out = reference_cuda(w, dev, steps=max(3, min(args.steps, 10)))
+        if rec is None:
+            ref_cuda = {"unavailable": out}
+        else:
+            (ref_res, ref_groups) = out
+            compare(w, got_e2e, ref_res)
+            rec["result_matches_ours"] = True
+            rec["groups"] = ref_groups
+            ref_cuda = rec
+
+    # CPU baseline: the reference's CPU path on the host cores (rank 0, N=1 only), bounded sample
     cpu = None
     if rank == 0 and world == 1:
-        ts = []
-        t_budget = time.perf_counter() + 20.0
-        while len(ts) < 3 and (not ts or time.perf_counter() < t_budget):
-            t0 = time.perf_counter()
-            w.oracle()
-            ts.append(time.perf_counter() - t0)
-        cpu = {"value": w.fact_rows / statistics.median(ts), "unit": "rows/s", "cores": 1, "kind": "port",
-               "sample": f"full-size query x{len(ts)} (median {statistics.median(ts):.3f} s), numpy oracle, 1 thread"}
+        sample_w = w.cpu_sample() if hasattr(w, "cpu_sample") else w
+        cpu, why = reference_cpu(sample_w, cpu_budget_s) if with_reference else (None, "not run")
+        if cpu is None:
+            ts = []
+            t_budget = time.perf_counter() + cpu_budget_s
+            while len(ts) < 3 and (not ts or time.perf_counter() < t_budget):
+                t0 = time.perf_counter()
+                sample_w.oracle()
+                ts.append(time.perf_counter() - t0)
+            cpu = {"value": sample_w.fact_rows / statistics.median(ts), "unit": "rows/s", "cores": 1, "kind": "port",
+                   "sample": f"full-size query x{len(ts)} (median {statistics.median(ts):.3f} s), numpy restatement "
+                             f"(oracle/tqp_oracle.py), 1 thread; the compiled reference: {why}"}
 
     peak, peak_src = peak_gbs()
     k_avg_s = (kms.value / max(kn.value, 1)) / 1000.0
@@ -946,7 +1223,13 @@ def run_ours(args, rank, world):
                      if peak_src == "measured" else "fallback 6.8 TB/s"},
         "cpu_baseline": cpu,
         "e2e": {"value": world * w.fact_rows / e2e_s, "unit": "rows/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "path": "drop-in operators, pinned host inputs"},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3, "path": e2e_path},
+        "e2e_operators": {"value": world * w.fact_rows / ops_s, "unit": "rows/s", "ms_per_step": ops_s * 1e3,
+                          "path": "drop-in operators one by one, pinned host inputs"},
+        "dropin": {"value": w.fact_rows / dropin_s, "unit": "rows/s", "ms_per_step": dropin_s * 1e3,
+                   "path": "drop-in operators over resident columns (host time included: synchronisations and "
+                           "Python)"},
+        "reference_cuda": ref_cuda,
         "clocks": clocks,
         "gpu_launches": launches,
     }
@@ -958,8 +1241,40 @@ def run_ours(args, rank, world):
         line["roofline"]["fp64"] = {"ops_per_launch": ops, "ops_per_passing_row": per_row, "achieved": got,
                                     "peak": fpk, "unit": "Gop/s", "frac": got / fpk if fpk else None,
                                     "peak_source": "measured in this run (four independent __dadd_rn chains per thread, full grid)"}
-    if rank == 0:
-        print(json.dumps(line))
+    return line
+
+
+def run_ours(args, rank, world):
+    import torch
+    import __graft_entry__ as G
+
+    G.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    names = [args.workload] if args.workload != "all" else [JoinAggTop10.name, FilterGroupBy.name, StarJoin.name,
+                                                            "batched", "serving"]
+    lines = {}
+    for name in names:
+        if name == "batched":
+            rec = run_batched_bench(args) if rank == 0 else None
+        elif name == "serving":
+            rec = run_serving_bench(args) if rank == 0 else None
+        else:
+            w = make_workload(argparse.Namespace(workload=name, scale=args.scale))
+            rec = measure_ours(args, w, rank, world, dev)
+            del w
+        lines[name] = rec
+        import gc
+        gc.collect()
+        torch.cuda.empty_cache()
+    if rank != 0:
+        return
+    head = lines[names[0]]
+    if len(names) > 1:
+        head = dict(head)
+        head["workloads"] = {n: lines[n] for n in names[1:]}
+    print(json.dumps(head))
 
 
 def main():
@@ -968,27 +1283,20 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batched", "serving"], default="join_agg_top10")
+    ap.add_argument("--workload", choices=["all"] + sorted(WORKLOADS) + ["batched", "serving"], default="all",
+                    help="all (default): the join query as the headline, every other workload as a sub-record")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="star_join only: table sizes x scale (a small case for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world = dist_setup(args.gpus)
-    if args.workload == "serving":
-        if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the reference answers one query at a time; its "
-                              "per-query CPU time is the other workloads' reference lines"}))
-        elif rank == 0:
-            run_serving_bench(args)
-        return
-    if args.workload == "batched":
-        if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the batched form has no reference counterpart"}))
-        elif rank == 0:
-            run_batched_bench(args)
-        return
     if args.impl == "reference":
+        if args.workload in ("batched", "serving"):
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "TQP-Inmem answers one query at a time: the "
+                                  "batched and served forms have no reference counterpart"}))
+            return
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world)

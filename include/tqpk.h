@@ -220,6 +220,13 @@ int tqpk_compact_noalloc(const tqpk_predicate* h_pred, const uint8_t* d_mask, in
                          const void* const* h_cols_in, const int32_t* h_dtypes, void* const* h_cols_out,
                          int64_t* d_count, tqpk_stream stream);
 
+/* [min, max] of an integer column over its n rows, read to the host (one
+ * synchronisation): the key domain a fused join sizes its directory by
+ * (hashjoin.py:50-56 sorts the build keys for the same purpose).  d_scratch:
+ * 256 bytes.  n == 0 gives min > max.                                     */
+int tqpk_key_range(const void* d_col, int32_t dtype, int64_t n, void* d_scratch, int64_t* h_min,
+                   int64_t* h_max, tqpk_stream stream);
+
 /* Test hook, no counterpart in the reference: the poll limit of the
  * compaction's look-back (<= its default) and a tile whose CTA publishes
  * nothing (-1: none).  With a tile stalled, its successors' bounded waits run

@@ -3,8 +3,8 @@
     python oracle/build_ref.py [SOURCE_TREE]
 
 SOURCE_TREE defaults to $TQP_REFERENCE, else /root/reference (where the TQP-Inmem tree is mounted
-in the build container).  Nothing is copied: each module is compiled to sourceless bytecode
-(oracle/reference.py says which modules and how).  __graft_entry__.build() runs this when the
+in the build container).  Nothing is copied: the modules are compiled into one bundle of code
+objects (oracle/reference.py says which modules and how).  __graft_entry__.build() runs this when the
 source tree is present; elsewhere (a GPU machine) the prebuilt oracle/_ref/ is used as it is.
 """
 from __future__ import annotations

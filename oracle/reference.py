@@ -7,9 +7,11 @@ and by nothing in the product.
 build() compiles the reference's operator path -- ``operators/{filter,like,hashjoin,aggregate,
 sort,project}.py``, ``IO/vortex_pipeline.py``, ``IO/pinned_mem.py``, ``variable.py``,
 ``constants.py``, ``conversion.py``, ``utility/{logger,tensor_utils}.py`` and four functions of
-``parsing.py`` -- from a TQP-Inmem source tree (``TQP_REFERENCE``) into sourceless bytecode under
-``oracle/_ref/`` (git-ignored).  The bytecode travels with a copy of this repository to a GPU
-machine, where the source tree is absent, and load() imports it there unchanged.
+``parsing.py`` -- from a TQP-Inmem source tree into one bundle of code objects,
+``oracle/_ref/tqp_inmem.bundle`` (git-ignored; Python's ``marshal`` format, so it is read by the
+same Python version only).  The bundle travels with a copy of this repository to a GPU machine,
+where the source tree is absent, and load() imports the modules from it through a finder of its
+own, unchanged.
 
 Three adaptations make the modules import without pandas, pyspark and pyparsing, and none of them
 touches the operators' arithmetic:
@@ -55,36 +57,64 @@ class ReferenceUnavailable(RuntimeError):
     """The compiled reference modules are missing or were built for another Python."""
 
 
-def _pyc(code: types.CodeType) -> bytes:
-    # header: magic, flags 0, and zero source mtime/size (a sourceless import checks only the magic)
-    return bytes(importlib.util.MAGIC_NUMBER) + bytes(12) + marshal.dumps(code)
+BUNDLE = OUT / "tqp_inmem.bundle"
+
+
+def _module_name(rel: str) -> tuple[str, bool]:
+    parts = rel[:-3].split("/")
+    if parts[-1] == "__init__":
+        return ".".join(parts[:-1]), True
+    return ".".join(parts), False
 
 
 def build(src=None) -> Path | None:
     """Compiles the reference's operator path into oracle/_ref/ when its source tree is present
-    (``src``, else ``TQP_REFERENCE``); returns oracle/_ref/, or None when neither the source nor a
-    previous build exists."""
-    src = Path(src or os.environ.get("TQP_REFERENCE", "")) if (src or os.environ.get("TQP_REFERENCE")) else None
+    (``src``); returns oracle/_ref/, or None when neither the source nor a previous build exists."""
+    src = Path(src) if src else None
     if src is None or not (src / "operators" / "aggregate.py").exists():
-        return OUT if (OUT / "manifest.json").exists() else None
+        return OUT if (OUT / "manifest.json").exists() and BUNDLE.exists() else None
     OUT.mkdir(parents=True, exist_ok=True)
-    built = []
+    mods, built = {}, []
     for rel, opt in MODULES:
-        path = src / rel
-        code = compile(path.read_text(), f"TQP-Inmem/{rel}", "exec", optimize=opt, dont_inherit=True)
-        dst = OUT / (rel[:-3] + ".pyc")
-        dst.parent.mkdir(parents=True, exist_ok=True)
-        dst.write_bytes(_pyc(code))
+        code = compile((src / rel).read_text(), f"TQP-Inmem/{rel}", "exec", optimize=opt, dont_inherit=True)
+        name, pkg = _module_name(rel)
+        mods[name] = (pkg, code)
         built.append(rel)
+    mods["operators"] = (True, compile("", "TQP-Inmem/operators", "exec", dont_inherit=True))  # a directory there
     tree = ast.parse((src / "parsing.py").read_text())
     body = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in PARSING_FUNCTIONS]
     imp = ast.parse("import re").body
-    code = compile(ast.Module(body=imp + body, type_ignores=[]), "TQP-Inmem/parsing.py", "exec", dont_inherit=True)
-    (OUT / "parsing.pyc").write_bytes(_pyc(code))
+    mods["parsing"] = (False, compile(ast.Module(body=imp + body, type_ignores=[]), "TQP-Inmem/parsing.py", "exec",
+                                      dont_inherit=True))
     built.append("parsing.py (get_id, get_name, get_literals, right_most)")
+    BUNDLE.write_bytes(marshal.dumps(mods))
     (OUT / "manifest.json").write_text(json.dumps({"magic": importlib.util.MAGIC_NUMBER.hex(),
                                                    "python": sys.version.split()[0], "modules": built}, indent=1))
     return OUT
+
+
+class _BundleImporter:
+    """Finds and loads the bundle's modules (a meta path finder and loader in one)."""
+
+    def __init__(self, mods):
+        self.mods = mods
+
+    def find_spec(self, name, path=None, target=None):
+        if name not in self.mods:
+            return None
+        pkg, _ = self.mods[name]
+        spec = importlib.util.spec_from_loader(name, self, origin=f"{BUNDLE}:{name}", is_package=pkg)
+        if pkg:
+            spec.submodule_search_locations = []
+        return spec
+
+    def create_module(self, spec):
+        return None
+
+    def exec_module(self, module):
+        pkg, code = self.mods[module.__name__]
+        module.__file__ = f"{BUNDLE}:{module.__name__}"
+        exec(code, module.__dict__)
 
 
 def _stub(name: str, **attrs) -> types.ModuleType:
@@ -103,7 +133,7 @@ _LOADED = None
 def available() -> tuple[bool, str]:
     """(True, '') when load() can import the compiled reference, else (False, why)."""
     man = OUT / "manifest.json"
-    if not man.exists():
+    if not man.exists() or not BUNDLE.exists():
         return False, "oracle/_ref was not built (the TQP-Inmem source tree was absent when build() ran)"
     magic = json.loads(man.read_text()).get("magic")
     if magic != importlib.util.MAGIC_NUMBER.hex():
@@ -132,8 +162,8 @@ def load() -> types.SimpleNamespace:
           DoubleType=None)
     _stub("pyparsing")
     _stub("expression", parse=None)
-    if str(OUT) not in sys.path:
-        sys.path.insert(0, str(OUT))
+    bundle = marshal.loads(BUNDLE.read_bytes())
+    sys.meta_path.insert(0, _BundleImporter(bundle))
     import importlib
     mods = {}
     for name in ("constants", "variable", "conversion", "parsing", "utility.logger", "IO.vortex_pipeline",
@@ -141,9 +171,8 @@ def load() -> types.SimpleNamespace:
                  "operators.project"):
         mods[name] = importlib.import_module(name)
     for name, m in mods.items():
-        f = getattr(m, "__file__", "") or ""
-        if not f.startswith(str(OUT)):
-            raise ReferenceUnavailable(f"module {name} resolved outside oracle/_ref ({f})")
+        if not isinstance(getattr(m, "__loader__", None), _BundleImporter):
+            raise ReferenceUnavailable(f"module {name} resolved outside oracle/_ref ({getattr(m, '__file__', '')})")
     lg = mods["utility.logger"]
     lg.set_perf_logger(None, False)           # as main.py does before running queries
     lg.set_message_logger(None, False)

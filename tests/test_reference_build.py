@@ -28,8 +28,8 @@ def ref():
 
 def test_modules_come_from_the_compiled_tree(ref):
     for name in ("filter", "hashjoin", "aggregate", "sort", "project", "variable", "pinned_mem"):
-        assert getattr(ref, name).__file__.startswith(str(reference.OUT))
-        assert getattr(ref, name).__file__.endswith(".pyc")
+        assert getattr(ref, name).__file__.startswith(str(reference.BUNDLE))
+        assert isinstance(getattr(ref, name).__loader__, reference._BundleImporter)
 
 
 def test_join_aggregate_topk_reproduces_its_golden_fixture(ref):

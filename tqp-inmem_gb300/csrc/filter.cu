@@ -458,6 +458,18 @@ extern "C" int tqpk_debug_compact_wait(int32_t spin_limit, int64_t stall_tile) {
   return TQPK_OK;
 }
 
+// [min, max] of one integer column over all n rows (one host synchronisation); d_scratch holds
+// 256 bytes.  An empty column gives min > max.
+extern "C" int tqpk_key_range(const void* d_col, int32_t dtype, int64_t n, void* d_scratch, int64_t* h_min,
+                              int64_t* h_max, tqpk_stream stream) {
+  if (n < 0 || !d_scratch || !h_min || !h_max || (n > 0 && !d_col)) return TQPK_EINVAL;
+  int64_t cnt = 0;
+  const void* cols[1] = {d_col};
+  const int32_t dts[1] = {dtype};
+  return key_ranges(nullptr, nullptr, n, 1, cols, dts, h_min, h_max, &cnt, d_scratch,
+                    static_cast<cudaStream_t>(stream));
+}
+
 extern "C" size_t tqpk_compact_workspace_bytes(int64_t n) { return compact_status_bytes(n < 0 ? 0 : n); }
 
 extern "C" int tqpk_compact(const tqpk_predicate* h_pred, const uint8_t* d_mask, int64_t n, int32_t ncols,

@@ -66,15 +66,29 @@ __global__ void __launch_bounds__(kBlock) k_pl_build(const __grid_constant__ tqp
   }
 }
 
-// The build side's membership bitmap: one atomicOr per passing build row; a bit that was
-// already set is a repeated key.
+// The build side's membership bitmap: one atomicOr per passing build row, its result unused (a
+// reduction the L2 applies without a reply).  The same grid first sets every group sum to -0.0
+// (the empty sum), so no separate fill pass runs.  The passing rows are counted (one atomic per
+// CTA); the top-k pass counts the bits set, and fewer bits than rows means a repeated key.
 __global__ void __launch_bounds__(kBlock) k_pl_build_bits(const __grid_constant__ tqpk_predicate P, PipeJoinArgs A,
-                                                          unsigned* __restrict__ bits, int* err_dup) {
+                                                          unsigned* __restrict__ bits, double* __restrict__ sum,
+                                                          unsigned long long* passing, int* err) {
+  __shared__ unsigned s_pass;
+  if (threadIdx.x == 0) s_pass = 0;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nthr = (int64_t)gridDim.x * blockDim.x;
+  {
+    const double2 e2 = make_double2(u2d(DenseSumSource::kEmptySum), u2d(DenseSumSource::kEmptySum));
+    const bool vec = (reinterpret_cast<uintptr_t>(sum) & 15u) == 0;
+    const int64_t pairs = vec ? A.slots / 2 : 0;
+    for (int64_t i = tid; i < pairs; i += nthr) reinterpret_cast<double2*>(sum)[i] = e2;
+    for (int64_t i = 2 * pairs + tid; i < A.slots; i += nthr) sum[i] = e2.x;
+  }
+  __syncthreads();
   const int64_t groups = (A.nb + 3) >> 2;
   const bool vec = ((reinterpret_cast<uintptr_t>(A.b_keys) & 15u) == 0);
   const bool pvec = A.b_pvec != 0;
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < groups;
-       g += (int64_t)gridDim.x * blockDim.x) {
+  unsigned npass = 0;
+  for (int64_t g = tid; g < groups; g += nthr) {
     const int64_t r0 = g << 2;
     uint32_t b = P.n_insn ? eval_pred4(P, r0, A.nb, pvec) : (A.nb - r0 >= 4 ? 0xfu : ((1u << (A.nb - r0)) - 1));
     if (!b) continue;
@@ -84,11 +98,15 @@ __global__ void __launch_bounds__(kBlock) k_pl_build_bits(const __grid_constant_
     for (int j = 0; j < 4; ++j) {
       if (!((b >> j) & 1u)) continue;
       const int64_t slot = x[j] - A.key_min;
-      if (slot < 0 || slot >= A.slots) { set_error(err_dup, TQPK_EINVAL); continue; }
-      const unsigned bit = 1u << (slot & 31);
-      if (atomicOr(&bits[slot >> 5], bit) & bit) set_error(err_dup, TQPK_EUNSUPPORTED);
+      if (slot < 0 || slot >= A.slots) { set_error(err, TQPK_EINVAL); continue; }
+      atomicOr(&bits[slot >> 5], 1u << (slot & 31));
+      ++npass;
     }
   }
+  npass = __reduce_add_sync(0xffffffffu, npass);
+  if ((threadIdx.x & 31) == 0 && npass) atomicAdd(&s_pass, npass);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_pass) atomicAdd(passing, (unsigned long long)s_pass);
 }
 
 __global__ void __launch_bounds__(kBlock) k_pl_probe_agg(const __grid_constant__ tqpk_predicate P,
@@ -152,19 +170,6 @@ __global__ void __launch_bounds__(kBlock) k_pl_probe_agg(const __grid_constant__
   }
 }
 
-// Writes the top-k slots as (build key, sum) rows.
-__global__ void k_pl_emit(const int64_t* idx, const int64_t* count, const double* sum, int64_t key_min, int k,
-                          int64_t* out_keys, double* out_vals, int64_t* out_count) {
-  const int64_t m = *count;
-  for (int j = threadIdx.x; j < k; j += blockDim.x) {
-    if (j < m) {
-      out_keys[j] = key_min + idx[j];
-      out_vals[j] = sum[idx[j]];
-    }
-  }
-  if (threadIdx.x == 0) *out_count = m;
-}
-
 constexpr int kPipeMaxK = 256;
 
 struct PipeLayout {
@@ -175,6 +180,7 @@ struct PipeLayout {
   int* err;
   unsigned* done;
   int64_t* top_count;
+  unsigned long long* passing;
   int64_t* top_idx;
   uint64_t* cand_key;
   int64_t* cand_slot;
@@ -192,7 +198,9 @@ static bool pipe_layout(void* ws, size_t bytes, int64_t slots, int grid, PipeLay
   L.groups = reinterpret_cast<unsigned long long*>(hdr);      // hdr[0..1]
   L.err = hdr + 2;                                            // hdr[2]
   L.done = reinterpret_cast<unsigned*>(hdr + 3);              // hdr[3]
-  L.top_count = reinterpret_cast<int64_t*>(hdr + 4);          // hdr[4..5]
+  L.top_count = reinterpret_cast<int64_t*>(hdr + 4);          // hdr[4..5]; the top-k's bound hdr[6..7], its
+                                                              // arrival counter hdr[8], bits set hdr[10..11]
+  L.passing = reinterpret_cast<unsigned long long*>(hdr + 12); // hdr[12..13]: passing build rows
   L.dir = c.take<int>(slots);
   L.sum = c.take<double>(slots);
   L.cnt = c.take<unsigned>(slots);
@@ -259,12 +267,15 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
   const bool bits = (stages & 16) != 0;      // membership bitmap in place of the row directory
   if (bits && (stages & 2)) return TQPK_EINVAL;
   if (stages & 1) {
-  TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 32, s));
+  TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 56, s));   // hdr[0..13]
   if (bits)
     TQPK_CUDA(cudaMemsetAsync(L.dir, 0, ((slots + 31) / 32) * 4, s));
   else
     TQPK_CUDA(cudaMemsetAsync(L.dir, 0xff, slots * 4, s));
-  if (sentinel) {
+  if (bits && !sentinel) return TQPK_EINVAL;        // the bitmap build fills the sentinel sums
+  if (bits) {
+    // the build kernel fills the sums
+  } else if (sentinel) {
     k_pl_fill_u64<<<grid_for(slots, 4), kBlock, 0, s>>>(reinterpret_cast<uint64_t*>(L.sum), slots,
                                                         DenseSumSource::kEmptySum);
     TQPK_CHECK_LAUNCH();
@@ -272,13 +283,15 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
     TQPK_CUDA(cudaMemsetAsync(L.sum, 0, slots * 8, s));
     TQPK_CUDA(cudaMemsetAsync(L.cnt, 0, slots * 4, s));
   }
-  if (nb > 0) {
+  if (bits) {                                        // also fills the sums: runs with no build rows too
     timing_before(KID_PIPE_BUILD, s);
-    if (bits)
-      k_pl_build_bits<<<grid_for((nb + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_build_pred), A,
-                                                                   reinterpret_cast<unsigned*>(L.dir), L.err);
-    else
-      k_pl_build<<<grid_for((nb + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_build_pred), A, L.dir, L.err);
+    k_pl_build_bits<<<grid_for(std::max<int64_t>((nb + 3) / 4, slots / 2), 8), kBlock, 0, s>>>(
+        *pred_or_empty(h_build_pred), A, reinterpret_cast<unsigned*>(L.dir), L.sum, L.passing, L.err);
+    timing_after(KID_PIPE_BUILD, s);
+    TQPK_CHECK_LAUNCH();
+  } else if (nb > 0) {
+    timing_before(KID_PIPE_BUILD, s);
+    k_pl_build<<<grid_for((nb + 3) / 4, 8), kBlock, 0, s>>>(*pred_or_empty(h_build_pred), A, L.dir, L.err);
     timing_after(KID_PIPE_BUILD, s);
     TQPK_CHECK_LAUNCH();
   }
@@ -291,17 +304,27 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
     TQPK_CHECK_LAUNCH();
   }
   if (stages & 4) {
-    TQPK_CUDA(cudaMemsetAsync(L.top_count + 1, 0, 16, s));  // the top-k cut and arrival counters of this run
-    TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 8, s));          // the group count the top-k pass accumulates
+    // the top-k's bound, arrival counter and bits-set count (hdr[6..11]) and the group count
+    TQPK_CUDA(cudaMemsetAsync(L.top_count + 1, 0, 24, s));
+    TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 8, s));
     DenseSumSource src{L.sum, sentinel ? nullptr : L.cnt, slots, A.desc};
     TopkOut O{L.top_idx, L.top_count, L.cand_key, L.cand_slot, L.done, L.groups,
-              reinterpret_cast<unsigned long long*>(L.top_count + 1), reinterpret_cast<unsigned*>(L.top_count + 2)};   // hdr[6..7], zeroed with the header
+              reinterpret_cast<unsigned long long*>(L.top_count + 1), reinterpret_cast<unsigned*>(L.top_count + 2)};
+    O.emit_keys = d_out_keys;          // the top rows straight from the top-k's last CTA
+    O.emit_vals = d_out_vals;
+    O.emit_count = d_out_count;
+    O.emit_sum = L.sum;
+    O.emit_key_min = key_min;
+    if (bits) {                        // occupancy also needs the slot's bit; the bit count checks the build
+      src.bits = reinterpret_cast<const unsigned*>(L.dir);
+      O.bits_set = reinterpret_cast<unsigned long long*>(L.top_count + 3);
+      O.bits_expected = L.passing;
+      O.err = L.err;
+    }
     timing_before(KID_PIPE_TOPK, s);
     int trc = topk_warp_launch(0, &src, k, grid, O, s);
     timing_after(KID_PIPE_TOPK, s);
     if (trc) return trc;
-    k_pl_emit<<<1, 256, 0, s>>>(L.top_idx, L.top_count, L.sum, key_min, k, d_out_keys, d_out_vals, d_out_count);
-    TQPK_CHECK_LAUNCH();
   }
   if ((stages & 4) && d_groups_out) TQPK_CUDA(cudaMemcpyAsync(d_groups_out, L.groups, 8, cudaMemcpyDeviceToDevice, s));
   return TQPK_OK;

@@ -94,6 +94,8 @@ struct DenseSumSource {
                          // occupied exactly when its bits are no longer those of -0.0
   int64_t n;
   int desc;
+  const unsigned* bits = nullptr;   // when set, only slots whose bit is set can be occupied (the join's
+                                    // build writes its passing keys' bits and initialises those sums)
   static constexpr uint64_t kEmptySum = 0x8000000000000000ull;
   __device__ __forceinline__ uint64_t order_key(double v) const {
     if (v == 0.0) v = 0.0;
@@ -102,8 +104,14 @@ struct DenseSumSource {
     const uint64_t u = (b & (1ull << 63)) ? ~b : (b | (1ull << 63));
     return desc ? ~u : u;
   }
+  // The membership nibble of slots i0..i0+3 (i0 % 4 == 0): all ones without a bitmap.
+  __device__ __forceinline__ unsigned bits4(int64_t i0) const {
+    if (!bits) return 0xfu;
+    return (__ldcg(&bits[i0 >> 5]) >> (i0 & 31)) & 0xfu;
+  }
   __device__ __forceinline__ bool get(int64_t i, uint64_t& k) const {
     if (i >= n) return false;
+    if (bits && !((__ldcg(&bits[i >> 5]) >> (i & 31)) & 1u)) return false;
     if (!cnt) {
       const double v = __ldcg(&sum[i]);
       if (d2u(v) == kEmptySum) return false;
@@ -135,7 +143,7 @@ struct DenseSumSource {
         k[q] = order_key(v[q]);
         ok |= (d2u(v[q]) != kEmptySum ? 1u : 0u) << q;
       }
-      return ok;
+      return ok & bits4(i0);
     }
     if (i0 + 4 <= n && ((reinterpret_cast<uintptr_t>(cnt) | reinterpret_cast<uintptr_t>(sum)) & 15u) == 0) {
       const uint4 cc = __ldcg(reinterpret_cast<const uint4*>(cnt + i0));
@@ -156,7 +164,7 @@ struct DenseSumSource {
       k[q] = order_key(v[q]);
       ok |= (c[q] != 0u ? 1u : 0u) << q;
     }
-    return ok;
+    return ok & bits4(i0);
   }
 };
 
@@ -168,6 +176,7 @@ struct ArraySource {
   int64_t n;
   int desc;
   __device__ __forceinline__ bool get(int64_t i, uint64_t& k) const;
+  __device__ __forceinline__ unsigned bits4(int64_t) const { return 0xfu; }
   __device__ __forceinline__ unsigned get4(int64_t i0, uint64_t* k) const {
     unsigned ok = 0;
 #pragma unroll
@@ -183,8 +192,21 @@ struct TopkOut {
   int64_t* cand_idx;
   unsigned* ticket;
   unsigned long long* valid_total;  // number of valid items seen (may be null)
-  unsigned long long* bound;        // ~(best known k-th key), raised with atomicMax; 0 = none (zeroed with the ticket)
+  unsigned long long* bound;        // the cut (written by the first pass)
   unsigned* arrive;                 // [2] CTAs done with the group-best and the filter pass (zeroed before the launch)
+  // Optional, for a dense group table: the last CTA also writes (key_min + slot, sum[slot]) of the
+  // top rows and their number (emit_keys null: not written) ...
+  int64_t* emit_keys = nullptr;
+  double* emit_vals = nullptr;
+  int64_t* emit_count = nullptr;
+  const double* emit_sum = nullptr;
+  int64_t emit_key_min = 0;
+  // ... and checks that the membership bits set (counted into bits_set, zeroed before the launch)
+  // are as many as the rows that set them (bits_expected): fewer means a repeated key, reported
+  // as TQPK_EUNSUPPORTED in *err.  bits_set null: no check.
+  unsigned long long* bits_set = nullptr;
+  const unsigned long long* bits_expected = nullptr;
+  int* err = nullptr;
 };
 
 // ---------------------------------------------------------------------------
@@ -257,29 +279,63 @@ template <class Src>
 __global__ void __launch_bounds__(256) k_tk_group_best(Src src, int64_t G, int k, TopkOut O) {
   __shared__ uint64_t red[8];
   const int64_t b0 = (int64_t)blockIdx.x * G, b1 = b0 + G < src.n ? b0 + G : src.n;
+  __shared__ unsigned s_valid, s_bits;
+  if (threadIdx.x == 0) { s_valid = 0; s_bits = 0; }
+  __syncthreads();
   uint64_t best = ~0ull;
-  unsigned valid = 0;
+  unsigned valid = 0, nbits = 0;
   for (int64_t i0 = b0 + threadIdx.x * 4; i0 < b1; i0 += 4 * (int64_t)blockDim.x) {
     uint64_t key[4];
-    const unsigned ok = src.get4(i0, key);
+    const unsigned tail = i0 + 4 <= b1 ? 0xfu : (1u << (b1 - i0)) - 1u;
+    const unsigned ok = src.get4(i0, key) & tail;
+    if (O.bits_set) nbits += __popc(src.bits4(i0) & tail);
+    valid += __popc(ok);
 #pragma unroll
     for (int q = 0; q < 4; ++q)
-      if (((ok >> q) & 1u) && i0 + q < b1) {
-        best = key[q] < best ? key[q] : best;
-        ++valid;
-      }
+      if ((ok >> q) & 1u) best = key[q] < best ? key[q] : best;
   }
+  // one atomic per CTA for each count: per-warp atomics on one address serialise in the L2
   valid = __reduce_add_sync(0xffffffffu, valid);
-  if ((threadIdx.x & 31) == 0 && valid && O.valid_total) atomicAdd(O.valid_total, (unsigned long long)valid);
-  block_min_u64(best, red);
+  nbits = __reduce_add_sync(0xffffffffu, nbits);
+  if ((threadIdx.x & 31) == 0) {
+    if (valid) atomicAdd(&s_valid, valid);
+    if (nbits) atomicAdd(&s_bits, nbits);
+  }
+  block_min_u64(best, red);        // its barriers order the shared counts too
   if (threadIdx.x == 0) {
     O.cand_key[kTopkCap + blockIdx.x] = best;
     if (blockIdx.x == 0) *O.ticket = 0;          // the candidate counter of the next pass
+    if (s_valid && O.valid_total) atomicAdd(O.valid_total, (unsigned long long)s_valid);
+    if (s_bits && O.bits_set) atomicAdd(O.bits_set, (unsigned long long)s_bits);
   }
   if (tk_last_cta(O.arrive)) tk_cut((int)gridDim.x, k, O);
 }
 
 constexpr int kTopkSortCap = 2048;   // candidates the final CTA sorts in shared memory
+
+// The last CTA's outputs: the count, the optional dense-table rows (key_min + slot, sum) and the
+// membership-bit check.  si[0..m) holds the winners' indices.  tk_finish: every thread of the
+// CTA; tk_finish_warp: one warp.
+__device__ __forceinline__ void tk_emit(int j, const TopkOut& O, const int64_t* si) {
+  if (O.emit_keys) {
+    O.emit_keys[j] = O.emit_key_min + si[j];
+    O.emit_vals[j] = __ldcg(&O.emit_sum[si[j]]);
+  }
+}
+__device__ __forceinline__ void tk_counts(int m, const TopkOut& O) {
+  *O.out_count = m;
+  if (O.emit_count) *O.emit_count = m;
+  if (O.bits_set && O.bits_expected && O.err && atomicAdd(O.bits_set, 0ull) != __ldcg(O.bits_expected))
+    set_error(O.err, TQPK_EUNSUPPORTED);     // fewer bits than passing build rows: a repeated key
+}
+__device__ __forceinline__ void tk_finish(int m, const TopkOut& O, const int64_t* si) {
+  for (int j = threadIdx.x; j < m; j += blockDim.x) tk_emit(j, O, si);
+  if (threadIdx.x == 0) tk_counts(m, O);
+}
+__device__ __forceinline__ void tk_finish_warp(int m, const TopkOut& O, const int64_t* si) {
+  for (int j = threadIdx.x & 31; j < m; j += 32) tk_emit(j, O, si);
+  if ((threadIdx.x & 31) == 0) tk_counts(m, O);
+}
 
 // The final step, in one CTA: sort the candidates under the cut by (key, index), or, when
 // ties put more than kTopkSortCap items under it, warp lists over every item.
@@ -310,7 +366,7 @@ __device__ __forceinline__ void tk_final(const Src& src, int k, TopkOut O) {
       }
     const int m = (int)cnt < k ? (int)cnt : k;
     for (int j = threadIdx.x; j < m; j += blockDim.x) O.out_idx[j] = si[j];
-    if (threadIdx.x == 0) *O.out_count = m;
+    tk_finish(m, O, si);
     return;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -344,9 +400,13 @@ __device__ __forceinline__ void tk_final(const Src& src, int k, TopkOut O) {
     const int p = r * 32 + lane;
     const bool v = p < k && M.idx[r] >= 0;
     c += __popc(__ballot_sync(0xffffffffu, v));
-    if (v) O.out_idx[p] = M.idx[r];
+    if (v) {
+      O.out_idx[p] = M.idx[r];
+      si[p] = M.idx[r];
+    }
   }
-  if (lane == 0) *O.out_count = c;
+  __syncwarp();
+  tk_finish_warp(c, O, si);
 }
 
 // Pass 2: the items at or under the cut are appended to the candidate list; the last CTA
@@ -378,7 +438,7 @@ __global__ void __launch_bounds__(256) k_tk_filter(Src src, int k, TopkOut O) {
 }
 
 // Host launcher: k <= 256.  The cand arrays hold topk_cand_entries(k) entries each;
-// O.ticket, O.bound, O.arrive[0..1] and O.valid_total must be zero before the call.
+// O.ticket, O.bound, O.arrive[0..1], O.valid_total and O.bits_set must be zero before the call.
 int topk_warp_launch(int kind, const void* src, int k, int grid, TopkOut O, cudaStream_t s);
 inline int topk_grid_size() { return num_sms(); }
 inline size_t topk_cand_entries(int k) {

@@ -115,6 +115,20 @@ def compact(cols: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = None,
     return [o[:m] for o in outs], m
 
 
+def key_range(col: torch.Tensor) -> Tuple[int, int]:
+    """(min, max) of an integer column over all its rows (one host read); min > max when empty."""
+    lib = L.load()
+    col = _col1d(col)
+    _check_cuda(col)
+    lo, hi = C.c_int64(0), C.c_int64(-1)
+    if col.numel() == 0:
+        return 0, -1
+    scratch = _ws(256, col.device)
+    L.check(lib.tqpk_key_range(col.data_ptr(), code_of(col.dtype), col.numel(), scratch.data_ptr(), C.byref(lo),
+                               C.byref(hi), _stream(col.device)), "tqpk_key_range")
+    return int(lo.value), int(hi.value)
+
+
 # ---------------------------------------------------------------- (d) group-by
 def _count_groups_from_keys(prog: AggregateProgram, plan, pred, n: int, device, s: int) -> int:
     """Occupied slots of the group table, from the key columns (and the mask) alone: a

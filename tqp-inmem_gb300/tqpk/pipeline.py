@@ -130,7 +130,10 @@ class JoinAggTopK:
         jit.launch(self._probe_handle, self._probe_grid, 256, self._probe_smem, self._probe_args, s,
                    L.KID_PIPE_PROBE)
 
-    def run(self, stream=None):
+    def run(self, stream=None, before_probe=None):
+        """Queues the whole query on `stream` (default: the current stream).  before_probe, when
+        given, is called between the build stage and the probe (e.g. to make the stream wait for
+        probe columns still being copied, so the build overlaps their copies)."""
         from . import jit
         s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
         from .predicate import has_strings
@@ -139,10 +142,34 @@ class JoinAggTopK:
             sent = 0 if self._tma_ok() else 8      # the generated register probe keeps occupancy in the sums
             bits = 16 if self._probe_uses_bits() else 0   # the build stage writes the membership bitmap
             self._stages(1 | sent | bits, s)
+            if before_probe is not None:
+                before_probe()
             self._jit_probe(s)
-            self._stages(4 | sent, s)
+            self._stages(4 | sent | bits, s)
+            self._sentinel = bool(sent)
         else:
+            if before_probe is not None:
+                before_probe()
             self._stages(7, s)
+            self._sentinel = False
+
+    def result_device(self):
+        """(keys int64[m], sums float64[m], m) as device tensors after the last run, with one host
+        read (the count and the error word together).  A repeated build key raises
+        NotImplementedError (TQPK_EUNSUPPORTED), an out-of-domain one ValueError."""
+        import ctypes
+        d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        if getattr(self, "_probe_smem", 0):
+            self.check_error()                      # the TMA-staged probe keeps its own error word
+        hdr = torch.empty(16, dtype=torch.int32, pin_memory=True)
+        cur = torch.cuda.current_stream(self.dev)
+        hdr[:4].copy_(self.ws[:16].view(torch.int32), non_blocking=True)       # hdr[2] = error word
+        hdr[4:6].copy_(self.out_count.view(torch.int32), non_blocking=True)
+        cur.synchronize()
+        err, m = int(hdr[2]), int(hdr[4:6].view(torch.int64)[0])
+        if err:
+            L.check(err, "fused join pipeline (repeated or out-of-domain build key)")
+        return self.out_keys[:m], self.out_vals[:m], m
 
 
     def capture(self):
@@ -168,6 +195,23 @@ class JoinAggTopK:
         L.check(self.lib.tqpk_pipeline_error(self.ws.data_ptr(), C.byref(err), s), "tqpk_pipeline_error")
         if err.value:
             L.check(err.value, "fused join pipeline (repeated or out-of-domain build key)")
+
+    def group_table(self):
+        """Every group of the last run, not only the top k: (build keys int64[G] ascending,
+        sums float64[G]), read from the slot table (synchronises)."""
+        self.check_error()
+        d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        L.check(self.lib.tqpk_pipeline_join_tables(self.ws.data_ptr(), self.ws.numel(), self.key_min, self.key_max,
+                                                   C.byref(d), C.byref(su), C.byref(oc)), "tqpk_pipeline_join_tables")
+        slots = self.key_max - self.key_min + 1
+        base = self.ws.data_ptr()
+        sums = self.ws[su.value - base: su.value - base + 8 * slots].view(torch.float64)
+        if getattr(self, "_sentinel", False):      # an empty slot keeps the bits of -0.0
+            occ = sums.view(torch.int64) != torch.iinfo(torch.int64).min
+        else:
+            occ = self.ws[oc.value - base: oc.value - base + 4 * slots].view(torch.int32) != 0
+        idx = torch.nonzero(occ).reshape(-1)
+        return (idx + self.key_min).cpu().numpy(), sums[idx].cpu().numpy()
 
     def result(self):
         """(keys int64[m], sums float64[m], groups) after the last run (synchronises)."""
@@ -341,6 +385,16 @@ class StarAggTopK:
 
     def replay(self):
         self.graph.replay()
+
+    def group_table(self):
+        """Every group of the last run (generated-probe path): (C keys int64[G] ascending,
+        sums float64[G], counts int64[G]) (synchronises)."""
+        if not getattr(self, "_jit_path", False):
+            raise NotImplementedError("the group table is read on the generated-probe path only")
+        self.result()                                  # raises on a recorded error
+        idx = torch.nonzero(self.cnt != 0).reshape(-1)
+        cmn = self.doms[2][0]
+        return ((idx + cmn).cpu().numpy(), self.sum[idx].cpu().numpy(), self.cnt[idx].to(torch.int64).cpu().numpy())
 
     def result(self):
         s = torch.cuda.current_stream(self.dev).cuda_stream

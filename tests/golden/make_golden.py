@@ -611,6 +611,80 @@ def sort_multikey(ref):
           {"specs": [[s, l] for s, l in specs], "types": types_}, outs)
 
 
+@case
+def late_materialisation_masks(ref):
+    """Operators whose inputs do not share one mask (vortex_pipeline.py:54-58 compacts each
+    masked input by its own mask): an aggregate over masked columns beside an already compacted
+    one, an aggregate over two different masks with equal counts, and a join whose probe side
+    mixes masked and compacted columns."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(53)
+    n = 20011
+    m900 = rng.random(n) < 0.6
+    kept = int(m900.sum())
+    m901 = np.roll(m900, 7)                                # another mask with the same count
+    cols = {1: rng.integers(0, 40, n).astype(np.int64), 3: rng.normal(100.0, 30.0, n),
+            6: rng.normal(5.0, 2.0, kept), 7: rng.integers(-50, 50, n).astype(np.int64),
+            900: m900, 901: m901}
+    types_ = {1: "int", 3: "float", 6: "float", 7: "int", 900: "bool", 901: "bool"}
+    res = ["k#1", [[["sum", ["v#3"]], "#", "601"], "AS", "s#611"], [[["sum", ["w#6"]], "#", "602"], "AS", "t#612"],
+           [[["count", ["1"]], "#", "603L"], "AS", "c#613"], [[["max", ["v#3"]], "#", "604"], "AS", "m#614"]]
+    mixed = {"name": "Aggregate", "is partial": False, "keys": ["k#1"], "input ids": [1, 3, 6], "results": res,
+             "out agg ids": [611, 612, 613, 614], "mask map": {1: 900, 3: 900}}
+    tg = _tg(V.Variable, {c: cols[c] for c in (1, 3, 6, 900)}, types_)
+    torch.manual_seed(3)
+    ag.tqp_hash_aggregate(False, tg, copy.deepcopy(mixed), _Pool(), None, "a")
+    outs = {f"mixed_{c}": tg[c].tensor.numpy() for c in (1, 611, 612, 613, 614)}
+    res2 = ["k#1", [[["sum", ["v#3"]], "#", "621"], "AS", "s#631"], [[["sum", ["x#7"]], "#", "622"], "AS", "t#632"]]
+    two = {"name": "Aggregate", "is partial": False, "keys": ["k#1"], "input ids": [1, 3, 7], "results": res2,
+           "out agg ids": [631, 632], "mask map": {1: 900, 3: 900, 7: 901}}
+    tg = _tg(V.Variable, {c: cols[c] for c in (1, 3, 7, 900, 901)}, types_)
+    torch.manual_seed(4)
+    ag.tqp_hash_aggregate(False, tg, copy.deepcopy(two), _Pool(), None, "a")
+    outs.update({f"two_{c}": tg[c].tensor.numpy() for c in (1, 631, 632)})
+    # join: build side filtered (mask 911), probe side = key and value masked by 912 beside a
+    # column already compacted by that filter
+    nb, npr = 3001, 12007
+    b_key = (rng.permutation(nb) + 1).astype(np.int32)
+    m911 = rng.random(nb) < 0.5
+    p_key = rng.integers(1, nb + 1, npr).astype(np.int32)
+    m912 = rng.random(npr) < 0.55
+    jcols = {11: b_key, 21: p_key, 23: rng.normal(10.0, 3.0, npr), 26: rng.integers(0, 9, int(m912.sum())).astype(np.int64),
+             911: m911, 912: m912}
+    jtypes = {11: "int", 21: "int", 23: "float", 26: "int", 911: "bool", 912: "bool"}
+    jargs = {"name": "Join", "left group": [11], "right group": [21, 23, 26], "materialized in": [11, 21, 23, 26],
+             "mask map": {11: 911, 21: 912, 23: 912}}
+    tg = _tg(V.Variable, jcols, jtypes)
+    hj.join_vortex(False, tg, copy.deepcopy(jargs), 11, 21, [], "inner", None, _Pool(), "j")
+    outs.update({f"join_{c}": tg[c].tensor.numpy() for c in (11, 21, 23, 26)})
+    ins = {str(k): v for k, v in cols.items()}
+    ins.update({f"j{k}": v for k, v in jcols.items()})
+    _save("late_materialisation_masks", ins, {"mixed": _jsonable(mixed), "two": _jsonable(two), "join": _jsonable(jargs),
+                                              "types": types_, "jtypes": jtypes}, outs)
+
+
+@case
+def join_outer_string_payload(ref):
+    """A right-outer join that must null-fill an int8 [N, w] build-side payload: the reference's
+    index_with_null (conversion.py:52-57) masks [M, w] rows with an [M] mask, which torch does
+    not broadcast, so the operator raises; the fixture records the error class."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(59)
+    nb, npr = 400, 1500
+    cols = {11: (rng.permutation(nb) + 1).astype(np.int32), 13: _strings(rng, ["RED", "GREEN", "BLUE"], nb, 10),
+            21: rng.integers(1, 2 * nb, npr).astype(np.int32)}
+    types_ = {11: "int", 13: "string", 21: "int"}
+    jargs = {"name": "Join", "left group": [11, 13], "right group": [21], "materialized in": [11, 13, 21]}
+    tg = _tg(V.Variable, cols, types_)
+    try:
+        hj.join_vortex(False, tg, copy.deepcopy(jargs), 11, 21, [], "right-outer", None, _Pool(), "j")
+        err = ""
+    except Exception as e:                     # noqa: BLE001  (recorded, not hidden)
+        err = type(e).__name__
+    _save("join_outer_string_payload", {str(k): v for k, v in cols.items()},
+          {"join": jargs, "types": types_, "error": err}, {"raised": np.array(err)})
+
+
 def main(argv):
     ref = load_reference()
     from oracle import reference

@@ -916,3 +916,44 @@ def test_project_substring_then_group_by_it():
     np.testing.assert_array_equal(tg[501].tensor.cpu().numpy().reshape(-1), agg[501].reshape(-1))
     assert_f64_close(tg[503].tensor.cpu().numpy().reshape(-1), agg[503].reshape(-1),
                      magnitude=np.abs(ref[401]).sum())
+
+
+def test_late_materialisation_masks_golden():
+    """Inputs that do not share one mask: each masked column is compacted by its own mask first,
+    as the reference's pipeline does (vortex_pipeline.py:54-58)."""
+    from tqpk.operators import join_vortex, tqp_hash_aggregate
+    ins, outs, args = load("late_materialisation_masks")
+    types = args["types"]
+    cols = {k: v for k, v in ins.items() if isinstance(k, int)}
+
+    def tg_of(ids, types_):
+        return {c: V(cols[c] if c in cols else None, types_[str(c)]) for c in ids}
+    for name, ids, out_ids in (("mixed", (1, 3, 6, 900), (611, 612, 613, 614)), ("two", (1, 3, 7, 900, 901), (631, 632))):
+        a = copy.deepcopy(args[name])
+        a["mask map"] = {int(k): v for k, v in a["mask map"].items()}
+        tg = tg_of(ids, types)
+        tqp_hash_aggregate(True, tg, a, None, None, "a")
+        order = np.argsort(outs[f"{name}_1"].reshape(-1), kind="stable")
+        np.testing.assert_array_equal(np_(tg[1].tensor).reshape(-1), outs[f"{name}_1"].reshape(-1)[order])
+        for c in out_ids:
+            g, o = outs[f"{name}_{c}"][order], np_(tg[c].tensor)
+            assert o.dtype == g.dtype, (c, o.dtype, g.dtype)
+            assert_f64_close(o, g) if g.dtype == np.float64 else np.testing.assert_array_equal(o, g)
+    jcols = {int(k[1:]): v for k, v in ins.items() if isinstance(k, str) and k.startswith("j")}
+    tg = {c: V(v, args["jtypes"][str(c)]) for c, v in jcols.items()}
+    j = copy.deepcopy(args["join"])
+    j["mask map"] = {int(k): v for k, v in j["mask map"].items()}
+    join_vortex(True, tg, j, 11, 21, [], "inner", None, None, "j")
+    for c in (11, 21, 23, 26):
+        np.testing.assert_array_equal(np_(tg[c].tensor).reshape(-1), outs[f"join_{c}"].reshape(-1))
+
+
+def test_join_outer_string_payload_raises_like_the_reference():
+    """The reference's null fill of an [N, w] payload does not broadcast and raises RuntimeError
+    (conversion.py:52-57); the drop-in raises the same class."""
+    from tqpk.operators import join_vortex
+    ins, outs, args = load("join_outer_string_payload")
+    assert args["error"] == "RuntimeError"
+    tg = tg_from(ins, args["types"])
+    with pytest.raises(RuntimeError):
+        join_vortex(True, tg, copy.deepcopy(args["join"]), 11, 21, [], "right-outer", None, None, "j")

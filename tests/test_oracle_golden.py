@@ -210,3 +210,27 @@ def test_oracle_projection_dtypes_follow_torch():
     out = O.tqp_project(cols, args)
     assert out[13].dtype == np.int32 and out[14].dtype == np.int64 and out[15].dtype == np.float64
     np.testing.assert_array_equal(out[14], [10, 40])
+
+
+def test_late_materialisation_masks():
+    ins, outs, args = load("late_materialisation_masks")
+    cols = {k: v for k, v in ins.items() if isinstance(k, int)}
+    mixed = dict(args["mixed"], **{"mask map": {int(k): v for k, v in args["mixed"]["mask map"].items()}})
+    got = O.tqp_hash_aggregate(cols, mixed)
+    (k,), vals = _by_key([outs["mixed_1"]], *[outs[f"mixed_{c}"] for c in (611, 612, 613, 614)])
+    (gk,), gvals = _by_key([got[1]], *[got[c] for c in (611, 612, 613, 614)])
+    np.testing.assert_array_equal(gk, k)
+    for a, b in zip(gvals, vals):
+        assert_f64_close(a, b) if b.dtype == np.float64 else np.testing.assert_array_equal(a, b)
+    two = dict(args["two"], **{"mask map": {int(k): v for k, v in args["two"]["mask map"].items()}})
+    got = O.tqp_hash_aggregate(cols, two)
+    (k,), vals = _by_key([outs["two_1"]], outs["two_631"], outs["two_632"])
+    (gk,), gvals = _by_key([got[1]], got[631], got[632])
+    np.testing.assert_array_equal(gk, k)
+    for a, b in zip(gvals, vals):
+        assert_f64_close(a, b) if b.dtype == np.float64 else np.testing.assert_array_equal(a, b)
+    jcols = {int(k[1:]): v for k, v in ins.items() if isinstance(k, str) and k.startswith("j")}
+    j = dict(args["join"], **{"mask map": {int(k): v for k, v in args["join"]["mask map"].items()}})
+    res, _ = O.join_vortex(jcols, j, 11, 21, "inner")
+    for c in (11, 21, 23, 26):
+        np.testing.assert_array_equal(res[c].reshape(-1), outs[f"join_{c}"].reshape(-1))

@@ -340,11 +340,71 @@ def _pred_code(P, prefix: str, lits: str = "lp") -> Tuple[List[int], str]:
     return sorted(used), (st[0] if st else "true")
 
 
-def _expr_code(S, upto: int, colpfx: str) -> Tuple[List[int], List[str]]:
-    """Statements computing registers r0..r{upto-1} for row j; returns (columns used, lines)."""
-    lines, used = [], set()
+def _reg_uses(S) -> Dict[int, int]:
+    """How many expression operands and accumulators read each register."""
+    uses: Dict[int, int] = {}
+    for i in range(S.n_expr):
+        X = S.expr[i]
+        if X.op in (L.X_ADD, L.X_SUB, L.X_MUL, L.X_DIV, L.X_SELECT):
+            uses[X.a] = uses.get(X.a, 0) + 1
+            uses[X.b] = uses.get(X.b, 0) + 1
+        if X.op in (L.X_TOF64, L.X_YEAR):
+            uses[X.a] = uses.get(X.a, 0) + 1
+        if X.op == L.X_SELECT:
+            uses[X.col] = uses.get(X.col, 0) + 1
+    for a in range(S.n_accs):
+        if S.accs[a].kind != L.ACC_COUNT_ROWS:
+            uses[S.accs[a].reg] = uses.get(S.accs[a].reg, 0) + 1
+    return uses
+
+
+def _one_minus(S, r: int) -> Optional[int]:
+    """b when register r is the F64 (1.0 - r_b), else None."""
+    X = S.expr[r]
+    if X.op != L.X_SUB or X.type != L.F64:
+        return None
+    one = S.expr[X.a]
+    if one.op != L.X_CONST or one.type != L.F64 or one.cf != 1.0:
+        return None
+    return X.b
+
+
+def _contractions(S, upto: int) -> Dict[int, Tuple[int, int]]:
+    """F64 products x * (1.0 - y) whose (1.0 - y) is read by nothing else: {register: (x, y, the
+    (1.0 - y) register)}.
+    The group-by evaluates them as fma(-x, y, x), x - x*y rounded once, where the plain form
+    rounds (1 - y) and the product: within an ulp of the term, and one FP64 instruction fewer
+    per row on the FP64-bound accumulation (the sums are compared at 1e-12 relative).  Per-row
+    results (projections, join values) keep the plain form."""
+    uses = _reg_uses(S)
+    into_acc = {S.accs[a].reg for a in _fusable_products(S)}   # those become fma(x, t, acc) instead
+    out = {}
     for i in range(upto):
         X = S.expr[i]
+        if X.op != L.X_MUL or X.type != L.F64 or i in into_acc:
+            continue
+        for x, t in ((X.a, X.b), (X.b, X.a)):
+            y = _one_minus(S, t)
+            if y is not None and uses.get(t, 0) == 1 and t < i and x < i:
+                out[i] = (x, y, t)
+                break
+    return out
+
+
+def _expr_code(S, upto: int, colpfx: str, contract: bool = False) -> Tuple[List[int], List[str]]:
+    """Statements computing registers r0..r{upto-1} for row j; returns (columns used, lines).
+    contract: products x * (1 - y) as one fused multiply-add (see _contractions)."""
+    lines, used = [], set()
+    fused = _contractions(S, upto) if contract else {}
+    skip = {t for (_, _, t) in fused.values()}
+    for i in range(upto):
+        X = S.expr[i]
+        if i in skip:
+            continue                  # (1 - y), folded into the fused multiply-add that reads it
+        if i in fused:
+            x, y, _ = fused[i]
+            lines.append(f"const double r{i} = __fma_rn(-r{x}, r{y}, r{x});")
+            continue
         f = X.type == L.F64
         t = "double" if f else "i64"
         if X.op == L.X_COL:
@@ -422,19 +482,7 @@ def _fusable_products(S) -> Dict[int, Tuple[int, int]]:
     (x, y)}.  Accumulating it as fma(x, y, acc) rounds once where the product + add round
     twice (0.5 ulp of the term; the sums are compared at 1e-12 relative), and saves one
     FP64 instruction per row on the FP64-bound group-by."""
-    uses: Dict[int, int] = {}
-    for i in range(S.n_expr):
-        X = S.expr[i]
-        if X.op in (L.X_ADD, L.X_SUB, L.X_MUL, L.X_DIV, L.X_SELECT):
-            uses[X.a] = uses.get(X.a, 0) + 1
-            uses[X.b] = uses.get(X.b, 0) + 1
-        if X.op in (L.X_TOF64, L.X_YEAR):
-            uses[X.a] = uses.get(X.a, 0) + 1
-        if X.op == L.X_SELECT:
-            uses[X.col] = uses.get(X.col, 0) + 1
-    for a in range(S.n_accs):
-        if S.accs[a].kind != L.ACC_COUNT_ROWS:
-            uses[S.accs[a].reg] = uses.get(S.accs[a].reg, 0) + 1
+    uses = _reg_uses(S)
     out = {}
     for a in range(S.n_accs):
         acc = S.accs[a]
@@ -460,7 +508,7 @@ def groupby_source(spec, pred, plan) -> Tuple[str, str, int, int]:
     T = int(plan.threads) if private else 256
     smem = K * A * 8 * T if private else (K * A * 8 if shared else 0)
     pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
-    ecols, elines = _expr_code(S, S.n_expr, "c")
+    ecols, elines = _expr_code(S, S.n_expr, "c", contract=True)
     kcols = list(range(S.n_keys))
     name = "tqpk_q_groupby"
     src = [PRELUDE, f'extern "C" __global__ void __launch_bounds__({T}) {name}(']

@@ -166,7 +166,7 @@ def _gb_functions(p: int, spec, pred) -> str:
     A = S.n_accs
     pcols, pexpr = jit._pred_code(pred, "p") if pred is not None else ([], "true")
     lit_decls, pexpr = _hoist(pexpr, "I")
-    ecols, elines = jit._expr_code(S, S.n_expr, "c")
+    ecols, elines = jit._expr_code(S, S.n_expr, "c", contract=True)   # sums only: x * (1 - y) as one FMA
     kcols = list(range(S.n_keys))
     src = [f"__device__ void gb_agg_{p}(const QInst& I, i64 b, i64 e, u64* sm) {{",
            f"  constexpr int A = {A};",

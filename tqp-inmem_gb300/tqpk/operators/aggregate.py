@@ -19,6 +19,7 @@ import torch
 
 from ..expr import compile_aggregate, needs_key_codes
 from ..ops import check_deferred, encode_keys, gather, groupby
+from ._materialize import materialize
 from ..variable import make_like, torch_to_type, wait_ready
 from .filter import _require_gpu
 
@@ -37,11 +38,18 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
                     transfer_set.append(v)
     mask_ids = set(agg_mask_map.values())
     data_ids = [c for c in transfer_set if c not in mask_ids]
-    if len(mask_ids) > 1:
-        raise NotImplementedError(f"aggregate inputs carry different masks {mask_ids}")
-    if mask_ids and any(c not in agg_mask_map for c in data_ids):
-        raise NotImplementedError("aggregate mixes masked and unmasked input columns")
-    mask = tensor_group[next(iter(mask_ids))].tensor if mask_ids else None
+    tg = tensor_group                                   # the columns read (outputs go to tensor_group)
+    if len(mask_ids) > 1 or (mask_ids and any(c not in agg_mask_map for c in data_ids)):
+        # columns under different masks, or masked beside already compacted ones: each masked
+        # column is compacted by its own mask first, as the reference's pipeline does for every
+        # input (vortex_pipeline.py:54-58), and the aggregate runs on the compacted columns
+        tg = dict(tensor_group)
+        tg.update(materialize(tensor_group, data_ids, agg_mask_map))
+        lengths = {tg[c].tensor.shape[0] for c in data_ids}
+        if len(lengths) > 1:
+            raise RuntimeError(f"aggregate inputs have different lengths after their masks: {sorted(lengths)}")
+        mask_ids, agg_mask_map = set(), {}
+    mask = tg[next(iter(mask_ids))].tensor if mask_ids else None
 
     key_ids, key_ids_new, key_types_name = [], [], []
     for tree in args["results"]:                        # aggregate.py:265-275
@@ -51,25 +59,25 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
         if isinstance(t, str) or (len(t) == 3 and t[1] == "AS" and isinstance(t[0], str)):
             kid = int((t if isinstance(t, str) else t[0]).split("#")[-1].replace("L", ""))
             key_ids.append(kid)
-            key_types_name.append(tensor_group[kid].tensor_type)
+            key_types_name.append(tg[kid].tensor_type)
     agg_ids = args["out agg ids"]
 
-    cols = {c: tensor_group[c].tensor for c in data_ids}
+    cols = {c: tg[c].tensor for c in data_ids}
     key_set = {int(k.split("#")[-1].replace("L", "")) for k in (args.get("keys") or [])}
-    wait_ready(*[tensor_group[c] for c in transfer_set if c in key_set or c in mask_ids])   # the plan's inputs
+    wait_ready(*[tg[c] for c in transfer_set if c in key_set or c in mask_ids])   # the plan's inputs
 
     def values_ready():
-        wait_ready(*[tensor_group[c] for c in transfer_set if c not in key_set and c not in mask_ids])
+        wait_ready(*[tg[c] for c in transfer_set if c not in key_set and c not in mask_ids])
 
     def _pending(v):
         ev = getattr(v, "ready", None)
         return ev is not None and not ev.query()
     # value columns still in flight (a host copy or a late gather): count the groups from the keys
-    values_late = any(_pending(tensor_group[c]) for c in transfer_set if c not in key_set and c not in mask_ids)
-    proto = tensor_group[data_ids[0]] if data_ids else None
+    values_late = any(_pending(tg[c]) for c in transfer_set if c not in key_set and c not in mask_ids)
+    proto = tg[data_ids[0]] if data_ids else None
     n = next(iter(cols.values())).shape[0] if cols else 0
     device = next(iter(cols.values())).device if cols else torch.device("cuda")
-    if all(tensor_group[c].tensor.numel() == 0 for c in transfer_set):
+    if all(tg[c].tensor.numel() == 0 for c in transfer_set):
         # vortex_pipeline.py:51-52: empty inputs give empty (float32) outputs
         keys_out = {k: torch.tensor([], device=device) for k in range(len(key_ids))}
         vals_out = {a: torch.tensor([], device=device) for a in agg_ids}
@@ -87,7 +95,7 @@ def tqp_hash_aggregate(gpu_enable, tensor_group, args, gpu_mem_pool, cpu_mem_poo
             keys_out[i] = k if k.dim() == 2 else k.reshape(G, 1)     # unique_key_cols[:, pos_l:pos_r]
     else:
         prog = compile_aggregate(args, cols, derived=True)
-        ranges = [getattr(tensor_group[kid], "_key_range", None) for kid in prog.key_ids]
+        ranges = [getattr(tg[kid], "_key_range", None) for kid in prog.key_ids]
         keys, vals_out, G, _ = groupby(prog, n, device, mask=mask, before_values=values_ready,
                                        key_ranges=ranges if ranges and all(r is not None for r in ranges) else None,
                                        values_late=values_late)

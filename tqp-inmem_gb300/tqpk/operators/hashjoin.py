@@ -28,6 +28,7 @@ from .. import _lib as L
 from ..ops import check_deferred, compact, filter_mask, gather, join_build, join_probe, mark_rows
 from ..predicate import compile_filter
 from ..variable import make_like, wait_ready
+from ._materialize import materialize
 from .filter import _require_gpu
 
 LEFT, RIGHT = 0, 1
@@ -41,13 +42,14 @@ def _normalize(v):
 
 
 def _side_mask(tensor_group, cols: List[int], mask_map: Dict[int, int], key: int):
-    """The one mask shared by a side's columns (None when the side is unfiltered)."""
+    """The one mask shared by a side's columns (None when the side is unfiltered), or the string
+    "mixed" when its columns carry different masks or some carry none."""
     masks = {mask_map.get(c) for c in cols}
-    if len(masks) > 1:
-        raise NotImplementedError(f"columns of one join side carry different masks {masks}")
-    m = masks.pop() if masks else None
     if key not in cols:
-        m = mask_map.get(key, m)
+        masks.add(mask_map.get(key))
+    if len(masks) > 1:
+        return "mixed"
+    m = masks.pop() if masks else None
     return tensor_group[m].tensor if m is not None else None
 
 
@@ -219,6 +221,17 @@ def join_vortex(gpu_enable, tensor_group, args, leftcol, rightcol, condition_lis
              for s in (LEFT, RIGHT)]
     tl = {k: tensor_group[k] for k in groupings[LEFT] if k in tensor_group}
     tr = {k: tensor_group[k] for k in groupings[RIGHT] if k in tensor_group}
+    for s, t in ((LEFT, tl), (RIGHT, tr)):
+        if isinstance(masks[s], str):
+            # a side whose columns carry different masks (or masked beside compacted ones): each
+            # masked column is compacted by its own mask first (vortex_pipeline.py:54-58) and the
+            # side joins unmasked
+            cols = set(side_cols[s]) | {join_key_index[s]}
+            t.update(materialize(tensor_group, cols, join_mask_map))
+            lengths = {t[c].tensor.shape[0] for c in cols}
+            if len(lengths) > 1:
+                raise RuntimeError(f"join inputs have different lengths after their masks: {sorted(lengths)}")
+            masks[s] = None
     if leftcol not in tl or rightcol not in tr:
         raise KeyError("join key is not in its side's group")
     bi, pi, nb_rows, key_range = _pairs(tl, tr, leftcol, rightcol, condition_list, type, masks[LEFT],

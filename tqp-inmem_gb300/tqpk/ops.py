@@ -458,7 +458,10 @@ def gather(cols: Sequence[torch.Tensor], idx: torch.Tensor, null_aware: bool = F
     lib = L.load()
     if any(c.dim() == 2 and c.shape[1] != 1 for c in cols):
         if null_aware:
-            raise NotImplementedError("null-filled rows of a 2-D column (right-outer join payload)")
+            # the reference's index_with_null masks [M, w] rows with an [M] mask, which does not
+            # broadcast: its right-outer join raises RuntimeError here too (conversion.py:52-57)
+            raise RuntimeError("null-filled rows of a 2-D column (right-outer join payload): the [M] null "
+                               "mask does not broadcast over [M, w] rows")
         out = [None] * len(cols)
         flat = [(i, c) for i, c in enumerate(cols) if not (c.dim() == 2 and c.shape[1] != 1)]
         for i, c in enumerate(cols):

@@ -87,7 +87,16 @@ __device__ __forceinline__ void set_error(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
 
-__device__ __forceinline__ uint64_t d2u(double d) { return static_cast<uint64_t>(__double_as_longlong(d)); }
+// The bits of a double through an opaque move: integer tests on those bits (the sign, -0.0, the
+// NaN exponent) stay integer instructions.  Through a plain reinterpretation the compiler may fold
+// such tests back into FP64 compares, and FP64 runs at 1/64 of the FP32 rate on this part
+// (measured: 2 FP64-pipe instructions per item in a top-k key transform, 7.2 against 2.8 us
+// per CTA).
+__device__ __forceinline__ uint64_t d2u(double d) {
+  uint64_t u;
+  asm("mov.b64 %0, %1;" : "=l"(u) : "d"(d));
+  return u;
+}
 __device__ __forceinline__ double u2d(uint64_t u) { return __longlong_as_double(static_cast<long long>(u)); }
 
 // Order-preserving map of a double onto uint64 (for min/max atomics and the
@@ -101,6 +110,16 @@ __device__ __forceinline__ double f64_from_ordered(uint64_t o) {
   return u2d(u);
 }
 
+// The bits of a float64 with -0.0 folded onto +0.0 and every NaN onto one quiet NaN, in integer
+// instructions only: on this part FP64 compares run at 1/64 of the FP32 rate, which made
+// comparisons the cost of passes that only rank or hash doubles.
+__device__ __forceinline__ uint64_t f64_canon_bits(uint64_t b) {
+  if ((b << 1) == 0) return 0;                                            // +-0.0
+  if ((b & 0x7ff0000000000000ull) == 0x7ff0000000000000ull && (b & 0x000fffffffffffffull))
+    return 0x7ff8000000000000ull;                                         // NaN
+  return b;
+}
+
 // Order-preserving uint64 image of a key of any dtype for sorting: signed ints
 // flip the sign bit; float64 flips sign-magnitude with -0.0 -> +0.0 and every
 // NaN mapped to the largest value (torch.sort's order); descending = bitwise
@@ -108,10 +127,7 @@ __device__ __forceinline__ double f64_from_ordered(uint64_t o) {
 __device__ __forceinline__ uint64_t sort_key_bits(uint64_t raw, int is_f64, int desc) {
   uint64_t u;
   if (is_f64) {
-    double d = __longlong_as_double(static_cast<long long>(raw));
-    if (d == 0.0) d = 0.0;
-    uint64_t b = static_cast<uint64_t>(__double_as_longlong(d));
-    if (d != d) b = 0x7ff8000000000000ull;
+    const uint64_t b = f64_canon_bits(raw);
     u = (b & (1ull << 63)) ? ~b : (b | (1ull << 63));
   } else {
     u = raw ^ (1ull << 63);
@@ -136,7 +152,7 @@ __device__ __forceinline__ double ld_f64(const void* p, int dt, int64_t i) {
   return static_cast<double>(ld_int(p, dt, i));
 }
 __device__ __forceinline__ uint64_t sort_key(const void* keys, int dt, int64_t i, int desc) {
-  const uint64_t raw = dt == TQPK_F64 ? static_cast<uint64_t>(__double_as_longlong(static_cast<const double*>(keys)[i]))
+  const uint64_t raw = dt == TQPK_F64 ? d2u(static_cast<const double*>(keys)[i])
                                       : static_cast<uint64_t>(ld_int(keys, dt, i));
   return sort_key_bits(raw, dt == TQPK_F64, desc);
 }

@@ -49,9 +49,8 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
 // -0.0 folded onto +0.0 (torch.unique sees them equal).
 __device__ __forceinline__ uint64_t key_bits(const void* p, int dt, int64_t row) {
   if (dt == TQPK_F64) {
-    double d = static_cast<const double*>(p)[row];
-    if (d == 0.0) d = 0.0;
-    return static_cast<uint64_t>(__double_as_longlong(d));
+    const uint64_t b = static_cast<const uint64_t*>(p)[row];
+    return (b << 1) == 0 ? 0 : b;                     // -0.0 as +0.0, in integer instructions
   }
   return static_cast<uint64_t>(ld_int(p, dt, row));
 }

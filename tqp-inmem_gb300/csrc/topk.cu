@@ -21,10 +21,7 @@ static int launch_r(const Src& src, int k, int grid, TopkOut O, cudaStream_t s) 
   const int ng = (int)std::max<int64_t>(1, (src.n + G - 1) / G);
   k_tk_group_best<Src><<<ng, 256, 0, s>>>(src, G, k, O);
   TQPK_CHECK_LAUNCH();
-  // the filter CTAs hold tk_final's 32 KB sort buffer: 4 per SM keeps them in one wave
-  const int64_t units = (src.n + 1023) / 1024;
-  k_tk_filter<R, Src><<<(int)std::max<int64_t>(1, std::min<int64_t>(units, (int64_t)num_sms() * 4)), 256, 0, s>>>(
-      src, k, O);
+  k_tk_filter<R, Src><<<ng, 256, 0, s>>>(src, G, k, O);     // the same groups
   TQPK_CHECK_LAUNCH();
   return TQPK_OK;
 }

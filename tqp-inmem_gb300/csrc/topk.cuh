@@ -98,9 +98,7 @@ struct DenseSumSource {
                                     // build writes its passing keys' bits and initialises those sums)
   static constexpr uint64_t kEmptySum = 0x8000000000000000ull;
   __device__ __forceinline__ uint64_t order_key(double v) const {
-    if (v == 0.0) v = 0.0;
-    uint64_t b = d2u(v);
-    if (isnan(v)) b = 0x7ff8000000000000ull;
+    const uint64_t b = f64_canon_bits(d2u(v));       // integer instructions only (no FP64 compares)
     const uint64_t u = (b & (1ull << 63)) ? ~b : (b | (1ull << 63));
     return desc ? ~u : u;
   }
@@ -255,7 +253,7 @@ __device__ __forceinline__ bool tk_last_cta(unsigned* arrive) {
   return last;
 }
 
-// The cut: the k-th best of the ng group bests (bitonic sort of the bests in one CTA).
+// The cut for k > 32: the k-th best of the ng group bests (bitonic sort of the bests in one CTA).
 __device__ __forceinline__ void tk_cut(int ng, int k, TopkOut O) {
   __shared__ uint64_t v[kTopkGroups];
   for (int i = threadIdx.x; i < kTopkGroups; i += blockDim.x) v[i] = i < ng ? __ldcg(&O.cand_key[kTopkCap + i]) : ~0ull;
@@ -273,6 +271,37 @@ __device__ __forceinline__ void tk_cut(int ng, int k, TopkOut O) {
   if (threadIdx.x == 0) *O.bound = v[(k <= kTopkGroups ? k : kTopkGroups) - 1];
 }
 
+// One CTA's walk over items [b0, b1) in quads (4 items per thread, 256 threads): kTopkQuads
+// quads per thread are loaded before any is looked at, so a thread keeps that many loads in
+// flight (the passes are latency-bound on tables resident in L2).  f(key, index, lane_has_item)
+// runs for every item slot in warp-uniform order (lanes without an item pass false), so f may use
+// warp collectives; valid / nbits count the items and the membership bits seen.
+constexpr int kTopkQuads = 4;
+template <class Src, class F>
+__device__ __forceinline__ void tk_scan_group(const Src& src, int64_t b0, int64_t b1, bool count_bits, F f,
+                                              unsigned& valid, unsigned& nbits) {
+  for (int64_t c0 = b0 + threadIdx.x * 4; c0 - threadIdx.x * 4 < b1; c0 += 4 * 256 * kTopkQuads) {
+    uint64_t key[kTopkQuads][4];
+    unsigned ok[kTopkQuads];
+#pragma unroll
+    for (int u = 0; u < kTopkQuads; ++u) {
+      const int64_t i0 = c0 + u * 1024;
+      ok[u] = 0;
+      if (i0 < b1) {
+        const unsigned tail = i0 + 4 <= b1 ? 0xfu : (1u << (b1 - i0)) - 1u;
+        ok[u] = src.get4(i0, key[u]) & tail;
+        if (count_bits) nbits += __popc(src.bits4(i0) & tail);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kTopkQuads; ++u) {
+      valid += __popc(ok[u]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) f(key[u][q], c0 + u * 1024 + q, ((ok[u] >> q) & 1u) != 0);
+    }
+  }
+}
+
 // Pass 1: each CTA keeps the best key of its group of G items; the last CTA to finish
 // computes the cut from all groups' bests.
 template <class Src>
@@ -284,16 +313,9 @@ __global__ void __launch_bounds__(256) k_tk_group_best(Src src, int64_t G, int k
   __syncthreads();
   uint64_t best = ~0ull;
   unsigned valid = 0, nbits = 0;
-  for (int64_t i0 = b0 + threadIdx.x * 4; i0 < b1; i0 += 4 * (int64_t)blockDim.x) {
-    uint64_t key[4];
-    const unsigned tail = i0 + 4 <= b1 ? 0xfu : (1u << (b1 - i0)) - 1u;
-    const unsigned ok = src.get4(i0, key) & tail;
-    if (O.bits_set) nbits += __popc(src.bits4(i0) & tail);
-    valid += __popc(ok);
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if ((ok >> q) & 1u) best = key[q] < best ? key[q] : best;
-  }
+  tk_scan_group(src, b0, b1, O.bits_set != nullptr, [&](uint64_t key, int64_t, bool has) {
+    if (has && key < best) best = key;          // slots without an item carry no key
+  }, valid, nbits);
   // one atomic per CTA for each count: per-warp atomics on one address serialise in the L2
   valid = __reduce_add_sync(0xffffffffu, valid);
   nbits = __reduce_add_sync(0xffffffffu, nbits);
@@ -308,7 +330,49 @@ __global__ void __launch_bounds__(256) k_tk_group_best(Src src, int64_t G, int k
     if (s_valid && O.valid_total) atomicAdd(O.valid_total, (unsigned long long)s_valid);
     if (s_bits && O.bits_set) atomicAdd(O.bits_set, (unsigned long long)s_bits);
   }
+  if (k <= 32) return;              // the filter pass derives its cut from the group bests itself
   if (tk_last_cta(O.arrive)) tk_cut((int)gridDim.x, k, O);
+}
+
+// The cut for k <= 32, computed by every CTA of the filter pass from the ng group bests (no
+// serial step between the passes): the groups that hold an item are dealt round-robin into k
+// bins and the cut is the largest of the bins' smallest keys.  Each bin's smallest key belongs to
+// an item of its own group, so at least k items lie at or under the cut, and the top k are among
+// them; for independent keys about k ln k items pass.  Fewer than k non-empty groups: ~0 (every
+// item passes).  Called by all threads.
+__device__ __forceinline__ uint64_t tk_bin_cut(int ng, int k, const TopkOut& O) {
+  __shared__ unsigned long long bin[32];
+  __shared__ unsigned s_ne;
+  __shared__ unsigned long long s_cut;
+  if (threadIdx.x < 32) bin[threadIdx.x] = ~0ull;
+  if (threadIdx.x == 0) { s_ne = 0; s_cut = 0; }
+  __syncthreads();
+  // the rank of a non-empty group among the non-empty ones decides its bin: groups are read in
+  // index order in chunks of 256, each chunk's non-empty ones numbered by a block scan
+  __shared__ int wsum[8];
+  for (int base = 0; base < ng; base += 256) {
+    const int g = base + threadIdx.x;
+    const uint64_t v = g < ng ? __ldcg(&O.cand_key[kTopkCap + g]) : ~0ull;
+    const bool ne = v != ~0ull;
+    const unsigned m = __ballot_sync(0xffffffffu, ne);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wsum[warp] = __popc(m);
+    __syncthreads();
+    int before = s_ne;
+    for (int w = 0; w < warp; ++w) before += wsum[w];
+    if (ne) atomicMin(&bin[(before + __popc(m & ((1u << lane) - 1u))) % k], (unsigned long long)v);
+    __syncthreads();
+    if (threadIdx.x == 0) for (int w = 0; w < 8; ++w) s_ne += wsum[w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 32) {
+    unsigned long long c = threadIdx.x < k ? bin[threadIdx.x] : 0ull;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) { const unsigned long long w = __shfl_xor_sync(0xffffffffu, c, o); c = w > c ? w : c; }
+    if (threadIdx.x == 0) s_cut = s_ne >= (unsigned)k ? c : ~0ull;
+  }
+  __syncthreads();
+  return s_cut;
 }
 
 constexpr int kTopkSortCap = 2048;   // candidates the final CTA sorts in shared memory
@@ -344,6 +408,31 @@ __device__ __forceinline__ void tk_final(const Src& src, int k, TopkOut O) {
   __shared__ uint64_t sk[kTopkSortCap];
   __shared__ int64_t si[kTopkSortCap];
   const unsigned cnt = __ldcg(O.ticket);
+  if (cnt <= 256u) {
+    // few candidates: each thread ranks one against all of them (one pass over shared memory,
+    // two barriers) and writes it at its rank when that is among the first k
+    if (threadIdx.x < cnt) {
+      sk[threadIdx.x] = __ldcg(&O.cand_key[threadIdx.x]);
+      si[threadIdx.x] = __ldcg(&O.cand_idx[threadIdx.x]);
+    }
+    __syncthreads();
+    int rank = 0;
+    uint64_t mk = 0;
+    int64_t mi = 0;
+    if (threadIdx.x < cnt) {
+      mk = sk[threadIdx.x];
+      mi = si[threadIdx.x];
+      for (int j = 0; j < (int)cnt; ++j) rank += tk_better(sk[j], si[j], mk, mi) ? 1 : 0;
+    }
+    __syncthreads();
+    if (threadIdx.x < cnt && rank < k) {
+      O.out_idx[rank] = mi;
+      si[rank] = mi;
+    }
+    __syncthreads();
+    tk_finish((int)cnt < k ? (int)cnt : k, O, si);
+    return;
+  }
   if (cnt <= (unsigned)kTopkSortCap) {
     int P = 2;
     while (P < (int)cnt) P <<= 1;
@@ -410,30 +499,26 @@ __device__ __forceinline__ void tk_final(const Src& src, int k, TopkOut O) {
 }
 
 // Pass 2: the items at or under the cut are appended to the candidate list; the last CTA
-// to finish sorts them (tk_final).  Blocks of 256 threads (tk_final's 8 warps).
+// to finish sorts them (tk_final).  Same groups of G items as pass 1, 256 threads per CTA
+// (tk_final's 8 warps).
 template <int R, class Src>
-__global__ void __launch_bounds__(256) k_tk_filter(Src src, int k, TopkOut O) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint64_t cut = __ldcg(O.bound);
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
-  for (int64_t base = (blockIdx.x * (int64_t)blockDim.x + warp * 32) * 4; base < src.n; base += stride) {
-    const int64_t i0 = base + lane * 4;
-    uint64_t key[4];
-    const unsigned ok = src.get4(i0, key);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const bool pass = ((ok >> q) & 1u) && key[q] <= cut;
-      const unsigned bal = __ballot_sync(0xffffffffu, pass);
-      if (!bal) continue;
-      unsigned at = 0;
-      if (lane == 0) at = atomicAdd(O.ticket, (unsigned)__popc(bal));
-      at = __shfl_sync(0xffffffffu, at, 0) + __popc(bal & ((1u << lane) - 1u));
-      if (pass && at < (unsigned)kTopkCap) {
-        O.cand_key[at] = key[q];
-        O.cand_idx[at] = i0 + q;
-      }
+__global__ void __launch_bounds__(256) k_tk_filter(Src src, int64_t G, int k, TopkOut O) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t cut = k <= 32 ? tk_bin_cut((int)gridDim.x, k, O) : __ldcg(O.bound);
+  const int64_t b0 = (int64_t)blockIdx.x * G, b1 = b0 + G < src.n ? b0 + G : src.n;
+  unsigned valid = 0, nbits = 0;
+  tk_scan_group(src, b0, b1, false, [&](uint64_t key, int64_t idx, bool has) {
+    const bool pass = has && key <= cut;
+    const unsigned bal = __ballot_sync(0xffffffffu, pass);
+    if (!bal) return;
+    unsigned at = 0;
+    if (lane == 0) at = atomicAdd(O.ticket, (unsigned)__popc(bal));
+    at = __shfl_sync(0xffffffffu, at, 0) + __popc(bal & ((1u << lane) - 1u));
+    if (pass && at < (unsigned)kTopkCap) {
+      O.cand_key[at] = key;
+      O.cand_idx[at] = idx;
     }
-  }
+  }, valid, nbits);
   if (tk_last_cta(O.arrive + 1)) tk_final<R>(src, k, O);
 }
 

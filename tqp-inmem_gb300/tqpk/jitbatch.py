@@ -97,10 +97,11 @@ __device__ __forceinline__ unsigned long long gtimer() {
   unsigned long long t; asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t)); return t;
 }
 __device__ __forceinline__ double from_ord(u64 u) { return u2d((u >> 63) ? (u & ~(1ull << 63)) : ~u); }
-__device__ __forceinline__ u64 sum_key(double v, int desc) {
-  if (v == 0.0) v = 0.0;
+__device__ __forceinline__ u64 sum_key(double v, int desc) {   // integer instructions only
   u64 b = d2u(v);
-  if (isnan(v)) b = 0x7ff8000000000000ull;
+  if ((b << 1) == 0) b = 0;                                         // -0.0 ranks as +0.0
+  else if ((b & 0x7ff0000000000000ull) == 0x7ff0000000000000ull && (b & 0x000fffffffffffffull))
+    b = 0x7ff8000000000000ull;                                      // every NaN as one
   const u64 u = (b >> 63) ? ~b : (b | (1ull << 63));
   return desc ? ~u : u;
 }

@@ -357,32 +357,49 @@ __global__ void __launch_bounds__(kBlock) k_emit_dense(const __grid_constant__ t
     uint64_t e = lookback_warp(status, tile, (uint64_t)total, err);
     if (threadIdx.x == 0) s_excl = e;
   }
+  // The tile's groups in output order (entry r: the slot offset in the tile; its output row is
+  // s_excl + r), then every (group, column) pair on its own thread.  A group's outputs (an average is an FP64
+  // division, a key a division of the slot index) are independent, and on this part FP64 runs at
+  // 1/64 rate: one thread per group made a few groups a long serial chain (6 groups, 8 outputs:
+  // 25 us for one CTA).
+  __shared__ uint16_t e_off[kTile];
+  {
+    int r = excl;
+    uint32_t b = bits;
+    while (b) {
+      const int j = __ffs(b) - 1;
+      b &= b - 1;
+      e_off[r++] = (uint16_t)(threadIdx.x * kItems + j);
+    }
+  }
   __syncthreads();
-  int64_t pos = (int64_t)s_excl + excl;
-  while (bits) {
-    const int j = __ffs(bits) - 1;
-    bits &= bits - 1;
-    const int64_t s = s0 + j;
-    for (int k = 0; k < G.nk; ++k) {
-      const int64_t key = G.kmin[k] + (s / G.kstride[k]) % G.krange[k];
-      store_as(E.key[k], E.key_dt[k], pos, (uint64_t)key, false);
+  const int per = G.nk + E.n;                       // columns written per group
+  const bool small = K < (int64_t(1) << 31);       // slot indices fit 32 bits: 32-bit key decoding
+  for (int w = threadIdx.x; w < total * per; w += kBlock) {
+    const int r = w / per, c = w - r * per;
+    const int64_t s = tile * kTile + e_off[r];
+    const int64_t pos = (int64_t)s_excl + r;
+    if (c < G.nk) {
+      const int k = c;
+      const int64_t q = small ? (int64_t)(((uint32_t)s / (uint32_t)G.kstride[k]) % (uint32_t)G.krange[k])
+                              : (s / G.kstride[k]) % G.krange[k];
+      store_as(E.key[k], E.key_dt[k], pos, (uint64_t)(G.kmin[k] + q), false);
+      continue;
     }
-    for (int o = 0; o < E.n; ++o) {
-      const tqpk_acc& a = S.accs[E.a[o]];
-      uint64_t v = gacc[(int64_t)E.a[o] * K + s];
-      bool f = a.type == TQPK_F64 && a.kind != TQPK_ACC_COUNT_ROWS && a.kind != TQPK_ACC_COUNT_NOTNULL;
-      if (f && (a.kind == TQPK_ACC_MIN || a.kind == TQPK_ACC_MAX)) v = d2u(f64_from_ordered(v));
-      if (E.op[o] == TQPK_OUT_AVG) {
-        const double num = f ? u2d(v) : (double)(int64_t)v;
-        const double den = (double)(int64_t)gacc[(int64_t)E.b[o] * K + s];
-        v = d2u(__ddiv_rn(num, den));
-        f = true;
-      } else if (a.kind == TQPK_ACC_COUNT_ROWS || a.kind == TQPK_ACC_COUNT_NOTNULL) {
-        f = false;
-      }
-      store_as(E.col[o], E.dt[o], pos, v, f);
+    const int o = c - G.nk;
+    const tqpk_acc& a = S.accs[E.a[o]];
+    uint64_t v = gacc[(int64_t)E.a[o] * K + s];
+    bool f = a.type == TQPK_F64 && a.kind != TQPK_ACC_COUNT_ROWS && a.kind != TQPK_ACC_COUNT_NOTNULL;
+    if (f && (a.kind == TQPK_ACC_MIN || a.kind == TQPK_ACC_MAX)) v = d2u(f64_from_ordered(v));
+    if (E.op[o] == TQPK_OUT_AVG) {
+      const double num = f ? u2d(v) : (double)(int64_t)v;
+      const double den = (double)(int64_t)gacc[(int64_t)E.b[o] * K + s];
+      v = d2u(__ddiv_rn(num, den));
+      f = true;
+    } else if (a.kind == TQPK_ACC_COUNT_ROWS || a.kind == TQPK_ACC_COUNT_NOTNULL) {
+      f = false;
     }
-    ++pos;
+    store_as(E.col[o], E.dt[o], pos, v, f);
   }
 }
 

@@ -46,16 +46,24 @@ PEAK_FALLBACK_GBS = 6800.0
 
 
 # ---------------------------------------------------------------------------- workloads
+_PINNED = {}
+
+
 def d2h_all(tensors):
-    """Results to pinned host memory: every copy queued, then one synchronisation."""
+    """Results to pinned host memory: every copy queued, then one synchronisation.  The pinned
+    buffers are kept per (column, dtype) and grown as needed (pinning memory costs tens of us a
+    call); the returned arrays are copies."""
     import torch
     out = {}
     for c, t in tensors.items():
-        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        buf = _PINNED.get((c, t.dtype))
+        if buf is None or buf.numel() < t.numel():
+            buf = _PINNED[(c, t.dtype)] = torch.empty(max(t.numel(), 1024), dtype=t.dtype, pin_memory=True)
+        h = buf[:t.numel()].view(t.shape)
         h.copy_(t, non_blocking=True)
         out[c] = h
     torch.cuda.current_stream().synchronize()
-    return out
+    return {c: h.clone() for c, h in out.items()}
 
 
 def plan_args(args):

@@ -186,10 +186,10 @@ def _run_join_agg_topk(tensor_group, m) -> bool:
     wait_ready(*build_vars)
     pipe.run(before_probe=lambda: wait_ready(*probe_vars))
     try:
-        keys, vals, count = pipe.result_device()
+        keys, vals, count = pipe.result_device(key_dtype=bv.tensor.dtype)   # cast queued before the read
     except NotImplementedError:                      # a repeated build key: the operator path runs instead
         return False
-    tensor_group[m["key_out"]] = make_like(bv, keys.to(bv.tensor.dtype).reshape(count, 1), bv.tensor_type)
+    tensor_group[m["key_out"]] = make_like(bv, keys.reshape(count, 1), bv.tensor_type)
     tensor_group[m["agg_out"]] = make_like(bv, vals, "float")
     return True
 

@@ -153,15 +153,19 @@ class JoinAggTopK:
             self._stages(7, s)
             self._sentinel = False
 
-    def result_device(self):
-        """(keys int64[m], sums float64[m], m) as device tensors after the last run, with one host
-        read (the count and the error word together).  A repeated build key raises
-        NotImplementedError (TQPK_EUNSUPPORTED), an out-of-domain one ValueError."""
+    def result_device(self, key_dtype=None):
+        """(keys [m], sums float64[m], m) as device tensors after the last run, with one host
+        read (the count and the error word together); keys as int64, or cast on the device to
+        key_dtype before that read.  A repeated build key raises NotImplementedError
+        (TQPK_EUNSUPPORTED), an out-of-domain one ValueError."""
         import ctypes
         d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
         if getattr(self, "_probe_smem", 0):
             self.check_error()                      # the TMA-staged probe keeps its own error word
-        hdr = torch.empty(16, dtype=torch.int32, pin_memory=True)
+        keys = self.out_keys if key_dtype in (None, torch.int64) else self.out_keys.to(key_dtype)
+        if not hasattr(self, "_hdr_host"):
+            self._hdr_host = torch.empty(16, dtype=torch.int32, pin_memory=True)
+        hdr = self._hdr_host
         cur = torch.cuda.current_stream(self.dev)
         hdr[:4].copy_(self.ws[:16].view(torch.int32), non_blocking=True)       # hdr[2] = error word
         hdr[4:6].copy_(self.out_count.view(torch.int32), non_blocking=True)
@@ -169,7 +173,7 @@ class JoinAggTopK:
         err, m = int(hdr[2]), int(hdr[4:6].view(torch.int64)[0])
         if err:
             L.check(err, "fused join pipeline (repeated or out-of-domain build key)")
-        return self.out_keys[:m], self.out_vals[:m], m
+        return keys[:m], self.out_vals[:m], m
 
 
     def capture(self):

@@ -231,7 +231,7 @@ __device__ void gb_agg_item(const BatchInst& I, int64_t b, int64_t e, uint64_t* 
         } else if (shared) {
           b_merge_atomic(&sm[slot[j] * A + a], ac, b_acc_value(ac, x));
         } else {
-          b_merge_atomic(&I.gacc[(int64_t)a * K + slot[j]], ac, b_acc_value(ac, x));
+          acc_merge_global(&I.gacc[(int64_t)a * K + slot[j]], ac, b_acc_value(ac, x));
         }
       }
     }
@@ -241,7 +241,7 @@ __device__ void gb_agg_item(const BatchInst& I, int64_t b, int64_t e, uint64_t* 
     for (int64_t c = threadIdx.x; c < K * A; c += T) {
       const tqpk_acc& a = S.accs[c % A];
       const uint64_t v = sm[c];
-      if (v != b_acc_init(a)) b_merge_atomic(&I.gacc[(c % A) * K + c / A], a, v);
+      if (v != b_acc_init(a)) acc_merge_global(&I.gacc[(c % A) * K + c / A], a, v);
     }
     __syncthreads();
     return;
@@ -255,7 +255,7 @@ __device__ void gb_agg_item(const BatchInst& I, int64_t b, int64_t e, uint64_t* 
     for (int t = lane; t < T; t += 32) v = b_combine(a, v, sm[c * T + t]);
 #pragma unroll
     for (int o = 16; o; o >>= 1) v = b_combine(a, v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane == 0 && v != b_acc_init(a)) b_merge_atomic(&I.gacc[(c % A) * K + c / A], a, v);
+    if (lane == 0 && v != b_acc_init(a)) acc_merge_global(&I.gacc[(c % A) * K + c / A], a, v);
   }
 }
 

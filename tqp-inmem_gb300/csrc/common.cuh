@@ -99,6 +99,53 @@ __device__ __forceinline__ uint64_t d2u(double d) {
 }
 __device__ __forceinline__ double u2d(uint64_t u) { return __longlong_as_double(static_cast<long long>(u)); }
 
+// Reductions into global memory whose result nobody reads: `red.global`, applied at the L2 with no
+// reply.  An atomicAdd through a pointer the compiler cannot place in global memory (one loaded
+// from a descriptor or selected between shared and global tables) is a generic atomic that returns
+// its old value, and the issuing warp waits for the round trip (measured on a 9.3 K-group batched
+// group-by: every update an L2 round trip, 122 stall cycles per issued instruction).
+__device__ __forceinline__ void gred_add(double* p, double v) {
+  asm volatile("red.global.add.f64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "d"(v) : "memory");
+}
+__device__ __forceinline__ void gred_add(uint64_t* p, uint64_t v) {
+  asm volatile("red.global.add.u64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ void gred_add(unsigned* p, unsigned v) {
+  asm volatile("red.global.add.u32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ void gred_min_u64(uint64_t* p, uint64_t v) {
+  asm volatile("red.global.min.u64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ void gred_max_u64(uint64_t* p, uint64_t v) {
+  asm volatile("red.global.max.u64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ void gred_min_s64(uint64_t* p, int64_t v) {
+  asm volatile("red.global.min.s64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ void gred_max_s64(uint64_t* p, int64_t v) {
+  asm volatile("red.global.max.s64 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+// Merge of a value (accumulator encoding: F64 sums as bits, F64 min/max as order keys) into a
+// global table cell.
+__device__ __forceinline__ void acc_merge_global(uint64_t* p, const tqpk_acc& a, uint64_t v) {
+  switch (a.kind) {
+    case TQPK_ACC_SUM:
+      if (a.type == TQPK_F64) gred_add(reinterpret_cast<double*>(p), u2d(v));
+      else gred_add(p, v);
+      break;
+    case TQPK_ACC_COUNT_ROWS:
+    case TQPK_ACC_COUNT_NOTNULL: gred_add(p, v); break;
+    case TQPK_ACC_MIN:
+      if (a.type == TQPK_F64) gred_min_u64(p, v);
+      else gred_min_s64(p, static_cast<int64_t>(v));
+      break;
+    case TQPK_ACC_MAX:
+      if (a.type == TQPK_F64) gred_max_u64(p, v);
+      else gred_max_s64(p, static_cast<int64_t>(v));
+      break;
+  }
+}
+
 // Order-preserving map of a double onto uint64 (for min/max atomics and the
 // radix sort): negative values have all bits flipped, others the sign bit.
 __device__ __forceinline__ uint64_t f64_ordered(double d) {

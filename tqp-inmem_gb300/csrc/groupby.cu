@@ -108,7 +108,7 @@ __device__ __forceinline__ void acc_row(const tqpk_groupby_spec& S, uint64_t* sm
   } else if (MODE == 2) {
     acc_merge_atomic(&sm[slot * S.n_accs + a], S.accs[a], acc_value(S.accs[a], x));
   } else {
-    acc_merge_atomic(&gacc[(int64_t)a * K + slot], S.accs[a], acc_value(S.accs[a], x));
+    acc_merge_global(&gacc[(int64_t)a * K + slot], S.accs[a], acc_value(S.accs[a], x));
   }
 }
 
@@ -191,13 +191,13 @@ __global__ void __launch_bounds__(256) k_groupby_dense(const __grid_constant__ t
       for (int t = lane; t < T; t += 32) v = combine_plain(a, v, sm[c * T + t]);
 #pragma unroll
       for (int o = 16; o; o >>= 1) v = combine_plain(a, v, __shfl_xor_sync(0xffffffffu, v, o));
-      if (lane == 0 && v != acc_init(a)) acc_merge_atomic(&gacc[(c % A) * K + c / A], a, v);
+      if (lane == 0 && v != acc_init(a)) acc_merge_global(&gacc[(c % A) * K + c / A], a, v);
     }
   } else {
     for (int64_t c = threadIdx.x; c < K * A; c += T) {
       const tqpk_acc& a = S.accs[c % A];
       const uint64_t v = sm[c];
-      if (v != acc_init(a)) acc_merge_atomic(&gacc[(c % A) * K + c / A], a, v);
+      if (v != acc_init(a)) acc_merge_global(&gacc[(c % A) * K + c / A], a, v);
     }
   }
 }
@@ -259,12 +259,12 @@ __global__ void __launch_bounds__(256) k_groupby_hash(const __grid_constant__ tq
         uint64_t r[16];
         expr_eval_small<16>(S.expr, S.n_expr, S.cols, S.col_dtypes, r0 + j, r);
         for (int a = 0; a < A; ++a)
-          acc_merge_atomic(&gacc[(int64_t)a * C + h], S.accs[a], acc_value(S.accs[a], reg_pick<16>(r, S.accs[a].reg)));
+          acc_merge_global(&gacc[(int64_t)a * C + h], S.accs[a], acc_value(S.accs[a], reg_pick<16>(r, S.accs[a].reg)));
       } else {
         uint64_t r[TQPK_MAX_EXPR];
         expr_eval_generic(S.expr, S.n_expr, S.cols, S.col_dtypes, r0 + j, r);
         for (int a = 0; a < A; ++a)
-          acc_merge_atomic(&gacc[(int64_t)a * C + h], S.accs[a], acc_value(S.accs[a], r[S.accs[a].reg]));
+          acc_merge_global(&gacc[(int64_t)a * C + h], S.accs[a], acc_value(S.accs[a], r[S.accs[a].reg]));
       }
     }
   }

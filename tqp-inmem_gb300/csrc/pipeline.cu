@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kBlock) k_pl_probe_agg(const __grid_constant__
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         if (!((m[u] >> j) & 1u)) continue;
-        atomicAdd(&sum[slot[u][j]], v[j]);
+        gred_add(&sum[slot[u][j]], v[j]);
         cnt[slot[u][j]] = 1u;  // occupancy (the top-k pass counts the groups)
       }
     }

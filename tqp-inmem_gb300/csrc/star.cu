@@ -138,8 +138,8 @@ __global__ void __launch_bounds__(kBlock) k_star_probe(const __grid_constant__ t
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         if (!((m[u] >> j) & 1u)) continue;
-        atomicAdd(&sum[k[u][j]], v[j]);
-        atomicAdd(&cnt[k[u][j]], 1u);
+        gred_add(&sum[k[u][j]], v[j]);
+        gred_add(&cnt[k[u][j]], 1u);
       }
     }
   }

@@ -45,6 +45,31 @@ __device__ __forceinline__ bool iscl(double x, double lit, double allowed) {
   double e = fabs(__dsub_rn(x, lit));
   return (x == lit) || (isfinite(e) && e <= allowed);
 }
+// reductions into global memory whose result nobody reads: `red.global`, applied at the L2 without a
+// reply.  An atomicAdd through a pointer the compiler cannot place in global memory (a table pointer
+// loaded from a descriptor) becomes a generic atomic that returns its old value, and the warp waits
+// for the round trip.
+__device__ __forceinline__ void gred_add(double* p, double v) {
+  asm volatile("red.global.add.f64 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "d"(v) : "memory");
+}
+__device__ __forceinline__ void gred_add(u64* p, u64 v) {
+  asm volatile("red.global.add.u64 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ void gred_add(unsigned* p, unsigned v) {
+  asm volatile("red.global.add.u32 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ void gred_min(u64* p, u64 v) {
+  asm volatile("red.global.min.u64 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ void gred_max(u64* p, u64 v) {
+  asm volatile("red.global.max.u64 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ void gred_min(i64* p, i64 v) {
+  asm volatile("red.global.min.s64 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
+__device__ __forceinline__ void gred_max(i64* p, i64 v) {
+  asm volatile("red.global.max.s64 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "l"(v) : "memory");
+}
 // bulk copies (TMA, 1-D) into shared memory, completed on an mbarrier
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
@@ -468,7 +493,16 @@ def _combine(a, x: str, y: str) -> str:
     return f"{fn}({x}, {y})" if a.type == L.F64 else f"(u64){fn}((i64)({x}), (i64)({y}))"
 
 
-def _merge_atomic(a, p: str, v: str) -> str:
+def _merge_atomic(a, p: str, v: str, glob: bool = False) -> str:
+    """Atomic merge of v (accumulator encoding) into the cell at p; glob: p is in global memory and
+    the merge is a reduction without a reply (the shared-memory tables keep the atomics)."""
+    if glob:
+        if a.kind == L.ACC_SUM and a.type == L.F64:
+            return f"gred_add((double*)({p}), u2d({v}));"
+        if a.kind in (L.ACC_SUM, L.ACC_COUNT_ROWS, L.ACC_COUNT_NOTNULL):
+            return f"gred_add((u64*)({p}), (u64)({v}));"
+        fn = "gred_min" if a.kind == L.ACC_MIN else "gred_max"
+        return f"{fn}((u64*)({p}), (u64)({v}));" if a.type == L.F64 else f"{fn}((i64*)({p}), (i64)({v}));"
     if a.kind == L.ACC_SUM:
         return (f"atomicAdd((double*)({p}), u2d({v}));" if a.type == L.F64
                 else f"atomicAdd((unsigned long long*)({p}), (unsigned long long)({v}));")
@@ -558,7 +592,7 @@ def groupby_source(spec, pred, plan) -> Tuple[str, str, int, int]:
         elif shared:
             src.append("      " + _merge_atomic(acc, f"&sm[slot * A + {a}]", v))
         else:
-            src.append("      " + _merge_atomic(acc, f"&gacc[{a} * K + slot]", v))
+            src.append("      " + _merge_atomic(acc, f"&gacc[{a} * K + slot]", v, glob=True))
     src.append("    }")
     src.append("  }")
     if private:
@@ -575,7 +609,7 @@ def groupby_source(spec, pred, plan) -> Tuple[str, str, int, int]:
             src.append(f"      for (int t = lane; t < T; t += 32) v = {_combine(acc, 'v', 'sm[c * T + t]')};")
             src.append("      for (int o = 16; o; o >>= 1) { const u64 w = __shfl_xor_sync(0xffffffffu, v, o); "
                        f"v = {_combine(acc, 'v', 'w')}; }}")
-            src.append(f"      if (lane == 0 && v != {init}) {_merge_atomic(acc, f'&gacc[{a} * K + s]', 'v')}")
+            src.append(f"      if (lane == 0 && v != {init}) {_merge_atomic(acc, f'&gacc[{a} * K + s]', 'v', glob=True)}")
             src.append("      break; }")
         src.append("    }")
         src.append("  }")
@@ -586,7 +620,7 @@ def groupby_source(spec, pred, plan) -> Tuple[str, str, int, int]:
         src.append("    switch (a) {")
         for a in range(A):
             acc = S.accs[a]
-            src.append(f"    case {a}: if (v != {_acc_init(acc)}) {_merge_atomic(acc, f'&gacc[{a} * K + s]', 'v')} break;")
+            src.append(f"    case {a}: if (v != {_acc_init(acc)}) {_merge_atomic(acc, f'&gacc[{a} * K + s]', 'v', glob=True)} break;")
         src.append("    }")
         src.append("  }")
     src.append("}")
@@ -654,9 +688,9 @@ def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[st
         lines.append("      " + re.sub(r"\bc(\d+)\.v\[j\]", r"Cs\1", l))
     if neg_zero_as_zero:     # the sums start at -0.0 (the empty marker); add a -0.0 value as +0.0
         lines.append(f"      const double vz = (double)r{val_reg};")
-        lines.append("      atomicAdd(&sum[slot], d2u(vz) == 0x8000000000000000ull ? 0.0 : vz);")
+        lines.append("      gred_add(&sum[slot], d2u(vz) == 0x8000000000000000ull ? 0.0 : vz);")
     else:
-        lines.append(f"      atomicAdd(&sum[slot], (double)r{val_reg});")
+        lines.append(f"      gred_add(&sum[slot], (double)r{val_reg});")
     lines += ["      " + x for x in extra]
     lines += ["    }", "    __syncwarp();"]
     return lines
@@ -1115,7 +1149,7 @@ def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_bl
                 "#pragma unroll",
                 "      for (int j = 0; j < 4; ++j)",
                 "        if (((m[u] >> j) & 1u) && __ldg(&dir_c[k[u][j]]) < 0) m[u] &= ~(1u << j);"]
-    src += _dense_tail(S, val_reg, ecols, elines, "nf", "k", ["atomicAdd(&cnt[slot], 1u);"], U=U,
+    src += _dense_tail(S, val_reg, ecols, elines, "nf", "k", ["gred_add(&cnt[slot], 1u);"], U=U,
                        l1_no_allocate=a_bits)
     src += ["  }", "}"]
     return "\n".join(src), name

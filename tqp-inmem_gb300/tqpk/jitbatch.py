@@ -187,8 +187,9 @@ def _gb_functions(p: int, spec, pred) -> str:
             "  // mode 4: global atomics only",
             "  const i64 copies = mode == 1 ? " + str(T) + " : I.copies;",
             "  const i64 me = threadIdx.x & (copies - 1);",
-            "  if (mode != 4) {",
-            f"    for (i64 i = threadIdx.x; i < K * A * copies; i += {T}) {{ const int a = (int)((i / copies) % A); "
+            "  const int lgc = __ffsll(copies) - 1;            // copies is a power of two",
+            "  if (mode != 4) {                                  // K * A * copies cells fit in 32 bits",
+            f"    for (int i = threadIdx.x; i < (int)(K * A * copies); i += {T}) {{ const int a = (i >> lgc) % A; "
             f"sm[i] = {inits}; }}",
             "    __syncthreads();",
             "  }",
@@ -206,26 +207,42 @@ def _gb_functions(p: int, spec, pred) -> str:
         acc = S.accs[a]
         v = jit._acc_value(acc)
         src.append(f"      {{ const u64 x = {v};")
-        src.append(f"        if (mode == 4) {{ {jit._merge_atomic(acc, f'&gacc[{a} * K + slot]', 'x')} }}")
+        src.append(f"        if (mode == 4) {{ {jit._merge_atomic(acc, f'&gacc[{a} * K + slot]', 'x', glob=True)} }}")
         src.append(f"        else if (mode == 1) {{ u64* c = &sm[(slot * A + {a}) * copies + me]; "
                    f"*c = {jit._combine(acc, '*c', 'x')}; }}")
         src.append(f"        else {{ {jit._merge_atomic(acc, f'&sm[(slot * A + {a}) * copies + me]', 'x')} }} }}")
     src += ["    }", "  }", "  if (mode == 4) return;", "  __syncthreads();",
-            "  // fold the copies of each cell and merge it into the global table",
-            "  for (i64 c = wid; c < K * A; c += " + str(T // 32) + ") {",
-            "    const int a = (int)(c % A); const i64 s = c / A;",
+            "  // fold the copies of each cell and merge it into the global table: mode 1 (256 copies of",
+            "  // at most 48 cells) one warp per cell, lanes over the copies; mode 2 one thread per cell,",
+            "  // its copies in turn (a warp-wide shuffle reduction would spend 5 x 32 FP64 combines on",
+            "  // every cell however few copies it has, and FP64 issues at 1/64 rate)",
+            "  if (mode == 1) {",
+            "  for (int c = wid; c < (int)(K * A); c += " + str(T // 32) + ") {",
+            "    const int a = c % A; const int s = c / A;",
             "    switch (a) {"]
     for a in range(A):
         acc = S.accs[a]
         init = jit._acc_init(acc)
         src += [f"    case {a}: {{",
                 f"      u64 v = {init};",
-                f"      for (i64 t = lane; t < copies; t += 32) v = {jit._combine(acc, 'v', 'sm[c * copies + t]')};",
+                f"      for (int t = lane; t < {T}; t += 32) v = {jit._combine(acc, 'v', f'sm[c * {T} + t]')};",
                 "      for (int o = 16; o; o >>= 1) { const u64 w = __shfl_xor_sync(0xffffffffu, v, o); "
                 f"v = {jit._combine(acc, 'v', 'w')}; }}",
-                f"      if (lane == 0 && v != {init}) {{ {jit._merge_atomic(acc, f'&gacc[{a} * K + s]', 'v')} }}",
+                f"      if (lane == 0 && v != {init}) {{ {jit._merge_atomic(acc, f'&gacc[{a} * K + s]', 'v', glob=True)} }}",
                 "      break; }"]
-    src += ["    }", "  }", "  __syncthreads();", "}"]
+    src += ["    }", "  }", "  } else {",
+            f"  for (int c = threadIdx.x; c < (int)(K * A); c += {T}) {{",
+            "    const int a = c % A; const int s = c / A;",
+            "    switch (a) {"]
+    for a in range(A):
+        acc = S.accs[a]
+        init = jit._acc_init(acc)
+        src += [f"    case {a}: {{",
+                f"      u64 v = {init};",
+                f"      for (int t = 0; t < (int)copies; ++t) v = {jit._combine(acc, 'v', '(sm[(c << lgc) + t])')};",
+                f"      if (v != {init}) {{ {jit._merge_atomic(acc, f'&gacc[{a} * K + s]', 'v', glob=True)} }}",
+                "      break; }"]
+    src += ["    }", "  }", "  }", "  __syncthreads();", "}"]
     # emit: the groups of slots [b, e) at their output offset
     src += [f"__device__ void gb_emit_{p}(const QInst& I, i64 item, i64 b, i64 e, int* sw) {{",
             "  __shared__ i64 s_base;",

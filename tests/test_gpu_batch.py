@@ -131,11 +131,13 @@ def test_batch_item_sizes_do_not_change_results(impl):
 
 
 def test_generated_batch_table_modes_and_empty_instances():
-    """Group tables of every placement (per thread, several shared copies, one per CTA, global) and
-    instances with no rows, in one generated batch."""
+    """Group tables of every placement (per thread, several shared copies, one per CTA, global), join
+    sums of every placement (per thread, shared copies, global) and instances with no rows, in one
+    generated batch."""
     from tqpk.jitbatch import QueryBatch, _mode
     shapes = [("groupby", 200_000, 4), ("groupby", 200_000, 150), ("groupby", 200_000, 1400),
-              ("groupby", 200_000, 30_000), ("groupby", 0, 9), ("join", 0, 100), ("join", 50_000, 1)]
+              ("groupby", 200_000, 30_000), ("groupby", 0, 9), ("join", 0, 100), ("join", 50_000, 1),
+              ("join", 300_000, 40), ("join", 300_000, 500), ("join", 100_000, 60_000)]
     insts, expected = [], []
     for i, (kind, rows, g) in enumerate(shapes):
         inst, exp = (make_groupby if kind == "groupby" else make_join)(rows, g, 300 + i)
@@ -145,6 +147,8 @@ def test_generated_batch_table_modes_and_empty_instances():
     placements = {(int(b.recs[i].mode), int(b.recs[i].copies)) for i, (kind, _, _) in enumerate(shapes)
                   if kind == "groupby"}
     assert {(1, 256), (2, 8), (2, 1), (4, 1)} <= placements
+    join_modes = {int(b.recs[i].mode) for i, (kind, rows, _) in enumerate(shapes) if kind == "join" and rows}
+    assert join_modes == {0, 1, 2}
     b.run()
     check(b.results(), expected)
 

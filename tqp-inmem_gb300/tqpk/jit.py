@@ -649,14 +649,15 @@ def _gather_pred(pred, prefix: str, lits: str, ptr_pfx: str, row: str, live: str
 
 def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[str], U: int = 2,
                 smem_vals: Optional[Dict[int, str]] = None, neg_zero_as_zero: bool = False,
-                l1_no_allocate: bool = False) -> List[str]:
+                l1_no_allocate: bool = False, sum_stmt: Optional[str] = None) -> List[str]:
     """Warp-dense value pass: the warp's matched rows (queued as row offsets and
     slots in shared memory) are spread over all 32 lanes, so each FP64
     instruction and atomic runs with full lanes instead of the ~1 in 4 a
     row-per-lane loop leaves active after the predicate and the lookups.
     Each lane holds U groups of 4 rows; value column c is read from global
     memory, or from the shared-memory stage smem_vals[c] (indexed by the row's
-    offset in the warp's 128 * U rows)."""
+    offset in the warp's 128 * U rows).  sum_stmt replaces the reduction of the value (the
+    double `vz`) into sum[slot]."""
     import re
     lines = [f"    const unsigned nm = {' + '.join(f'__popc(m[{u}])' for u in range(U))};",
              "    unsigned incl = nm;",
@@ -686,7 +687,10 @@ def _dense_tail(S, val_reg: int, ecols, elines, n: str, key: str, extra: List[st
             lines.append(f"      const {t} Cs{c} = __ldg((const {t}*)cp{c} + row);")
     for l in elines:
         lines.append("      " + re.sub(r"\bc(\d+)\.v\[j\]", r"Cs\1", l))
-    if neg_zero_as_zero:     # the sums start at -0.0 (the empty marker); add a -0.0 value as +0.0
+    if sum_stmt is not None:
+        lines.append(f"      const double vz = (double)r{val_reg};")
+        lines.append("      " + sum_stmt)
+    elif neg_zero_as_zero:     # the sums start at -0.0 (the empty marker); add a -0.0 value as +0.0
         lines.append(f"      const double vz = (double)r{val_reg};")
         lines.append("      gred_add(&sum[slot], d2u(vz) == 0x8000000000000000ull ? 0.0 : vz);")
     else:

@@ -16,10 +16,11 @@ Work items are (instance, phase, begin, end), ordered phase-major; a CTA takes
 the next item with an atomic ticket and, for phase p > 0, waits (bounded) until
 every phase p-1 item of the same instance has finished.  Phases:
 
-* group-by: 0 accumulate rows [b, e) into the instance's table (per-thread,
-  per-warp, per-CTA shared-memory tables merged into the global one, or
-  global atomics, chosen by table size), 1 count the occupied slots of
-  [b, e), 2 write the groups of [b, e) at their offset (key order);
+* group-by: 0 accumulate rows [b, e) into the instance's table (per-thread or
+  shared copies of a shared-memory table merged into the global one, or
+  reductions straight into the global table, chosen by table size), 1 count
+  the occupied slots of [b, e), 2 write the groups of [b, e) at their offset
+  (key order);
 * join: 0 build the key directory from build rows [b, e), 1 probe rows [b, e)
   (predicate, lookup, value, FP64 sum per build key), 2 per-item top-k of
   slots [b, e), 3 merge the per-item lists (one item).
@@ -184,7 +185,7 @@ def _gb_functions(p: int, spec, pred) -> str:
     inits = " : ".join(f"(a == {i}) ? {jit._acc_init(S.accs[i])}" for i in range(A)) + " : 0ull"
     src += ["  // table copies in shared memory: one per thread (mode 1, plain updates), or `copies`",
             "  // (a power of two) shared by threads tid % copies with shared-memory atomics (mode 2);",
-            "  // mode 4: global atomics only",
+            "  // mode 4: reductions into the global table only",
             "  const i64 copies = mode == 1 ? " + str(T) + " : I.copies;",
             "  const i64 me = threadIdx.x & (copies - 1);",
             "  const int lgc = __ffsll(copies) - 1;            // copies is a power of two",
@@ -246,11 +247,14 @@ def _gb_functions(p: int, spec, pred) -> str:
     # emit: the groups of slots [b, e) at their output offset
     src += [f"__device__ void gb_emit_{p}(const QInst& I, i64 item, i64 b, i64 e, int* sw) {{",
             "  __shared__ i64 s_base;",
-            "  if (threadIdx.x == 0) {",
+            "  if (threadIdx.x < 32) {            // groups of the items before this one: warp 0's lanes in turn",
             "    i64 base = 0;",
-            "    for (i64 r = 0; r < item; ++r) base += __ldcg(&I.range_count[r]);",
-            "    s_base = base;",
-            "    if (item == I.ni[2] - 1 && I.out_groups) *I.out_groups = base + __ldcg(&I.range_count[item]);",
+            "    for (i64 r = threadIdx.x; r < item; r += 32) base += __ldcg(&I.range_count[r]);",
+            "    for (int o = 16; o; o >>= 1) base += __shfl_xor_sync(0xffffffffu, base, o);",
+            "    if (threadIdx.x == 0) {",
+            "      s_base = base;",
+            "      if (item == I.ni[2] - 1 && I.out_groups) *I.out_groups = base + __ldcg(&I.range_count[item]);",
+            "    }",
             "  }",
             "  __syncthreads();",
             "  const i64 K = I.slots;",
@@ -324,7 +328,7 @@ def _join_functions(p: int, spec, val_reg: int, ppred, bpred) -> str:
     pcols, pexpr = jit._pred_code(ppred, "p") if ppred is not None else ([], "true")
     plit, pexpr = _hoist(pexpr, "I")
     ecols, elines = jit._expr_code(S, val_reg + 1, "c")
-    src += [f"__device__ void jn_probe_{p}(const QInst& I, i64 b, i64 e) {{",
+    src += [f"__device__ void jn_probe_{p}(const QInst& I, i64 b, i64 e, u64* sm) {{",
             "  __shared__ unsigned char q_off[8][256];",
             "  __shared__ int q_slot[8][256];",
             "  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;",
@@ -332,7 +336,16 @@ def _join_functions(p: int, spec, val_reg: int, ppred, bpred) -> str:
             "  const bool vp = I.flags & 1, vf = I.flags & 8;",
             "  const int* __restrict__ dir = I.dir;",
             "  double* __restrict__ sum = I.sum;",
-            "  unsigned* __restrict__ occ = I.occ;"]
+            "  unsigned* __restrict__ occ = I.occ;",
+            "  // sums of a small key domain gather in shared memory first (many rows per key: reductions",
+            "  // into a few global cells queue at the L2): mode 1 one copy per thread, mode 2 `copies`",
+            "  // copies shared by threads tid % copies; cells start at -0.0, the untouched marker",
+            "  const int jm = I.mode, copies = jm == 1 ? " + str(T) + " : I.copies;",
+            "  const int lgc = __ffs(copies) - 1, me = threadIdx.x & (copies - 1);",
+            "  if (jm) {",
+            f"    for (int i = threadIdx.x; i < (int)slots * copies; i += {T}) sm[i] = 0x8000000000000000ull;",
+            "    __syncthreads();",
+            "  }"]
     src += ["  " + d for d in plit]
     if ppred is not None:
         src += ["  " + d for d in _ptr_decls(pcols, ppred.dtypes, "pc", "pp")]
@@ -365,8 +378,25 @@ def _join_functions(p: int, spec, val_reg: int, ppred, bpred) -> str:
             "#pragma unroll",
             "      for (int j = 0; j < 4; ++j)",
             "        if (((m[u] >> j) & 1u) && __ldcg(&dir[sl[u][j]]) < 0) m[u] &= ~(1u << j);"]
-    src += jit._dense_tail(S, val_reg, ecols, elines, "np", "sl", ["occ[slot] = 1u;"])
-    src += ["  }", "}"]
+    sum_stmt = ("if (jm == 0) { gred_add(&sum[slot], vz); occ[slot] = 1u; } else { "
+                "const double va = d2u(vz) == 0x8000000000000000ull ? 0.0 : vz; "
+                "double* cell = (double*)&sm[((int)slot << lgc) + me]; "
+                "if (jm == 1) *cell = __dadd_rn(*cell, va); else atomicAdd(cell, va); }")
+    src += jit._dense_tail(S, val_reg, ecols, elines, "np", "sl", [], sum_stmt=sum_stmt)
+    src += ["  }",
+            "  if (jm) {            // fold each key's copies (untouched ones skipped) into the global sums",
+            "    __syncthreads();",
+            f"    for (int s = threadIdx.x; s < (int)slots; s += {T}) {{",
+            "      double t = 0.0; bool hit = false;",
+            "      for (int c = 0; c < copies; ++c) {",
+            "        const u64 x = sm[(s << lgc) + ((c + s) & (copies - 1))];   // staggered: fewer bank conflicts",
+            "        if (x != 0x8000000000000000ull) { t = __dadd_rn(t, u2d(x)); hit = true; }",
+            "      }",
+            "      if (hit) { gred_add(&sum[s], t); occ[s] = 1u; }",
+            "    }",
+            "    __syncthreads();",
+            "  }",
+            "}"]
     return "\n".join(src)
 
 
@@ -441,10 +471,11 @@ __device__ void jn_topk_merge(const QInst& I, u64* sk, i64* si) {
     const bool v = lane < k && m.idx >= 0;
     const int cnt = __popc(__ballot_sync(0xffffffffu, v));
     if (v) { I.out_keys[lane] = I.kmin[0] + m.idx; I.out_vals[lane] = __ldcg(&I.sum[m.idx]); }
+    i64 groups = 0;
+    for (i64 r = lane; r < parts; r += 32) groups += __ldcg(&I.range_count[r]);
+    for (int o = 16; o; o >>= 1) groups += __shfl_xor_sync(0xffffffffu, groups, o);
     if (lane == 0) {
       *I.out_count = cnt;
-      i64 groups = 0;
-      for (i64 r = 0; r < parts; ++r) groups += __ldcg(&I.range_count[r]);
       if (I.out_groups) *I.out_groups = groups;
     }
   }
@@ -465,7 +496,7 @@ def batch_source(gb_progs, join_progs) -> str:
     gb_emit = "\n".join(f"        case {p}: gb_emit_{p}(I, W.begin / I.range_slots, W.begin, W.end, sw); break;"
                         for p in range(len(gb_progs)))
     jb = "\n".join(f"        case {p}: jn_build_{p}(I, W.begin, W.end, err); break;" for p in range(len(join_progs)))
-    jp = "\n".join(f"        case {p}: jn_probe_{p}(I, W.begin, W.end); break;" for p in range(len(join_progs)))
+    jp = "\n".join(f"        case {p}: jn_probe_{p}(I, W.begin, W.end, sm); break;" for p in range(len(join_progs)))
     parts.append(f"""
 extern "C" __global__ void __launch_bounds__({T}) tqpk_qb_run(const QInst* __restrict__ insts,
     const WorkItem* __restrict__ items, int n_items, unsigned* ticket, unsigned long long* done, int* err,
@@ -582,6 +613,18 @@ def _mode(K: int, A: int) -> Tuple[int, int]:
     if fit >= 1:
         return 2, 1 << int(math.floor(math.log2(fit)))
     return 4, 1
+
+
+def _join_mode(slots: int, rows_per_item: int) -> Tuple[int, int]:
+    """(mode, copies) of a join probe's sums: a shared-memory table per item when the key domain
+    is small next to the item (one copy per thread, mode 1, or the shared copies that fit, mode 2),
+    else reductions straight into the global sums (mode 0)."""
+    fit = SMEM // max(1, slots * 8)
+    if fit >= T:
+        return 1, T
+    if fit >= 1 and slots * 4 <= rows_per_item:
+        return 2, 1 << int(math.floor(math.log2(fit)))
+    return 0, 1
 
 
 def _aligned(*ts) -> bool:
@@ -725,6 +768,7 @@ class QueryBatch:
         R.fk_dt, R.bk_dt = code_of(pk.dtype), code_of(bk.dtype)
         rb = self.tuner.rows_per_item("join_build", bk.numel())
         rp = self.tuner.rows_per_item("join_probe", pk.numel())
+        R.mode, R.copies = _join_mode(slots, rp)
         R.range_slots = min(1 << 14, -(-slots // 256) * 256)
         R.ni[0] = -(-bk.numel() // rb) if bk.numel() else 0
         R.ni[1] = -(-pk.numel() // rp) if pk.numel() else 0

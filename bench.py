@@ -213,11 +213,11 @@ class JoinAggTop10:
             else:
                 tqp_sort(True, tg, a, True, "t")
             i += 1
-        res = d2h_all({11: tg[11].tensor, 302: tg[302].tensor})
-        keys, vals = res[11], res[302]
+        from tqpk.variable import host_values      # the fused path read the rows with its count
+        keys, vals = host_values(tg[11]), host_values(tg[302])
         h2d = sum(h.numel() * h.element_size() for h in self.host.values())
-        d2h = keys.numel() * keys.element_size() + vals.numel() * vals.element_size()
-        return (keys.numpy().reshape(-1), vals.numpy()), h2d, d2h
+        d2h = keys.nbytes + vals.nbytes
+        return (keys.reshape(-1), vals), h2d, d2h
 
     def oracle(self, cols=None):
         from oracle import tqp_oracle as O

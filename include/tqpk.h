@@ -433,7 +433,12 @@ void* tqpk_groupby_table(void* d_ws);
  * caller-launched probe, not with bit 1): the reset + build stage writes the
  * build side's membership bitmap (bit s of word s / 32 for key key_min + s,
  * (slots + 31) / 32 words at the directory's address) instead of its row
- * directory; a repeated key still sets TQPK_EUNSUPPORTED.                   */
+ * directory; a repeated key still sets TQPK_EUNSUPPORTED.  Bit 5 (with bit
+ * 4): the reset stage clears the header and the bitmap but launches no build
+ * kernel; the caller's build (a query-specialised kernel) sets every group
+ * sum to -0.0, the bit of each passing build key (an out-of-domain key sets
+ * TQPK_EINVAL in the error word) and adds the passing rows to the count whose
+ * address tqpk_pipeline_join_words gives, as the library's build does.      */
 int tqpk_pipeline_join_agg_topk_stages(int32_t stages, const void* d_build_keys, int32_t build_dtype, int64_t nb,
                                        const tqpk_predicate* h_build_pred, int64_t key_min, int64_t key_max,
                                        const void* d_probe_fk, int32_t probe_dtype, int64_t np,
@@ -443,6 +448,9 @@ int tqpk_pipeline_join_agg_topk_stages(int32_t stages, const void* d_build_keys,
                                        int64_t* d_groups_out, tqpk_stream stream);
 int tqpk_pipeline_join_tables(void* d_ws, size_t ws_bytes, int64_t key_min, int64_t key_max, void** dir, void** sum,
                               void** occ);
+/* The pipeline's error word and passing-build-row count (uint64), for a caller-launched build. */
+int tqpk_pipeline_join_words(void* d_ws, size_t ws_bytes, int64_t key_min, int64_t key_max, int32_t** err,
+                             uint64_t** passing);
 
 /* ---- resident directories and dense slot tables (dense.cu) ---------------
  * Replaces the per-call build of operators/hashjoin.py:24-177 (torch.sort of

@@ -83,6 +83,11 @@ def test_probe_kernels_compile_with_and_without_build_filter():
         ok, log = jit.check_compiles(src)
         assert ok, log[:2000]
         assert ("cp_async16(&q_v" in src) == st
+    for b in (bp, None):                     # the fused join's generated bitmap build
+        src, name = jit.join_build_bits_source(b.struct if b else None)
+        ok, log = jit.check_compiles(src)
+        assert ok, log[:2000]
+        assert name == "tqpk_q_join_build_bits" and "red.global.or.b32" in src
 
 
 def test_generated_batch_kernel_compiles_and_record_layout_matches():

@@ -68,6 +68,10 @@ def test_fused_run_matches_the_operators(nb, np_, limit, desc):
     np.testing.assert_array_equal(got_k.cpu().numpy(), exp_k.cpu().numpy())
     assert tg[302].tensor.dtype == torch.float64 and tg[302].tensor_type == "float"
     assert_f64_close(tg[302].tensor.cpu().numpy(), exp[302].tensor.cpu().numpy())
+    # the rows read back with the count equal the device columns bit for bit
+    from tqpk.variable import host_values
+    np.testing.assert_array_equal(host_values(tg[11]), got_k.cpu().numpy())
+    np.testing.assert_array_equal(host_values(tg[302]).view(np.uint64), tg[302].tensor.cpu().numpy().view(np.uint64))
 
 
 def test_fused_run_from_columns_still_copying():

@@ -41,22 +41,38 @@ __global__ void __launch_bounds__(kBlock) k_dir_build(const __grid_constant__ tq
     ld4_int(keys, dt, r0, n, kvec, x);
     int64_t pl[4] = {r0, r0 + 1, r0 + 2, r0 + 3};
     if (payload) ld4_int(payload, pdt, r0, n, plvec, pl);
+    // The four rows' next-table lookups, then their four claims, are issued before any result is
+    // used: each is an L2 round trip, and one row after another a thread would wait for eight.
+    int64_t slot[4];
+    bool put[4], ok[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      if (!((live >> j) & 1u)) break;
-      const int64_t slot = x[j] - kmin;
-      if (slot < 0 || slot >= slots) { set_error(err, TQPK_EINVAL); continue; }
+      slot[j] = x[j] - kmin;
+      const bool in = (live >> j) & 1u;
+      put[j] = in && slot[j] >= 0 && slot[j] < slots;
+      if (in && !put[j]) set_error(err, TQPK_EINVAL);
       // a payload outside int32, or equal to the empty marker, cannot name a key of the
       // next (int32) domain: the row stays in the directory as a non-matching entry
-      bool ok = ((pass >> j) & 1u) && pl[j] >= (int64_t)INT32_MIN && pl[j] <= (int64_t)INT32_MAX &&
-                pl[j] != (int64_t)empty;
-      if (ok && next) {        // composed with the next table: keep a payload key that has a row there
-        const int64_t q = pl[j] - next_min;
-        ok = q >= 0 && q < next_slots && __ldg(&next[q]) >= 0;
-      }
-      const int v = ok ? (int)pl[j] : fail_value;
-      if (atomicCAS(&dir[slot], empty, v) != empty) set_error(err, TQPK_EUNSUPPORTED);  // repeated key
+      ok[j] = put[j] && ((pass >> j) & 1u) && pl[j] >= (int64_t)INT32_MIN && pl[j] <= (int64_t)INT32_MAX &&
+              pl[j] != (int64_t)empty;
     }
+    if (next) {                // composed with the next table: keep a payload key that has a row there
+      int nx[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t q = pl[j] - next_min;
+        ok[j] = ok[j] && q >= 0 && q < next_slots;
+        nx[j] = ok[j] ? __ldg(&next[q]) : -1;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) ok[j] = ok[j] && nx[j] >= 0;
+    }
+    int old[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) old[j] = put[j] ? atomicCAS(&dir[slot[j]], empty, ok[j] ? (int)pl[j] : fail_value) : empty;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (old[j] != empty) set_error(err, TQPK_EUNSUPPORTED);  // repeated key
   }
 }
 

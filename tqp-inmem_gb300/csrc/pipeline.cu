@@ -56,13 +56,17 @@ __global__ void __launch_bounds__(kBlock) k_pl_build(const __grid_constant__ tqp
     if (!b) continue;
     int64_t x[4];
     ld4_int(A.b_keys, A.b_dt, r0, A.nb, vec, x);
+    int old[4];           // the four claims in flight together, their results read afterwards
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      if (!((b >> j) & 1u)) continue;
       const int64_t slot = x[j] - A.key_min;
-      if (slot < 0 || slot >= A.slots) { set_error(err_dup, TQPK_EINVAL); continue; }
-      if (atomicCAS(&dir[slot], -1, (int)(r0 + j)) != -1) set_error(err_dup, TQPK_EUNSUPPORTED);
+      const bool in = (b >> j) & 1u, put = in && slot >= 0 && slot < A.slots;
+      if (in && !put) set_error(err_dup, TQPK_EINVAL);
+      old[j] = put ? atomicCAS(&dir[slot], -1, (int)(r0 + j)) : -1;
     }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (old[j] != -1) set_error(err_dup, TQPK_EUNSUPPORTED);
   }
 }
 
@@ -266,6 +270,7 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
   const bool sentinel = (stages & 8) != 0;   // occupancy carried by the sums (see DenseSumSource)
   const bool bits = (stages & 16) != 0;      // membership bitmap in place of the row directory
   if (bits && (stages & 2)) return TQPK_EINVAL;
+  if ((stages & 32) && !bits) return TQPK_EINVAL;   // a caller-launched build writes the bitmap form
   if (stages & 1) {
   TQPK_CUDA(cudaMemsetAsync(L.groups, 0, 56, s));   // hdr[0..13]
   if (bits)
@@ -283,7 +288,9 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
     TQPK_CUDA(cudaMemsetAsync(L.sum, 0, slots * 8, s));
     TQPK_CUDA(cudaMemsetAsync(L.cnt, 0, slots * 4, s));
   }
-  if (bits) {                                        // also fills the sums: runs with no build rows too
+  if (bits && (stages & 32)) {
+    // the caller launches the build (tqpk_pipeline_join_words gives it the counters)
+  } else if (bits) {                                 // also fills the sums: runs with no build rows too
     timing_before(KID_PIPE_BUILD, s);
     k_pl_build_bits<<<grid_for(std::max<int64_t>((nb + 3) / 4, slots / 2), 8), kBlock, 0, s>>>(
         *pred_or_empty(h_build_pred), A, reinterpret_cast<unsigned*>(L.dir), L.sum, L.passing, L.err);
@@ -315,11 +322,11 @@ static int pipeline_join(int stages, const void* d_build_keys, int32_t build_dty
     O.emit_count = d_out_count;
     O.emit_sum = L.sum;
     O.emit_key_min = key_min;
+    O.err = L.err;                     // the single-launch top-k's bounded barrier reports here
     if (bits) {                        // occupancy also needs the slot's bit; the bit count checks the build
       src.bits = reinterpret_cast<const unsigned*>(L.dir);
       O.bits_set = reinterpret_cast<unsigned long long*>(L.top_count + 3);
       O.bits_expected = L.passing;
-      O.err = L.err;
     }
     timing_before(KID_PIPE_TOPK, s);
     int trc = topk_warp_launch(0, &src, k, grid, O, s);
@@ -367,6 +374,17 @@ extern "C" int tqpk_pipeline_join_tables(void* d_ws, size_t ws_bytes, int64_t ke
   *dir = L.dir;
   *sum = L.sum;
   *occ = L.cnt;
+  return TQPK_OK;
+}
+
+extern "C" int tqpk_pipeline_join_words(void* d_ws, size_t ws_bytes, int64_t key_min, int64_t key_max, int32_t** err,
+                                        uint64_t** passing) {
+  PipeLayout L;
+  if (!d_ws || !err || !passing || key_max < key_min ||
+      !pipe_layout(d_ws, ws_bytes, key_max - key_min + 1, topk_grid(), L))
+    return TQPK_EINVAL;
+  *err = L.err;
+  *passing = reinterpret_cast<uint64_t*>(L.passing);
   return TQPK_OK;
 }
 

@@ -49,18 +49,22 @@ __global__ void __launch_bounds__(kBlock) k_star_build(const __grid_constant__ t
     ld4_int(keys, dt, r0, n, kvec, x);
     int64_t pl[4] = {1, 1, 1, 1};
     if (mode == 1) ld4_int(payload, pdt, r0, n, false, pl);
+    int old[4];           // the four claims in flight together, their results read afterwards
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      if (r0 + j >= n) break;
       const int64_t slot = x[j] - kmin;
-      if (slot < 0 || slot >= slots) { set_error(err, TQPK_EINVAL); continue; }
+      const bool in = r0 + j < n, put = in && slot >= 0 && slot < slots;
+      if (in && !put) set_error(err, TQPK_EINVAL);
       // every dimension row claims its key (duplicates are errors); A rows failing
       // the predicate store 0 so the fact probe drops them
       // a payload outside int32 cannot name a C key (the C domain is int32): out-of-domain marker
       const int v = (mode == 0) ? (int)((b >> j) & 1u)
                                 : ((pl[j] <= (int64_t)INT32_MIN + 1 || pl[j] > INT32_MAX) ? INT32_MIN + 1 : (int)pl[j]);
-      if (atomicCAS(&dir[slot], INT32_MIN, v) != INT32_MIN) set_error(err, TQPK_EUNSUPPORTED);
+      old[j] = put ? atomicCAS(&dir[slot], INT32_MIN, v) : INT32_MIN;
     }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (old[j] != INT32_MIN) set_error(err, TQPK_EUNSUPPORTED);
   }
 }
 
@@ -281,6 +285,7 @@ extern "C" int tqpk_pipeline_star_agg_topk(
   TopkOut O{L.top_idx, L.top_count, L.cand_key, L.cand_idx, L.ticket, L.groups,
             reinterpret_cast<unsigned long long*>(L.top_count + 1),    // zeroed with the header
             reinterpret_cast<unsigned*>(L.top_count + 2)};
+  O.err = L.err;                       // the single-launch top-k (k <= 32) reports a barrier timeout here
   rc = topk_warp_launch(0, &src, k, grid, O, s);
   if (rc) return rc;
   k_star_emit<<<1, 256, 0, s>>>(L.top_idx, L.top_count, L.sum, L.cnt, c_min, k, d_out_keys, d_out_vals, d_out_counts,

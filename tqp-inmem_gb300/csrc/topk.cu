@@ -12,6 +12,21 @@ __device__ __forceinline__ bool ArraySource::get(int64_t i, uint64_t& k) const {
   return true;
 }
 
+// CTAs of k_tk_fused<Src> that fit on the device at once (the cooperative launch's limit).
+template <class Src>
+static int fused_capacity() {
+  static int cap = -1;
+  if (cap < 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tk_fused<Src>, 256, 0) != cudaSuccess) {
+      (void)cudaGetLastError();
+      per_sm = 0;
+    }
+    cap = per_sm * num_sms();
+  }
+  return cap;
+}
+
 template <int R, class Src>
 static int launch_r(const Src& src, int k, int grid, TopkOut O, cudaStream_t s) {
   (void)grid;
@@ -19,6 +34,20 @@ static int launch_r(const Src& src, int k, int grid, TopkOut O, cudaStream_t s) 
   int64_t G = 4;
   while (G * kTopkGroups < src.n) G <<= 1;
   const int ng = (int)std::max<int64_t>(1, (src.n + G - 1) / G);
+  if (R == 1 && G <= kTopkFusedMaxG && O.err && ng <= fused_capacity<Src>()) {
+    // one cooperative launch: all ng CTAs resident together, so the grid barrier inside completes
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.gridDim = dim3(ng);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    TQPK_CUDA(cudaLaunchKernelEx(&cfg, k_tk_fused<Src>, src, G, k, O, (int)kSpinLimit));
+    return TQPK_OK;
+  }
   k_tk_group_best<Src><<<ng, 256, 0, s>>>(src, G, k, O);
   TQPK_CHECK_LAUNCH();
   k_tk_filter<R, Src><<<ng, 256, 0, s>>>(src, G, k, O);     // the same groups

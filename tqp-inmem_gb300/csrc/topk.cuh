@@ -522,6 +522,91 @@ __global__ void __launch_bounds__(256) k_tk_filter(Src src, int64_t G, int k, To
   if (tk_last_cta(O.arrive + 1)) tk_final<R>(src, k, O);
 }
 
+// Both passes in one cooperative launch, for k <= 32 and groups of at most one tk_scan_group
+// sweep (G <= 4096 items: kTopkQuads quads per thread): each thread loads its items once and
+// keeps their keys in registers across a grid barrier, after which every CTA derives the cut from
+// the group bests (tk_bin_cut) and filters the keys it holds.  One launch and one pass over the
+// table instead of two.  The barrier wait is bounded: on expiry the CTA records TQPK_ETIMEOUT in
+// *O.err (required) and leaves.
+constexpr int64_t kTopkFusedMaxG = 4 * 256 * kTopkQuads;
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+template <class Src>
+__global__ void __launch_bounds__(256) k_tk_fused(Src src, int64_t G, int k, TopkOut O, int spin_limit) {
+  __shared__ uint64_t red[8];
+  __shared__ unsigned s_valid, s_bits;
+  __shared__ int s_fail;
+  const int lane = threadIdx.x & 31;
+  const int64_t b0 = (int64_t)blockIdx.x * G, b1 = b0 + G < src.n ? b0 + G : src.n;
+  if (threadIdx.x == 0) { s_valid = 0; s_bits = 0; s_fail = 0; }
+  __syncthreads();
+  uint64_t key[kTopkQuads][4];
+  unsigned ok[kTopkQuads];
+  unsigned valid = 0, nbits = 0;
+  const int64_t c0 = b0 + threadIdx.x * 4;
+#pragma unroll
+  for (int u = 0; u < kTopkQuads; ++u) {
+    const int64_t i0 = c0 + u * 1024;
+    ok[u] = 0;
+    if (i0 < b1) {
+      const unsigned tail = i0 + 4 <= b1 ? 0xfu : (1u << (b1 - i0)) - 1u;
+      ok[u] = src.get4(i0, key[u]) & tail;
+      if (O.bits_set) nbits += __popc(src.bits4(i0) & tail);
+    }
+  }
+  uint64_t best = ~0ull;
+#pragma unroll
+  for (int u = 0; u < kTopkQuads; ++u) {
+    valid += __popc(ok[u]);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (((ok[u] >> q) & 1u) && key[u][q] < best) best = key[u][q];
+  }
+  valid = __reduce_add_sync(0xffffffffu, valid);
+  nbits = __reduce_add_sync(0xffffffffu, nbits);
+  if (lane == 0) {
+    if (valid) atomicAdd(&s_valid, valid);
+    if (nbits) atomicAdd(&s_bits, nbits);
+  }
+  block_min_u64(best, red);
+  if (threadIdx.x == 0) {
+    O.cand_key[kTopkCap + blockIdx.x] = best;
+    if (blockIdx.x == 0) *O.ticket = 0;
+    if (s_valid && O.valid_total) atomicAdd(O.valid_total, (unsigned long long)s_valid);
+    if (s_bits && O.bits_set) atomicAdd(O.bits_set, (unsigned long long)s_bits);
+    // grid barrier: every CTA's group best (and the ticket reset) before any cut is taken
+    __threadfence();
+    atomicAdd(O.arrive, 1u);
+    int spins = 0;
+    while (ld_acquire_u32(O.arrive) < gridDim.x) {
+      if (++spins > spin_limit) { s_fail = 1; set_error(O.err, TQPK_ETIMEOUT); break; }
+      __nanosleep(64);
+    }
+  }
+  __syncthreads();
+  if (s_fail) return;
+  const uint64_t cut = tk_bin_cut((int)gridDim.x, k, O);
+#pragma unroll
+  for (int u = 0; u < kTopkQuads; ++u)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const bool pass = ((ok[u] >> q) & 1u) && key[u][q] <= cut;
+      const unsigned bal = __ballot_sync(0xffffffffu, pass);
+      if (!bal) continue;
+      unsigned at = 0;
+      if (lane == 0) at = atomicAdd(O.ticket, (unsigned)__popc(bal));
+      at = __shfl_sync(0xffffffffu, at, 0) + __popc(bal & ((1u << lane) - 1u));
+      if (pass && at < (unsigned)kTopkCap) {
+        O.cand_key[at] = key[u][q];
+        O.cand_idx[at] = c0 + u * 1024 + q;
+      }
+    }
+  if (tk_last_cta(O.arrive + 1)) tk_final<1>(src, k, O);
+}
+
 // Host launcher: k <= 256.  The cand arrays hold topk_cand_entries(k) entries each;
 // O.ticket, O.bound, O.arrive[0..1], O.valid_total and O.bits_set must be zero before the call.
 int topk_warp_launch(int kind, const void* src, int k, int grid, TopkOut O, cudaStream_t s);

@@ -136,6 +136,7 @@ SIGNATURES = {
                                                      _P(Predicate), _P(GroupbySpec), _I32, _I32, _I32, _VP, _SZ, _VP,
                                                      _VP, _VP, _VP, _VP]),
     "tqpk_pipeline_join_tables": (C.c_int, [_VP, _SZ, _I64, _I64, _P(_VP), _P(_VP), _P(_VP)]),
+    "tqpk_pipeline_join_words": (C.c_int, [_VP, _SZ, _I64, _I64, _P(_VP), _P(_VP)]),
     "tqpk_directory_build": (C.c_int, [_VP, _I32, _I64, _P(Predicate), _VP, _I32, _I64, _I64, _I32, _I32, _VP, _VP,
                                        _VP]),
     "tqpk_directory_build_next": (C.c_int, [_VP, _I32, _I64, _P(Predicate), _VP, _I32, _I64, _I64, _I32, _I32,

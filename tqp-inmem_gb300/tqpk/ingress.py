@@ -61,28 +61,30 @@ class ColumnStager:
               mem_pool=None) -> Dict[int, Variable]:
         main = torch.cuda.current_stream(self.device)
         ids = list(order or []) + [c for c in host if c not in set(order or [])]
-        dst, ptrs = {}, {}
+        pool = mem_pool if mem_pool is not None and hasattr(mem_pool, "malloc_like") else None
+        # The side stream waits once for the work queued on `main` so far: memory the allocator
+        # hands out below may have been used by it.  Each column is allocated (on `main`) right
+        # before its copy is queued, so the first copy starts after one allocation, not all.
+        self.stream.wait_stream(main)
+        out = {}
         for c in ids:
             h = host[c]
-            if mem_pool is not None and hasattr(mem_pool, "malloc_like"):
-                ptrs[c], dst[c] = mem_pool.malloc_like(torch.empty(h.shape, dtype=h.dtype, device=self.device))
+            ptr = None
+            if pool is not None:
+                ptr, d = pool.malloc_like(torch.empty(h.shape, dtype=h.dtype, device=self.device))
             else:
-                dst[c] = torch.empty(h.shape, dtype=h.dtype, device=self.device)
-        self.stream.wait_stream(main)           # the buffers were allocated (and maybe used) on `main`
-        out = {}
-        with torch.cuda.stream(self.stream):
-            for c in ids:
-                h = host[c]
-                if not h.is_pinned():
-                    h = h.pin_memory()
-                dst[c].copy_(h, non_blocking=True)
-                dst[c].record_stream(self.stream)
-                ev = torch.cuda.Event()
+                d = torch.empty(h.shape, dtype=h.dtype, device=self.device)
+            if not h.is_pinned():
+                h = h.pin_memory()
+            ev = torch.cuda.Event()
+            with torch.cuda.stream(self.stream):
+                d.copy_(h, non_blocking=True)
                 ev.record(self.stream)
-                v = Variable(dst[c], types[c], ready=ev)
-                if c in ptrs:
-                    v.backing_mem_ptr = ptrs[c]
-                out[c] = v
+            d.record_stream(self.stream)
+            v = Variable(d, types[c], ready=ev)
+            if ptr is not None:
+                v.backing_mem_ptr = ptr
+            out[c] = v
         return out
 
 

@@ -1054,6 +1054,82 @@ def join_probe_args(a: "_Args", spec, pred, bpred, fk, np_: int, key_min: int, s
     return a
 
 
+def join_build_bits_source(pred) -> Tuple[str, str]:
+    """CUDA source of the fused join's build stage in the membership-bitmap form, the build
+    predicate compiled in (the library's k_pl_build_bits interprets it: ~110 instructions a row):
+    every group sum set to -0.0 (the empty marker), one `red.or` per passing build row into the
+    bitmap (bit s of word s / 32 for key key_min + s), the passing rows counted (one atomic per
+    CTA), an out-of-domain key reported as TQPK_EINVAL (-1) in *err.  A repeated key shows later
+    as fewer bits set than rows counted (the top-k's check)."""
+    pcols, pexpr = _pred_code(pred, "p") if pred is not None else ([], "true")
+    name = "tqpk_q_join_build_bits"
+    params = [f"const void* __restrict__ pp{c}" for c in range(pred.n_cols if pred is not None else 0)]
+    params += ["const PL lp", "const void* __restrict__ bk", "int bk_dt", "i64 nb", "i64 key_min", "i64 slots",
+               "unsigned* __restrict__ bits", "double* __restrict__ sum", "u64* __restrict__ passing",
+               "int* __restrict__ err", "int vp", "int vk"]
+    key_load = ("const V4<i64> K = (bk_dt == 4) ? ld4((const long long*)bk, r0, nb, vk != 0) : "
+                "[&]{ V4<int> t = ld4((const int*)bk, r0, nb, vk != 0); V4<i64> o; "
+                "for (int q = 0; q < 4; ++q) o.v[q] = t.v[q]; return o; }();")
+    src = [PRELUDE,
+           "__device__ __forceinline__ void gred_or(unsigned* p, unsigned v) {",
+           '  asm volatile("red.global.or.b32 [%0], %1;" :: "l"(__cvta_generic_to_global(p)), "r"(v) : "memory");',
+           "}",
+           f'extern "C" __global__ void __launch_bounds__(256) {name}(',
+           "    " + ",\n    ".join(params) + ") {",
+           "  __shared__ unsigned s_pass;",
+           "  if (threadIdx.x == 0) s_pass = 0;",
+           "  const i64 tid = blockIdx.x * (i64)blockDim.x + threadIdx.x, nthr = (i64)gridDim.x * blockDim.x;",
+           "  {  // the sums start at -0.0, 16-byte stores",
+           "    const double e = __longlong_as_double((long long)0x8000000000000000ull);",
+           "    const bool v2 = (reinterpret_cast<unsigned long long>(sum) & 15u) == 0;",
+           "    const i64 pairs = v2 ? slots / 2 : 0;",
+           "    for (i64 i = tid; i < pairs; i += nthr) reinterpret_cast<double2*>(sum)[i] = make_double2(e, e);",
+           "    for (i64 i = 2 * pairs + tid; i < slots; i += nthr) sum[i] = e;",
+           "  }",
+           "  __syncthreads();",
+           "  unsigned npass = 0;",
+           "  for (i64 g = tid; g < ((nb + 3) >> 2); g += nthr) {",
+           "    const i64 r0 = g << 2;"]
+    src += ["    " + l for l in _load_lines(pcols, pred.dtypes, "P", "pp", "nb", "vp != 0")] if pred is not None else []
+    src += ["    " + key_load,
+            "#pragma unroll",
+            "    for (int j = 0; j < 4; ++j) {",
+            f"      if (r0 + j >= nb || !({_rename(pexpr, 'p', 'P')})) continue;",
+            "      const i64 slot = K.v[j] - key_min;",
+            "      if (slot < 0 || slot >= slots) { atomicCAS(err, 0, -1); continue; }",
+            "      gred_or(&bits[slot >> 5], 1u << (slot & 31));",
+            "      ++npass;",
+            "    }",
+            "  }",
+            "  npass = __reduce_add_sync(0xffffffffu, npass);",
+            "  if ((threadIdx.x & 31) == 0 && npass) atomicAdd(&s_pass, npass);",
+            "  __syncthreads();",
+            "  if (threadIdx.x == 0 && s_pass) atomicAdd(passing, (u64)s_pass);",
+            "}"]
+    return "\n".join(src), name
+
+
+def join_build_bits_args(a: "_Args", pred, bk, nb: int, key_min: int, slots: int, bits_ptr: int, sum_ptr: int,
+                         passing_ptr: int, err_ptr: int, pred_tensors=()):
+    """Parameters of join_build_bits_source's kernel, in order."""
+    if pred is not None:
+        for c in range(pred.n_cols):
+            a.ptr(pred.cols[c])
+    a.blob(pred_lits(pred))
+    a.ptr(bk.data_ptr() if nb else None)
+    a.i32(L.I64 if bk.dtype.itemsize == 8 else L.I32)
+    a.i64(nb)
+    a.i64(key_min)
+    a.i64(slots)
+    a.ptr(bits_ptr)
+    a.ptr(sum_ptr)
+    a.ptr(passing_ptr)
+    a.ptr(err_ptr)
+    a.i32(_aligned(*pred_tensors) if pred is not None else 1)
+    a.i32(_aligned(bk))
+    return a
+
+
 # ---------------------------------------------------------------------------- star probe
 def star_probe_source(spec, val_reg: int, fpred, apred, U: int = PROBE_U, min_blocks: int = 0,
                       early_fb: bool = False, stream_cs: bool = False, composed: bool = False,

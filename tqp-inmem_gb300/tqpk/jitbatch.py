@@ -318,12 +318,16 @@ def _join_functions(p: int, spec, val_reg: int, ppred, bpred) -> str:
     src += ["    const V4<i64> BK = (I.bk_dt == 4) ? ld4((const long long*)I.kc[1], r0, n, false) : "
             "[&]{ V4<int> t = ld4((const int*)I.kc[1], r0, n, false); V4<i64> o; "
             "for (int q = 0; q < 4; ++q) o.v[q] = t.v[q]; return o; }();",
-            "#pragma unroll", "    for (int j = 0; j < 4; ++j) {", "      if (r0 + j >= e) break;",
-            f"      if (!({jit._rename(bexpr, 'p', 'P')})) continue;",
+            "    int old[4];       // the four claims in flight together, their results read afterwards",
+            "#pragma unroll", "    for (int j = 0; j < 4; ++j) {",
+            f"      const bool in = r0 + j < e && ({jit._rename(bexpr, 'p', 'P')});",
             "      const i64 slot = BK.v[j] - kmin;",
-            "      if (slot < 0 || slot >= slots) { set_err(err, -1); continue; }",
-            "      if (atomicCAS(&I.dir[slot], -1, (int)(r0 + j)) != -1) set_err(err, -7);",
-            "    }", "  }", "}"]
+            "      const bool put = in && slot >= 0 && slot < slots;",
+            "      if (in && !put) set_err(err, -1);",
+            "      old[j] = put ? atomicCAS(&I.dir[slot], -1, (int)(r0 + j)) : -1;",
+            "    }",
+            "#pragma unroll", "    for (int j = 0; j < 4; ++j) if (old[j] != -1) set_err(err, -7);",
+            "  }", "}"]
     # probe: predicate, lookup, warp-dense value pass
     pcols, pexpr = jit._pred_code(ppred, "p") if ppred is not None else ([], "true")
     plit, pexpr = _hoist(pexpr, "I")

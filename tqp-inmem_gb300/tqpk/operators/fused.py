@@ -23,7 +23,9 @@ Recognised shape (the plan main.py:152-253 runs for a filtered equi-join + aggre
 It runs as tqpk.pipeline.JoinAggTopK: the build side's membership bitmap, one probe pass that
 accumulates the sums in a slot table, one top-k pass.  Its outputs are the take-ordered
 operator's: the key column ([m, 1], the build key's dtype and type) and the sum column (float64)
-in the stable order of the operator path (sum, then ascending key).  The intermediate columns of
+in the stable order of the operator path (sum, then ascending key); each output also carries `host`,
+its rows as a numpy array, brought back by the same device-to-host read as the row count
+(tqpk.variable.host_values reads it).  The intermediate columns of
 the run (the filters' masks, the joined columns, the full group table) are not produced; the
 plan's later operators only read the take-ordered operator's outputs in this shape.
 
@@ -189,8 +191,10 @@ def _run_join_agg_topk(tensor_group, m) -> bool:
         keys, vals, count = pipe.result_device(key_dtype=bv.tensor.dtype)   # cast queued before the read
     except NotImplementedError:                      # a repeated build key: the operator path runs instead
         return False
-    tensor_group[m["key_out"]] = make_like(bv, keys.reshape(count, 1), bv.tensor_type)
-    tensor_group[m["agg_out"]] = make_like(bv, vals, "float")
+    tensor_group[m["key_out"]] = kv = make_like(bv, keys.reshape(count, 1), bv.tensor_type)
+    tensor_group[m["agg_out"]] = sv = make_like(bv, vals, "float")
+    hk, hs = pipe.result_host                         # read together with the count
+    kv.host, sv.host = hk.reshape(count, 1), hs
     return True
 
 

@@ -34,6 +34,7 @@ from .predicate import compile_filter
 JOIN_DIR_BITS = True
 JOIN_BITS_MAX_BYTES = 256 << 10
 JOIN_SHARED_PERCENT = None
+JOIN_JIT_BUILD = True         # the bitmap build with its predicate compiled in (tqpk.jit.join_build_bits_source)
 
 
 class JoinAggTopK:
@@ -130,6 +131,30 @@ class JoinAggTopK:
         jit.launch(self._probe_handle, self._probe_grid, 256, self._probe_smem, self._probe_args, s,
                    L.KID_PIPE_PROBE)
 
+    def _jit_build(self, s):
+        """The membership-bitmap build as a query-specialised kernel (stage bit 5: the library's
+        reset stage clears the header and the bitmap, this kernel does the rest)."""
+        from . import jit
+        if not hasattr(self, "_build_handle"):
+            bp = self.bpred.struct if self.bpred else None
+            src, name = jit.join_build_bits_source(bp)
+            self._build_handle = jit.compile_kernel(src, name)
+            d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
+            L.check(self.lib.tqpk_pipeline_join_tables(self.ws.data_ptr(), self.ws.numel(), self.key_min,
+                                                       self.key_max, C.byref(d), C.byref(su), C.byref(oc)),
+                    "tqpk_pipeline_join_tables")
+            er, ps = C.c_void_p(), C.c_void_p()
+            L.check(self.lib.tqpk_pipeline_join_words(self.ws.data_ptr(), self.ws.numel(), self.key_min,
+                                                      self.key_max, C.byref(er), C.byref(ps)),
+                    "tqpk_pipeline_join_words")
+            slots = self.key_max - self.key_min + 1
+            self._build_args = jit.join_build_bits_args(
+                jit._Args(), bp, self.bk, self.bk.numel(), self.key_min, slots, d.value, su.value, ps.value, er.value,
+                pred_tensors=self.bpred.tensors if self.bpred else ())
+            self._build_grid = jit.occupancy_grid(self._build_handle, 256, 0,
+                                                  max((self.bk.numel() + 3) // 4, slots // 2, 1))
+        jit.launch(self._build_handle, self._build_grid, 256, 0, self._build_args, s, L.KID_PIPE_BUILD)
+
     def run(self, stream=None, before_probe=None):
         """Queues the whole query on `stream` (default: the current stream).  before_probe, when
         given, is called between the build stage and the probe (e.g. to make the stream wait for
@@ -141,7 +166,11 @@ class JoinAggTopK:
                 and not has_strings(self.ppred.struct if self.ppred else None)):
             sent = 0 if self._tma_ok() else 8      # the generated register probe keeps occupancy in the sums
             bits = 16 if self._probe_uses_bits() else 0   # the build stage writes the membership bitmap
-            self._stages(1 | sent | bits, s)
+            if bits and JOIN_JIT_BUILD and not has_strings(self.bpred.struct if self.bpred else None):
+                self._stages(1 | sent | bits | 32, s)      # reset only; the generated build follows
+                self._jit_build(s)
+            else:
+                self._stages(1 | sent | bits, s)
             if before_probe is not None:
                 before_probe()
             self._jit_probe(s)
@@ -156,23 +185,28 @@ class JoinAggTopK:
     def result_device(self, key_dtype=None):
         """(keys [m], sums float64[m], m) as device tensors after the last run, with one host
         read (the count and the error word together); keys as int64, or cast on the device to
-        key_dtype before that read.  A repeated build key raises NotImplementedError
-        (TQPK_EUNSUPPORTED), an out-of-domain one ValueError."""
-        import ctypes
-        d, su, oc = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        key_dtype before that read.  The same read brings the k result rows to pinned host
+        memory: `result_host` is then (keys, sums) as numpy arrays of m rows.  A repeated build
+        key raises NotImplementedError (TQPK_EUNSUPPORTED), an out-of-domain one ValueError."""
         if getattr(self, "_probe_smem", 0):
             self.check_error()                      # the TMA-staged probe keeps its own error word
         keys = self.out_keys if key_dtype in (None, torch.int64) else self.out_keys.to(key_dtype)
         if not hasattr(self, "_hdr_host"):
             self._hdr_host = torch.empty(16, dtype=torch.int32, pin_memory=True)
+            self._vals_host = torch.empty(self.k, dtype=torch.float64, pin_memory=True)
+        if getattr(self, "_keys_host", None) is None or self._keys_host.dtype != keys.dtype:
+            self._keys_host = torch.empty(self.k, dtype=keys.dtype, pin_memory=True)
         hdr = self._hdr_host
         cur = torch.cuda.current_stream(self.dev)
         hdr[:4].copy_(self.ws[:16].view(torch.int32), non_blocking=True)       # hdr[2] = error word
         hdr[4:6].copy_(self.out_count.view(torch.int32), non_blocking=True)
+        self._keys_host.copy_(keys, non_blocking=True)
+        self._vals_host.copy_(self.out_vals, non_blocking=True)
         cur.synchronize()
         err, m = int(hdr[2]), int(hdr[4:6].view(torch.int64)[0])
         if err:
             L.check(err, "fused join pipeline (repeated or out-of-domain build key)")
+        self.result_host = (self._keys_host[:m].numpy().copy(), self._vals_host[:m].numpy().copy())
         return keys[:m], self.out_vals[:m], m
 
 

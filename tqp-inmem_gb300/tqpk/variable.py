@@ -60,6 +60,15 @@ def wait_ready(*variables) -> None:
             torch.cuda.current_stream(v.tensor.device).wait_event(ev)
 
 
+def host_values(v):
+    """A column's rows as a numpy array: the copy its producer already brought to the host with
+    its own result read (`host`, set by the fused pipelines), else one device-to-host copy."""
+    h = getattr(v, "host", None)
+    if h is not None and tuple(h.shape) == tuple(v.tensor.shape):
+        return h
+    return v.tensor.cpu().numpy()
+
+
 def torch_to_type(dtype) -> str:
     """variable.py:45-52"""
     if dtype == float_dtype:

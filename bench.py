@@ -88,6 +88,14 @@ class JoinAggTop10:
             "build_filter": f"date < {datagen.BUILD_DATE_LT}", "probe_filter": f"date > {datagen.PROBE_DATE_GT}",
             "k": 10, "key_dtype": "int32", "l2": "flushed between steps (256 MB write)",
         }
+        self.set_args()
+        self.cols = {11: self.t["b_key"], 12: self.t["b_date"], 21: self.t["p_fk"], 22: self.t["p_date"],
+                     23: self.t["p_price"], 24: self.t["p_discount"]}
+        self.types = {11: "int", 12: "date", 21: "int", 22: "date", 23: "float", 24: "float"}
+
+    def set_args(self):
+        """The operators' argument dicts of the query."""
+        from tqpk import datagen
         self.f1 = {"filter tree": [["bd#12", "<", str(datagen.BUILD_DATE_LT)]], "materialized in": [12],
                    "out mask id": 901}
         self.f2 = {"filter tree": [["pd#22", ">", str(datagen.PROBE_DATE_GT)]], "materialized in": [22],
@@ -99,9 +107,6 @@ class JoinAggTop10:
                       "results": ["k#11", [[["sum", self.value_tree], "#", "301"], "AS", "rev#302"]],
                       "out agg ids": [302]}
         self.targs = {"limit": 10, "input ids": [11, 302], "key ids": [302], "key orders": [True]}
-        self.cols = {11: self.t["b_key"], 12: self.t["b_date"], 21: self.t["p_fk"], 22: self.t["p_date"],
-                     23: self.t["p_price"], 24: self.t["p_discount"]}
-        self.types = {11: "int", 12: "date", 21: "int", 22: "date", 23: "float", 24: "float"}
 
     # algorithmic bytes: every input column read once, the outputs written once
     def algorithmic_bytes(self):
@@ -589,6 +594,8 @@ class Batched:
                                                {22: d["p_date"], 23: d["p_price"], 24: d["p_discount"]},
                                                [["pd#22", ">", "1170"]], [["p#23", "*", ["1.0", "-", "d#24"]]], k=10))
                 self.plain_args.append(("join", d))
+        # every instance's input columns, each read once by the batch
+        self.input_bytes = sum(t.numel() * t.element_size() for _, d in self.plain_args for t in d.values())
         from tqpk import jit
         if jit.available():
             from tqpk.jitbatch import QueryBatch
@@ -599,6 +606,57 @@ class Batched:
 
     def run_batched(self):
         self.batch.replay()
+
+    def cpu_baseline(self, budget_s: float):
+        """TQP-Inmem's operators on their CPU path (torch CPU, every host core) over the instances
+        in order until budget_s is spent, as rows/s of that sample, turned into queries/s of the
+        64-instance mix (its total rows at that rate).  None with the reason when the reference is
+        not available."""
+        import torch
+        R, why = reference_modules()
+        if R is None:
+            return {"unavailable": why}
+        from oracle import reference
+        torch.set_num_threads(os.cpu_count() or 1)
+        pool = reference.CpuPool()
+        done_rows, spent, done = 0, 0.0, 0
+        with reference.cpu_mode():
+            for sp, (kind, d) in zip(self.specs, self.plain_args):
+                if spent >= budget_s:
+                    break
+                cols = {c: t.cpu().numpy() for c, t in d.items()}
+                t0 = time.perf_counter()
+                if kind == "groupby":
+                    types = {c: "float" if c <= 4 else ("date" if c == 7 else "int") for c in cols}
+                    tg = _ref_tensor_group(R, cols, types)
+                    R.filter.tqp_filter(False, tg, {"filter tree": [["ship_date#7", "<=", "2470"]],
+                                                    "materialized in": [7], "out mask id": 900}, None, None, pool, "f")
+                    R.aggregate.tqp_hash_aggregate(False, tg, {"is partial": False, "keys": ["flag#5", "status#6"],
+                                                               "input ids": [1, 2, 3, 4, 5, 6], "results": self.AGG,
+                                                               "out agg ids": list(self.AGG_IDS),
+                                                               "mask map": {c: 900 for c in range(1, 7)}},
+                                                   pool, None, "a")
+                    rows = sp["rows"]
+                else:
+                    j = object.__new__(JoinAggTop10)        # this instance's tables, the query's arguments
+                    j.set_args()
+                    j.cols = {11: cols["b_key"], 12: cols["b_date"], 21: cols["p_fk"], 22: cols["p_date"],
+                              23: cols["p_price"], 24: cols["p_discount"]}
+                    j.types = {11: "int", 12: "date", 21: "int", 22: "date", 23: "float", 24: "float"}
+                    tg = _ref_tensor_group(R, j.cols, j.types)
+                    torch.manual_seed(0)
+                    j.ref_plan(R, tg, pool, False, lambda: None)
+                    rows = sp["rows"] + sp["groups"]
+                spent += time.perf_counter() - t0
+                done_rows += rows
+                done += 1
+        rate = done_rows / spent
+        total = sum(sp["rows"] + (sp["groups"] if sp["kind"] == "join" else 0) for sp in self.specs)
+        return {"value": len(self.specs) / (total / rate), "unit": "queries/s", "cores": torch.get_num_threads(),
+                "kind": "reference",
+                "sample": f"the first {done} of the {len(self.specs)} instances ({done_rows} rows, {spent:.1f} s) through "
+                          f"TQP-Inmem's operators (oracle/_ref), gpu_enable=False, torch {torch.__version__} CPU: "
+                          f"{rate:.3g} rows/s, scaled to the mix's {total} rows"}
 
     def run_plain(self):
         """Every instance alone through the drop-in operators (the reference's per-operator path)."""
@@ -699,13 +757,39 @@ def run_batched_bench(args):
         plain_times.append(time.perf_counter() - t0)
     plain_s = statistics.median(plain_times)
     n = len(w.specs)
+    # end to end: the replay and every instance's result rows read back (two device-to-host reads);
+    # the tables stay resident, as in the serving loop
+    e2e, d2h = None, 0
+    if hasattr(w.batch, "results_host"):
+        ts = []
+        for _ in range(max(3, min(args.steps, 10))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            w.run_batched()
+            res, d2h = w.batch.results_host()
+            ts.append(time.perf_counter() - t0)
+        w.compare(plain_res, res)
+        e2e_s = statistics.median(ts)
+        e2e = {"value": n / e2e_s, "unit": "queries/s", "ms_per_step": e2e_s * 1e3, "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": d2h,
+               "path": "graph replay + every instance's result rows to pinned host memory; tables resident"}
+    kernel_s = kms.value / max(kn.value, 1) / 1000.0
+    peak, peak_src = peak_gbs()
+    achieved = w.input_bytes / kernel_s / 1e9
+    cpu = w.cpu_baseline(budget_s=12.0)
     line = {"metric": "queries/s", "value": n / (batched_ms / 1000.0), "unit": "queries/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": dict(w.config, plain_queries_per_s=n / plain_s, speedup_vs_plain=(n / (batched_ms / 1000.0)) /
                            (n / plain_s), batched_rows_per_s=w.fact_rows / (batched_ms / 1000.0),
-                           kernel_ms=kms.value / max(kn.value, 1)),
-            "clocks": clocks, "gpu_launches": launches}
+                           kernel_ms=kernel_s * 1e3),
+            "roofline": {"bound": "hbm", "kernel": "tqpk_qb_run", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": w.input_bytes,
+                         "launches": kn.value, "avg_launch_us": kernel_s * 1e6,
+                         "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                         else "fallback 6.8 TB/s",
+                         "note": "every instance's input columns read once per launch"},
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "gpu_launches": launches}
     return line
 
 

@@ -112,6 +112,10 @@ def test_batch_uneven_instances_vs_oracle(impl):
     for _ in range(2):                          # graph replays give the same results
         b.replay()
         check(b.results(), expected)
+    if hasattr(b, "results_host"):              # the two-read form returns the same rows
+        res, nbytes = b.results_host()
+        check(res, expected)
+        assert nbytes > 0
 
 
 @pytest.mark.parametrize("impl", ["library", "generated"])

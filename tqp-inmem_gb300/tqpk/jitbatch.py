@@ -488,6 +488,23 @@ __device__ void jn_topk_merge(const QInst& I, u64* sk, i64* si) {
 """
 
 
+# result packing: span i copies desc[3i+1] bytes from address desc[3i] to out + desc[3i+2]
+# (sources 256-byte aligned allocations, offsets multiples of 16: 16-byte pieces, then bytes)
+_PACK_SRC = r"""
+extern "C" __global__ void tqpk_pack_spans(const long long* __restrict__ desc, int n, unsigned char* __restrict__ out) {
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x, nt = (long long)gridDim.x * blockDim.x;
+  for (int i = 0; i < n; ++i) {
+    const unsigned char* src = (const unsigned char*)desc[3 * i];
+    const long long nb = desc[3 * i + 1];
+    unsigned char* dst = out + desc[3 * i + 2];
+    const long long n16 = nb >> 4;
+    for (long long j = tid; j < n16; j += nt) ((uint4*)dst)[j] = ((const uint4*)src)[j];
+    for (long long j = (n16 << 4) + tid; j < nb; j += nt) dst[j] = src[j];
+  }
+}
+"""
+
+
 def batch_source(gb_progs, join_progs) -> str:
     """gb_progs: [(spec, pred, outputs)], join_progs: [(spec, val_reg, ppred, bpred)]."""
     parts = [jit.PRELUDE, _BATCH_PRELUDE, _struct_c(), _GENERIC]
@@ -848,6 +865,89 @@ class QueryBatch:
         err = int(self.ctl[4:8].view(torch.int32).item())
         if err:
             L.check(err, "batched run")
+
+    def results_host(self):
+        """results() with two device-to-host reads in all: every instance's row and group counts
+        (and the error word) packed into one copy; then one generated kernel packs every result
+        row (each column's first rows, 16-byte aligned spans) and one copy brings them to pinned
+        memory.  Returns (results, bytes read); the arrays are views of that pinned buffer, valid
+        until the next call (copy what is kept longer)."""
+        if not hasattr(self, "_span_cols"):
+            self._count_src, self._span_cols = [self.ctl[4:8].view(torch.int32).to(torch.int64)], []
+            for o in self.outs:             # (tensor, index of its row count in the packed counts)
+                if o["kind"] == "join":
+                    at = len(self._count_src)
+                    self._count_src += [o["count"], o["groups"]]
+                    self._span_cols += [(o["keys"], at), (o["vals"], at)]
+                else:
+                    at = len(self._count_src)
+                    self._count_src.append(o["groups"])
+                    self._span_cols += [(t, at) for t in list(o["keys"]) + list(o["outs"])]
+            self._span_src = np.array([t.data_ptr() for t, _ in self._span_cols], dtype=np.int64)
+            self._span_es = np.array([t.element_size() for t, _ in self._span_cols], dtype=np.int64)
+            self._span_at = np.array([at for _, at in self._span_cols], dtype=np.int64)
+            self._k_pack = jit.compile_kernel(_PACK_SRC, "tqpk_pack_spans")
+        st = torch.cuda.current_stream(self.dev)
+        self._count_src[0] = self.ctl[4:8].view(torch.int32).to(torch.int64)   # the error word, this run
+        counts = torch.cat(self._count_src)
+        hc = self._pinned("counts", counts.numel(), torch.int64)
+        hc.copy_(counts, non_blocking=True)
+        st.synchronize()
+        c = hc.numpy().copy()
+        if c[0]:
+            L.check(int(c[0]), "batched run")
+        rows = c[self._span_at]
+        nbytes = rows * self._span_es
+        offs = np.zeros(len(nbytes), dtype=np.int64)
+        if len(nbytes) > 1:
+            offs[1:] = np.cumsum((nbytes + 15) // 16 * 16)[:-1]
+        total = int(offs[-1] + nbytes[-1]) if len(nbytes) else 0
+        desc = self._pinned("desc", 3 * len(nbytes), torch.int64)
+        dn = desc.numpy().reshape(-1, 3)
+        dn[:, 0], dn[:, 1], dn[:, 2] = self._span_src, nbytes, offs
+        ddesc = self._device_buf("desc", desc.numel() * 8).view(torch.int64)
+        ddesc.copy_(desc, non_blocking=True)
+        packed = self._device_buf("rows", max(total, 16))
+        a = jit._Args()
+        a.ptr(ddesc.data_ptr())
+        a.i32(len(nbytes))
+        a.ptr(packed.data_ptr())
+        jit.launch(self._k_pack, max(1, min(4 * 152, (total // 16 + 255) // 256)), 256, 0, a, st.cuda_stream)
+        hp = self._pinned("rows", total, torch.uint8)
+        hp.copy_(packed[:total], non_blocking=True)
+        st.synchronize()
+        buf = hp.numpy()
+        arrays = [buf[o:o + n].view(np.dtype(str(t.dtype).replace("torch.", "")))
+                  for (t, _), o, n in zip(self._span_cols, offs.tolist(), nbytes.tolist())]
+        res, i, pos = [], 0, 1
+        for o in self.outs:
+            if o["kind"] == "join":
+                res.append((arrays[i], arrays[i + 1], int(c[pos + 1])))
+                i += 2
+                pos += 2
+            else:
+                nk = len(o["keys"])
+                keys = arrays[i:i + nk]
+                i += nk
+                outs = {oid: arr for (oid, *_), arr in zip(o["prog"].outputs, arrays[i:i + len(o["outs"])])}
+                i += len(o["outs"])
+                res.append((outs, keys, int(c[pos])))
+                pos += 1
+        return res, int(counts.numel() * 8 + total)
+
+    def _device_buf(self, name, nbytes):
+        bufs = self.__dict__.setdefault("_dev_bufs", {})
+        b = bufs.get(name)
+        if b is None or b.numel() < nbytes:
+            b = bufs[name] = torch.empty(max(nbytes, 1 << 16), dtype=torch.uint8, device=self.dev)
+        return b[:nbytes]
+
+    def _pinned(self, name, n, dtype):
+        bufs = self.__dict__.setdefault("_host_bufs", {})
+        b = bufs.get(name)
+        if b is None or b.numel() < n or b.dtype != dtype:
+            b = bufs[name] = torch.empty(max(n, 1024), dtype=dtype, pin_memory=True)
+        return b[:n]
 
     def results(self):
         self.check_error()

@@ -75,3 +75,63 @@ def test_float_build_keys_and_cpu_columns_run_nothing():
     tg, ops, args = plan()
     assert try_fused(True, tg, ops, args, 0) == 0          # CPU tensors: the operators run
     assert try_fused(False, tg, ops, args, 0) == 0
+
+
+def star_plan():
+    """The star query as the plan executor holds it: Filter(A), three joins, Aggregate by the C
+    key (sum and count), take ordered."""
+    ops = [3, 4, 5, 6, 7, 8]
+    args = {
+        3: {"name": "Filter", "filter tree": [["cat#32", "=", "1"]], "materialized in": [32], "out mask id": 901},
+        4: {"name": "Join", "left keys": [31], "right keys": [41], "join type": "Inner", "left group": [31, 32],
+            "right group": [41, 42, 43, 44], "materialized in": [31, 41, 42, 43, 44], "mask map": {31: 901}},
+        5: {"name": "Join", "left keys": [51], "right keys": [42], "join type": "Inner", "left group": [51, 52],
+            "right group": [31, 41, 42, 43, 44], "materialized in": [51, 52, 42, 43, 44]},
+        6: {"name": "Join", "left keys": [61], "right keys": [52], "join type": "Inner", "left group": [61],
+            "right group": [51, 52, 42, 43, 44], "materialized in": [61, 52, 43, 44]},
+        7: {"name": "Aggregate", "is partial": False, "keys": ["c#61"], "input ids": [61, 43, 44],
+            "results": ["c#61", [[["sum", [["p#43", "*", ["1.0", "-", "d#44"]]]], "#", "71"], "AS", "rev#72"],
+                        [[["count", ["1"]], "#", "73L"], "AS", "cnt#74"]], "out agg ids": [72, 74]},
+        8: {"name": "take ordered", "limit": 100, "input ids": [61, 72, 74], "key ids": [72], "key orders": [True]},
+    }
+    i32 = lambda n: Variable(torch.arange(1, n + 1, dtype=torch.int32), "int")  # noqa: E731
+    tg = {31: i32(8), 32: Variable(torch.ones(8, dtype=torch.uint8), "int"), 41: i32(20), 42: i32(20),
+          43: Variable(torch.ones(20, dtype=torch.float64), "float"),
+          44: Variable(torch.zeros(20, dtype=torch.float64), "float"), 51: i32(10), 52: i32(10), 61: i32(5)}
+    return tg, ops, args
+
+
+def test_recognises_the_star_plan():
+    from tqpk.operators.fused import _match_star_agg_topk
+    tg, ops, args = star_plan()
+    assert _match_join_agg_topk(tg, ops, args, 0) is None
+    m = _match_star_agg_topk(tg, ops, args, 0)
+    assert m is not None and m["n_ops"] == 6
+    assert m["keys"] == (31, 41, 51, 42, 61, 52) and set(m["filters"]) == {"a"}
+    assert (m["k"], m["desc"], m["key_out"], m["agg_out"], m["cnt_out"], m["vcols"]) == (100, True, 61, 72, 74, [43, 44])
+    a = copy.deepcopy(args)                       # without the count
+    a[7]["results"].pop()
+    a[7]["out agg ids"] = [72]
+    a[8]["input ids"] = [61, 72]
+    m = _match_star_agg_topk(tg, ops, a, 0)
+    assert m is not None and m["cnt_out"] is None
+
+
+@pytest.mark.parametrize("change", [
+    lambda a: a[5].update({"right keys": [31]}),          # B joined on A's key, not a fact column
+    lambda a: a[6].update({"right keys": [42]}),          # C joined on a fact column, not B's
+    lambda a: a[6].update({"join type": "LeftOuter"}),
+    lambda a: a[5].update({"mask map": {51: 901}}),
+    lambda a: a[7].update({"keys": ["b#51"]}),
+    lambda a: a[7]["results"].append([[["sum", ["p#43"]], "#", "75"], "AS", "s#76"]),
+    lambda a: a[7]["results"].__setitem__(1, [[["sum", ["b#52"]], "#", "71"], "AS", "rev#72"]),
+    lambda a: a[8].update({"input ids": [61, 72]}),
+    lambda a: a[8].update({"limit": 1000}),
+    lambda a: a[3].update({"materialized in": [43]}),
+])
+def test_other_star_shapes_are_left_to_the_operators(change):
+    from tqpk.operators.fused import _match_star_agg_topk
+    tg, ops, args = star_plan()
+    a = copy.deepcopy(args)
+    change(a)
+    assert _match_star_agg_topk(tg, ops, a, 0) is None

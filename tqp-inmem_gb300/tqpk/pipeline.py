@@ -363,7 +363,7 @@ class StarAggTopK:
         self._probe_args = a
         self._probe_grid = jit.occupancy_grid(self._probe, 256, 0, jit.probe_units(fa.numel()))
 
-    def _run_jit(self, s):
+    def _run_jit(self, s, before_probe=None):
         from . import jit
         if not hasattr(self, "_probe"):
             self._jit_setup()
@@ -387,19 +387,26 @@ class StarAggTopK:
                     "tqpk_directory_bits")
         self.sum.zero_()
         self.cnt.zero_()
+        if before_probe is not None:
+            before_probe()
         jit.launch(self._probe, self._probe_grid, 256, 0, self._probe_args, s, L.KID_STAR_PROBE)
         L.check(self.lib.tqpk_dense_topk(self.sum.data_ptr(), self.cnt.data_ptr(), self.sum.numel(), cmn, self.k,
                                          int(self.desc), self.tws.data_ptr(), self.tws.numel(),
                                          self.out_keys.data_ptr(), self.out_vals.data_ptr(), self.out_cnts.data_ptr(),
                                          self.out_count.data_ptr(), self.groups.data_ptr(), s), "tqpk_dense_topk")
 
-    def run(self, stream=None):
+    def run(self, stream=None, before_probe=None):
+        """Queues the query on `stream` (default: the current stream).  before_probe, when given,
+        is called after the dimension directories are queued and before the fact probe (e.g. to
+        make the stream wait for fact columns still being copied)."""
         s = (stream or torch.cuda.current_stream(self.dev)).cuda_stream
         self._jit_path = self._jit_ok()
         if self._jit_path:
             with torch.cuda.stream(stream or torch.cuda.current_stream(self.dev)):
-                self._run_jit(s)
+                self._run_jit(s, before_probe)
             return
+        if before_probe is not None:
+            before_probe()
         fa, fb, ak, bk, bc, ck = self.t
         (amn, amx), (bmn, bmx), (cmn, cmx) = self.doms
         L.check(self.lib.tqpk_pipeline_star_agg_topk(
@@ -423,6 +430,33 @@ class StarAggTopK:
 
     def replay(self):
         self.graph.replay()
+
+    def result_device(self):
+        """(C keys [m], sums float64[m], counts int64[m], m) as device tensors after the last run,
+        with one host read: the error words, the row count and the k result rows together
+        (`result_host` then holds the rows as numpy arrays).  A repeated dimension key raises
+        NotImplementedError, an out-of-domain one ValueError."""
+        cur = torch.cuda.current_stream(self.dev)
+        if not hasattr(self, "_hdr_host"):
+            self._hdr_host = torch.empty(8, dtype=torch.int64, pin_memory=True)
+            self._rows_host = [torch.empty(self.k, dtype=t.dtype, pin_memory=True)
+                               for t in (self.out_keys, self.out_vals, self.out_cnts)]
+        hdr = self._hdr_host
+        if getattr(self, "_jit_path", False):        # the three directory builds' error words
+            hdr[:3].copy_(self.err.to(torch.int64), non_blocking=True)
+        else:                                         # the library pipeline's error word (header int 2)
+            hdr[1:3] = 0
+            hdr[:1].copy_(self.ws[8:12].view(torch.int32).to(torch.int64), non_blocking=True)
+        hdr[3:4].copy_(self.out_count, non_blocking=True)
+        for h, t in zip(self._rows_host, (self.out_keys, self.out_vals, self.out_cnts)):
+            h.copy_(t, non_blocking=True)
+        cur.synchronize()
+        errs = [int(x) for x in hdr[:3].tolist() if x]
+        if errs:
+            L.check(errs[0], "star pipeline (repeated or out-of-domain dimension key)")
+        m = int(hdr[3])
+        self.result_host = tuple(h[:m].numpy().copy() for h in self._rows_host)
+        return self.out_keys[:m], self.out_vals[:m], self.out_cnts[:m], m
 
     def group_table(self):
         """Every group of the last run (generated-probe path): (C keys int64[G] ascending,

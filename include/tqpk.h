@@ -106,6 +106,12 @@ typedef struct {
  * are earlier register numbers.  Arithmetic follows torch's promotion:
  * registers are float64 or int64 (`type`); float64 arithmetic is IEEE
  * round-to-nearest per operation (no contraction), as torch evaluates it.
+ * A register of type TQPK_F32 (registers only; no column has it) holds a
+ * float32 in its low 32 bits: torch's result for an integer tensor with a
+ * Python float, an integer true division or a CASE mixing a float literal
+ * with integers (torch's default float dtype), computed in float32 with
+ * round-to-nearest.  TQPK_X_TOF32 converts an int64 register to float32,
+ * TQPK_X_F32TOF64 a float32 register to float64 (exact).
  * TQPK_X_SELECT is torch.where(a != 0, b, col) (CASE WHEN, aggregate.py:76-87;
  * register `col` holds the ELSE value, the condition is a 0/1 register, e.g.
  * a bool column).  TQPK_X_YEAR maps int64 days since 1990-01-01 to the year
@@ -113,10 +119,12 @@ typedef struct {
  * 1990-1999; days before 1990 give 1990, days from 2000 on the calendar year,
  * where the reference's year table has no entry).                         */
 enum { TQPK_X_COL = 1, TQPK_X_CONST = 2, TQPK_X_ADD = 3, TQPK_X_SUB = 4, TQPK_X_MUL = 5,
-       TQPK_X_DIV = 6, TQPK_X_TOF64 = 7, TQPK_X_SELECT = 8, TQPK_X_YEAR = 9 };
+       TQPK_X_DIV = 6, TQPK_X_TOF64 = 7, TQPK_X_SELECT = 8, TQPK_X_YEAR = 9, TQPK_X_TOF32 = 10,
+       TQPK_X_F32TOF64 = 11 };
+enum { TQPK_F32 = 7 };   /* expression register type (float32 in the low 32 bits) */
 
 typedef struct {
-  int32_t op, type; /* type: TQPK_I64 or TQPK_F64 */
+  int32_t op, type; /* type: TQPK_I64, TQPK_F64 or TQPK_F32 */
   int32_t a, b;     /* operand registers */
   int32_t col;      /* TQPK_X_COL: column slot; TQPK_X_SELECT: ELSE register */
   int32_t pad;

@@ -352,19 +352,21 @@ class _V:
 def _promote(a, b):
     """torch result type of a binary op between arrays/Python scalars.
 
-    Supported: f64 with anything -> f64; integers with integers -> int64.
-    An integer tensor with a Python float (or a true division of integers)
-    gives float32 in torch; that case is rejected, as it is by the product.
+    f64 with anything -> f64; a float32 array with integers or Python numbers, or an integer
+    array with a Python float -> float32 (torch's default float dtype); integers with integers
+    -> the wider integer dtype.
     """
     def kind(x):
         if isinstance(x, np.ndarray):
+            if x.dtype == np.float32:
+                return "g"
             return "f" if x.dtype.kind == "f" else ("b" if x.dtype == bool else "i")
         return "pf" if isinstance(x, float) else "pi"
     ka, kb = kind(a), kind(b)
     if "f" in (ka, kb):
         return np.float64
-    if ("pf" in (ka, kb)):
-        raise NotImplementedError("integer column with a float literal promotes to float32 in torch")
+    if "g" in (ka, kb) or "pf" in (ka, kb):
+        return np.float32
     # integer tensors: the wider tensor dtype (a Python int does not widen it); bool counts as int64
     order = [np.int8, np.uint8, np.int16, np.int32, np.int64]
     ints = [x.dtype.type for x in (a, b) if isinstance(x, np.ndarray) and x.dtype != bool]
@@ -382,14 +384,15 @@ _AGG_CALLS = ("sum", "avg", "count", "min", "max")
 
 def _where(mask, a, b):
     """torch.where(mask, a, b) with torch's promotion of arrays and Python scalars
-    (aggregate.py:87).  A float literal with integers (or two float literals) is
-    float32 in torch and is rejected, as it is by the product."""
+    (aggregate.py:87).  A float literal with integers (or two float literals), or a float32
+    branch without a float64 one, is float32 in torch (its default float dtype)."""
     arrs = [x for x in (a, b) if isinstance(x, np.ndarray)]
     pys = [x for x in (a, b) if not isinstance(x, np.ndarray)]
-    if any(x.dtype.kind == "f" for x in arrs):
+    if any(x.dtype == np.float64 for x in arrs):
         dt = np.float64
-    elif any(isinstance(x, float) for x in pys):
-        raise NotImplementedError("CASE mixing a float literal with integers is float32 in torch")
+    elif any(x.dtype == np.float32 for x in arrs) or any(isinstance(x, float) for x in pys):
+        f32 = [x.astype(np.float32) if isinstance(x, np.ndarray) else np.float32(x) for x in (a, b)]
+        return np.where(mask, f32[0], f32[1]).astype(np.float32)
     elif not arrs:
         dt = np.int64
     else:
@@ -483,11 +486,9 @@ def eval_agg_expr(tree, cols: Dict[int, np.ndarray], ctx=None):
         return (np.logical_and if op == "AND" else np.logical_or)(L, R)
     if op not in ("+", "-", "*", "/"):
         return _agg_compare(op, L, R)
-    if op == "/":
-        t = np.float64 if _promote(L, R) == np.float64 else None
-        if t is None:
-            raise NotImplementedError("integer true division promotes to float32 in torch")
     t = _promote(L, R)
+    if op == "/" and t != np.float64:
+        t = np.float32                                             # integer true division: float32
     La = np.asarray(L, dtype=t) if not isinstance(L, np.ndarray) else L.astype(t, copy=False)
     Ra = np.asarray(R, dtype=t) if not isinstance(R, np.ndarray) else R.astype(t, copy=False)
     with np.errstate(all="ignore"):
@@ -533,6 +534,24 @@ def reduce_groups(fn: str, v, inverse: np.ndarray, G: int, n: int) -> np.ndarray
     two_step = G > 0 and n / G >= (1 << 16)                         # :127-131
     S = max(1, n // (G << 6)) if two_step else 1
     is_int = v.dtype.kind in "iub"
+    if v.dtype == np.float32 and fn in ("sum", "avg"):
+        # float32 values: torch accumulates in float32, in row order (bincount / scatter_reduce on
+        # the CPU), the 2-step sub-slots then summed per group; the 2-step avg is float64 (:170)
+        if two_step:
+            flat = inverse * S + (np.arange(inverse.size) % S)
+            part = np.zeros(G * S, np.float32)
+            np.add.at(part, flat, v)
+            s = part.reshape(G, S).sum(axis=1, dtype=np.float32)
+            if fn == "avg":
+                with np.errstate(all="ignore"):
+                    return s.astype(np.float64) / _sum_2steps(inverse, np.ones(n), G, S)
+            return s
+        s = np.zeros(G, np.float32)
+        np.add.at(s, inverse, v)
+        if fn == "avg":
+            with np.errstate(all="ignore"):
+                return (s / np.bincount(inverse, minlength=G).astype(np.float32)).astype(np.float32)
+        return s
     if two_step and fn in ("sum", "avg", "count"):
         vv = (v != NULL).astype(np.float64) if fn == "count" else v.astype(np.float64)
         s = _sum_2steps(inverse, vv, G, S)

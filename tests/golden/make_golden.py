@@ -582,6 +582,47 @@ def aggregate_two_step(ref):
 
 
 @case
+def aggregate_float32(ref):
+    """torch's float32 results: an integer column with a Python float, integer true division and a
+    CASE mixing a float literal with integers (aggregate.py:76-87, :203-233), under sum, avg, min,
+    max and count; float32 meeting a float64 column widens to float64.  Two aggregates: 4 groups
+    (the 1-step path: float32 bincount sums) and 2 groups of 70,000 rows (the 2-step path, whose avg
+    is float64, :170)."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(29)
+    ins, outs, args = {}, {}, {}
+    for tag, n, g in (("one", 30000, 4), ("two", 140000, 2)):
+        cols = {1: rng.integers(0, g, n).astype(np.int64),
+                2: rng.integers(1, 51, n).astype(np.int64),
+                3: rng.integers(1, 10, n).astype(np.int64),
+                4: (rng.integers(90000, 10495001, n) / 100.0).astype(np.float64)}
+        types_ = {1: "int", 2: "int", 3: "int", 4: "float"}
+        results = ["g#1",
+                   [[["sum", [["q#2", "*", "1.5"]]], "#", "801"], "AS", "a#901"],
+                   [[["avg", [["q#2", "*", "0.1"]]], "#", "802"], "AS", "b#902"],
+                   [[["sum", [["q#2", "/", "d#3"]]], "#", "803"], "AS", "c#903"],
+                   [[["min", [["q#2", "*", "1.5"]]], "#", "804"], "AS", "d#904"],
+                   [[["max", [["d#3", "/", "q#2"]]], "#", "805"], "AS", "e#905"],
+                   [[["sum", ["CASE", "WHEN", ["q#2", ">", "25"], "THEN", "1.0", "ELSE", "0", "END"]], "#", "806"],
+                    "AS", "f#906"],
+                   [[["count", [["q#2", "*", "0.5"]]], "#", "807L"], "AS", "h#907L"],
+                   [[["sum", [["p#4", "*", ["q#2", "*", "0.5"]]]], "#", "808"], "AS", "i#908"],
+                   [[["sum", [[["q#2", "*", "0.25"], "+", "d#3"]]], "#", "809"], "AS", "j#909"]]
+        aargs = {"name": "Aggregate", "is partial": False, "keys": ["g#1"], "input ids": [1, 2, 3, 4],
+                 "results": results, "out agg ids": [901, 902, 903, 904, 905, 906, 907, 908, 909]}
+        tg = _tg(V.Variable, cols, types_)
+        torch.manual_seed(7)
+        ag.tqp_hash_aggregate(False, tg, copy.deepcopy(aargs), _Pool(), None, "a")
+        for c in [1] + aargs["out agg ids"]:
+            outs[f"{tag}_{c}"] = tg[c].tensor.numpy()
+            outs[f"{tag}_{c}_type"] = np.array(tg[c].tensor_type)
+        for c, v in cols.items():
+            ins[f"{tag}_{c}"] = v
+        args[tag] = {"aggregate": aargs, "types": types_}
+    _save("aggregate_float32", ins, args, outs)
+
+
+@case
 def sort_multikey(ref):
     """tqp_sort: multi-key (desc float, asc int, desc int), ties, limit; plus [G,1] 2-D keys."""
     f, hj, ag, so, V = ref

@@ -54,6 +54,21 @@ def test_groupby_kernel_compiles_for_each_table_mode():
         ok, log = jit.check_compiles(src)
         assert ok, log[:2000]
         assert "2470" not in src and "1000.5" not in src    # literals are bound at launch
+    # float32 registers (an integer column with a Python float, integer true division, CASE with
+    # a float literal beside integers) in the generated accumulation and projection kernels
+    q = {1: torch.zeros(64, dtype=torch.int64), 2: torch.zeros(64, dtype=torch.int64), 5: d[5]}
+    res32 = ["flag#5", [[["sum", [["q#1", "*", "1.5"]]], "#", "1"], "AS", "a#11"],
+             [[["max", [["q#1", "/", "d#2"]]], "#", "2"], "AS", "b#12"],
+             [[["sum", ["CASE", "WHEN", ["q#1", ">", "25"], "THEN", "1.0", "ELSE", "0", "END"]], "#", "3"], "AS", "c#13"]]
+    p32 = compile_aggregate({"is partial": False, "keys": ["flag#5"], "input ids": [1, 2, 5], "results": res32,
+                             "out agg ids": [11, 12, 13]}, q, derived=True)
+    plan = L.GbPlan()
+    plan.mode, plan.threads, plan.slots = L.GB_DENSE_PRIVATE, 256, 3
+    plan.key_stride[0] = 1
+    src, name, T, smem = jit.groupby_source(p32.spec, None, plan)
+    ok, log = jit.check_compiles(src)
+    assert ok, log[:2000]
+    assert "__fmul_rn" in src and "__fdiv_rn" in src and "__ll2float_rn" in src
 
 
 def test_probe_kernels_compile_with_and_without_build_filter():

@@ -91,5 +91,13 @@ def test_aggregate_dtypes_follow_torch():
            [[["max", ["x#2"]], "#", "3"], "AS", "c#13"]]
     prog = compile_aggregate({"keys": None, "results": res}, t)
     assert [o[4] for o in prog.outputs] == [torch.int32, torch.int64, torch.float64]
-    with pytest.raises(NotImplementedError):
-        compile_aggregate({"keys": None, "results": [[[["sum", [["d#1", "*", "0.5"]]], "#", "1"], "AS", "a#1"]]}, t)
+    # an integer column with a Python float is float32 in torch: float32 registers, the sum
+    # accumulated in float64 and returned as float32
+    p32 = compile_aggregate({"keys": None, "results": [[[["sum", [["d#1", "*", "0.5"]]], "#", "1"], "AS", "a#1"],
+                                                       [[["avg", [["d#1", "/", "d#1"]]], "#", "2"], "AS", "b#2"]]}, t)
+    types = [p32.spec.expr[i].type for i in range(p32.spec.n_expr)]
+    assert L.F32 in types and p32.casts == {1: (torch.float32, False), 2: (torch.float32, True)}
+    assert all(p32.spec.expr[p32.spec.accs[a].reg].type != L.F32 for a in range(1, p32.spec.n_accs))
+    with pytest.raises(NotImplementedError):      # arithmetic over such an aggregate stays off the kernels
+        compile_aggregate({"keys": None, "results": [[["2", "*", [[["sum", [["d#1", "*", "0.5"]]], "#", "1"]]],
+                                                      "AS", "a#1"]]}, t, derived=True)

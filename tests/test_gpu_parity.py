@@ -460,6 +460,35 @@ def test_aggregate_two_step_golden():
         assert_f64_close(o, g) if g.dtype == np.float64 else np.testing.assert_array_equal(o, g)
 
 
+@pytest.mark.parametrize("tag", ["one", "two"])
+def test_aggregate_float32_golden(tag):
+    """torch's float32 results (an integer column with a Python float, integer true division,
+    CASE mixing a float literal with integers) against the reference's own outputs: dtypes and
+    column types as the reference gives them (float32, typed "string" by its torch_to_type; the
+    2-step path's avg float64), min / max / count exact; sums are accumulated in float64 here and
+    rounded once, the reference adds in float32 row by row, so they agree within that rounding
+    (2e-4 relative for 7,500-70,000 rows per group)."""
+    from tqpk.operators import tqp_hash_aggregate
+    ins, outs, args = load("aggregate_float32")
+    a = args[tag]
+    cols = {int(k.split("_")[1]): v for k, v in ins.items() if isinstance(k, str) and k.startswith(tag + "_")}
+    tg = {c: V(v, a["types"][str(c)]) for c, v in cols.items()}
+    tqp_hash_aggregate(True, tg, copy.deepcopy(a["aggregate"]), None, None, "a")
+    g1 = outs[f"{tag}_1"].reshape(-1)
+    order = np.argsort(g1, kind="stable")
+    np.testing.assert_array_equal(np_(tg[1].tensor).reshape(-1), g1[order])
+    for i in a["aggregate"]["out agg ids"]:
+        g, o = outs[f"{tag}_{i}"][order], np_(tg[i].tensor)
+        assert o.dtype == g.dtype, (i, o.dtype, g.dtype)
+        assert tg[i].tensor_type == str(outs[f"{tag}_{i}_type"].reshape(-1)[0]), i
+        if i in (904, 905, 907):                            # min, max, count: exact
+            np.testing.assert_array_equal(o, g)
+        elif g.dtype == np.float32 or i == 902:
+            np.testing.assert_allclose(o, g, rtol=2e-4, atol=0)
+        else:
+            assert_f64_close(o, g)
+
+
 def test_aggregate_high_cardinality_vs_oracle():
     from tqpk.operators import tqp_hash_aggregate
     rng = np.random.default_rng(9)

@@ -234,3 +234,32 @@ def test_late_materialisation_masks():
     res, _ = O.join_vortex(jcols, j, 11, 21, "inner")
     for c in (11, 21, 23, 26):
         np.testing.assert_array_equal(res[c].reshape(-1), outs[f"join_{c}"].reshape(-1))
+
+
+def f32_tag(ins, outs, tag):
+    """One aggregate of the float32 fixture: its inputs, its outputs ordered by key."""
+    cols = {int(k.split("_")[1]): v for k, v in ins.items() if isinstance(k, str) and k.startswith(tag + "_")}
+    return cols, {k[len(tag) + 1:]: v for k, v in outs.items() if k.startswith(tag + "_")}
+
+
+@pytest.mark.parametrize("tag", ["one", "two"])
+def test_aggregate_float32(tag):
+    """torch's float32 results (an integer column with a Python float, integer true division, a
+    CASE mixing a float literal with integers): the 1-step path's float32 sums are the
+    reference's row-order float32 additions, bit for bit; the 2-step path's per-group sum of
+    float32 sub-slots may differ in its last bits (summation order)."""
+    ins, outs, args = load("aggregate_float32")
+    cols, out = f32_tag(ins, outs, tag)
+    a = args[tag]["aggregate"]
+    agg = O.tqp_hash_aggregate(cols, a)
+    ids = a["out agg ids"]
+    (k,), vals = _by_key([out["1"]], *[out[str(i)] for i in ids])
+    np.testing.assert_array_equal(agg[1].reshape(-1), k)
+    for i, g in zip(ids, vals):
+        assert agg[i].dtype == g.dtype, (i, agg[i].dtype, g.dtype)
+        if tag == "two" and (g.dtype == np.float32 or i == 902):    # 902: float64 avg of a float32 sum
+            np.testing.assert_allclose(agg[i], g, rtol=2e-6, atol=0)
+        elif g.dtype == np.float64:
+            assert_f64_close(agg[i], g)
+        else:
+            np.testing.assert_array_equal(agg[i], g, err_msg=str(i))

@@ -278,10 +278,29 @@ __host__ __device__ __forceinline__ int64_t expr_year(int64_t d) {
   return yoe + era * 400 + (mp >= 10 ? 1 : 0);
 }
 
+__device__ __forceinline__ uint64_t f32_bits(float x) { return static_cast<uint64_t>(__float_as_uint(x)); }
+__device__ __forceinline__ float bits_f32(uint64_t u) { return __uint_as_float(static_cast<unsigned>(u)); }
+
+// float32 registers (torch's default float dtype: integer with a Python float, integer true division)
+__device__ __forceinline__ uint64_t expr_apply_f32(const tqpk_expr_insn& X, uint64_t a, uint64_t b) {
+  switch (X.op) {
+    case TQPK_X_CONST: return f32_bits(__double2float_rn(X.cf));
+    case TQPK_X_TOF32: return f32_bits(__ll2float_rn(static_cast<long long>(a)));
+    case TQPK_X_ADD: return f32_bits(__fadd_rn(bits_f32(a), bits_f32(b)));
+    case TQPK_X_SUB: return f32_bits(__fsub_rn(bits_f32(a), bits_f32(b)));
+    case TQPK_X_MUL: return f32_bits(__fmul_rn(bits_f32(a), bits_f32(b)));
+    case TQPK_X_DIV: return f32_bits(__fdiv_rn(bits_f32(a), bits_f32(b)));
+  }
+  return 0;
+}
+
 __device__ __forceinline__ uint64_t expr_apply(const tqpk_expr_insn& X, uint64_t a, uint64_t b, uint64_t c,
                                               const void* const* cols, const int* dts, int64_t row) {
   const bool f = X.type == TQPK_F64;
+  if (X.type == TQPK_F32 && X.op != TQPK_X_SELECT) return expr_apply_f32(X, a, b);
   switch (X.op) {
+    case TQPK_X_F32TOF64:
+      return static_cast<uint64_t>(__double_as_longlong(static_cast<double>(bits_f32(a))));
     case TQPK_X_SELECT: return a != 0 ? b : c;
     case TQPK_X_YEAR: return static_cast<uint64_t>(expr_year(static_cast<int64_t>(a)));
     case TQPK_X_COL:

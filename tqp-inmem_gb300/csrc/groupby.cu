@@ -494,11 +494,18 @@ static int check_spec(const tqpk_groupby_spec* S, bool has_rows = true) {
   }
   for (int i = 0; i < S->n_expr; ++i) {
     const tqpk_expr_insn& X = S->expr[i];
-    if (X.type != TQPK_F64 && X.type != TQPK_I64) return TQPK_EDTYPE;
-    if (X.op == TQPK_X_COL && (X.col < 0 || X.col >= S->n_cols)) return TQPK_EINVAL;
+    if (X.type != TQPK_F64 && X.type != TQPK_I64 && X.type != TQPK_F32) return TQPK_EDTYPE;
+    if (X.op == TQPK_X_COL && (X.col < 0 || X.col >= S->n_cols || X.type == TQPK_F32)) return TQPK_EINVAL;
     if (X.op >= TQPK_X_ADD && X.op <= TQPK_X_DIV && (X.a < 0 || X.a >= i || X.b < 0 || X.b >= i)) return TQPK_EINVAL;
-    if (X.op == TQPK_X_TOF64 && (X.a < 0 || X.a >= i)) return TQPK_EINVAL;
-    if (X.op == TQPK_X_DIV && X.type != TQPK_F64) return TQPK_EUNSUPPORTED;
+    if (X.op >= TQPK_X_ADD && X.op <= TQPK_X_DIV && (S->expr[X.a].type != X.type || S->expr[X.b].type != X.type))
+      return TQPK_EDTYPE;                    // operands of the register's own type (conversions are explicit)
+    if (X.op == TQPK_X_TOF64 && (X.a < 0 || X.a >= i || X.type != TQPK_F64 || S->expr[X.a].type != TQPK_I64))
+      return TQPK_EINVAL;
+    if (X.op == TQPK_X_TOF32 && (X.a < 0 || X.a >= i || X.type != TQPK_F32 || S->expr[X.a].type != TQPK_I64))
+      return TQPK_EINVAL;
+    if (X.op == TQPK_X_F32TOF64 && (X.a < 0 || X.a >= i || X.type != TQPK_F64 || S->expr[X.a].type != TQPK_F32))
+      return TQPK_EINVAL;
+    if (X.op == TQPK_X_DIV && X.type == TQPK_I64) return TQPK_EUNSUPPORTED;
     if (X.op == TQPK_X_SELECT) {
       if (X.a < 0 || X.a >= i || X.b < 0 || X.b >= i || X.col < 0 || X.col >= i) return TQPK_EINVAL;
       if (S->expr[X.a].type != TQPK_I64 || S->expr[X.b].type != X.type || S->expr[X.col].type != X.type)
@@ -506,12 +513,13 @@ static int check_spec(const tqpk_groupby_spec* S, bool has_rows = true) {
     }
     if (X.op == TQPK_X_YEAR && (X.a < 0 || X.a >= i || X.type != TQPK_I64 || S->expr[X.a].type != TQPK_I64))
       return TQPK_EINVAL;
-    if (X.op < TQPK_X_COL || X.op > TQPK_X_YEAR) return TQPK_EINVAL;
+    if (X.op < TQPK_X_COL || X.op > TQPK_X_F32TOF64) return TQPK_EINVAL;
   }
   for (int a = 0; a < S->n_accs; ++a) {
     const tqpk_acc& A = S->accs[a];
     if (A.kind < TQPK_ACC_SUM || A.kind > TQPK_ACC_MAX) return TQPK_EINVAL;
     if (A.kind != TQPK_ACC_COUNT_ROWS && (A.reg < 0 || A.reg >= S->n_expr)) return TQPK_EINVAL;
+    if (A.kind != TQPK_ACC_COUNT_ROWS && S->expr[A.reg].type == TQPK_F32) return TQPK_EDTYPE;  // accumulate float64
   }
   return TQPK_OK;
 }

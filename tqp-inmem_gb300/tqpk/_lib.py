@@ -24,6 +24,8 @@ P_STRCMP, P_PREFIX, P_CONTAINS, P_LIKE2 = 9, 10, 11, 12
 LT, LE, GT, GE, EQ, NE, ISCLOSE = 0, 1, 2, 3, 4, 5, 6
 DOM_I64, DOM_F64, DOM_F32 = 0, 1, 2
 X_COL, X_CONST, X_ADD, X_SUB, X_MUL, X_DIV, X_TOF64, X_SELECT, X_YEAR = 1, 2, 3, 4, 5, 6, 7, 8, 9
+X_TOF32, X_F32TOF64 = 10, 11
+F32 = 7                      # expression register type only: float32 in the low 32 bits
 ACC_SUM, ACC_COUNT_NOTNULL, ACC_COUNT_ROWS, ACC_MIN, ACC_MAX = 1, 2, 3, 4, 5
 GB_GLOBAL_ONE, GB_DENSE_PRIVATE, GB_DENSE_SHARED, GB_DENSE_GLOBAL, GB_HASH = 0, 1, 2, 3, 4
 OUT_ACC, OUT_AVG = 0, 1

@@ -28,7 +28,7 @@ import torch
 
 from . import _lib as L
 from .dtypes import code_of, dtype_of
-from .expr import compile_aggregate
+from .expr import compile_aggregate, require_f64_outputs
 from .predicate import compile_filter
 
 
@@ -155,6 +155,7 @@ class Batch:
         ppred = compile_filter(inst.probe_filter, inst.probe_cols) if inst.probe_filter is not None else None
         prog = compile_aggregate({"keys": None, "results": [[[["sum", inst.value_tree], "#", "1"], "AS", "v#1"]]},
                                  inst.probe_cols)
+        require_f64_outputs(prog, "batched join")
         vreg = prog.spec.accs[prog.outputs[0][2]].reg
         kmin, kmax = map(int, inst.key_domain)
         ws = torch.empty(self.lib.tqpk_batch_join_workspace_bytes(kmin, kmax), dtype=torch.uint8, device=dev)
@@ -178,6 +179,7 @@ class Batch:
         dev = next(iter(cols.values())).device
         self.dev = dev
         prog = compile_aggregate(inst.args, cols)
+        require_f64_outputs(prog, "batched group-by")
         pred = compile_filter(inst.filter_tree, inst.filter_cols) if inst.filter_tree is not None else None
         nk = prog.spec.n_keys
         kmin = (C.c_int64 * nk)(*[int(d[0]) for d in inst.key_domains])

@@ -16,8 +16,13 @@ Output: a ``tqpk_groupby_spec`` with
 Arithmetic follows torch's promotion (``aggregate.py:203-233`` applies
 torch.add/sub/mul/div to tensors and Python numbers): float64 wins; integer
 tensors with Python ints stay integer.  An integer tensor combined with a
-Python float, or an integer true division, is float32 in torch; those are
-rejected with NotImplementedError rather than computed differently.
+Python float, an integer true division, or a CASE mixing a float literal with
+integers is float32 in torch (its default float dtype): those registers are
+float32 (TQPK_F32), computed in float32 with round-to-nearest as torch does,
+and widened exactly to float64 where they meet a float64 tensor.  An
+aggregate of a float32 expression accumulates in float64 and its output is
+rounded to float32 (``casts``), the dtype the reference returns (its own
+float32 sums round at every row).
 
 With ``derived=True`` (the operator path) the rest of the reference's
 expression language compiles too:
@@ -73,6 +78,10 @@ class _Node:
     f64: bool
     dtype: torch.dtype
 
+    @property
+    def f32(self) -> bool:
+        return self.dtype == torch.float32
+
 
 @dataclass
 class AggregateProgram:
@@ -83,6 +92,9 @@ class AggregateProgram:
     outputs: List[Tuple[int, int, int, int, torch.dtype]] = field(default_factory=list)  # (out id, op, a, b, dtype)
     masks: List[Tuple[Any, torch.Tensor]] = field(default_factory=list)   # (condition predicate, its bool column)
     post: List[Tuple[int, Any, torch.dtype]] = field(default_factory=list)  # (out id, arithmetic over hidden ids, dtype)
+    # outputs computed in float64 whose reference dtype is float32: out id -> (dtype, avg result id of the
+    # reference's 2-step path, which stays float64 there: aggregate.py:170)
+    casts: Dict[int, Tuple[torch.dtype, bool]] = field(default_factory=dict)
     encoded: bool = False     # the kernel groups by one int32 code column standing for the key tuple
 
 
@@ -112,12 +124,12 @@ class _Builder:
         self.accs: List[tuple] = [(L.ACC_COUNT_ROWS, L.I64, 0, 0, 0.0)]
         self.acc_memo: Dict[tuple, int] = {}
 
-    def _insn(self, key, op, f64, a=0, b=0, col=0, ci=0, cf=0.0) -> int:
+    def _insn(self, key, op, f64, a=0, b=0, col=0, ci=0, cf=0.0, f32=False) -> int:
         if key in self.memo:
             return self.memo[key]
         if len(self.expr) >= L.MAX_EXPR:
             raise NotImplementedError(f"aggregate expressions exceed {L.MAX_EXPR} instructions")
-        self.expr.append((op, L.F64 if f64 else L.I64, a, b, col, ci, cf))
+        self.expr.append((op, L.F32 if f32 else L.F64 if f64 else L.I64, a, b, col, ci, cf))
         self.memo[key] = len(self.expr) - 1
         return self.memo[key]
 
@@ -144,8 +156,25 @@ class _Builder:
             return _Node(self._insn(("cf", v), L.X_CONST, True, cf=v), True, torch.float64)
         return _Node(self._insn(("ci", v), L.X_CONST, False, ci=int(v)), False, torch.int64)
 
+    def const32(self, v) -> _Node:
+        """A Python number taken into a float32 operation (torch casts it to float32)."""
+        return _Node(self._insn(("cf32", float(v)), L.X_CONST, False, cf=float(v), f32=True), False, torch.float32)
+
     def to_f64(self, n: _Node) -> int:
-        return n.reg if n.f64 else self._insn(("tof64", n.reg), L.X_TOF64, True, a=n.reg)
+        if n.f64:
+            return n.reg
+        if n.f32:
+            return self._insn(("f32tof64", n.reg), L.X_F32TOF64, True, a=n.reg)
+        return self._insn(("tof64", n.reg), L.X_TOF64, True, a=n.reg)
+
+    def to_f32(self, x) -> int:
+        """An integer node or a Python number as a float32 register."""
+        if not isinstance(x, _Node):
+            return self.const32(x).reg
+        if x.f32:
+            return x.reg
+        assert not x.f64
+        return self._insn(("tof32", x.reg), L.X_TOF32, False, a=x.reg, f32=True)
 
     def value(self, tree):
         """aggregate.py:58-233 arithmetic: returns a _Node or a Python number."""
@@ -204,8 +233,11 @@ class _Builder:
         pys = [x for x in (t, e) if not isinstance(x, _Node)]
         if any(n.f64 for n in nodes):
             f64, dtype = True, torch.float64
-        elif any(isinstance(x, float) for x in pys):
-            raise NotImplementedError("CASE mixing a float literal with integers is float32 in torch")
+        elif any(n.f32 for n in nodes) or any(isinstance(x, float) for x in pys):
+            # torch.where with a float32 branch, or a float literal beside integers: float32
+            rt, re_ = self.to_f32(t), self.to_f32(e)
+            reg = self._insn(("sel32", c.reg, rt, re_), L.X_SELECT, False, a=c.reg, b=rt, col=re_, f32=True)
+            return _Node(reg, False, torch.float32)
         elif not nodes:
             f64, dtype = False, torch.int64
         else:
@@ -230,13 +262,17 @@ class _Builder:
         # torch promotion of the pair
         def kind(x):
             if isinstance(x, _Node):
-                return "f" if x.f64 else "i"
+                return "f" if x.f64 else "g" if x.f32 else "i"
             return "pf" if isinstance(x, float) else "pi"
         ka, kb = kind(a), kind(b)
         if "f" in (ka, kb):
             f64, dtype = True, torch.float64
-        elif "pf" in (ka, kb) or op == "/":
-            raise NotImplementedError("integer tensor with a float literal (or integer division) is float32 in torch")
+        elif "g" in (ka, kb) or "pf" in (ka, kb) or op == "/":
+            # float32 (torch's default float dtype): a float32 tensor with integers or Python numbers,
+            # an integer tensor with a Python float, or an integer true division
+            ra, rb = self.to_f32(a), self.to_f32(b)
+            reg = self._insn((op, ra, rb, "f32"), op_code, False, a=ra, b=rb, f32=True)
+            return _Node(reg, False, torch.float32)
         else:
             ints = [x.dtype for x in (a, b) if isinstance(x, _Node)]
             dtype = max(ints, key=lambda d: _INT_ORDER[d])
@@ -260,6 +296,13 @@ class _Builder:
             self.accs.append((kind, L.F64 if node.f64 else L.I64, node.reg, init_i, init_f))
             self.acc_memo[key] = len(self.accs) - 1
         return self.acc_memo[key]
+
+
+def require_f64_outputs(prog: "AggregateProgram", what: str) -> None:
+    """The fused and batched paths write float64 / int64 results only: an aggregate of a float32
+    expression (torch's float32 result) is left to the operator path."""
+    if prog.casts:
+        raise NotImplementedError(f"{what}: an aggregate of a float32 expression runs on the operator path")
 
 
 def _call_of(t):
@@ -303,6 +346,12 @@ def _add_output(b: _Builder, prog: AggregateProgram, oid: int, fn: str, arg):
         return
     if scalar:                                              # aggregate.py:149-152: full(cnt_rows, v)
         v = b.const(v)
+    if v.f32:
+        # a float32 expression: accumulated from its exact float64 value; the output is rounded to
+        # float32 (sum, min, max, and avg of the 1-step path; the 2-step avg is float64, :170)
+        v = _Node(b.to_f64(v), True, torch.float64)
+        if fn != "count":
+            prog.casts[oid] = (torch.float32, fn == "avg")
     if fn == "sum":
         a = b.acc(L.ACC_SUM, v)
         prog.outputs.append((oid, L.OUT_ACC, a, 0, torch.float64 if v.f64 else torch.int64))
@@ -368,7 +417,7 @@ def _rebind(proto: AggregateProgram, col_ids: List[int], columns: Dict[int, torc
         s.cols[i] = t.data_ptr()
     return AggregateProgram(spec=s, tensors=tensors, key_ids=list(proto.key_ids),
                             key_outputs=list(proto.key_outputs), outputs=list(proto.outputs), masks=[],
-                            post=list(proto.post), encoded=False)
+                            post=list(proto.post), encoded=False, casts=dict(proto.casts))
 
 
 def _compile_aggregate(args: dict, columns: Dict[int, torch.Tensor], derived: bool,
@@ -398,6 +447,8 @@ def _compile_aggregate(args: dict, columns: Dict[int, torch.Tensor], derived: bo
             raise NotImplementedError(f"aggregate result {tree!r} has no aggregate call")
         for hid, fn, arg in calls:
             _add_output(b, prog, hid, fn, arg)
+            if hid in prog.casts:
+                raise NotImplementedError("arithmetic over an aggregate of a float32 expression")
         dts = {hid: dt for (hid, _, _, _, dt) in prog.outputs if hid in {c[0] for c in calls}}
         trial = compile_projection([lifted], {h: torch.empty(0, dtype=dt) for h, dt in dts.items()})
         prog.post.append((oid, lifted, trial.outputs[0][1]))
@@ -468,7 +519,8 @@ def compile_projection(trees, columns: Dict[int, torch.Tensor], derived: bool = 
         v = b.value(expr)
         if not isinstance(v, _Node):
             raise NotImplementedError(f"projection of a literal {expr!r}")
-        outs.append((v.reg, v.dtype))
+        # a float32 result is written through its exact float64 value and narrowed afterwards
+        outs.append((b.to_f64(v) if v.f32 else v.reg, v.dtype))
     spec = L.GroupbySpec()
     spec.n_keys = 0
     spec.n_cols = len(b.col_tensors)

@@ -432,6 +432,20 @@ def _expr_code(S, upto: int, colpfx: str, contract: bool = False) -> Tuple[List[
             x, y, _ = fused[i]
             lines.append(f"const double r{i} = __fma_rn(-r{x}, r{y}, r{x});")
             continue
+        if X.type == L.F32:          # float32 register: torch's default float dtype, round-to-nearest
+            if X.op == L.X_CONST:            # the Python number cast to float32, as torch does
+                lines.append(f"const float r{i} = __double2float_rn({_hexf(X.cf)});")
+            elif X.op == L.X_TOF32:
+                lines.append(f"const float r{i} = __ll2float_rn(r{X.a});")
+            elif X.op == L.X_SELECT:
+                lines.append(f"const float r{i} = r{X.a} != 0 ? r{X.b} : r{X.col};")
+            else:
+                fn = {L.X_ADD: "__fadd_rn", L.X_SUB: "__fsub_rn", L.X_MUL: "__fmul_rn", L.X_DIV: "__fdiv_rn"}[X.op]
+                lines.append(f"const float r{i} = {fn}(r{X.a}, r{X.b});")
+            continue
+        if X.op == L.X_F32TOF64:
+            lines.append(f"const double r{i} = (double)r{X.a};")
+            continue
         f = X.type == L.F64
         t = "double" if f else "i64"
         if X.op == L.X_COL:

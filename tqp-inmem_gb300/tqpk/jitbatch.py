@@ -42,7 +42,7 @@ from . import _lib as L
 from . import jit
 from .batch import Autotuner, GroupByInstance, JoinInstance
 from .dtypes import code_of, dtype_of
-from .expr import compile_aggregate
+from .expr import compile_aggregate, require_f64_outputs
 from .predicate import compile_filter
 
 SMEM = 96 * 1024          # dynamic shared memory of the persistent kernel (group tables)
@@ -715,6 +715,7 @@ class QueryBatch:
         dev = next(iter(cols.values())).device
         self.dev = dev
         prog = compile_aggregate(inst.args, cols)
+        require_f64_outputs(prog, "batched group-by")
         pred = compile_filter(inst.filter_tree, inst.filter_cols) if inst.filter_tree is not None else None
         _no_strings(pred)
         S = prog.spec
@@ -775,6 +776,7 @@ class QueryBatch:
         _no_strings(ppred)
         prog = compile_aggregate({"keys": None, "results": [[[["sum", inst.value_tree], "#", "1"], "AS", "v#1"]]},
                                  inst.probe_cols)
+        require_f64_outputs(prog, "batched join")
         S = prog.spec
         vreg = S.accs[prog.outputs[0][2]].reg
         key = _join_functions(0, S, vreg, ppred.struct if ppred else None, bpred.struct if bpred else None)

@@ -192,9 +192,12 @@ def _run_join_agg_topk(tensor_group, m) -> bool:
     if kmax - kmin + 1 > (1 << 31):
         return False
     pcols = {c: tensor_group[c].tensor.reshape(-1) for c in set(m["vcols"]) | (set(fp["materialized in"]) if fp else set())}
-    pipe = JoinAggTopK(bk, kmin, kmax, pv.tensor.reshape(-1), _fcols(tensor_group, fb) if fb else {},
-                       fb["filter tree"] if fb else None, pcols, fp["filter tree"] if fp else None,
-                       m["value_tree"], k=m["k"], descending=m["desc"])
+    try:
+        pipe = JoinAggTopK(bk, kmin, kmax, pv.tensor.reshape(-1), _fcols(tensor_group, fb) if fb else {},
+                           fb["filter tree"] if fb else None, pcols, fp["filter tree"] if fp else None,
+                           m["value_tree"], k=m["k"], descending=m["desc"])
+    except NotImplementedError:                      # e.g. a float32 sum: the operators run instead
+        return False
     wait_ready(*build_vars)
     pipe.run(before_probe=lambda: wait_ready(*probe_vars))
     try:

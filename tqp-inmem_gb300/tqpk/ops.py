@@ -233,6 +233,15 @@ def groupby(prog: AggregateProgram, n: int, device, mask: Optional[torch.Tensor]
                                       _vp_array([k.data_ptr() for k in keys]), len(outs), _i32_array(ops),
                                       _vp_array([o.data_ptr() for o in outs]), s), "tqpk_groupby_emit")
     res = {oid: o for (oid, *_), o in zip(prog.outputs, outs)}
+    if prog.casts:
+        # aggregates of float32 expressions, accumulated in float64, returned as float32 as the
+        # reference returns them, except the avg of its 2-step path (rows / groups >= 2^16), which
+        # is float64 there (aggregate.py:127-131, :170)
+        rows = int(plan.n_rows) if (pred is not None or mask is not None) else n
+        two_step = G > 0 and rows / G >= (1 << 16)
+        for oid, (dt, is_avg) in prog.casts.items():
+            if oid in res and not (is_avg and two_step):
+                res[oid] = res[oid].to(dt)
     if prog.post:
         # arithmetic over aggregates (aggregate.py:197-233): a projection over the group columns
         from .expr import _HIDDEN_ID, compile_projection
@@ -491,13 +500,16 @@ def project(prog, n: int, device) -> List[torch.Tensor]:
     from . import jit
     from .dtypes import code_of
     _check_cuda(*prog.tensors)
-    outs = [torch.empty(n, dtype=dt, device=device) for (_, dt) in prog.outputs]
+    # float32 results (torch's default float dtype) are written as their exact float64 values,
+    # then narrowed: the same float32
+    wdt = [torch.float64 if dt == torch.float32 else dt for (_, dt) in prog.outputs]
+    outs = [torch.empty(n, dtype=dt, device=device) for dt in wdt]
     if n == 0 or not outs:
-        return outs
+        return [o.to(dt) for o, (_, dt) in zip(outs, prog.outputs)]
     fill_masks(prog.masks, device)
     if not jit.available():
         raise NotImplementedError("projection needs the runtime compiler (NVRTC)")
-    src, name = jit.project_source(prog.spec, [(r, code_of(dt)) for (r, dt) in prog.outputs])
+    src, name = jit.project_source(prog.spec, [(r, code_of(dt)) for (r, _), dt in zip(prog.outputs, wdt)])
     h = jit.compile_kernel(src, name)
     a = jit._Args()
     for c in range(prog.spec.n_cols):
@@ -507,7 +519,7 @@ def project(prog, n: int, device) -> List[torch.Tensor]:
     a.i64(n)
     a.i32(jit._aligned(*prog.tensors))
     jit.launch(h, jit.occupancy_grid(h, 256, 0, (n + 3) // 4), 256, 0, a, _stream(device))
-    return outs
+    return [o if o.dtype == dt else o.to(dt) for o, (_, dt) in zip(outs, prog.outputs)]
 
 
 def mark_rows(idx: torch.Tensor, n: int) -> torch.Tensor:

@@ -19,7 +19,7 @@ import torch
 
 from . import _lib as L
 from .dtypes import code_of
-from .expr import compile_aggregate
+from .expr import compile_aggregate, require_f64_outputs
 from .predicate import compile_filter
 
 
@@ -51,6 +51,7 @@ class JoinAggTopK:
         prog = compile_aggregate({"keys": None, "results": [[[["sum", value_tree], "#", "1"], "AS", "v#1"]]},
                                  probe_cols)
         self.prog = prog
+        require_f64_outputs(prog, "JoinAggTopK")
         self.value_reg = prog.spec.accs[prog.outputs[0][2]].reg
         if not 1 <= k <= 256:
             raise NotImplementedError("the fused top-k handles k <= 256")
@@ -279,6 +280,7 @@ class StarAggTopK:
         self.prog = compile_aggregate({"keys": None, "results": [[[["sum", value_tree], "#", "1"], "AS", "v#1"]]},
                                       fact_cols)
         self.value_reg = self.prog.spec.accs[self.prog.outputs[0][2]].reg
+        require_f64_outputs(self.prog, "StarAggTopK")
         if not 1 <= k <= 256:
             raise NotImplementedError("the fused top-k handles k <= 256")
         self.k, self.desc = int(k), bool(descending)
@@ -503,6 +505,7 @@ class GroupByPipeline:
         a = dict(args)
         a.pop("mask map", None)
         self.prog = compile_aggregate(a, columns)
+        require_f64_outputs(self.prog, "GroupByPipeline")
         self.pred = compile_filter(filter_tree, filter_cols) if filter_tree is not None else None
         if self.pred is not None and has_strings(self.pred.struct):
             raise NotImplementedError("string predicates run on the operator path")

@@ -127,7 +127,9 @@ typedef struct {
   int32_t op, type; /* type: TQPK_I64, TQPK_F64 or TQPK_F32 */
   int32_t a, b;     /* operand registers */
   int32_t col;      /* TQPK_X_COL: column slot; TQPK_X_SELECT: ELSE register */
-  int32_t pad;
+  int32_t wrap;     /* integer ADD/SUB/MUL: 0, or TQPK_I8 / TQPK_U8 / TQPK_I32 when torch's result
+                       dtype is that narrower integer: the int64 result is wrapped to it (two's
+                       complement), as torch's int8 / uint8 / int32 arithmetic wraps */
   int64_t ci;       /* TQPK_X_CONST integer value */
   double cf;        /* TQPK_X_CONST float value */
 } tqpk_expr_insn;

@@ -531,6 +531,14 @@ def reduce_groups(fn: str, v, inverse: np.ndarray, G: int, n: int) -> np.ndarray
         v = np.full(n, v, np.int64)
     elif isinstance(v, float):
         v = np.full(n, v, np.float64)
+    if v.ndim == 2:                                                 # string slices (substring)
+        # sum and count squeeze their values (:179-182); min/max scatter them by a 1-D index and
+        # avg's bincount takes 1-D weights only, which the reference fails on
+        if fn not in ("sum", "count"):
+            raise RuntimeError(f"{fn} of [N, w] values fails in the reference")
+        v = np.squeeze(v) if v.size >= 2 else v.reshape(-1)
+        if v.ndim != 1:
+            raise RuntimeError("bincount of [N, w] weights fails in the reference")
     two_step = G > 0 and n / G >= (1 << 16)                         # :127-131
     S = max(1, n // (G << 6)) if two_step else 1
     is_int = v.dtype.kind in "iub"

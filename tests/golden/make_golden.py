@@ -619,7 +619,42 @@ def aggregate_float32(ref):
         for c, v in cols.items():
             ins[f"{tag}_{c}"] = v
         args[tag] = {"aggregate": aargs, "types": types_}
+        if tag == "one":                 # the same expressions as a projection (project.py:20-67)
+            from operators import project as pj
+            pargs = {"name": "Project", "rename map": {}, "materialized in": [2, 3, 4],
+                     "used expr": [[[["q#2", "*", "1.5"]], "AS", "x#41"], [[["q#2", "/", "d#3"]], "AS", "y#42"],
+                                   [[["p#4", "*", ["q#2", "*", "0.5"]]], "AS", "z#43"]],
+                     "materialized out": [41, 42, 43]}
+            tg = _tg(V.Variable, cols, types_)
+            pj.tqp_project(False, tg, copy.deepcopy(pargs), None, _Pool(), "p")
+            for c in pargs["materialized out"]:
+                outs[f"proj_{c}"] = tg[c].tensor.numpy().copy()
+                outs[f"proj_{c}_type"] = np.array([tg[c].tensor_type])
+            args["project"] = pargs
     _save("aggregate_float32", ins, args, outs)
+
+
+@case
+def aggregate_substring(ref):
+    """substring(col, l, 1) as an aggregate value (aggregate.py:114-119): sum and count of the
+    one-byte slice (squeezed to [N], :179-182), alone and times a Python int."""
+    f, hj, ag, so, V = ref
+    rng = np.random.default_rng(37)
+    n = 12000
+    cols = {1: rng.integers(0, 5, n).astype(np.int64),
+            2: _strings(rng, ["BRAZIL", "CANADA", "PERU", "ARGENTINA", "CHINA", "EGYPT"], n, 25)}
+    types_ = {1: "int", 2: "string"}
+    results = ["g#1",
+               [[["sum", [["substring", ["c#2", "1", "1"]]]], "#", "501"], "AS", "a#601"],
+               [[["count", [["substring", ["c#2", "2", "1"]]]], "#", "502L"], "AS", "b#602L"],
+               [[["sum", [[["substring", ["c#2", "3", "1"]], "*", "2"]]], "#", "503"], "AS", "c#603"]]
+    aargs = {"name": "Aggregate", "is partial": False, "keys": ["g#1"], "input ids": [1, 2],
+             "results": results, "out agg ids": [601, 602, 603]}
+    tg = _tg(V.Variable, cols, types_)
+    torch.manual_seed(11)
+    ag.tqp_hash_aggregate(False, tg, copy.deepcopy(aargs), _Pool(), None, "a")
+    outs = {str(c): tg[c].tensor.numpy() for c in [1, 601, 602, 603]}
+    _save("aggregate_substring", {str(k): v for k, v in cols.items()}, {"aggregate": aargs, "types": types_}, outs)
 
 
 @case

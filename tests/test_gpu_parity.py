@@ -489,6 +489,37 @@ def test_aggregate_float32_golden(tag):
             assert_f64_close(o, g)
 
 
+def test_project_float32_golden():
+    """Float32 projections (an integer column times a Python float, integer true division) are the
+    reference's values bit for bit, typed as it types them."""
+    from tqpk.operators import tqp_project
+    ins, outs, args = load("aggregate_float32")
+    a = args["one"]
+    cols = {int(k.split("_")[1]): v for k, v in ins.items() if isinstance(k, str) and k.startswith("one_")}
+    tg = {c: V(v, a["types"][str(c)]) for c, v in cols.items()}
+    tqp_project(True, tg, copy.deepcopy(args["project"]), None, None, "p")
+    for c in args["project"]["materialized out"]:
+        g, o = outs[f"proj_{c}"], np_(tg[c].tensor)
+        assert o.dtype == g.dtype, (c, o.dtype, g.dtype)
+        assert tg[c].tensor_type == str(outs[f"proj_{c}_type"].reshape(-1)[0]), c
+        np.testing.assert_array_equal(o, g)
+
+
+def test_aggregate_substring_golden():
+    """sum / count of a one-byte substring of a string column (the reference squeezes the [N, 1]
+    slice), and the slice times 2, which wraps in int8 as torch's int8 arithmetic does."""
+    from tqpk.operators import tqp_hash_aggregate
+    ins, outs, args = load("aggregate_substring")
+    tg = tg_from(ins, args["types"])
+    tqp_hash_aggregate(True, tg, copy.deepcopy(args["aggregate"]), None, None, "a")
+    order = np.argsort(outs["1"].reshape(-1), kind="stable")
+    np.testing.assert_array_equal(np_(tg[1].tensor), outs["1"][order])
+    for i in args["aggregate"]["out agg ids"]:
+        g, o = outs[str(i)][order], np_(tg[i].tensor)
+        assert o.dtype == g.dtype
+        np.testing.assert_array_equal(o, g)
+
+
 def test_aggregate_high_cardinality_vs_oracle():
     from tqpk.operators import tqp_hash_aggregate
     rng = np.random.default_rng(9)

@@ -263,3 +263,27 @@ def test_aggregate_float32(tag):
             assert_f64_close(agg[i], g)
         else:
             np.testing.assert_array_equal(agg[i], g, err_msg=str(i))
+
+
+def test_project_float32():
+    """The same float32 expressions as a projection: the oracle's float32 arithmetic is the
+    reference's bit for bit (and float64 where a float64 column takes part)."""
+    ins, outs, args = load("aggregate_float32")
+    cols, _ = f32_tag(ins, outs, "one")
+    proj = O.tqp_project(cols, args["project"])
+    for c in args["project"]["materialized out"]:
+        g = outs[f"proj_{c}"]
+        assert proj[c].dtype == g.dtype, c
+        np.testing.assert_array_equal(proj[c], g)
+
+
+def test_aggregate_substring():
+    """sum / count of a one-byte substring (alone and times 2, which wraps in int8 as torch's does)."""
+    ins, outs, args = load("aggregate_substring")
+    agg = O.tqp_hash_aggregate(dict(ins), args["aggregate"])
+    ids = args["aggregate"]["out agg ids"]
+    (k,), vals = _by_key([outs["1"]], *[outs[str(i)] for i in ids])
+    np.testing.assert_array_equal(agg[1].reshape(-1), k)
+    for i, g in zip(ids, vals):
+        assert agg[i].dtype == g.dtype, i
+        np.testing.assert_array_equal(agg[i], g)

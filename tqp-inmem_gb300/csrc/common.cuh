@@ -294,10 +294,25 @@ __device__ __forceinline__ uint64_t expr_apply_f32(const tqpk_expr_insn& X, uint
   return 0;
 }
 
+// An int64 result narrowed to torch's result dtype (two's complement wrap of int8 / uint8 / int32).
+__device__ __forceinline__ uint64_t int_wrap(uint64_t v, int wrap) {
+  switch (wrap) {
+    case TQPK_I8: return static_cast<uint64_t>(static_cast<int64_t>(static_cast<int8_t>(v)));
+    case TQPK_U8: return static_cast<uint64_t>(static_cast<uint8_t>(v));
+    case TQPK_I32: return static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(v)));
+  }
+  return v;
+}
+
 __device__ __forceinline__ uint64_t expr_apply(const tqpk_expr_insn& X, uint64_t a, uint64_t b, uint64_t c,
                                               const void* const* cols, const int* dts, int64_t row) {
   const bool f = X.type == TQPK_F64;
   if (X.type == TQPK_F32 && X.op != TQPK_X_SELECT) return expr_apply_f32(X, a, b);
+  if (X.wrap && X.type == TQPK_I64 && X.op >= TQPK_X_ADD && X.op <= TQPK_X_MUL) {
+    const uint64_t r = X.op == TQPK_X_ADD ? a + b : X.op == TQPK_X_SUB ? a - b
+                     : static_cast<uint64_t>(static_cast<int64_t>(a) * static_cast<int64_t>(b));
+    return int_wrap(r, X.wrap);
+  }
   switch (X.op) {
     case TQPK_X_F32TOF64:
       return static_cast<uint64_t>(__double_as_longlong(static_cast<double>(bits_f32(a))));

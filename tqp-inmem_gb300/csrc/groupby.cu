@@ -506,6 +506,9 @@ static int check_spec(const tqpk_groupby_spec* S, bool has_rows = true) {
     if (X.op == TQPK_X_F32TOF64 && (X.a < 0 || X.a >= i || X.type != TQPK_F64 || S->expr[X.a].type != TQPK_F32))
       return TQPK_EINVAL;
     if (X.op == TQPK_X_DIV && X.type == TQPK_I64) return TQPK_EUNSUPPORTED;
+    if (X.wrap && (X.type != TQPK_I64 || X.op < TQPK_X_ADD || X.op > TQPK_X_MUL ||
+                   (X.wrap != TQPK_I8 && X.wrap != TQPK_U8 && X.wrap != TQPK_I32)))
+      return TQPK_EINVAL;
     if (X.op == TQPK_X_SELECT) {
       if (X.a < 0 || X.a >= i || X.b < 0 || X.b >= i || X.col < 0 || X.col >= i) return TQPK_EINVAL;
       if (S->expr[X.a].type != TQPK_I64 || S->expr[X.b].type != X.type || S->expr[X.col].type != X.type)

@@ -50,7 +50,7 @@ class Predicate(C.Structure):
 
 class ExprInsn(C.Structure):
     _fields_ = [("op", C.c_int32), ("type", C.c_int32), ("a", C.c_int32), ("b", C.c_int32),
-                ("col", C.c_int32), ("pad", C.c_int32), ("ci", C.c_int64), ("cf", C.c_double)]
+                ("col", C.c_int32), ("wrap", C.c_int32), ("ci", C.c_int64), ("cf", C.c_double)]
 
 
 class Acc(C.Structure):

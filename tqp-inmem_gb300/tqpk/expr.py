@@ -77,6 +77,7 @@ class _Node:
     reg: int
     f64: bool
     dtype: torch.dtype
+    wide: bool = False        # a one-byte substring: the reference's [N, 1] slice (aggregate.py:114-119)
 
     @property
     def f32(self) -> bool:
@@ -124,12 +125,12 @@ class _Builder:
         self.accs: List[tuple] = [(L.ACC_COUNT_ROWS, L.I64, 0, 0, 0.0)]
         self.acc_memo: Dict[tuple, int] = {}
 
-    def _insn(self, key, op, f64, a=0, b=0, col=0, ci=0, cf=0.0, f32=False) -> int:
+    def _insn(self, key, op, f64, a=0, b=0, col=0, ci=0, cf=0.0, f32=False, wrap=0) -> int:
         if key in self.memo:
             return self.memo[key]
         if len(self.expr) >= L.MAX_EXPR:
             raise NotImplementedError(f"aggregate expressions exceed {L.MAX_EXPR} instructions")
-        self.expr.append((op, L.F32 if f32 else L.F64 if f64 else L.I64, a, b, col, ci, cf))
+        self.expr.append((op, L.F32 if f32 else L.F64 if f64 else L.I64, a, b, col, ci, cf, wrap))
         self.memo[key] = len(self.expr) - 1
         return self.memo[key]
 
@@ -197,6 +198,8 @@ class _Builder:
             literal, _, cast_type = tree[1][0].split(" ")
             if cast_type == "double":
                 return self.value(literal)
+        if len(tree) == 2 and tree[0] == "substring":
+            return self.substring(tree[1])
         if self.derived:
             if len(tree) == 8 and tree[0] == "CASE":
                 assert tree[1] == "WHEN" and tree[3] == "THEN" and tree[5] == "ELSE" and tree[7] == "END"
@@ -209,6 +212,27 @@ class _Builder:
             if (len(tree) == 2 and tree[0] in ("NOT", "StartsWith")) or (len(tree) == 3 and tree[1] in _COND_OPS):
                 return self.condition(tree)
         raise NotImplementedError(f"aggregate expression {tree!r} is not on the kernel path")
+
+    def substring(self, arg) -> _Node:
+        """substring(col, l, w) as a value (aggregate.py:114-119): the reference slices the [N, w]
+        string rows; only a one-byte slice gives weights its sum / count accept (squeezed to [N],
+        :179-182), so w = 1 is a column of those bytes (copied out of the rows), and anything wider
+        fails in the reference and raises here."""
+        sub, l, w = arg
+        cid, l, w = get_id(sub), int(l) - 1, int(w)
+        col = self.columns[cid]
+        if col.dim() != 2 or col.dtype not in (torch.int8, torch.uint8) or not 0 <= l < col.shape[1]:
+            raise NotImplementedError(f"substring of a {tuple(col.shape)} {col.dtype} column")
+        if w != 1:
+            raise NotImplementedError("a substring wider than one byte as an aggregate value (the reference's "
+                                      "bincount rejects [N, w] weights)")
+        key = ("substr", cid, l)
+        if key not in self.mask_memo:
+            hid = _HIDDEN_ID * 3 + len(self.mask_memo)
+            self.columns[hid] = col[:, l].contiguous()
+            self.mask_memo[key] = hid
+        n = self.column(self.mask_memo[key])
+        return _Node(n.reg, n.f64, n.dtype, wide=True)
 
     def condition(self, tree) -> _Node:
         """A boolean sub-expression as a bool column, filled by the filter kernel before the
@@ -229,6 +253,8 @@ class _Builder:
         """torch.where(c, t, e) with torch's promotion of the two branches."""
         if not isinstance(c, _Node) or c.dtype != torch.bool:
             raise NotImplementedError("CASE WHEN needs a boolean condition")
+        if any(isinstance(x, _Node) and x.wide for x in (c, t, e)):
+            raise NotImplementedError("a one-byte substring inside CASE WHEN")
         nodes = [x for x in (t, e) if isinstance(x, _Node)]
         pys = [x for x in (t, e) if not isinstance(x, _Node)]
         if any(n.f64 for n in nodes):
@@ -249,7 +275,11 @@ class _Builder:
                 dtype = torch.int64
             f64 = False
         regs = []
+        narrow = {torch.int8: "int8", torch.uint8: "uint8", torch.int32: "int32"}.get(dtype) if not f64 else None
         for x in (t, e):
+            if not isinstance(x, _Node) and narrow:       # a Python int taken into an int8/uint8/int32 where
+                import numpy as np                          # torch casts it to that dtype (wrapping)
+                x = int(np.array(int(x) & ((1 << 64) - 1), dtype=np.uint64).astype(narrow))
             n = x if isinstance(x, _Node) else self.const(float(x) if f64 else int(x))
             regs.append(self.to_f64(n) if f64 else n.reg)
         reg = self._insn(("sel", c.reg, regs[0], regs[1], f64), L.X_SELECT, f64, a=c.reg, b=regs[0], col=regs[1])
@@ -259,6 +289,11 @@ class _Builder:
         op_code = {"+": L.X_ADD, "-": L.X_SUB, "*": L.X_MUL, "/": L.X_DIV}[op]
         if not isinstance(a, _Node) and not isinstance(b, _Node):
             return {"+": a + b, "-": a - b, "*": a * b, "/": a / b}[op]
+        wides = [x.wide for x in (a, b) if isinstance(x, _Node)]
+        if any(wides) and not all(wides):
+            raise NotImplementedError("a one-byte substring with a column: the reference broadcasts [N, 1] "
+                                      "against [N]")
+        wide = any(wides)
         # torch promotion of the pair
         def kind(x):
             if isinstance(x, _Node):
@@ -272,7 +307,7 @@ class _Builder:
             # an integer tensor with a Python float, or an integer true division
             ra, rb = self.to_f32(a), self.to_f32(b)
             reg = self._insn((op, ra, rb, "f32"), op_code, False, a=ra, b=rb, f32=True)
-            return _Node(reg, False, torch.float32)
+            return _Node(reg, False, torch.float32, wide=wide)
         else:
             ints = [x.dtype for x in (a, b) if isinstance(x, _Node)]
             dtype = max(ints, key=lambda d: _INT_ORDER[d])
@@ -285,8 +320,10 @@ class _Builder:
         nb = b if isinstance(b, _Node) else self.const(float(b) if f64 else int(b))
         ra = self.to_f64(na) if f64 else na.reg
         rb = self.to_f64(nb) if f64 else nb.reg
-        reg = self._insn((op, ra, rb, f64), op_code, f64, a=ra, b=rb)
-        return _Node(reg, f64, dtype)
+        # torch's int8 / uint8 / int32 arithmetic wraps at its own width
+        wrap = 0 if f64 else {torch.int8: L.I8, torch.uint8: L.U8, torch.int32: L.I32}.get(dtype, 0)
+        reg = self._insn((op, ra, rb, f64, wrap), op_code, f64, a=ra, b=rb, wrap=wrap)
+        return _Node(reg, f64, dtype, wide=wide)
 
     def acc(self, kind: int, node: _Node, init_i=0, init_f=0.0) -> int:
         key = (kind, node.reg, node.f64, init_i, init_f)
@@ -346,6 +383,10 @@ def _add_output(b: _Builder, prog: AggregateProgram, oid: int, fn: str, arg):
         return
     if scalar:                                              # aggregate.py:149-152: full(cnt_rows, v)
         v = b.const(v)
+    if v.wide and fn not in ("sum", "count"):
+        # min/max scatter [N, 1] values by an [N] index and avg's bincount takes 1-D weights only: the
+        # reference fails on these (only sum and count squeeze their values first, :179-182)
+        raise NotImplementedError(f"{fn} of a substring: the reference fails on its [N, 1] values")
     if v.f32:
         # a float32 expression: accumulated from its exact float64 value; the output is rounded to
         # float32 (sum, min, max, and avg of the 1-step path; the 2-step avg is float64, :170)
@@ -396,7 +437,7 @@ def compile_aggregate(args: dict, columns: Dict[int, torch.Tensor], derived: boo
         if hit is not None:
             return _rebind(hit[0], hit[1], columns)
     prog, col_ids = _compile_aggregate(args, columns, derived, key_codes)
-    if sig is not None and not prog.masks:
+    if sig is not None and not prog.masks and all(c < _HIDDEN_ID for c in col_ids):   # no derived columns
         if len(_AGG_MEMO) >= _AGG_MEMO_MAX:
             _AGG_MEMO.clear()
         _AGG_MEMO[sig] = (prog, col_ids)
@@ -479,8 +520,8 @@ def _compile_aggregate(args: dict, columns: Dict[int, torch.Tensor], derived: bo
         s.col_dtypes[i] = code_of(t.dtype)
     prog.tensors.extend(b.col_tensors)
     s.n_expr = len(b.expr)
-    for i, (op, ty, a, bb, col, ci, cf) in enumerate(b.expr):
-        s.expr[i] = L.ExprInsn(op, ty, a, bb, col, 0, ci, cf)
+    for i, (op, ty, a, bb, col, ci, cf, wrap) in enumerate(b.expr):
+        s.expr[i] = L.ExprInsn(op, ty, a, bb, col, wrap, ci, cf)
     s.n_accs = len(b.accs)
     for i, (kind, ty, reg, ii, ff) in enumerate(b.accs):
         s.accs[i] = L.Acc(kind, ty, reg, 0, ii, ff)
@@ -528,9 +569,9 @@ def compile_projection(trees, columns: Dict[int, torch.Tensor], derived: bool = 
         spec.cols[i] = t.data_ptr()
         spec.col_dtypes[i] = code_of(t.dtype)
     spec.n_expr = len(b.expr)
-    for i, (op, ty, a, bb, col, ci, cf) in enumerate(b.expr):
+    for i, (op, ty, a, bb, col, ci, cf, wrap) in enumerate(b.expr):
         X = spec.expr[i]
-        X.op, X.type, X.a, X.b, X.col, X.ci, X.cf = op, ty, a, bb, col, ci, cf
+        X.op, X.type, X.a, X.b, X.col, X.ci, X.cf, X.wrap = op, ty, a, bb, col, ci, cf, wrap
     spec.n_accs = 1
     spec.accs[0].kind, spec.accs[0].type = L.ACC_COUNT_ROWS, L.I64
     return ProjectionProgram(spec=spec, tensors=list(b.col_tensors), outputs=outs, masks=b.masks)

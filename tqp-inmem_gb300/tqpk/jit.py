@@ -466,7 +466,9 @@ def _expr_code(S, upto: int, colpfx: str, contract: bool = False) -> Tuple[List[
                 lines.append(f"const double r{i} = {fn}(r{X.a}, r{X.b});")
             else:
                 op = {L.X_ADD: "+", L.X_SUB: "-", L.X_MUL: "*"}[X.op]
-                lines.append(f"const i64 r{i} = r{X.a} {op} r{X.b};")
+                cast = {L.I8: "(signed char)", L.U8: "(unsigned char)", L.I32: "(int)"}.get(X.wrap, "")
+                expr = f"(u64)r{X.a} {op} (u64)r{X.b}" if X.op != L.X_MUL else f"r{X.a} {op} r{X.b}"
+                lines.append(f"const i64 r{i} = (i64){cast}({expr});" if cast else f"const i64 r{i} = r{X.a} {op} r{X.b};")
     return sorted(used), lines
 
 

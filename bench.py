@@ -601,15 +601,20 @@ class Batched:
            [[["count", ["1"]], "#", "108L"], "AS", "h#208"]]
     AGG_IDS = [201, 202, 203, 204, 205, 206, 207, 208]
 
-    def __init__(self, n_instances=64):
+    def __init__(self, n_instances=64, scale: float = 1.0):
         from tqpk import datagen
         self.dg = datagen
         self.specs = datagen.batch_specs(n_instances, seed=3)
+        if scale != 1.0:          # every instance's rows x scale, the same group counts (profiler captures)
+            for sp in self.specs:
+                sp["rows"] = max(1000, int(sp["rows"] * scale))
         self.fact_rows = sum(s["rows"] for s in self.specs)
         self.config = {"workload": "64 uneven instances: filter+group-by and join+aggregate+top-10, one persistent "
                                    "launch (CUDA graph) vs per-instance drop-in operators",
                        "instances": n_instances, "total_rows": self.fact_rows,
                        "rows_range": [10_000, 10_000_000], "group_range": [4, 1_000_000]}
+        if scale != 1.0:
+            self.config["scale"] = scale
 
     def setup_device(self, dev):
         import torch
@@ -762,7 +767,7 @@ def run_batched_bench(args):
     G.build()
     lib = L.load()
     dev = torch.device("cuda", 0)
-    w = Batched()
+    w = Batched(scale=args.scale)
     w.setup_device(dev)
     w.run_batched()
     torch.cuda.synchronize()
@@ -1432,7 +1437,7 @@ def main():
     ap.add_argument("--workload", choices=["all"] + sorted(WORKLOADS) + ["batched", "serving"], default="all",
                     help="all (default): the join query as the headline, every other workload as a sub-record")
     ap.add_argument("--scale", type=float, default=1.0,
-                    help="star_join only: table sizes x scale (a small case for profiler captures)")
+                    help="star_join and batched only: table sizes x scale (a small case for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

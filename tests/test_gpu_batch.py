@@ -139,7 +139,7 @@ def test_generated_batch_table_modes_and_empty_instances():
     sums of every placement (per thread, shared copies, global) and instances with no rows, in one
     generated batch."""
     from tqpk.jitbatch import QueryBatch, _mode
-    shapes = [("groupby", 200_000, 4), ("groupby", 200_000, 150), ("groupby", 200_000, 1400),
+    shapes = [("groupby", 200_000, 2), ("groupby", 200_000, 150), ("groupby", 200_000, 500),
               ("groupby", 200_000, 30_000), ("groupby", 0, 9), ("join", 0, 100), ("join", 50_000, 1),
               ("join", 300_000, 40), ("join", 300_000, 500), ("join", 100_000, 60_000)]
     insts, expected = [], []
@@ -150,7 +150,8 @@ def test_generated_batch_table_modes_and_empty_instances():
     b = QueryBatch(insts)
     placements = {(int(b.recs[i].mode), int(b.recs[i].copies)) for i, (kind, _, _) in enumerate(shapes)
                   if kind == "groupby"}
-    assert {(1, 256), (2, 8), (2, 1), (4, 1)} <= placements
+    assert (1, 256) in placements and (2, 1) in placements and (4, 1) in placements
+    assert any(m == 2 and 1 < c < 256 for m, c in placements)
     join_modes = {int(b.recs[i].mode) for i, (kind, rows, _) in enumerate(shapes) if kind == "join" and rows}
     assert join_modes == {0, 1, 2}
     b.run()

@@ -45,7 +45,12 @@ from .dtypes import code_of, dtype_of
 from .expr import compile_aggregate, require_f64_outputs
 from .predicate import compile_filter
 
-SMEM = 96 * 1024          # dynamic shared memory of the persistent kernel (group tables)
+# dynamic shared memory of the persistent kernel (group tables, join sums) and its CTAs per SM:
+# 64-instance batch 2.32 ms with 96 KB at 2 CTAs per SM, 2.06 ms with 48 KB at 3, 1.95 ms with 32 KB
+# at 4 (more warps to cover the reductions' and loads' latency outweigh the smaller shared tables),
+# 2.37 ms at 5 (registers spill)
+SMEM = 32 * 1024
+MIN_CTAS = 4
 T = 256                   # threads per CTA
 MAXK = 32                 # join top-k bound (one warp-list row per lane)
 
@@ -519,7 +524,7 @@ def batch_source(gb_progs, join_progs) -> str:
     jb = "\n".join(f"        case {p}: jn_build_{p}(I, W.begin, W.end, err); break;" for p in range(len(join_progs)))
     jp = "\n".join(f"        case {p}: jn_probe_{p}(I, W.begin, W.end, sm); break;" for p in range(len(join_progs)))
     parts.append(f"""
-extern "C" __global__ void __launch_bounds__({T}) tqpk_qb_run(const QInst* __restrict__ insts,
+extern "C" __global__ void __launch_bounds__({T}, {MIN_CTAS}) tqpk_qb_run(const QInst* __restrict__ insts,
     const WorkItem* __restrict__ items, int n_items, unsigned* ticket, unsigned long long* done, int* err,
     unsigned long long* trace) {{
   extern __shared__ u64 sm[];

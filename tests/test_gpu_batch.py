@@ -171,3 +171,18 @@ def test_generated_batch_dependency_wait_times_out():
     torch.cuda.synchronize()
     with pytest.raises(TimeoutError):
         b.check_error()
+
+
+def test_generated_batch_key_outside_its_domain_is_reported():
+    """A group key outside the instance's declared key domain: the row is skipped (no table write
+    past the domain) and the batch reports TQPK_EINVAL (ValueError)."""
+    from tqpk.batch import GroupByInstance
+    from tqpk.jitbatch import QueryBatch
+    inst, _ = make_groupby(50_000, 150, 401)
+    (a0, a1), (b0, b1) = inst.key_domains
+    narrow = GroupByInstance(args=inst.args, columns=inst.columns, filter_tree=inst.filter_tree,
+                             filter_cols=inst.filter_cols, key_domains=[(a0, a1 - 1), (b0, b1)])
+    b = QueryBatch([narrow])
+    b.run()
+    with pytest.raises(ValueError):
+        b.results()

@@ -175,7 +175,7 @@ def _gb_functions(p: int, spec, pred) -> str:
     lit_decls, pexpr = _hoist(pexpr, "I")
     ecols, elines = jit._expr_code(S, S.n_expr, "c", contract=True)   # sums only: x * (1 - y) as one FMA
     kcols = list(range(S.n_keys))
-    src = [f"__device__ void gb_agg_{p}(const QInst& I, i64 b, i64 e, u64* sm) {{",
+    src = [f"__device__ void gb_agg_{p}(const QInst& I, i64 b, i64 e, u64* sm, int* err) {{",
            f"  constexpr int A = {A};",
            "  const i64 K = I.slots, n = I.n;",
            "  const int mode = I.mode, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;",
@@ -186,7 +186,7 @@ def _gb_functions(p: int, spec, pred) -> str:
         src += ["  " + d for d in _ptr_decls(pcols, pred.dtypes, "pc", "pp")]
     src += ["  " + d for d in _ptr_decls(kcols, S.key_dtypes, "kc", "kp")]
     src += ["  " + d for d in _ptr_decls(ecols, S.col_dtypes, "vc", "cp")]
-    src += [f"  const i64 km{k} = I.kmin[{k}], ks{k} = I.kstride[{k}];" for k in kcols]
+    src += [f"  const i64 km{k} = I.kmin[{k}], ks{k} = I.kstride[{k}], kr{k} = I.krange[{k}];" for k in kcols]
     inits = " : ".join(f"(a == {i}) ? {jit._acc_init(S.accs[i])}" for i in range(A)) + " : 0ull"
     src += ["  // table copies in shared memory: one per thread (mode 1, plain updates), or `copies`",
             "  // (a power of two) shared by threads tid % copies with shared-memory atomics (mode 2);",
@@ -207,6 +207,11 @@ def _gb_functions(p: int, spec, pred) -> str:
     src += ["#pragma unroll", "    for (int j = 0; j < 4; ++j) {", "      if (r0 + j >= e) break;",
             f"      if (!({jit._rename(pexpr, 'p', 'P')})) continue;"]
     slot = " + ".join(f"((i64)Kc{k}.v[j] - km{k}) * ks{k}" for k in kcols) or "0"
+    # a key outside its declared domain would index past the table: the row is skipped and the
+    # batch reports TQPK_EINVAL
+    if kcols:
+        src.append("      if (" + " || ".join(f"(u64)((i64)Kc{k}.v[j] - km{k}) >= (u64)kr{k}" for k in kcols)
+                   + ") { set_err(err, -1); continue; }")
     src.append(f"      const i64 slot = {slot};")
     src += ["      " + jit._rename(l, "c", "Cv") for l in elines]
     for a in range(A):
@@ -518,7 +523,7 @@ def batch_source(gb_progs, join_progs) -> str:
         parts.append(body + "\n" + _gb_emit_outputs(p, spec, outputs))
     for p, (spec, vreg, ppred, bpred) in enumerate(join_progs):
         parts.append(_join_functions(p, spec, vreg, ppred, bpred))
-    gb_agg = "\n".join(f"        case {p}: gb_agg_{p}(I, W.begin, W.end, sm); break;" for p in range(len(gb_progs)))
+    gb_agg = "\n".join(f"        case {p}: gb_agg_{p}(I, W.begin, W.end, sm, err); break;" for p in range(len(gb_progs)))
     gb_emit = "\n".join(f"        case {p}: gb_emit_{p}(I, W.begin / I.range_slots, W.begin, W.end, sw); break;"
                         for p in range(len(gb_progs)))
     jb = "\n".join(f"        case {p}: jn_build_{p}(I, W.begin, W.end, err); break;" for p in range(len(join_progs)))

@@ -350,3 +350,20 @@ def test_groupby_pipeline_domains_and_graph_replay(n, groups):
         for oid in args["out agg ids"]:
             e = ref[oid]
             (assert_f64_close if e.dtype == np.float64 else np.testing.assert_array_equal)(outs[oid].cpu().numpy(), e)
+
+
+def test_groupby_pipeline_key_outside_declared_domain_raises():
+    """GroupByPipeline's key domains are table statistics given by the caller: a key outside them is
+    not written past the table; result() raises ValueError (TQPK_EINVAL)."""
+    from tqpk import datagen
+    from tqpk.pipeline import GroupByPipeline
+    t, (a, b) = datagen.groupby_instance_tables(100_000, 40, 5)
+    ids = {"quantity": 1, "price": 2, "discount": 3, "tax": 4, "flag": 5, "status": 6, "ship_date": 7}
+    d = {ids[k]: torch.from_numpy(v).cuda() for k, v in t.items()}
+    args = {"is partial": False, "keys": ["flag#5", "status#6"], "input ids": [1, 2, 5, 6],
+            "results": ["flag#5", "status#6", [[["sum", ["quantity#1"]], "#", "1"], "AS", "q#101"]],
+            "out agg ids": [101]}
+    p = GroupByPipeline(args, {c: d[c] for c in (1, 2, 5, 6)}, None, {}, [(0, a - 2), (0, b - 1)])
+    p.run()
+    with pytest.raises(ValueError):
+        p.result()

@@ -210,7 +210,8 @@ def _shape_key(*structs) -> bytes:
     return b"|".join(out)
 
 
-def run_groupby(spec, pred, plan, ws, n: int, stream: int, pred_tensors=(), key_tensors=(), col_tensors=()):
+def run_groupby(spec, pred, plan, ws, n: int, stream: int, pred_tensors=(), key_tensors=(), col_tensors=(),
+                err_ptr=None):
     """Accumulation pass of ops.groupby as a query-specialised kernel (table in ws).  The
     generated kernel is looked up by the shape of the spec, predicate and plan, so a
     repeated query shape skips the source generation."""
@@ -236,6 +237,7 @@ def run_groupby(spec, pred, plan, ws, n: int, stream: int, pred_tensors=(), key_
     a.i32(_aligned(*pred_tensors) if pred is not None else 1)
     a.i32(_aligned(*key_tensors))
     a.i32(_aligned(*col_tensors))
+    a.ptr(err_ptr)
     grid = occupancy_grid(h, T, smem, (n + 3) // 4)
     launch(h, grid, T, smem, a, stream, L.KID_GROUPBY)
 
@@ -568,7 +570,7 @@ def groupby_source(spec, pred, plan) -> Tuple[str, str, int, int]:
     params += ["const PL lp"]
     params += [f"const void* __restrict__ kp{k}" for k in kcols]
     params += [f"const void* __restrict__ cp{c}" for c in range(S.n_cols)]
-    params += ["i64 n", "u64* __restrict__ gacc", "int vp", "int vk", "int vc"]
+    params += ["i64 n", "u64* __restrict__ gacc", "int vp", "int vk", "int vc", "int* __restrict__ err"]
     src.append("    " + ",\n    ".join(params) + ") {")
     src.append(f"  constexpr int T = {T}; constexpr int A = {A}; constexpr i64 K = {K}LL;")
     inits = " : ".join(f"(a == {i}) ? {_acc_init(S.accs[i])}" for i in range(A)) + " : 0ull"
@@ -591,6 +593,12 @@ def groupby_source(spec, pred, plan) -> Tuple[str, str, int, int]:
     src.append("    for (int j = 0; j < 4; ++j) {")
     src.append("      if (r0 + j >= n) break;")
     src.append(f"      if (!({_rename(pexpr, 'p', 'P')})) continue;")
+    # a key outside the plan's domain (key domains given as table statistics) would index past
+    # the table: the row is skipped and TQPK_EINVAL recorded in *err (when given)
+    if kcols:
+        src.append("      if (" + " || ".join(f"(u64)((i64)Kc{k}.v[j] - ({int(plan.key_min[k])}LL)) >= "
+                                              f"{int(plan.key_range[k])}ull" for k in kcols)
+                   + ") { if (err) atomicCAS(err, 0, -1); continue; }")
     slot = " + ".join(f"((i64)Kc{k}.v[j] - ({int(plan.key_min[k])}LL)) * {int(plan.key_stride[k])}LL" for k in kcols) or "0"
     src.append(f"      const i64 slot = {slot};")
     src += ["      " + _rename(l, "c", "Cv") for l in elines]

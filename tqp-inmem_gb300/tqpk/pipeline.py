@@ -546,6 +546,8 @@ class GroupByPipeline:
         self.args.i32(jit._aligned(*self.pred.tensors) if self.pred is not None else 1)
         self.args.i32(jit._aligned(*self.prog.tensors[:nk]))
         self.args.i32(jit._aligned(*self.prog.tensors[nk:]))
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)    # a key outside its domain
+        self.args.ptr(self.err.data_ptr())
         self.grid = jit.occupancy_grid(self.kernel, self.T, self.smem, (self.n + 3) // 4)
 
     def run(self, stream=None):
@@ -554,6 +556,8 @@ class GroupByPipeline:
         S = self.prog.spec
         L.check(self.lib.tqpk_groupby_prepare(C.byref(S), C.byref(self.plan), self.ws.data_ptr(), self.ws.numel(), s),
                 "tqpk_groupby_prepare")
+        with torch.cuda.stream(stream or torch.cuda.current_stream(self.dev)):
+            self.err.zero_()
         if self.n > 0:
             jit.launch(self.kernel, self.grid, self.T, self.smem, self.args, s, L.KID_GROUPBY)
         L.check(self.lib.tqpk_groupby_emit_async(C.byref(S), C.byref(self.plan), self.ws.data_ptr(), self._kp,
@@ -572,8 +576,12 @@ class GroupByPipeline:
         self.graph.replay()
 
     def result(self):
-        """(key columns [G], {out id: column [G]}, G) after the last run (synchronises)."""
+        """(key columns [G], {out id: column [G]}, G) after the last run (synchronises).  A key
+        outside its declared domain raises ValueError (TQPK_EINVAL)."""
         G = int(self.groups.item())
         if G < 0:
             L.check(G, "group-by emit")
+        e = int(self.err.item())
+        if e:
+            L.check(e, "group-by (a key outside its declared domain)")
         return ([k[:G] for k in self.keys], {oid: o[:G] for (oid, *_), o in zip(self.prog.outputs, self.outs)}, G)

@@ -444,6 +444,7 @@ class GpuExecutor:
         a.i32(1)
         a.i32(1)
         a.i32(1)
+        a.ptr(None)             # error word: none (the plan's domains come from the data)
         if n > 0:
             jit.launch(self.gb_kernel, self.gb_grid, self.gb_T, self.gb_smem, a, s, L.KID_GROUPBY)
         kp = (C.c_void_p * max(nk, 1))(*[k.data_ptr() for k in keys])

@@ -217,8 +217,11 @@ struct TopkOut {
 // kTopkCap), and the last CTA of that pass sorts the list bitonically by
 // (key, index) in shared memory.  When ties push more than kTopkSortCap items
 // under the cut, that CTA falls back to the warp lists over all items (same
-// result, slower).  The cut itself is computed by the last CTA of the first
-// pass, so the whole top-k is two launches.
+// result, slower).  For k > 32 the cut is computed by the last CTA of the
+// first pass and the top-k is two launches; for k <= 32 every CTA of the
+// second pass derives the cut from the group bests (tk_bin_cut), and when
+// each CTA's group fits one sweep of its threads the two passes run as one
+// cooperative launch with a grid barrier between them (k_tk_fused below).
 constexpr int kTopkCap = 4096;
 constexpr int kTopkGroups = 512;     // >= 2 x the largest k: the cut stays near the k-th item
 constexpr int kTopkCand = kTopkCap + kTopkGroups;   // cand_key entries used: candidates, then group bests

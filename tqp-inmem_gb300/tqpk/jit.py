@@ -317,11 +317,19 @@ def launch(handle: int, grid: int, block: int, smem: int, args: _Args, stream: i
     L.check(L.load().tqpk_jit_launch(handle, grid, block, smem, arr, timing_kid, stream), "tqpk_jit_launch")
 
 
+_occ_cache: Dict[Tuple[int, int, int], int] = {}
+
+
 def occupancy_grid(handle: int, block: int, smem: int, work_units: int) -> int:
-    lib = L.load()
-    per_sm = max(1, lib.tqpk_jit_occupancy(handle, block, smem))
+    """Blocks for work_units threads, capped at one full wave (resident CTAs per SM, from the
+    occupancy API once per kernel and launch shape, x SMs)."""
+    key = (handle, block, smem)
+    cap = _occ_cache.get(key)
+    if cap is None:
+        lib = L.load()
+        cap = _occ_cache[key] = max(1, lib.tqpk_jit_occupancy(handle, block, smem)) * lib.tqpk_num_sms()
     g = (work_units + block - 1) // block
-    return max(1, min(g, per_sm * lib.tqpk_num_sms()))
+    return max(1, min(g, cap))
 
 
 # ---------------------------------------------------------------------------- code pieces

@@ -54,6 +54,7 @@ def test_groupby_kernel_compiles_for_each_table_mode():
         ok, log = jit.check_compiles(src)
         assert ok, log[:2000]
         assert "2470" not in src and "1000.5" not in src    # literals are bound at launch
+        assert "atomicCAS(err, 0, -1)" in src                # keys outside the plan's domain
     # float32 registers (an integer column with a Python float, integer true division, CASE with
     # a float literal beside integers) in the generated accumulation and projection kernels
     q = {1: torch.zeros(64, dtype=torch.int64), 2: torch.zeros(64, dtype=torch.int64), 5: d[5]}
@@ -123,6 +124,12 @@ def test_generated_batch_kernel_compiles_and_record_layout_matches():
     probe = src + "\nstatic_assert(sizeof(QInst) == %d, \"record size\");\n" % C_sizeof(QB.QInst)
     ok, log = jit.check_compiles(probe)
     assert ok, log[:3000]
+    # group keys checked against the instance's domain; global tables updated by reductions; the
+    # persistent kernel's 4 CTAs per SM; the result-packing kernel of results_host
+    assert ">= (u64)kr0" in src and "set_err(err, -1)" in src and "gred_add(" in src
+    assert f"__launch_bounds__(256, {QB.MIN_CTAS}) tqpk_qb_run" in src
+    ok, log = jit.check_compiles(QB._PACK_SRC)
+    assert ok, log[:2000]
 
 
 def C_sizeof(t):

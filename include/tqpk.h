@@ -244,6 +244,14 @@ int tqpk_key_range(const void* d_col, int32_t dtype, int64_t n, void* d_scratch,
  * restores the defaults.  Process-wide and not thread-safe.              */
 int tqpk_debug_compact_wait(int32_t spin_limit, int64_t stall_tile);
 
+/* Test hook, no counterpart in the reference: the poll limit (<= its
+ * default) of the single-launch top-k's grid barrier (k <= 32, the fused
+ * pipelines) and a number of arrivals (0-1024) it also waits for that never
+ * come.  With missing > 0 every CTA's bounded wait runs out and the pipeline
+ * reports TQPK_ETIMEOUT in its error word.  (2097152, 0) restores the
+ * defaults.  Process-wide and not thread-safe.                            */
+int tqpk_debug_topk_barrier(int32_t spin_limit, int32_t missing);
+
 /* ---- (d) group-by aggregation ----------------------------------------- */
 /* Computes the key ranges of the rows passing the filter (d_mask or h_pred,
  * either may be NULL) and picks the kernel.  Synchronises.                */

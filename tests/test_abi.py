@@ -103,3 +103,12 @@ def test_compaction_wait_hook_checks_arguments(lib):
     assert lib.tqpk_debug_compact_wait(1 << 22, -1) == _lib.EINVAL
     assert lib.tqpk_debug_compact_wait(16, -2) == _lib.EINVAL
     assert lib.tqpk_debug_compact_wait(1 << 21, -1) == _lib.OK          # the defaults
+
+
+def test_topk_barrier_hook_checks_arguments(lib):
+    from tqpk import _lib
+    assert lib.tqpk_debug_topk_barrier(-1, 0) == _lib.EINVAL
+    assert lib.tqpk_debug_topk_barrier((1 << 21) + 1, 0) == _lib.EINVAL
+    assert lib.tqpk_debug_topk_barrier(100, -1) == _lib.EINVAL
+    assert lib.tqpk_debug_topk_barrier(100, 1025) == _lib.EINVAL
+    assert lib.tqpk_debug_topk_barrier(1 << 21, 0) == _lib.OK           # the defaults

@@ -93,3 +93,32 @@ def test_compaction_correct_after_a_timeout(lib):
         keep = mask.cpu().numpy()
         assert m == int(keep.sum())
         np.testing.assert_array_equal(out[:m].cpu().numpy(), col.cpu().numpy()[keep])
+
+
+def test_topk_grid_barrier_timeout_is_reported(lib):
+    """The single-launch top-k's grid barrier (fused join pipeline, k <= 32) made to wait for an
+    arrival that never comes: every CTA's bounded wait runs out, the pipeline's error word holds
+    TQPK_ETIMEOUT and result_device raises TimeoutError; the next run, with the defaults back, is
+    the same as the one before."""
+    from tqpk import _lib as L, datagen
+    from tqpk.pipeline import JoinAggTopK
+    t = {k: torch.from_numpy(v).cuda() for k, v in datagen.join_tables(100_000, 400_003, 71).items()}
+    pipe = JoinAggTopK(t["b_key"], 1, 100_000, t["p_fk"], {12: t["b_date"]}, [["bd#12", "<", "1170"]],
+                       {22: t["p_date"], 23: t["p_price"], 24: t["p_discount"]}, [["pd#22", ">", "1170"]],
+                       [["p#23", "*", ["1.0", "-", "d#24"]]], k=10)
+    pipe.run()
+    keys0, vals0, m0 = pipe.result_device()
+    keys0, vals0 = keys0.cpu().numpy(), vals0.cpu().numpy()
+    assert lib.tqpk_debug_topk_barrier(4096, 1) == L.OK
+    try:
+        pipe.run()
+        with pytest.raises(TimeoutError):
+            pipe.result_device()
+    finally:
+        assert lib.tqpk_debug_topk_barrier(DEFAULT_SPIN_LIMIT, 0) == L.OK
+    pipe.run()
+    keys1, vals1, m1 = pipe.result_device()
+    assert m1 == m0 == 10
+    np.testing.assert_array_equal(keys1.cpu().numpy(), keys0)
+    np.testing.assert_allclose(vals1.cpu().numpy(), vals0, rtol=1e-12)
+

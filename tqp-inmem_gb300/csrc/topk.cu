@@ -12,6 +12,11 @@ __device__ __forceinline__ bool ArraySource::get(int64_t i, uint64_t& k) const {
   return true;
 }
 
+// Test hook (tqpk_debug_topk_barrier): the poll limit of the single-launch top-k's grid barrier and
+// a number of arrivals it also waits for that never come.
+static int g_tk_spin_limit = kSpinLimit;
+static int g_tk_missing = 0;
+
 // CTAs of k_tk_fused<Src> that fit on the device at once (the cooperative launch's limit).
 template <class Src>
 static int fused_capacity() {
@@ -45,7 +50,7 @@ static int launch_r(const Src& src, int k, int grid, TopkOut O, cudaStream_t s) 
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    TQPK_CUDA(cudaLaunchKernelEx(&cfg, k_tk_fused<Src>, src, G, k, O, (int)kSpinLimit));
+    TQPK_CUDA(cudaLaunchKernelEx(&cfg, k_tk_fused<Src>, src, G, k, O, g_tk_spin_limit, g_tk_missing));
     return TQPK_OK;
   }
   k_tk_group_best<Src><<<ng, 256, 0, s>>>(src, G, k, O);
@@ -80,6 +85,16 @@ __global__ void k_topk_positions_to_perm(const int64_t* idx, const int64_t* coun
 }  // namespace tqpk
 
 using namespace tqpk;
+
+// Test hook: the poll limit of the single-launch top-k's grid barrier, and arrivals it also waits
+// for that never come (its bounded wait then runs out: TQPK_ETIMEOUT in the caller's error word).
+// (kSpinLimit, 0) restores the defaults.  Not thread-safe; for tests only.
+extern "C" int tqpk_debug_topk_barrier(int32_t spin_limit, int32_t missing) {
+  if (spin_limit < 0 || spin_limit > kSpinLimit || missing < 0 || missing > 1024) return TQPK_EINVAL;
+  g_tk_spin_limit = spin_limit;
+  g_tk_missing = missing;
+  return TQPK_OK;
+}
 
 extern "C" size_t tqpk_topk_workspace_bytes(int64_t n, int64_t k) {
   if (n < 0) n = 0;

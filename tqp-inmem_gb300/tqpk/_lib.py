@@ -150,6 +150,7 @@ SIGNATURES = {
     "tqpk_compact_noalloc_max_rows": (_I64, []),
     "tqpk_compact_noalloc": (C.c_int, [_P(Predicate), _VP, _I64, _I32, _P(_VP), _P(_I32), _P(_VP), _VP, _VP]),
     "tqpk_debug_compact_wait": (C.c_int, [_I32, _I64]),
+    "tqpk_debug_topk_barrier": (C.c_int, [_I32, _I32]),
     "tqpk_key_range": (C.c_int, [_VP, _I32, _I64, _VP, _P(_I64), _P(_I64), _VP]),
     "tqpk_timing_begin": (C.c_int, [_I32]),
     "tqpk_timing_end": (C.c_int, [_P(C.c_double), _P(_I32)]),

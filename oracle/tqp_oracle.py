@@ -290,10 +290,23 @@ def _cond_ids(tree, out):
 
 
 def index_with_null(data: np.ndarray, idx: np.ndarray) -> np.ndarray:
-    """conversion.py:52-57"""
+    """conversion.py:52-57: data[idx] with NULL rows where idx is NULL.
+
+    The reference fills with ``masked_fill_(mask, null)``, which broadcasts the [K] mask against
+    the gathered rows from the right.  For a 2-D [K, w] result that works only for K == 1 (the
+    row) or K == w (column j of every row where idx[j] is NULL); any other K raises RuntimeError,
+    and so does this restatement."""
     m = idx == NULL
-    out = data[np.where(m, 0, idx)]
-    out = out.copy()
+    out = data[np.where(m, 0, idx)].copy()
+    if out.ndim == 2:
+        K, w = out.shape
+        if K == w:
+            out[:, m] = NULL
+        elif K == 1:
+            out[m] = NULL
+        else:
+            raise RuntimeError(f"the [{K}] null mask does not broadcast over [{K}, {w}] rows")
+        return out
     out[m] = NULL
     return out
 

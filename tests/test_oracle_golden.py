@@ -287,3 +287,12 @@ def test_aggregate_substring():
     for i, g in zip(ids, vals):
         assert agg[i].dtype == g.dtype, i
         np.testing.assert_array_equal(agg[i], g)
+
+
+def test_join_outer_string_payload_raises():
+    """The reference's right-outer join raised RuntimeError on this fixture: the null fill of an
+    [N, w] build-side column broadcasts its [K] mask over the [K, w] rows (conversion.py:52-57)."""
+    ins, outs, args = load("join_outer_string_payload")
+    assert str(outs["raised"].reshape(-1)[0]) == args["error"] == "RuntimeError"
+    with pytest.raises(RuntimeError):
+        O.join_vortex(dict(ins), args["join"], 11, 21, "right-outer")

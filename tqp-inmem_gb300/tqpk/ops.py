@@ -462,24 +462,42 @@ def encode_keys(keys: Sequence[torch.Tensor], mask: Optional[torch.Tensor] = Non
 
 
 def gather(cols: Sequence[torch.Tensor], idx: torch.Tensor, null_aware: bool = False) -> List[torch.Tensor]:
-    """out_c = col_c[idx]; with null_aware an index of -64 yields -64 (index_with_null).
-    2-D (string) columns are gathered row by row."""
-    lib = L.load()
-    if any(c.dim() == 2 and c.shape[1] != 1 for c in cols):
-        if null_aware:
-            # the reference's index_with_null masks [M, w] rows with an [M] mask, which does not
-            # broadcast: its right-outer join raises RuntimeError here too (conversion.py:52-57)
-            raise RuntimeError("null-filled rows of a 2-D column (right-outer join payload): the [M] null "
-                               "mask does not broadcast over [M, w] rows")
+    """out_c = col_c[idx], shaped as torch's indexing shapes it: [K] for a 1-D column, [K, w] for a
+    2-D [N, w] column (string rows gathered row by row; [N, 1] through the 1-D kernel).  With
+    null_aware an index of -64 yields -64, as the reference's index_with_null (conversion.py:52-57);
+    a 2-D column follows that function's broadcast rule (_index_with_null_2d)."""
+    if any(c.dim() == 2 for c in cols):
         out = [None] * len(cols)
-        flat = [(i, c) for i, c in enumerate(cols) if not (c.dim() == 2 and c.shape[1] != 1)]
-        for i, c in enumerate(cols):
-            if c.dim() == 2 and c.shape[1] != 1:
-                out[i] = gather_rows(c, idx)
+        flat = [i for i, c in enumerate(cols) if c.dim() == 1 or (c.shape[1] == 1 and not null_aware)]
+        rows = set(range(len(cols))) - set(flat)
+        for i in sorted(rows):
+            out[i] = _index_with_null_2d(cols[i], idx) if null_aware else gather_rows(cols[i], idx)
         if flat:
-            for (i, _), o in zip(flat, gather([c for _, c in flat], idx)):
-                out[i] = o
+            for i, o in zip(flat, _gather_1d([cols[i].reshape(-1) for i in flat], idx, null_aware)):
+                out[i] = o.reshape(-1, 1) if cols[i].dim() == 2 else o
         return out
+    return _gather_1d(cols, idx, null_aware)
+
+
+def _index_with_null_2d(col: torch.Tensor, idx: torch.Tensor) -> torch.Tensor:
+    """index_with_null (conversion.py:52-57) of a 2-D [N, w] column.  The reference gathers with
+    null indices read as row 0, then calls masked_fill_ with the [K] null mask, which torch
+    broadcasts against the [K, w] rows from the right.  K == 1 fills the row, K == w fills column j
+    of every row whose index j is null, and any other K is refused with RuntimeError (the
+    reference's right-outer join raises there).  The same three outcomes here."""
+    K, w = int(idx.numel()), int(col.shape[1])
+    if K not in (1, w):
+        raise RuntimeError(f"index_with_null: the [{K}] null mask does not broadcast over [{K}, {w}] rows "
+                           "(a right-outer join's 2-D build-side column)")
+    null = idx == L.NULL_INDEX
+    out = gather([col], idx.masked_fill(null, 0))[0]
+    out.masked_fill_(null, L.NULL_INDEX)
+    return out
+
+
+def _gather_1d(cols: Sequence[torch.Tensor], idx: torch.Tensor, null_aware: bool) -> List[torch.Tensor]:
+    """tqpk_gather of 1-D columns (at most MAX_COLS per launch)."""
+    lib = L.load()
     cols = [_col1d(c) for c in cols]
     _check_cuda(idx, *cols)
     n = int(idx.numel())
@@ -487,7 +505,7 @@ def gather(cols: Sequence[torch.Tensor], idx: torch.Tensor, null_aware: bool = F
     if n == 0 or not cols:
         return outs
     if len(cols) > L.MAX_COLS:
-        return gather(cols[:L.MAX_COLS], idx, null_aware) + gather(cols[L.MAX_COLS:], idx, null_aware)
+        return _gather_1d(cols[:L.MAX_COLS], idx, null_aware) + _gather_1d(cols[L.MAX_COLS:], idx, null_aware)
     L.check(lib.tqpk_gather(len(cols), _vp_array([c.data_ptr() for c in cols]),
                             _i32_array([code_of(c.dtype) for c in cols]), idx.contiguous().data_ptr(), n,
                             int(bool(null_aware)), _vp_array([o.data_ptr() for o in outs]), _stream(idx.device)),

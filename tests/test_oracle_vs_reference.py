@@ -1,0 +1,297 @@
+"""The oracle against the reference's own operators on seeded random inputs (CPU).
+
+The golden fixtures pin the oracle on fixed cases.  Here the compiled reference (oracle/_ref, its
+CPU path: gpu_enable=False on CPU tensors) and the oracle run side by side on randomly drawn filter
+trees, group-bys, sorts and joins (with masks, duplicate and missing keys, extra join conditions
+and every join type), so that the oracle the GPU tests check the kernels against is pinned beyond
+the fixtures.  Keys, masks, counts, orders and integer results are compared exactly, float64
+results within 1e-12 relative.
+"""
+import copy
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+ROOT = Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+from golden_io import assert_f64_close  # noqa: E402
+from oracle import reference  # noqa: E402
+from oracle import tqp_oracle as O  # noqa: E402
+
+TYPES = {1: "date", 2: "float", 3: "int", 4: "int", 5: "float", 6: "int", 7: "string", 8: "float"}
+NAMES = {1: "d", 2: "x", 3: "k", 4: "c", 5: "y", 6: "a", 7: "s", 8: "z"}
+
+
+class _Pool:
+    def malloc_like(self, t):
+        return 0, torch.empty_like(t)
+
+
+@pytest.fixture(scope="module")
+def ref():
+    ok, why = reference.available()
+    if not ok:
+        pytest.skip(why)
+    R = reference.load()
+    with reference.cpu_mode():
+        yield R
+
+
+def columns(rng, n):
+    words = [b"RED", b"GREEN", b"BLUE", b"GOLD", b"GREY"]
+    pick = rng.integers(0, len(words), n)
+    s = np.zeros((n, 6), np.int8)
+    for i, w in enumerate(words):
+        s[pick == i, :len(w)] = np.frombuffer(w, np.uint8).astype(np.int8)
+    return {
+        1: rng.integers(0, 2557, n).astype(np.int32),                       # a date (days)
+        2: rng.integers(0, 11, n).astype(np.float64) / 100.0,               # a discount
+        3: rng.integers(-50, 51, n).astype(np.int64),
+        4: rng.integers(ord("A"), ord("G"), n).astype(np.uint8),            # a one-byte flag
+        5: np.round(rng.uniform(-10, 200, n), 2),
+        6: rng.integers(0, 7, n).astype(np.int32),
+        7: s,
+        8: rng.integers(90000, 10495001, n).astype(np.float64) / 100.0,     # a price
+    }
+
+
+def tg_of(R, cols):
+    V = R.variable.Variable
+    return {c: V(torch.from_numpy(np.ascontiguousarray(a)), TYPES.get(c, "int")) for c, a in cols.items()}
+
+
+def col(c):
+    return f"{NAMES[c]}#{c}"
+
+
+# ------------------------------------------------------------------ filter
+def leaf(rng):
+    c = int(rng.choice([1, 2, 3, 4, 5]))
+    op = str(rng.choice(["<", "<=", ">", ">=", "="]))
+    if c == 1:
+        # date strings are left out: the reference parses them with pandas, absent here
+        lit = str(rng.choice(["1170", "2470", "100.5", "0", "2557", "42"]))
+    elif c == 2:
+        lit = str(rng.choice(["0.05", "0.06", "0.0", "0.1", "0.07"]))
+    elif c == 3:
+        if rng.random() < 0.25:
+            return [col(3), "IN", [str(v) for v in rng.integers(-60, 60, int(rng.integers(1, 5)))]]
+        lit = str(rng.choice(["0", "-7", "49", "12.5", "-50"]))
+    elif c == 4:
+        return [col(4), "=", chr(int(rng.integers(ord("A"), ord("H"))))]
+    else:
+        lit = str(rng.choice(["100.5", "-3.25", "0", "0.0", "150"]))
+    return [col(c), op, lit]
+
+
+def tree(rng, depth=0):
+    r = rng.random()
+    if depth >= 3 or r < 0.35:
+        return leaf(rng)
+    if r < 0.45:
+        return ["NOT", [tree(rng, depth + 1)]]
+    if r < 0.5:
+        return [["isnotnull", [col(3)]], "AND", tree(rng, depth + 1)]
+    return [tree(rng, depth + 1), str(rng.choice(["AND", "OR"])), tree(rng, depth + 1)]
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_filter_trees(ref, seed):
+    rng = np.random.default_rng(100 + seed)
+    cols = columns(rng, 3001)
+    for i in range(12):
+        t = tree(rng)
+        used = sorted({c for c in (1, 2, 3, 4, 5) if col(c) in repr(t)})
+        tg = tg_of(ref, {c: cols[c] for c in used})
+        args = {"name": "Filter", "filter tree": [t], "materialized in": used, "out mask id": 900}
+        try:
+            ref.filter.tqp_filter(False, tg, copy.deepcopy(args), None, None, _Pool(), "f")
+        except Exception as e:                      # noqa: BLE001  the oracle must raise the same class
+            with pytest.raises(type(e)):
+                O.eval_filter([t], {c: cols[c] for c in used}, 3001)
+            continue
+        expect = tg[900].tensor.numpy().reshape(-1)
+        got = np.asarray(O.eval_filter([t], {c: cols[c] for c in used}, 3001)).reshape(-1)
+        np.testing.assert_array_equal(got, expect, err_msg=repr(t))
+
+
+# ------------------------------------------------------------------ aggregate
+AGGS = [
+    ["sum", [col(5)]], ["avg", [col(2)]], ["min", [col(5)]], ["max", [col(3)]], ["sum", [col(3)]],
+    ["count", ["1"]], ["count", [col(3)]], ["avg", [col(3)]], ["min", [col(1)]], ["max", [col(8)]],
+    ["sum", [[col(8), "*", ["1.0", "-", col(2)]]]],
+    ["sum", [[[col(8), "*", ["1.0", "-", col(2)]], "*", ["1.0", "+", col(2)]]]],
+    ["sum", [[col(3), "*", "2"]]], ["max", [[col(5), "+", col(2)]]], ["avg", [col(8)]],
+    # torch's float32 results: an integer column with a float literal, integer true division,
+    # a CASE mixing a float literal with integers
+    ["sum", [[col(3), "*", "0.5"]]], ["avg", [[col(6), "/", [col(6), "+", "1"]]]], ["max", [[col(6), "*", "2.5"]]],
+    ["sum", ["CASE", "WHEN", [col(3), ">", "25"], "THEN", "1.0", "ELSE", "0", "END"]],
+    # integer arithmetic in the narrower type (uint8 wraps), mixed integer widths
+    ["sum", [[col(4), "+", col(4)]]], ["min", [[col(6), "-", col(3)]]],
+    # string conditions
+    ["sum", ["CASE", "WHEN", [col(7), "=", "GREEN"], "THEN", col(8), "ELSE", "0.0", "END"]],
+    ["sum", ["CASE", "WHEN", ["StartsWith", [col(7), "GR"]], "THEN", "1", "ELSE", "0", "END"]],
+]
+KEYS = [[], [col(6)], [col(6), col(4)], [col(3)], [col(7)], [col(4), col(7)]]
+
+
+def _key_order(keys):
+    flat = []
+    for k in keys:
+        k = k.reshape(k.shape[0], -1)
+        flat += [k[:, j] for j in range(k.shape[1])]
+    return np.lexsort(flat[::-1]) if flat else np.zeros(1, np.int64)
+
+
+@pytest.mark.parametrize("seed", range(24 + len(KEYS)))
+def test_group_by(ref, seed):
+    """Seeds below 24 draw 2-5 expressions; the last len(KEYS) seeds run every expression under
+    each key set."""
+    rng = np.random.default_rng(200 + seed)
+    n = int(rng.integers(1, 4000))
+    cols = columns(rng, n)
+    keys = KEYS[seed % len(KEYS)]
+    picks = rng.choice(len(AGGS), int(rng.integers(2, 6)), replace=False) if seed < 24 else np.arange(len(AGGS))
+    results = list(keys) + [[[AGGS[p], "#", f"{400 + i}" + ("L" if AGGS[p][0] == "count" else "")], "AS",
+                             f"r#{500 + i}"] for i, p in enumerate(picks)]
+    key_ids = [int(k.split("#")[1]) for k in keys]
+    used = sorted({c for c in cols if col(c) in repr(results)})
+    args = {"name": "Aggregate", "is partial": False, "keys": keys or None, "input ids": used, "results": results,
+            "out agg ids": [500 + i for i in range(len(picks))]}
+    cols_in = {c: cols[c] for c in used}
+    if seed % 2:                                     # behind a filter's mask
+        cols_in[900] = cols[1] > 1000
+        args["mask map"] = {c: 900 for c in used}
+    tg = tg_of(ref, cols_in)
+    if 900 in cols_in:
+        tg[900] = ref.variable.Variable(torch.from_numpy(cols_in[900]), "bool")
+    torch.manual_seed(seed)
+    ref.aggregate.tqp_hash_aggregate(False, tg, copy.deepcopy(args), _Pool(), None, "a")
+    got = O.tqp_hash_aggregate(cols_in, copy.deepcopy(args))
+    ek = [tg[k].tensor.numpy() for k in key_ids]
+    gk = [got[k] for k in key_ids]
+    eo, go = _key_order(ek), _key_order(gk)
+    for e, g in zip(ek, gk):
+        assert e.shape == g.shape and e.dtype == g.dtype
+        np.testing.assert_array_equal(g[go], e[eo])
+    for oid in args["out agg ids"]:
+        e, g = tg[oid].tensor.numpy(), got[oid]
+        assert e.dtype == g.dtype and e.shape == g.shape, (oid, e.dtype, g.dtype, e.shape, g.shape)
+        if keys:
+            e, g = e[eo], g[go]
+        if e.dtype == np.float32:                    # summation order may move the last bits
+            np.testing.assert_allclose(g, e, rtol=2e-6, atol=2e-6 * max(1.0, float(np.abs(e).max(initial=0))))
+        elif e.dtype.kind == "f":
+            assert_f64_close(g, e)
+        else:
+            np.testing.assert_array_equal(g, e)
+
+
+# ------------------------------------------------------------------ project
+PROJ = [
+    [["year", [col(1)]], "AS", "p#41"],
+    [["CASE", "WHEN", [col(7), "=", "GREEN"], "THEN", col(8), "ELSE", "0.0", "END"], "AS", "p#42"],
+    [[[col(8), "*", ["1.0", "-", col(2)]]], "AS", "p#43"],
+    [[col(3), "<", "10"], "AS", "p#44"],
+    [[[col(3), "*", "1.5"]], "AS", "p#45"],
+    [[[col(6), "/", [col(6), "+", "1"]]], "AS", "p#46"],
+    [[[col(4), "+", col(4)]], "AS", "p#47"],
+    [[[col(6), "-", col(3)]], "AS", "p#48"],
+    [["CASE", "WHEN", [col(3), ">", "25"], "THEN", "1.0", "ELSE", "0", "END"], "AS", "p#49"],
+    [[[col(5), "*", col(6)]], "AS", "p#50"],
+]
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_project(ref, seed):
+    rng = np.random.default_rng(500 + seed)
+    n = int(rng.integers(1, 3000))
+    cols = columns(rng, n)
+    picks = sorted(rng.choice(len(PROJ), 4, replace=False))
+    exprs = [PROJ[p] for p in picks]
+    outs = [41 + int(p) for p in picks]
+    used = sorted({c for c in cols if col(c) in repr(exprs)})
+    args = {"name": "Project", "rename map": {}, "materialized in": used, "used expr": exprs, "materialized out": outs}
+    tg = tg_of(ref, {c: cols[c] for c in used})
+    ref.project.tqp_project(False, tg, copy.deepcopy(args), None, _Pool(), "p")
+    got = O.tqp_project({c: cols[c] for c in used}, copy.deepcopy(args))
+    for c in outs:
+        e = tg[c].tensor.numpy()
+        assert got[c].dtype == e.dtype and got[c].shape == e.shape, (c, got[c].dtype, e.dtype)
+        np.testing.assert_array_equal(got[c], e, err_msg=str(c))
+
+
+# ------------------------------------------------------------------ sort
+@pytest.mark.parametrize("seed", range(16))
+def test_sort(ref, seed):
+    rng = np.random.default_rng(300 + seed)
+    n = int(rng.integers(1, 3000))
+    cols = columns(rng, n)
+    cols[5] = np.round(cols[5] / 20) * 20                                   # ties in the float key
+    nk = int(rng.integers(1, 4))
+    key_ids = [int(c) for c in rng.choice([1, 3, 4, 5, 6, 7], nk, replace=False)]
+    inputs = sorted(set(key_ids) | {int(c) for c in rng.choice([2, 3, 8], 2, replace=False)})
+    args = {"input ids": inputs, "key ids": key_ids, "key orders": [bool(b) for b in rng.integers(0, 2, nk)]}
+    with_limit = bool(seed % 2)
+    if with_limit:
+        args["limit"] = int(rng.integers(1, n + 1))
+    tg = tg_of(ref, {c: cols[c] for c in inputs})
+    ref.sort.tqp_sort(False, tg, copy.deepcopy(args), with_limit, "s")
+    got = O.tqp_sort({c: cols[c] for c in inputs}, args, with_limit)
+    for c in inputs:
+        np.testing.assert_array_equal(got[c], tg[c].tensor.numpy(), err_msg=f"column {c} of {args}")
+
+
+# ------------------------------------------------------------------ join
+JOIN_TYPES = ["inner", "right-semi", "right-anti", "right-outer"]
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_join(ref, seed):
+    rng = np.random.default_rng(400 + seed)
+    jtype = JOIN_TYPES[seed % 4]
+    nb, npr = int(rng.integers(1, 800)), int(rng.integers(1, 2500))
+    unique = seed % 3 != 0
+    bkey = (rng.permutation(nb) + 1) if unique else rng.integers(1, max(2, nb // 3), nb)
+    cols = {11: bkey.astype(np.int32), 12: rng.integers(0, 5, nb).astype(np.int32),
+            13: rng.integers(0, 2557, nb).astype(np.int32),
+            21: rng.integers(1, nb + 40, npr).astype(np.int32), 22: rng.integers(0, 5, npr).astype(np.int32),
+            23: rng.integers(90000, 10495001, npr).astype(np.float64) / 100.0,
+            24: rng.integers(0, 2557, npr).astype(np.int32)}
+    types_ = {11: "int", 12: "int", 13: "date", 21: "int", 22: "int", 23: "float", 24: "date"}
+    masked = seed % 2 == 0
+    cols[901] = cols[13] < 1700
+    cols[902] = cols[24] > 900
+    args = {"name": "Join", "left group": [11, 12, 13], "right group": [21, 22, 23, 24],
+            "materialized in": [11, 12, 21, 22, 23]}
+    if masked:
+        args["mask map"] = {11: 901, 12: 901, 21: 902, 22: 902, 23: 902}
+    conds = [["#12", "=", "#22"]] if seed % 3 == 1 else []
+    V = ref.variable.Variable
+    tg = {c: V(torch.from_numpy(a), types_.get(c, "bool")) for c, a in cols.items()}
+    try:
+        rows = ref.hashjoin.join_vortex(False, tg, copy.deepcopy(args), 11, 21, copy.deepcopy(conds), jtype, None,
+                                        _Pool(), "j")
+    except RuntimeError:
+        with pytest.raises(RuntimeError):
+            O.join_vortex(cols, copy.deepcopy(args), 11, 21, jtype, conds)
+        return
+    got, got_rows = O.join_vortex(cols, copy.deepcopy(args), 11, 21, jtype, conds)
+    assert got_rows == rows
+    # the probe side comes in the reference's order (its matched probe rows ascending, hashjoin.py:65,93)
+    for c in (21, 22, 23):
+        np.testing.assert_array_equal(np.asarray(got[c]), tg[c].tensor.numpy(), err_msg=f"column {c}, {jtype}")
+    # the build rows that match one probe row come in the order of the reference's torch.sort of the
+    # build keys (hashjoin.py:43), which is not a stable sort: compared as a multiset of whole rows
+    left = [c for c in (11, 12) if tg[c].tensor.numel()]
+    for c in (11, 12):
+        assert np.asarray(got[c]).shape == tuple(tg[c].tensor.shape), (c, jtype)
+    if left:
+        e = np.stack([tg[c].tensor.numpy().astype(np.float64) for c in left + [21, 22, 23]], 1)
+        g = np.stack([np.asarray(got[c]).astype(np.float64) for c in left + [21, 22, 23]], 1)
+        np.testing.assert_array_equal(g[np.lexsort(g.T[::-1])], e[np.lexsort(e.T[::-1])], err_msg=jtype)

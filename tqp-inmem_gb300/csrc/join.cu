@@ -16,8 +16,10 @@
 //           reference's searchsorted, on a deduplicated array).
 // The probe is one single-pass kernel per join type: each thread looks up 16
 // probe rows, the per-row match counts are scanned in the block and across
-// tiles with the decoupled look-back, and the pairs are written in the
-// reference's order (ascending probe row, then ascending build row).  Rows
+// tiles with the decoupled look-back, and the pairs are written by ascending
+// probe row, as the reference's are, then ascending build row (the reference
+// sorts build keys with an unstable torch.sort, hashjoin.py:43, so its order
+// of one key's duplicate build rows is not fixed; this is the stable one).  Rows
 // failing either side's filter mask are skipped in place: the inputs are
 // never compacted, and the emitted ids index the original columns.
 #include <algorithm>

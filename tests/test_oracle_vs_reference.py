@@ -295,3 +295,61 @@ def test_join(ref, seed):
         e = np.stack([tg[c].tensor.numpy().astype(np.float64) for c in left + [21, 22, 23]], 1)
         g = np.stack([np.asarray(got[c]).astype(np.float64) for c in left + [21, 22, 23]], 1)
         np.testing.assert_array_equal(g[np.lexsort(g.T[::-1])], e[np.lexsort(e.T[::-1])], err_msg=jtype)
+
+
+# ------------------------------------------------------------------ the drop-in's compilers
+def _tensors(cols):
+    return {c: torch.from_numpy(np.ascontiguousarray(a)) for c, a in cols.items()}
+
+
+@pytest.mark.parametrize("keys", KEYS, ids=[",".join(k) or "global" for k in KEYS])
+def test_drop_in_aggregate_dtypes_follow_the_reference(ref, keys):
+    """tqpk.expr.compile_aggregate decides each output's dtype on the host (the kernels write what
+    it says; float32 results are rounded from float64 by its `casts`).  Those decisions, and the
+    type names the drop-in gives the outputs, equal the reference's for every expression above."""
+    from tqpk.expr import compile_aggregate, needs_key_codes
+    from tqpk.variable import torch_to_type
+    rng = np.random.default_rng(600)
+    cols = columns(rng, 300)
+    key_ids = [int(k.split("#")[1]) for k in keys]
+    for i, agg in enumerate(AGGS):
+        results = list(keys) + [[[agg, "#", "400" + ("L" if agg[0] == "count" else "")], "AS", "r#500"]]
+        # at least one input column (with none, both return empty float32 columns before compiling)
+        used = sorted({c for c in cols if col(c) in repr(results)} | {3})
+        args = {"name": "Aggregate", "is partial": False, "keys": keys or None, "input ids": used,
+                "results": results, "out agg ids": [500]}
+        tg = tg_of(ref, {c: cols[c] for c in used})
+        torch.manual_seed(i)
+        ref.aggregate.tqp_hash_aggregate(False, tg, copy.deepcopy(args), _Pool(), None, "a")
+        tc = _tensors({c: cols[c] for c in used})
+        # string keys are numbered first (tqpk.ops.encode_keys) and the kernel groups by the code
+        codes = torch.zeros(300, dtype=torch.int32) if needs_key_codes(args, tc) else None
+        prog = compile_aggregate(copy.deepcopy(args), tc, derived=True, key_codes=codes)
+        dt = {o[0]: o[4] for o in prog.outputs}[500]
+        if 500 in prog.casts:                        # the 2-step path (>= 2^16 rows per group) is not reached here
+            dt = prog.casts[500][0]
+        e = tg[500]
+        assert dt == e.tensor.dtype, (agg, dt, e.tensor.dtype)
+        assert torch_to_type(dt) == e.tensor_type, (agg, torch_to_type(dt), e.tensor_type)
+        for k in key_ids:
+            assert tg[k].tensor.dtype == torch.from_numpy(cols[k][:1]).dtype
+
+
+def test_drop_in_projection_dtypes_follow_the_reference(ref):
+    """tqpk.expr.compile_projection's output dtypes and the drop-in's type names against the
+    reference's tqp_project, for every projection expression above."""
+    from tqpk.expr import compile_projection
+    from tqpk.variable import torch_to_type
+    rng = np.random.default_rng(601)
+    cols = columns(rng, 300)
+    for p, expr in enumerate(PROJ):
+        used = sorted({c for c in cols if col(c) in repr(expr)})
+        out = 41 + p
+        args = {"name": "Project", "rename map": {}, "materialized in": used, "used expr": [expr],
+                "materialized out": [out]}
+        tg = tg_of(ref, {c: cols[c] for c in used})
+        ref.project.tqp_project(False, tg, copy.deepcopy(args), None, _Pool(), "p")
+        prog = compile_projection([copy.deepcopy(expr)], _tensors({c: cols[c] for c in used}), derived=True)
+        (dt,) = [d for (_, d) in prog.outputs]
+        assert dt == tg[out].tensor.dtype, (expr, dt, tg[out].tensor.dtype)
+        assert torch_to_type(dt) == tg[out].tensor_type, (expr, torch_to_type(dt), tg[out].tensor_type)

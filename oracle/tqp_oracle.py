@@ -183,7 +183,7 @@ def eval_filter(tree, cols: Dict[int, np.ndarray], rows: int | None = None, subq
                 mask |= L == float(r)
         return mask
     if op not in ("<=", ">=", "<", ">", "=", "AND", "OR"):         # :129-140
-        raise NotImplementedError(f"filter operation {op!r} is not on the oracle's path")
+        raise ValueError(f"Unsupported Operation: {op}")             # the reference's error class
     L = eval_filter(tree[0], cols, rows, subquery)
     R = eval_filter(tree[-1], cols, rows, subquery)
     if op == "AND":

@@ -72,7 +72,7 @@ def col(c):
 # ------------------------------------------------------------------ filter
 def leaf(rng):
     c = int(rng.choice([1, 2, 3, 4, 5]))
-    op = str(rng.choice(["<", "<=", ">", ">=", "="]))
+    op = str(rng.choice(["<", "<=", ">", ">=", "=", "<>"], p=[0.19, 0.19, 0.19, 0.19, 0.19, 0.05]))
     if c == 1:
         # date strings are left out: the reference parses them with pandas, absent here
         lit = str(rng.choice(["1170", "2470", "100.5", "0", "2557", "42"]))
@@ -118,6 +118,73 @@ def test_filter_trees(ref, seed):
         expect = tg[900].tensor.numpy().reshape(-1)
         got = np.asarray(O.eval_filter([t], {c: cols[c] for c in used}, 3001)).reshape(-1)
         np.testing.assert_array_equal(got, expect, err_msg=repr(t))
+
+
+def _model_program(prog, cols):
+    """A numpy model of the kernels' predicate interpreter (eval_pred4 and pred_leaf4 in
+    csrc/common.cuh) for the numeric instructions: int64 compares, a float32 compare of the
+    converted value with the float32 literal, float64 compares and isclose."""
+    from tqpk import _lib as L
+    cmp = {L.LT: np.less, L.LE: np.less_equal, L.GT: np.greater, L.GE: np.greater_equal, L.EQ: np.equal,
+           L.NE: np.not_equal}
+    S, st = prog.struct, []
+    n = next(iter(cols.values())).shape[0]
+    for k in range(S.n_insn):
+        I = S.insn[k]
+        if I.op == L.P_CMP:
+            x = cols[prog.col_ids[I.col]].reshape(-1)
+            if I.domain == L.DOM_F64:
+                xd = x.astype(np.float64)
+                if I.cmp == L.ISCLOSE:
+                    err = np.abs(xd - I.lit_f)
+                    st.append((xd == I.lit_f) | (np.isfinite(err) & (err <= I.lit_aux)))
+                else:
+                    st.append(cmp[I.cmp](xd, I.lit_f))
+            elif I.domain == L.DOM_F32:
+                st.append(cmp[I.cmp](x.astype(np.int64).astype(np.float32), np.float32(I.lit_f)))
+            else:
+                st.append(cmp[I.cmp](x.astype(np.int64), np.int64(I.lit_i)))
+        elif I.op == L.P_AND:
+            b = st.pop()
+            st[-1] = st[-1] & b
+        elif I.op == L.P_OR:
+            b = st.pop()
+            st[-1] = st[-1] | b
+        elif I.op == L.P_NOT:
+            st[-1] = ~st[-1]
+        elif I.op in (L.P_TRUE, L.P_FALSE):
+            st.append(np.full(n, I.op == L.P_TRUE))
+        else:
+            raise NotImplementedError(f"instruction {I.op} is not modelled")
+    assert len(st) == 1
+    return st[0]
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_drop_in_filter_compiler_follows_the_reference(ref, seed):
+    """tqpk.predicate.compile_filter turns the reference's trees and literals into the kernels'
+    instructions on the host: the eps of float literals, isclose for float equality, float32
+    for an integer column against a float literal, date and character literals, IN lists and
+    isnotnull.  Its programs, run by a numpy model of the kernels' interpreter, give the
+    reference's masks; trees the reference rejects are rejected with the same exception class."""
+    from tqpk.predicate import compile_filter
+    rng = np.random.default_rng(700 + seed)
+    cols = columns(rng, 2001)
+    for i in range(12):
+        t = tree(rng)
+        used = sorted({c for c in (1, 2, 3, 4, 5) if col(c) in repr(t)})
+        tg = tg_of(ref, {c: cols[c] for c in used})
+        args = {"name": "Filter", "filter tree": [t], "materialized in": used, "out mask id": 900}
+        tc = {c: torch.from_numpy(cols[c]) for c in used}
+        try:
+            ref.filter.tqp_filter(False, tg, copy.deepcopy(args), None, None, _Pool(), "f")
+        except Exception as e:                      # noqa: BLE001  the compiler must raise the same class
+            with pytest.raises(type(e)):
+                compile_filter([copy.deepcopy(t)], tc)
+            continue
+        prog = compile_filter([copy.deepcopy(t)], tc)
+        got = _model_program(prog, {c: cols[c] for c in used})
+        np.testing.assert_array_equal(got, tg[900].tensor.numpy().reshape(-1), err_msg=repr(t))
 
 
 # ------------------------------------------------------------------ aggregate

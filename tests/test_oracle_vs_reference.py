@@ -70,8 +70,29 @@ def col(c):
 
 
 # ------------------------------------------------------------------ filter
+WORDS = ["RED", "GREEN", "BLUE", "GOLD", "GREY", "PINK"]
+
+
+def string_leaf(rng):
+    k = int(rng.integers(0, 7))
+    if k == 0:
+        return [col(7), "=", str(rng.choice(WORDS))]
+    if k == 1:
+        return ["StartsWith", [col(7), str(rng.choice(["GR", "B", "GO", "RE", "PI"]))]]
+    if k == 2:
+        return [str(rng.choice(["Contains", "EndsWith"])), [col(7), str(rng.choice(["E", "EE", "LD", "EN", "Y"]))]]
+    if k == 3:
+        return [col(7), "LIKE", str(rng.choice(["%G%E%", "%R%D%", "%E%N%", "%B%E%"]))]
+    if k == 4:
+        return [col(7), "IN", [str(w) for w in rng.choice(WORDS, int(rng.integers(1, 4)), replace=False)]]
+    # a multi-character literal is compared for equality whatever the operator (filter.py:151-158)
+    return [col(7), str(rng.choice(["<", ">=", "<>"])), str(rng.choice(WORDS))]
+
+
 def leaf(rng):
-    c = int(rng.choice([1, 2, 3, 4, 5]))
+    c = int(rng.choice([1, 2, 3, 4, 5, 7]))
+    if c == 7:
+        return string_leaf(rng)
     op = str(rng.choice(["<", "<=", ">", ">=", "=", "<>"], p=[0.19, 0.19, 0.19, 0.19, 0.19, 0.05]))
     if c == 1:
         # date strings are left out: the reference parses them with pandas, absent here
@@ -106,7 +127,7 @@ def test_filter_trees(ref, seed):
     cols = columns(rng, 3001)
     for i in range(12):
         t = tree(rng)
-        used = sorted({c for c in (1, 2, 3, 4, 5) if col(c) in repr(t)})
+        used = sorted({c for c in (1, 2, 3, 4, 5, 7) if col(c) in repr(t)})
         tg = tg_of(ref, {c: cols[c] for c in used})
         args = {"name": "Filter", "filter tree": [t], "materialized in": used, "out mask id": 900}
         try:
@@ -144,6 +165,29 @@ def _model_program(prog, cols):
                 st.append(cmp[I.cmp](x.astype(np.int64).astype(np.float32), np.float32(I.lit_f)))
             else:
                 st.append(cmp[I.cmp](x.astype(np.int64), np.int64(I.lit_i)))
+        elif I.op in (L.P_STRCMP, L.P_PREFIX, L.P_CONTAINS, L.P_LIKE2):   # str_leaf4 on int8 [N, w] rows
+            a = cols[prog.col_ids[I.col]].astype(np.int64)
+            w = S.widths[I.col]
+            pool = np.ctypeslib.as_array(S.strpool).astype(np.uint8).astype(np.int8).astype(np.int64)
+            code = I.lit_i & 0xFFFFFFFFFFFFFFFF
+
+            def at(off, ln, pos=0):
+                return (a[:, pos:pos + ln] == pool[off:off + ln]).all(axis=1)
+            if I.op == L.P_STRCMP:
+                st.append(cmp[I.cmp](a[:, :w], pool[code & 0xFFFFFFFF:(code & 0xFFFFFFFF) + w]).all(axis=1))
+            elif I.op == L.P_PREFIX:
+                st.append(at(code & 0xFFFFFFFF, code >> 32))
+            elif I.op == L.P_CONTAINS:
+                ln = code >> 32
+                st.append(np.any([at(code & 0xFFFFFFFF, ln, p) for p in range(w - ln + 1)], axis=0)
+                          if w >= ln else np.zeros(n, bool))
+            else:
+                oa, na, ob, nb = code & 0xFFFF, (code >> 16) & 0xFFFF, (code >> 32) & 0xFFFF, code >> 48
+                seen, out = np.zeros(n, bool), np.zeros(n, bool)
+                for p in range(w - na - nb + 1):
+                    seen |= at(oa, na, p)
+                    out |= seen & at(ob, nb, p + na)
+                st.append(out)
         elif I.op == L.P_AND:
             b = st.pop()
             st[-1] = st[-1] & b
@@ -172,7 +216,7 @@ def test_drop_in_filter_compiler_follows_the_reference(ref, seed):
     cols = columns(rng, 2001)
     for i in range(12):
         t = tree(rng)
-        used = sorted({c for c in (1, 2, 3, 4, 5) if col(c) in repr(t)})
+        used = sorted({c for c in (1, 2, 3, 4, 5, 7) if col(c) in repr(t)})
         tg = tg_of(ref, {c: cols[c] for c in used})
         args = {"name": "Filter", "filter tree": [t], "materialized in": used, "out mask id": 900}
         tc = {c: torch.from_numpy(cols[c]) for c in used}

@@ -370,6 +370,8 @@ def _promote(a, b):
     -> the wider integer dtype.
     """
     def kind(x):
+        if isinstance(x, np.ndarray) and x.ndim == 0:                # a 0-dim tensor: a scalar of its kind
+            return "pf" if x.dtype.kind == "f" else "pi"
         if isinstance(x, np.ndarray):
             if x.dtype == np.float32:
                 return "g"
@@ -382,7 +384,7 @@ def _promote(a, b):
         return np.float32
     # integer tensors: the wider tensor dtype (a Python int does not widen it); bool counts as int64
     order = [np.int8, np.uint8, np.int16, np.int32, np.int64]
-    ints = [x.dtype.type for x in (a, b) if isinstance(x, np.ndarray) and x.dtype != bool]
+    ints = [x.dtype.type for x in (a, b) if isinstance(x, np.ndarray) and x.ndim > 0 and x.dtype != bool]
     if not ints:
         return np.int64
     if len(ints) == 2 and {ints[0], ints[1]} == {np.int8, np.uint8}:
@@ -395,15 +397,24 @@ _YEAR_EDGES = np.cumsum([365 if y % 4 else 366 for y in range(1990, 2000)])     
 _AGG_CALLS = ("sum", "avg", "count", "min", "max")
 
 
+def _is_float_scalar(x) -> bool:
+    return isinstance(x, float) or (isinstance(x, np.ndarray) and x.ndim == 0 and x.dtype.kind == "f")
+
+
+def _scalar(x):
+    """A 0-dim result (two literals combined) as the Python number torch compares it as."""
+    return x.item() if isinstance(x, np.ndarray) and x.ndim == 0 else x
+
+
 def _where(mask, a, b):
     """torch.where(mask, a, b) with torch's promotion of arrays and Python scalars
     (aggregate.py:87).  A float literal with integers (or two float literals), or a float32
     branch without a float64 one, is float32 in torch (its default float dtype)."""
-    arrs = [x for x in (a, b) if isinstance(x, np.ndarray)]
-    pys = [x for x in (a, b) if not isinstance(x, np.ndarray)]
+    arrs = [x for x in (a, b) if isinstance(x, np.ndarray) and x.ndim > 0]
+    pys = [x for x in (a, b) if not (isinstance(x, np.ndarray) and x.ndim > 0)]     # 0-dim tensors too
     if any(x.dtype == np.float64 for x in arrs):
         dt = np.float64
-    elif any(x.dtype == np.float32 for x in arrs) or any(isinstance(x, float) for x in pys):
+    elif any(x.dtype == np.float32 for x in arrs) or any(_is_float_scalar(x) for x in pys):
         f32 = [x.astype(np.float32) if isinstance(x, np.ndarray) else np.float32(x) for x in (a, b)]
         return np.where(mask, f32[0], f32[1]).astype(np.float32)
     elif not arrs:
@@ -421,6 +432,7 @@ def _where(mask, a, b):
 
 def _agg_compare(op: str, L, R):
     """ops[op](L, R) of aggregate.py:224-233 for arrays and Python numbers."""
+    L, R = _scalar(L), _scalar(R)
     if isinstance(L, np.ndarray) and isinstance(R, np.ndarray):
         return _cmp(op, L, R)
     if isinstance(L, np.ndarray):
@@ -505,7 +517,9 @@ def eval_agg_expr(tree, cols: Dict[int, np.ndarray], ctx=None):
     La = np.asarray(L, dtype=t) if not isinstance(L, np.ndarray) else L.astype(t, copy=False)
     Ra = np.asarray(R, dtype=t) if not isinstance(R, np.ndarray) else R.astype(t, copy=False)
     with np.errstate(all="ignore"):
-        return {"+": np.add, "-": np.subtract, "*": np.multiply, "/": np.true_divide}[op](La, Ra)
+        # two literals give a 0-dim tensor in torch (int64, or float32 with its rounding), kept as
+        # a 0-d array: it promotes like a scalar but keeps the float32 value
+        return np.asarray({"+": np.add, "-": np.subtract, "*": np.multiply, "/": np.true_divide}[op](La, Ra))
 
 
 def group_rows(key_cols: Sequence[np.ndarray]) -> Tuple[List[np.ndarray], np.ndarray]:
@@ -544,6 +558,8 @@ def reduce_groups(fn: str, v, inverse: np.ndarray, G: int, n: int) -> np.ndarray
         v = np.full(n, v, np.int64)
     elif isinstance(v, float):
         v = np.full(n, v, np.float64)
+    elif isinstance(v, np.ndarray) and v.ndim == 0:
+        raise RuntimeError("an aggregate of a 0-dim tensor (two literals) fails in the reference")
     if v.ndim == 2:                                                 # string slices (substring)
         # sum and count squeeze their values (:179-182); min/max scatter them by a 1-D index and
         # avg's bincount takes 1-D weights only, which the reference fails on

@@ -464,3 +464,238 @@ def test_drop_in_projection_dtypes_follow_the_reference(ref):
         (dt,) = [d for (_, d) in prog.outputs]
         assert dt == tg[out].tensor.dtype, (expr, dt, tg[out].tensor.dtype)
         assert torch_to_type(dt) == tg[out].tensor_type, (expr, torch_to_type(dt), tg[out].tensor_type)
+
+
+# ------------------------------------------------------------------ expression programs
+def _year(d):
+    """The kernels' expr_year: days since 1990-01-01 to the proleptic Gregorian year (days before
+    1990 in 1990), H. Hinnant's civil_from_days."""
+    d = np.asarray(d, np.int64)
+    z = d + 7305 + 719468
+    era = z // 146097
+    doe = z - era * 146097
+    yoe = (doe - doe // 1460 + doe // 36524 - doe // 146096) // 365
+    doy = doe - (365 * yoe + yoe // 4 - yoe // 100)
+    mp = (5 * doy + 2) // 153
+    return np.where(d < 0, 1990, yoe + era * 400 + (mp >= 10))
+
+
+def _model_registers(spec, tensors, n):
+    """A numpy model of the kernels' expression interpreter (expr_apply, expr_apply_f32 and
+    int_wrap in csrc/common.cuh): int64, float64 and float32 registers, round-to-nearest float32
+    arithmetic, integer results wrapped to int8 / uint8 / int32 where torch's dtype is narrower."""
+    from tqpk import _lib as L
+    by_ptr = {t.data_ptr(): t for t in tensors}
+    wrap = {L.I8: np.int8, L.U8: np.uint8, L.I32: np.int32}
+    regs = []
+    with np.errstate(over="ignore", invalid="ignore", divide="ignore"):
+        for i in range(spec.n_expr):
+            X = spec.expr[i]
+            a = regs[X.a] if 0 <= X.a < i else None
+            b = regs[X.b] if 0 <= X.b < i else None
+            arith = {L.X_ADD: np.add, L.X_SUB: np.subtract, L.X_MUL: np.multiply, L.X_DIV: np.divide}
+            if X.type == L.F32 and X.op != L.X_SELECT:
+                if X.op == L.X_CONST:
+                    r = np.full(n, np.float32(X.cf))
+                elif X.op == L.X_TOF32:
+                    r = a.astype(np.int64).astype(np.float32)
+                else:
+                    r = arith[X.op](a.astype(np.float32), b.astype(np.float32)).astype(np.float32)
+            elif X.wrap and X.type == L.I64 and X.op in (L.X_ADD, L.X_SUB, L.X_MUL):
+                r = arith[X.op](a.astype(np.int64), b.astype(np.int64)).astype(wrap[X.wrap]).astype(np.int64)
+            elif X.op == L.X_F32TOF64:
+                r = a.astype(np.float32).astype(np.float64)
+            elif X.op == L.X_SELECT:
+                r = np.where(a != 0, b, regs[X.col])
+            elif X.op == L.X_YEAR:
+                r = _year(a)
+            elif X.op == L.X_COL:
+                t = by_ptr[spec.cols[X.col]]
+                c = t.reshape(-1).numpy() if t.dim() == 2 and t.shape[1] == 1 else t.numpy()
+                r = c.astype(np.float64) if X.type == L.F64 else c.astype(np.int64)
+            elif X.op == L.X_CONST:
+                r = np.full(n, X.cf if X.type == L.F64 else X.ci, np.float64 if X.type == L.F64 else np.int64)
+            elif X.op == L.X_TOF64:
+                r = a.astype(np.int64).astype(np.float64)
+            elif X.op == L.X_DIV:
+                r = np.divide(a.astype(np.float64), b.astype(np.float64))
+            elif X.type == L.F64:
+                r = arith[X.op](a.astype(np.float64), b.astype(np.float64))
+            else:
+                r = arith[X.op](a.astype(np.int64), b.astype(np.int64))
+            regs.append(r)
+    return regs
+
+
+def _model_aggregate(prog, cols, key_ids, n):
+    """The group-by of a compiled AggregateProgram under the model above: the condition columns
+    filled from their predicates, the accumulators per group (keys ascending), the outputs as the
+    emission writes them (csrc/groupby.cu: avg = float64 sum / count, counts as integers), the
+    float32 casts, then the arithmetic over aggregates as a projection over the groups."""
+    from tqpk import _lib as L
+    from tqpk.expr import _HIDDEN_ID, compile_projection
+    for pred, t in prog.masks:
+        t.numpy()[:] = _model_program(pred, cols)
+    regs = _model_registers(prog.spec, list(prog.tensors) + [t for _, t in prog.masks], n)
+    if key_ids:
+        stacked = np.concatenate([cols[k].reshape(n, -1).astype(np.int64) for k in key_ids], 1)
+        _, inv = np.unique(stacked, axis=0, return_inverse=True)
+        inv = inv.reshape(-1)
+        G = int(inv.max()) + 1
+    else:
+        inv, G = np.zeros(n, np.int64), 1
+    accs = []
+    for a in range(prog.spec.n_accs):
+        A = prog.spec.accs[a]
+        if A.kind == L.ACC_COUNT_ROWS:
+            accs.append((np.bincount(inv, minlength=G).astype(np.int64), False, True))
+            continue
+        f = A.type == L.F64
+        r = regs[A.reg].astype(np.float64 if f else np.int64)
+        if A.kind == L.ACC_COUNT_NOTNULL:                # values equal to the null marker are not counted
+            accs.append((np.bincount(inv, weights=(r != L.NULL_INDEX), minlength=G).astype(np.int64), False, True))
+            continue
+        if A.kind == L.ACC_SUM:
+            v = np.zeros(G, r.dtype)
+            np.add.at(v, inv, r)
+        else:                                             # min / max start from the record's initial value
+            v = np.full(G, A.init_f if f else A.init_i, r.dtype)
+            (np.minimum if A.kind == L.ACC_MIN else np.maximum).at(v, inv, r)
+        accs.append((v, f, False))
+    res = {}
+    for oid, op, ia, ib, dt in prog.outputs:
+        v, f, is_count = accs[ia]
+        if op == L.OUT_AVG:
+            v = v.astype(np.float64) / accs[ib][0].astype(np.float64)
+        res[oid] = torch.from_numpy(np.ascontiguousarray(v)).to(dt)
+    for oid, (dt, is_avg) in prog.casts.items():      # rows per group stay below the 2-step path here
+        if oid in res:
+            res[oid] = res[oid].to(dt)
+    if prog.post:
+        hidden = {oid: res.pop(oid) for oid in list(res) if oid >= _HIDDEN_ID}
+        for oid, tree, dt in prog.post:
+            pp = compile_projection([tree], hidden)
+            (reg, pdt), = pp.outputs
+            res[oid] = torch.from_numpy(np.ascontiguousarray(_model_registers(pp.spec, pp.tensors, G)[reg])).to(pdt)
+    return res
+
+
+ARITH_COLS = [5, 2, 8, 3, 6, 4]           # float64, float64, float64, int64, int32, uint8
+LITS = ["1.0", "2", "0.5", "1", "3", "0.25"]
+
+
+def num_expr(rng, depth=0):
+    r = rng.random()
+    if depth >= 2 or r < 0.3:
+        if rng.random() < 0.1:                   # two literals: a 0-dim tensor in torch
+            return [str(rng.choice(LITS)), str(rng.choice(["+", "-", "*", "/"])), str(rng.choice(LITS))]
+        return col(int(rng.choice(ARITH_COLS))) if rng.random() < 0.75 else str(rng.choice(LITS))
+    if r < 0.38:
+        cond = [col(int(rng.choice([3, 5, 6]))), str(rng.choice(["<", ">", "<=", ">="])), str(rng.choice(["0", "3", "25"]))]
+        if rng.random() < 0.3:
+            cond = [col(7), "=", str(rng.choice(WORDS))]
+        return ["CASE", "WHEN", cond, "THEN", num_expr(rng, depth + 1), "ELSE", num_expr(rng, depth + 1), "END"]
+    op = str(rng.choice(["+", "-", "*", "/"], p=[0.3, 0.3, 0.3, 0.1]))
+    if op == "/":                            # divisors that are never zero
+        return [num_expr(rng, depth + 1), "/", [[col(6), "+", "1"], col(8), "2", "0.5"][int(rng.integers(0, 4))]]
+    return [num_expr(rng, depth + 1), op, num_expr(rng, depth + 1)]
+
+
+def _has_col(t):
+    return "#" in repr(t)
+
+
+@pytest.mark.parametrize("seed", range(64))
+def test_drop_in_expression_programs_follow_the_reference(ref, seed):
+    """Random arithmetic / CASE expressions over float64, int64, int32 and uint8 columns under sum,
+    avg, min, max and count, grouped by a key: the drop-in's compiled program, run by the numpy
+    model of the kernels' interpreter, against the reference's values and dtypes (and the oracle
+    against the reference).  Float64 within 1e-12 relative, float32 within its summation rounding,
+    integers exact."""
+    from tqpk.expr import compile_aggregate, needs_key_codes
+    rng = np.random.default_rng(800 + seed)
+    n = int(rng.integers(1, 2000))
+    cols = columns(rng, n)
+    keys = [KEYS[1], KEYS[2], KEYS[3], KEYS[4]][seed % 4]
+    key_ids = [int(k.split("#")[1]) for k in keys]
+    results, fns = list(keys), []
+    for i in range(4):
+        e = num_expr(rng)
+        while not _has_col(e):
+            e = num_expr(rng)
+        fn = str(rng.choice(["sum", "avg", "min", "max", "count"]))
+        arg = e if isinstance(e, list) and e and e[0] == "CASE" else [e]
+        results.append([[[fn, arg], "#", f"{400 + i}" + ("L" if fn == "count" else "")], "AS", f"r#{500 + i}"])
+        fns.append(fn)
+    used = sorted({c for c in cols if col(c) in repr(results)})
+    args = {"name": "Aggregate", "is partial": False, "keys": keys, "input ids": used, "results": results,
+            "out agg ids": [500 + i for i in range(4)]}
+    tg = tg_of(ref, {c: cols[c] for c in used})
+    torch.manual_seed(seed)
+    tc = {c: torch.from_numpy(np.ascontiguousarray(cols[c])) for c in used}
+    codes = torch.zeros(n, dtype=torch.int32) if needs_key_codes(args, tc) else None
+    try:
+        ref.aggregate.tqp_hash_aggregate(False, tg, copy.deepcopy(args), _Pool(), None, "a")
+    except Exception as e:                              # noqa: BLE001  both must raise the same class
+        with pytest.raises(type(e)):
+            O.tqp_hash_aggregate({c: cols[c] for c in used}, copy.deepcopy(args))
+        with pytest.raises(type(e)):
+            compile_aggregate(copy.deepcopy(args), tc, derived=True, key_codes=codes)
+        return
+    oracle = O.tqp_hash_aggregate({c: cols[c] for c in used}, copy.deepcopy(args))
+    try:
+        prog = compile_aggregate(copy.deepcopy(args), tc, derived=True, key_codes=codes)
+    except NotImplementedError as e:                    # the program's size limits raise, never truncate
+        assert "exceed" in str(e), e
+        prog = None
+    model = _model_aggregate(prog, {c: cols[c] for c in used}, key_ids, n) if prog is not None else {}
+    eo = _key_order([tg[k].tensor.numpy() for k in key_ids])
+    go = _key_order([oracle[k] for k in key_ids])
+    for i in range(4):
+        oid = 500 + i
+        e = tg[oid].tensor.numpy()[eo]
+        checks = [("oracle", oracle[oid][go])] + ([("drop-in", model[oid].numpy())] if model else [])
+        for name, g in checks:
+            assert g.dtype == e.dtype, (name, results[len(keys) + i], g.dtype, e.dtype)
+            if e.dtype == np.float32:
+                np.testing.assert_allclose(g, e, rtol=2e-6, atol=2e-6 * max(1.0, float(np.abs(e).max(initial=0))),
+                                           err_msg=f"{name}: {results[len(keys) + i]}")
+            elif e.dtype.kind == "f":
+                assert_f64_close(g, e)
+            else:
+                np.testing.assert_array_equal(g, e, err_msg=f"{name}: {results[len(keys) + i]}")
+
+
+@pytest.mark.parametrize("fn", ["sum", "avg", "min", "max", "count"])
+def test_aggregate_of_literals(ref, fn):
+    """An aggregate of two combined literals fails in the reference (torch gives a 0-dim tensor its
+    reductions reject); the oracle and the drop-in's compiler raise the same class.  A bare literal
+    is expanded to one value per row (aggregate.py:149-152) by all three."""
+    from tqpk.expr import compile_aggregate
+    rng = np.random.default_rng(900)
+    cols = columns(rng, 200)
+    for arg, fails in ((["2", "+", "0.25"], True), (["3", "*", "2"], True), ("2", False), ("0.5", False)):
+        res = [[[fn, [arg]], "#", "400" + ("L" if fn == "count" else "")], "AS", "r#500"]
+        args = {"name": "Aggregate", "is partial": False, "keys": [col(6)], "input ids": [3, 6],
+                "results": [col(6), res], "out agg ids": [500]}
+        tg = tg_of(ref, {3: cols[3], 6: cols[6]})
+        tc = {c: torch.from_numpy(cols[c]) for c in (3, 6)}
+        try:
+            ref.aggregate.tqp_hash_aggregate(False, tg, copy.deepcopy(args), _Pool(), None, "a")
+            raised = None
+        except Exception as e:                          # noqa: BLE001
+            raised = type(e)
+        assert (raised is not None) == fails, (fn, arg, raised)
+        if raised is not None:
+            with pytest.raises(raised):
+                O.tqp_hash_aggregate({3: cols[3], 6: cols[6]}, copy.deepcopy(args))
+            with pytest.raises(raised):
+                compile_aggregate(copy.deepcopy(args), tc, derived=True)
+            continue
+        prog = compile_aggregate(copy.deepcopy(args), tc, derived=True)
+        model = _model_aggregate(prog, {3: cols[3], 6: cols[6]}, [6], 200)[500].numpy()
+        oracle = O.tqp_hash_aggregate({3: cols[3], 6: cols[6]}, copy.deepcopy(args))[500]
+        e = tg[500].tensor.numpy()[_key_order([tg[6].tensor.numpy()])]
+        for g in (model, oracle):
+            assert g.dtype == e.dtype, (fn, arg, g.dtype, e.dtype)
+            np.testing.assert_allclose(g, e, rtol=1e-6)

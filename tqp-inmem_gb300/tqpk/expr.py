@@ -56,6 +56,27 @@ _COND_OPS = ("<=", ">=", "<", ">", "=", "<>", "AND", "OR")
 _HIDDEN_ID = 1 << 40          # ids of hidden per-group columns (aggregate calls inside a result expression)
 
 
+class _Literal0Int(int):
+    """Two integer literals combined by + - *: torch returns a 0-dim int64 tensor, which promotes
+    like a Python int."""
+
+
+class _Literal0F32(float):
+    """Two literals combined with a float among them, or divided: torch returns a 0-dim float32
+    tensor (its default float dtype), computed in float32.  It promotes like a Python float, with
+    the float32 value: 2 + 0.1 is 2.0999999046325684 when it meets a float64 column."""
+
+
+def _fold_literals(op: str, a, b):
+    """torch.add / sub / mul / div of two Python numbers (aggregate.py:233)."""
+    if isinstance(a, float) or isinstance(b, float) or op == "/":
+        import numpy as np
+        fa, fb = np.float32(a), np.float32(b)
+        with np.errstate(all="ignore"):
+            return _Literal0F32({"+": fa + fb, "-": fa - fb, "*": fa * fb, "/": fa / fb}[op])
+    return _Literal0Int({"+": a + b, "-": a - b, "*": a * b}[op])
+
+
 def _strip(t):
     while isinstance(t, list) and len(t) == 1:
         t = t[0]
@@ -288,7 +309,7 @@ class _Builder:
     def binary(self, op: str, a, b):
         op_code = {"+": L.X_ADD, "-": L.X_SUB, "*": L.X_MUL, "/": L.X_DIV}[op]
         if not isinstance(a, _Node) and not isinstance(b, _Node):
-            return {"+": a + b, "-": a - b, "*": a * b, "/": a / b}[op]
+            return _fold_literals(op, a, b)
         wides = [x.wide for x in (a, b) if isinstance(x, _Node)]
         if any(wides) and not all(wides):
             raise NotImplementedError("a one-byte substring with a column: the reference broadcasts [N, 1] "
@@ -377,6 +398,11 @@ def _lift_calls(t, calls: list, base: int):
 
 def _add_output(b: _Builder, prog: AggregateProgram, oid: int, fn: str, arg):
     v = b.value(arg)
+    if isinstance(v, (_Literal0Int, _Literal0F32)):
+        # the reference's reductions take a 0-dim tensor as their values and fail (bincount /
+        # scatter_reduce want one value per row); a bare literal is expanded instead (:149-152)
+        raise RuntimeError(f"{fn} of two combined literals: the reference's reductions reject the 0-dim "
+                           "tensor they give")
     scalar = not isinstance(v, _Node)
     if fn == "count" and scalar and v != L.NULL_INDEX:      # count(1): every row counts
         prog.outputs.append((oid, L.OUT_ACC, 0, 0, torch.int64))

@@ -318,23 +318,45 @@ PROJ = [
 ]
 
 
-@pytest.mark.parametrize("seed", range(12))
-def test_project(ref, seed):
+@pytest.mark.parametrize("seed", range(32))
+def test_project(ref, seed, monkeypatch):
+    """Four of the expressions above and three random trees per projection (more than one
+    32-instruction program: the operator splits them)."""
     rng = np.random.default_rng(500 + seed)
     n = int(rng.integers(1, 3000))
     cols = columns(rng, n)
     picks = sorted(rng.choice(len(PROJ), 4, replace=False))
     exprs = [PROJ[p] for p in picks]
     outs = [41 + int(p) for p in picks]
+    for j in range(3):                       # random arithmetic / CASE trees (not a bare column)
+        e = num_expr(rng)
+        while not (isinstance(e, list) and _has_col(e)):
+            e = num_expr(rng)
+        exprs.append([e if e[0] == "CASE" else [e], "AS", f"q#{60 + j}"])
+        outs.append(60 + j)
     used = sorted({c for c in cols if col(c) in repr(exprs)})
     args = {"name": "Project", "rename map": {}, "materialized in": used, "used expr": exprs, "materialized out": outs}
     tg = tg_of(ref, {c: cols[c] for c in used})
     ref.project.tqp_project(False, tg, copy.deepcopy(args), None, _Pool(), "p")
     got = O.tqp_project({c: cols[c] for c in used}, copy.deepcopy(args))
+    # the drop-in operator, its projection programs run by the interpreter model instead of the kernel
+    from tqpk.operators import project as P
+    from tqpk.variable import Variable
+
+    def model_project(prog, rows, device):
+        for pred, t in prog.masks:
+            t.numpy()[:] = _model_program(pred, cols)
+        regs = _model_registers(prog.spec, list(prog.tensors) + [t for _, t in prog.masks], rows)
+        return [torch.from_numpy(np.ascontiguousarray(regs[r])).to(dt) for r, dt in prog.outputs]
+    monkeypatch.setattr(P, "project", model_project)
+    mine = {c: Variable(torch.from_numpy(np.ascontiguousarray(cols[c])), TYPES[c]) for c in used}
+    P.tqp_project(True, mine, copy.deepcopy(args), None, None, "p")
     for c in outs:
         e = tg[c].tensor.numpy()
-        assert got[c].dtype == e.dtype and got[c].shape == e.shape, (c, got[c].dtype, e.dtype)
-        np.testing.assert_array_equal(got[c], e, err_msg=str(c))
+        assert mine[c].tensor_type == tg[c].tensor_type, (c, mine[c].tensor_type, tg[c].tensor_type)
+        for name, g in (("oracle", got[c]), ("drop-in", mine[c].tensor.numpy())):
+            assert g.dtype == e.dtype and g.shape == e.shape, (name, c, g.dtype, e.dtype)
+            np.testing.assert_array_equal(g, e, err_msg=f"{name}: {c}")
 
 
 # ------------------------------------------------------------------ sort

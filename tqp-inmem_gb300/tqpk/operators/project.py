@@ -32,6 +32,34 @@ def _substring_of(tree):
     return None
 
 
+def _is_size_limit(e: NotImplementedError) -> bool:
+    return "exceed" in str(e) or "more than" in str(e)
+
+
+def projection_programs(trees, columns):
+    """The computed expressions as projection programs: one while they fit the program's limits
+    (32 instructions, 16 columns), else consecutive runs of expressions, each one program and one
+    launch.  An expression too large for a program of its own still raises."""
+    try:
+        return [compile_projection(trees, columns, derived=True)]
+    except NotImplementedError as e:
+        if len(trees) == 1 or not _is_size_limit(e):
+            raise
+    progs, run, last = [], [], None
+    for t in trees:
+        try:
+            last_try = compile_projection(run + [t], columns, derived=True)
+        except NotImplementedError as e:
+            if not run or not _is_size_limit(e):
+                raise
+            progs.append(last)
+            run, last_try = [], compile_projection([t], columns, derived=True)
+        run.append(t)
+        last = last_try
+    progs.append(last)
+    return progs
+
+
 def tqp_project(gpu_enable, tensor_group, args, cpu_mem_pool, gpu_mem_pool, name="project"):
     _require_gpu(gpu_enable)
     check_deferred()
@@ -48,8 +76,10 @@ def tqp_project(gpu_enable, tensor_group, args, cpu_mem_pool, gpu_mem_pool, name
         wait_ready(*inputs.values())
         nums = iter([])
         if numeric:
-            prog = compile_projection(numeric, {k: v.tensor for k, v in inputs.items()}, derived=True)
-            nums = iter(project(prog, rows, first.tensor.device))
+            results = []
+            for prog in projection_programs(numeric, {k: v.tensor for k, v in inputs.items()}):
+                results += project(prog, rows, first.tensor.device)
+            nums = iter(results)
         outs = []
         for sub in subs:
             if sub is None:

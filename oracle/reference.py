@@ -5,7 +5,7 @@ vectors), by bench.py (the reference arm and the reference's torch CUDA path bes
 and by nothing in the product.
 
 build() compiles the reference's operator path -- ``operators/{filter,like,hashjoin,aggregate,
-sort,project}.py``, ``IO/vortex_pipeline.py``, ``IO/pinned_mem.py``, ``variable.py``,
+sort,project,scan}.py``, ``IO/vortex_pipeline.py``, ``IO/pinned_mem.py``, ``variable.py``,
 ``constants.py``, ``conversion.py``, ``utility/{logger,tensor_utils}.py`` and four functions of
 ``parsing.py`` -- from a TQP-Inmem source tree into one bundle of code objects,
 ``oracle/_ref/tqp_inmem.bundle`` (git-ignored; Python's ``marshal`` format, so it is read by the
@@ -48,7 +48,7 @@ MODULES = [
     ("utility/__init__.py", 0), ("utility/logger.py", 0), ("utility/tensor_utils.py", 0),
     ("IO/__init__.py", 0), ("IO/vortex_pipeline.py", 1), ("IO/pinned_mem.py", 0),
     ("operators/like.py", 0), ("operators/filter.py", 0), ("operators/hashjoin.py", 0),
-    ("operators/aggregate.py", 0), ("operators/sort.py", 0), ("operators/project.py", 0),
+    ("operators/aggregate.py", 0), ("operators/sort.py", 0), ("operators/project.py", 0), ("operators/scan.py", 0),
 ]
 PARSING_FUNCTIONS = {"get_id", "get_name", "get_literals", "right_most"}
 
@@ -143,7 +143,7 @@ def available() -> tuple[bool, str]:
 
 def load() -> types.SimpleNamespace:
     """The reference's modules, imported from oracle/_ref/: filter, hashjoin, aggregate, sort,
-    project, variable, pinned_mem."""
+    project, scan, variable, pinned_mem."""
     global _LOADED
     if _LOADED is not None:
         return _LOADED
@@ -168,7 +168,7 @@ def load() -> types.SimpleNamespace:
     mods = {}
     for name in ("constants", "variable", "conversion", "parsing", "utility.logger", "IO.vortex_pipeline",
                  "IO.pinned_mem", "operators.filter", "operators.hashjoin", "operators.aggregate", "operators.sort",
-                 "operators.project"):
+                 "operators.project", "operators.scan"):
         mods[name] = importlib.import_module(name)
     for name, m in mods.items():
         if not isinstance(getattr(m, "__loader__", None), _BundleImporter):
@@ -178,7 +178,8 @@ def load() -> types.SimpleNamespace:
     lg.set_message_logger(None, False)
     _LOADED = types.SimpleNamespace(filter=mods["operators.filter"], hashjoin=mods["operators.hashjoin"],
                                     aggregate=mods["operators.aggregate"], sort=mods["operators.sort"],
-                                    project=mods["operators.project"], variable=mods["variable"],
+                                    project=mods["operators.project"], scan=mods["operators.scan"],
+                                    variable=mods["variable"],
                                     pinned_mem=mods["IO.pinned_mem"])
     return _LOADED
 

@@ -59,3 +59,34 @@ def test_scan_missing_column_file_raises(tmp_path):
     with pytest.raises(Exception):
         tqp_scan(False, {}, {"output names": ["l_comment"], "output ids": [9]}, {"tensors path": str(tmp_path)},
                  dict(schema, L_COMMENT="variable text"), 1, None)
+
+
+def test_scan_matches_the_reference(tmp_path):
+    """The drop-in tqp_scan against the reference's own (operators/scan.py, compiled into
+    oracle/_ref) on the same column files, both on their CPU path: values, dtypes, type names,
+    the primary-key flag and the row count."""
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    if str(root) not in sys.path:
+        sys.path.insert(0, str(root))
+    from oracle import reference
+    ok, why = reference.available()
+    if not ok:
+        pytest.skip(why)
+    R = reference.load()
+    from tqpk.operators import tqp_scan
+    _, schema = _tables(tmp_path)
+    args = {"output names": ["l_orderkey", "l_quantity", "l_shipdate", "l_shipmode", "l_linenumber"],
+            "output ids": [1, 2, 3, 4, 5]}
+    ref_tg, tg = {}, {}
+    with reference.cpu_mode():
+        ref_rows = R.scan.tqp_scan(False, ref_tg, dict(args), {"tensors path": str(tmp_path)}, schema, 1, None)
+    rows = tqp_scan(False, tg, dict(args), {"tensors path": str(tmp_path)}, schema, 1, None)
+    assert rows == ref_rows
+    for cid in args["output ids"]:
+        e, g = ref_tg[cid], tg[cid]
+        assert (g.tensor_type, g.tensor.dtype, tuple(g.tensor.shape)) == (e.tensor_type, e.tensor.dtype,
+                                                                          tuple(e.tensor.shape)), cid
+        assert bool(g.is_sorted) == bool(e.is_sorted), cid
+        assert torch.equal(g.tensor, e.tensor), cid

@@ -27,7 +27,7 @@ def ref():
 
 
 def test_modules_come_from_the_compiled_tree(ref):
-    for name in ("filter", "hashjoin", "aggregate", "sort", "project", "variable", "pinned_mem"):
+    for name in ("filter", "hashjoin", "aggregate", "sort", "project", "scan", "variable", "pinned_mem"):
         assert getattr(ref, name).__file__.startswith(str(reference.BUNDLE))
         assert isinstance(getattr(ref, name).__loader__, reference._BundleImporter)
 

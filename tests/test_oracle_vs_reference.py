@@ -25,6 +25,7 @@ from oracle import tqp_oracle as O  # noqa: E402
 
 TYPES = {1: "date", 2: "float", 3: "int", 4: "int", 5: "float", 6: "int", 7: "string", 8: "float"}
 NAMES = {1: "d", 2: "x", 3: "k", 4: "c", 5: "y", 6: "a", 7: "s", 8: "z"}
+NULL = O.NULL
 
 
 class _Pool:
@@ -188,6 +189,13 @@ def _model_program(prog, cols):
                     seen |= at(oa, na, p)
                     out |= seen & at(ob, nb, p + na)
                 st.append(out)
+        elif I.op == L.P_CMPCOL:                      # column against column, the second slot in lit_i
+            x = cols[prog.col_ids[I.col]].reshape(-1)
+            y = cols[prog.col_ids[int(I.lit_i)]].reshape(-1)
+            t = np.float64 if I.domain == L.DOM_F64 else np.int64
+            st.append(cmp[I.cmp](x.astype(t), y.astype(t)))
+        elif I.op == L.P_MASK:                        # a bool column, nonzero bytes true
+            st.append(cols[prog.col_ids[I.col]].reshape(-1).astype(np.uint8) != 0)
         elif I.op == L.P_AND:
             b = st.pop()
             st[-1] = st[-1] & b
@@ -721,3 +729,115 @@ def test_aggregate_of_literals(ref, fn):
         for g in (model, oracle):
             assert g.dtype == e.dtype, (fn, arg, g.dtype, e.dtype)
             np.testing.assert_allclose(g, e, rtol=1e-6)
+
+
+# ------------------------------------------------------------------ the drop-in join operator
+@pytest.fixture()
+def cpu_join_kernels(monkeypatch):
+    """tqpk.operators.hashjoin with the library calls it makes replaced by numpy models of their
+    documented results: the directory build and probe (the oracle's index join, pinned above, on the
+    rows passing each side's mask, original row ids out; an outer probe without any pair still
+    gives every unmatched row a null build index), the predicate mask (the interpreter model),
+    compaction, row marking and the gathers."""
+    from types import SimpleNamespace
+    from tqpk import ops
+    from tqpk.operators import hashjoin as H
+
+    def join_build(keys, mask=None):
+        k = keys.reshape(-1).numpy()
+        m = np.ones(k.size, bool) if mask is None else mask.numpy().astype(bool)
+        sel = k[m]
+        plan = SimpleNamespace(key_min=int(sel.min()) if sel.size else 0, key_max=int(sel.max()) if sel.size else -1,
+                               nb_rows=int(m.sum()))
+        return SimpleNamespace(keys=k, mask=m, plan=plan)
+
+    def join_probe(b, probe_keys, probe_mask=None, join_type="inner"):
+        pk = probe_keys.reshape(-1).numpy()
+        pm = np.ones(pk.size, bool) if probe_mask is None else probe_mask.numpy().astype(bool)
+        bsel, psel = np.nonzero(b.mask)[0], np.nonzero(pm)[0]
+        li, ri = O.join_indices(b.keys[b.mask], pk[pm], join_type)
+        pi = psel[ri]
+        if join_type in ("right-semi", "right-anti"):
+            bi = np.zeros(0, np.int64)
+        elif join_type == "right-outer" and li.size == 0:
+            bi = np.full(pi.size, NULL, np.int64)
+        else:
+            bi = np.where(li == NULL, NULL, bsel[np.where(li == NULL, 0, li)]) if li.size else li
+        return torch.from_numpy(bi.astype(np.int64)), torch.from_numpy(pi.astype(np.int64))
+
+    def filter_mask(pred, n, device, with_count=False):
+        cols = {cid: t.numpy() for cid, t in zip(pred.col_ids, pred.tensors)}
+        m = torch.from_numpy(np.asarray(_model_program(pred, cols), bool).reshape(-1)) if n else torch.zeros(0, dtype=torch.bool)
+        return m, (torch.tensor([int(m.sum())]) if with_count else None)
+
+    def compact(cols, mask=None, pred=None, with_row_ids=False):
+        m = mask.reshape(-1)
+        outs = [c.reshape(-1)[m] for c in cols] + ([torch.nonzero(m).reshape(-1)] if with_row_ids else [])
+        return outs, int(m.sum())
+
+    def mark_rows(idx, n):
+        f = torch.zeros(n, dtype=torch.bool)
+        f[idx] = True
+        return f
+
+    def gather_1d(cols, idx, null_aware):
+        outs = []
+        for c in cols:
+            c = c.reshape(-1)
+            nul = idx == NULL
+            o = c[idx.masked_fill(nul, 0)].clone()
+            if null_aware:
+                o[nul] = NULL
+            outs.append(o)
+        return outs
+
+    for name, f in (("join_build", join_build), ("join_probe", join_probe), ("filter_mask", filter_mask),
+                    ("compact", compact), ("mark_rows", mark_rows)):
+        monkeypatch.setattr(H, name, f)
+    monkeypatch.setattr(ops, "_gather_1d", gather_1d)
+    monkeypatch.setattr(ops, "gather_rows", lambda col, idx: col[idx])
+    return H
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_drop_in_join_operator_follows_the_reference(ref, cpu_join_kernels, seed):
+    """The drop-in join_vortex (masks popped from `mask map`, pairs, extra conditions on the
+    gathered pair columns, semi / anti / outer derived from the kept pairs, gathered outputs)
+    against the reference's on the random joins above."""
+    from tqpk.variable import Variable
+    rng = np.random.default_rng(400 + seed)
+    jtype = JOIN_TYPES[seed % 4]
+    nb, npr = int(rng.integers(1, 800)), int(rng.integers(1, 2500))
+    unique = seed % 3 != 0
+    bkey = (rng.permutation(nb) + 1) if unique else rng.integers(1, max(2, nb // 3), nb)
+    cols = {11: bkey.astype(np.int32), 12: rng.integers(0, 5, nb).astype(np.int32),
+            13: rng.integers(0, 2557, nb).astype(np.int32),
+            21: rng.integers(1, nb + 40, npr).astype(np.int32), 22: rng.integers(0, 5, npr).astype(np.int32),
+            23: rng.integers(90000, 10495001, npr).astype(np.float64) / 100.0,
+            24: rng.integers(0, 2557, npr).astype(np.int32)}
+    types_ = {11: "int", 12: "int", 13: "date", 21: "int", 22: "int", 23: "float", 24: "date"}
+    cols[901] = cols[13] < 1700
+    cols[902] = cols[24] > 900
+    args = {"name": "Join", "left group": [11, 12, 13], "right group": [21, 22, 23, 24],
+            "materialized in": [11, 12, 21, 22, 23]}
+    if seed % 2 == 0:
+        args["mask map"] = {11: 901, 12: 901, 21: 902, 22: 902, 23: 902}
+    conds = [["#12", "=", "#22"]] if seed % 3 == 1 else []
+    V = ref.variable.Variable
+    tg = {c: V(torch.from_numpy(a), types_.get(c, "bool")) for c, a in cols.items()}
+    rows = ref.hashjoin.join_vortex(False, tg, copy.deepcopy(args), 11, 21, copy.deepcopy(conds), jtype, None,
+                                    _Pool(), "j")
+    mine = {c: Variable(torch.from_numpy(a.copy()), types_.get(c, "bool")) for c, a in cols.items()}
+    got_rows = cpu_join_kernels.join_vortex(True, mine, copy.deepcopy(args), 11, 21, copy.deepcopy(conds), jtype,
+                                            None, None, "j")
+    assert got_rows == rows
+    for c in (21, 22, 23):
+        np.testing.assert_array_equal(mine[c].tensor.numpy(), tg[c].tensor.numpy(), err_msg=f"column {c}, {jtype}")
+    left = [c for c in (11, 12) if tg[c].tensor.numel()]
+    for c in (11, 12):
+        assert tuple(mine[c].tensor.shape) == tuple(tg[c].tensor.shape), (c, jtype)
+        assert mine[c].tensor.dtype == tg[c].tensor.dtype, (c, jtype)
+    if left:
+        e = np.stack([tg[c].tensor.numpy().astype(np.float64) for c in left + [21, 22, 23]], 1)
+        g = np.stack([mine[c].tensor.numpy().astype(np.float64) for c in left + [21, 22, 23]], 1)
+        np.testing.assert_array_equal(g[np.lexsort(g.T[::-1])], e[np.lexsort(e.T[::-1])], err_msg=jtype)

@@ -557,23 +557,19 @@ def _model_registers(spec, tensors, n):
     return regs
 
 
-def _model_aggregate(prog, cols, key_ids, n):
-    """The group-by of a compiled AggregateProgram under the model above: the condition columns
-    filled from their predicates, the accumulators per group (keys ascending), the outputs as the
-    emission writes them (csrc/groupby.cu: avg = float64 sum / count, counts as integers), the
-    float32 casts, then the arithmetic over aggregates as a projection over the groups."""
+def _fill_conditions(prog):
+    """The bool columns of the program's conditions, from their predicates (filled by the filter
+    kernel before the program runs)."""
+    for pred, t in prog.masks:
+        t.numpy()[:] = _model_program(pred, {cid: x.numpy() for cid, x in zip(pred.col_ids, pred.tensors)})
+
+
+def _model_outputs(prog, regs, inv, G):
+    """The accumulators per group, the outputs as the emission writes them (csrc/groupby.cu: avg =
+    float64 sum / count, counts as integers), the float32 casts, then the arithmetic over
+    aggregates as a projection over the groups."""
     from tqpk import _lib as L
     from tqpk.expr import _HIDDEN_ID, compile_projection
-    for pred, t in prog.masks:
-        t.numpy()[:] = _model_program(pred, cols)
-    regs = _model_registers(prog.spec, list(prog.tensors) + [t for _, t in prog.masks], n)
-    if key_ids:
-        stacked = np.concatenate([cols[k].reshape(n, -1).astype(np.int64) for k in key_ids], 1)
-        _, inv = np.unique(stacked, axis=0, return_inverse=True)
-        inv = inv.reshape(-1)
-        G = int(inv.max()) + 1
-    else:
-        inv, G = np.zeros(n, np.int64), 1
     accs = []
     for a in range(prog.spec.n_accs):
         A = prog.spec.accs[a]
@@ -608,6 +604,58 @@ def _model_aggregate(prog, cols, key_ids, n):
             (reg, pdt), = pp.outputs
             res[oid] = torch.from_numpy(np.ascontiguousarray(_model_registers(pp.spec, pp.tensors, G)[reg])).to(pdt)
     return res
+
+
+def _model_aggregate(prog, cols, key_ids, n):
+    """A compiled AggregateProgram under the model above, grouped by the input key columns
+    (keys ascending)."""
+    _fill_conditions(prog)
+    regs = _model_registers(prog.spec, list(prog.tensors) + [t for _, t in prog.masks], n)
+    if key_ids:
+        stacked = np.concatenate([cols[k].reshape(n, -1).astype(np.int64) for k in key_ids], 1)
+        _, inv = np.unique(stacked, axis=0, return_inverse=True)
+        inv = inv.reshape(-1)
+        G = int(inv.max()) + 1
+    else:
+        inv, G = np.zeros(n, np.int64), 1
+    return _model_outputs(prog, regs, inv, G)
+
+
+def _model_groupby(prog, n, device=None, mask=None, before_values=None, key_ranges=None, values_late=False):
+    """tqpk.ops.groupby under the model: the rows passing the filter mask grouped by the program's
+    own key columns (or its key code), keys ascending; (key columns, outputs, groups, plan)."""
+    from tqpk.dtypes import dtype_of
+    if before_values is not None:
+        before_values()
+    _fill_conditions(prog)
+    tensors = list(prog.tensors) + [t for _, t in prog.masks]
+    by_ptr = {t.data_ptr(): t for t in tensors}
+    sel = np.ones(n, bool) if mask is None else mask.reshape(-1).numpy().astype(bool)
+    regs = [r[sel] for r in _model_registers(prog.spec, tensors, n)]
+    S = prog.spec
+    keys = [by_ptr[S.keys[k]].reshape(-1).numpy()[sel].astype(np.int64) for k in range(S.n_keys)]
+    if keys:
+        uniq, inv = np.unique(np.stack(keys, 1), axis=0, return_inverse=True)
+        inv, G = inv.reshape(-1), uniq.shape[0]
+    else:
+        uniq, inv, G = np.zeros((1, 0), np.int64), np.zeros(int(sel.sum()), np.int64), 1
+    res = _model_outputs(prog, regs, inv, G)
+    key_cols = [torch.from_numpy(np.ascontiguousarray(uniq[:, k])).to(dtype_of(S.key_dtypes[k]))
+                for k in range(S.n_keys)]
+    return key_cols, res, G, None
+
+
+def _model_encode_keys(key_cols, mask):
+    """tqpk.ops.encode_keys under the model: int32 codes in key-tuple order for the rows passing
+    the mask, a representative row per code, the number of codes."""
+    n = key_cols[0].shape[0]
+    sel = np.ones(n, bool) if mask is None else mask.reshape(-1).numpy().astype(bool)
+    rows = np.nonzero(sel)[0]
+    stacked = np.concatenate([k.reshape(n, -1).numpy().astype(np.int64) for k in key_cols], 1)[rows]
+    uniq, first, inv = np.unique(stacked, axis=0, return_index=True, return_inverse=True)
+    codes = np.zeros(n, np.int32)
+    codes[rows] = inv.reshape(-1)
+    return torch.from_numpy(codes), torch.from_numpy(rows[first].astype(np.int64)), int(uniq.shape[0])
 
 
 ARITH_COLS = [5, 2, 8, 3, 6, 4]           # float64, float64, float64, int64, int32, uint8
@@ -841,3 +889,62 @@ def test_drop_in_join_operator_follows_the_reference(ref, cpu_join_kernels, seed
         e = np.stack([tg[c].tensor.numpy().astype(np.float64) for c in left + [21, 22, 23]], 1)
         g = np.stack([mine[c].tensor.numpy().astype(np.float64) for c in left + [21, 22, 23]], 1)
         np.testing.assert_array_equal(g[np.lexsort(g.T[::-1])], e[np.lexsort(e.T[::-1])], err_msg=jtype)
+
+
+# ------------------------------------------------------------------ the drop-in aggregate operator
+@pytest.mark.parametrize("seed", range(24))
+def test_drop_in_aggregate_operator_follows_the_reference(ref, monkeypatch, seed):
+    """The drop-in tqp_hash_aggregate (`mask map` handling, key codes for string keys, outputs
+    written as [G, 1] keys and typed aggregates) against the reference, with its library calls
+    (the group-by, the key numbering, the gathers) replaced by the models above."""
+    from tqpk import ops
+    from tqpk.operators import aggregate as A
+    from tqpk.variable import Variable
+    monkeypatch.setattr(A, "groupby", _model_groupby)
+    monkeypatch.setattr(A, "encode_keys", _model_encode_keys)
+    monkeypatch.setattr(ops, "_gather_1d", lambda cols, idx, null_aware: [c.reshape(-1)[idx] for c in cols])
+    monkeypatch.setattr(ops, "gather_rows", lambda col, idx: col[idx])
+    rng = np.random.default_rng(1000 + seed)
+    n = int(rng.integers(1, 3000))
+    cols = columns(rng, n)
+    keys = KEYS[seed % len(KEYS)]
+    picks = rng.choice(len(AGGS), int(rng.integers(2, 7)), replace=False)
+    results = list(keys) + [[[AGGS[p], "#", f"{400 + i}" + ("L" if AGGS[p][0] == "count" else "")], "AS",
+                             f"r#{500 + i}"] for i, p in enumerate(picks)]
+    key_ids = [int(k.split("#")[1]) for k in keys]
+    used = sorted({c for c in cols if col(c) in repr(results)} | {3})
+    args = {"name": "Aggregate", "is partial": False, "keys": keys or None, "input ids": used, "results": results,
+            "out agg ids": [500 + i for i in range(len(picks))]}
+    cols_in = {c: cols[c] for c in used}
+    if (seed // len(KEYS)) % 2:                      # behind a filter's mask
+        cols_in[900] = cols[1] > 1000
+        args["mask map"] = {c: 900 for c in used}
+    tg = tg_of(ref, cols_in)
+    mine = {c: Variable(torch.from_numpy(np.ascontiguousarray(a).copy()), TYPES.get(c, "int")) for c, a in cols_in.items()}
+    if 900 in cols_in:
+        tg[900] = ref.variable.Variable(torch.from_numpy(cols_in[900]), "bool")
+        mine[900] = Variable(torch.from_numpy(cols_in[900].copy()), "bool")
+    torch.manual_seed(seed)
+    rows = ref.aggregate.tqp_hash_aggregate(False, tg, copy.deepcopy(args), _Pool(), None, "a")
+    got_rows = A.tqp_hash_aggregate(True, mine, copy.deepcopy(args), None, None, "a")
+    assert got_rows == rows
+    eo = _key_order([tg[k].tensor.numpy() for k in key_ids])
+    go = _key_order([mine[k].tensor.numpy() for k in key_ids])
+    for k in key_ids:
+        e, g = tg[k], mine[k]
+        assert (g.tensor_type, g.tensor.dtype, tuple(g.tensor.shape)) == (e.tensor_type, e.tensor.dtype,
+                                                                          tuple(e.tensor.shape)), k
+        np.testing.assert_array_equal(g.tensor.numpy()[go], e.tensor.numpy()[eo])
+    for oid in args["out agg ids"]:
+        e, g = tg[oid], mine[oid]
+        assert (g.tensor_type, g.tensor.dtype, tuple(g.tensor.shape)) == (e.tensor_type, e.tensor.dtype,
+                                                                          tuple(e.tensor.shape)), oid
+        ev, gv = e.tensor.numpy(), g.tensor.numpy()
+        if keys:
+            ev, gv = ev[eo], gv[go]
+        if ev.dtype == np.float32:
+            np.testing.assert_allclose(gv, ev, rtol=2e-6, atol=2e-6 * max(1.0, float(np.abs(ev).max(initial=0))))
+        elif ev.dtype.kind == "f":
+            assert_f64_close(gv, ev)
+        else:
+            np.testing.assert_array_equal(gv, ev)

@@ -948,3 +948,89 @@ def test_drop_in_aggregate_operator_follows_the_reference(ref, monkeypatch, seed
             assert_f64_close(gv, ev)
         else:
             np.testing.assert_array_equal(gv, ev)
+
+
+# ------------------------------------------------------------------ the drop-in filter and sort operators
+@pytest.mark.parametrize("seed", range(8))
+def test_drop_in_filter_operator_follows_the_reference(ref, monkeypatch, seed):
+    """tqp_filter with its mask kernel replaced by the interpreter model: the mask column it writes
+    (id, dtype, type name, values) against the reference's, for random numeric and string trees."""
+    from tqpk.operators import filter as F
+    from tqpk.variable import Variable
+
+    def filter_mask(pred, n, device, with_count=False):
+        m = np.asarray(_model_program(pred, {cid: t.numpy() for cid, t in zip(pred.col_ids, pred.tensors)}), bool)
+        return torch.from_numpy(m.reshape(-1).copy()), None
+    monkeypatch.setattr(F, "filter_mask", filter_mask)
+    rng = np.random.default_rng(1100 + seed)
+    cols = columns(rng, 1500)
+    for i in range(10):
+        t = tree(rng)
+        used = sorted({c for c in (1, 2, 3, 4, 5, 7) if col(c) in repr(t)})
+        args = {"name": "Filter", "filter tree": [t], "materialized in": used, "out mask id": 900}
+        tg = tg_of(ref, {c: cols[c] for c in used})
+        mine = {c: Variable(torch.from_numpy(cols[c].copy()), TYPES[c]) for c in used}
+        try:
+            ref.filter.tqp_filter(False, tg, copy.deepcopy(args), None, None, _Pool(), "f")
+        except Exception as e:                      # noqa: BLE001  the same class from the operator
+            with pytest.raises(type(e)):
+                F.tqp_filter(True, mine, copy.deepcopy(args), None, None, None, "f")
+            continue
+        F.tqp_filter(True, mine, copy.deepcopy(args), None, None, None, "f")
+        e, g = tg[900], mine[900]
+        assert (g.tensor_type, g.tensor.dtype) == (e.tensor_type, e.tensor.dtype), repr(t)
+        np.testing.assert_array_equal(g.tensor.numpy().reshape(-1), e.tensor.numpy().reshape(-1), err_msg=repr(t))
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_drop_in_sort_operator_follows_the_reference(ref, monkeypatch, seed):
+    """tqp_sort with its kernels replaced by models (a stable sort of keys[perm] per pass, the
+    oracle's pinned order; the string rows' 8-byte words as order-preserving integers): the LSD
+    passes over keys and string words, the stable top-k for the limit and the gathers against the
+    reference's sorted columns."""
+    from tqpk import ops
+    from tqpk.operators import sort as S
+    from tqpk.variable import Variable
+
+    def argsort_stable(keys, descending=False, perm_in=None):
+        k = keys.reshape(-1).numpy()
+        p = np.arange(k.size) if perm_in is None else perm_in.numpy()
+        return torch.from_numpy(p[O._stable_order(k[p], bool(descending))].astype(np.int64))
+
+    def topk_stable(keys, k, descending=False, perm_in=None):
+        return argsort_stable(keys, descending, perm_in)[:k]
+
+    def string_words(col, word):
+        b = col.numpy()[:, 8 * word:8 * word + 8].astype(np.int64)
+        b = np.pad(b, ((0, 0), (0, 8 - b.shape[1])))
+        b = (b + 128 if col.dtype == torch.int8 else b).astype(np.uint64)   # bytes in the column type's order
+        out = np.zeros(b.shape[0], np.uint64)
+        for j in range(8):                                      # big-endian unsigned word
+            out = (out << np.uint64(8)) | b[:, j]
+        return torch.from_numpy((out ^ np.uint64(1 << 63)).view(np.int64))   # the same order as int64
+    for name, f in (("argsort_stable", argsort_stable), ("topk_stable", topk_stable), ("string_words", string_words),
+                    ("gather_rows", lambda col, idx: col[idx])):
+        monkeypatch.setattr(S, name, f)
+    monkeypatch.setattr(ops, "_gather_1d", lambda cols, idx, null_aware: [c.reshape(-1)[idx] for c in cols])
+    monkeypatch.setattr(ops, "gather_rows", lambda col, idx: col[idx])
+    rng = np.random.default_rng(1200 + seed)
+    n = int(rng.integers(1, 3000))
+    cols = columns(rng, n)
+    cols[5] = np.round(cols[5] / 20) * 20
+    nk = int(rng.integers(1, 4))
+    key_ids = [int(c) for c in rng.choice([1, 3, 4, 5, 6, 7], nk, replace=False)]
+    inputs = sorted(set(key_ids) | {int(c) for c in rng.choice([2, 3, 8], 2, replace=False)})
+    args = {"input ids": inputs, "key ids": key_ids, "key orders": [bool(b) for b in rng.integers(0, 2, nk)]}
+    with_limit = bool(seed % 2)
+    if with_limit:
+        args["limit"] = int(rng.integers(1, n + 1))
+    tg = tg_of(ref, {c: cols[c] for c in inputs})
+    mine = {c: Variable(torch.from_numpy(cols[c].copy()), TYPES[c]) for c in inputs}
+    rows = ref.sort.tqp_sort(False, tg, copy.deepcopy(args), with_limit, "s")
+    got_rows = S.tqp_sort(True, mine, copy.deepcopy(args), with_limit, "s")
+    assert got_rows == rows
+    for c in inputs:
+        e, g = tg[c], mine[c]
+        assert (g.tensor_type, g.tensor.dtype, tuple(g.tensor.shape)) == (e.tensor_type, e.tensor.dtype,
+                                                                          tuple(e.tensor.shape)), c
+        np.testing.assert_array_equal(g.tensor.numpy(), e.tensor.numpy(), err_msg=f"column {c} of {args}")

@@ -1034,3 +1034,88 @@ def test_drop_in_sort_operator_follows_the_reference(ref, monkeypatch, seed):
         assert (g.tensor_type, g.tensor.dtype, tuple(g.tensor.shape)) == (e.tensor_type, e.tensor.dtype,
                                                                           tuple(e.tensor.shape)), c
         np.testing.assert_array_equal(g.tensor.numpy(), e.tensor.numpy(), err_msg=f"column {c} of {args}")
+
+
+# ------------------------------------------------------------------ whole plans through the drop-in operators
+def _install_models(monkeypatch):
+    """Every library call of the drop-in operators replaced by the models above."""
+    from types import SimpleNamespace  # noqa: F401
+    from tqpk import ops
+    from tqpk.operators import aggregate as A, filter as F, hashjoin as H, sort as S
+
+    def filter_mask(pred, n, device, with_count=False):
+        m = np.asarray(_model_program(pred, {cid: t.numpy() for cid, t in zip(pred.col_ids, pred.tensors)}), bool)
+        m = torch.from_numpy(m.reshape(-1).copy()) if n else torch.zeros(0, dtype=torch.bool)
+        return m, (torch.tensor([int(m.sum())]) if with_count else None)
+
+    def argsort_stable(keys, descending=False, perm_in=None):
+        k = keys.reshape(-1).numpy()
+        p = np.arange(k.size) if perm_in is None else perm_in.numpy()
+        return torch.from_numpy(p[O._stable_order(k[p], bool(descending))].astype(np.int64))
+
+    monkeypatch.setattr(F, "filter_mask", filter_mask)
+    monkeypatch.setattr(A, "groupby", _model_groupby)
+    monkeypatch.setattr(A, "encode_keys", _model_encode_keys)
+    monkeypatch.setattr(S, "argsort_stable", argsort_stable)
+    monkeypatch.setattr(S, "topk_stable", lambda keys, k, descending=False, perm_in=None:
+                        argsort_stable(keys, descending, perm_in)[:k])
+    monkeypatch.setattr(S, "gather_rows", lambda col, idx: col[idx])
+    monkeypatch.setattr(ops, "gather_rows", lambda col, idx: col[idx])
+    return A, F, H, S
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_drop_in_plans_follow_the_reference(ref, monkeypatch, cpu_join_kernels, seed):
+    """Filter (build) -> Filter (probe) -> Join -> Aggregate by the build key -> Sort, run by the
+    reference's operators and by the drop-in's (library calls modelled) in the order main.py's
+    executor runs them: the final columns, their dtypes and type names."""
+    from tqpk.variable import Variable
+    A, F, H, S = _install_models(monkeypatch)
+    rng = np.random.default_rng(1300 + seed)
+    nb, npr = int(rng.integers(50, 1500)), int(rng.integers(100, 5000))
+    bkey = (rng.permutation(nb) + 1) if seed % 3 else rng.integers(1, nb // 2 + 2, nb)
+    cols = {11: bkey.astype(np.int32), 12: rng.integers(0, 2557, nb).astype(np.int32),
+            21: rng.integers(1, nb + 40, npr).astype(np.int32), 22: rng.integers(0, 2557, npr).astype(np.int32),
+            23: rng.integers(90000, 10495001, npr).astype(np.float64) / 100.0,
+            24: rng.integers(0, 11, npr).astype(np.float64) / 100.0}
+    types_ = {11: "int", 12: "date", 21: "int", 22: "date", 23: "float", 24: "float"}
+    f1 = {"name": "Filter", "filter tree": [["bd#12", "<", str(int(rng.integers(500, 2000)))]], "materialized in": [12],
+          "out mask id": 901}
+    f2 = {"name": "Filter", "filter tree": [["pd#22", ">", str(int(rng.integers(300, 1500)))]], "materialized in": [22],
+          "out mask id": 902}
+    jargs = {"name": "Join", "left group": [11, 12], "right group": [21, 22, 23, 24], "materialized in": [11, 21, 23, 24],
+             "mask map": {11: 901, 21: 902, 23: 902, 24: 902}, "left keys": [11], "right keys": [21],
+             "join type": "Inner"}
+    value = [["price#23", "*", ["1.0", "-", "disc#24"]]] if seed % 2 else [["price#23", "*", "disc#24"]]
+    aargs = {"name": "Aggregate", "is partial": False, "keys": ["bkey#11"], "input ids": [11, 23, 24],
+             "results": ["bkey#11", [[["sum", value], "#", "301"], "AS", "revenue#302"],
+                         [[["count", ["1"]], "#", "303L"], "AS", "n#304"]], "out agg ids": [302, 304]}
+    if seed % 4 < 2:
+        sargs = {"name": "take ordered", "limit": int(rng.integers(1, 30)), "input ids": [11, 302, 304],
+                 "key ids": [302, 11], "key orders": [True, False]}
+    else:                                                # by the group key, ascending: the sort is the identity
+        sargs = {"name": "Sort", "input ids": [11, 302, 304], "key ids": [11], "key orders": [False]}
+    limit = "limit" in sargs
+
+    def run(filter_, join, aggregate, sort, V, gpu, pool):
+        tg = {c: V(torch.from_numpy(a.copy()), types_[c]) for c, a in cols.items()}
+        filter_(gpu, tg, copy.deepcopy(f1), None, None, pool, "f1")
+        filter_(gpu, tg, copy.deepcopy(f2), None, None, pool, "f2")
+        join(gpu, tg, copy.deepcopy(jargs), 11, 21, [], "inner", None, pool, "j")
+        torch.manual_seed(seed)
+        aggregate(gpu, tg, copy.deepcopy(aargs), pool, None, "a")
+        sort(gpu, tg, copy.deepcopy(sargs), limit, "s")
+        return tg
+
+    e = run(ref.filter.tqp_filter, ref.hashjoin.join_vortex, ref.aggregate.tqp_hash_aggregate, ref.sort.tqp_sort,
+            ref.variable.Variable, False, _Pool())
+    g = run(F.tqp_filter, H.join_vortex, A.tqp_hash_aggregate, S.tqp_sort, Variable, True, None)
+    # the reference's group order is a random hash's, so only a sort on keys it can tell apart
+    # fixes its rows; ties in the sum are ordered by the key here (the second sort key)
+    for c in sargs["input ids"]:
+        ev, gv = e[c].tensor.numpy(), g[c].tensor.numpy()
+        assert (g[c].tensor_type, gv.dtype, gv.shape) == (e[c].tensor_type, ev.dtype, ev.shape), c
+        if ev.dtype.kind == "f":
+            assert_f64_close(gv, ev)
+        else:
+            np.testing.assert_array_equal(gv, ev, err_msg=str(c))

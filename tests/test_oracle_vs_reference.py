@@ -1119,3 +1119,73 @@ def test_drop_in_plans_follow_the_reference(ref, monkeypatch, cpu_join_kernels, 
             assert_f64_close(gv, ev)
         else:
             np.testing.assert_array_equal(gv, ev, err_msg=str(c))
+
+
+def _full_results(o):
+    """Whole result expressions with output id o: arithmetic over aggregates, year(), a CASE counted
+    against the null marker, one-byte substrings under sum and count (aggregate.py:100-101,
+    :114-119, :179-182, :197-233)."""
+    disc = [[col(8), "*", ["1.0", "-", col(2)]]]
+    return [
+        [[["100.0", "*", [["sum", ["CASE", "WHEN", ["StartsWith", [col(7), "GR"]], "THEN", disc, "ELSE", "0.0", "END"]],
+                          "#", "7001"]], "/", [["sum", disc], "#", "7002"]], "AS", f"p#{o}"],
+        [[[["sum", ["CASE", "WHEN", [col(7), "=", "GREEN"], "THEN", col(8), "ELSE", "0.0", "END"]], "#", "7003"], "/",
+          [["sum", col(8)], "#", "7004"]], "AS", f"q#{o}"],
+        [[["min", [["year", [col(1)]]]], "#", "7005"], "AS", f"y#{o}"],
+        [[["sum", [["year", [col(1)]]]], "#", "7006L"], "AS", f"v#{o}L"],
+        [[["count", ["CASE", "WHEN", [col(8), ">", "50000.5"], "THEN", col(5), "ELSE", "-64.0", "END"]], "#", "7007L"],
+         "AS", f"c#{o}L"],
+        [[["sum", [["substring", [col(7), "1", "1"]]]], "#", "7008"], "AS", f"s#{o}"],
+        [[["count", [["substring", [col(7), "2", "1"]]]], "#", "7009L"], "AS", f"t#{o}L"],
+        [[["sum", [[["substring", [col(7), "3", "1"]], "*", "2"]]], "#", "7010"], "AS", f"u#{o}"],
+    ]
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_drop_in_aggregate_operator_whole_expressions(ref, monkeypatch, seed):
+    """As above, with arithmetic over aggregates, year(), a CASE counted against the null marker
+    and one-byte substrings among the results."""
+    from tqpk import ops
+    from tqpk.operators import aggregate as A
+    from tqpk.variable import Variable
+    monkeypatch.setattr(A, "groupby", _model_groupby)
+    monkeypatch.setattr(A, "encode_keys", _model_encode_keys)
+    monkeypatch.setattr(ops, "_gather_1d", lambda cols, idx, null_aware: [c.reshape(-1)[idx] for c in cols])
+    monkeypatch.setattr(ops, "gather_rows", lambda col, idx: col[idx])
+    rng = np.random.default_rng(1400 + seed)
+    n = int(rng.integers(1, 3000))
+    cols = columns(rng, n)
+    keys = [KEYS[0], KEYS[1], KEYS[2], KEYS[3]][seed % 4]
+    whole = _full_results(0)
+    picks = rng.choice(len(whole), int(rng.integers(2, 4)), replace=False)
+    results = list(keys) + [_full_results(600 + i)[p] for i, p in enumerate(picks)]
+    out_ids = [600 + i for i in range(len(picks))]
+    extra = int(rng.integers(0, len(AGGS)))
+    results.append([[AGGS[extra], "#", "7100" + ("L" if AGGS[extra][0] == "count" else "")], "AS", "r#700"])
+    out_ids.append(700)
+    key_ids = [int(k.split("#")[1]) for k in keys]
+    used = sorted({c for c in cols if col(c) in repr(results)} | {3})
+    args = {"name": "Aggregate", "is partial": False, "keys": keys or None, "input ids": used, "results": results,
+            "out agg ids": out_ids}
+    cols_in = {c: cols[c] for c in used}
+    tg = tg_of(ref, cols_in)
+    mine = {c: Variable(torch.from_numpy(np.ascontiguousarray(a).copy()), TYPES.get(c, "int")) for c, a in cols_in.items()}
+    torch.manual_seed(seed)
+    rows = ref.aggregate.tqp_hash_aggregate(False, tg, copy.deepcopy(args), _Pool(), None, "a")
+    got_rows = A.tqp_hash_aggregate(True, mine, copy.deepcopy(args), None, None, "a")
+    assert got_rows == rows
+    eo = _key_order([tg[k].tensor.numpy() for k in key_ids])
+    go = _key_order([mine[k].tensor.numpy() for k in key_ids])
+    for oid in out_ids:
+        e, g = tg[oid], mine[oid]
+        assert (g.tensor_type, g.tensor.dtype, tuple(g.tensor.shape)) == (e.tensor_type, e.tensor.dtype,
+                                                                          tuple(e.tensor.shape)), (oid, results)
+        ev, gv = e.tensor.numpy(), g.tensor.numpy()
+        if keys:
+            ev, gv = ev[eo], gv[go]
+        if ev.dtype == np.float32:
+            np.testing.assert_allclose(gv, ev, rtol=2e-6, atol=2e-6 * max(1.0, float(np.abs(ev).max(initial=0))))
+        elif ev.dtype.kind == "f":
+            assert_f64_close(gv, ev)
+        else:
+            np.testing.assert_array_equal(gv, ev, err_msg=str(oid))

@@ -1189,3 +1189,57 @@ def test_drop_in_aggregate_operator_whole_expressions(ref, monkeypatch, seed):
             assert_f64_close(gv, ev)
         else:
             np.testing.assert_array_equal(gv, ev, err_msg=str(oid))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_drop_in_star_plan_follows_the_reference(ref, monkeypatch, cpu_join_kernels, seed):
+    """The star plan (Filter A; fact ⋈ A; ⋈ B; ⋈ C; sum and count by the C key; take ordered),
+    each join's outputs the next one's inputs, through the reference's operators and the
+    drop-in's (library calls modelled)."""
+    from tqpk import datagen
+    from tqpk.variable import Variable
+    A, F, H, S = _install_models(monkeypatch)
+    t = datagen.star_tables(20_000, 2_000, 3_000, 400, 70 + seed)
+    cols = {31: t["a_key"], 32: t["a_cat"], 41: t["f_fka"], 42: t["f_fkb"], 43: t["f_price"], 44: t["f_discount"],
+            51: t["b_key"], 52: t["b_fkc"], 61: t["c_key"]}
+    types_ = {31: "int", 32: "int", 41: "int", 42: "int", 43: "float", 44: "float", 51: "int", 52: "int", 61: "int"}
+    results = ["c#61", [[["sum", [["p#43", "*", ["1.0", "-", "d#44"]]]], "#", "71"], "AS", "rev#72"],
+               [[["count", ["1"]], "#", "73L"], "AS", "cnt#74"]]
+    plan = [
+        ("f", {"name": "Filter", "filter tree": [["cat#32", "=", "1"]], "materialized in": [32], "out mask id": 901}),
+        ("j", {"name": "Join", "left group": [31, 32], "right group": [41, 42, 43, 44],
+               "materialized in": [31, 41, 42, 43, 44], "mask map": {31: 901}}, 31, 41),
+        ("j", {"name": "Join", "left group": [51, 52], "right group": [31, 41, 42, 43, 44],
+               "materialized in": [51, 52, 42, 43, 44]}, 51, 42),
+        ("j", {"name": "Join", "left group": [61], "right group": [51, 52, 42, 43, 44],
+               "materialized in": [61, 52, 43, 44]}, 61, 52),
+        ("a", {"name": "Aggregate", "is partial": False, "keys": ["c#61"], "input ids": [61, 43, 44],
+               "results": results, "out agg ids": [72, 74]}),
+        ("t", {"name": "take ordered", "limit": 25, "input ids": [61, 72, 74], "key ids": [72], "key orders": [True]}),
+    ]
+
+    def run(filter_, join, aggregate, sort, V, gpu, pool):
+        tg = {c: V(torch.from_numpy(a.copy()), types_[c]) for c, a in cols.items()}
+        for step in plan:
+            kind, a = step[0], copy.deepcopy(step[1])
+            if kind == "f":
+                filter_(gpu, tg, a, None, None, pool, "f")
+            elif kind == "j":
+                join(gpu, tg, a, step[2], step[3], [], "inner", None, pool, "j")
+            elif kind == "a":
+                torch.manual_seed(seed)
+                aggregate(gpu, tg, a, pool, None, "a")
+            else:
+                sort(gpu, tg, a, True, "t")
+        return tg
+
+    e = run(ref.filter.tqp_filter, ref.hashjoin.join_vortex, ref.aggregate.tqp_hash_aggregate, ref.sort.tqp_sort,
+            ref.variable.Variable, False, _Pool())
+    g = run(F.tqp_filter, H.join_vortex, A.tqp_hash_aggregate, S.tqp_sort, Variable, True, None)
+    for c in (61, 72, 74):
+        ev, gv = e[c].tensor.numpy(), g[c].tensor.numpy()
+        assert (g[c].tensor_type, gv.dtype, gv.shape) == (e[c].tensor_type, ev.dtype, ev.shape), c
+        if ev.dtype.kind == "f":
+            assert_f64_close(gv, ev)
+        else:
+            np.testing.assert_array_equal(gv, ev, err_msg=str(c))

@@ -1,0 +1,146 @@
+"""GPU parity on random inputs: the generators of tests/test_oracle_vs_reference.py (whose oracle runs
+there beside the reference's own operators) through the CUDA path, against the oracle.
+
+Masks bit-exact; float64 sums and averages within 1e-12 relative, or 1e-12 of the group's sum of
+|terms| where they cancel (over its count for an average); float32 results within 2e-4 of the same
+scale (their row-by-row float32 summation); integers, minima and maxima exact.
+"""
+import copy
+
+import numpy as np
+import pytest
+import torch
+
+from golden_io import assert_f64_close
+from oracle import tqp_oracle as O
+from test_oracle_vs_reference import AGGS, KEYS, TYPES, col, columns, num_expr, tree, _has_col, _key_order
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need CUDA")
+    from tqpk import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def _vars(cols):
+    from tqpk.variable import Variable
+    return {c: Variable(torch.from_numpy(np.ascontiguousarray(a)).cuda(), TYPES.get(c, "bool")) for c, a in cols.items()}
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_filter_random_trees_vs_oracle(seed):
+    """Random numeric and string predicate trees through tqp_filter."""
+    from tqpk.operators import tqp_filter
+    rng = np.random.default_rng(2100 + seed)
+    cols = columns(rng, 40_003)
+    ran = 0
+    for i in range(12):
+        t = tree(rng)
+        used = sorted({c for c in (1, 2, 3, 4, 5, 7) if col(c) in repr(t)})
+        args = {"name": "Filter", "filter tree": [t], "materialized in": used, "out mask id": 900}
+        try:
+            expect = np.asarray(O.eval_filter([t], {c: cols[c] for c in used}, 40_003)).reshape(-1)
+        except (TypeError, ValueError) as e:        # the reference rejects these too
+            with pytest.raises(type(e)):
+                tqp_filter(True, _vars({c: cols[c] for c in used}), copy.deepcopy(args), None, None, None, "f")
+            continue
+        tg = _vars({c: cols[c] for c in used})
+        try:
+            tqp_filter(True, tg, copy.deepcopy(args), None, None, None, "f")
+        except NotImplementedError as e:            # a program longer than the kernel's 32 instructions
+            assert "longer than" in str(e), e
+            continue
+        np.testing.assert_array_equal(tg[900].tensor.cpu().numpy().reshape(-1), expect, err_msg=repr(t))
+        ran += 1
+    assert ran >= 6
+
+
+def _check(got, exp, magnitude, what):
+    assert got.dtype == exp.dtype and got.shape == exp.shape, (what, got.dtype, exp.dtype)
+    if exp.dtype == np.float32:
+        # the reference adds float32 values row by row; the kernels add their float64 images and
+        # round once: within 2e-4 of the larger of the result and the group's sum of |terms|
+        scale = np.abs(exp.astype(np.float64))
+        if magnitude is not None:
+            scale = np.maximum(scale, magnitude)
+        ok = (np.abs(got.astype(np.float64) - exp.astype(np.float64)) <= 2e-4 * scale) | (got == exp)
+        assert np.all(ok), (what, got[~ok][:5], exp[~ok][:5])
+    elif exp.dtype.kind == "f":
+        assert_f64_close(got, exp, magnitude=magnitude)
+    else:
+        np.testing.assert_array_equal(got, exp, err_msg=what)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_group_by_random_expressions_vs_oracle(seed):
+    """Random arithmetic / CASE expressions over float64, int64, int32 and uint8 columns, and the
+    fixed expression set, under sum / avg / min / max / count, grouped by int32, uint8, int64 and
+    string keys, some behind a filter's mask, through tqp_hash_aggregate."""
+    from tqpk.operators import tqp_hash_aggregate
+    rng = np.random.default_rng(2200 + seed)
+    n = int(rng.integers(50, 30_000))
+    cols = columns(rng, n)
+    keys = KEYS[seed % len(KEYS)]
+    results, args_of = list(keys), {}
+    for i in range(4):
+        if i < 2:
+            e = num_expr(rng)
+            while not _has_col(e):
+                e = num_expr(rng)
+            fn = str(rng.choice(["sum", "avg", "min", "max", "count"]))
+            arg = e if isinstance(e, list) and e and e[0] == "CASE" else [e]
+            call = [fn, arg]
+        else:
+            call = AGGS[int(rng.integers(0, len(AGGS)))]
+        results.append([[call, "#", f"{400 + i}" + ("L" if call[0] == "count" else "")], "AS", f"r#{500 + i}"])
+        args_of[500 + i] = call[1]
+    used = sorted({c for c in cols if col(c) in repr(results)} | {3})
+    args = {"name": "Aggregate", "is partial": False, "keys": keys or None, "input ids": used, "results": results,
+            "out agg ids": [500 + i for i in range(4)]}
+    cols_in = {c: cols[c] for c in used}
+    if seed % 3 == 1:
+        cols_in[900] = cols[1] > 1000
+        args["mask map"] = {c: 900 for c in used}
+    exp = O.tqp_hash_aggregate(cols_in, copy.deepcopy(args))
+    tg = _vars(cols_in)
+    try:
+        tqp_hash_aggregate(True, tg, copy.deepcopy(args), None, None, "a")
+    except NotImplementedError as e:                # a program beyond the kernel's limits
+        assert "exceed" in str(e) or "more than" in str(e), e
+        pytest.skip(str(e))
+    key_ids = [int(k.split("#")[1]) for k in keys]
+    eo = _key_order([exp[k] for k in key_ids])
+    go = _key_order([tg[k].tensor.cpu().numpy() for k in key_ids])
+    for k in key_ids:
+        np.testing.assert_array_equal(tg[k].tensor.cpu().numpy()[go], exp[k][eo])
+    masked = {c: (a[cols_in[900]] if 900 in cols_in else a) for c, a in cols_in.items() if c != 900}
+    rows = next(iter(masked.values())).shape[0]
+    if key_ids:
+        _, inverse = O.group_rows([masked[k] for k in key_ids])          # the oracle's (ascending) groups
+        G = int(inverse.max()) + 1 if inverse.size else 0
+    else:
+        inverse, G = np.zeros(rows, np.int64), 1
+    for oid in args["out agg ids"]:
+        # float64 sums: within 1e-12 of the group's sum of |terms| (any two summation orders are);
+        # averages: that over the group's count
+        magnitude = None
+        try:
+            v = O.eval_agg_expr(args_of[oid], masked)
+            if isinstance(v, np.ndarray) and v.ndim == 1 and v.size == rows:
+                a = np.abs(np.where(np.isfinite(v.astype(np.float64)), v.astype(np.float64), 0.0))
+                magnitude = np.bincount(inverse, weights=a, minlength=G)
+                if results[len(keys) + oid - 500][0][0][0] == "avg":
+                    magnitude = magnitude / np.maximum(np.bincount(inverse, minlength=G), 1)
+                magnitude = magnitude[eo] if key_ids else magnitude
+        except Exception:                           # noqa: BLE001  a bound only, where it evaluates
+            magnitude = None
+        g = tg[oid].tensor.cpu().numpy()
+        e = exp[oid]
+        if key_ids:
+            g, e = g[go], e[eo]
+        _check(g, e, magnitude, f"{oid}: {results[len(keys) + oid - 500]}")

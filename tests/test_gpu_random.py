@@ -3,7 +3,8 @@ there beside the reference's own operators) through the CUDA path, against the o
 
 Masks bit-exact; float64 sums and averages within 1e-12 relative, or 1e-12 of the group's sum of
 |terms| where they cancel (over its count for an average); float32 results within 2e-4 of the same
-scale (their row-by-row float32 summation); integers, minima and maxima exact.
+scale (their row-by-row float32 summation); integers exact.  Float64 minima and maxima are
+within the same bound: the generated group-by evaluates x * (1 - y) as one fused multiply-add.
 """
 import copy
 

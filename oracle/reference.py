@@ -16,8 +16,11 @@ own, unchanged.
 Three adaptations make the modules import without pandas, pyspark and pyparsing, and none of them
 touches the operators' arithmetic:
 
-1. ``pandas``/``pyspark``/``pyparsing``/``expression`` are empty stand-in modules (only
-   ``pd.Timestamp`` is evaluated at import time, by ``conversion.py``).
+1. ``pandas``/``pyspark``/``pyparsing``/``expression`` are stand-in modules.  Only
+   ``pd.Timestamp`` is used on the operator path: ``conversion.py`` makes its epoch at import time
+   and turns a date literal into days with ``(pd.Timestamp(s) - epoch).days`` (``date_to_float``,
+   :26-29).  The stand-in parses an ISO date and gives that day difference, as pandas does for
+   two midnight timestamps.
 2. ``parsing`` is compiled from the reference's own ``get_id``/``get_name``/``get_literals``/
    ``right_most`` function bodies alone (the rest of that file drives Spark).
 3. ``IO/vortex_pipeline.py`` is compiled with assertions off: its two asserts check that the
@@ -151,9 +154,18 @@ def load() -> types.SimpleNamespace:
     if not ok:
         raise ReferenceUnavailable(why)
 
-    class _Timestamp:                         # conversion.py computes one epoch at import time
-        def __init__(self, *a, **k):
-            pass
+    import datetime
+
+    class _Delta:
+        def __init__(self, days):
+            self.days = days
+
+    class _Timestamp:                         # ISO dates at midnight: the day difference pandas gives
+        def __init__(self, s, *a, **k):
+            self.date = datetime.date.fromisoformat(str(s))
+
+        def __sub__(self, other):
+            return _Delta((self.date - other.date).days)
 
     _stub("pandas", Timestamp=_Timestamp, Timedelta=None, DataFrame=None)
     _stub("pyspark")

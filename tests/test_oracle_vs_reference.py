@@ -96,8 +96,7 @@ def leaf(rng):
         return string_leaf(rng)
     op = str(rng.choice(["<", "<=", ">", ">=", "=", "<>"], p=[0.19, 0.19, 0.19, 0.19, 0.19, 0.05]))
     if c == 1:
-        # date strings are left out: the reference parses them with pandas, absent here
-        lit = str(rng.choice(["1170", "2470", "100.5", "0", "2557", "42"]))
+        lit = str(rng.choice(["1170", "2470", "100.5", "1993-03-15", "1995-01-01", "1989-12-31", "42"]))
     elif c == 2:
         lit = str(rng.choice(["0.05", "0.06", "0.0", "0.1", "0.07"]))
     elif c == 3:

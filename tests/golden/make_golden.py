@@ -176,6 +176,11 @@ def filter_predicates(ref):
         ["y#5", "<=", "0"],
         ["d#1", "<=", "100.5"],
         [["NOT", [["d#1", "<", "1000"]]], "AND", [["y#5", ">", "0.0"], "OR", ["k#3", "=", "3"]]],
+        # date literals: days since 1990-01-01 (conversion.py:26-29), one before the epoch
+        ["d#1", "<", "1993-03-15"],
+        [["d#1", ">=", "1994-01-01"], "AND", ["d#1", "<", "1995-01-01"]],
+        ["d#1", "=", "1992-02-29"],
+        ["d#1", ">", "1989-12-31"],
     ]
     outs = {}
     for i, tree in enumerate(trees):

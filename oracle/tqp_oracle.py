@@ -160,7 +160,7 @@ def eval_filter(tree, cols: Dict[int, np.ndarray], rows: int | None = None, subq
             literal, _, cast_type = tree[1][0].split(" ")
             if cast_type == "double":
                 return eval_filter(literal, cols, rows, subquery)
-        raise NotImplementedError(f"filter function {tree[0]!r} is not on the oracle's path")
+        raise ValueError(f"Unsupported Function: {tree[0]}")            # :87, the reference's error
     op = tree[-2]
     if op == "LIKE":                                               # :121-127
         L = eval_filter(tree[0], cols, rows, subquery)

@@ -14,7 +14,7 @@ import torch
 
 from golden_io import assert_f64_close
 from oracle import tqp_oracle as O
-from test_oracle_vs_reference import AGGS, KEYS, TYPES, col, columns, num_expr, tree, _has_col, _key_order
+from test_oracle_vs_reference import AGGS, KEYS, SUBQUERY, TYPES, col, columns, num_expr, tree, _has_col, _key_order
 
 pytestmark = pytest.mark.gpu
 
@@ -45,14 +45,14 @@ def test_filter_random_trees_vs_oracle(seed):
         used = sorted({c for c in (1, 2, 3, 4, 5, 7) if col(c) in repr(t)})
         args = {"name": "Filter", "filter tree": [t], "materialized in": used, "out mask id": 900}
         try:
-            expect = np.asarray(O.eval_filter([t], {c: cols[c] for c in used}, 40_003)).reshape(-1)
+            expect = np.asarray(O.eval_filter([t], {c: cols[c] for c in used}, 40_003, SUBQUERY)).reshape(-1)
         except (TypeError, ValueError) as e:        # the reference rejects these too
             with pytest.raises(type(e)):
-                tqp_filter(True, _vars({c: cols[c] for c in used}), copy.deepcopy(args), None, None, None, "f")
+                tqp_filter(True, _vars({c: cols[c] for c in used}), copy.deepcopy(args), SUBQUERY, None, None, "f")
             continue
         tg = _vars({c: cols[c] for c in used})
         try:
-            tqp_filter(True, tg, copy.deepcopy(args), None, None, None, "f")
+            tqp_filter(True, tg, copy.deepcopy(args), SUBQUERY, None, None, "f")
         except NotImplementedError as e:            # a program longer than the kernel's 32 instructions
             assert "longer than" in str(e), e
             continue

@@ -90,10 +90,18 @@ def string_leaf(rng):
     return [col(7), str(rng.choice(["<", ">=", "<>"])), str(rng.choice(WORDS))]
 
 
+SUBQUERY = 25.375            # a scalar subquery's result, as the executor passes it (main.py:267)
+
+
 def leaf(rng):
     c = int(rng.choice([1, 2, 3, 4, 5, 7]))
     if c == 7:
         return string_leaf(rng)
+    r = rng.random()
+    if r < 0.06 and c in (2, 3, 5):
+        return [col(c), str(rng.choice(["<", "<=", ">", ">="])), "Subquery"]
+    if r < 0.12 and c in (2, 3, 5):               # cast(column as double) (filter.py:78-83)
+        return [["cast", [f"{col(c)} as double"]], str(rng.choice(["<", ">="])), str(rng.choice(["10", "0.5", "-3"]))]
     op = str(rng.choice(["<", "<=", ">", ">=", "=", "<>"], p=[0.19, 0.19, 0.19, 0.19, 0.19, 0.05]))
     if c == 1:
         lit = str(rng.choice(["1170", "2470", "100.5", "1993-03-15", "1995-01-01", "1989-12-31", "42"]))
@@ -131,13 +139,13 @@ def test_filter_trees(ref, seed):
         tg = tg_of(ref, {c: cols[c] for c in used})
         args = {"name": "Filter", "filter tree": [t], "materialized in": used, "out mask id": 900}
         try:
-            ref.filter.tqp_filter(False, tg, copy.deepcopy(args), None, None, _Pool(), "f")
+            ref.filter.tqp_filter(False, tg, copy.deepcopy(args), SUBQUERY, None, _Pool(), "f")
         except Exception as e:                      # noqa: BLE001  the oracle must raise the same class
             with pytest.raises(type(e)):
-                O.eval_filter([t], {c: cols[c] for c in used}, 3001)
+                O.eval_filter([t], {c: cols[c] for c in used}, 3001, SUBQUERY)
             continue
         expect = tg[900].tensor.numpy().reshape(-1)
-        got = np.asarray(O.eval_filter([t], {c: cols[c] for c in used}, 3001)).reshape(-1)
+        got = np.asarray(O.eval_filter([t], {c: cols[c] for c in used}, 3001, SUBQUERY)).reshape(-1)
         np.testing.assert_array_equal(got, expect, err_msg=repr(t))
 
 
@@ -228,12 +236,12 @@ def test_drop_in_filter_compiler_follows_the_reference(ref, seed):
         args = {"name": "Filter", "filter tree": [t], "materialized in": used, "out mask id": 900}
         tc = {c: torch.from_numpy(cols[c]) for c in used}
         try:
-            ref.filter.tqp_filter(False, tg, copy.deepcopy(args), None, None, _Pool(), "f")
+            ref.filter.tqp_filter(False, tg, copy.deepcopy(args), SUBQUERY, None, _Pool(), "f")
         except Exception as e:                      # noqa: BLE001  the compiler must raise the same class
             with pytest.raises(type(e)):
-                compile_filter([copy.deepcopy(t)], tc)
+                compile_filter([copy.deepcopy(t)], tc, SUBQUERY)
             continue
-        prog = compile_filter([copy.deepcopy(t)], tc)
+        prog = compile_filter([copy.deepcopy(t)], tc, SUBQUERY)
         got = _model_program(prog, {c: cols[c] for c in used})
         np.testing.assert_array_equal(got, tg[900].tensor.numpy().reshape(-1), err_msg=repr(t))
 
@@ -970,12 +978,12 @@ def test_drop_in_filter_operator_follows_the_reference(ref, monkeypatch, seed):
         tg = tg_of(ref, {c: cols[c] for c in used})
         mine = {c: Variable(torch.from_numpy(cols[c].copy()), TYPES[c]) for c in used}
         try:
-            ref.filter.tqp_filter(False, tg, copy.deepcopy(args), None, None, _Pool(), "f")
+            ref.filter.tqp_filter(False, tg, copy.deepcopy(args), SUBQUERY, None, _Pool(), "f")
         except Exception as e:                      # noqa: BLE001  the same class from the operator
             with pytest.raises(type(e)):
-                F.tqp_filter(True, mine, copy.deepcopy(args), None, None, None, "f")
+                F.tqp_filter(True, mine, copy.deepcopy(args), SUBQUERY, None, None, "f")
             continue
-        F.tqp_filter(True, mine, copy.deepcopy(args), None, None, None, "f")
+        F.tqp_filter(True, mine, copy.deepcopy(args), SUBQUERY, None, None, "f")
         e, g = tg[900], mine[900]
         assert (g.tensor_type, g.tensor.dtype) == (e.tensor_type, e.tensor.dtype), repr(t)
         np.testing.assert_array_equal(g.tensor.numpy().reshape(-1), e.tensor.numpy().reshape(-1), err_msg=repr(t))

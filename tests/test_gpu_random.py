@@ -145,3 +145,47 @@ def test_group_by_random_expressions_vs_oracle(seed):
         if key_ids:
             g, e = g[go], e[eo]
         _check(g, e, magnitude, f"{oid}: {results[len(keys) + oid - 500]}")
+
+
+JOIN_TYPES = ["inner", "right-semi", "right-anti", "right-outer"]
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_join_random_key_dtypes_vs_oracle(seed):
+    """Random joins of every type whose build and probe keys have different integer dtypes (the
+    reference joins them, hashjoin.py:39-65), dense and sparse key domains, with masks, through
+    join_vortex: the probe side in the reference's order, the build rows as a multiset per probe row
+    (the reference's build-key sort is unstable)."""
+    from tqpk.operators import join_vortex
+    from tqpk.variable import Variable
+    rng = np.random.default_rng(2300 + seed)
+    jtype = JOIN_TYPES[seed % 4]
+    bdt, pdt = [(np.int32, np.int64), (np.int64, np.int32), (np.int64, np.int64), (np.int32, np.uint8)][(seed // 4) % 4]
+    nb, npr = int(rng.integers(50, 5000)), int(rng.integers(100, 40_000))
+    hi = 250 if pdt == np.uint8 else nb + 40
+    bkey = rng.permutation(min(nb, hi - 1)) + 1 if seed % 3 else rng.integers(1, max(2, min(nb, hi) // 3), nb)
+    pkey = rng.integers(1, hi, npr)
+    if seed % 2 and bdt == np.int64 and pdt == np.int64:       # a sparse key domain (the sorted directory)
+        bkey, pkey = bkey * 1_000_003 + 17, pkey * 1_000_003 + 17
+    cols = {11: bkey.astype(bdt), 12: rng.integers(0, 5, bkey.size).astype(np.int32),
+            21: pkey.astype(pdt), 22: rng.integers(0, 5, npr).astype(np.int32),
+            23: rng.integers(90000, 10495001, npr).astype(np.float64) / 100.0}
+    cols[901] = rng.random(bkey.size) < 0.8
+    cols[902] = rng.random(npr) < 0.7
+    args = {"name": "Join", "left group": [11, 12], "right group": [21, 22, 23], "materialized in": [11, 12, 21, 22, 23]}
+    if seed % 5 != 0:
+        args["mask map"] = {11: 901, 12: 901, 21: 902, 22: 902, 23: 902}
+    types_ = {11: "int", 12: "int", 21: "int", 22: "int", 23: "float", 901: "bool", 902: "bool"}
+    exp, exp_rows = O.join_vortex(cols, copy.deepcopy(args), 11, 21, jtype)
+    tg = {c: Variable(torch.from_numpy(np.ascontiguousarray(a)).cuda(), types_[c]) for c, a in cols.items()}
+    rows = join_vortex(True, tg, copy.deepcopy(args), 11, 21, [], jtype, None, None, "j")
+    assert rows == exp_rows
+    for c in (21, 22, 23):
+        np.testing.assert_array_equal(tg[c].tensor.cpu().numpy(), np.asarray(exp[c]), err_msg=f"{c} {jtype}")
+    left = [c for c in (11, 12) if np.asarray(exp[c]).size]
+    for c in (11, 12):
+        assert tuple(tg[c].tensor.shape) == np.asarray(exp[c]).shape, (c, jtype)
+    if left:
+        e = np.stack([np.asarray(exp[c]).astype(np.float64) for c in left + [21, 22, 23]], 1)
+        g = np.stack([tg[c].tensor.cpu().numpy().astype(np.float64) for c in left + [21, 22, 23]], 1)
+        np.testing.assert_array_equal(g[np.lexsort(g.T[::-1])], e[np.lexsort(e.T[::-1])], err_msg=jtype)

@@ -1017,34 +1017,3 @@ def test_join_outer_string_payload_raises_like_the_reference():
     tg = tg_from(ins, args["types"])
     with pytest.raises(RuntimeError):
         join_vortex(True, tg, copy.deepcopy(args["join"]), 11, 21, [], "right-outer", None, None, "j")
-
-
-@pytest.mark.parametrize("shape", ["k_equals_w", "one_row", "column_n1"])
-def test_join_outer_two_dimensional_build_columns(shape):
-    """A right-outer join's 2-D build-side columns are null-filled by the reference's broadcast
-    rule (conversion.py:52-57): K == w output rows fill column j of every row whose build index j
-    is null, K == 1 is a plain gather, and an [N, 1] column with K > 1 raises RuntimeError.  The
-    oracle follows the rule and is checked against the reference's own function on the CPU."""
-    from tqpk.operators import join_vortex
-    left_keys = np.arange(10, dtype=np.int32)
-    right_keys = {"k_equals_w": [1, 100, 3, 200], "one_row": [7], "column_n1": [1, 100, 3]}[shape]
-    right_keys = np.asarray(right_keys, dtype=np.int32)
-    payload = (np.arange(40, dtype=np.int64).reshape(10, 4) % 91 + 33).astype(np.int8)   # [10, 4] rows
-    if shape == "column_n1":
-        payload = np.arange(100, 110, dtype=np.int64).reshape(10, 1)
-    cols = {11: left_keys, 12: payload, 21: right_keys}
-    args = {"left group": [11, 12], "right group": [21], "materialized in": [11, 12, 21]}
-    tg = {11: V(left_keys), 12: V(payload, "string" if payload.dtype == np.int8 else "int"), 21: V(right_keys)}
-    if shape == "column_n1":
-        with pytest.raises(RuntimeError):
-            O.join_vortex(cols, copy.deepcopy(args), 11, 21, "right-outer")
-        with pytest.raises(RuntimeError):
-            join_vortex(True, tg, copy.deepcopy(args), 11, 21, [], "right-outer", None, None, "j")
-        return
-    ref, ref_rows = O.join_vortex(cols, copy.deepcopy(args), 11, 21, "right-outer")
-    rows = join_vortex(True, tg, copy.deepcopy(args), 11, 21, [], "right-outer", None, None, "j")
-    assert rows == ref_rows
-    for c in (11, 12, 21):
-        got = np_(tg[c].tensor)
-        assert got.shape == np.asarray(ref[c]).shape, c
-        np.testing.assert_array_equal(got, ref[c], err_msg=str(c))

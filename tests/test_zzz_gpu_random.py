@@ -1,5 +1,7 @@
 """GPU parity on random inputs: the generators of tests/test_oracle_vs_reference.py (whose oracle runs
-there beside the reference's own operators) through the CUDA path, against the oracle.
+there beside the reference's own operators) through the CUDA path, against the oracle; and the
+right-outer null fill of 2-D build-side columns.  The file is named so pytest collects it after the
+other GPU tests: under -x, a failure here leaves their results standing.
 
 Masks bit-exact; float64 sums and averages within 1e-12 relative, or 1e-12 of the group's sum of
 |terms| where they cancel (over its count for an average); float32 results within 2e-4 of the same
@@ -26,6 +28,15 @@ def lib():
     from tqpk import build, _lib
     build.build()
     return _lib.load()
+
+
+def _v(a, t="int"):
+    from tqpk.variable import Variable
+    return Variable(torch.from_numpy(np.ascontiguousarray(a)).cuda(), t)
+
+
+def np_(t):
+    return t.detach().cpu().numpy()
 
 
 def _vars(cols):
@@ -189,3 +200,34 @@ def test_join_random_key_dtypes_vs_oracle(seed):
         e = np.stack([np.asarray(exp[c]).astype(np.float64) for c in left + [21, 22, 23]], 1)
         g = np.stack([tg[c].tensor.cpu().numpy().astype(np.float64) for c in left + [21, 22, 23]], 1)
         np.testing.assert_array_equal(g[np.lexsort(g.T[::-1])], e[np.lexsort(e.T[::-1])], err_msg=jtype)
+
+
+@pytest.mark.parametrize("shape", ["k_equals_w", "one_row", "column_n1"])
+def test_join_outer_two_dimensional_build_columns(shape):
+    """A right-outer join's 2-D build-side columns are null-filled by the reference's broadcast
+    rule (conversion.py:52-57): K == w output rows fill column j of every row whose build index j
+    is null, K == 1 is a plain gather, and an [N, 1] column with K > 1 raises RuntimeError.  The
+    oracle follows the rule and is checked against the reference's own function on the CPU."""
+    from tqpk.operators import join_vortex
+    left_keys = np.arange(10, dtype=np.int32)
+    right_keys = {"k_equals_w": [1, 100, 3, 200], "one_row": [7], "column_n1": [1, 100, 3]}[shape]
+    right_keys = np.asarray(right_keys, dtype=np.int32)
+    payload = (np.arange(40, dtype=np.int64).reshape(10, 4) % 91 + 33).astype(np.int8)   # [10, 4] rows
+    if shape == "column_n1":
+        payload = np.arange(100, 110, dtype=np.int64).reshape(10, 1)
+    cols = {11: left_keys, 12: payload, 21: right_keys}
+    args = {"left group": [11, 12], "right group": [21], "materialized in": [11, 12, 21]}
+    tg = {11: _v(left_keys), 12: _v(payload, "string" if payload.dtype == np.int8 else "int"), 21: _v(right_keys)}
+    if shape == "column_n1":
+        with pytest.raises(RuntimeError):
+            O.join_vortex(cols, copy.deepcopy(args), 11, 21, "right-outer")
+        with pytest.raises(RuntimeError):
+            join_vortex(True, tg, copy.deepcopy(args), 11, 21, [], "right-outer", None, None, "j")
+        return
+    ref, ref_rows = O.join_vortex(cols, copy.deepcopy(args), 11, 21, "right-outer")
+    rows = join_vortex(True, tg, copy.deepcopy(args), 11, 21, [], "right-outer", None, None, "j")
+    assert rows == ref_rows
+    for c in (11, 12, 21):
+        got = np_(tg[c].tensor)
+        assert got.shape == np.asarray(ref[c]).shape, c
+        np.testing.assert_array_equal(got, ref[c], err_msg=str(c))

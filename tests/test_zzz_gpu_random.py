@@ -231,3 +231,33 @@ def test_join_outer_two_dimensional_build_columns(shape):
         got = np_(tg[c].tensor)
         assert got.shape == np.asarray(ref[c]).shape, c
         np.testing.assert_array_equal(got, ref[c], err_msg=str(c))
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_project_random_expressions_vs_oracle(seed):
+    """Random arithmetic / CASE trees and the fixed projection set (year(), string conditions,
+    float32 and uint8 results, a substring slice) through tqp_project: row-wise results, so equal
+    to the oracle's bit for bit, with the same dtypes."""
+    from test_oracle_vs_reference import PROJ
+    from tqpk.operators import tqp_project
+    rng = np.random.default_rng(2400 + seed)
+    n = int(rng.integers(1, 50_000))
+    cols = columns(rng, n)
+    picks = sorted(rng.choice(len(PROJ), 4, replace=False))
+    exprs = [PROJ[p] for p in picks]
+    outs = [41 + int(p) for p in picks]
+    for j in range(3):
+        e = num_expr(rng)
+        while not (isinstance(e, list) and _has_col(e)):
+            e = num_expr(rng)
+        exprs.append([e if e[0] == "CASE" else [e], "AS", f"q#{60 + j}"])
+        outs.append(60 + j)
+    used = sorted({c for c in cols if col(c) in repr(exprs)})
+    args = {"name": "Project", "rename map": {}, "materialized in": used, "used expr": exprs, "materialized out": outs}
+    exp = O.tqp_project({c: cols[c] for c in used}, copy.deepcopy(args))
+    tg = _vars({c: cols[c] for c in used})
+    tqp_project(True, tg, copy.deepcopy(args), None, None, "p")
+    for c in outs:
+        got = tg[c].tensor.cpu().numpy()
+        assert got.dtype == exp[c].dtype and got.shape == exp[c].shape, (c, got.dtype, exp[c].dtype)
+        np.testing.assert_array_equal(got, exp[c], err_msg=str(exprs[outs.index(c)]))

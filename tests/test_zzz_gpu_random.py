@@ -261,3 +261,28 @@ def test_project_random_expressions_vs_oracle(seed):
         got = tg[c].tensor.cpu().numpy()
         assert got.dtype == exp[c].dtype and got.shape == exp[c].shape, (c, got.dtype, exp[c].dtype)
         np.testing.assert_array_equal(got, exp[c], err_msg=str(exprs[outs.index(c)]))
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_sort_random_keys_vs_oracle(seed):
+    """Random multi-key sorts through tqp_sort: int, date, uint8, float keys with ties (and both
+    zeros), string keys, either direction, with and without a limit (the stable top-k)."""
+    from tqpk.operators import tqp_sort
+    rng = np.random.default_rng(2500 + seed)
+    n = int(rng.integers(1, 60_000))
+    cols = columns(rng, n)
+    cols[5] = np.round(cols[5] / 20) * 20                     # ties, and -0.0 beside 0.0
+    nk = int(rng.integers(1, 4))
+    key_ids = [int(c) for c in rng.choice([1, 3, 4, 5, 6, 7], nk, replace=False)]
+    inputs = sorted(set(key_ids) | {int(c) for c in rng.choice([2, 3, 8], 2, replace=False)})
+    args = {"input ids": inputs, "key ids": key_ids, "key orders": [bool(b) for b in rng.integers(0, 2, nk)]}
+    with_limit = bool(seed % 2)
+    if with_limit:
+        args["limit"] = int(rng.integers(1, min(n, 300) + 1))
+    exp = O.tqp_sort({c: cols[c] for c in inputs}, args, with_limit)
+    tg = _vars({c: cols[c] for c in inputs})
+    tqp_sort(True, tg, copy.deepcopy(args), with_limit, "s")
+    for c in inputs:
+        got = tg[c].tensor.cpu().numpy()
+        assert got.dtype == exp[c].dtype and got.shape == exp[c].shape, (c, args)
+        np.testing.assert_array_equal(got, exp[c], err_msg=f"column {c} of {args}")

@@ -263,7 +263,20 @@ AGGS = [
     ["sum", ["CASE", "WHEN", [col(7), "=", "GREEN"], "THEN", col(8), "ELSE", "0.0", "END"]],
     ["sum", ["CASE", "WHEN", ["StartsWith", [col(7), "GR"]], "THEN", "1", "ELSE", "0", "END"]],
 ]
-KEYS = [[], [col(6)], [col(6), col(4)], [col(3)], [col(7)], [col(4), col(7)]]
+KEYS = [[], [col(6)], [col(6), col(4)], [col(3)], [col(7)], [col(4), col(7)], [col(2)], [col(5), col(6)]]
+
+
+def _tuple_codes(key_cols, n):
+    """Row codes of key tuples in ascending tuple order: each column ranked by value (floats too;
+    -0.0 equals 0.0), string columns byte by byte, then the tuples of ranks."""
+    ranks = []
+    for k in key_cols:
+        k = np.asarray(k).reshape(n, -1)
+        for j in range(k.shape[1]):
+            v = k[:, j]
+            v = np.where(v == 0, 0, v) if v.dtype.kind == "f" else v
+            ranks.append(np.unique(v, return_inverse=True)[1].reshape(-1))
+    return np.stack(ranks, 1) if ranks else np.zeros((n, 0), np.int64)
 
 
 def _key_order(keys):
@@ -623,8 +636,7 @@ def _model_aggregate(prog, cols, key_ids, n):
     _fill_conditions(prog)
     regs = _model_registers(prog.spec, list(prog.tensors) + [t for _, t in prog.masks], n)
     if key_ids:
-        stacked = np.concatenate([cols[k].reshape(n, -1).astype(np.int64) for k in key_ids], 1)
-        _, inv = np.unique(stacked, axis=0, return_inverse=True)
+        _, inv = np.unique(_tuple_codes([cols[k] for k in key_ids], n), axis=0, return_inverse=True)
         inv = inv.reshape(-1)
         G = int(inv.max()) + 1
     else:
@@ -662,7 +674,7 @@ def _model_encode_keys(key_cols, mask):
     n = key_cols[0].shape[0]
     sel = np.ones(n, bool) if mask is None else mask.reshape(-1).numpy().astype(bool)
     rows = np.nonzero(sel)[0]
-    stacked = np.concatenate([k.reshape(n, -1).numpy().astype(np.int64) for k in key_cols], 1)[rows]
+    stacked = _tuple_codes([k.numpy() for k in key_cols], n)[rows]
     uniq, first, inv = np.unique(stacked, axis=0, return_index=True, return_inverse=True)
     codes = np.zeros(n, np.int32)
     codes[rows] = inv.reshape(-1)
